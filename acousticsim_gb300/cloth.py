@@ -1,0 +1,318 @@
+"""Host-side mirror of AcousticSim's cloth-simulator API for the GPU cloth.
+
+`BaraffClothGpu` takes the reference's JSON configuration keys and exposes the
+methods of cBaraffClothGpu / cBaseCloth (src/sim/cloth/BaraffClothGpu.h:16-27,
+src/sim/cloth/BaseCloth.h:19-46) on top of the C ABI in libcloth_gb300.so.
+Every call goes to the native library; there is no other implementation.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from typing import Iterable, Sequence
+
+import numpy as np
+
+from . import _native as N
+
+
+class ClothContext:
+    """One device and one CUDA stream (cloth_ctx)."""
+
+    def __init__(self, device: int = 0):
+        import weakref
+        self._h = C.c_void_p()
+        self._cloths = weakref.WeakSet()
+        N.call("cloth_ctx_create", int(device), C.byref(self._h))
+
+    @property
+    def handle(self):
+        return self._h
+
+    def synchronize(self) -> None:
+        N.call("cloth_ctx_synchronize", self._h)
+
+    def set_profiling(self, on: bool) -> None:
+        N.call("cloth_ctx_set_profiling", self._h, int(bool(on)))
+
+    def reset_profile(self) -> None:
+        N.call("cloth_ctx_reset_profile", self._h)
+
+    def profile(self) -> dict:
+        ms = (C.c_double * N.NUM_PHASES)()
+        n = (C.c_longlong * N.NUM_PHASES)()
+        N.call("cloth_ctx_get_profile", self._h, ms, n)
+        return {N.PHASE_NAMES[k]: {"ms": ms[k], "launches": n[k]} for k in range(N.NUM_PHASES)}
+
+    def stream_ptr(self) -> int:
+        s = C.c_void_p()
+        N.call("cloth_ctx_get_stream", self._h, C.byref(s))
+        return int(s.value or 0)
+
+    def device_bytes(self) -> int:
+        b = C.c_size_t()
+        N.call("cloth_ctx_device_bytes", self._h, C.byref(b))
+        return int(b.value)
+
+    def batch_step(self, cloths: Sequence["BaraffClothGpu"], dt: float = 0.0,
+                   params: N.SolveParams | None = None, stats: bool = True):
+        n = len(cloths)
+        arr = (C.c_void_p * n)(*[c.handle for c in cloths])
+        st = (N.SolveStats * n)() if stats else None
+        N.call("cloth_batch_step", self._h, arr, n, float(dt),
+               C.byref(params) if params is not None else None, st)
+        return [s.as_dict() for s in st] if stats else None
+
+    def close(self) -> None:
+        # the context frees every cloth it holds; their handles die with it
+        for c in list(self._cloths):
+            c._h = C.c_void_p()
+        if self._h:
+            N.load().cloth_ctx_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def build_grid(cloth_size=(1.0, 1.0), subdivision=(19, 19), init_pos=(0.0, 0.0, 0.0),
+               uv_rotation_deg: float = 0.0) -> dict:
+    """cTriangulator::BuildGeometry for "regular_triangle"; arrays in numpy."""
+    g = N.GridDesc((C.c_double * 2)(*cloth_size), (C.c_int * 2)(*subdivision),
+                   (C.c_double * 3)(*init_pos), float(uv_rotation_deg))
+    nv, nt, ne = C.c_int(), C.c_int(), C.c_int()
+    N.call("cloth_grid_build", C.byref(g), C.byref(nv), C.byref(nt), C.byref(ne),
+           None, None, None, None)
+    pos = np.zeros((nv.value, 3), np.float64)
+    uv = np.zeros((nv.value, 2), np.float32)
+    tris = np.zeros((nt.value, 3), np.int32)
+    edges = np.zeros((ne.value, 4), np.int32)
+    N.call("cloth_grid_build", C.byref(g), None, None, None, N.ptr(pos, C.c_double),
+           N.ptr(uv, C.c_float), N.ptr(tris, C.c_int), N.ptr(edges, C.c_int))
+    return {"pos": pos, "uv": uv, "tris": tris, "edges": edges}
+
+
+def _vec(conf: dict, key: str, default=None):
+    v = conf.get(key, default)
+    if v is None:
+        raise KeyError(f"config key '{key}' is missing")
+    return list(v)
+
+
+class BaraffClothGpu:
+    """cBaraffClothGpu on the GB300 library.
+
+    conf uses the reference's keys: geometry_type ("regular_triangle"),
+    cloth_size, subdivision, cloth_init_pos, cloth_init_orientation (zero),
+    cloth_uv_rotation, cloth_stretch_stiffness, cloth_bending_stiffness,
+    cloth_density, rayleigh_damping_a/b, default_timestep and
+    constraints.static_point.  A mesh dict (pos, uv, tris[, edges]) may be
+    passed instead of the grid keys.
+    """
+
+    def __init__(self, ctx: ClothContext, conf: dict | None = None, mesh: dict | None = None):
+        self.ctx = ctx
+        self._h = C.c_void_p()
+        if conf is not None:
+            self.Init(conf, mesh)
+
+    # ---------------------------------------------------------------- init
+    def Init(self, conf: dict, mesh: dict | None = None) -> None:
+        """cBaraffClothGpu::Init (BaraffClothGpu.cpp:24-49)."""
+        if mesh is None:
+            gt = conf.get("geometry_type", "regular_triangle")
+            if gt != "regular_triangle":
+                raise ValueError(f"geometry_type '{gt}' is not supported")
+            orient = conf.get("cloth_init_orientation", [0, 0, 0, 0])
+            if any(float(a) != 0.0 for a in orient):
+                raise ValueError("cloth_init_orientation must be zero")
+            mesh = build_grid(tuple(_vec(conf, "cloth_size")), tuple(int(s) for s in _vec(conf, "subdivision")),
+                              tuple(_vec(conf, "cloth_init_pos", [0, 0, 0])[:3]),
+                              float(conf.get("cloth_uv_rotation", 0)))
+        self.mesh = {k: np.ascontiguousarray(v) for k, v in mesh.items()}
+        pos = np.ascontiguousarray(self.mesh["pos"], np.float64)
+        uv = np.ascontiguousarray(self.mesh["uv"], np.float32)
+        tris = np.ascontiguousarray(self.mesh["tris"], np.int32)
+        edges = self.mesh.get("edges")
+        ne = 0
+        eptr = None
+        if edges is not None:
+            edges = np.ascontiguousarray(edges, np.int32)
+            ne = edges.shape[0]
+            eptr = N.ptr(edges, C.c_int)
+        md = N.MeshDesc(pos.shape[0], tris.shape[0], ne, N.ptr(pos, C.c_double),
+                        N.ptr(uv, C.c_float), N.ptr(tris, C.c_int), eptr)
+        self.material = self._material(conf)
+        N.call("cloth_create", self.ctx.handle, C.byref(md), C.byref(self.material),
+               C.byref(self._h))
+        self.ctx._cloths.add(self)
+        self.nv, self.nt = pos.shape[0], tris.shape[0]
+        cons = conf.get("constraints", {})
+        if "static_point" in cons:
+            uvs = np.ascontiguousarray(np.asarray(cons["static_point"], np.float32).reshape(-1, 2))
+            ids = self.FindVerticesIdFromUV(uvs)
+            self.AddConstraintStaticVertices(ids)
+
+    @staticmethod
+    def _material(conf: dict) -> N.Material:
+        ks = _vec(conf, "cloth_stretch_stiffness")[:3]
+        kb = _vec(conf, "cloth_bending_stiffness")[:2]
+        return N.Material((C.c_float * 3)(*ks), (C.c_float * 2)(*kb),
+                          float(conf["cloth_density"]), float(conf.get("rayleigh_damping_a", 0.0)),
+                          float(conf.get("rayleigh_damping_b", 0.0)),
+                          float(conf["default_timestep"]), float(conf.get("gravity", -9.8)),
+                          int(conf.get("fix_fv_norm", 0)))
+
+    @property
+    def handle(self):
+        return self._h
+
+    def SetMaterial(self, conf: dict) -> None:
+        self.material = self._material(conf)
+        N.call("cloth_set_material", self._h, C.byref(self.material))
+
+    # ---------------------------------------------------------------- pins
+    def FindVerticesIdFromUV(self, uvs: np.ndarray) -> np.ndarray:
+        uvs = np.ascontiguousarray(uvs, np.float32).reshape(-1, 2)
+        out = np.zeros(uvs.shape[0], np.int32)
+        N.call("cloth_find_vertices_from_uv", self._h, N.ptr(uvs, C.c_float), uvs.shape[0],
+               N.ptr(out, C.c_int))
+        return out
+
+    def AddConstraintStaticVertices(self, vids: Iterable[int]) -> None:
+        v = np.ascontiguousarray(np.asarray(list(vids), np.int32))
+        N.call("cloth_add_static_vertices", self._h, N.ptr(v, C.c_int), v.size)
+
+    def ClearConstraintStaticVertices(self) -> None:
+        N.call("cloth_clear_static_vertices", self._h)
+
+    def GetConstraintStaticVertices(self) -> list[int]:
+        n = C.c_int()
+        N.call("cloth_get_static_vertices", self._h, None, 0, C.byref(n))
+        out = np.zeros(max(1, n.value), np.int32)
+        N.call("cloth_get_static_vertices", self._h, N.ptr(out, C.c_int), n.value, C.byref(n))
+        return out[: n.value].tolist()
+
+    def ApplyUserPerturbForceOnce(self, vid: int, target) -> None:
+        """Drag point for the next step (BaraffClothGpu.cpp:266-281)."""
+        t = np.ascontiguousarray(np.asarray(target, np.float32).reshape(3))
+        N.call("cloth_set_drag_point", self._h, int(vid), N.ptr(t, C.c_float))
+
+    # ---------------------------------------------------------------- state
+    def SetPos(self, x: np.ndarray) -> None:
+        x = np.ascontiguousarray(x, np.float64).reshape(-1)
+        N.call("cloth_set_pos", self._h, N.ptr(x, C.c_double), x.size // 3)
+
+    def SetPrePos(self, x: np.ndarray) -> None:
+        x = np.ascontiguousarray(x, np.float64).reshape(-1)
+        N.call("cloth_set_pre_pos", self._h, N.ptr(x, C.c_double), x.size // 3)
+
+    def GetPos(self) -> np.ndarray:
+        x = np.zeros(self.nv * 3, np.float64)
+        N.call("cloth_get_pos", self._h, N.ptr(x, C.c_double), self.nv)
+        return x
+
+    def GetPrePos(self) -> np.ndarray:
+        x = np.zeros(self.nv * 3, np.float64)
+        N.call("cloth_get_pre_pos", self._h, N.ptr(x, C.c_double), self.nv)
+        return x
+
+    def GetInitPos(self) -> np.ndarray:
+        return np.asarray(self.mesh["pos"], np.float64).reshape(-1).copy()
+
+    def GetNumOfVertices(self) -> int:
+        return self.nv
+
+    def GetNumOfTriangles(self) -> int:
+        return self.nt
+
+    def Reset(self) -> None:
+        N.call("cloth_reset", self._h)
+
+    # ---------------------------------------------------------------- step
+    def UpdatePos(self, dt: float = 0.0, params: N.SolveParams | None = None) -> dict:
+        """One implicit step; like the reference, dt <= 0 means default_timestep."""
+        st = N.SolveStats()
+        N.call("cloth_step", self._h, float(dt), C.byref(params) if params is not None else None,
+               C.byref(st))
+        return st.as_dict()
+
+    Update = UpdatePos
+
+    def step_async(self, dt: float = 0.0, params: N.SolveParams | None = None) -> None:
+        N.call("cloth_step", self._h, float(dt), C.byref(params) if params is not None else None,
+               None)
+
+    def step_host(self, x_in, xpre_in, x_out, dt: float = 0.0,
+                  params: N.SolveParams | None = None) -> None:
+        """Step with host buffers (upload x, x_pre; download x), as UpdatePos exchanges them."""
+        N.call("cloth_step_host", self._h, float(dt),
+               C.byref(params) if params is not None else None,
+               N.ptr(x_in, C.c_double) if x_in is not None else None,
+               N.ptr(xpre_in, C.c_double) if xpre_in is not None else None,
+               N.ptr(x_out, C.c_double) if x_out is not None else None, None)
+
+    # ---------------------------------------------------------------- seam
+    def assemble(self, dt: float = 0.0) -> None:
+        N.call("cloth_assemble", self._h, float(dt))
+
+    def solve(self, params: N.SolveParams | None = None) -> dict:
+        st = N.SolveStats()
+        N.call("cloth_solve", self._h, C.byref(params) if params is not None else None,
+               C.byref(st))
+        return st.as_dict()
+
+    def advance(self) -> None:
+        N.call("cloth_advance", self._h)
+
+    def stats(self) -> dict:
+        st = N.SolveStats()
+        N.call("cloth_get_stats", self._h, C.byref(st))
+        return st.as_dict()
+
+    def get_dx(self) -> np.ndarray:
+        dx = np.zeros(self.nv * 3, np.float64)
+        N.call("cloth_get_dx", self._h, N.ptr(dx, C.c_double), self.nv)
+        return dx
+
+    def export_system(self) -> dict:
+        W = N.ELL_REF_WIDTH
+        ell = np.zeros((self.nv, W), np.int32)
+        A = np.zeros((self.nv, W, 3, 3), np.float32)
+        b = np.zeros((self.nv, 3), np.float32)
+        f = np.zeros((self.nv, 3), np.float32)
+        kb = np.zeros((self.nv, W), np.float32)
+        N.call("cloth_export_system", self._h, N.ptr(ell, C.c_int), N.ptr(A, C.c_float),
+               N.ptr(b, C.c_float), N.ptr(f, C.c_float), N.ptr(kb, C.c_float))
+        return {"ell": ell, "A": A, "b": b, "fint": f, "kbend": kb}
+
+    def export_triangles(self) -> dict:
+        f = np.zeros((self.nt, 3, 3), np.float32)
+        h = np.zeros((self.nt, 9, 3, 3), np.float32)
+        N.call("cloth_export_triangles", self._h, N.ptr(f, C.c_float), N.ptr(h, C.c_float))
+        return {"fint": f, "hess": h}
+
+    def export_tables(self) -> dict:
+        ne = C.c_int()
+        N.call("cloth_num_vertices", self._h, None, None, C.byref(ne))
+        st = np.zeros((ne.value, 4), np.int32)
+        coef = np.zeros((self.nt, 12), np.float32)
+        area = np.zeros(self.nt, np.float32)
+        mass = np.zeros(self.nv, np.float32)
+        ts = np.zeros((self.nt, 9), np.int32)
+        N.call("cloth_export_tables", self._h, N.ptr(st, C.c_int), N.ptr(coef, C.c_float),
+               N.ptr(area, C.c_float), N.ptr(mass, C.c_float), N.ptr(ts, C.c_int))
+        return {"stencil": st, "coef": coef, "area": area, "mass": mass, "tri_slot": ts}
+
+    def close(self) -> None:
+        if self._h:
+            N.load().cloth_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,1560 @@
+// C ABI of the GB300 implicit cloth step: contexts, cloth instances, the
+// step driver (one CUDA graph per launch set, PCG as a device-side while loop),
+// batches and exports.  Declarations and reference mapping: include/cloth_gb300.h.
+#include "../../include/cloth_gb300.h"
+#include "device.cuh"
+#include "topology.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <vector>
+
+namespace cloth {
+__global__ void k_pins(InstDesc *const *descs, const int *inst_list, int ninst);
+__global__ void k_tri(InstDesc *const *descs, const Tile *tiles, const BatchCtl *ctl);
+__global__ void k_row(InstDesc *const *descs, const Tile *tiles, BatchCtl *ctl);
+__global__ void k_cond(const BatchCtl *ctl, cudaGraphConditionalHandle h);
+__global__ void k_spmv(InstDesc *const *descs, const Tile *tiles, BatchCtl *ctl,
+                       int use_cond, cudaGraphConditionalHandle h);
+__global__ void k_update(InstDesc *const *descs, const Tile *tiles, BatchCtl *ctl,
+                         int use_cond, cudaGraphConditionalHandle h);
+__global__ void k_advance(InstDesc *const *descs, const Tile *tiles,
+                          const BatchCtl *ctl);
+__global__ void k_sync_x32(InstDesc *d);
+} // namespace cloth
+
+using namespace cloth;
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const std::string &msg)
+{
+    g_err = msg;
+    return code;
+}
+
+#define CK(call)                                                               \
+    do                                                                         \
+    {                                                                          \
+        cudaError_t e_ = (call);                                               \
+        if (e_ != cudaSuccess)                                                 \
+            return fail(CLOTH_ERR_CUDA,                                        \
+                        std::string(#call) + ": " + cudaGetErrorString(e_));   \
+    } while (0)
+
+size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+// Sub-allocations of one cudaMalloc, 256-byte aligned.
+struct Layout
+{
+    size_t off = 0;
+    template <class T> size_t take(size_t n)
+    {
+        size_t o = off;
+        off = align_up(off + n * sizeof(T), 256);
+        return o;
+    }
+};
+
+enum Phase
+{
+    PH_PINS = 0,
+    PH_TRI,
+    PH_ROW,
+    PH_SPMV,
+    PH_UPDATE,
+    PH_ADVANCE
+};
+
+struct Batch;
+
+} // namespace
+
+struct cloth_ctx_s
+{
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    std::recursive_mutex mu;
+    int num_sms = 0;
+    int occ_tri = 1, occ_row = 1, occ_spmv = 1, occ_update = 1;
+    bool prof = false;
+    double prof_ms[CLOTH_NUM_PHASES] = {};
+    long long prof_n[CLOTH_NUM_PHASES] = {};
+    std::vector<cudaEvent_t> ev_pool;
+    std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> ev_pending;
+    size_t bytes = 0;
+    std::vector<cloth_s *> cloths;
+    std::unique_ptr<Batch> last_batch;
+};
+
+struct cloth_s
+{
+    cloth_ctx *ctx = nullptr;
+    Mesh mesh;
+    Tables tab;
+    Material mat;
+    std::vector<int> static_pins;
+    int drag_vid = -1;
+    float drag_tgt[3] = {0, 0, 0};
+    bool pins_dirty = true;
+    int npins_uploaded = 0;
+    char *arena = nullptr;
+    size_t arena_bytes = 0;
+    InstDesc h;               // host copy of the descriptor
+    InstDesc *d_desc = nullptr;
+    InstState *d_state = nullptr;
+    bool desc_dirty = true;
+    bool assembled = false;
+    double dt_set = -1.0;
+    std::unique_ptr<Batch> self;
+};
+
+namespace {
+
+struct Batch
+{
+    cloth_ctx *ctx = nullptr;
+    std::vector<cloth_s *> members;
+    char *mem = nullptr;
+    InstDesc **d_descs = nullptr;
+    int *d_inst = nullptr;
+    Tile *d_rt = nullptr, *d_tt = nullptr;
+    BatchCtl *d_ctl = nullptr;
+    int n_rt = 0, n_tt = 0;
+    int grid_tri = 1, grid_row = 1, grid_spmv = 1, grid_update = 1;
+    cudaGraphExec_t step_exec = nullptr;
+    cudaGraphExec_t solve_exec = nullptr;
+    ~Batch()
+    {
+        if (step_exec)
+            cudaGraphExecDestroy(step_exec);
+        if (solve_exec)
+            cudaGraphExecDestroy(solve_exec);
+        if (mem)
+            cudaFree(mem);
+    }
+};
+
+cloth_solve_params default_params()
+{
+    cloth_solve_params p;
+    p.max_iters = 1000;
+    p.rel_tol = 1e-6;
+    p.abs_tol = 0.0;
+    p.check_every = 1;
+    p.warm_start = 1;
+    return p;
+}
+
+// ------------------------------------------------------------ profiling
+cudaEvent_t take_event(cloth_ctx *c)
+{
+    if (c->ev_pool.empty())
+    {
+        cudaEvent_t e;
+        cudaEventCreate(&e);
+        return e;
+    }
+    cudaEvent_t e = c->ev_pool.back();
+    c->ev_pool.pop_back();
+    return e;
+}
+
+struct PhaseTimer
+{
+    cloth_ctx *c;
+    int ph;
+    cudaEvent_t a = nullptr;
+    PhaseTimer(cloth_ctx *c_, int ph_) : c(c_), ph(ph_)
+    {
+        if (c->prof)
+        {
+            a = take_event(c);
+            cudaEventRecord(a, c->stream);
+        }
+    }
+    ~PhaseTimer()
+    {
+        if (c->prof)
+        {
+            cudaEvent_t b = take_event(c);
+            cudaEventRecord(b, c->stream);
+            c->ev_pending.push_back({ph, {a, b}});
+        }
+    }
+};
+
+void drain_profile(cloth_ctx *c)
+{
+    if (c->ev_pending.empty())
+        return;
+    cudaStreamSynchronize(c->stream);
+    for (auto &p : c->ev_pending)
+    {
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, p.second.first, p.second.second);
+        c->prof_ms[p.first] += ms;
+        c->prof_n[p.first] += 1;
+        c->ev_pool.push_back(p.second.first);
+        c->ev_pool.push_back(p.second.second);
+    }
+    c->ev_pending.clear();
+}
+
+// ------------------------------------------------------------ cloth upload
+int upload_tables(cloth_s *c)
+{
+    const Tables &t = c->tab;
+    const int n = t.nv, T = t.nt, W = t.width;
+    const int S = int(align_up(size_t(n), 32));
+    const int ntr = (n + kTile - 1) / kTile, ntt = (T + kTile - 1) / kTile;
+    const size_t WS = size_t(W) * S;
+    Layout L;
+    size_t o_tri = L.take<int4>(T), o_tcoef = L.take<float4>(3 * size_t(T)),
+           o_tdest = L.take<int4>(3 * size_t(T));
+    size_t o_col = L.take<int>(WS), o_hsrc = L.take<uint32_t>(WS),
+           o_kb = L.take<float>(WS), o_A0 = L.take<float4>(WS),
+           o_A1 = L.take<float2>(WS);
+    size_t o_rowinfo = L.take<int>(n), o_fptr = L.take<int>(n + 1),
+           o_mass = L.take<float>(n), o_grav = L.take<float>(n);
+    size_t o_pv = L.take<int>(n + 1), o_pt = L.take<float4>(n + 1);
+    size_t o_hrec = L.take<HRec>(9 * size_t(T)), o_frec = L.take<float4>(3 * size_t(T));
+    size_t o_M0 = L.take<float4>(n), o_M1 = L.take<float2>(n), o_b = L.take<float4>(n);
+    size_t o_x64 = L.take<double>(3 * size_t(n)), o_xp64 = L.take<double>(3 * size_t(n));
+    size_t o_x32 = L.take<float4>(n), o_dx = L.take<float4>(n), o_r = L.take<float4>(n),
+           o_z = L.take<float4>(n), o_p0 = L.take<float4>(n), o_p1 = L.take<float4>(n),
+           o_q = L.take<float4>(n);
+    size_t o_part = L.take<double>(3 * size_t(ntr));
+    size_t o_st = L.take<InstState>(1), o_desc = L.take<InstDesc>(1);
+    const size_t bytes = L.off;
+
+    char *base = nullptr;
+    if (cudaMalloc(&base, bytes) != cudaSuccess)
+    {
+        cudaGetLastError();
+        return fail(CLOTH_ERR_OOM, "cloth_create: device allocation of " +
+                                       std::to_string(bytes) + " bytes failed");
+    }
+    c->arena = base;
+    c->arena_bytes = bytes;
+    cudaStream_t s = c->ctx->stream;
+    CK(cudaMemsetAsync(base, 0, bytes, s));
+
+    // host staging in device layout
+    std::vector<int4> tri(T);
+    std::vector<float4> tcoef(3 * size_t(T));
+    std::vector<int4> tdest(3 * size_t(T));
+    for (int i = 0; i < T; i++)
+    {
+        const int *v = &c->mesh.tris[size_t(i) * 3];
+        int a;
+        std::memcpy(&a, &t.area[i], 4);
+        tri[i] = make_int4(v[0], v[1], v[2], a);
+        const float *cf = &t.coef[size_t(i) * 12];
+        tcoef[3 * i + 0] = make_float4(cf[0], cf[1], cf[2], cf[3]);
+        tcoef[3 * i + 1] = make_float4(cf[4], cf[5], cf[6], cf[7]);
+        tcoef[3 * i + 2] = make_float4(cf[8], cf[9], cf[10], cf[11]);
+        const int *hd = &t.h_dest[size_t(i) * 9];
+        const int *fd = &t.f_dest[size_t(i) * 3];
+        tdest[3 * i + 0] = make_int4(hd[0], hd[1], hd[2], hd[3]);
+        tdest[3 * i + 1] = make_int4(hd[4], hd[5], hd[6], hd[7]);
+        tdest[3 * i + 2] = make_int4(hd[8], fd[0], fd[1], fd[2]);
+    }
+    std::vector<int> col(WS, 0), rowinfo(n);
+    std::vector<uint32_t> hsrc(WS, 0u);
+    std::vector<float> kb(WS, 0.f), mass(n), grav(n);
+    for (int v = 0; v < n; v++)
+    {
+        int len = t.rowptr[v + 1] - t.rowptr[v];
+        rowinfo[v] = len | (t.diag_slot[v] << 8);
+        for (int sl = 0; sl < len; sl++)
+        {
+            size_t k = size_t(t.rowptr[v]) + sl;
+            size_t o = size_t(sl) * S + v;
+            col[o] = t.cols[k];
+            hsrc[o] = (uint32_t(t.h_start[k]) << 5) | uint32_t(t.h_count[k]);
+            kb[o] = t.kbend[k];
+        }
+        mass[v] = float(t.mass[v]);
+        grav[v] = float(c->mat.gravity * t.mass[v]);
+    }
+    std::vector<double> x64(c->mesh.pos);
+    std::vector<float4> x32(n);
+    for (int v = 0; v < n; v++)
+        x32[v] = make_float4(float(x64[3 * v]), float(x64[3 * v + 1]),
+                             float(x64[3 * v + 2]), 0.f);
+
+    CK(cudaMemcpyAsync(base + o_tri, tri.data(), tri.size() * sizeof(int4),
+                       cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(base + o_tcoef, tcoef.data(), tcoef.size() * sizeof(float4),
+                       cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(base + o_tdest, tdest.data(), tdest.size() * sizeof(int4),
+                       cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(base + o_col, col.data(), WS * sizeof(int),
+                       cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(base + o_hsrc, hsrc.data(), WS * sizeof(uint32_t),
+                       cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(base + o_kb, kb.data(), WS * sizeof(float),
+                       cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(base + o_rowinfo, rowinfo.data(), n * sizeof(int),
+                       cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(base + o_fptr, t.f_rowptr.data(), (n + 1) * sizeof(int),
+                       cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(base + o_mass, mass.data(), n * sizeof(float),
+                       cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(base + o_grav, grav.data(), n * sizeof(float),
+                       cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(base + o_x64, x64.data(), x64.size() * sizeof(double),
+                       cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(base + o_xp64, x64.data(), x64.size() * sizeof(double),
+                       cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(base + o_x32, x32.data(), x32.size() * sizeof(float4),
+                       cudaMemcpyHostToDevice, s));
+
+    InstDesc &h = c->h;
+    std::memset(&h, 0, sizeof(h));
+    h.nv = n;
+    h.nt = T;
+    h.width = W;
+    h.stride = S;
+    h.ntile_rows = ntr;
+    h.ntile_tris = ntt;
+    h.tri = reinterpret_cast<const int4 *>(base + o_tri);
+    h.tcoef = reinterpret_cast<const float4 *>(base + o_tcoef);
+    h.tdest = reinterpret_cast<const int4 *>(base + o_tdest);
+    h.col = reinterpret_cast<const int *>(base + o_col);
+    h.hsrc = reinterpret_cast<const uint32_t *>(base + o_hsrc);
+    h.kb = reinterpret_cast<const float *>(base + o_kb);
+    h.rowinfo = reinterpret_cast<const int *>(base + o_rowinfo);
+    h.fptr = reinterpret_cast<const int *>(base + o_fptr);
+    h.mass = reinterpret_cast<const float *>(base + o_mass);
+    h.grav = reinterpret_cast<const float *>(base + o_grav);
+    h.pin_vid = reinterpret_cast<const int *>(base + o_pv);
+    h.pin_tgt = reinterpret_cast<const float4 *>(base + o_pt);
+    h.npins = 0;
+    h.hrec = reinterpret_cast<HRec *>(base + o_hrec);
+    h.frec = reinterpret_cast<float4 *>(base + o_frec);
+    h.A0 = reinterpret_cast<float4 *>(base + o_A0);
+    h.A1 = reinterpret_cast<float2 *>(base + o_A1);
+    h.M0 = reinterpret_cast<float4 *>(base + o_M0);
+    h.M1 = reinterpret_cast<float2 *>(base + o_M1);
+    h.b = reinterpret_cast<float4 *>(base + o_b);
+    h.x64 = reinterpret_cast<double *>(base + o_x64);
+    h.xp64 = reinterpret_cast<double *>(base + o_xp64);
+    h.x32 = reinterpret_cast<float4 *>(base + o_x32);
+    h.dx = reinterpret_cast<float4 *>(base + o_dx);
+    h.r = reinterpret_cast<float4 *>(base + o_r);
+    h.z = reinterpret_cast<float4 *>(base + o_z);
+    h.p0 = reinterpret_cast<float4 *>(base + o_p0);
+    h.p1 = reinterpret_cast<float4 *>(base + o_p1);
+    h.q = reinterpret_cast<float4 *>(base + o_q);
+    h.part = reinterpret_cast<double *>(base + o_part);
+    h.st = reinterpret_cast<InstState *>(base + o_st);
+    c->d_state = h.st;
+    c->d_desc = reinterpret_cast<InstDesc *>(base + o_desc);
+    CK(cudaStreamSynchronize(s));
+    return CLOTH_OK;
+}
+
+void set_material_fields(cloth_s *c)
+{
+    c->h.k_warp = c->mat.stretch_k[0];
+    c->h.k_weft = c->mat.stretch_k[1];
+    c->h.k_bias = c->mat.stretch_k[2];
+    c->h.fix_fv_norm = c->mat.fix_fv_norm;
+    c->desc_dirty = true;
+}
+
+void set_params(cloth_s *c, const cloth_solve_params *p)
+{
+    cloth_solve_params q = p ? *p : default_params();
+    InstDesc &h = c->h;
+    int mi = std::max(0, q.max_iters);
+    int ce = std::max(1, q.check_every);
+    double rt = q.rel_tol > 0 ? q.rel_tol * q.rel_tol : 0.0;
+    double at = q.abs_tol > 0 ? q.abs_tol * q.abs_tol : 0.0;
+    int ws = q.warm_start ? 1 : 0;
+    if (h.max_iters != mi || h.check_every != ce || h.rel_tol2 != rt ||
+        h.abs_tol2 != at || h.warm_start != ws)
+    {
+        h.max_iters = mi;
+        h.check_every = ce;
+        h.rel_tol2 = rt;
+        h.abs_tol2 = at;
+        h.warm_start = ws;
+        c->desc_dirty = true;
+    }
+}
+
+void set_dt(cloth_s *c, double dt)
+{
+    if (!(dt > 0))
+        dt = c->mat.default_timestep;
+    if (dt == c->dt_set)
+        return;
+    c->dt_set = dt;
+    // float arithmetic as AssembleSystemMatrixKernel / AssembleSystemRHSKernel
+    // evaluate it (BaraffClothGpu.cu:264, 270, 316)
+    float h = float(dt);
+    c->h.h2 = h * h;
+    c->h.c_mass = 1 + h * c->mat.rayleigh_a;
+    c->h.c_stiff = h * c->mat.rayleigh_b - h * h;
+    c->desc_dirty = true;
+}
+
+// Static points plus the drag point of this step; targets are float.
+int sync_pins(cloth_s *c)
+{
+    if (!c->pins_dirty)
+        return CLOTH_OK;
+    std::vector<int> vid;
+    std::vector<float4> tgt;
+    for (int v : c->static_pins)
+    {
+        vid.push_back(v);
+        const double *p = &c->mesh.pos[size_t(v) * 3];
+        tgt.push_back(make_float4(float(p[0]), float(p[1]), float(p[2]), 0.f));
+    }
+    if (c->drag_vid >= 0)
+    {
+        vid.push_back(c->drag_vid);
+        tgt.push_back(make_float4(c->drag_tgt[0], c->drag_tgt[1], c->drag_tgt[2], 0.f));
+    }
+    if (int(vid.size()) > c->tab.nv + 1)
+        return fail(CLOTH_ERR_INVALID, "too many pinned vertices");
+    cudaStream_t s = c->ctx->stream;
+    if (!vid.empty())
+    {
+        CK(cudaMemcpyAsync(const_cast<int *>(c->h.pin_vid), vid.data(),
+                           vid.size() * sizeof(int), cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(const_cast<float4 *>(c->h.pin_tgt), tgt.data(),
+                           tgt.size() * sizeof(float4), cudaMemcpyHostToDevice, s));
+        CK(cudaStreamSynchronize(s));
+    }
+    if (c->h.npins != int(vid.size()))
+    {
+        c->h.npins = int(vid.size());
+        c->desc_dirty = true;
+    }
+    c->pins_dirty = false;
+    return CLOTH_OK;
+}
+
+int sync_desc(cloth_s *c)
+{
+    if (!c->desc_dirty)
+        return CLOTH_OK;
+    CK(cudaMemcpy(c->d_desc, &c->h, sizeof(InstDesc), cudaMemcpyHostToDevice));
+    c->desc_dirty = false;
+    return CLOTH_OK;
+}
+
+// ------------------------------------------------------------ batches
+int make_batch(cloth_ctx *ctx, const std::vector<cloth_s *> &members,
+               std::unique_ptr<Batch> &out)
+{
+    auto b = std::make_unique<Batch>();
+    b->ctx = ctx;
+    b->members = members;
+    std::vector<Tile> rt, tt;
+    std::vector<InstDesc *> descs;
+    std::vector<int> inst;
+    for (size_t i = 0; i < members.size(); i++)
+    {
+        cloth_s *c = members[i];
+        descs.push_back(c->d_desc);
+        inst.push_back(int(i));
+        for (int s = 0; s < c->tab.nv; s += kTile)
+            rt.push_back(Tile{int(i), s});
+        for (int s = 0; s < c->tab.nt; s += kTile)
+            tt.push_back(Tile{int(i), s});
+    }
+    b->n_rt = int(rt.size());
+    b->n_tt = int(tt.size());
+    Layout L;
+    size_t o_d = L.take<InstDesc *>(descs.size()), o_i = L.take<int>(inst.size()),
+           o_rt = L.take<Tile>(rt.size()), o_tt = L.take<Tile>(tt.size()),
+           o_c = L.take<BatchCtl>(1);
+    CK(cudaMalloc(&b->mem, L.off));
+    b->d_descs = reinterpret_cast<InstDesc **>(b->mem + o_d);
+    b->d_inst = reinterpret_cast<int *>(b->mem + o_i);
+    b->d_rt = reinterpret_cast<Tile *>(b->mem + o_rt);
+    b->d_tt = reinterpret_cast<Tile *>(b->mem + o_tt);
+    b->d_ctl = reinterpret_cast<BatchCtl *>(b->mem + o_c);
+    BatchCtl ctl = {0, b->n_rt, b->n_tt, 0};
+    CK(cudaMemcpy(b->d_descs, descs.data(), descs.size() * sizeof(InstDesc *),
+                  cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(b->d_inst, inst.data(), inst.size() * sizeof(int),
+                  cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(b->d_rt, rt.data(), rt.size() * sizeof(Tile), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(b->d_tt, tt.data(), tt.size() * sizeof(Tile), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(b->d_ctl, &ctl, sizeof(ctl), cudaMemcpyHostToDevice));
+    // one tile per block while that fits in a few waves; grid-stride beyond
+    auto cap = [&](int occ) { return std::max(1, ctx->num_sms * occ * 8); };
+    b->grid_tri = std::max(1, std::min(b->n_tt, cap(ctx->occ_tri)));
+    b->grid_row = std::max(1, std::min(b->n_rt, cap(ctx->occ_row)));
+    b->grid_spmv = std::max(1, std::min(b->n_rt, cap(ctx->occ_spmv)));
+    b->grid_update = std::max(1, std::min(b->n_rt, cap(ctx->occ_update)));
+    out = std::move(b);
+    return CLOTH_OK;
+}
+
+int add_kernel(cudaGraph_t g, cudaGraphNode_t *node, const cudaGraphNode_t *deps,
+               size_t ndeps, void *func, int grid, int block, void **args)
+{
+    cudaKernelNodeParams p;
+    std::memset(&p, 0, sizeof(p));
+    p.func = func;
+    p.gridDim = dim3(grid);
+    p.blockDim = dim3(block);
+    p.kernelParams = args;
+    CK(cudaGraphAddKernelNode(node, g, deps, ndeps, &p));
+    return CLOTH_OK;
+}
+
+// Graph of the PCG loop: k_cond, then while (any active) { spmv; update }.
+// With full = true the assembly in front and the position update behind are
+// part of the graph too (one launch per step).
+int build_graph(Batch *b, bool full, cudaGraphExec_t *exec)
+{
+    cudaGraph_t g = nullptr;
+    CK(cudaGraphCreate(&g, 0));
+    int rc = CLOTH_OK;
+    cudaGraphConditionalHandle hnd;
+    cudaGraphNode_t last = nullptr, n = nullptr;
+    int one = 1, zero = 0;
+    int ninst = int(b->members.size());
+    int gpins = std::max(1, std::min(ninst, 1024));
+    void *a_pins[] = {&b->d_descs, &b->d_inst, &ninst};
+    void *a_tri[] = {&b->d_descs, &b->d_tt, &b->d_ctl};
+    void *a_row[] = {&b->d_descs, &b->d_rt, &b->d_ctl};
+    void *a_cond[] = {&b->d_ctl, &hnd};
+    void *a_spmv[] = {&b->d_descs, &b->d_rt, &b->d_ctl, &one, &hnd};
+    void *a_upd[] = {&b->d_descs, &b->d_rt, &b->d_ctl, &one, &hnd};
+    void *a_adv[] = {&b->d_descs, &b->d_rt, &b->d_ctl};
+    (void)zero;
+    auto chain = [&](void *f, int grid, void **args) {
+        if (rc != CLOTH_OK)
+            return;
+        rc = add_kernel(g, &n, last ? &last : nullptr, last ? 1 : 0, f, grid,
+                        f == (void *)k_cond ? 1 : kTile, args);
+        last = n;
+    };
+    if (cudaGraphConditionalHandleCreate(&hnd, g, 1, cudaGraphCondAssignDefault) !=
+        cudaSuccess)
+    {
+        cudaGraphDestroy(g);
+        return fail(CLOTH_ERR_CUDA, "cudaGraphConditionalHandleCreate failed");
+    }
+    if (full)
+    {
+        cudaMemsetParams mp;
+        std::memset(&mp, 0, sizeof(mp));
+        mp.dst = &b->d_ctl->n_active;
+        mp.value = 0;
+        mp.elementSize = 4;
+        mp.width = 1;
+        mp.height = 1;
+        if (cudaGraphAddMemsetNode(&n, g, nullptr, 0, &mp) != cudaSuccess)
+            rc = fail(CLOTH_ERR_CUDA, "cudaGraphAddMemsetNode failed");
+        last = n;
+        chain((void *)k_pins, gpins, a_pins);
+        chain((void *)k_tri, b->grid_tri, a_tri);
+        chain((void *)k_row, b->grid_row, a_row);
+    }
+    chain((void *)k_cond, 1, a_cond);
+    if (rc == CLOTH_OK)
+    {
+        cudaGraphNodeParams cp = {cudaGraphNodeTypeConditional};
+        cp.conditional.handle = hnd;
+        cp.conditional.type = cudaGraphCondTypeWhile;
+        cp.conditional.size = 1;
+        cudaGraphNode_t cn;
+        if (cudaGraphAddNode(&cn, g, &last, nullptr, 1, &cp) != cudaSuccess)
+            rc = fail(CLOTH_ERR_CUDA, "cudaGraphAddNode(conditional) failed");
+        else
+        {
+            cudaGraph_t body = cp.conditional.phGraph_out[0];
+            cudaGraphNode_t k1, k2;
+            rc = add_kernel(body, &k1, nullptr, 0, (void *)k_spmv, b->grid_spmv,
+                            kTile, a_spmv);
+            if (rc == CLOTH_OK)
+                rc = add_kernel(body, &k2, &k1, 1, (void *)k_update,
+                                b->grid_update, kTile, a_upd);
+            last = cn;
+        }
+    }
+    if (full)
+        chain((void *)k_advance, b->grid_row, a_adv);
+    if (rc == CLOTH_OK && cudaGraphInstantiate(exec, g, 0) != cudaSuccess)
+        rc = fail(CLOTH_ERR_CUDA, "cudaGraphInstantiate failed");
+    cudaGraphDestroy(g);
+    cudaGetLastError();
+    return rc;
+}
+
+// Host-driven launches of the same kernels (used when profiling, so every
+// phase gets its own CUDA events; the arithmetic is identical).
+int launch_assemble(Batch *b)
+{
+    cloth_ctx *ctx = b->ctx;
+    cudaStream_t s = ctx->stream;
+    int ninst = int(b->members.size());
+    CK(cudaMemsetAsync(&b->d_ctl->n_active, 0, sizeof(int), s));
+    {
+        PhaseTimer t(ctx, PH_PINS);
+        k_pins<<<std::max(1, std::min(ninst, 1024)), kTile, 0, s>>>(b->d_descs,
+                                                                  b->d_inst, ninst);
+    }
+    {
+        PhaseTimer t(ctx, PH_TRI);
+        k_tri<<<b->grid_tri, kTile, 0, s>>>(b->d_descs, b->d_tt, b->d_ctl);
+    }
+    {
+        PhaseTimer t(ctx, PH_ROW);
+        k_row<<<b->grid_row, kTile, 0, s>>>(b->d_descs, b->d_rt, b->d_ctl);
+    }
+    CK(cudaGetLastError());
+    return CLOTH_OK;
+}
+
+int launch_solve_host(Batch *b, int max_iters)
+{
+    cloth_ctx *ctx = b->ctx;
+    cudaStream_t s = ctx->stream;
+    cudaGraphConditionalHandle none = 0;
+    int *h_active = nullptr;
+    CK(cudaMallocHost(&h_active, sizeof(int)));
+    int rc = CLOTH_OK;
+    const int chunk = 8;
+    for (int it = 0; it < max_iters + chunk; it += chunk)
+    {
+        for (int k = 0; k < chunk; k++)
+        {
+            {
+                PhaseTimer t(ctx, PH_SPMV);
+                k_spmv<<<b->grid_spmv, kTile, 0, s>>>(b->d_descs, b->d_rt, b->d_ctl,
+                                                       0, none);
+            }
+            {
+                PhaseTimer t(ctx, PH_UPDATE);
+                k_update<<<b->grid_update, kTile, 0, s>>>(b->d_descs, b->d_rt,
+                                                           b->d_ctl, 0, none);
+            }
+        }
+        if (cudaMemcpyAsync(h_active, &b->d_ctl->n_active, sizeof(int),
+                            cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+            cudaStreamSynchronize(s) != cudaSuccess)
+        {
+            rc = fail(CLOTH_ERR_CUDA, "solve: readback failed");
+            break;
+        }
+        if (*h_active <= 0)
+            break;
+    }
+    cudaFreeHost(h_active);
+    return rc;
+}
+
+int launch_advance(Batch *b)
+{
+    PhaseTimer t(b->ctx, PH_ADVANCE);
+    k_advance<<<b->grid_row, kTile, 0, b->ctx->stream>>>(b->d_descs, b->d_rt, b->d_ctl);
+    CK(cudaGetLastError());
+    return CLOTH_OK;
+}
+
+int read_stats(Batch *b, cloth_solve_stats *stats)
+{
+    if (!stats)
+        return CLOTH_OK;
+    CK(cudaStreamSynchronize(b->ctx->stream));
+    for (size_t i = 0; i < b->members.size(); i++)
+    {
+        InstState st;
+        CK(cudaMemcpy(&st, b->members[i]->d_state, sizeof(st), cudaMemcpyDeviceToHost));
+        cloth_solve_stats &o = stats[i];
+        o.iters = st.iter;
+        o.status = st.status;
+        o.res_norm = std::sqrt(std::max(0.0, st.rr));
+        o.rhs_norm = std::sqrt(std::max(0.0, st.bb));
+        o.rel_residual = o.rhs_norm > 0 ? o.res_norm / o.rhs_norm : o.res_norm;
+    }
+    return CLOTH_OK;
+}
+
+int max_iters_of(const Batch *b)
+{
+    int m = 0;
+    for (auto *c : b->members)
+        m = std::max(m, c->h.max_iters);
+    return m;
+}
+
+// Prepare every member for a step with dt and params.
+int prepare(const std::vector<cloth_s *> &members, double dt,
+            const cloth_solve_params *params)
+{
+    for (auto *c : members)
+    {
+        set_params(c, params);
+        set_dt(c, dt);
+        int rc = sync_pins(c);
+        if (rc != CLOTH_OK)
+            return rc;
+        rc = sync_desc(c);
+        if (rc != CLOTH_OK)
+            return rc;
+    }
+    return CLOTH_OK;
+}
+
+// After a step the drag point is dropped (BaraffClothGpu.cpp:260-262).
+void end_step(const std::vector<cloth_s *> &members)
+{
+    for (auto *c : members)
+    {
+        if (c->drag_vid >= 0)
+        {
+            c->drag_vid = -1;
+            c->pins_dirty = true;
+        }
+        c->assembled = false;
+    }
+}
+
+int run_step(Batch *b, double dt, const cloth_solve_params *params,
+             cloth_solve_stats *stats)
+{
+    cloth_ctx *ctx = b->ctx;
+    int rc = prepare(b->members, dt, params);
+    if (rc != CLOTH_OK)
+        return rc;
+    if (ctx->prof)
+    {
+        rc = launch_assemble(b);
+        if (rc == CLOTH_OK)
+            rc = launch_solve_host(b, max_iters_of(b));
+        if (rc == CLOTH_OK)
+            rc = launch_advance(b);
+    }
+    else
+    {
+        if (!b->step_exec)
+        {
+            rc = build_graph(b, true, &b->step_exec);
+            if (rc != CLOTH_OK)
+                return rc;
+        }
+        CK(cudaGraphLaunch(b->step_exec, ctx->stream));
+    }
+    if (rc != CLOTH_OK)
+        return rc;
+    end_step(b->members);
+    return read_stats(b, stats);
+}
+
+Batch *self_batch(cloth_s *c, int *rc)
+{
+    *rc = CLOTH_OK;
+    if (!c->self)
+        *rc = make_batch(c->ctx, {c}, c->self);
+    return c->self.get();
+}
+
+bool valid_params(const cloth_solve_params *p)
+{
+    return !p || (p->max_iters >= 0 && p->max_iters <= 100000000 &&
+                  p->rel_tol >= 0 && p->abs_tol >= 0);
+}
+
+} // namespace
+
+// ====================================================================== ABI
+extern "C" {
+
+int cloth_abi_version(void) { return CLOTH_ABI_VERSION; }
+
+const char *cloth_last_error(void) { return g_err.c_str(); }
+
+const char *cloth_status_string(int s)
+{
+    switch (s)
+    {
+    case CLOTH_OK: return "ok";
+    case CLOTH_ERR_INVALID: return "invalid argument";
+    case CLOTH_ERR_CUDA: return "CUDA error";
+    case CLOTH_ERR_OOM: return "out of device memory";
+    case CLOTH_ERR_BUDGET: return "device-memory budget exceeded";
+    case CLOTH_ERR_MESH: return "unsupported mesh";
+    case CLOTH_ERR_NAN: return "NaN or Inf in the solve";
+    case CLOTH_ERR_BREAKDOWN: return "PCG breakdown (zero denominator)";
+    case CLOTH_ERR_MAXITER: return "PCG stopped at max_iters";
+    case CLOTH_ERR_TIMEOUT: return "device wait timed out";
+    case CLOTH_ERR_UNSUPPORTED: return "unsupported";
+    case CLOTH_ERR_STATE: return "call out of order";
+    default: return "unknown status";
+    }
+}
+
+int cloth_ctx_create(int device, cloth_ctx **out)
+{
+    if (!out)
+        return fail(CLOTH_ERR_INVALID, "cloth_ctx_create: out is NULL");
+    *out = nullptr;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= 0)
+    {
+        cudaGetLastError();
+        return fail(CLOTH_ERR_CUDA, "cloth_ctx_create: no CUDA device");
+    }
+    if (device < 0 || device >= ndev)
+        return fail(CLOTH_ERR_INVALID, "cloth_ctx_create: bad device index");
+    CK(cudaSetDevice(device));
+    auto c = std::make_unique<cloth_ctx>();
+    c->device = device;
+    CK(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+    CK(cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device));
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c->occ_tri, k_tri, kTile, 0));
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c->occ_row, k_row, kTile, 0));
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c->occ_spmv, k_spmv, kTile, 0));
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c->occ_update, k_update, kTile, 0));
+    *out = c.release();
+    return CLOTH_OK;
+}
+
+int cloth_ctx_destroy(cloth_ctx *ctx)
+{
+    if (!ctx)
+        return CLOTH_OK;
+    {
+        std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+        cudaSetDevice(ctx->device);
+        cudaStreamSynchronize(ctx->stream);
+        ctx->last_batch.reset();
+        for (auto *c : std::vector<cloth_s *>(ctx->cloths))
+        {
+            c->self.reset();
+            if (c->arena)
+                cudaFree(c->arena);
+            delete c;
+        }
+        ctx->cloths.clear();
+        for (auto &p : ctx->ev_pending)
+        {
+            cudaEventDestroy(p.second.first);
+            cudaEventDestroy(p.second.second);
+        }
+        for (auto e : ctx->ev_pool)
+            cudaEventDestroy(e);
+        cudaStreamDestroy(ctx->stream);
+    }
+    delete ctx;
+    return CLOTH_OK;
+}
+
+int cloth_ctx_synchronize(cloth_ctx *ctx)
+{
+    if (!ctx)
+        return fail(CLOTH_ERR_INVALID, "ctx is NULL");
+    std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+    CK(cudaStreamSynchronize(ctx->stream));
+    return CLOTH_OK;
+}
+
+int cloth_ctx_set_profiling(cloth_ctx *ctx, int enable)
+{
+    if (!ctx)
+        return fail(CLOTH_ERR_INVALID, "ctx is NULL");
+    std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+    drain_profile(ctx);
+    ctx->prof = enable != 0;
+    return CLOTH_OK;
+}
+
+int cloth_ctx_get_profile(cloth_ctx *ctx, double *ms_total, long long *launches)
+{
+    if (!ctx)
+        return fail(CLOTH_ERR_INVALID, "ctx is NULL");
+    std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+    drain_profile(ctx);
+    for (int k = 0; k < CLOTH_NUM_PHASES; k++)
+    {
+        if (ms_total)
+            ms_total[k] = ctx->prof_ms[k];
+        if (launches)
+            launches[k] = ctx->prof_n[k];
+    }
+    return CLOTH_OK;
+}
+
+int cloth_ctx_reset_profile(cloth_ctx *ctx)
+{
+    if (!ctx)
+        return fail(CLOTH_ERR_INVALID, "ctx is NULL");
+    std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+    drain_profile(ctx);
+    for (int k = 0; k < CLOTH_NUM_PHASES; k++)
+    {
+        ctx->prof_ms[k] = 0;
+        ctx->prof_n[k] = 0;
+    }
+    return CLOTH_OK;
+}
+
+int cloth_ctx_device_bytes(cloth_ctx *ctx, size_t *bytes)
+{
+    if (!ctx || !bytes)
+        return fail(CLOTH_ERR_INVALID, "NULL argument");
+    std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+    *bytes = ctx->bytes;
+    return CLOTH_OK;
+}
+
+int cloth_ctx_get_stream(cloth_ctx *ctx, void **stream)
+{
+    if (!ctx || !stream)
+        return fail(CLOTH_ERR_INVALID, "NULL argument");
+    *stream = reinterpret_cast<void *>(ctx->stream);
+    return CLOTH_OK;
+}
+
+int cloth_grid_build(const cloth_grid_desc *grid, int *nv, int *nt, int *ne,
+                     double *pos, float *uv, int *tris, int *edges)
+{
+    if (!grid)
+        return fail(CLOTH_ERR_INVALID, "grid is NULL");
+    GridDesc g;
+    std::memcpy(g.size, grid->cloth_size, sizeof(g.size));
+    std::memcpy(g.subdiv, grid->subdivision, sizeof(g.subdiv));
+    std::memcpy(g.init_pos, grid->init_pos, sizeof(g.init_pos));
+    g.uv_rotation_deg = grid->uv_rotation_deg;
+    Mesh m;
+    std::string err;
+    if (!build_grid(g, m, err))
+        return fail(CLOTH_ERR_INVALID, err);
+    if (nv)
+        *nv = m.nv;
+    if (nt)
+        *nt = m.nt;
+    if (ne)
+        *ne = m.ne;
+    if (pos)
+        std::memcpy(pos, m.pos.data(), m.pos.size() * sizeof(double));
+    if (uv)
+        std::memcpy(uv, m.uv.data(), m.uv.size() * sizeof(float));
+    if (tris)
+        std::memcpy(tris, m.tris.data(), m.tris.size() * sizeof(int));
+    if (edges)
+        std::memcpy(edges, m.edges.data(), m.edges.size() * sizeof(int));
+    return CLOTH_OK;
+}
+
+static bool copy_mesh(const cloth_mesh_desc *mesh, Mesh &m, std::string &err)
+{
+    if (!mesh || mesh->nv <= 0 || mesh->nt <= 0 || !mesh->pos || !mesh->uv ||
+        !mesh->tris || mesh->ne < 0 || (mesh->ne > 0 && !mesh->edges))
+    {
+        err = "bad mesh description";
+        return false;
+    }
+    m.nv = mesh->nv;
+    m.nt = mesh->nt;
+    m.pos.assign(mesh->pos, mesh->pos + size_t(m.nv) * 3);
+    m.uv.assign(mesh->uv, mesh->uv + size_t(m.nv) * 2);
+    m.tris.assign(mesh->tris, mesh->tris + size_t(m.nt) * 3);
+    if (mesh->ne > 0)
+    {
+        m.ne = mesh->ne;
+        m.edges.assign(mesh->edges, mesh->edges + size_t(m.ne) * 4);
+        return true;
+    }
+    return derive_edges(m, err);
+}
+
+static void copy_material(const cloth_material *mat, Material &mt)
+{
+    std::memcpy(mt.stretch_k, mat->stretch_k, sizeof(mt.stretch_k));
+    std::memcpy(mt.bending_k, mat->bending_k, sizeof(mt.bending_k));
+    mt.density = mat->density;
+    mt.rayleigh_a = mat->rayleigh_a;
+    mt.rayleigh_b = mat->rayleigh_b;
+    mt.default_timestep = mat->default_timestep;
+    mt.gravity = mat->gravity;
+    mt.fix_fv_norm = mat->fix_fv_norm;
+}
+
+int cloth_host_tables(const cloth_mesh_desc *mesh, const cloth_material *mat,
+                      int *ne, int *width, int *ell, int *stencil, float *coef,
+                      float *area, double *mass, float *kbend, int *tri_slot)
+{
+    if (!mesh || !mat)
+        return fail(CLOTH_ERR_INVALID, "cloth_host_tables: NULL argument");
+    Mesh m;
+    Material mt;
+    Tables t;
+    std::string err;
+    if (!copy_mesh(mesh, m, err))
+        return fail(CLOTH_ERR_MESH, err);
+    copy_material(mat, mt);
+    if (!build_tables(m, mt, t, err))
+        return fail(CLOTH_ERR_MESH, err);
+    const int R = CLOTH_ELL_REF_WIDTH;
+    if (ne)
+        *ne = m.ne;
+    if (width)
+        *width = t.width;
+    for (int v = 0; v < t.nv; v++)
+    {
+        const int len = t.rowptr[v + 1] - t.rowptr[v];
+        for (int s = 0; s < R; s++)
+        {
+            const size_t k = size_t(t.rowptr[v]) + s;
+            if (ell)
+                ell[size_t(v) * R + s] = s < len ? t.cols[k] : -1;
+            if (kbend)
+                kbend[size_t(v) * R + s] = s < len ? t.kbend[k] : 0.f;
+        }
+    }
+    if (stencil)
+        std::memcpy(stencil, t.stencil.data(), t.stencil.size() * sizeof(int));
+    if (coef)
+        std::memcpy(coef, t.coef.data(), t.coef.size() * sizeof(float));
+    if (area)
+        std::memcpy(area, t.area.data(), t.area.size() * sizeof(float));
+    if (mass)
+        std::memcpy(mass, t.mass.data(), t.mass.size() * sizeof(double));
+    if (tri_slot)
+        std::memcpy(tri_slot, t.tri_slot.data(), t.tri_slot.size() * sizeof(int));
+    return CLOTH_OK;
+}
+
+int cloth_create(cloth_ctx *ctx, const cloth_mesh_desc *mesh,
+                 const cloth_material *mat, cloth_t **out)
+{
+    if (!ctx || !mesh || !mat || !out)
+        return fail(CLOTH_ERR_INVALID, "cloth_create: NULL argument");
+    *out = nullptr;
+    if (mesh->nv <= 0 || mesh->nt <= 0 || !mesh->pos || !mesh->uv || !mesh->tris ||
+        (mesh->ne > 0 && !mesh->edges) || mesh->ne < 0)
+        return fail(CLOTH_ERR_INVALID, "cloth_create: bad mesh description");
+    if (!(mat->density > 0) || !(mat->default_timestep > 0))
+        return fail(CLOTH_ERR_INVALID, "cloth_create: density and timestep must be > 0");
+    std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+    CK(cudaSetDevice(ctx->device));
+    auto c = std::make_unique<cloth_s>();
+    c->ctx = ctx;
+    Mesh &m = c->mesh;
+    std::string err;
+    if (!copy_mesh(mesh, m, err))
+        return fail(CLOTH_ERR_MESH, err);
+    Material &mt = c->mat;
+    copy_material(mat, mt);
+    if (!build_tables(m, mt, c->tab, err))
+        return fail(CLOTH_ERR_MESH, err);
+    int rc = upload_tables(c.get());
+    if (rc != CLOTH_OK)
+    {
+        if (c->arena)
+            cudaFree(c->arena);
+        return rc;
+    }
+    set_material_fields(c.get());
+    set_params(c.get(), nullptr);
+    set_dt(c.get(), mt.default_timestep);
+    rc = sync_desc(c.get());
+    if (rc != CLOTH_OK)
+    {
+        cudaFree(c->arena);
+        return rc;
+    }
+    ctx->bytes += c->arena_bytes;
+    ctx->cloths.push_back(c.get());
+    *out = c.release();
+    return CLOTH_OK;
+}
+
+int cloth_destroy(cloth_t *c)
+{
+    if (!c)
+        return CLOTH_OK;
+    cloth_ctx *ctx = c->ctx;
+    std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    if (ctx->last_batch)
+        for (auto *m : ctx->last_batch->members)
+            if (m == c)
+            {
+                ctx->last_batch.reset();
+                break;
+            }
+    c->self.reset();
+    if (c->arena)
+        cudaFree(c->arena);
+    ctx->bytes -= c->arena_bytes;
+    ctx->cloths.erase(std::remove(ctx->cloths.begin(), ctx->cloths.end(), c),
+                      ctx->cloths.end());
+    delete c;
+    return CLOTH_OK;
+}
+
+int cloth_num_vertices(const cloth_t *c, int *nv, int *nt, int *ne)
+{
+    if (!c)
+        return fail(CLOTH_ERR_INVALID, "cloth is NULL");
+    if (nv)
+        *nv = c->mesh.nv;
+    if (nt)
+        *nt = c->mesh.nt;
+    if (ne)
+        *ne = c->mesh.ne;
+    return CLOTH_OK;
+}
+
+int cloth_set_material(cloth_t *c, const cloth_material *mat)
+{
+    if (!c || !mat)
+        return fail(CLOTH_ERR_INVALID, "NULL argument");
+    std::lock_guard<std::recursive_mutex> lk(c->ctx->mu);
+    CK(cudaSetDevice(c->ctx->device));
+    Material &mt = c->mat;
+    bool bend = mt.bending_k[0] != mat->bending_k[0] || mt.bending_k[1] != mat->bending_k[1];
+    std::memcpy(mt.stretch_k, mat->stretch_k, sizeof(mt.stretch_k));
+    std::memcpy(mt.bending_k, mat->bending_k, sizeof(mt.bending_k));
+    mt.rayleigh_a = mat->rayleigh_a;
+    mt.rayleigh_b = mat->rayleigh_b;
+    mt.fix_fv_norm = mat->fix_fv_norm;
+    if (mat->default_timestep > 0)
+        mt.default_timestep = mat->default_timestep;
+    if (bend)
+    {
+        rebuild_bending(c->mesh, mt, c->tab);
+        const Tables &t = c->tab;
+        std::vector<float> kb(size_t(t.width) * c->h.stride, 0.f);
+        for (int v = 0; v < t.nv; v++)
+            for (int s = 0; s < t.rowptr[v + 1] - t.rowptr[v]; s++)
+                kb[size_t(s) * c->h.stride + v] = t.kbend[size_t(t.rowptr[v]) + s];
+        CK(cudaMemcpy(const_cast<float *>(c->h.kb), kb.data(), kb.size() * sizeof(float),
+                      cudaMemcpyHostToDevice));
+    }
+    set_material_fields(c);
+    c->dt_set = -1.0; // damping may have changed
+    return CLOTH_OK;
+}
+
+int cloth_find_vertices_from_uv(const cloth_t *c, const float *uv, int n, int *vids)
+{
+    if (!c || (n > 0 && (!uv || !vids)) || n < 0)
+        return fail(CLOTH_ERR_INVALID, "bad argument");
+    find_vertices_from_uv(c->mesh, uv, n, vids);
+    return CLOTH_OK;
+}
+
+int cloth_add_static_vertices(cloth_t *c, const int *vids, int n)
+{
+    if (!c || n < 0 || (n > 0 && !vids))
+        return fail(CLOTH_ERR_INVALID, "bad argument");
+    std::lock_guard<std::recursive_mutex> lk(c->ctx->mu);
+    for (int k = 0; k < n; k++)
+        if (vids[k] < 0 || vids[k] >= c->mesh.nv)
+            return fail(CLOTH_ERR_INVALID, "static vertex id out of range");
+    for (int k = 0; k < n; k++)
+        if (std::find(c->static_pins.begin(), c->static_pins.end(), vids[k]) ==
+            c->static_pins.end())
+            c->static_pins.push_back(vids[k]);
+    c->pins_dirty = true;
+    return CLOTH_OK;
+}
+
+int cloth_clear_static_vertices(cloth_t *c)
+{
+    if (!c)
+        return fail(CLOTH_ERR_INVALID, "cloth is NULL");
+    std::lock_guard<std::recursive_mutex> lk(c->ctx->mu);
+    c->static_pins.clear();
+    c->pins_dirty = true;
+    return CLOTH_OK;
+}
+
+int cloth_get_static_vertices(const cloth_t *c, int *vids, int cap, int *n)
+{
+    if (!c || !n)
+        return fail(CLOTH_ERR_INVALID, "bad argument");
+    *n = int(c->static_pins.size());
+    for (int k = 0; k < std::min(cap, *n) && vids; k++)
+        vids[k] = c->static_pins[k];
+    return CLOTH_OK;
+}
+
+int cloth_set_drag_point(cloth_t *c, int vid, const float target[3])
+{
+    if (!c || !target || vid < 0 || vid >= c->mesh.nv)
+        return fail(CLOTH_ERR_INVALID, "bad drag point");
+    std::lock_guard<std::recursive_mutex> lk(c->ctx->mu);
+    c->drag_vid = vid;
+    std::memcpy(c->drag_tgt, target, sizeof(c->drag_tgt));
+    c->pins_dirty = true;
+    return CLOTH_OK;
+}
+
+static int set_state(cloth_t *c, const double *x, int nv, bool pre)
+{
+    if (!c || !x || nv != c->mesh.nv)
+        return fail(CLOTH_ERR_INVALID, "set_pos: bad argument");
+    std::lock_guard<std::recursive_mutex> lk(c->ctx->mu);
+    CK(cudaSetDevice(c->ctx->device));
+    cudaStream_t s = c->ctx->stream;
+    CK(cudaMemcpyAsync(pre ? c->h.xp64 : c->h.x64, x, size_t(nv) * 3 * sizeof(double),
+                       cudaMemcpyHostToDevice, s));
+    if (!pre)
+        k_sync_x32<<<std::min(1024, (nv + 255) / 256), 256, 0, s>>>(c->d_desc);
+    CK(cudaGetLastError());
+    c->assembled = false;
+    return CLOTH_OK;
+}
+
+int cloth_set_pos(cloth_t *c, const double *x, int nv) { return set_state(c, x, nv, false); }
+int cloth_set_pre_pos(cloth_t *c, const double *x, int nv) { return set_state(c, x, nv, true); }
+
+static int get_state(cloth_t *c, double *x, int nv, bool pre)
+{
+    if (!c || !x || nv != c->mesh.nv)
+        return fail(CLOTH_ERR_INVALID, "get_pos: bad argument");
+    std::lock_guard<std::recursive_mutex> lk(c->ctx->mu);
+    CK(cudaSetDevice(c->ctx->device));
+    cudaStream_t s = c->ctx->stream;
+    CK(cudaMemcpyAsync(x, pre ? c->h.xp64 : c->h.x64, size_t(nv) * 3 * sizeof(double),
+                       cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    return CLOTH_OK;
+}
+
+int cloth_get_pos(cloth_t *c, double *x, int nv) { return get_state(c, x, nv, false); }
+int cloth_get_pre_pos(cloth_t *c, double *x, int nv) { return get_state(c, x, nv, true); }
+
+int cloth_reset(cloth_t *c)
+{
+    if (!c)
+        return fail(CLOTH_ERR_INVALID, "cloth is NULL");
+    std::lock_guard<std::recursive_mutex> lk(c->ctx->mu);
+    int rc = cloth_set_pos(c, c->mesh.pos.data(), c->mesh.nv);
+    if (rc == CLOTH_OK)
+        rc = cloth_set_pre_pos(c, c->mesh.pos.data(), c->mesh.nv);
+    if (rc != CLOTH_OK)
+        return rc;
+    CK(cudaMemsetAsync(c->h.dx, 0, size_t(c->mesh.nv) * sizeof(float4), c->ctx->stream));
+    CK(cudaStreamSynchronize(c->ctx->stream));
+    return CLOTH_OK;
+}
+
+int cloth_step(cloth_t *c, double dt, const cloth_solve_params *params,
+               cloth_solve_stats *stats)
+{
+    if (!c || !valid_params(params))
+        return fail(CLOTH_ERR_INVALID, "cloth_step: bad argument");
+    std::lock_guard<std::recursive_mutex> lk(c->ctx->mu);
+    CK(cudaSetDevice(c->ctx->device));
+    int rc;
+    Batch *b = self_batch(c, &rc);
+    if (rc != CLOTH_OK)
+        return rc;
+    return run_step(b, dt, params, stats);
+}
+
+int cloth_step_host(cloth_t *c, double dt, const cloth_solve_params *params,
+                    const double *x_in, const double *x_pre_in, double *x_out,
+                    cloth_solve_stats *stats)
+{
+    if (!c)
+        return fail(CLOTH_ERR_INVALID, "cloth is NULL");
+    std::lock_guard<std::recursive_mutex> lk(c->ctx->mu);
+    int rc = CLOTH_OK;
+    if (x_in)
+        rc = cloth_set_pos(c, x_in, c->mesh.nv);
+    if (rc == CLOTH_OK && x_pre_in)
+        rc = cloth_set_pre_pos(c, x_pre_in, c->mesh.nv);
+    if (rc == CLOTH_OK)
+        rc = cloth_step(c, dt, params, stats);
+    if (rc == CLOTH_OK && x_out)
+        rc = cloth_get_pos(c, x_out, c->mesh.nv);
+    return rc;
+}
+
+int cloth_assemble(cloth_t *c, double dt)
+{
+    if (!c)
+        return fail(CLOTH_ERR_INVALID, "cloth is NULL");
+    std::lock_guard<std::recursive_mutex> lk(c->ctx->mu);
+    CK(cudaSetDevice(c->ctx->device));
+    int rc;
+    Batch *b = self_batch(c, &rc);
+    if (rc != CLOTH_OK)
+        return rc;
+    set_dt(c, dt);
+    rc = sync_pins(c);
+    if (rc == CLOTH_OK)
+        rc = sync_desc(c);
+    if (rc == CLOTH_OK)
+        rc = launch_assemble(b);
+    if (rc == CLOTH_OK)
+        c->assembled = true;
+    return rc;
+}
+
+int cloth_solve(cloth_t *c, const cloth_solve_params *params, cloth_solve_stats *stats)
+{
+    if (!c || !valid_params(params))
+        return fail(CLOTH_ERR_INVALID, "cloth_solve: bad argument");
+    std::lock_guard<std::recursive_mutex> lk(c->ctx->mu);
+    if (!c->assembled)
+        return fail(CLOTH_ERR_STATE, "cloth_solve: call cloth_assemble first");
+    CK(cudaSetDevice(c->ctx->device));
+    int rc;
+    Batch *b = self_batch(c, &rc);
+    if (rc != CLOTH_OK)
+        return rc;
+    // The PCG start (r0, z0, rho0) was formed by the assembly with the
+    // parameters current then; max_iters / tolerances apply from here on.
+    set_params(c, params);
+    rc = sync_desc(c);
+    if (rc != CLOTH_OK)
+        return rc;
+    if (c->ctx->prof)
+        rc = launch_solve_host(b, c->h.max_iters);
+    else
+    {
+        if (!b->solve_exec)
+            rc = build_graph(b, false, &b->solve_exec);
+        if (rc == CLOTH_OK && cudaGraphLaunch(b->solve_exec, c->ctx->stream) != cudaSuccess)
+            rc = fail(CLOTH_ERR_CUDA, "cudaGraphLaunch failed");
+    }
+    if (rc != CLOTH_OK)
+        return rc;
+    return read_stats(b, stats);
+}
+
+int cloth_advance(cloth_t *c)
+{
+    if (!c)
+        return fail(CLOTH_ERR_INVALID, "cloth is NULL");
+    std::lock_guard<std::recursive_mutex> lk(c->ctx->mu);
+    CK(cudaSetDevice(c->ctx->device));
+    int rc;
+    Batch *b = self_batch(c, &rc);
+    if (rc != CLOTH_OK)
+        return rc;
+    rc = launch_advance(b);
+    end_step({c});
+    return rc;
+}
+
+int cloth_get_stats(cloth_t *c, cloth_solve_stats *stats)
+{
+    if (!c || !stats)
+        return fail(CLOTH_ERR_INVALID, "NULL argument");
+    std::lock_guard<std::recursive_mutex> lk(c->ctx->mu);
+    CK(cudaSetDevice(c->ctx->device));
+    CK(cudaStreamSynchronize(c->ctx->stream));
+    InstState st;
+    CK(cudaMemcpy(&st, c->d_state, sizeof(st), cudaMemcpyDeviceToHost));
+    stats->iters = st.iter;
+    stats->status = st.status;
+    stats->res_norm = std::sqrt(std::max(0.0, st.rr));
+    stats->rhs_norm = std::sqrt(std::max(0.0, st.bb));
+    stats->rel_residual = stats->rhs_norm > 0 ? stats->res_norm / stats->rhs_norm
+                                              : stats->res_norm;
+    return CLOTH_OK;
+}
+
+int cloth_get_dx(cloth_t *c, double *dx, int nv)
+{
+    if (!c || !dx || nv != c->mesh.nv)
+        return fail(CLOTH_ERR_INVALID, "bad argument");
+    std::lock_guard<std::recursive_mutex> lk(c->ctx->mu);
+    CK(cudaSetDevice(c->ctx->device));
+    std::vector<float4> v(nv);
+    CK(cudaStreamSynchronize(c->ctx->stream));
+    CK(cudaMemcpy(v.data(), c->h.dx, size_t(nv) * sizeof(float4), cudaMemcpyDeviceToHost));
+    for (int i = 0; i < nv; i++)
+    {
+        dx[3 * i] = v[i].x;
+        dx[3 * i + 1] = v[i].y;
+        dx[3 * i + 2] = v[i].z;
+    }
+    return CLOTH_OK;
+}
+
+int cloth_export_system(cloth_t *c, int *ell, float *A, float *b, float *fint,
+                        float *kbend)
+{
+    if (!c)
+        return fail(CLOTH_ERR_INVALID, "cloth is NULL");
+    std::lock_guard<std::recursive_mutex> lk(c->ctx->mu);
+    CK(cudaSetDevice(c->ctx->device));
+    CK(cudaStreamSynchronize(c->ctx->stream));
+    const Tables &t = c->tab;
+    const int n = t.nv, S = c->h.stride, W = t.width, R = CLOTH_ELL_REF_WIDTH;
+    const size_t WS = size_t(W) * S;
+    if (ell)
+        for (int v = 0; v < n; v++)
+            for (int s = 0; s < R; s++)
+            {
+                int len = t.rowptr[v + 1] - t.rowptr[v];
+                ell[size_t(v) * R + s] = s < len ? t.cols[size_t(t.rowptr[v]) + s] : -1;
+            }
+    if (A)
+    {
+        std::vector<float4> a0(WS);
+        std::vector<float2> a1(WS);
+        CK(cudaMemcpy(a0.data(), c->h.A0, WS * sizeof(float4), cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(a1.data(), c->h.A1, WS * sizeof(float2), cudaMemcpyDeviceToHost));
+        std::fill(A, A + size_t(n) * R * 9, 0.f);
+        for (int v = 0; v < n; v++)
+            for (int s = 0; s < t.rowptr[v + 1] - t.rowptr[v]; s++)
+            {
+                size_t o = size_t(s) * S + v;
+                float e[6] = {a0[o].x, a0[o].y, a0[o].z, a0[o].w, a1[o].x, a1[o].y};
+                float full[9] = {e[0], e[1], e[2], e[1], e[3], e[4], e[2], e[4], e[5]};
+                std::memcpy(A + (size_t(v) * R + s) * 9, full, sizeof(full));
+            }
+    }
+    if (b)
+    {
+        std::vector<float4> bv(n);
+        CK(cudaMemcpy(bv.data(), c->h.b, size_t(n) * sizeof(float4), cudaMemcpyDeviceToHost));
+        for (int v = 0; v < n; v++)
+        {
+            b[3 * v] = bv[v].x;
+            b[3 * v + 1] = bv[v].y;
+            b[3 * v + 2] = bv[v].z;
+        }
+    }
+    if (fint)
+    {
+        // stretch part from the force records, bending part -K_b x
+        std::vector<float4> fr(size_t(t.nt) * 3), x32(n);
+        CK(cudaMemcpy(fr.data(), c->h.frec, fr.size() * sizeof(float4), cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(x32.data(), c->h.x32, x32.size() * sizeof(float4), cudaMemcpyDeviceToHost));
+        for (int v = 0; v < n; v++)
+        {
+            float f[3] = {0, 0, 0};
+            for (int k = t.f_rowptr[v]; k < t.f_rowptr[v + 1]; k++)
+            {
+                f[0] += fr[k].x;
+                f[1] += fr[k].y;
+                f[2] += fr[k].z;
+            }
+            for (int s = 0; s < t.rowptr[v + 1] - t.rowptr[v]; s++)
+            {
+                size_t k = size_t(t.rowptr[v]) + s;
+                const float4 xc = x32[t.cols[k]];
+                f[0] -= t.kbend[k] * xc.x;
+                f[1] -= t.kbend[k] * xc.y;
+                f[2] -= t.kbend[k] * xc.z;
+            }
+            std::memcpy(fint + 3 * size_t(v), f, sizeof(f));
+        }
+    }
+    if (kbend)
+    {
+        std::fill(kbend, kbend + size_t(n) * R, 0.f);
+        for (int v = 0; v < n; v++)
+            for (int s = 0; s < t.rowptr[v + 1] - t.rowptr[v]; s++)
+                kbend[size_t(v) * R + s] = t.kbend[size_t(t.rowptr[v]) + s];
+    }
+    return CLOTH_OK;
+}
+
+int cloth_export_triangles(cloth_t *c, float *fint, float *hess)
+{
+    if (!c)
+        return fail(CLOTH_ERR_INVALID, "cloth is NULL");
+    std::lock_guard<std::recursive_mutex> lk(c->ctx->mu);
+    CK(cudaSetDevice(c->ctx->device));
+    CK(cudaStreamSynchronize(c->ctx->stream));
+    const Tables &t = c->tab;
+    if (fint)
+    {
+        std::vector<float4> fr(size_t(t.nt) * 3);
+        CK(cudaMemcpy(fr.data(), c->h.frec, fr.size() * sizeof(float4), cudaMemcpyDeviceToHost));
+        for (int i = 0; i < t.nt; i++)
+            for (int a = 0; a < 3; a++)
+            {
+                const float4 v = fr[t.f_dest[size_t(i) * 3 + a]];
+                float *o = fint + size_t(i) * 9 + a * 3;
+                o[0] = v.x;
+                o[1] = v.y;
+                o[2] = v.z;
+            }
+    }
+    if (hess)
+    {
+        std::vector<HRec> hr(size_t(t.nt) * 9);
+        CK(cudaMemcpy(hr.data(), c->h.hrec, hr.size() * sizeof(HRec), cudaMemcpyDeviceToHost));
+        for (int i = 0; i < t.nt; i++)
+            for (int ab = 0; ab < 9; ab++)
+            {
+                const HRec &r = hr[t.h_dest[size_t(i) * 9 + ab]];
+                float e[6] = {r.h0.x, r.h0.y, r.h0.z, r.h0.w, r.h1.x, r.h1.y};
+                float full[9] = {e[0], e[1], e[2], e[1], e[3], e[4], e[2], e[4], e[5]};
+                std::memcpy(hess + (size_t(i) * 9 + ab) * 9, full, sizeof(full));
+            }
+    }
+    return CLOTH_OK;
+}
+
+int cloth_export_tables(const cloth_t *c, int *stencil, float *coef, float *area,
+                        float *mass, int *tri_slot)
+{
+    if (!c)
+        return fail(CLOTH_ERR_INVALID, "cloth is NULL");
+    const Tables &t = c->tab;
+    if (stencil)
+        std::memcpy(stencil, t.stencil.data(), t.stencil.size() * sizeof(int));
+    if (coef)
+        std::memcpy(coef, t.coef.data(), t.coef.size() * sizeof(float));
+    if (area)
+        std::memcpy(area, t.area.data(), t.area.size() * sizeof(float));
+    if (mass)
+        for (int v = 0; v < t.nv; v++)
+            mass[v] = float(t.mass[v]);
+    if (tri_slot)
+        std::memcpy(tri_slot, t.tri_slot.data(), t.tri_slot.size() * sizeof(int));
+    return CLOTH_OK;
+}
+
+int cloth_batch_step(cloth_ctx *ctx, cloth_t *const *cloths, int n, double dt,
+                     const cloth_solve_params *params, cloth_solve_stats *stats)
+{
+    if (!ctx || !cloths || n <= 0 || !valid_params(params))
+        return fail(CLOTH_ERR_INVALID, "cloth_batch_step: bad argument");
+    std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+    std::vector<cloth_s *> members(cloths, cloths + n);
+    for (auto *c : members)
+        if (!c || c->ctx != ctx)
+            return fail(CLOTH_ERR_INVALID, "cloth_batch_step: cloth of another context");
+    {
+        std::vector<cloth_s *> sorted(members);
+        std::sort(sorted.begin(), sorted.end());
+        if (std::adjacent_find(sorted.begin(), sorted.end()) != sorted.end())
+            return fail(CLOTH_ERR_INVALID, "cloth_batch_step: cloth listed twice");
+    }
+    CK(cudaSetDevice(ctx->device));
+    if (!ctx->last_batch || ctx->last_batch->members != members)
+    {
+        ctx->last_batch.reset();
+        int rc = make_batch(ctx, members, ctx->last_batch);
+        if (rc != CLOTH_OK)
+            return rc;
+    }
+    return run_step(ctx->last_batch.get(), dt, params, stats);
+}
+
+} // extern "C"

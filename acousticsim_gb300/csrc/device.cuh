@@ -1,0 +1,109 @@
+// Device-side data layout of the implicit cloth step (sm_103a).
+//
+// One cloth instance = one InstDesc (pointers into its device arena) plus one
+// InstState (its FP64 PCG scalars and convergence bookkeeping).  Kernels walk a
+// list of 128-row (or 128-triangle) tiles; a tile never straddles instances,
+// so every reduction is per instance and a cloth's arithmetic does not depend
+// on which other cloths share the launch.
+//
+// Block ELL, slot-major: entry (row, slot) of an array with per-slot planes is
+// at [slot * stride + row], so a warp's 32 rows read 32 consecutive elements of
+// each plane.  A 3x3 block is symmetric (stretch, shear, bending, mass and the
+// Rayleigh terms all are), so it is stored as 6 floats:
+//   A0 = (a00, a01, a02, a11)  as float4,   A1 = (a12, a22) as float2.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace cloth {
+
+constexpr int kTile = 128;     // rows or triangles per tile = threads per block
+constexpr int kMaxWidth = 32;  // ELL width limit (tCudaVector32i in the reference)
+
+// Triangle record of the assembly pass: one per (triangle, a, b), 32 bytes.
+// h = upper triangle of the 3x3 block (00 01 02 11 12 22), pad = 0.
+struct __align__(16) HRec
+{
+    float4 h0; // 00 01 02 11
+    float4 h1; // 12 22 pad pad
+};
+
+struct InstState
+{
+    // FP64 PCG scalars
+    double rho;     // r.z of the current iterate
+    double pq;      // p.Ap of the current iteration
+    double alpha, beta;
+    double rr;      // ||r||^2
+    double bb;      // ||b||^2
+    double rr0;     // ||r0||^2
+    // control
+    int iter;
+    int active;
+    int status;
+    unsigned ticket;
+};
+
+struct InstDesc
+{
+    int nv, nt, width, stride;   // stride: padded row count of slot-major planes
+    int ntile_rows, ntile_tris;
+    int warm_start;
+    int fix_fv_norm;
+    int max_iters;
+    int check_every;
+    double rel_tol2; // rel_tol^2 (0 = off)
+    double abs_tol2; // abs_tol^2 (0 = off)
+    float k_warp, k_weft, k_bias;
+    float h2;        // dt^2
+    float c_mass;    // 1 + dt * rayleigh_a
+    float c_stiff;   // dt * rayleigh_b - dt^2
+    // triangles
+    const int4 *tri;      // (v0, v1, v2, float_as_int(rest area))
+    const float4 *tcoef;  // 3 per triangle: FuWW FvWW FuD FvD (12 floats)
+    const int4 *tdest;    // 3 per triangle: h_dest[9], f_dest[3]
+    // rows
+    const int *col;       // [slot][stride] column (vertex) ids
+    const uint32_t *hsrc; // [slot][stride] first record << 5 | record count
+    const float *kb;      // [slot][stride] bending scalar (+K_b)
+    const int *rowinfo;   // len | diag_slot << 8
+    const int *fptr;      // nv+1 force-record ranges
+    const float *mass;    // nv
+    const float *grav;    // nv: gravity force (y component)
+    // pins
+    const int *pin_vid;     // npins
+    const float4 *pin_tgt;  // npins
+    int npins;
+    // records written by the triangle pass
+    HRec *hrec;
+    float4 *frec;
+    // assembled system
+    float4 *A0;
+    float2 *A1;
+    float4 *M0; // block-Jacobi inverse, symmetric: (00 01 02 11)
+    float2 *M1; // (12 22)
+    float4 *b;
+    // state and PCG vectors (nv float4 each; .w unused except x32.w)
+    double *x64, *xp64;  // nv*3
+    float4 *x32;         // float copy of x; .w = 1 on pinned vertices
+    float4 *dx, *r, *z, *p0, *p1, *q;
+    double *part;        // 3 * ntile_rows reduction partials
+    InstState *st;
+};
+
+struct Tile
+{
+    int inst;
+    int start;
+};
+
+// Batch-wide control words (one per launch set).
+struct BatchCtl
+{
+    int n_active;    // instances still iterating
+    int n_tiles_rows;
+    int n_tiles_tris;
+    int pad;
+};
+
+} // namespace cloth

@@ -1,0 +1,664 @@
+// Kernels of the implicit cloth step (sm_103a).
+//
+//   k_pins         snap pinned vertices to their targets      (UpdateConstraintVertexPos)
+//   k_tri          triangle-parallel stretch/shear force and 3x3 Hessian blocks,
+//                  written without atomics through the precomputed
+//                  triangle -> record map                     (UpdateStretch_K_fint)
+//   k_row          row-parallel reduction of the records in fixed order, bending
+//                  (K -= K_b, f -= K_b x), A = (h b - h^2) K + (1 + h a) M, RHS,
+//                  pin projection, block-Jacobi inverse and the PCG start
+//                  r = b - A dx0, z = M^-1 r                  (AddBendingHessianAndIntForce,
+//                                                              AssembleSystemRHS/Matrix,
+//                                                              BlockJacobPreconditioner,
+//                                                              Calc_r0_d0_r0Minvr0)
+//   k_spmv         p = z + beta p (recomputed at the gathered columns), q = A p,
+//                  FP64 p.q                                   (Calc_dTAd_zi, UpdateDirection)
+//   k_update       dx += alpha p, r -= alpha q, z = M^-1 r, FP64 r.z and r.r,
+//                  per-instance convergence test              (Calc_rnext_rnextMinvrnext_xnext)
+//   k_advance      x_pre = x, x += dx in FP64                 (BaraffClothGpu.cpp:246-258)
+//
+// Reference kernels: src/sim/cloth/BaraffClothGpu.cu, src/sim/cloth/gpu_solvers/PCGSolver.cu.
+#include "device.cuh"
+
+namespace cloth {
+
+namespace {
+
+__device__ __forceinline__ float3 operator+(float3 a, float3 b)
+{
+    return make_float3(a.x + b.x, a.y + b.y, a.z + b.z);
+}
+__device__ __forceinline__ float3 operator-(float3 a, float3 b)
+{
+    return make_float3(a.x - b.x, a.y - b.y, a.z - b.z);
+}
+__device__ __forceinline__ float3 operator*(float s, float3 a)
+{
+    return make_float3(s * a.x, s * a.y, s * a.z);
+}
+__device__ __forceinline__ float3 xyz(float4 v) { return make_float3(v.x, v.y, v.z); }
+__device__ __forceinline__ float4 f4(float3 v, float w = 0.f)
+{
+    return make_float4(v.x, v.y, v.z, w);
+}
+__device__ __forceinline__ double ddot(float3 a, float3 b)
+{
+    return double(a.x) * double(b.x) + double(a.y) * double(b.y) +
+           double(a.z) * double(b.z);
+}
+// sum of squares in component order, as tCudaMatrix::norm (CudaMatrix.h:314-320)
+__device__ __forceinline__ float norm3(float3 a)
+{
+    float s = a.x * a.x;
+    s = s + a.y * a.y;
+    s = s + a.z * a.z;
+    return sqrtf(s);
+}
+// symmetric 3x3 (00 01 02 11 12 22) times vector
+__device__ __forceinline__ float3 symv(const float *s, float3 v)
+{
+    return make_float3(s[0] * v.x + s[1] * v.y + s[2] * v.z,
+                       s[1] * v.x + s[3] * v.y + s[4] * v.z,
+                       s[2] * v.x + s[4] * v.y + s[5] * v.z);
+}
+__device__ __forceinline__ void load_sym(const float4 *a0, const float2 *a1,
+                                         size_t o, float *s)
+{
+    float4 u = a0[o];
+    float2 w = a1[o];
+    s[0] = u.x;
+    s[1] = u.y;
+    s[2] = u.z;
+    s[3] = u.w;
+    s[4] = w.x;
+    s[5] = w.y;
+}
+
+// Symmetric 3x3 inverse by the adjugate, as tCudaMatrix::inverse
+// (CudaMatrix.h:362-398) evaluates it for a symmetric block.
+__device__ __forceinline__ void sym_inverse(const float *a, float *m)
+{
+    // a = [[a0 a1 a2] [a1 a3 a4] [a2 a4 a5]]
+    float c00 = a[3] * a[5] - a[4] * a[4];
+    float c01 = a[2] * a[4] - a[1] * a[5];
+    float c02 = a[1] * a[4] - a[2] * a[3];
+    float c11 = a[0] * a[5] - a[2] * a[2];
+    float c12 = a[2] * a[1] - a[0] * a[4];
+    float c22 = a[0] * a[3] - a[1] * a[1];
+    float det = a[0] * c00 + a[1] * c01 + a[2] * c02;
+    float inv = float(1.0 / double(det));
+    m[0] = c00 * inv;
+    m[1] = c01 * inv;
+    m[2] = c02 * inv;
+    m[3] = c11 * inv;
+    m[4] = c12 * inv;
+    m[5] = c22 * inv;
+}
+
+// Sum N doubles over the block; thread 0 gets the totals. Fixed order.
+template <int N>
+__device__ __forceinline__ void block_sum(double (&v)[N], double (*sh)[kTile / 32])
+{
+#pragma unroll
+    for (int k = 0; k < N; k++)
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1)
+            v[k] += __shfl_down_sync(0xffffffffu, v[k], o);
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    if (l == 0)
+#pragma unroll
+        for (int k = 0; k < N; k++)
+            sh[k][w] = v[k];
+    __syncthreads();
+    if (threadIdx.x == 0)
+#pragma unroll
+        for (int k = 0; k < N; k++)
+        {
+            double s = sh[k][0];
+#pragma unroll
+            for (int j = 1; j < kTile / 32; j++)
+                s += sh[k][j];
+            v[k] = s;
+        }
+    __syncthreads();
+}
+
+// Publish this tile's N partials and find out whether it is the instance's
+// last tile. When it is, every thread of the block returns true and totals
+// holds the instance sums (summed in tile order, deterministic).
+template <int N>
+__device__ bool tile_reduce(const InstDesc &d, int tile_idx, double (&v)[N],
+                            double (&totals)[N], double (*sh)[kTile / 32],
+                            int *flag)
+{
+    block_sum<N>(v, sh);
+    const int nt = d.ntile_rows;
+    if (threadIdx.x == 0)
+    {
+#pragma unroll
+        for (int k = 0; k < N; k++)
+            d.part[k * nt + tile_idx] = v[k];
+        __threadfence();
+        unsigned prev = atomicAdd(&d.st->ticket, 1u);
+        *flag = (prev == unsigned(nt - 1));
+    }
+    __syncthreads();
+    if (!*flag)
+        return false;
+    __threadfence();
+    double s[N];
+#pragma unroll
+    for (int k = 0; k < N; k++)
+        s[k] = 0.0;
+    // fixed thread -> tile assignment, then a fixed-order block sum
+    for (int i = threadIdx.x; i < nt; i += kTile)
+#pragma unroll
+        for (int k = 0; k < N; k++)
+            s[k] += __ldcg(&d.part[k * nt + i]);
+    block_sum<N>(s, sh);
+#pragma unroll
+    for (int k = 0; k < N; k++)
+        totals[k] = s[k];
+    return true;
+}
+
+__device__ __forceinline__ bool test_converged(const InstDesc &d,
+                                               const InstState &s, double rr)
+{
+    bool ok = false;
+    if (d.rel_tol2 > 0.0 && rr <= d.rel_tol2 * s.bb)
+        ok = true;
+    if (d.abs_tol2 > 0.0 && rr <= d.abs_tol2)
+        ok = true;
+    return ok;
+}
+
+// An instance leaves the loop: the thread that retires the last active one
+// clears the graph's while condition.
+__device__ __forceinline__ void retire(BatchCtl *ctl, bool use_cond,
+                                       cudaGraphConditionalHandle h)
+{
+    int prev = atomicSub(&ctl->n_active, 1);
+    if (use_cond && prev == 1)
+        cudaGraphSetConditional(h, 0u);
+}
+
+// One stretch component (warp/weft or the 45-degree bias frame) of one
+// triangle: UpdateComponent / CalcFint / CalcHessian (BaraffClothGpu.cu:7-109).
+// Adds the force columns to f and -S*(Ku cu cu^T Du + Kv cv cv^T Dv) to the six
+// unique blocks hb[pair][6] (pairs 00 01 02 11 12 22).
+// F = c0 x0 + c1 x1 + c2 x2 is evaluated as c1 e1 + c2 e2 + (c0+c1+c2) x0 with
+// the edge vectors e1 = x1 - x0, e2 = x2 - x0 formed from the FP64 positions:
+// the same value, without the cancellation of three O(|c| |x|) terms in FP32.
+__device__ __forceinline__ float3 deformation(const float *c, float3 e1, float3 e2,
+                                              float3 x0)
+{
+    const float s = float((double(c[0]) + double(c[1])) + double(c[2]));
+    return c[1] * e1 + c[2] * e2 + s * x0;
+}
+
+__device__ __forceinline__ void stretch_component(
+    float Ku, float Kv, float S, const float *cu, const float *cv, float3 e1,
+    float3 e2, float3 x0, bool fix_fv, float3 *f, float (*hb)[6])
+{
+    float3 Fu = deformation(cu, e1, e2, x0);
+    float3 Fv = deformation(cv, e1, e2, x0);
+    float nu = norm3(Fu), nv = norm3(Fv);
+    float Cu = nu - 1.f, Cv = nv - 1.f;
+    float3 uh = make_float3(Fu.x / nu, Fu.y / nu, Fu.z / nu);
+    float3 vh = make_float3(Fv.x / nv, Fv.y / nv, Fv.z / nv);
+    // CalcFint: u_base = -S Ku Cu Fu/|Fu|, v_base likewise
+    float su = -S * Ku * Cu, sv = -S * Kv * Cv;
+    float3 ub = su * uh, vb = sv * vh;
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+        f[i] = f[i] + (cu[i] * ub + cv[i] * vb);
+    // CalcHessian: D = n n^T / |F| + [|F| > 1] (1 - 1/|F|) I. The reference
+    // uses |Fu| for the weft term as well (BaraffClothGpu.cu:54-55).
+    float nvh = fix_fv ? nv : nu;
+    float iu = float(1.0 / double(nu)), iv = float(1.0 / double(nvh));
+    float eu = (nu > 1.f) ? float(1.0 - 1.0 / double(nu)) : 0.f;
+    float ev = (nvh > 1.f) ? float(1.0 - 1.0 / double(nvh)) : 0.f;
+    float Du[6] = {iu * uh.x * uh.x + eu, iu * uh.x * uh.y, iu * uh.x * uh.z,
+                   iu * uh.y * uh.y + eu, iu * uh.y * uh.z, iu * uh.z * uh.z + eu};
+    float Dv[6] = {iv * vh.x * vh.x + ev, iv * vh.x * vh.y, iv * vh.x * vh.z,
+                   iv * vh.y * vh.y + ev, iv * vh.y * vh.z, iv * vh.z * vh.z + ev};
+    const int pa[6] = {0, 0, 0, 1, 1, 2}, pb[6] = {0, 1, 2, 1, 2, 2};
+#pragma unroll
+    for (int p = 0; p < 6; p++)
+    {
+        float wu = -S * (Ku * cu[pa[p]] * cu[pb[p]]);
+        float wv = -S * (Kv * cv[pa[p]] * cv[pb[p]]);
+#pragma unroll
+        for (int k = 0; k < 6; k++)
+            hb[p][k] += wu * Du[k] + wv * Dv[k];
+    }
+}
+
+} // namespace
+
+// ------------------------------------------------------------------ pins
+// UpdateConstraintVertexPos (BaraffClothGpu.cpp:411-436): pinned vertices are
+// put at their target in x and x_pre; x32.w marks them for the row pass.
+__global__ void k_pins(InstDesc *const *descs, const int *inst_list, int ninst)
+{
+    for (int i = blockIdx.x; i < ninst; i += gridDim.x)
+    {
+        const InstDesc &d = *descs[inst_list[i]];
+        for (int k = threadIdx.x; k < d.npins; k += blockDim.x)
+        {
+            int v = d.pin_vid[k];
+            float4 t = d.pin_tgt[k];
+            double tx = t.x, ty = t.y, tz = t.z;
+            d.x64[3 * v + 0] = tx;
+            d.x64[3 * v + 1] = ty;
+            d.x64[3 * v + 2] = tz;
+            d.xp64[3 * v + 0] = tx;
+            d.xp64[3 * v + 1] = ty;
+            d.xp64[3 * v + 2] = tz;
+            d.x32[v] = make_float4(t.x, t.y, t.z, 1.f);
+        }
+    }
+}
+
+// ------------------------------------------------------------------ triangles
+__global__ void __launch_bounds__(kTile) k_tri(InstDesc *const *descs,
+                                               const Tile *tiles,
+                                               const BatchCtl *ctl)
+{
+    const int ntiles = ctl->n_tiles_tris;
+    for (int ti = blockIdx.x; ti < ntiles; ti += gridDim.x)
+    {
+        const Tile tl = tiles[ti];
+        const InstDesc &d = *descs[tl.inst];
+        const int t = tl.start + threadIdx.x;
+        if (t >= d.nt)
+            continue;
+        const int4 tv = d.tri[t];
+        const float S = __int_as_float(tv.w);
+        const float4 c0 = d.tcoef[3 * t + 0], c1 = d.tcoef[3 * t + 1],
+                     c2 = d.tcoef[3 * t + 2];
+        const float cuw[3] = {c0.x, c0.y, c0.z}, cvw[3] = {c0.w, c1.x, c1.y};
+        const float cud[3] = {c1.z, c1.w, c2.x}, cvd[3] = {c2.y, c2.z, c2.w};
+        const double *p0 = d.x64 + 3 * tv.x, *p1 = d.x64 + 3 * tv.y,
+                     *p2 = d.x64 + 3 * tv.z;
+        const double a0 = p0[0], a1 = p0[1], a2 = p0[2];
+        const float3 x0 = make_float3(float(a0), float(a1), float(a2));
+        const float3 e1 = make_float3(float(p1[0] - a0), float(p1[1] - a1),
+                                      float(p1[2] - a2));
+        const float3 e2 = make_float3(float(p2[0] - a0), float(p2[1] - a1),
+                                      float(p2[2] - a2));
+        float3 f[3] = {make_float3(0, 0, 0), make_float3(0, 0, 0),
+                       make_float3(0, 0, 0)};
+        float hb[6][6];
+#pragma unroll
+        for (int p = 0; p < 6; p++)
+#pragma unroll
+            for (int k = 0; k < 6; k++)
+                hb[p][k] = 0.f;
+        const bool fix = d.fix_fv_norm != 0;
+        stretch_component(d.k_warp, d.k_weft, S, cuw, cvw, e1, e2, x0, fix, f, hb);
+        stretch_component(d.k_bias, d.k_bias, S, cud, cvd, e1, e2, x0, fix, f, hb);
+
+        const int4 g0 = d.tdest[3 * t + 0], g1 = d.tdest[3 * t + 1],
+                   g2 = d.tdest[3 * t + 2];
+        // h_dest[a*3+b] for a,b in 0..2, then f_dest[0..2]
+        const int hd[9] = {g0.x, g0.y, g0.z, g0.w, g1.x, g1.y, g1.z, g1.w, g2.x};
+        const int fd[3] = {g2.y, g2.z, g2.w};
+        const int pa[6] = {0, 0, 0, 1, 1, 2}, pb[6] = {0, 1, 2, 1, 2, 2};
+#pragma unroll
+        for (int p = 0; p < 6; p++)
+        {
+            HRec r;
+            r.h0 = make_float4(hb[p][0], hb[p][1], hb[p][2], hb[p][3]);
+            r.h1 = make_float4(hb[p][4], hb[p][5], 0.f, 0.f);
+            d.hrec[hd[pa[p] * 3 + pb[p]]] = r;
+            if (pa[p] != pb[p])
+                d.hrec[hd[pb[p] * 3 + pa[p]]] = r;
+        }
+#pragma unroll
+        for (int a = 0; a < 3; a++)
+            d.frec[fd[a]] = f4(f[a]);
+    }
+}
+
+// ------------------------------------------------------------------ rows
+__global__ void __launch_bounds__(kTile) k_row(InstDesc *const *descs,
+                                               const Tile *tiles, BatchCtl *ctl)
+{
+    __shared__ double sh[3][kTile / 32];
+    __shared__ int flag;
+    const int ntiles = ctl->n_tiles_rows;
+    for (int ti = blockIdx.x; ti < ntiles; ti += gridDim.x)
+    {
+        const Tile tl = tiles[ti];
+        const InstDesc &d = *descs[tl.inst];
+        const int row = tl.start + threadIdx.x;
+        double part[3] = {0.0, 0.0, 0.0};
+        if (row < d.nv)
+        {
+            const int info = d.rowinfo[row];
+            const int len = info & 255, ds = (info >> 8) & 255;
+            const float4 xv = d.x32[row];
+            const bool fixv = xv.w != 0.f;
+            const float m = d.mass[row];
+            float3 f = make_float3(0, 0, 0);
+            for (int k = d.fptr[row]; k < d.fptr[row + 1]; k++)
+                f = f + xyz(d.frec[k]);
+            float3 acc = make_float3(0, 0, 0);
+            float ad[6] = {0, 0, 0, 0, 0, 0};
+            for (int s = 0; s < len; s++)
+            {
+                const size_t o = size_t(s) * d.stride + row;
+                const int c = d.col[o];
+                const uint32_t hs = d.hsrc[o];
+                const float kbv = d.kb[o];
+                float K[6] = {0, 0, 0, 0, 0, 0};
+                const uint32_t r0 = hs >> 5, cnt = hs & 31u;
+                for (uint32_t k = 0; k < cnt; k++)
+                {
+                    const HRec h = d.hrec[r0 + k];
+                    K[0] += h.h0.x;
+                    K[1] += h.h0.y;
+                    K[2] += h.h0.z;
+                    K[3] += h.h0.w;
+                    K[4] += h.h1.x;
+                    K[5] += h.h1.y;
+                }
+                const float4 xc = (c == row) ? xv : d.x32[c];
+                // bending: K -= K_b (K_b = kb I), f += -K_b x
+                f = f - kbv * xyz(xc);
+                K[0] -= kbv;
+                K[3] -= kbv;
+                K[5] -= kbv;
+                float A[6];
+#pragma unroll
+                for (int k = 0; k < 6; k++)
+                    A[k] = d.c_stiff * K[k];
+                bool zero = false;
+                if (s == ds)
+                {
+                    const float md = m * d.c_mass;
+                    A[0] += md;
+                    A[3] += md;
+                    A[5] += md;
+#pragma unroll
+                    for (int k = 0; k < 6; k++)
+                        ad[k] = A[k];
+                }
+                else if (fixv || xc.w != 0.f)
+                {
+                    zero = true;
+#pragma unroll
+                    for (int k = 0; k < 6; k++)
+                        A[k] = 0.f;
+                }
+                d.A0[o] = make_float4(A[0], A[1], A[2], A[3]);
+                d.A1[o] = make_float2(A[4], A[5]);
+                if (d.warm_start && !zero && !fixv)
+                    acc = acc + symv(A, xyz(d.dx[c]));
+            }
+            // AssembleSystemRHSKernel (BaraffClothGpu.cu:301-344)
+            const float3 g = make_float3(0.f, d.grav[row], 0.f);
+            const float3 xc = make_float3(float(d.x64[3 * row + 0]),
+                                          float(d.x64[3 * row + 1]),
+                                          float(d.x64[3 * row + 2]));
+            const float3 xp = make_float3(float(d.xp64[3 * row + 0]),
+                                          float(d.xp64[3 * row + 1]),
+                                          float(d.xp64[3 * row + 2]));
+            float3 b = d.h2 * (g + f) + m * (xc - xp);
+            if (fixv)
+                b = make_float3(0, 0, 0);
+            float M[6];
+            sym_inverse(ad, M);
+            float3 r = b - acc;
+            if (fixv || !d.warm_start)
+                d.dx[row] = make_float4(0, 0, 0, 0);
+            if (fixv)
+                r = make_float3(0, 0, 0);
+            const float3 z = symv(M, r);
+            d.b[row] = f4(b);
+            d.r[row] = f4(r);
+            d.z[row] = f4(z);
+            d.M0[row] = make_float4(M[0], M[1], M[2], M[3]);
+            d.M1[row] = make_float2(M[4], M[5]);
+            part[0] = ddot(r, z);
+            part[1] = ddot(r, r);
+            part[2] = ddot(b, b);
+        }
+        double tot[3];
+        if (tile_reduce<3>(d, tl.start / kTile, part, tot, sh, &flag) &&
+            threadIdx.x == 0)
+        {
+            InstState &st = *d.st;
+            st.ticket = 0u;
+            st.rho = tot[0];
+            st.rr = tot[1];
+            st.rr0 = tot[1];
+            st.bb = tot[2];
+            st.beta = 0.0;
+            st.alpha = 0.0;
+            st.pq = 0.0;
+            st.iter = 0;
+            st.status = 0;
+            if (!isfinite(tot[0]) || !isfinite(tot[1]) || !isfinite(tot[2]))
+            {
+                st.status = 6; // CLOTH_ERR_NAN
+                st.active = 0;
+            }
+            else if (d.max_iters <= 0 || test_converged(d, st, tot[1]))
+            {
+                st.active = 0;
+            }
+            else
+            {
+                st.active = 1;
+                atomicAdd(&ctl->n_active, 1);
+            }
+        }
+    }
+}
+
+// Sets the while condition from the active count (one thread).
+__global__ void k_cond(const BatchCtl *ctl, cudaGraphConditionalHandle h)
+{
+    cudaGraphSetConditional(h, ctl->n_active > 0 ? 1u : 0u);
+}
+
+// ------------------------------------------------------------------ PCG
+__global__ void __launch_bounds__(kTile) k_spmv(InstDesc *const *descs,
+                                                const Tile *tiles,
+                                                BatchCtl *ctl, int use_cond,
+                                                cudaGraphConditionalHandle h)
+{
+    __shared__ double sh[1][kTile / 32];
+    __shared__ int flag;
+    const int ntiles = ctl->n_tiles_rows;
+    for (int ti = blockIdx.x; ti < ntiles; ti += gridDim.x)
+    {
+        const Tile tl = tiles[ti];
+        const InstDesc &d = *descs[tl.inst];
+        InstState *stp = d.st;
+        if (!stp->active)
+            continue;
+        const int it = stp->iter;
+        const float beta = float(stp->beta);
+        const float4 *pold = (it & 1) ? d.p1 : d.p0;
+        float4 *pnew = (it & 1) ? d.p0 : d.p1;
+        const int row = tl.start + threadIdx.x;
+        double part[1] = {0.0};
+        if (row < d.nv)
+        {
+            const int len = d.rowinfo[row] & 255;
+            float3 pv = xyz(d.z[row]);
+            if (beta != 0.f)
+                pv = pv + beta * xyz(pold[row]);
+            pnew[row] = f4(pv);
+            float3 q = make_float3(0, 0, 0);
+            for (int s = 0; s < len; s++)
+            {
+                const size_t o = size_t(s) * d.stride + row;
+                const int c = d.col[o];
+                float A[6];
+                load_sym(d.A0, d.A1, o, A);
+                float3 pc;
+                if (c == row)
+                    pc = pv;
+                else
+                {
+                    pc = xyz(d.z[c]);
+                    if (beta != 0.f)
+                        pc = pc + beta * xyz(pold[c]);
+                }
+                q = q + symv(A, pc);
+            }
+            d.q[row] = f4(q);
+            part[0] = ddot(pv, q);
+        }
+        double tot[1];
+        if (tile_reduce<1>(d, tl.start / kTile, part, tot, sh, &flag) &&
+            threadIdx.x == 0)
+        {
+            InstState &st = *stp;
+            st.ticket = 0u;
+            st.pq = tot[0];
+            if (!isfinite(tot[0]))
+            {
+                st.status = 6;
+                st.active = 0;
+                retire(ctl, use_cond, h);
+            }
+            else if (tot[0] == 0.0)
+            {
+                // PCGSolver.cu:259-263 clamps alpha to zero; nothing moves
+                // afterwards, so the loop ends here.
+                st.status = 7;
+                st.active = 0;
+                retire(ctl, use_cond, h);
+            }
+            else
+                st.alpha = st.rho / tot[0];
+        }
+    }
+}
+
+__global__ void __launch_bounds__(kTile) k_update(InstDesc *const *descs,
+                                                  const Tile *tiles,
+                                                  BatchCtl *ctl, int use_cond,
+                                                  cudaGraphConditionalHandle h)
+{
+    __shared__ double sh[2][kTile / 32];
+    __shared__ int flag;
+    const int ntiles = ctl->n_tiles_rows;
+    for (int ti = blockIdx.x; ti < ntiles; ti += gridDim.x)
+    {
+        const Tile tl = tiles[ti];
+        const InstDesc &d = *descs[tl.inst];
+        InstState *stp = d.st;
+        if (!stp->active)
+            continue;
+        const int it = stp->iter;
+        const float alpha = float(stp->alpha);
+        const float4 *pnew = (it & 1) ? d.p0 : d.p1;
+        const int row = tl.start + threadIdx.x;
+        double part[2] = {0.0, 0.0};
+        if (row < d.nv)
+        {
+            const float3 p = xyz(pnew[row]);
+            const float3 qv = xyz(d.q[row]);
+            float3 x = xyz(d.dx[row]);
+            float3 r = xyz(d.r[row]);
+            x = make_float3(fmaf(alpha, p.x, x.x), fmaf(alpha, p.y, x.y),
+                            fmaf(alpha, p.z, x.z));
+            r = make_float3(fmaf(-alpha, qv.x, r.x), fmaf(-alpha, qv.y, r.y),
+                            fmaf(-alpha, qv.z, r.z));
+            float M[6];
+            load_sym(d.M0, d.M1, row, M);
+            const float3 z = symv(M, r);
+            d.dx[row] = f4(x);
+            d.r[row] = f4(r);
+            d.z[row] = f4(z);
+            part[0] = ddot(r, z);
+            part[1] = ddot(r, r);
+        }
+        double tot[2];
+        if (tile_reduce<2>(d, tl.start / kTile, part, tot, sh, &flag) &&
+            threadIdx.x == 0)
+        {
+            InstState &st = *stp;
+            st.ticket = 0u;
+            const double rho_new = tot[0];
+            st.beta = (st.rho == 0.0) ? 0.0 : rho_new / st.rho;
+            st.rho = rho_new;
+            st.rr = tot[1];
+            st.iter = it + 1;
+            const int n = st.iter;
+            bool stop = false;
+            if (!isfinite(tot[0]) || !isfinite(tot[1]))
+            {
+                st.status = 6;
+                stop = true;
+            }
+            else
+            {
+                const bool check =
+                    ((n - 1) % d.check_every) == 0 || n >= d.max_iters;
+                if (check && test_converged(d, st, tot[1]))
+                {
+                    st.status = 0;
+                    stop = true;
+                }
+                else if (n >= d.max_iters)
+                {
+                    st.status = 8; // CLOTH_ERR_MAXITER
+                    stop = true;
+                }
+            }
+            if (stop)
+            {
+                st.active = 0;
+                retire(ctl, use_cond, h);
+            }
+        }
+    }
+}
+
+// ------------------------------------------------------------------ advance
+__global__ void __launch_bounds__(kTile) k_advance(InstDesc *const *descs,
+                                                   const Tile *tiles,
+                                                   const BatchCtl *ctl)
+{
+    const int ntiles = ctl->n_tiles_rows;
+    for (int ti = blockIdx.x; ti < ntiles; ti += gridDim.x)
+    {
+        const Tile tl = tiles[ti];
+        const InstDesc &d = *descs[tl.inst];
+        const int row = tl.start + threadIdx.x;
+        if (row >= d.nv)
+            continue;
+        const float4 dxv = d.dx[row];
+        double x[3];
+        const double dd[3] = {double(dxv.x), double(dxv.y), double(dxv.z)};
+#pragma unroll
+        for (int k = 0; k < 3; k++)
+        {
+            const double xo = d.x64[3 * row + k];
+            d.xp64[3 * row + k] = xo;
+            x[k] = xo + dd[k];
+            d.x64[3 * row + k] = x[k];
+        }
+        d.x32[row] = make_float4(float(x[0]), float(x[1]), float(x[2]), 0.f);
+    }
+}
+
+// x32 from x64 after a host upload; clears the pin marks (k_pins sets them).
+__global__ void k_sync_x32(InstDesc *d_ptr)
+{
+    const InstDesc &d = *d_ptr;
+    for (int row = blockIdx.x * blockDim.x + threadIdx.x; row < d.nv;
+         row += gridDim.x * blockDim.x)
+        d.x32[row] = make_float4(float(d.x64[3 * row]), float(d.x64[3 * row + 1]),
+                                 float(d.x64[3 * row + 2]), 0.f);
+}
+
+} // namespace cloth

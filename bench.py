@@ -1,0 +1,400 @@
+"""Benchmark of the implicit cloth step: cloth steps/s at a 512x512 grid.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Workload (one "step"): one Baraff-Witkin implicit step of a 512x512-vertex
+cloth (262,144 vertices, 522,242 triangles), 1 m x 1 m, density 0.1, stretch
+1e3 / shear 1e2, bending 1e-3, Rayleigh a = 0.01, top corners pinned, gravity,
+dt = 2 ms; seeded perturbation x += N(0, 1e-3), v = N(0, 0.01); FP32
+assembly/SpMV with FP64 PCG reductions, PCG to 1e-6 relative residual,
+warm-started from the previous step as the reference does.
+
+N > 1 (torchrun): replicas only - every rank steps its own cloth, no
+collective on the data path; value = steps/s summed over ranks.
+--impl reference times the CPU restatement of the same step (oracle port, all
+host threads) on the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "cloth steps/s at 512² grid; served solves/s + p99 vs plain GPU PCG @1e-6 res"
+N_SIDE = 512
+DT = 2e-3
+REL_TOL = 1e-6
+MAX_ITERS = 20000
+L2_FLUSH_BYTES = 512 << 20
+
+
+def workload_conf(n=N_SIDE, dt=DT) -> dict:
+    return {"geometry_type": "regular_triangle", "cloth_size": [1.0, 1.0],
+            "subdivision": [n - 1, n - 1], "cloth_init_pos": [0.0, 0.0, 0.0],
+            "cloth_uv_rotation": 0, "cloth_stretch_stiffness": [1e3, 1e3, 1e2],
+            "cloth_bending_stiffness": [1e-3, 1e-3], "cloth_density": 0.1,
+            "rayleigh_damping_a": 0.01, "rayleigh_damping_b": 0.0,
+            "default_timestep": dt,
+            "constraints": {"static_point": [[-0.5, 0.5], [0.5, 0.5]]}}
+
+
+def initial_state(pos: np.ndarray, seed: int, dt=DT):
+    rng = np.random.default_rng(seed)
+    p = pos.reshape(-1, 3)
+    x = p + rng.normal(0.0, 1e-3, p.shape)
+    v = rng.normal(0.0, 1e-2, p.shape)
+    return x.reshape(-1).copy(), (x - dt * v).reshape(-1).copy()
+
+
+def config_block(extra=None) -> dict:
+    c = {"workload": f"single cloth {N_SIDE}x{N_SIDE} grid ({N_SIDE * N_SIDE} vertices, "
+                     f"{2 * (N_SIDE - 1) ** 2} triangles), dt={DT}, PCG rel_tol={REL_TOL}",
+         "grid": N_SIDE, "dt": DT, "rel_tol": REL_TOL,
+         "l2": f"flushed between steps ({L2_FLUSH_BYTES >> 20} MiB write)"}
+    if extra:
+        c.update(extra)
+    return c
+
+
+# ---------------------------------------------------------------- distributed
+def dist_init(n_gpus: int):
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group("gloo")
+        pg = dist
+    return rank, world, local, pg
+
+
+def barrier(pg):
+    if pg is not None:
+        pg.barrier()
+
+
+def max_over_ranks(pg, v: float) -> float:
+    if pg is None:
+        return v
+    import torch
+    t = torch.tensor([v], dtype=torch.float64)
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
+def sum_over_ranks(pg, v: float) -> float:
+    if pg is None:
+        return v
+    import torch
+    t = torch.tensor([v], dtype=torch.float64)
+    pg.all_reduce(t, op=pg.ReduceOp.SUM)
+    return float(t.item())
+
+
+# ---------------------------------------------------------------- clocks
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines: list[str] = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.th = threading.Thread(target=self._read, daemon=True)
+            self.th.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=2)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            p = [s.strip() for s in ln.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                smax.append(float(p[2]))
+            except ValueError:
+                continue
+            for nm, val in zip(names, p[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "samples": len(sm), "reasons": sorted(reasons)}
+
+
+# ---------------------------------------------------------------- helpers
+def measured_peaks() -> dict:
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return {"hbm_gbs": d.get("hbm_gbs"), "source": "measured"}
+    return {"hbm_gbs": 6800.0, "source": "fallback"}
+
+
+def ncu_traffic(kernel: str) -> float | None:
+    """DRAM bytes per launch of `kernel` from the committed ncu summary, if any."""
+    p = ROOT / "profiles" / "ncu_traffic.json"
+    if not p.exists():
+        return None
+    d = json.loads(p.read_text())
+    v = d.get(kernel, {}).get("dram_bytes_per_launch_full_workload")
+    return float(v) if v is not None else None
+
+
+def algorithmic_bytes(nv: int, nnzb: int) -> dict:
+    """Unique bytes one launch must move (FP32 6-float symmetric blocks, int32
+    columns, float4 vectors):
+      spmv_dot   : 24*nnzb (A) + 4*nnzb (cols) + 4*nv (row info)
+                   + 16*nv (z) + 16*nv (p_old) + 16*nv (p_new write) + 16*nv (q write)
+      update_dot : 16*nv * (p, q, dx, r read + dx, r, z write) + 24*nv (M^-1)
+    """
+    spmv = 28 * nnzb + 68 * nv
+    update = 16 * 7 * nv + 24 * nv
+    return {"spmv_dot": spmv, "update_dot": update}
+
+
+def count_nnzb(n_side: int) -> int:
+    from acousticsim_gb300 import _native as N
+    import ctypes as C
+    from acousticsim_gb300 import build_grid
+    m = build_grid((1.0, 1.0), (n_side - 1, n_side - 1))
+    conf = workload_conf(n_side)
+    mat = N.Material((C.c_float * 3)(*conf["cloth_stretch_stiffness"]),
+                     (C.c_float * 2)(*conf["cloth_bending_stiffness"]), 0.1, 0.01, 0.0, DT,
+                     -9.8, 0)
+    pos, uv, tris, edges = (np.ascontiguousarray(m[k]) for k in ("pos", "uv", "tris", "edges"))
+    md = N.MeshDesc(pos.shape[0], tris.shape[0], edges.shape[0], N.ptr(pos, C.c_double),
+                    N.ptr(uv, C.c_float), N.ptr(tris, C.c_int), N.ptr(edges, C.c_int))
+    ell = np.zeros((pos.shape[0], 32), np.int32)
+    N.call("cloth_host_tables", C.byref(md), C.byref(mat), None, None, N.ptr(ell, C.c_int),
+           None, None, None, None, None, None)
+    return int((ell >= 0).sum())
+
+
+# ---------------------------------------------------------------- CPU baseline
+def cpu_port_step_time(threads: int, sample_steps: int = 1, n_side: int = N_SIDE) -> dict:
+    """Times the FP64 CPU restatement of the same step (oracle port)."""
+    from acousticsim_gb300 import build_grid
+    from oracle import oracle as orc
+    conf = workload_conf(n_side)
+    mesh = build_grid((1.0, 1.0), (n_side - 1, n_side - 1))
+    pins = [n_side - 1, n_side * n_side - 1]
+    oc = orc.OracleCloth(mesh, conf, pins)
+    x, xp = initial_state(mesh["pos"], 1234)
+    oc.x, oc.xpre = x, xp
+    t0 = time.perf_counter()
+    iters = []
+    for _ in range(sample_steps):
+        it, _ = oc.step(rel_tol=REL_TOL, max_iters=MAX_ITERS, threads=threads)
+        iters.append(it)
+    dt = time.perf_counter() - t0
+    return {"seconds": dt, "steps": sample_steps, "pcg_iters": iters}
+
+
+# ---------------------------------------------------------------- reference arm
+def run_reference(args, rank, world, pg):
+    if rank != 0:
+        return
+    from acousticsim_gb300 import build as b
+    b.build_oracle()
+    from oracle import oracle as orc
+    threads = orc.max_threads()
+    # one full 512x512 step of the port takes tens of seconds, so the timed
+    # sample is min(K, 2) full steps after a small-grid warm-up
+    for _ in range(args.warmup):
+        cpu_port_step_time(threads, 1, 64)
+    n = max(1, min(args.steps, 2))
+    r = cpu_port_step_time(threads, n)
+    value = r["steps"] / r["seconds"]
+    line = {"metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": args.gpus,
+            "steps": n, "warmup": args.warmup,
+            "ms_per_step": 1e3 * r["seconds"] / r["steps"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "impl": "reference", "config": config_block({"pcg_iters": r["pcg_iters"]}),
+            "cpu_baseline": {"value": value, "unit": "steps/s", "cores": threads, "kind": "port",
+                             "sample": f"{r['steps']} full {N_SIDE}x{N_SIDE} steps, FP64 oracle "
+                                       f"port (oracle/cloth_oracle.c), {threads} OpenMP threads"},
+            "e2e": {"value": value, "unit": "steps/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------- our arm
+def run_ours(args, rank, world, local, pg):
+    import torch
+    from acousticsim_gb300 import BaraffClothGpu, ClothContext, params
+    from acousticsim_gb300 import build as b
+    b.build_all()
+    torch.cuda.set_device(local)
+    ctx = ClothContext(local)
+    stream = torch.cuda.ExternalStream(ctx.stream_ptr(), device=torch.device("cuda", local))
+    conf = workload_conf()
+    cloth = BaraffClothGpu(ctx, conf)
+    x0, xp0 = initial_state(cloth.GetInitPos(), 1234 + rank)
+    cloth.SetPos(x0)
+    cloth.SetPrePos(xp0)
+    p = params(max_iters=MAX_ITERS, rel_tol=REL_TOL)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=f"cuda:{local}")
+
+    for _ in range(args.warmup):
+        cloth.UpdatePos(0.0, p)
+
+    # ---- device-resident timed region: K steps, CUDA events per step on the
+    # library's stream, L2 flushed between steps (outside the events)
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(args.steps)]
+    iters = []
+    clocks = ClockSampler(local)
+    clocks.start()
+    barrier(pg)
+    torch.cuda.synchronize()
+    wall0 = time.perf_counter()
+    for k in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush.fill_(float(k))
+        ev[k][0].record(stream)
+        cloth.step_async(0.0, p)
+        ev[k][1].record(stream)
+        st = cloth.stats()
+        iters.append(st["iters"])
+        if st["status"] != "OK":
+            raise RuntimeError(f"step {k}: {st}")
+    torch.cuda.synchronize()
+    barrier(pg)
+    wall = time.perf_counter() - wall0
+    clk = clocks.stop()
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    t_max = max_over_ranks(pg, sum(step_ms) / 1e3)
+    steps_total = sum_over_ranks(pg, float(args.steps))
+    value = steps_total / t_max if t_max > 0 else 0.0
+    launches = sum(5 + 2 * i for i in iters)
+
+    # ---- e2e: the same steps through the C ABI with host buffers, pinned
+    nv = cloth.nv
+    hx = torch.empty(nv * 3, dtype=torch.float64, pin_memory=True).numpy()
+    hxp = torch.empty(nv * 3, dtype=torch.float64, pin_memory=True).numpy()
+    hout = torch.empty(nv * 3, dtype=torch.float64, pin_memory=True).numpy()
+    hx[:] = cloth.GetPos()
+    hxp[:] = cloth.GetPrePos()
+    barrier(pg)
+    torch.cuda.synchronize()
+    e0 = time.perf_counter()
+    for k in range(args.steps):
+        cloth.step_host(hx, hxp, hout, 0.0, p)
+        hxp[:] = hx
+        hx[:] = hout
+    torch.cuda.synchronize()
+    e_t = max_over_ranks(pg, time.perf_counter() - e0)
+    e2e = {"value": steps_total / e_t, "unit": "steps/s",
+           "h2d_bytes_per_step": 2 * nv * 3 * 8, "d2h_bytes_per_step": nv * 3 * 8,
+           "path": "cloth_step_host (C ABI): upload x and x_pre, step, download x"}
+
+    # ---- roofline: an instrumented pass of the same steps, CUDA events around
+    # every launch (host-driven launches of the same kernels)
+    ctx.set_profiling(True)
+    ctx.reset_profile()
+    for _ in range(min(args.steps, 5)):
+        cloth.UpdatePos(0.0, p)
+    prof = ctx.profile()
+    ctx.set_profiling(False)
+    nnzb = count_nnzb(N_SIDE)
+    alg = algorithmic_bytes(nv, nnzb)
+    sp = prof["spmv_dot"]
+    up = prof["update_dot"]
+    peak = measured_peaks()
+    spmv_ms = sp["ms"] / max(1, sp["launches"])
+    achieved = alg["spmv_dot"] / (spmv_ms * 1e-3) / 1e9
+    total_ms = sum(v["ms"] for v in prof.values())
+    shares = {k: round(v["ms"] / total_ms, 4) if total_ms else None for k, v in prof.items()}
+    roof = {"bound": "hbm", "kernel": "k_spmv (SpMV fused with p update and FP64 p.Ap)",
+            "achieved": achieved, "peak": peak["hbm_gbs"], "unit": "GB/s",
+            "frac": achieved / peak["hbm_gbs"], "peak_source": f"{peak['source']} hbm_gbs",
+            "traffic": ncu_traffic("k_spmv"),
+            "algorithmic_bytes_per_launch": alg["spmv_dot"],
+            "avg_launch_ms": spmv_ms,
+            "update_kernel": {"achieved": alg["update_dot"] / (up["ms"] / max(1, up["launches"]) * 1e-3) / 1e9,
+                              "algorithmic_bytes_per_launch": alg["update_dot"]},
+            "phase_share": shares,
+            "nnzb": nnzb}
+
+    # ---- CPU baseline: the FP64 port on the host cores, bounded sample
+    cpu = None
+    if rank == 0:
+        from oracle import oracle as orc
+        threads = orc.max_threads()
+        r = cpu_port_step_time(threads, 1)
+        cpu = {"value": r["steps"] / r["seconds"], "unit": "steps/s", "cores": threads,
+               "kind": "port",
+               "sample": f"1 full {N_SIDE}x{N_SIDE} step (FP64 oracle port, {r['pcg_iters'][0]} "
+                         f"PCG iterations), {threads} OpenMP threads"}
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": world,
+                "steps": args.steps, "warmup": args.warmup,
+                "ms_per_step": 1e3 * t_max / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32 (FP64 PCG reductions)",
+                "data": "synthetic (seeded perturbation of the flat 512x512 cloth)",
+                "config": config_block({"parallelism": f"replicas x{world}",
+                                        "pcg_iters_per_step": iters,
+                                        "wall_s_timed_region": wall}),
+                "e2e": e2e, "gpu_launches": launches, "clocks": clk,
+                "roofline": roof, "cpu_baseline": cpu}
+        print(json.dumps(line), flush=True)
+    cloth.close()
+    ctx.close()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    args = ap.parse_args()
+    rank, world, local, pg = dist_init(args.gpus)
+    if args.impl == "reference":
+        run_reference(args, rank, world, pg)
+    else:
+        run_ours(args, rank, world, local, pg)
+    if pg is not None:
+        pg.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,231 @@
+/*
+ * cloth_gb300.h - C ABI of the GB300 (sm_103a) Baraff-Witkin implicit cloth step.
+ *
+ * This library is a drop-in for AcousticSim's GPU cloth path
+ * (cloth_type "fem_gpu", class cBaraffClothGpu).  Every entry point below names
+ * the reference interface it replaces (paths are relative to the reference
+ * project root).  Conventions:
+ *   - every call returns an int status (CLOTH_OK = 0) and never throws;
+ *     cloth_last_error() gives a one-line message for the calling thread;
+ *   - all pointers are HOST pointers unless the name ends in _dev;
+ *   - arrays are packed row-major: positions nv*3, uv nv*2, triangles nt*3;
+ *   - 3x3 blocks exported to the caller are row-major: (i,j) -> [3*i+j];
+ *   - the library owns all device memory of a cloth; a context owns one CUDA
+ *     stream, and calls on one context are serialised by an internal mutex.
+ */
+#ifndef CLOTH_GB300_H
+#define CLOTH_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CLOTH_ABI_VERSION 1
+#define CLOTH_ELL_REF_WIDTH 32 /* tCudaVector32i, src/sim/cloth/BaraffClothGpu.h:19 */
+
+enum cloth_status {
+    CLOTH_OK = 0,
+    CLOTH_ERR_INVALID = 1,     /* bad argument or size */
+    CLOTH_ERR_CUDA = 2,        /* a CUDA runtime call failed */
+    CLOTH_ERR_OOM = 3,         /* device allocation failed */
+    CLOTH_ERR_BUDGET = 4,      /* admission refused: device-memory budget */
+    CLOTH_ERR_MESH = 5,        /* mesh unsupported (non-manifold edge, row wider than 32) */
+    CLOTH_ERR_NAN = 6,         /* NaN/Inf met in the solve (per-instance status) */
+    CLOTH_ERR_BREAKDOWN = 7,   /* PCG denominator was zero (alpha or beta clamped) */
+    CLOTH_ERR_MAXITER = 8,     /* solve stopped at max_iters above tolerance (per-instance status) */
+    CLOTH_ERR_TIMEOUT = 9,     /* a bounded device wait gave up */
+    CLOTH_ERR_UNSUPPORTED = 10,
+    CLOTH_ERR_STATE = 11       /* call out of order (e.g. solve before assemble) */
+};
+
+typedef struct cloth_ctx_s cloth_ctx;
+typedef struct cloth_s cloth_t;
+
+/* Regular grid as cTriangulator::BuildGeometry_UniformTriangle builds it
+ * (src/geometries/Triangulator.cpp:141-457, 621-658). JSON keys in quotes. */
+typedef struct {
+    double cloth_size[2];   /* "cloth_size": [height, width] in metres */
+    int subdivision[2];     /* "subdivision": [height_div, width_div] */
+    double init_pos[3];     /* "cloth_init_pos" (orientation must be zero) */
+    float uv_rotation_deg;  /* "cloth_uv_rotation": 0, 45 or 90 */
+} cloth_grid_desc;
+
+/* Triangle mesh handed to cloth_create (cBaseCloth::InitGeometry,
+ * src/sim/cloth/BaseCloth.cpp:292-416). */
+typedef struct {
+    int nv, nt, ne;        /* ne = 0 with edges = NULL: edges are derived */
+    const double *pos;     /* nv*3 rest positions; also the initial state */
+    const float *uv;       /* nv*2 material coordinates (tVertex::muv) */
+    const int *tris;       /* nt*3 vertex ids */
+    const int *edges;      /* ne*4: v0, v1, tri0, tri1 (tri1 = -1: boundary) */
+} cloth_mesh_desc;
+
+/* Material and step parameters (cBaraffClothGpu::Init,
+ * src/sim/cloth/BaraffClothGpu.cpp:24-49; JSON keys in quotes). */
+typedef struct {
+    float stretch_k[3];       /* "cloth_stretch_stiffness": warp, weft, bias (shear) */
+    float bending_k[2];       /* "cloth_bending_stiffness": u, v */
+    float density;            /* "cloth_density" (kg/m^2) */
+    float rayleigh_a;         /* "rayleigh_damping_a" */
+    float rayleigh_b;         /* "rayleigh_damping_b" */
+    double default_timestep;  /* "default_timestep" */
+    double gravity;           /* -9.8 (BaraffClothGpu.cpp:561) */
+    int fix_fv_norm;          /* 0: reference Hessian, whose weft term uses |Fu|
+                                 (BaraffClothGpu.cu:55); 1: use |Fv| */
+} cloth_material;
+
+/* PCG controls (PCGSolver::Solve, src/sim/cloth/gpu_solvers/PCGSolver.cu:332-481).
+ * The reference runs at most 100 iterations and stops when the absolute
+ * residual norm drops below 1e-10, tested every 10th iteration. */
+typedef struct {
+    int max_iters;
+    double rel_tol;      /* stop when ||r|| <= rel_tol * ||b||  (0 disables) */
+    double abs_tol;      /* stop when ||r|| <= abs_tol          (0 disables) */
+    int check_every;     /* test after iterations 1, 1+k, 1+2k, ... and at max_iters */
+    int warm_start;      /* 1: start from the previous dx (reference); 0: from zero */
+} cloth_solve_params;
+
+typedef struct {
+    int iters;            /* PCG iterations run */
+    int status;           /* CLOTH_OK, CLOTH_ERR_MAXITER, CLOTH_ERR_NAN, CLOTH_ERR_BREAKDOWN */
+    double res_norm;      /* ||r|| of the recurrence residual at exit (FP64 reduction) */
+    double rhs_norm;      /* ||b|| */
+    double rel_residual;  /* res_norm / rhs_norm */
+} cloth_solve_stats;
+
+/* ---------------------------------------------------------------- library */
+int cloth_abi_version(void);
+const char *cloth_last_error(void);
+const char *cloth_status_string(int status);
+
+/* ---------------------------------------------------------------- context */
+/* New: one device + one CUDA stream + kernel timers. */
+int cloth_ctx_create(int device, cloth_ctx **out);
+int cloth_ctx_destroy(cloth_ctx *ctx);
+int cloth_ctx_synchronize(cloth_ctx *ctx);
+/* Per-phase CUDA-event timers (cTimeUtil::Begin/End, src/utils/TimeUtil.hpp:7-32).
+ * Phases: 0 pins, 1 triangle assembly, 2 row assembly + PCG init,
+ * 3 SpMV + p.Ap, 4 update + residual, 5 position update. */
+#define CLOTH_NUM_PHASES 6
+int cloth_ctx_set_profiling(cloth_ctx *ctx, int enable);
+int cloth_ctx_get_profile(cloth_ctx *ctx, double *ms_total, long long *launches);
+int cloth_ctx_reset_profile(cloth_ctx *ctx);
+/* Device bytes held by all cloths of the context. */
+int cloth_ctx_device_bytes(cloth_ctx *ctx, size_t *bytes);
+/* The context's cudaStream_t, so callers can order their own work and CUDA
+ * events with the library's launches. */
+int cloth_ctx_get_stream(cloth_ctx *ctx, void **stream);
+
+/* ---------------------------------------------------------------- topology */
+/* cTriangulator::BuildGeometry (Triangulator.cpp:32-139) for "regular_triangle".
+ * Query sizes with all output pointers NULL, then fill. edges: ne*4 (v0, v1,
+ * tri0, tri1); boundary edges have tri1 = -1. */
+int cloth_grid_build(const cloth_grid_desc *grid, int *nv, int *nt, int *ne,
+                     double *pos, float *uv, int *tris, int *edges);
+
+/* Host-only (no device needed): the init-time tables cloth_create builds, in
+ * the reference's layout. Call with all outputs NULL to get *ne and *width.
+ * ell nv*32 (-1 padded, as InitELLMatrix), stencil ne*4, coef nt*12, area nt,
+ * mass nv, kbend nv*32 (+K_b scalar per block), tri_slot nt*9. */
+int cloth_host_tables(const cloth_mesh_desc *mesh, const cloth_material *mat,
+                      int *ne, int *width, int *ell, int *stencil, float *coef,
+                      float *area, double *mass, float *kbend, int *tri_slot);
+
+/* ---------------------------------------------------------------- cloth */
+/* cBaraffClothGpu::Init (BaraffClothGpu.cpp:24-49): builds the edge stencils,
+ * the vertex-sorted ELL pattern, the triangle->slot map, stretch coefficients
+ * (InitStretchCoef, :517-553), the constant Q-bending matrix
+ * (InitBendingMatrix/UpdateBendingMatrix, :573-680), lumped masses and gravity,
+ * and uploads everything. The initial state is x = x_pre = mesh->pos. */
+int cloth_create(cloth_ctx *ctx, const cloth_mesh_desc *mesh,
+                 const cloth_material *mat, cloth_t **out);
+int cloth_destroy(cloth_t *cloth);
+int cloth_num_vertices(const cloth_t *cloth, int *nv, int *nt, int *ne);
+/* Changes stretch/bending stiffness and damping (the reference's ImGui sliders,
+ * BaraffClothGpu.cpp:282-291, and UpdateBendingMatrix). */
+int cloth_set_material(cloth_t *cloth, const cloth_material *mat);
+
+/* Static points: cBaseCloth::InitConstraint / FindVerticesIdFromUV
+ * (BaseCloth.cpp:151-235), AddConstraintStaticVertices /
+ * ClearConstraintStaticVertices (BaseCloth.cpp:553-563). Targets are the rest
+ * positions, as cBaraffClothGpu::InitConstraint sets (BaraffClothGpu.cpp:372-384). */
+int cloth_find_vertices_from_uv(const cloth_t *cloth, const float *uv, int n,
+                                int *vids);
+int cloth_add_static_vertices(cloth_t *cloth, const int *vids, int n);
+int cloth_clear_static_vertices(cloth_t *cloth);
+int cloth_get_static_vertices(const cloth_t *cloth, int *vids, int cap, int *n);
+/* Drag point for the next step only (ApplyUserPerturbForceOnce,
+ * BaraffClothGpu.cpp:266-281). */
+int cloth_set_drag_point(cloth_t *cloth, int vid, const float target[3]);
+
+/* State (cBaseCloth::SetPos/SetPrePos/GetPos, BaseCloth.cpp:97-112;
+ * UpdatePosToCuda/UpdatePosToCpu, BaraffClothGpu.cpp:304-335). Positions are
+ * kept in FP64 on the device, as the reference keeps them on the host. */
+int cloth_set_pos(cloth_t *cloth, const double *x, int nv);
+int cloth_set_pre_pos(cloth_t *cloth, const double *x, int nv);
+int cloth_get_pos(cloth_t *cloth, double *x, int nv);
+int cloth_get_pre_pos(cloth_t *cloth, double *x, int nv);
+/* cBaraffClothGpu::Reset (BaraffClothGpu.cpp:293-299): x = x_pre = rest, dx = 0. */
+int cloth_reset(cloth_t *cloth);
+
+/* One implicit step (cBaraffClothGpu::UpdatePos, BaraffClothGpu.cpp:152-265):
+ * snap pins, assemble A and b, PCG, x_pre = x, x += dx; all on the device.
+ * dt <= 0 uses default_timestep. params NULL = library defaults
+ * (rel_tol 1e-6, max_iters 1000, check every iteration, warm start).
+ * stats may be NULL; when given, the call waits for the step to finish. */
+int cloth_step(cloth_t *cloth, double dt, const cloth_solve_params *params,
+               cloth_solve_stats *stats);
+/* The same step with host buffers, as the reference's UpdatePos exchanges them:
+ * upload x and x_pre, step, download x (any of the pointers may be NULL). */
+int cloth_step_host(cloth_t *cloth, double dt, const cloth_solve_params *params,
+                    const double *x_in, const double *x_pre_in, double *x_out,
+                    cloth_solve_stats *stats);
+
+/* ---------------------------------------------------------------- seam */
+/* Assembled system: replaces BaraffClothGpu::UpdateStretchStiffnessMatrixAndFint,
+ * AddBendingHessianAndIntForce, AssembleSystemRHS and AssembleSystemMatrix
+ * (BaraffClothGpu.cpp:52-82, BaraffClothGpu.cu:127-483). Snaps pins first,
+ * then builds A (pin-projected), b, the block-Jacobi inverse and the PCG start. */
+int cloth_assemble(cloth_t *cloth, double dt);
+/* Replaces PCGSolver::Solve (PCGSolver.cu:332-481) on the assembled system;
+ * the solution stays on the device as dx (cloth_get_dx). */
+int cloth_solve(cloth_t *cloth, const cloth_solve_params *params,
+                cloth_solve_stats *stats);
+/* x_pre = x; x += dx (BaraffClothGpu.cpp:246-258). */
+int cloth_advance(cloth_t *cloth);
+/* Statistics of the cloth's last solve (waits for the context's stream). */
+int cloth_get_stats(cloth_t *cloth, cloth_solve_stats *stats);
+int cloth_get_dx(cloth_t *cloth, double *dx, int nv);
+
+/* Exports in the reference's layout for parity checks: ell (nv*32, -1 padded,
+ * as mELLVidToGlobalVid), A (nv*32*9, row-major blocks, pinned rows/columns
+ * zeroed off the diagonal), b (nv*3), fint (nv*3: stretch + bending force),
+ * kbend (nv*32: bending scalar per block, the +K_b of mBendingStiffnessMatrixCuda).
+ * Any output pointer may be NULL. */
+int cloth_export_system(cloth_t *cloth, int *ell, float *A, float *b,
+                        float *fint, float *kbend);
+/* Per-triangle results of the last assembly: fint nt*9 (force on local vertex
+ * a at [3a+k]) and hess nt*81 (block (a,b) at [9*(3a+b)], row-major). */
+int cloth_export_triangles(cloth_t *cloth, float *fint, float *hess);
+/* Init-time tables: stencil ne*4 (mEdgeAffectVertexId, -1 on the boundary),
+ * coef nt*12 (Fu/Fv warp-weft, Fu/Fv diagonal), area nt, mass nv,
+ * tri_slot nt*9 (ELL slot of vertex b in row of vertex a). */
+int cloth_export_tables(const cloth_t *cloth, int *stencil, float *coef,
+                        float *area, float *mass, int *tri_slot);
+
+/* ---------------------------------------------------------------- batch */
+/* Many cloths of uneven sizes stepped together: one launch per phase covers
+ * every instance (a packed tile list over all of them), each instance keeps its
+ * own FP64 scalars, convergence test and iteration count, and the PCG loop is a
+ * CUDA graph with a device-side while condition. All cloths must share ctx.
+ * Each instance's result is bit-identical to stepping it alone. */
+int cloth_batch_step(cloth_ctx *ctx, cloth_t *const *cloths, int n, double dt,
+                     const cloth_solve_params *params, cloth_solve_stats *stats);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* CLOTH_GB300_H */

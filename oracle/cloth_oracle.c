@@ -1,0 +1,599 @@
+/*
+ * cloth_oracle.c - CPU restatement of AcousticSim's implicit cloth step.
+ * TEST INFRASTRUCTURE ONLY (see cloth_oracle.h): the checker of the GPU path,
+ * never part of it.  Each function cites the reference lines it restates.
+ * Built with -ffp-contract=off so x86 and Arm hosts round identically.
+ */
+#include "cloth_oracle.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#define W CLOTH_ORC_W
+
+int orc_max_threads(void)
+{
+#ifdef _OPENMP
+    return omp_get_max_threads();
+#else
+    return 1;
+#endif
+}
+
+/* ------------------------------------------------------------------ grid */
+int orc_grid(const double size[2], const int subdiv[2], const double init_pos[3],
+             float uv_rotation_deg, int *nv_out, int *nt_out, int *ne_out,
+             double *pos, float *uv, int *tris, int *edges)
+{
+    const int hd = subdiv[0], wd = subdiv[1];
+    if (hd < 1 || wd < 1)
+        return -1;
+    const int lines_h = hd + 1; /* vertices per column strip */
+    const int nv = (wd + 1) * lines_h, nt = 2 * wd * hd;
+    const int ne = (wd + 1) * hd + lines_h * wd + hd * wd;
+    if (nv_out)
+        *nv_out = nv;
+    if (nt_out)
+        *nt_out = nt;
+    if (ne_out)
+        *ne_out = ne;
+    if (!pos && !uv && !tris && !edges)
+        return 0;
+    /* Triangulator.cpp:417-455: vertex (i, j) at (i*w_unit, j*h_unit) minus the
+     * centre, i over the width divisions (outer), j over the height ones. */
+    const double h_unit = size[0] / hd, w_unit = size[1] / wd;
+    /* RotateMaterialCoordsAfterReset (:621-658): the angle is rounded to float
+     * and the 2x2 rotation is applied in float. */
+    const float ang = (float)(uv_rotation_deg / 180.0 * M_PI);
+    const float cr = (float)cos((double)ang), sr = (float)sin((double)ang);
+    for (int i = 0; i <= wd; i++)
+        for (int j = 0; j <= hd; j++)
+        {
+            const int v = i * lines_h + j;
+            double p[3];
+            p[0] = i * w_unit - size[1] / 2;
+            p[1] = j * h_unit - size[0] / 2;
+            p[2] = 0.0;
+            for (int k = 0; k < 3; k++)
+                p[k] += init_pos[k];
+            if (pos)
+                for (int k = 0; k < 3; k++)
+                    pos[3 * v + k] = p[k];
+            if (uv)
+            {
+                const float mx = (float)(p[0] + (-init_pos[0]));
+                const float my = (float)(p[1] + (-init_pos[1]));
+                uv[2 * v] = cr * mx + (-sr) * my;
+                uv[2 * v + 1] = sr * mx + cr * my;
+            }
+        }
+    /* Triangulator.cpp:192-389: two triangles per cell, diagonal direction by
+     * the parity of (row + col); edges numbered by row strips. */
+    const int per_row = 2 * hd + lines_h;
+    int t = 0;
+    for (int row = 0; row < wd; row++)
+        for (int col = 0; col < hd; col++)
+        {
+            const int a = row * lines_h + col; /* upper-left  */
+            const int bq = a + 1;              /* upper-right */
+            const int cq = a + lines_h;        /* lower-left  */
+            const int d = cq + 1;              /* lower-right */
+            const int even = ((row + col) & 1) == 0;
+            const int e_top = row * per_row + col;
+            const int e_left = row * per_row + hd + 2 * col;
+            const int e_skew = e_left + 1, e_right = e_left + 2;
+            const int e_bottom = e_top + per_row;
+            const int t0 = t, t1 = t + 1;
+            if (tris)
+            {
+                int *o = tris + 3 * t;
+                if (even)
+                {
+                    o[0] = a; o[1] = cq; o[2] = d;
+                    o[3] = a; o[4] = d;  o[5] = bq;
+                }
+                else
+                {
+                    o[0] = a;  o[1] = cq; o[2] = bq;
+                    o[3] = cq; o[4] = d;  o[5] = bq;
+                }
+            }
+            t += 2;
+            if (!edges)
+                continue;
+#define SETE(id, v0, v1, ta, tb)                                               \
+    do                                                                         \
+    {                                                                          \
+        edges[4 * (id) + 0] = (v0);                                            \
+        edges[4 * (id) + 1] = (v1);                                            \
+        edges[4 * (id) + 2] = (ta);                                            \
+        edges[4 * (id) + 3] = (tb);                                            \
+    } while (0)
+            if (even)
+                SETE(e_skew, a, d, t0, t1);
+            else
+                SETE(e_skew, bq, cq, t0, t1);
+            {
+                const int ta = even ? t0 : t1;
+                SETE(e_bottom, cq, d, ta, row == wd - 1 ? -1 : ta + 2 * hd);
+            }
+            SETE(e_right, bq, d, t1, col == hd - 1 ? -1 : t1 + 1);
+            if (row == 0)
+                SETE(e_top, a, bq, even ? t1 : t0, -1);
+            if (col == 0)
+                SETE(e_left, a, cq, t0, -1);
+#undef SETE
+        }
+    return 0;
+}
+
+/* ------------------------------------------------------------------ tables */
+static double cot_ref(const double *A, const double *B, const double *C)
+{
+    /* CalcCotangent (QBendingMaterial.cpp:11-19): dots rounded to float. */
+    double ab[3], ac[3];
+    for (int k = 0; k < 3; k++)
+    {
+        ab[k] = B[k] - A[k];
+        ac[k] = C[k] - A[k];
+    }
+    const float d_bc = (float)((ab[0] * ac[0] + ab[1] * ac[1]) + ab[2] * ac[2]);
+    const float d_bb = (float)((ab[0] * ab[0] + ab[1] * ab[1]) + ab[2] * ab[2]);
+    const float d_cc = (float)((ac[0] * ac[0] + ac[1] * ac[1]) + ac[2] * ac[2]);
+    const float den = d_bb * d_cc - d_bc * d_bc;
+    return (double)(d_bc / sqrtf(den));
+}
+
+static int row_insert(int *row, int *len, int v)
+{
+    int k = 0;
+    while (k < *len && row[k] < v)
+        k++;
+    if (k < *len && row[k] == v)
+        return 0;
+    if (*len >= W)
+        return -1;
+    memmove(row + k + 1, row + k, sizeof(int) * (size_t)(*len - k));
+    row[k] = v;
+    (*len)++;
+    return 0;
+}
+
+static int row_find(const int *row, int v)
+{
+    for (int k = 0; k < W && row[k] >= 0; k++)
+        if (row[k] == v)
+            return k;
+    return -1;
+}
+
+static int third_vertex(const int *tri, int a, int b)
+{
+    /* SelectAnotherVerteix (BaseCloth.cpp:281-290) */
+    int best = -1;
+    for (int k = 0; k < 3; k++)
+        if (tri[k] != a && tri[k] != b && (best < 0 || tri[k] < best))
+            best = tri[k];
+    return best;
+}
+
+int orc_tables(int nv, int nt, int ne, const double *pos, const float *uv,
+               const int *tris, const int *edges, float density,
+               const float bending_k[2], int *stencil, float *area, double *mass,
+               int *ell, float *coef, float *diag16, float *edge_k, double *kbend)
+{
+    /* stencils: BaseCloth.cpp:383-405 */
+    for (int e = 0; e < ne; e++)
+    {
+        const int *ed = edges + 4 * e;
+        int *s = stencil + 4 * e;
+        if (ed[3] < 0)
+        {
+            s[0] = s[1] = s[2] = s[3] = -1;
+            continue;
+        }
+        s[0] = ed[0];
+        s[1] = ed[1];
+        s[2] = third_vertex(tris + 3 * ed[2], ed[0], ed[1]);
+        s[3] = third_vertex(tris + 3 * ed[3], ed[0], ed[1]);
+    }
+    /* areas (MathUtil2.cpp:353-357) and masses (BaseCloth.cpp:418-446) */
+    for (int v = 0; v < nv; v++)
+        mass[v] = 0.0;
+    for (int t = 0; t < nt; t++)
+    {
+        const double *p0 = pos + 3 * tris[3 * t], *p1 = pos + 3 * tris[3 * t + 1],
+                     *p2 = pos + 3 * tris[3 * t + 2];
+        double u[3], w[3], c[3];
+        for (int k = 0; k < 3; k++)
+        {
+            u[k] = p1[k] - p0[k];
+            w[k] = p2[k] - p0[k];
+        }
+        c[0] = u[1] * w[2] - u[2] * w[1];
+        c[1] = u[2] * w[0] - u[0] * w[2];
+        c[2] = u[0] * w[1] - u[1] * w[0];
+        double sq = c[0] * c[0] + c[1] * c[1];
+        sq = sq + c[2] * c[2];
+        area[t] = (float)(0.5 * sqrt(sq));
+        for (int k = 0; k < 3; k++)
+            mass[tris[3 * t + k]] += (double)area[t] / 3;
+    }
+    for (int v = 0; v < nv; v++)
+        mass[v] = mass[v] * (double)density;
+    /* ELL: BaraffClothGpu.cpp:438-500 */
+    int *len = (int *)calloc((size_t)nv, sizeof(int));
+    for (size_t k = 0; k < (size_t)nv * W; k++)
+        ell[k] = -1;
+    int bad = 0;
+    for (int v = 0; v < nv; v++)
+        bad |= row_insert(ell + (size_t)v * W, &len[v], v);
+    for (int e = 0; e < ne && !bad; e++)
+    {
+        const int *s = stencil + 4 * e;
+        if (s[0] < 0)
+            continue;
+        for (int i = 0; i < 4; i++)
+            for (int j = 0; j < 4; j++)
+                bad |= row_insert(ell + (size_t)s[i] * W, &len[s[i]], s[j]);
+    }
+    for (int t = 0; t < nt && !bad; t++)
+        for (int a = 0; a < 3; a++)
+            for (int b = 0; b < 3; b++)
+                bad |= row_insert(ell + (size_t)tris[3 * t + a] * W,
+                                  &len[tris[3 * t + a]], tris[3 * t + b]);
+    free(len);
+    if (bad)
+        return -1;
+    /* stretch coefficients: BaraffClothGpu.cpp:504-553, BaraffMaterial.cpp:18-32 */
+    const double q = M_PI / 4, rc = cos(q), rs = sin(q);
+    for (int t = 0; t < nt; t++)
+    {
+        const float *u0 = uv + 2 * tris[3 * t], *u1 = uv + 2 * tris[3 * t + 1],
+                    *u2 = uv + 2 * tris[3 * t + 2];
+        const double m00 = (double)(u1[0] - u0[0]), m01 = (double)(u2[0] - u0[0]);
+        const double m10 = (double)(u1[1] - u0[1]), m11 = (double)(u2[1] - u0[1]);
+        const double id = 1.0 / (m00 * m11 - m10 * m01);
+        double inv[2][2];
+        inv[0][0] = m11 * id;
+        inv[0][1] = -m01 * id;
+        inv[1][0] = -m10 * id;
+        inv[1][1] = m00 * id;
+        float *c = coef + 12 * t;
+        for (int pass = 0; pass < 2; pass++)
+        {
+            double mm[2][2];
+            if (pass == 0)
+                memcpy(mm, inv, sizeof(mm));
+            else /* inv * R45^T, R45 = [[c, -s], [s, c]] */
+                for (int i = 0; i < 2; i++)
+                {
+                    mm[i][0] = inv[i][0] * rc + inv[i][1] * (-rs);
+                    mm[i][1] = inv[i][0] * rs + inv[i][1] * rc;
+                }
+            const float fa = (float)mm[0][0], fb = (float)mm[0][1],
+                        fc = (float)mm[1][0], fd = (float)mm[1][1];
+            float *o = c + 6 * pass;
+            o[0] = -fa - fc;
+            o[1] = fa;
+            o[2] = fc;
+            o[3] = -fb - fd;
+            o[4] = fb;
+            o[5] = fd;
+        }
+    }
+    /* bending: BaraffClothGpu.cpp:579-680, QBendingMaterial.cpp:20-43 (its
+     * Clamp calls discard their results, so nothing is clamped) */
+    for (size_t k = 0; k < (size_t)nv * W; k++)
+        kbend[k] = 0.0;
+    for (int e = 0; e < ne; e++)
+    {
+        const int *ed = edges + 4 * e;
+        float dx = uv[2 * ed[1]] - uv[2 * ed[0]];
+        float dy = uv[2 * ed[1] + 1] - uv[2 * ed[0] + 1];
+        const float n2 = dx * dx + dy * dy;
+        if (n2 > 0.f)
+        {
+            const float n = sqrtf(n2);
+            dx = dx / n;
+            dy = dy / n;
+        }
+        float th = acosf(dx * 1.f + dy * 0.f);
+        if (th > M_PI / 2.0f)
+            th = (float)(M_PI - th);
+        const float ct = cosf(th), st = sinf(th);
+        edge_k[e] = bending_k[0] * ct * ct + bending_k[1] * st * st;
+        float *dg = diag16 + 16 * e;
+        for (int k = 0; k < 16; k++)
+            dg[k] = 0.f;
+        const int *s = stencil + 4 * e;
+        if (s[0] < 0)
+            continue;
+        const float pre = (float)(3.0 / (area[ed[2]] + area[ed[3]]));
+        const double *x0 = pos + 3 * s[0], *x1 = pos + 3 * s[1],
+                     *x2 = pos + 3 * s[2], *x3 = pos + 3 * s[3];
+        const double c01 = cot_ref(x0, x1, x2), c02 = cot_ref(x0, x1, x3);
+        const double c03 = cot_ref(x1, x0, x2), c04 = cot_ref(x1, x0, x3);
+        const double cw[4] = {c03 + c04, c01 + c02, -c01 - c03, -c02 - c04};
+        for (int i = 0; i < 4; i++)
+            for (int j = 0; j < 4; j++)
+            {
+                dg[4 * i + j] = (float)(cw[i] * cw[j] * (double)pre);
+                const float val = dg[4 * i + j] * edge_k[e];
+                const int slot = row_find(ell + (size_t)s[i] * W, s[j]);
+                kbend[(size_t)s[i] * W + slot] += (double)val;
+            }
+    }
+    return 0;
+}
+
+/* ------------------------------------------------------------------ forces */
+static void stretch_term(double Ku, double Kv, double S, const float *cu,
+                         const float *cv, const double *x0, const double *x1,
+                         const double *x2, int fix_fv, double *f, double *h)
+{
+    /* BaraffMaterial.cpp:82-172 */
+    double Fu[3], Fv[3];
+    for (int k = 0; k < 3; k++)
+    {
+        Fu[k] = cu[0] * x0[k] + cu[1] * x1[k] + cu[2] * x2[k];
+        Fv[k] = cv[0] * x0[k] + cv[1] * x1[k] + cv[2] * x2[k];
+    }
+    const double nu = sqrt(Fu[0] * Fu[0] + Fu[1] * Fu[1] + Fu[2] * Fu[2]);
+    const double nv = sqrt(Fv[0] * Fv[0] + Fv[1] * Fv[1] + Fv[2] * Fv[2]);
+    double un[3], vn[3];
+    for (int k = 0; k < 3; k++)
+    {
+        un[k] = nu > 0 ? Fu[k] / nu : Fu[k];
+        vn[k] = nv > 0 ? Fv[k] / nv : Fv[k];
+    }
+    const double Cu = nu - 1, Cv = nv - 1;
+    for (int a = 0; a < 3; a++)
+        for (int k = 0; k < 3; k++)
+            f[3 * a + k] += -S * Ku * Cu * un[k] * cu[a] + -S * Kv * Cv * vn[k] * cv[a];
+    /* the weft term reuses |Fu| unless fix_fv (BaraffMaterial.cpp:141-142) */
+    const double nvh = fix_fv ? nv : nu;
+    double Du[9], Dv[9];
+    for (int r = 0; r < 3; r++)
+        for (int c = 0; c < 3; c++)
+        {
+            Du[3 * r + c] = un[r] * un[c] / nu + (r == c && nu > 1 ? 1 - 1 / nu : 0);
+            Dv[3 * r + c] = vn[r] * vn[c] / nvh + (r == c && nvh > 1 ? 1 - 1 / nvh : 0);
+        }
+    for (int a = 0; a < 3; a++)
+        for (int b = 0; b < 3; b++)
+            for (int k = 0; k < 9; k++)
+                h[9 * (3 * a + b) + k] +=
+                    -S * (Ku * cu[a] * cu[b] * Du[k] + Kv * cv[a] * cv[b] * Dv[k]);
+}
+
+void orc_triangles(int nt, const int *tris, const float *coef, const float *area,
+                   const double *x, const float stretch_k[3], int fix_fv_norm,
+                   double *fint, double *hess)
+{
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static)
+#endif
+    for (int t = 0; t < nt; t++)
+    {
+        const double *x0 = x + 3 * tris[3 * t], *x1 = x + 3 * tris[3 * t + 1],
+                     *x2 = x + 3 * tris[3 * t + 2];
+        double *f = fint + 9 * (size_t)t, *h = hess + 81 * (size_t)t;
+        memset(f, 0, 9 * sizeof(double));
+        memset(h, 0, 81 * sizeof(double));
+        const float *c = coef + 12 * (size_t)t;
+        stretch_term(stretch_k[0], stretch_k[1], area[t], c, c + 3, x0, x1, x2,
+                     fix_fv_norm, f, h);
+        stretch_term(stretch_k[2], stretch_k[2], area[t], c + 6, c + 9, x0, x1, x2,
+                     fix_fv_norm, f, h);
+    }
+}
+
+/* ------------------------------------------------------------------ system */
+void orc_system(int nv, int nt, const int *tris, const int *ell,
+                const double *tri_f, const double *tri_h, const double *kbend,
+                const double *mass, double gravity, const double *x,
+                const double *xpre, const unsigned char *fixed, double dt,
+                float ray_a, float ray_b, double *A, double *b, double *fint)
+{
+    /* K = stretch - K_b;  A = (1 + dt a) M + (dt b - dt^2) K
+     * (BaraffClothGpu.cu:240-281, 445-483); b = dt^2 (g + f) + M (x - x_pre)
+     * (:301-344) */
+    double *K = (double *)calloc((size_t)nv * W * 9, sizeof(double));
+    for (size_t k = 0; k < (size_t)nv * 3; k++)
+        fint[k] = 0.0;
+    for (int t = 0; t < nt; t++)
+        for (int a = 0; a < 3; a++)
+        {
+            const int va = tris[3 * t + a];
+            for (int k = 0; k < 3; k++)
+                fint[3 * va + k] += tri_f[9 * (size_t)t + 3 * a + k];
+            for (int bb = 0; bb < 3; bb++)
+            {
+                const int slot = row_find(ell + (size_t)va * W, tris[3 * t + bb]);
+                double *blk = K + ((size_t)va * W + slot) * 9;
+                const double *hb = tri_h + 81 * (size_t)t + 9 * (3 * a + bb);
+                for (int k = 0; k < 9; k++)
+                    blk[k] += hb[k];
+            }
+        }
+    for (int v = 0; v < nv; v++)
+        for (int s = 0; s < W; s++)
+        {
+            const int c = ell[(size_t)v * W + s];
+            if (c < 0)
+                break;
+            const double kb = kbend[(size_t)v * W + s];
+            double *blk = K + ((size_t)v * W + s) * 9;
+            for (int k = 0; k < 3; k++)
+            {
+                blk[4 * k] -= kb;
+                fint[3 * v + k] -= kb * x[3 * c + k];
+            }
+        }
+    const double cs = dt * (double)ray_b - dt * dt;
+    const double cm = 1 + dt * (double)ray_a;
+    for (int v = 0; v < nv; v++)
+    {
+        for (int s = 0; s < W; s++)
+        {
+            const int c = ell[(size_t)v * W + s];
+            double *ab = A + ((size_t)v * W + s) * 9;
+            const double *kb = K + ((size_t)v * W + s) * 9;
+            for (int k = 0; k < 9; k++)
+                ab[k] = c < 0 ? 0.0 : cs * kb[k];
+            if (c == v)
+                for (int k = 0; k < 3; k++)
+                    ab[4 * k] += cm * mass[v];
+            else if (c >= 0 && (fixed[v] || fixed[c]))
+                for (int k = 0; k < 9; k++)
+                    ab[k] = 0.0;
+        }
+        for (int k = 0; k < 3; k++)
+        {
+            const double g = (k == 1) ? gravity * mass[v] : 0.0;
+            b[3 * v + k] = fixed[v] ? 0.0
+                                    : dt * dt * (g + fint[3 * v + k]) +
+                                          mass[v] * (x[3 * v + k] - xpre[3 * v + k]);
+        }
+    }
+    free(K);
+}
+
+void orc_spmv(int nv, const int *ell, const double *A, const double *x, double *y)
+{
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static)
+#endif
+    for (int v = 0; v < nv; v++)
+    {
+        double acc[3] = {0, 0, 0};
+        for (int s = 0; s < W; s++)
+        {
+            const int c = ell[(size_t)v * W + s];
+            if (c < 0)
+                break;
+            const double *a = A + ((size_t)v * W + s) * 9;
+            for (int r = 0; r < 3; r++)
+                acc[r] += a[3 * r] * x[3 * c] + a[3 * r + 1] * x[3 * c + 1] +
+                          a[3 * r + 2] * x[3 * c + 2];
+        }
+        for (int r = 0; r < 3; r++)
+            y[3 * v + r] = acc[r];
+    }
+}
+
+/* deterministic parallel dot: fixed chunks, summed in chunk order */
+static double pdot(size_t n, const double *a, const double *b, int nth)
+{
+    enum { CH = 64 };
+    double part[CH] = {0};
+    const size_t step = (n + CH - 1) / CH;
+#ifdef _OPENMP
+#pragma omp parallel for num_threads(nth) schedule(static)
+#endif
+    for (int c = 0; c < CH; c++)
+    {
+        double s = 0;
+        const size_t lo = (size_t)c * step, hi = lo + step < n ? lo + step : n;
+        for (size_t i = lo; i < hi; i++)
+            s += a[i] * b[i];
+        part[c] = s;
+    }
+    double s = 0;
+    for (int c = 0; c < CH; c++)
+        s += part[c];
+    (void)nth;
+    return s;
+}
+
+int orc_pcg(int nv, const int *ell, const double *A, const double *b,
+            const unsigned char *fixed, double *x, int max_iters, double rel_tol,
+            double *res, int nthreads)
+{
+#ifdef _OPENMP
+    if (nthreads > 0)
+        omp_set_num_threads(nthreads);
+#endif
+    const int nth = nthreads > 0 ? nthreads : 1;
+    const size_t n3 = (size_t)nv * 3;
+    double *Mi = (double *)malloc((size_t)nv * 9 * sizeof(double));
+    double *r = (double *)malloc(n3 * sizeof(double));
+    double *z = (double *)malloc(n3 * sizeof(double));
+    double *p = (double *)malloc(n3 * sizeof(double));
+    double *q = (double *)malloc(n3 * sizeof(double));
+    /* block-Jacobi inverse of the diagonal blocks (PCGSolver.cu:23-47) */
+    for (int v = 0; v < nv; v++)
+    {
+        const int s = row_find(ell + (size_t)v * W, v);
+        const double *a = A + ((size_t)v * W + s) * 9;
+        double *m = Mi + 9 * (size_t)v;
+        m[0] = a[4] * a[8] - a[5] * a[7];
+        m[1] = a[2] * a[7] - a[1] * a[8];
+        m[2] = a[1] * a[5] - a[2] * a[4];
+        m[3] = a[5] * a[6] - a[3] * a[8];
+        m[4] = a[0] * a[8] - a[2] * a[6];
+        m[5] = a[2] * a[3] - a[0] * a[5];
+        m[6] = a[3] * a[7] - a[4] * a[6];
+        m[7] = a[1] * a[6] - a[0] * a[7];
+        m[8] = a[0] * a[4] - a[1] * a[3];
+        const double det = a[0] * m[0] + a[1] * m[3] + a[2] * m[6];
+        for (int k = 0; k < 9; k++)
+            m[k] /= det;
+    }
+    for (int v = 0; v < nv; v++)
+        if (fixed[v])
+            x[3 * v] = x[3 * v + 1] = x[3 * v + 2] = 0.0;
+    orc_spmv(nv, ell, A, x, q);
+    for (size_t i = 0; i < n3; i++)
+        r[i] = fixed[i / 3] ? 0.0 : b[i] - q[i];
+    for (int v = 0; v < nv; v++)
+        for (int k = 0; k < 3; k++)
+        {
+            const double *m = Mi + 9 * (size_t)v + 3 * k;
+            z[3 * v + k] = m[0] * r[3 * v] + m[1] * r[3 * v + 1] + m[2] * r[3 * v + 2];
+        }
+    memcpy(p, z, n3 * sizeof(double));
+    double rho = pdot(n3, r, z, nth);
+    const double bb = pdot(n3, b, b, nth);
+    double rr = pdot(n3, r, r, nth);
+    int it = 0;
+    while (it < max_iters && !(rr <= rel_tol * rel_tol * bb))
+    {
+        orc_spmv(nv, ell, A, p, q);
+        const double pq = pdot(n3, p, q, nth);
+        if (pq == 0.0)
+            break;
+        const double alpha = rho / pq;
+        for (size_t i = 0; i < n3; i++)
+        {
+            x[i] += alpha * p[i];
+            r[i] -= alpha * q[i];
+        }
+        for (int v = 0; v < nv; v++)
+            for (int k = 0; k < 3; k++)
+            {
+                const double *m = Mi + 9 * (size_t)v + 3 * k;
+                z[3 * v + k] = m[0] * r[3 * v] + m[1] * r[3 * v + 1] + m[2] * r[3 * v + 2];
+            }
+        const double rho2 = pdot(n3, r, z, nth);
+        rr = pdot(n3, r, r, nth);
+        const double beta = rho == 0.0 ? 0.0 : rho2 / rho;
+        rho = rho2;
+        for (size_t i = 0; i < n3; i++)
+            p[i] = z[i] + beta * p[i];
+        it++;
+    }
+    if (res)
+        *res = sqrt(rr);
+    free(Mi);
+    free(r);
+    free(z);
+    free(p);
+    free(q);
+    return it;
+}

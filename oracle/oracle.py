@@ -1,0 +1,190 @@
+"""ctypes front of oracle/libcloth_oracle.so - the CPU restatement of
+AcousticSim's implicit cloth step.
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and the
+CPU-baseline leg of bench.py, as the checker.  The GPU product never uses it.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+LIB = Path(__file__).resolve().parent / "libcloth_oracle.so"
+W = 32
+_lib = None
+
+PD = C.POINTER(C.c_double)
+PF = C.POINTER(C.c_float)
+PI = C.POINTER(C.c_int)
+PU8 = C.POINTER(C.c_ubyte)
+
+
+def lib() -> C.CDLL:
+    global _lib
+    if _lib is None:
+        if not LIB.exists():
+            raise ImportError(f"{LIB} missing: run `python -m acousticsim_gb300.build`")
+        L = C.CDLL(str(LIB))
+        L.orc_grid.argtypes = [PD, PI, PD, C.c_float, PI, PI, PI, PD, PF, PI, PI]
+        L.orc_tables.argtypes = [C.c_int, C.c_int, C.c_int, PD, PF, PI, PI, C.c_float, PF,
+                                 PI, PF, PD, PI, PF, PF, PF, PD]
+        L.orc_triangles.argtypes = [C.c_int, PI, PF, PF, PD, PF, C.c_int, PD, PD]
+        L.orc_triangles.restype = None
+        L.orc_system.argtypes = [C.c_int, C.c_int, PI, PI, PD, PD, PD, PD, C.c_double, PD, PD,
+                                 PU8, C.c_double, C.c_float, C.c_float, PD, PD, PD]
+        L.orc_system.restype = None
+        L.orc_spmv.argtypes = [C.c_int, PI, PD, PD, PD]
+        L.orc_spmv.restype = None
+        L.orc_pcg.argtypes = [C.c_int, PI, PD, PD, PU8, PD, C.c_int, C.c_double, PD, C.c_int]
+        L.orc_max_threads.restype = C.c_int
+        _lib = L
+    return _lib
+
+
+def _p(a, t):
+    return a.ctypes.data_as(C.POINTER(t))
+
+
+def grid(size=(1.0, 1.0), subdiv=(19, 19), init_pos=(0.0, 0.0, 0.0), uv_rot=0.0) -> dict:
+    L = lib()
+    s = np.asarray(size, np.float64)
+    d = np.asarray(subdiv, np.int32)
+    ip = np.asarray(init_pos, np.float64)
+    nv, nt, ne = C.c_int(), C.c_int(), C.c_int()
+    rc = L.orc_grid(_p(s, C.c_double), _p(d, C.c_int), _p(ip, C.c_double), float(uv_rot),
+                    C.byref(nv), C.byref(nt), C.byref(ne), None, None, None, None)
+    assert rc == 0
+    pos = np.zeros((nv.value, 3))
+    uv = np.zeros((nv.value, 2), np.float32)
+    tris = np.zeros((nt.value, 3), np.int32)
+    edges = np.zeros((ne.value, 4), np.int32)
+    L.orc_grid(_p(s, C.c_double), _p(d, C.c_int), _p(ip, C.c_double), float(uv_rot),
+               None, None, None, _p(pos, C.c_double), _p(uv, C.c_float), _p(tris, C.c_int),
+               _p(edges, C.c_int))
+    return {"pos": pos, "uv": uv, "tris": tris, "edges": edges}
+
+
+def tables(mesh: dict, density: float, bending_k) -> dict:
+    L = lib()
+    pos = np.ascontiguousarray(mesh["pos"], np.float64)
+    uv = np.ascontiguousarray(mesh["uv"], np.float32)
+    tris = np.ascontiguousarray(mesh["tris"], np.int32)
+    edges = np.ascontiguousarray(mesh["edges"], np.int32)
+    nv, nt, ne = pos.shape[0], tris.shape[0], edges.shape[0]
+    kb = np.asarray(bending_k, np.float32)
+    out = {"stencil": np.zeros((ne, 4), np.int32), "area": np.zeros(nt, np.float32),
+           "mass": np.zeros(nv), "ell": np.zeros((nv, W), np.int32),
+           "coef": np.zeros((nt, 12), np.float32), "diag16": np.zeros((ne, 16), np.float32),
+           "edge_k": np.zeros(ne, np.float32), "kbend": np.zeros((nv, W))}
+    rc = L.orc_tables(nv, nt, ne, _p(pos, C.c_double), _p(uv, C.c_float), _p(tris, C.c_int),
+                      _p(edges, C.c_int), float(density), _p(kb, C.c_float),
+                      _p(out["stencil"], C.c_int), _p(out["area"], C.c_float),
+                      _p(out["mass"], C.c_double), _p(out["ell"], C.c_int),
+                      _p(out["coef"], C.c_float), _p(out["diag16"], C.c_float),
+                      _p(out["edge_k"], C.c_float), _p(out["kbend"], C.c_double))
+    if rc != 0:
+        raise ValueError("oracle: ELL row wider than 32")
+    return out
+
+
+def triangles(mesh: dict, tab: dict, x: np.ndarray, stretch_k, fix_fv_norm=0):
+    L = lib()
+    tris = np.ascontiguousarray(mesh["tris"], np.int32)
+    nt = tris.shape[0]
+    x = np.ascontiguousarray(x, np.float64).reshape(-1)
+    ks = np.asarray(stretch_k, np.float32)
+    f = np.zeros((nt, 3, 3))
+    h = np.zeros((nt, 9, 3, 3))
+    L.orc_triangles(nt, _p(tris, C.c_int), _p(tab["coef"], C.c_float),
+                    _p(tab["area"], C.c_float), _p(x, C.c_double), _p(ks, C.c_float),
+                    int(fix_fv_norm), _p(f, C.c_double), _p(h, C.c_double))
+    return f, h
+
+
+def system(mesh: dict, tab: dict, tri_f, tri_h, x, xpre, fixed, dt, ray_a, ray_b,
+           gravity=-9.8):
+    L = lib()
+    tris = np.ascontiguousarray(mesh["tris"], np.int32)
+    nv, nt = tab["ell"].shape[0], tris.shape[0]
+    x = np.ascontiguousarray(x, np.float64).reshape(-1)
+    xpre = np.ascontiguousarray(xpre, np.float64).reshape(-1)
+    fixed = np.ascontiguousarray(fixed, np.uint8)
+    A = np.zeros((nv, W, 3, 3))
+    b = np.zeros((nv, 3))
+    f = np.zeros((nv, 3))
+    L.orc_system(nv, nt, _p(tris, C.c_int), _p(tab["ell"], C.c_int),
+                 _p(np.ascontiguousarray(tri_f), C.c_double),
+                 _p(np.ascontiguousarray(tri_h), C.c_double), _p(tab["kbend"], C.c_double),
+                 _p(tab["mass"], C.c_double), float(gravity), _p(x, C.c_double),
+                 _p(xpre, C.c_double), _p(fixed, C.c_ubyte), float(dt), float(ray_a),
+                 float(ray_b), _p(A, C.c_double), _p(b, C.c_double), _p(f, C.c_double))
+    return A, b, f
+
+
+def spmv(ell, A, x):
+    nv = ell.shape[0]
+    x = np.ascontiguousarray(x, np.float64).reshape(-1)
+    y = np.zeros(nv * 3)
+    lib().orc_spmv(nv, _p(ell, C.c_int), _p(np.ascontiguousarray(A), C.c_double),
+                   _p(x, C.c_double), _p(y, C.c_double))
+    return y
+
+
+def pcg(ell, A, b, fixed, x0=None, max_iters=100000, rel_tol=1e-12, threads=1):
+    nv = ell.shape[0]
+    x = np.zeros(nv * 3) if x0 is None else np.array(x0, np.float64).reshape(-1)
+    fixed = np.ascontiguousarray(fixed, np.uint8)
+    res = C.c_double()
+    it = lib().orc_pcg(nv, _p(ell, C.c_int), _p(np.ascontiguousarray(A), C.c_double),
+                       _p(np.ascontiguousarray(b, np.float64).reshape(-1), C.c_double),
+                       _p(fixed, C.c_ubyte), _p(x, C.c_double), int(max_iters),
+                       float(rel_tol), C.byref(res), int(threads))
+    return x, it, res.value
+
+
+def max_threads() -> int:
+    return int(lib().orc_max_threads())
+
+
+class OracleCloth:
+    """FP64 CPU step of the GPU path (Q-bending, block-Jacobi PCG, pins)."""
+
+    def __init__(self, mesh: dict, conf: dict, pins):
+        self.mesh = mesh
+        self.conf = conf
+        self.tab = tables(mesh, conf["cloth_density"], conf["cloth_bending_stiffness"][:2])
+        nv = mesh["pos"].shape[0]
+        self.fixed = np.zeros(nv, np.uint8)
+        self.fixed[np.asarray(pins, np.int64)] = 1
+        self.pins = np.asarray(pins, np.int64)
+        self.x = mesh["pos"].reshape(-1).astype(np.float64).copy()
+        self.xpre = self.x.copy()
+        self.dx = np.zeros_like(self.x)
+
+    def snap_pins(self):
+        tgt = self.mesh["pos"].astype(np.float32).astype(np.float64).reshape(-1, 3)
+        x = self.x.reshape(-1, 3)
+        xp = self.xpre.reshape(-1, 3)
+        x[self.pins] = tgt[self.pins]
+        xp[self.pins] = tgt[self.pins]
+
+    def system(self, dt=None):
+        c = self.conf
+        dt = c["default_timestep"] if dt is None else dt
+        self.snap_pins()
+        tf, th = triangles(self.mesh, self.tab, self.x, c["cloth_stretch_stiffness"][:3],
+                           c.get("fix_fv_norm", 0))
+        A, b, f = system(self.mesh, self.tab, tf, th, self.x, self.xpre, self.fixed, dt,
+                         c.get("rayleigh_damping_a", 0.0), c.get("rayleigh_damping_b", 0.0))
+        return A, b, f, tf, th
+
+    def step(self, dt=None, rel_tol=1e-10, max_iters=100000, threads=1):
+        A, b, _, _, _ = self.system(dt)
+        dx, it, res = pcg(self.tab["ell"], A, b, self.fixed, self.dx, max_iters, rel_tol,
+                          threads)
+        self.dx = dx
+        self.xpre = self.x.copy()
+        self.x = self.x + dx
+        return it, res

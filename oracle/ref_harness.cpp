@@ -1,0 +1,501 @@
+// Test infrastructure only: this program links the reference's own CPU cloth
+// code (built by oracle/Makefile from the reference sources) and writes golden
+// arrays for the parity tests.  Nothing in the product loads or runs it.
+//
+// Modes
+//   topo   <cfg.json> <outdir>                     mesh, index maps, init-time data
+//   system <cfg.json> <x.bin> <xpre.bin> <outdir>  per-triangle f/H, bending, A, b, dx
+//   step   <cfg.json> <nsteps> [x.bin xpre.bin]    time the stock "fem" UpdatePos
+//
+// Where the reference's GPU host code (src/sim/cloth/BaraffClothGpu.cpp) cannot
+// be compiled (it pulls in MSVC-only CUDA headers), the few lines of its init
+// routines are restated here on top of the reference helpers it calls
+// (CalcBaraffStretchCoef, CalcCotangentCoeff, cRotUtil::RotMat2D), each with
+// the file:line it follows.  Blocks are written row-major: (i,j) -> [3*i+j].
+#include "geometries/Primitives.h"
+#include "sim/cloth/BaraffCloth.h"
+#include "sim/cloth/BaraffMaterial.h"
+#include "sim/cloth/QBendingMaterial.h"
+#include "utils/JsonUtil.h"
+#include "utils/RotUtil.h"
+#include <Eigen/SparseCholesky>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <fstream>
+#include <iostream>
+#include <set>
+#include <string>
+#include <vector>
+
+// reference helpers (src/sim/cloth/BaraffMaterial.cpp:18, QBendingMaterial.cpp:20)
+extern void CalcBaraffStretchCoef(const tMatrix2d &mat, tVector3d &coef_u,
+                                  tVector3d &coef_v);
+extern tVector CalcCotangentCoeff(const tVector3d &x0, const tVector3d &x1,
+                                  const tVector3d &x2, const tVector3d &x3);
+
+static const int kEll = 32; // tCudaVector32i width (BaraffClothGpu.h:19)
+
+// ------------------------------------------------------------------ output
+struct Dump
+{
+    std::string dir;
+    std::ofstream manifest;
+    explicit Dump(const std::string &d) : dir(d), manifest(d + "/manifest.txt") {}
+    template <class T>
+    void put(const std::string &name, const char *dtype,
+             const std::vector<T> &v, std::vector<long> shape)
+    {
+        std::ofstream f(dir + "/" + name + ".bin", std::ios::binary);
+        f.write(reinterpret_cast<const char *>(v.data()), v.size() * sizeof(T));
+        manifest << name << " " << dtype;
+        for (long s : shape)
+            manifest << " " << s;
+        manifest << "\n";
+    }
+};
+
+static std::vector<double> read_doubles(const std::string &path, size_t n)
+{
+    std::vector<double> v(n);
+    std::ifstream f(path, std::ios::binary);
+    f.read(reinterpret_cast<char *>(v.data()), n * sizeof(double));
+    if (!f)
+    {
+        std::cerr << "short read " << path << "\n";
+        exit(2);
+    }
+    return v;
+}
+
+// ------------------------------------------------------------------ probes
+struct MatProbe : public cBaraffMaterial
+{
+    const tEigenArr<tMatrix3d> &tri_fint() const { return mTriFint; }
+    const tEigenArr<tMatrix3d> &tri_hessian() const { return mTriHessian; }
+};
+
+struct Probe : public cBaraffCloth
+{
+    using cBaraffCloth::cBaraffCloth;
+    Json::Value conf;
+
+    int nv() const { return GetNumOfVertices(); }
+    int ne() const { return GetNumOfEdges(); }
+    int nt() const { return GetNumOfTriangles(); }
+
+    // GPU-path vertex mass: cBaraffClothGpu::InitMass -> cBaseCloth::InitMass
+    // (BaseCloth.cpp:418-446).  cBaraffCloth overrides InitMass with its own
+    // variant, so the base routine is called explicitly here.
+    std::vector<double> gpu_mass()
+    {
+        cBaseCloth::InitMass(conf);
+        std::vector<double> m(nv());
+        for (int i = 0; i < nv(); i++)
+            m[i] = mVertexArray[i]->mMass;
+        return m;
+    }
+
+    // cBaraffClothGpu::InitELLMatrix (BaraffClothGpu.cpp:438-500)
+    std::vector<int> ell()
+    {
+        std::vector<std::set<int>> aff(nv());
+        for (int e = 0; e < ne(); e++)
+        {
+            if (mEdgeArray[e]->mIsBoundary)
+                continue;
+            tVector4i c = mEdgeAffectVertexId[e];
+            for (int i = 0; i < 4; i++)
+                for (int j = 0; j < 4; j++)
+                    aff[c[i]].insert(c[j]);
+        }
+        for (auto &t : mTriangleArray)
+        {
+            int v[3] = {t->mId0, t->mId1, t->mId2};
+            for (int j = 0; j < 3; j++)
+                aff[v[j]].insert(v[j]);
+        }
+        std::vector<int> out(size_t(nv()) * kEll, -1);
+        for (int i = 0; i < nv(); i++)
+        {
+            int j = 0;
+            for (int c : aff[i])
+            {
+                if (j >= kEll)
+                {
+                    std::cerr << "row " << i << " wider than 32\n";
+                    exit(3);
+                }
+                out[size_t(i) * kEll + j++] = c;
+            }
+        }
+        return out;
+    }
+
+    // cBaraffClothGpu::InitStretchCoef (BaraffClothGpu.cpp:504-553)
+    std::vector<float> stretch_coef()
+    {
+        std::vector<float> out(size_t(nt()) * 12);
+        tMatrix2d R45 = cRotUtil::RotMat2D(M_PI / 4);
+        for (int i = 0; i < nt(); i++)
+        {
+            auto tri = mTriangleArray[i];
+            auto v0 = mVertexArray[tri->mId0], v1 = mVertexArray[tri->mId1],
+                 v2 = mVertexArray[tri->mId2];
+            tMatrix2d Dminv;
+            Dminv.col(0) = (v1->muv - v0->muv).cast<double>();
+            Dminv.col(1) = (v2->muv - v0->muv).cast<double>();
+            Dminv = Dminv.inverse().eval();
+            tVector3d u, v;
+            CalcBaraffStretchCoef(Dminv, u, v);
+            for (int k = 0; k < 3; k++)
+            {
+                out[size_t(i) * 12 + 0 + k] = float(u[k]);
+                out[size_t(i) * 12 + 3 + k] = float(v[k]);
+            }
+            Dminv = Dminv * R45.transpose();
+            CalcBaraffStretchCoef(Dminv, u, v);
+            for (int k = 0; k < 3; k++)
+            {
+                out[size_t(i) * 12 + 6 + k] = float(u[k]);
+                out[size_t(i) * 12 + 9 + k] = float(v[k]);
+            }
+        }
+        return out;
+    }
+
+    // cBaraffClothGpu::InitBendingMatrix / UpdateBendingMatrix
+    // (BaraffClothGpu.cpp:573-626, 655-672): per-edge 4x4 scalar table and
+    // the direction-blended edge stiffness.
+    void bending(float Ku, float Kv, std::vector<float> &diag16,
+                 std::vector<float> &edge_k)
+    {
+        diag16.assign(size_t(ne()) * 16, 0.f);
+        edge_k.assign(ne(), 0.f);
+        for (int e = 0; e < ne(); e++)
+        {
+            auto ce = mEdgeArray[e];
+            tVector2f dir =
+                (mVertexArray[ce->mId1]->muv - mVertexArray[ce->mId0]->muv)
+                    .normalized();
+            float theta = std::acos(dir.dot(tVector2f(1, 0)));
+            if (theta > M_PI / 2.0f)
+                theta = M_PI - theta;
+            float cos_t = std::cos(theta), sin_t = std::sin(theta);
+            edge_k[e] = Ku * cos_t * cos_t + Kv * sin_t * sin_t;
+            if (ce->mIsBoundary)
+                continue;
+            float prefix = 3.0 / (mTriangleInitArea[ce->mTriangleId0] +
+                                  mTriangleInitArea[ce->mTriangleId1]);
+            tVector4i s = mEdgeAffectVertexId[e];
+            tVector coef = CalcCotangentCoeff(
+                mVertexArray[s[0]]->mPos.segment(0, 3),
+                mVertexArray[s[1]]->mPos.segment(0, 3),
+                mVertexArray[s[2]]->mPos.segment(0, 3),
+                mVertexArray[s[3]]->mPos.segment(0, 3));
+            for (int i = 0; i < 4; i++)
+                for (int j = 0; j < 4; j++)
+                    diag16[size_t(e) * 16 + i * 4 + j] =
+                        coef[i] * coef[j] * prefix;
+        }
+    }
+
+    void dump_topo(Dump &d)
+    {
+        int n = nv(), E = ne(), T = nt();
+        std::vector<double> pos(size_t(n) * 3);
+        std::vector<float> uv(size_t(n) * 2);
+        for (int i = 0; i < n; i++)
+        {
+            for (int k = 0; k < 3; k++)
+                pos[size_t(i) * 3 + k] = mVertexArray[i]->mPos[k];
+            uv[size_t(i) * 2 + 0] = mVertexArray[i]->muv[0];
+            uv[size_t(i) * 2 + 1] = mVertexArray[i]->muv[1];
+        }
+        std::vector<int> tris(size_t(T) * 3), edges(size_t(E) * 5),
+            stencil(size_t(E) * 4);
+        for (int t = 0; t < T; t++)
+        {
+            tris[size_t(t) * 3 + 0] = mTriangleArray[t]->mId0;
+            tris[size_t(t) * 3 + 1] = mTriangleArray[t]->mId1;
+            tris[size_t(t) * 3 + 2] = mTriangleArray[t]->mId2;
+        }
+        for (int e = 0; e < E; e++)
+        {
+            auto ce = mEdgeArray[e];
+            int row[5] = {ce->mId0, ce->mId1, ce->mTriangleId0,
+                          ce->mTriangleId1, ce->mIsBoundary ? 1 : 0};
+            for (int k = 0; k < 5; k++)
+                edges[size_t(e) * 5 + k] = row[k];
+            for (int k = 0; k < 4; k++)
+                stencil[size_t(e) * 4 + k] = mEdgeAffectVertexId[e][k];
+        }
+        std::vector<float> area(mTriangleInitArea.begin(),
+                                mTriangleInitArea.end());
+        std::vector<int> pins(mConstraint_StaticPointIds.begin(),
+                              mConstraint_StaticPointIds.end());
+        std::vector<double> mass_cpu(n);
+        for (int i = 0; i < n; i++)
+            mass_cpu[i] = mMassMatrixDiag[3 * i];
+
+        d.put("pos", "f8", pos, {n, 3});
+        d.put("uv", "f4", uv, {n, 2});
+        d.put("tris", "i4", tris, {T, 3});
+        d.put("edges", "i4", edges, {E, 5});
+        d.put("stencil", "i4", stencil, {E, 4});
+        d.put("tri_area", "f4", area, {T});
+        d.put("pins", "i4", pins, {long(pins.size())});
+        d.put("mass_cpu", "f8", mass_cpu, {n});
+        d.put("mass_gpu", "f8", gpu_mass(), {n});
+        d.put("ell", "i4", ell(), {n, kEll});
+        d.put("stretch_coef", "f4", stretch_coef(), {T, 12});
+        std::vector<float> diag16, edge_k;
+        tVector2d kb = cJsonUtil::ReadVectorJson(
+                           cJsonUtil::ParseAsValue("cloth_bending_stiffness",
+                                                   conf))
+                           .segment(0, 2);
+        bending(float(kb[0]), float(kb[1]), diag16, edge_k);
+        d.put("bend_diag16", "f4", diag16, {E, 16});
+        d.put("bend_edge_k", "f4", edge_k, {E});
+    }
+
+    // Reference assembled system for one GPU-path step on the given state:
+    // stretch/shear from cBaraffMaterial::Update (double), bending from
+    // cQBendingMaterial (the GPU's bending model, BaraffClothGpu.cpp:184-207),
+    // A and b by the GPU formula (BaraffClothGpu.cu:240-344), pins handled as
+    // the GPU solver does (PCGSolver.cu:126-136, 185-222), solved directly.
+    void dump_system(Dump &d, std::vector<double> x, std::vector<double> xpre)
+    {
+        int n = nv(), T = nt();
+        // Q-bending is built from the rest state, as InitBendingMatrix is.
+        auto qb = std::make_shared<cQBendingMaterial>();
+        tVector2d kb = cJsonUtil::ReadVectorJson(
+                           cJsonUtil::ParseAsValue("cloth_bending_stiffness",
+                                                   conf))
+                           .segment(0, 2);
+        qb->Init(mVertexArray, mEdgeArray, mTriangleArray,
+                 kb[0] * tVector3d::Ones());
+        tVector3d ks = cJsonUtil::ReadVectorJson(
+                           cJsonUtil::ParseAsValue("cloth_stretch_stiffness",
+                                                   conf))
+                           .segment(0, 3);
+        auto mat = std::make_shared<MatProbe>();
+        mat->Init(shared_from_this(), ks);
+        std::vector<double> mass = gpu_mass();
+        // the bending tables come from the rest state, before SetPos below
+        std::vector<float> diag16, edge_k;
+        bending(float(kb[0]), float(kb[1]), diag16, edge_k);
+
+        // UpdateConstraintVertexPos (BaraffClothGpu.cpp:411-436)
+        for (int vid : mConstraint_StaticPointIds)
+            for (int k = 0; k < 3; k++)
+            {
+                double t = double(float(mClothInitPos[3 * vid + k]));
+                x[3 * vid + k] = t;
+                xpre[3 * vid + k] = t;
+            }
+        tVectorXd X = Eigen::Map<tVectorXd>(x.data(), 3 * n);
+        tVectorXd XP = Eigen::Map<tVectorXd>(xpre.data(), 3 * n);
+        SetPos(X);
+        SetPrePos(XP);
+
+        mat->Update();
+        std::vector<double> tf(size_t(T) * 9), th(size_t(T) * 81);
+        for (int t = 0; t < T; t++)
+        {
+            const tMatrix3d &F = mat->tri_fint()[t];
+            for (int i = 0; i < 3; i++) // vertex i = column i
+                for (int k = 0; k < 3; k++)
+                    tf[size_t(t) * 9 + i * 3 + k] = F(k, i);
+            for (int b = 0; b < 9; b++)
+            {
+                const tMatrix3d &H = mat->tri_hessian()[size_t(t) * 9 + b];
+                for (int r = 0; r < 3; r++)
+                    for (int c = 0; c < 3; c++)
+                        th[size_t(t) * 81 + b * 9 + r * 3 + c] = H(r, c);
+            }
+        }
+        tVectorXd f_st = mat->CalcTotalForce();
+        tSparseMatd K_st = mat->CalcTotalStiffnessMatrix();
+        // CPU Q-bending (reference code, isotropic stiffness K_u): the
+        // cross-check the reference itself makes (BaraffClothGpu.cpp:184-207).
+        tSparseMatd K_qb = qb->GetStiffnessMatrix(); // = -Kb
+        // GPU bending: per-edge 4x4 table times the direction-blended edge
+        // stiffness, value * I3 per block (UpdateBendingStiffnessMatrixKernel,
+        // BaraffClothGpu.cu:387-426), summed in double.
+        std::vector<Eigen::Triplet<double>> btrip;
+        for (int e = 0; e < ne(); e++)
+        {
+            if (mEdgeArray[e]->mIsBoundary)
+                continue;
+            tVector4i s = mEdgeAffectVertexId[e];
+            for (int i = 0; i < 4; i++)
+                for (int j = 0; j < 4; j++)
+                {
+                    float value = diag16[size_t(e) * 16 + i * 4 + j] * edge_k[e];
+                    for (int k = 0; k < 3; k++)
+                        btrip.emplace_back(3 * s[i] + k, 3 * s[j] + k, double(value));
+                }
+        }
+        tSparseMatd Kb_gpu(3 * n, 3 * n);
+        Kb_gpu.setFromTriplets(btrip.begin(), btrip.end());
+        tVectorXd f_bd = -(Kb_gpu * X);
+        tSparseMatd K = K_st - Kb_gpu;
+
+        double dt = cJsonUtil::ParseAsDouble("default_timestep", conf);
+        double ra = cJsonUtil::ParseAsDouble("rayleigh_damping_a", conf);
+        double rb = cJsonUtil::ParseAsDouble("rayleigh_damping_b", conf);
+        std::vector<int> ellmap = ell();
+        std::vector<double> A(size_t(n) * kEll * 9, 0.0),
+            Kst(size_t(n) * kEll * 9, 0.0), Kbd(size_t(n) * kEll, 0.0),
+            Kbg(size_t(n) * kEll, 0.0);
+        tSparseMatd Kd = K; // row-major: coeff lookups
+        for (int i = 0; i < n; i++)
+            for (int s = 0; s < kEll; s++)
+            {
+                int j = ellmap[size_t(i) * kEll + s];
+                if (j < 0)
+                    break;
+                for (int r = 0; r < 3; r++)
+                    for (int c = 0; c < 3; c++)
+                    {
+                        double kv = Kd.coeff(3 * i + r, 3 * j + c);
+                        double a = (dt * rb - dt * dt) * kv;
+                        if (i == j && r == c)
+                            a += (1 + dt * ra) * mass[i];
+                        A[(size_t(i) * kEll + s) * 9 + r * 3 + c] = a;
+                        Kst[(size_t(i) * kEll + s) * 9 + r * 3 + c] =
+                            K_st.coeff(3 * i + r, 3 * j + c);
+                    }
+                Kbd[size_t(i) * kEll + s] = -K_qb.coeff(3 * i, 3 * j);
+                Kbg[size_t(i) * kEll + s] = Kb_gpu.coeff(3 * i, 3 * j);
+            }
+        std::vector<double> b(size_t(n) * 3);
+        for (int i = 0; i < n; i++)
+            for (int k = 0; k < 3; k++)
+            {
+                double g = (k == 1) ? -9.8 * mass[i] : 0.0;
+                b[3 * i + k] = dt * dt * (g + f_st[3 * i + k] + f_bd[3 * i + k]) +
+                               mass[i] * (x[3 * i + k] - xpre[3 * i + k]);
+            }
+
+        // Solve the pin-projected system (free rows and columns) exactly.
+        std::vector<int> dof_of(3 * n, -1);
+        std::vector<char> fixed(n, 0);
+        for (int vid : mConstraint_StaticPointIds)
+            fixed[vid] = 1;
+        int nf = 0;
+        for (int i = 0; i < n; i++)
+            if (!fixed[i])
+                for (int k = 0; k < 3; k++)
+                    dof_of[3 * i + k] = nf++;
+        std::vector<Eigen::Triplet<double>> trip;
+        for (int i = 0; i < n; i++)
+        {
+            if (fixed[i])
+                continue;
+            for (int s = 0; s < kEll; s++)
+            {
+                int j = ellmap[size_t(i) * kEll + s];
+                if (j < 0)
+                    break;
+                if (fixed[j])
+                    continue;
+                for (int r = 0; r < 3; r++)
+                    for (int c = 0; c < 3; c++)
+                        trip.emplace_back(
+                            dof_of[3 * i + r], dof_of[3 * j + c],
+                            A[(size_t(i) * kEll + s) * 9 + r * 3 + c]);
+            }
+        }
+        Eigen::SparseMatrix<double> Af(nf, nf);
+        Af.setFromTriplets(trip.begin(), trip.end());
+        tVectorXd bf(nf);
+        for (int i = 0; i < 3 * n; i++)
+            if (dof_of[i] >= 0)
+                bf[dof_of[i]] = b[i];
+        Eigen::SimplicialLDLT<Eigen::SparseMatrix<double>> ldlt(Af);
+        if (ldlt.info() != Eigen::Success)
+        {
+            std::cerr << "LDLT factorisation failed\n";
+            exit(4);
+        }
+        tVectorXd dxf = ldlt.solve(bf);
+        std::vector<double> dx(size_t(n) * 3, 0.0);
+        for (int i = 0; i < 3 * n; i++)
+            if (dof_of[i] >= 0)
+                dx[i] = dxf[dof_of[i]];
+
+        std::vector<double> fst(f_st.data(), f_st.data() + 3 * n),
+            fbd(f_bd.data(), f_bd.data() + 3 * n), xs(x), xps(xpre);
+        d.put("x", "f8", xs, {n, 3});
+        d.put("xpre", "f8", xps, {n, 3});
+        d.put("tri_fint", "f8", tf, {T, 3, 3});
+        d.put("tri_hess", "f8", th, {T, 9, 3, 3});
+        d.put("f_stretch", "f8", fst, {n, 3});
+        d.put("f_bend", "f8", fbd, {n, 3});
+        d.put("K_stretch", "f8", Kst, {n, kEll, 3, 3});
+        d.put("Kb_cpu", "f8", Kbd, {n, kEll});
+        d.put("Kb_gpu", "f8", Kbg, {n, kEll});
+        d.put("A", "f8", A, {n, kEll, 3, 3});
+        d.put("b", "f8", b, {n, 3});
+        d.put("dx", "f8", dx, {n, 3});
+    }
+
+    void step(int nsteps)
+    {
+        double dt = cJsonUtil::ParseAsDouble("default_timestep", conf);
+        auto t0 = std::chrono::steady_clock::now();
+        for (int s = 0; s < nsteps; s++)
+            UpdatePos(dt);
+        auto t1 = std::chrono::steady_clock::now();
+        double ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
+        printf("STEP_MS %.3f NV %d NT %d STEPS %d\n", ms / nsteps, nv(), nt(),
+               nsteps);
+    }
+};
+
+int main(int argc, char **argv)
+{
+    if (argc < 3)
+    {
+        std::cerr << "usage: ref_harness topo|system|step <cfg.json> ...\n";
+        return 1;
+    }
+    std::string mode = argv[1];
+    Json::Value conf;
+    if (!cJsonUtil::LoadJson(argv[2], conf))
+        return 1;
+    auto c = std::make_shared<Probe>(0);
+    c->conf = conf;
+    c->Init(conf);
+    if (mode == "topo" && argc >= 4)
+    {
+        Dump d(argv[3]);
+        c->dump_topo(d);
+    }
+    else if (mode == "system" && argc >= 6)
+    {
+        size_t n3 = size_t(c->nv()) * 3;
+        Dump d(argv[5]);
+        c->dump_system(d, read_doubles(argv[3], n3), read_doubles(argv[4], n3));
+    }
+    else if (mode == "step" && argc >= 4)
+    {
+        if (argc >= 6)
+        {
+            size_t n3 = size_t(c->nv()) * 3;
+            std::vector<double> x = read_doubles(argv[4], n3),
+                                xp = read_doubles(argv[5], n3);
+            c->SetPos(Eigen::Map<tVectorXd>(x.data(), n3));
+            c->SetPrePos(Eigen::Map<tVectorXd>(xp.data(), n3));
+        }
+        c->step(std::atoi(argv[3]));
+    }
+    else
+    {
+        std::cerr << "bad arguments\n";
+        return 1;
+    }
+    return 0;
+}

@@ -1,0 +1,230 @@
+"""GPU parity: the sm_103a path through the C ABI against the reference's own
+arrays (golden fixtures) and against the FP64 CPU oracle.
+
+Tolerances: index maps and tables bit-exact; forces, Hessian blocks, A and b
+within 1e-5 relative (per array, ||gpu - ref|| / ||ref||); dx to the PCG
+tolerance measured as the true FP64 residual of the GPU solution."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN_CASES, load_golden, project_pins, rel
+
+pytestmark = pytest.mark.gpu
+
+TOL_ASSEMBLY = 1e-5
+
+
+def make(ctx, conf):
+    from acousticsim_gb300 import BaraffClothGpu
+    return BaraffClothGpu(ctx, conf)
+
+
+@pytest.fixture(scope="module")
+def orc(built):
+    from oracle import oracle
+    return oracle
+
+
+@pytest.mark.parametrize("case", GOLDEN_CASES)
+def test_tables_and_pins_match_reference(ctx, case):
+    g, conf = load_golden(case)
+    c = make(ctx, conf)
+    t = c.export_tables()
+    assert np.array_equal(t["stencil"], g["topo_stencil"])
+    assert np.array_equal(t["coef"], g["topo_stretch_coef"])
+    assert np.array_equal(t["area"], g["topo_tri_area"])
+    assert np.array_equal(t["mass"], g["topo_mass_gpu"].astype(np.float32))
+    assert sorted(c.GetConstraintStaticVertices()) == sorted(g["topo_pins"].tolist())
+    ell, tris = g["topo_ell"], g["topo_tris"]
+    for a in range(3):
+        for b in range(3):
+            assert np.array_equal(ell[tris[:, a], t["tri_slot"][:, 3 * a + b]], tris[:, b])
+    c.close()
+
+
+@pytest.mark.parametrize("case", GOLDEN_CASES)
+def test_assembly_matches_reference(ctx, case):
+    g, conf = load_golden(case)
+    c = make(ctx, conf)
+    c.SetPos(g["x_in"])
+    c.SetPrePos(g["xpre_in"])
+    c.assemble()
+    s = c.export_system()
+    tr = c.export_triangles()
+    GA, Gb = project_pins(g["sys_A"], g["sys_b"], g["topo_ell"], g["topo_pins"])
+    assert np.array_equal(s["ell"], g["topo_ell"])
+    errs = {
+        "tri_fint": rel(tr["fint"], g["sys_tri_fint"]),
+        "tri_hess": rel(tr["hess"], g["sys_tri_hess"]),
+        "fint": rel(s["fint"], g["sys_f_stretch"] + g["sys_f_bend"]),
+        "kbend": rel(s["kbend"], g["sys_Kb_gpu"]),
+        "A": rel(s["A"], GA),
+        "b": rel(s["b"], Gb),
+    }
+    print(case, errs)
+    for k, e in errs.items():
+        assert e < TOL_ASSEMBLY, (k, e)
+    c.close()
+
+
+@pytest.mark.parametrize("case", GOLDEN_CASES)
+def test_solve_matches_direct_solve(ctx, orc, case):
+    from acousticsim_gb300 import params
+    g, conf = load_golden(case)
+    c = make(ctx, conf)
+    c.SetPos(g["x_in"])
+    c.SetPrePos(g["xpre_in"])
+    c.assemble()
+    st = c.solve(params(max_iters=20000, rel_tol=1e-6))
+    assert st["status"] == "OK", st
+    assert st["rel_residual"] <= 1e-6
+    dx = c.get_dx()
+    GA, Gb = project_pins(g["sys_A"], g["sys_b"], g["topo_ell"], g["topo_pins"])
+    # true residual of the GPU solution on the FP64 reference system
+    r = Gb.reshape(-1) - orc.spmv(g["topo_ell"], GA, dx)
+    true_rel = np.linalg.norm(r) / np.linalg.norm(Gb)
+    err = rel(dx, g["sys_dx"].reshape(-1))
+    print(case, "iters", st["iters"], "true residual", true_rel, "dx error", err)
+    assert true_rel < 5e-6
+    assert err < 1e-3
+    c.close()
+
+
+def test_reference_solver_schedule(ctx):
+    """PCGSolver::Solve tests ||r|| after iterations 1, 11, 21, ... and stops at 100."""
+    from acousticsim_gb300 import REFERENCE_PARAMS, params
+    g, conf = load_golden("grid20")
+    c = make(ctx, conf)
+    c.SetPos(g["x_in"])
+    c.SetPrePos(g["xpre_in"])
+    c.assemble()
+    st = c.solve(params(**REFERENCE_PARAMS))
+    assert st["iters"] in [1 + 10 * k for k in range(10)] + [100]
+    assert st["status"] in ("OK", "MAXITER")
+    c.close()
+
+
+def _grid_conf(n, dt=2e-3, ks=(1e3, 1e3, 1e2), kb=(1e-3, 1e-3), pins=True):
+    conf = {"geometry_type": "regular_triangle", "cloth_size": [1.0, 1.0],
+            "subdivision": [n - 1, n - 1], "cloth_init_pos": [0.0, 0.0, 0.0],
+            "cloth_uv_rotation": 0, "cloth_stretch_stiffness": list(ks),
+            "cloth_bending_stiffness": list(kb), "cloth_density": 0.1,
+            "rayleigh_damping_a": 0.01, "rayleigh_damping_b": 0.0, "default_timestep": dt}
+    if pins:
+        conf["constraints"] = {"static_point": [[-0.5, 0.5], [0.5, 0.5]]}
+    return conf
+
+
+def _perturbed(c, seed, dt, sx=1e-3, sv=1e-2):
+    rng = np.random.default_rng(seed)
+    x0 = c.GetInitPos().reshape(-1, 3)
+    x = x0 + rng.normal(0, sx, x0.shape)
+    v = rng.normal(0, sv, x0.shape)
+    return x.reshape(-1), (x - dt * v).reshape(-1)
+
+
+def test_multi_step_trajectory_vs_oracle(ctx, orc):
+    """20 steps of a 48x48 cloth against the FP64 oracle stepping the same state."""
+    from acousticsim_gb300 import params
+    n, dt = 48, 2e-3
+    conf = _grid_conf(n, dt)
+    c = make(ctx, conf)
+    x, xp = _perturbed(c, 7, dt)
+    c.SetPos(x)
+    c.SetPrePos(xp)
+    oc = orc.OracleCloth(c.mesh, conf, c.GetConstraintStaticVertices())
+    oc.x, oc.xpre = x.copy(), xp.copy()
+    for _ in range(20):
+        st = c.UpdatePos(0.0, params(max_iters=20000, rel_tol=1e-7))
+        assert st["status"] == "OK", st
+        oc.step(rel_tol=1e-12)
+    xg = c.GetPos()
+    disp_err = rel(xg - x, oc.x - x)
+    print("displacement error after 20 steps", disp_err)
+    assert disp_err < 1e-3
+    pins = c.GetConstraintStaticVertices()
+    x0 = c.GetInitPos().reshape(-1, 3)
+    tgt = x0[pins].astype(np.float32).astype(np.float64)
+    assert np.array_equal(xg.reshape(-1, 3)[pins], tgt)
+    c.close()
+
+
+def test_batch_equals_alone_bit_exact(ctx):
+    """Each cloth's result in a mixed batch is bit-identical to stepping it alone."""
+    from acousticsim_gb300 import params
+    p = params(max_iters=5000, rel_tol=1e-6)
+    sizes = [17, 40, 23]
+    dts = [2e-3, 3e-3, 1e-3]
+    alone, mixed = [], []
+    for k, (n, dt) in enumerate(zip(sizes, dts)):
+        conf = _grid_conf(n, dt, ks=(10 ** (2 + k), 10 ** (2 + k), 10 ** (1 + k)))
+        a = make(ctx, conf)
+        m = make(ctx, conf)
+        x, xp = _perturbed(a, 100 + k, dt)
+        for c in (a, m):
+            c.SetPos(x)
+            c.SetPrePos(xp)
+        alone.append(a)
+        mixed.append(m)
+    ref = []
+    for a in alone:
+        for _ in range(3):
+            a.UpdatePos(0.0, p)
+        ref.append(a.GetPos())
+    for _ in range(3):
+        stats = ctx.batch_step(mixed, 0.0, p)
+        assert all(s["status"] == "OK" for s in stats), stats
+    for r, m in zip(ref, mixed):
+        assert np.array_equal(r, m.GetPos())
+    for c in alone + mixed:
+        c.close()
+
+
+def test_step_host_equals_device_step(ctx):
+    from acousticsim_gb300 import params
+    conf = _grid_conf(24)
+    p = params(max_iters=5000, rel_tol=1e-6)
+    a, b = make(ctx, conf), make(ctx, conf)
+    x, xp = _perturbed(a, 3, 2e-3)
+    a.SetPos(x)
+    a.SetPrePos(xp)
+    a.UpdatePos(0.0, p)
+    out = np.zeros_like(x)
+    b.step_host(x, xp, out, 0.0, p)
+    assert np.array_equal(out, a.GetPos())
+    a.close()
+    b.close()
+
+
+def test_drag_point_and_reset(ctx):
+    conf = _grid_conf(16)
+    c = make(ctx, conf)
+    tgt = np.array([0.1, 0.2, 0.3], np.float32)
+    c.ApplyUserPerturbForceOnce(5, tgt)
+    c.UpdatePos()
+    assert np.array_equal(c.GetPos().reshape(-1, 3)[5], tgt.astype(np.float64))
+    c.UpdatePos()  # drag released: vertex 5 moves again
+    assert not np.array_equal(c.GetPos().reshape(-1, 3)[5], tgt.astype(np.float64))
+    c.Reset()
+    assert np.array_equal(c.GetPos(), c.GetInitPos())
+    assert np.array_equal(c.get_dx(), np.zeros(c.nv * 3))
+    c.close()
+
+
+def test_status_codes(ctx):
+    from acousticsim_gb300 import params
+    conf = _grid_conf(16)
+    c = make(ctx, conf)
+    x, xp = _perturbed(c, 1, 2e-3)
+    c.SetPos(x)
+    c.SetPrePos(xp)
+    st = c.UpdatePos(0.0, params(max_iters=2, rel_tol=1e-12))
+    assert st["status"] == "MAXITER" and st["iters"] == 2
+    x = c.GetPos()
+    x[7] = np.nan
+    c.SetPos(x)
+    st = c.UpdatePos(0.0, params(max_iters=50, rel_tol=1e-6))
+    assert st["status"] == "NAN"
+    c.close()

@@ -1,0 +1,106 @@
+"""Pins the CPU oracle (oracle/cloth_oracle.c) to the reference itself: every
+golden fixture was written by the reference's own CPU code (oracle/ref_harness.cpp,
+tests/golden/make_golden.py).  Index maps and init-time tables must be bit-exact."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN_CASES, load_golden, project_pins, rel
+
+
+@pytest.fixture(scope="module")
+def orc(built):
+    from oracle import oracle
+    return oracle
+
+
+def _mesh(orc, conf):
+    return orc.grid(conf["cloth_size"], conf["subdivision"], conf["cloth_init_pos"],
+                    conf["cloth_uv_rotation"])
+
+
+@pytest.mark.parametrize("case", GOLDEN_CASES)
+def test_grid_numbering_bit_exact(orc, case):
+    g, conf = load_golden(case)
+    m = _mesh(orc, conf)
+    assert np.array_equal(m["pos"], g["topo_pos"])
+    assert np.array_equal(m["uv"], g["topo_uv"])
+    assert np.array_equal(m["tris"], g["topo_tris"])
+    assert np.array_equal(m["edges"], g["topo_edges"][:, :4])
+    # boundary flag of the reference = no second triangle
+    assert np.array_equal(m["edges"][:, 3] < 0, g["topo_edges"][:, 4] == 1)
+
+
+@pytest.mark.parametrize("case", GOLDEN_CASES)
+def test_tables_bit_exact(orc, case):
+    g, conf = load_golden(case)
+    m = _mesh(orc, conf)
+    t = orc.tables(m, conf["cloth_density"], conf["cloth_bending_stiffness"])
+    assert np.array_equal(t["stencil"], g["topo_stencil"])
+    assert np.array_equal(t["area"], g["topo_tri_area"])
+    assert np.array_equal(t["mass"], g["topo_mass_gpu"])
+    assert np.array_equal(t["ell"], g["topo_ell"])
+    assert np.array_equal(t["coef"], g["topo_stretch_coef"])
+    assert np.array_equal(t["diag16"], g["topo_bend_diag16"])
+    assert np.array_equal(t["edge_k"], g["topo_bend_edge_k"])
+    assert rel(t["kbend"], g["sys_Kb_gpu"]) < 1e-12
+
+
+@pytest.mark.parametrize("case", GOLDEN_CASES)
+def test_triangle_forces_and_hessians(orc, case):
+    g, conf = load_golden(case)
+    m = _mesh(orc, conf)
+    t = orc.tables(m, conf["cloth_density"], conf["cloth_bending_stiffness"])
+    oc = orc.OracleCloth(m, conf, g["topo_pins"])
+    oc.x = g["x_in"].reshape(-1).copy()
+    oc.xpre = g["xpre_in"].reshape(-1).copy()
+    A, b, f, tf, th = oc.system()
+    assert rel(tf, g["sys_tri_fint"]) < 1e-12
+    assert rel(th, g["sys_tri_hess"]) < 1e-12
+    assert rel(f, g["sys_f_stretch"] + g["sys_f_bend"]) < 1e-12
+    GA, Gb = project_pins(g["sys_A"], g["sys_b"], g["topo_ell"], g["topo_pins"])
+    # the reference stores the Rayleigh coefficients as float, the harness
+    # used the JSON doubles: agreement to float precision of those constants
+    assert rel(A, GA) < 1e-7
+    assert rel(b, Gb) < 1e-12
+
+
+@pytest.mark.parametrize("case", GOLDEN_CASES)
+def test_pcg_matches_direct_solve(orc, case):
+    g, conf = load_golden(case)
+    m = _mesh(orc, conf)
+    oc = orc.OracleCloth(m, conf, g["topo_pins"])
+    oc.x = g["x_in"].reshape(-1).copy()
+    oc.xpre = g["xpre_in"].reshape(-1).copy()
+    A, b, _, _, _ = oc.system()
+    dx, it, res = orc.pcg(oc.tab["ell"], A, b, oc.fixed, rel_tol=1e-13)
+    assert res <= 1e-13 * np.linalg.norm(b) * 1.0001
+    assert rel(dx, g["sys_dx"].reshape(-1)) < 1e-6
+
+
+def test_isotropic_bending_equals_cpu_qbending():
+    """With K_u = K_v the GPU bending (per-edge table * blended stiffness) must
+    equal the reference's CPU Q-bending matrix (BaraffClothGpu.cpp:184-207)."""
+    for case in ("grid20", "small_rot90"):
+        g, _ = load_golden(case)
+        assert rel(g["sys_Kb_gpu"], g["sys_Kb_cpu"]) < 1e-6
+
+
+def test_oracle_rejects_wide_rows(orc):
+    # a fan of 40 triangles around vertex 0: its ELL row has 41 entries
+    n = 40
+    ang = np.linspace(0, 2 * np.pi, n, endpoint=False)
+    pos = np.zeros((n + 1, 3))
+    pos[1:, 0] = np.cos(ang)
+    pos[1:, 1] = np.sin(ang)
+    uv = pos[:, :2].astype(np.float32)
+    tris = np.array([[0, 1 + k, 1 + (k + 1) % n] for k in range(n)], np.int32)
+    edges = []
+    for k in range(n):
+        a, b = 1 + k, 1 + (k + 1) % n
+        edges.append([0, a, (k - 1) % n, k])
+        edges.append([min(a, b), max(a, b), k, -1])
+    mesh = {"pos": pos, "uv": uv, "tris": tris, "edges": np.array(edges, np.int32)}
+    with pytest.raises(ValueError):
+        orc.tables(mesh, 0.1, [1e-3, 1e-3])
