@@ -20,6 +20,9 @@ STATUS_NAMES = {
 NUM_PHASES = 6
 PHASE_NAMES = ["pins", "tri_assemble", "row_assemble", "spmv_dot", "update_dot", "advance"]
 ELL_REF_WIDTH = 32
+SOLVER_PERSISTENT = 0
+SOLVER_GRAPH_LOOP = 1
+SOLVER_NAMES = {0: "persistent", 1: "graph_loop"}
 
 
 class GridDesc(C.Structure):
@@ -47,12 +50,13 @@ class SolveParams(C.Structure):
 
 class SolveStats(C.Structure):
     _fields_ = [("iters", C.c_int), ("status", C.c_int), ("res_norm", C.c_double),
-                ("rhs_norm", C.c_double), ("rel_residual", C.c_double)]
+                ("rhs_norm", C.c_double), ("rel_residual", C.c_double), ("solver", C.c_int)]
 
     def as_dict(self) -> dict:
         return {"iters": self.iters, "status": STATUS_NAMES.get(self.status, str(self.status)),
                 "res_norm": self.res_norm, "rhs_norm": self.rhs_norm,
-                "rel_residual": self.rel_residual}
+                "rel_residual": self.rel_residual,
+                "solver": SOLVER_NAMES.get(self.solver, str(self.solver))}
 
 
 P = C.c_void_p
@@ -71,6 +75,7 @@ SIGNATURES = {
     "cloth_ctx_set_profiling": (C.c_int, [P, C.c_int]),
     "cloth_ctx_get_profile": (C.c_int, [P, PD, C.POINTER(C.c_longlong)]),
     "cloth_ctx_reset_profile": (C.c_int, [P]),
+    "cloth_ctx_set_solver": (C.c_int, [P, C.c_int]),
     "cloth_ctx_device_bytes": (C.c_int, [P, C.POINTER(C.c_size_t)]),
     "cloth_ctx_get_stream": (C.c_int, [P, C.POINTER(P)]),
     "cloth_grid_build": (C.c_int, [C.POINTER(GridDesc), PI, PI, PI, PD, PF, PI, PI]),

@@ -43,6 +43,11 @@ class ClothContext:
         N.call("cloth_ctx_get_profile", self._h, ms, n)
         return {N.PHASE_NAMES[k]: {"ms": ms[k], "launches": n[k]} for k in range(N.NUM_PHASES)}
 
+    def set_solver(self, solver: str) -> None:
+        """'persistent' (default; falls back when the set does not fit) or 'graph_loop'."""
+        code = {"persistent": N.SOLVER_PERSISTENT, "graph_loop": N.SOLVER_GRAPH_LOOP}[solver]
+        N.call("cloth_ctx_set_solver", self._h, code)
+
     def stream_ptr(self) -> int:
         s = C.c_void_p()
         N.call("cloth_ctx_get_stream", self._h, C.byref(s))

@@ -25,6 +25,7 @@ __global__ void k_update(InstDesc *const *descs, const Tile *tiles, BatchCtl *ct
 __global__ void k_advance(InstDesc *const *descs, const Tile *tiles,
                           const BatchCtl *ctl);
 __global__ void k_sync_x32(InstDesc *d);
+__global__ void k_pcg_persistent(InstDesc *const *descs, const TeamBlock *work);
 } // namespace cloth
 
 using namespace cloth;
@@ -83,6 +84,8 @@ struct cloth_ctx_s
     std::recursive_mutex mu;
     int num_sms = 0;
     int occ_tri = 1, occ_row = 1, occ_spmv = 1, occ_update = 1;
+    int max_smem_optin = 0;
+    int solver = 0; // 0: persistent cooperative PCG when the set fits, 1: graph loop
     bool prof = false;
     double prof_ms[CLOTH_NUM_PHASES] = {};
     long long prof_n[CLOTH_NUM_PHASES] = {};
@@ -128,6 +131,11 @@ struct Batch
     BatchCtl *d_ctl = nullptr;
     int n_rt = 0, n_tt = 0;
     int grid_tri = 1, grid_row = 1, grid_spmv = 1, grid_update = 1;
+    // persistent solver plan
+    bool persist_ok = false;
+    TeamBlock *d_work = nullptr;
+    int grid_persist = 0;
+    size_t smem_persist = 0;
     cudaGraphExec_t step_exec = nullptr;
     cudaGraphExec_t solve_exec = nullptr;
     ~Batch()
@@ -138,6 +146,8 @@ struct Batch
             cudaGraphExecDestroy(solve_exec);
         if (mem)
             cudaFree(mem);
+        if (d_work)
+            cudaFree(d_work);
     }
 };
 
@@ -456,6 +466,8 @@ int sync_desc(cloth_s *c)
 }
 
 // ------------------------------------------------------------ batches
+int plan_persistent(cloth_ctx *ctx, Batch *b);
+
 int make_batch(cloth_ctx *ctx, const std::vector<cloth_s *> &members,
                std::unique_ptr<Batch> &out)
 {
@@ -501,7 +513,143 @@ int make_batch(cloth_ctx *ctx, const std::vector<cloth_s *> &members,
     b->grid_row = std::max(1, std::min(b->n_rt, cap(ctx->occ_row)));
     b->grid_spmv = std::max(1, std::min(b->n_rt, cap(ctx->occ_spmv)));
     b->grid_update = std::max(1, std::min(b->n_rt, cap(ctx->occ_update)));
+    int rc = plan_persistent(ctx, b.get());
+    if (rc != CLOTH_OK)
+        return rc;
     out = std::move(b);
+    return CLOTH_OK;
+}
+
+// Team plan of the persistent solver: every instance gets blocks in
+// proportion to its rows (at least one), rows split in 32-aligned chunks, and
+// each block's staged range covers the columns of its rows.
+int plan_persistent(cloth_ctx *ctx, Batch *b)
+{
+    b->persist_ok = false;
+    if (ctx->solver != 0)
+        return CLOTH_OK;
+    const size_t smem_cap_bytes =
+        std::min<size_t>(size_t(std::max(ctx->max_smem_optin, 48 * 1024)) - 4096,
+                         200 * 1024);
+    const int cap_entries = int(smem_cap_bytes / sizeof(float4));
+    // occupancy at the largest staging size we may request
+    int occ = 0;
+    if (cudaFuncSetAttribute(k_pcg_persistent, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             int(smem_cap_bytes)) != cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_pcg_persistent, kPBlock,
+                                                      smem_cap_bytes) != cudaSuccess ||
+        occ <= 0)
+    {
+        cudaGetLastError();
+        return CLOTH_OK;
+    }
+    const int G = ctx->num_sms * occ;
+    const int n = int(b->members.size());
+    if (n > G)
+        return CLOTH_OK;
+    long long total = 0;
+    for (auto *c : b->members)
+        total += c->tab.nv;
+    std::vector<int> nb(n);
+    int used = 0;
+    for (int i = 0; i < n; i++)
+    {
+        const Tables &t = b->members[i]->tab;
+        const int maxb = std::max(1, std::min((t.nv + 31) / 32, (t.nv + kTile - 1) / kTile));
+        long long want = (long long)G * t.nv / std::max(1ll, total);
+        nb[i] = int(std::max(1ll, std::min<long long>(want, maxb)));
+        used += nb[i];
+    }
+    // hand spare blocks to the instances with the most rows per block
+    while (used < G)
+    {
+        int best = -1;
+        double best_load = 0;
+        for (int i = 0; i < n; i++)
+        {
+            const Tables &t = b->members[i]->tab;
+            const int maxb = std::max(1, std::min((t.nv + 31) / 32, (t.nv + kTile - 1) / kTile));
+            if (nb[i] >= maxb)
+                continue;
+            double load = double(t.nv) / nb[i];
+            if (load > best_load)
+            {
+                best_load = load;
+                best = i;
+            }
+        }
+        if (best < 0)
+            break;
+        nb[best]++;
+        used++;
+    }
+    while (used > G)
+    {
+        int worst = -1;
+        double lo = 1e300;
+        for (int i = 0; i < n; i++)
+            if (nb[i] > 1 && double(b->members[i]->tab.nv) / nb[i] < lo)
+            {
+                lo = double(b->members[i]->tab.nv) / nb[i];
+                worst = i;
+            }
+        if (worst < 0)
+            return CLOTH_OK;
+        nb[worst]--;
+        used--;
+    }
+    std::vector<TeamBlock> work;
+    int max_entries = 0;
+    for (int i = 0; i < n; i++)
+    {
+        const Tables &t = b->members[i]->tab;
+        const int chunk = ((t.nv + nb[i] - 1) / nb[i] + 31) / 32 * 32;
+        int rank = 0;
+        std::vector<TeamBlock> team;
+        for (int r0 = 0; r0 < t.nv; r0 += chunk)
+        {
+            TeamBlock w;
+            w.inst = i;
+            w.rank = rank++;
+            w.row0 = r0;
+            w.row1 = std::min(t.nv, r0 + chunk);
+            int lo = w.row0, hi = w.row1 - 1;
+            for (int v = w.row0; v < w.row1; v++)
+            {
+                lo = std::min(lo, t.cols[t.rowptr[v]]);
+                hi = std::max(hi, t.cols[t.rowptr[v + 1] - 1]);
+            }
+            w.halo0 = lo;
+            w.halo1 = hi + 1;
+            w.pad = 0;
+            team.push_back(w);
+        }
+        for (auto &w : team)
+        {
+            w.nblk = int(team.size());
+            if (w.halo1 - w.halo0 > cap_entries)
+                w.halo0 = w.halo1 = -1;
+            else
+                max_entries = std::max(max_entries, w.halo1 - w.halo0);
+            work.push_back(w);
+        }
+    }
+    while (int(work.size()) < G)
+        work.push_back(TeamBlock{-1, 0, 0, 0, 0, -1, -1, 0});
+    b->smem_persist = size_t(max_entries) * sizeof(float4);
+    int occ2 = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ2, k_pcg_persistent, kPBlock,
+                                                      b->smem_persist) != cudaSuccess ||
+        occ2 * ctx->num_sms < int(work.size()))
+    {
+        cudaGetLastError();
+        return CLOTH_OK;
+    }
+    CK(cudaMalloc(&b->d_work, work.size() * sizeof(TeamBlock)));
+    CK(cudaMemcpy(b->d_work, work.data(), work.size() * sizeof(TeamBlock),
+                  cudaMemcpyHostToDevice));
+    b->grid_persist = int(work.size());
+    b->persist_ok = true;
     return CLOTH_OK;
 }
 
@@ -568,8 +716,36 @@ int build_graph(Batch *b, bool full, cudaGraphExec_t *exec)
         chain((void *)k_tri, b->grid_tri, a_tri);
         chain((void *)k_row, b->grid_row, a_row);
     }
-    chain((void *)k_cond, 1, a_cond);
-    if (rc == CLOTH_OK)
+    if (b->persist_ok)
+    {
+        void *a_per[] = {&b->d_descs, &b->d_work};
+        if (rc == CLOTH_OK)
+        {
+            cudaKernelNodeParams p;
+            std::memset(&p, 0, sizeof(p));
+            p.func = (void *)k_pcg_persistent;
+            p.gridDim = dim3(b->grid_persist);
+            p.blockDim = dim3(kPBlock);
+            p.sharedMemBytes = unsigned(b->smem_persist);
+            p.kernelParams = a_per;
+            if (cudaGraphAddKernelNode(&n, g, last ? &last : nullptr, last ? 1 : 0, &p) !=
+                cudaSuccess)
+                rc = fail(CLOTH_ERR_CUDA, "cudaGraphAddKernelNode(persistent) failed");
+            else
+            {
+                cudaLaunchAttributeValue v;
+                std::memset(&v, 0, sizeof(v));
+                v.cooperative = 1;
+                if (cudaGraphKernelNodeSetAttribute(n, cudaLaunchAttributeCooperative, &v) !=
+                    cudaSuccess)
+                    rc = fail(CLOTH_ERR_CUDA, "cooperative attribute on graph node failed");
+                last = n;
+            }
+        }
+    }
+    else
+        chain((void *)k_cond, 1, a_cond);
+    if (rc == CLOTH_OK && !b->persist_ok)
     {
         cudaGraphNodeParams cp = {cudaGraphNodeTypeConditional};
         cp.conditional.handle = hnd;
@@ -624,10 +800,22 @@ int launch_assemble(Batch *b)
     return CLOTH_OK;
 }
 
+int launch_persistent(Batch *b)
+{
+    cloth_ctx *ctx = b->ctx;
+    PhaseTimer t(ctx, PH_SPMV);
+    void *args[] = {&b->d_descs, &b->d_work};
+    CK(cudaLaunchCooperativeKernel((void *)k_pcg_persistent, dim3(b->grid_persist),
+                                   dim3(kPBlock), args, b->smem_persist, ctx->stream));
+    return CLOTH_OK;
+}
+
 int launch_solve_host(Batch *b, int max_iters)
 {
     cloth_ctx *ctx = b->ctx;
     cudaStream_t s = ctx->stream;
+    if (b->persist_ok)
+        return launch_persistent(b);
     cudaGraphConditionalHandle none = 0;
     int *h_active = nullptr;
     CK(cudaMallocHost(&h_active, sizeof(int)));
@@ -685,6 +873,7 @@ int read_stats(Batch *b, cloth_solve_stats *stats)
         o.res_norm = std::sqrt(std::max(0.0, st.rr));
         o.rhs_norm = std::sqrt(std::max(0.0, st.bb));
         o.rel_residual = o.rhs_norm > 0 ? o.res_norm / o.rhs_norm : o.res_norm;
+        o.solver = b->persist_ok ? CLOTH_SOLVER_PERSISTENT : CLOTH_SOLVER_GRAPH_LOOP;
     }
     return CLOTH_OK;
 }
@@ -821,6 +1010,8 @@ int cloth_ctx_create(int device, cloth_ctx **out)
     c->device = device;
     CK(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
     CK(cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device));
+    CK(cudaDeviceGetAttribute(&c->max_smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin,
+                              device));
     CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c->occ_tri, k_tri, kTile, 0));
     CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c->occ_row, k_row, kTile, 0));
     CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c->occ_spmv, k_spmv, kTile, 0));
@@ -905,6 +1096,19 @@ int cloth_ctx_reset_profile(cloth_ctx *ctx)
         ctx->prof_ms[k] = 0;
         ctx->prof_n[k] = 0;
     }
+    return CLOTH_OK;
+}
+
+int cloth_ctx_set_solver(cloth_ctx *ctx, int solver)
+{
+    if (!ctx || (solver != CLOTH_SOLVER_PERSISTENT && solver != CLOTH_SOLVER_GRAPH_LOOP))
+        return fail(CLOTH_ERR_INVALID, "cloth_ctx_set_solver: bad argument");
+    std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+    cudaStreamSynchronize(ctx->stream);
+    ctx->solver = solver;
+    ctx->last_batch.reset();
+    for (auto *c : ctx->cloths)
+        c->self.reset();
     return CLOTH_OK;
 }
 
@@ -1370,6 +1574,8 @@ int cloth_get_stats(cloth_t *c, cloth_solve_stats *stats)
     stats->rhs_norm = std::sqrt(std::max(0.0, st.bb));
     stats->rel_residual = stats->rhs_norm > 0 ? stats->res_norm / stats->rhs_norm
                                               : stats->res_norm;
+    stats->solver = (c->self && c->self->persist_ok) ? CLOTH_SOLVER_PERSISTENT
+                                                     : CLOTH_SOLVER_GRAPH_LOOP;
     return CLOTH_OK;
 }
 

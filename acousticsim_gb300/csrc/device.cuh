@@ -42,6 +42,11 @@ struct InstState
     int active;
     int status;
     unsigned ticket;
+    // team barrier of the persistent solver (reset by the assembly)
+    unsigned bar_count;
+    unsigned bar_gen;
+    int bar_err;
+    int pad;
 };
 
 struct InstDesc
@@ -96,6 +101,23 @@ struct Tile
     int inst;
     int start;
 };
+
+// One block of the persistent PCG grid: a contiguous row range of one
+// instance.  The instance's blocks form its team and meet at team barriers;
+// p is staged in shared memory over [halo0, halo1), which covers every column
+// the block's rows touch (halo0 = -1: the range did not fit, gather from L2).
+struct TeamBlock
+{
+    int inst;   // index in the launch set, -1 = idle block
+    int rank;   // rank in the team
+    int nblk;   // team size
+    int row0, row1;
+    int halo0, halo1;
+    int pad;
+};
+
+constexpr int kPBlock = 512;                 // threads per persistent block
+constexpr unsigned kSpinLimit = 1u << 25;    // bounded barrier wait (~seconds)
 
 // Batch-wide control words (one per launch set).
 struct BatchCtl

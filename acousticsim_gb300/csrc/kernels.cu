@@ -441,6 +441,8 @@ __global__ void __launch_bounds__(kTile) k_row(InstDesc *const *descs,
             st.pq = 0.0;
             st.iter = 0;
             st.status = 0;
+            st.bar_count = 0u;
+            st.bar_err = 0;
             if (!isfinite(tot[0]) || !isfinite(tot[1]) || !isfinite(tot[2]))
             {
                 st.status = 6; // CLOTH_ERR_NAN
@@ -620,6 +622,271 @@ __global__ void __launch_bounds__(kTile) k_update(InstDesc *const *descs,
                 retire(ctl, use_cond, h);
             }
         }
+    }
+}
+
+// ------------------------------------------------------------------ persistent PCG
+// One cooperative launch runs every PCG iteration of every instance in the
+// launch set.  Each block owns a contiguous row range of one instance; the
+// instance's blocks (its team) meet at two barriers per iteration, after
+// which every block sums the team's per-block partials in the same fixed
+// order, so all of them derive bit-identical alpha, beta and stop decisions
+// without a third synchronisation.  Data written by other blocks inside the
+// kernel (z, p, partials) is read through L2 (ld.global.cg); A is read-only.
+namespace {
+
+// All threads of the block get the block sums of v[0..N) (fixed order).
+template <int N>
+__device__ __forceinline__ void block_allreduce(double (&v)[N], double *sh)
+{
+    constexpr int NW = kPBlock / 32;
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < N; k++)
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1)
+            v[k] += __shfl_xor_sync(0xffffffffu, v[k], o);
+    if ((threadIdx.x & 31) == 0)
+#pragma unroll
+        for (int k = 0; k < N; k++)
+            sh[k * NW + (threadIdx.x >> 5)] = v[k];
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < N; k++)
+    {
+        double t = sh[k * NW];
+#pragma unroll
+        for (int j = 1; j < NW; j++)
+            t += sh[k * NW + j];
+        v[k] = t;
+    }
+}
+
+// Barrier of the nblk blocks of one team. Returns false when the bounded
+// wait gave up (then the team's error flag is set and the solve stops).
+__device__ __forceinline__ bool team_barrier(InstState *st, int nblk)
+{
+    __shared__ int ok;
+    __syncthreads();
+    if (threadIdx.x == 0)
+    {
+        ok = 1;
+        if (nblk > 1)
+        {
+            __threadfence();
+            volatile unsigned *gen = &st->bar_gen;
+            const unsigned g = *gen;
+            if (atomicAdd(&st->bar_count, 1u) == unsigned(nblk - 1))
+            {
+                atomicExch(&st->bar_count, 0u);
+                __threadfence();
+                atomicAdd(&st->bar_gen, 1u);
+            }
+            else
+            {
+                unsigned n = 0;
+                while (*gen == g)
+                {
+                    if (++n > kSpinLimit)
+                    {
+                        atomicExch(&st->bar_err, 1);
+                        break;
+                    }
+                    __nanosleep(64);
+                }
+            }
+            __threadfence();
+            if (*(volatile int *)&st->bar_err)
+                ok = 0;
+        }
+    }
+    __syncthreads();
+    return ok != 0;
+}
+
+__device__ __forceinline__ float4 ldcg4(const float4 *p) { return __ldcg(p); }
+
+} // namespace
+
+__global__ void __launch_bounds__(kPBlock, 1)
+    k_pcg_persistent(InstDesc *const *descs, const TeamBlock *work)
+{
+    extern __shared__ float4 sp[];
+    __shared__ double red[3 * (kPBlock / 32)];
+    const TeamBlock w = work[blockIdx.x];
+    if (w.inst < 0)
+        return;
+    const InstDesc d = *descs[w.inst];
+    InstState *st = d.st;
+    if (!__ldcg(&st->active))
+        return;
+    const int nt = d.ntile_rows;
+    double rho = __ldcg(&st->rho);
+    const double bb = __ldcg(&st->bb);
+    double beta = 0.0, alpha = 0.0, pq = 0.0, rr = __ldcg(&st->rr);
+    int it = 0, status = 0;
+    const bool staged = w.halo0 >= 0;
+    const int tid = threadIdx.x;
+    for (;;)
+    {
+        const float4 *pold = (it & 1) ? d.p1 : d.p0;
+        float4 *pnew = (it & 1) ? d.p0 : d.p1;
+        const float bf = float(beta);
+        const bool first = (beta == 0.0);
+        // ---- p = z + beta p_old over the staged range
+        if (staged)
+        {
+            for (int i = tid; i < w.halo1 - w.halo0; i += kPBlock)
+            {
+                const int c = w.halo0 + i;
+                float4 pn = ldcg4(d.z + c);
+                if (!first)
+                {
+                    const float4 po = ldcg4(pold + c);
+                    pn.x = fmaf(bf, po.x, pn.x);
+                    pn.y = fmaf(bf, po.y, pn.y);
+                    pn.z = fmaf(bf, po.z, pn.z);
+                }
+                sp[i] = pn;
+            }
+            __syncthreads();
+        }
+        // ---- q = A p on own rows, p.q
+        double part[1] = {0.0};
+        for (int row = w.row0 + tid; row < w.row1; row += kPBlock)
+        {
+            float3 pv;
+            if (staged)
+                pv = xyz(sp[row - w.halo0]);
+            else
+            {
+                pv = xyz(ldcg4(d.z + row));
+                if (!first)
+                {
+                    const float3 po = xyz(ldcg4(pold + row));
+                    pv = pv + bf * po;
+                }
+            }
+            pnew[row] = f4(pv);
+            const int len = __ldg(d.rowinfo + row) & 255;
+            float3 q = make_float3(0, 0, 0);
+            for (int s = 0; s < len; s++)
+            {
+                const size_t o = size_t(s) * d.stride + row;
+                const int c = __ldg(d.col + o);
+                const float4 a0 = __ldg(d.A0 + o);
+                const float2 a1 = __ldg(d.A1 + o);
+                const float A[6] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y};
+                float3 pc;
+                if (staged)
+                    pc = xyz(sp[c - w.halo0]);
+                else if (c == row)
+                    pc = pv;
+                else
+                {
+                    pc = xyz(ldcg4(d.z + c));
+                    if (!first)
+                        pc = pc + bf * xyz(ldcg4(pold + c));
+                }
+                q = q + symv(A, pc);
+            }
+            d.q[row] = f4(q);
+            part[0] += ddot(pv, q);
+        }
+        block_allreduce<1>(part, red);
+        if (tid == 0)
+            d.part[w.rank] = part[0];
+        if (!team_barrier(st, w.nblk))
+        {
+            status = 9; // CLOTH_ERR_TIMEOUT
+            break;
+        }
+        {
+            double t[1] = {0.0};
+            for (int k = tid; k < w.nblk; k += kPBlock)
+                t[0] += __ldcg(d.part + k);
+            block_allreduce<1>(t, red);
+            pq = t[0];
+        }
+        if (!isfinite(pq))
+        {
+            status = 6;
+            break;
+        }
+        if (pq == 0.0)
+        {
+            status = 7;
+            break;
+        }
+        alpha = rho / pq;
+        const float af = float(alpha);
+        // ---- dx += alpha p, r -= alpha q, z = M^-1 r; r.z, r.r
+        double p2[2] = {0.0, 0.0};
+        for (int row = w.row0 + tid; row < w.row1; row += kPBlock)
+        {
+            const float3 p = staged ? xyz(sp[row - w.halo0]) : xyz(pnew[row]);
+            const float3 qv = xyz(d.q[row]);
+            float3 x = xyz(d.dx[row]);
+            float3 r = xyz(d.r[row]);
+            x = make_float3(fmaf(af, p.x, x.x), fmaf(af, p.y, x.y), fmaf(af, p.z, x.z));
+            r = make_float3(fmaf(-af, qv.x, r.x), fmaf(-af, qv.y, r.y),
+                            fmaf(-af, qv.z, r.z));
+            float M[6];
+            load_sym(d.M0, d.M1, row, M);
+            const float3 z = symv(M, r);
+            d.dx[row] = f4(x);
+            d.r[row] = f4(r);
+            d.z[row] = f4(z);
+            p2[0] += ddot(r, z);
+            p2[1] += ddot(r, r);
+        }
+        block_allreduce<2>(p2, red);
+        if (tid == 0)
+        {
+            d.part[nt + w.rank] = p2[0];
+            d.part[2 * nt + w.rank] = p2[1];
+        }
+        if (!team_barrier(st, w.nblk))
+        {
+            status = 9;
+            break;
+        }
+        double t[2] = {0.0, 0.0};
+        for (int k = tid; k < w.nblk; k += kPBlock)
+        {
+            t[0] += __ldcg(d.part + nt + k);
+            t[1] += __ldcg(d.part + 2 * nt + k);
+        }
+        block_allreduce<2>(t, red);
+        const double rho_new = t[0];
+        rr = t[1];
+        beta = (rho == 0.0) ? 0.0 : rho_new / rho;
+        rho = rho_new;
+        it++;
+        if (!isfinite(rho_new) || !isfinite(rr))
+        {
+            status = 6;
+            break;
+        }
+        const bool check = ((it - 1) % d.check_every) == 0 || it >= d.max_iters;
+        if (check && test_converged(d, *st, rr))
+            break;
+        if (it >= d.max_iters)
+        {
+            status = 8;
+            break;
+        }
+    }
+    if (w.rank == 0 && tid == 0)
+    {
+        st->iter = it;
+        st->status = status;
+        st->rho = rho;
+        st->rr = rr;
+        st->pq = pq;
+        st->alpha = alpha;
+        st->beta = beta;
+        st->active = 0;
     }
 }
 

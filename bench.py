@@ -178,15 +178,16 @@ def ncu_traffic(kernel: str) -> float | None:
 
 
 def algorithmic_bytes(nv: int, nnzb: int) -> dict:
-    """Unique bytes one launch must move (FP32 6-float symmetric blocks, int32
-    columns, float4 vectors):
-      spmv_dot   : 24*nnzb (A) + 4*nnzb (cols) + 4*nv (row info)
-                   + 16*nv (z) + 16*nv (p_old) + 16*nv (p_new write) + 16*nv (q write)
-      update_dot : 16*nv * (p, q, dx, r read + dx, r, z write) + 24*nv (M^-1)
+    """Unique bytes one PCG iteration must move (FP32 6-float symmetric blocks,
+    int32 columns, float4 vectors):
+      SpMV phase   : 24*nnzb (A) + 4*nnzb (cols) + 4*nv (row info)
+                     + 16*nv (z) + 16*nv (p_old) + 16*nv (p write) + 16*nv (q write)
+      update phase : 16*nv (q) + 16*nv (dx) + 16*nv (r) + 24*nv (M^-1 read)
+                     + 48*nv (dx, r, z write)   [p comes from shared memory]
     """
     spmv = 28 * nnzb + 68 * nv
-    update = 16 * 7 * nv + 24 * nv
-    return {"spmv_dot": spmv, "update_dot": update}
+    update = 120 * nv
+    return {"spmv_dot": spmv, "update_dot": update, "iteration": spmv + update}
 
 
 def count_nnzb(n_side: int) -> int:
@@ -303,7 +304,8 @@ def run_ours(args, rank, world, local, pg):
     t_max = max_over_ranks(pg, sum(step_ms) / 1e3)
     steps_total = sum_over_ranks(pg, float(args.steps))
     value = steps_total / t_max if t_max > 0 else 0.0
-    launches = sum(5 + 2 * i for i in iters)
+    per_step = 5 if st["solver"] == "persistent" else None
+    launches = sum(per_step if per_step else 5 + 2 * i for i in iters)
 
     # ---- e2e: the same steps through the C ABI with host buffers, pinned
     nv = cloth.nv
@@ -326,32 +328,42 @@ def run_ours(args, rank, world, local, pg):
            "path": "cloth_step_host (C ABI): upload x and x_pre, step, download x"}
 
     # ---- roofline: an instrumented pass of the same steps, CUDA events around
-    # every launch (host-driven launches of the same kernels)
+    # every launch on the library's stream (host-driven launches of the same
+    # kernels; the persistent solver is one launch per step)
     ctx.set_profiling(True)
     ctx.reset_profile()
+    prof_iters = []
     for _ in range(min(args.steps, 5)):
-        cloth.UpdatePos(0.0, p)
+        prof_iters.append(cloth.UpdatePos(0.0, p)["iters"])
     prof = ctx.profile()
     ctx.set_profiling(False)
     nnzb = count_nnzb(N_SIDE)
     alg = algorithmic_bytes(nv, nnzb)
-    sp = prof["spmv_dot"]
-    up = prof["update_dot"]
     peak = measured_peaks()
-    spmv_ms = sp["ms"] / max(1, sp["launches"])
-    achieved = alg["spmv_dot"] / (spmv_ms * 1e-3) / 1e9
     total_ms = sum(v["ms"] for v in prof.values())
     shares = {k: round(v["ms"] / total_ms, 4) if total_ms else None for k, v in prof.items()}
-    roof = {"bound": "hbm", "kernel": "k_spmv (SpMV fused with p update and FP64 p.Ap)",
+    solver = st["solver"]
+    sp = prof["spmv_dot"]
+    if solver == "persistent":
+        # one launch per step runs all iterations: bytes per launch = iterations x
+        # bytes per iteration
+        launch_ms = sp["ms"] / max(1, sp["launches"])
+        bytes_launch = alg["iteration"] * float(np.mean(prof_iters))
+        kname = "k_pcg_persistent (all PCG iterations of the step in one cooperative launch)"
+    else:
+        launch_ms = sp["ms"] / max(1, sp["launches"])
+        bytes_launch = alg["spmv_dot"]
+        kname = "k_spmv (SpMV fused with p update and FP64 p.Ap)"
+    achieved = bytes_launch / (launch_ms * 1e-3) / 1e9
+    roof = {"bound": "hbm", "kernel": kname,
             "achieved": achieved, "peak": peak["hbm_gbs"], "unit": "GB/s",
             "frac": achieved / peak["hbm_gbs"], "peak_source": f"{peak['source']} hbm_gbs",
-            "traffic": ncu_traffic("k_spmv"),
-            "algorithmic_bytes_per_launch": alg["spmv_dot"],
-            "avg_launch_ms": spmv_ms,
-            "update_kernel": {"achieved": alg["update_dot"] / (up["ms"] / max(1, up["launches"]) * 1e-3) / 1e9,
-                              "algorithmic_bytes_per_launch": alg["update_dot"]},
-            "phase_share": shares,
-            "nnzb": nnzb}
+            "traffic": ncu_traffic("k_pcg_persistent" if solver == "persistent" else "k_spmv"),
+            "algorithmic_bytes_per_launch": bytes_launch,
+            "algorithmic_bytes_per_iteration": alg["iteration"],
+            "avg_launch_ms": launch_ms,
+            "us_per_pcg_iteration": 1e3 * sp["ms"] / max(1, sum(prof_iters)),
+            "phase_share": shares, "solver": solver, "nnzb": nnzb}
 
     # ---- CPU baseline: the FP64 port on the host cores, bounded sample
     cpu = None

@@ -94,7 +94,15 @@ typedef struct {
     double res_norm;      /* ||r|| of the recurrence residual at exit (FP64 reduction) */
     double rhs_norm;      /* ||b|| */
     double rel_residual;  /* res_norm / rhs_norm */
+    int solver;           /* CLOTH_SOLVER_PERSISTENT or CLOTH_SOLVER_GRAPH_LOOP */
 } cloth_solve_stats;
+
+/* PCG drivers. PERSISTENT: one cooperative launch runs all iterations of every
+ * instance (team barriers between the SpMV and update phases); used whenever
+ * the launch set fits in the resident blocks, else GRAPH_LOOP: two kernels per
+ * iteration inside a CUDA-graph while loop with a device-side condition. */
+#define CLOTH_SOLVER_PERSISTENT 0
+#define CLOTH_SOLVER_GRAPH_LOOP 1
 
 /* ---------------------------------------------------------------- library */
 int cloth_abi_version(void);
@@ -113,6 +121,8 @@ int cloth_ctx_synchronize(cloth_ctx *ctx);
 int cloth_ctx_set_profiling(cloth_ctx *ctx, int enable);
 int cloth_ctx_get_profile(cloth_ctx *ctx, double *ms_total, long long *launches);
 int cloth_ctx_reset_profile(cloth_ctx *ctx);
+/* Preferred PCG driver for launch sets built after the call. */
+int cloth_ctx_set_solver(cloth_ctx *ctx, int solver);
 /* Device bytes held by all cloths of the context. */
 int cloth_ctx_device_bytes(cloth_ctx *ctx, size_t *bytes);
 /* The context's cudaStream_t, so callers can order their own work and CUDA

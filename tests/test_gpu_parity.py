@@ -69,8 +69,18 @@ def test_assembly_matches_reference(ctx, case):
     c.close()
 
 
+SOLVERS = ["persistent", "graph_loop"]
+
+
+@pytest.fixture(params=SOLVERS)
+def solver(request, ctx):
+    ctx.set_solver(request.param)
+    yield request.param
+    ctx.set_solver("persistent")
+
+
 @pytest.mark.parametrize("case", GOLDEN_CASES)
-def test_solve_matches_direct_solve(ctx, orc, case):
+def test_solve_matches_direct_solve(ctx, orc, case, solver):
     from acousticsim_gb300 import params
     g, conf = load_golden(case)
     c = make(ctx, conf)
@@ -79,6 +89,7 @@ def test_solve_matches_direct_solve(ctx, orc, case):
     c.assemble()
     st = c.solve(params(max_iters=20000, rel_tol=1e-6))
     assert st["status"] == "OK", st
+    assert st["solver"] == solver
     assert st["rel_residual"] <= 1e-6
     dx = c.get_dx()
     GA, Gb = project_pins(g["sys_A"], g["sys_b"], g["topo_ell"], g["topo_pins"])
@@ -92,7 +103,7 @@ def test_solve_matches_direct_solve(ctx, orc, case):
     c.close()
 
 
-def test_reference_solver_schedule(ctx):
+def test_reference_solver_schedule(ctx, solver):
     """PCGSolver::Solve tests ||r|| after iterations 1, 11, 21, ... and stops at 100."""
     from acousticsim_gb300 import REFERENCE_PARAMS, params
     g, conf = load_golden("grid20")
@@ -125,7 +136,7 @@ def _perturbed(c, seed, dt, sx=1e-3, sv=1e-2):
     return x.reshape(-1), (x - dt * v).reshape(-1)
 
 
-def test_multi_step_trajectory_vs_oracle(ctx, orc):
+def test_multi_step_trajectory_vs_oracle(ctx, orc, solver):
     """20 steps of a 48x48 cloth against the FP64 oracle stepping the same state."""
     from acousticsim_gb300 import params
     n, dt = 48, 2e-3
@@ -151,7 +162,7 @@ def test_multi_step_trajectory_vs_oracle(ctx, orc):
     c.close()
 
 
-def test_batch_equals_alone_bit_exact(ctx):
+def test_batch_equals_alone_bit_exact(ctx, solver):
     """Each cloth's result in a mixed batch is bit-identical to stepping it alone."""
     from acousticsim_gb300 import params
     p = params(max_iters=5000, rel_tol=1e-6)
@@ -179,6 +190,46 @@ def test_batch_equals_alone_bit_exact(ctx):
     for r, m in zip(ref, mixed):
         assert np.array_equal(r, m.GetPos())
     for c in alone + mixed:
+        c.close()
+
+
+def test_solvers_agree(ctx):
+    """Persistent and graph-loop drivers run the same recurrence; only the
+    order of the FP64 reductions differs."""
+    from acousticsim_gb300 import params
+    p = params(max_iters=5000, rel_tol=1e-6)
+    conf = _grid_conf(64)
+    out = {}
+    for sv in ("persistent", "graph_loop"):
+        ctx.set_solver(sv)
+        c = make(ctx, conf)
+        x, xp = _perturbed(c, 11, 2e-3)
+        c.SetPos(x)
+        c.SetPrePos(xp)
+        st = c.UpdatePos(0.0, p)
+        assert st["status"] == "OK" and st["solver"] == sv, st
+        out[sv] = (c.GetPos() - x, st["iters"])
+        c.close()
+    ctx.set_solver("persistent")
+    assert abs(out["persistent"][1] - out["graph_loop"][1]) <= 2
+    assert rel(out["persistent"][0], out["graph_loop"][0]) < 1e-4
+
+
+def test_persistent_many_instances(ctx):
+    """A set with more instances than one block each still solves (teams of
+    one block need no grid barrier; large ones span many blocks)."""
+    from acousticsim_gb300 import params
+    p = params(max_iters=5000, rel_tol=1e-6)
+    cl = []
+    for k, n in enumerate([16, 16, 130, 20, 64]):
+        c = make(ctx, _grid_conf(n))
+        x, xp = _perturbed(c, 50 + k, 2e-3)
+        c.SetPos(x)
+        c.SetPrePos(xp)
+        cl.append(c)
+    stats = ctx.batch_step(cl, 0.0, p)
+    assert all(s["status"] == "OK" and s["solver"] == "persistent" for s in stats), stats
+    for c in cl:
         c.close()
 
 
