@@ -555,7 +555,7 @@ int plan_persistent(cloth_ctx *ctx, Batch *b)
     for (int i = 0; i < n; i++)
     {
         const Tables &t = b->members[i]->tab;
-        const int maxb = std::max(1, std::min((t.nv + 31) / 32, (t.nv + kTile - 1) / kTile));
+        const int maxb = std::max(1, (t.nv + kTile - 1) / kTile);
         long long want = (long long)G * t.nv / std::max(1ll, total);
         nb[i] = int(std::max(1ll, std::min<long long>(want, maxb)));
         used += nb[i];
@@ -568,7 +568,7 @@ int plan_persistent(cloth_ctx *ctx, Batch *b)
         for (int i = 0; i < n; i++)
         {
             const Tables &t = b->members[i]->tab;
-            const int maxb = std::max(1, std::min((t.nv + 31) / 32, (t.nv + kTile - 1) / kTile));
+            const int maxb = std::max(1, (t.nv + kTile - 1) / kTile);
             if (nb[i] >= maxb)
                 continue;
             double load = double(t.nv) / nb[i];
@@ -603,7 +603,11 @@ int plan_persistent(cloth_ctx *ctx, Batch *b)
     for (int i = 0; i < n; i++)
     {
         const Tables &t = b->members[i]->tab;
-        const int chunk = ((t.nv + nb[i] - 1) / nb[i] + 31) / 32 * 32;
+        // 128-row aligned ranges keep the reduction tiles of an instance the
+        // same whatever the team size
+        const int chunk = ((t.nv + nb[i] - 1) / nb[i] + kTile - 1) / kTile * kTile;
+        if (chunk > kMaxBlockRows)
+            return CLOTH_OK;
         int rank = 0;
         std::vector<TeamBlock> team;
         for (int r0 = 0; r0 < t.nv; r0 += chunk)

@@ -117,6 +117,7 @@ struct TeamBlock
 };
 
 constexpr int kPBlock = 512;                 // threads per persistent block
+constexpr int kMaxBlockRows = 16384;         // rows one persistent block may own
 constexpr unsigned kSpinLimit = 1u << 25;    // bounded barrier wait (~seconds)
 
 // Batch-wide control words (one per launch set).

@@ -667,6 +667,9 @@ __device__ __forceinline__ void block_allreduce(double (&v)[N], double *sh)
 __device__ __forceinline__ bool team_barrier(InstState *st, int nblk)
 {
     __shared__ int ok;
+    // every thread's global writes (vectors, partials) are made visible
+    // device-wide before the block arrives
+    __threadfence();
     __syncthreads();
     if (threadIdx.x == 0)
     {
@@ -711,8 +714,12 @@ __device__ __forceinline__ float4 ldcg4(const float4 *p) { return __ldcg(p); }
 __global__ void __launch_bounds__(kPBlock, 1)
     k_pcg_persistent(InstDesc *const *descs, const TeamBlock *work)
 {
+    constexpr int NW = kPBlock / 32;
     extern __shared__ float4 sp[];
-    __shared__ double red[3 * (kPBlock / 32)];
+    __shared__ double red[3 * NW];
+    // per-32-row chunk sums of this block (team ranges are 128-row aligned
+    // and at most kMaxBlockRows long)
+    __shared__ double csum[2][kMaxBlockRows / 32];
     const TeamBlock w = work[blockIdx.x];
     if (w.inst < 0)
         return;
@@ -722,11 +729,27 @@ __global__ void __launch_bounds__(kPBlock, 1)
         return;
     const int nt = d.ntile_rows;
     double rho = __ldcg(&st->rho);
-    const double bb = __ldcg(&st->bb);
     double beta = 0.0, alpha = 0.0, pq = 0.0, rr = __ldcg(&st->rr);
     int it = 0, status = 0;
     const bool staged = w.halo0 >= 0;
-    const int tid = threadIdx.x;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int nch = (w.row1 - w.row0 + 31) / 32;
+    const int ntl = (w.row1 - w.row0 + kTile - 1) / kTile;
+    const int tile0 = w.row0 / kTile;
+    // Tile partials (fixed order over the tile's four 32-row chunks) go to
+    // d.part[k*nt + tile]; the team sums them over all the instance's tiles in
+    // a fixed thread assignment, independent of the team's size.
+    auto publish = [&](int nq) {
+        __syncthreads();
+        for (int t = tid; t < ntl; t += kPBlock)
+            for (int k = 0; k < nq; k++)
+            {
+                double v = 0.0;
+                for (int c = 4 * t; c < min(4 * t + 4, nch); c++)
+                    v += csum[k][c];
+                d.part[k * nt + tile0 + t] = v;
+            }
+    };
     for (;;)
     {
         const float4 *pold = (it & 1) ? d.p1 : d.p0;
@@ -751,51 +774,65 @@ __global__ void __launch_bounds__(kPBlock, 1)
             }
             __syncthreads();
         }
-        // ---- q = A p on own rows, p.q
-        double part[1] = {0.0};
-        for (int row = w.row0 + tid; row < w.row1; row += kPBlock)
+        // ---- q = A p on own rows, p.q per 32-row chunk
+        for (int ch = warp; ch < nch; ch += NW)
         {
-            float3 pv;
-            if (staged)
-                pv = xyz(sp[row - w.halo0]);
-            else
+            const int row = w.row0 + ch * 32 + lane;
+            double part = 0.0;
+            if (row < w.row1)
             {
-                pv = xyz(ldcg4(d.z + row));
-                if (!first)
-                {
-                    const float3 po = xyz(ldcg4(pold + row));
-                    pv = pv + bf * po;
-                }
-            }
-            pnew[row] = f4(pv);
-            const int len = __ldg(d.rowinfo + row) & 255;
-            float3 q = make_float3(0, 0, 0);
-            for (int s = 0; s < len; s++)
-            {
-                const size_t o = size_t(s) * d.stride + row;
-                const int c = __ldg(d.col + o);
-                const float4 a0 = __ldg(d.A0 + o);
-                const float2 a1 = __ldg(d.A1 + o);
-                const float A[6] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y};
-                float3 pc;
+                float3 pv;
                 if (staged)
-                    pc = xyz(sp[c - w.halo0]);
-                else if (c == row)
-                    pc = pv;
+                    pv = xyz(sp[row - w.halo0]);
                 else
                 {
-                    pc = xyz(ldcg4(d.z + c));
+                    const float4 zz = ldcg4(d.z + row);
+                    pv = xyz(zz);
                     if (!first)
-                        pc = pc + bf * xyz(ldcg4(pold + c));
+                    {
+                        const float4 po = ldcg4(pold + row);
+                        pv = make_float3(fmaf(bf, po.x, zz.x), fmaf(bf, po.y, zz.y),
+                                         fmaf(bf, po.z, zz.z));
+                    }
                 }
-                q = q + symv(A, pc);
+                pnew[row] = f4(pv);
+                const int len = __ldg(d.rowinfo + row) & 255;
+                float3 q = make_float3(0, 0, 0);
+                for (int s = 0; s < len; s++)
+                {
+                    const size_t o = size_t(s) * d.stride + row;
+                    const int c = __ldg(d.col + o);
+                    const float4 a0 = __ldg(d.A0 + o);
+                    const float2 a1 = __ldg(d.A1 + o);
+                    const float A[6] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y};
+                    float3 pc;
+                    if (staged)
+                        pc = xyz(sp[c - w.halo0]);
+                    else if (c == row)
+                        pc = pv;
+                    else
+                    {
+                        const float4 zz = ldcg4(d.z + c);
+                        pc = xyz(zz);
+                        if (!first)
+                        {
+                            const float4 po = ldcg4(pold + c);
+                            pc = make_float3(fmaf(bf, po.x, zz.x), fmaf(bf, po.y, zz.y),
+                                             fmaf(bf, po.z, zz.z));
+                        }
+                    }
+                    q = q + symv(A, pc);
+                }
+                d.q[row] = f4(q);
+                part = ddot(pv, q);
             }
-            d.q[row] = f4(q);
-            part[0] += ddot(pv, q);
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1)
+                part += __shfl_xor_sync(0xffffffffu, part, o);
+            if (lane == 0)
+                csum[0][ch] = part;
         }
-        block_allreduce<1>(part, red);
-        if (tid == 0)
-            d.part[w.rank] = part[0];
+        publish(1);
         if (!team_barrier(st, w.nblk))
         {
             status = 9; // CLOTH_ERR_TIMEOUT
@@ -803,7 +840,7 @@ __global__ void __launch_bounds__(kPBlock, 1)
         }
         {
             double t[1] = {0.0};
-            for (int k = tid; k < w.nblk; k += kPBlock)
+            for (int k = tid; k < nt; k += kPBlock)
                 t[0] += __ldcg(d.part + k);
             block_allreduce<1>(t, red);
             pq = t[0];
@@ -820,42 +857,52 @@ __global__ void __launch_bounds__(kPBlock, 1)
         }
         alpha = rho / pq;
         const float af = float(alpha);
-        // ---- dx += alpha p, r -= alpha q, z = M^-1 r; r.z, r.r
-        double p2[2] = {0.0, 0.0};
-        for (int row = w.row0 + tid; row < w.row1; row += kPBlock)
+        // ---- dx += alpha p, r -= alpha q, z = M^-1 r; r.z and r.r per chunk
+        for (int ch = warp; ch < nch; ch += NW)
         {
-            const float3 p = staged ? xyz(sp[row - w.halo0]) : xyz(pnew[row]);
-            const float3 qv = xyz(d.q[row]);
-            float3 x = xyz(d.dx[row]);
-            float3 r = xyz(d.r[row]);
-            x = make_float3(fmaf(af, p.x, x.x), fmaf(af, p.y, x.y), fmaf(af, p.z, x.z));
-            r = make_float3(fmaf(-af, qv.x, r.x), fmaf(-af, qv.y, r.y),
-                            fmaf(-af, qv.z, r.z));
-            float M[6];
-            load_sym(d.M0, d.M1, row, M);
-            const float3 z = symv(M, r);
-            d.dx[row] = f4(x);
-            d.r[row] = f4(r);
-            d.z[row] = f4(z);
-            p2[0] += ddot(r, z);
-            p2[1] += ddot(r, r);
+            const int row = w.row0 + ch * 32 + lane;
+            double pr = 0.0, prr = 0.0;
+            if (row < w.row1)
+            {
+                const float3 p = staged ? xyz(sp[row - w.halo0]) : xyz(pnew[row]);
+                const float3 qv = xyz(d.q[row]);
+                float3 x = xyz(d.dx[row]);
+                float3 r = xyz(d.r[row]);
+                x = make_float3(fmaf(af, p.x, x.x), fmaf(af, p.y, x.y), fmaf(af, p.z, x.z));
+                r = make_float3(fmaf(-af, qv.x, r.x), fmaf(-af, qv.y, r.y),
+                                fmaf(-af, qv.z, r.z));
+                float M[6];
+                load_sym(d.M0, d.M1, row, M);
+                const float3 z = symv(M, r);
+                d.dx[row] = f4(x);
+                d.r[row] = f4(r);
+                d.z[row] = f4(z);
+                pr = ddot(r, z);
+                prr = ddot(r, r);
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1)
+            {
+                pr += __shfl_xor_sync(0xffffffffu, pr, o);
+                prr += __shfl_xor_sync(0xffffffffu, prr, o);
+            }
+            if (lane == 0)
+            {
+                csum[0][ch] = pr;
+                csum[1][ch] = prr;
+            }
         }
-        block_allreduce<2>(p2, red);
-        if (tid == 0)
-        {
-            d.part[nt + w.rank] = p2[0];
-            d.part[2 * nt + w.rank] = p2[1];
-        }
+        publish(2);
         if (!team_barrier(st, w.nblk))
         {
             status = 9;
             break;
         }
         double t[2] = {0.0, 0.0};
-        for (int k = tid; k < w.nblk; k += kPBlock)
+        for (int k = tid; k < nt; k += kPBlock)
         {
-            t[0] += __ldcg(d.part + nt + k);
-            t[1] += __ldcg(d.part + 2 * nt + k);
+            t[0] += __ldcg(d.part + k);
+            t[1] += __ldcg(d.part + nt + k);
         }
         block_allreduce<2>(t, red);
         const double rho_new = t[0];
