@@ -555,7 +555,7 @@ int plan_persistent(cloth_ctx *ctx, Batch *b)
     for (int i = 0; i < n; i++)
     {
         const Tables &t = b->members[i]->tab;
-        const int maxb = std::max(1, (t.nv + kTile - 1) / kTile);
+        const int maxb = std::max(1, (t.nv + kRedRows - 1) / kRedRows);
         long long want = (long long)G * t.nv / std::max(1ll, total);
         nb[i] = int(std::max(1ll, std::min<long long>(want, maxb)));
         used += nb[i];
@@ -568,7 +568,7 @@ int plan_persistent(cloth_ctx *ctx, Batch *b)
         for (int i = 0; i < n; i++)
         {
             const Tables &t = b->members[i]->tab;
-            const int maxb = std::max(1, (t.nv + kTile - 1) / kTile);
+            const int maxb = std::max(1, (t.nv + kRedRows - 1) / kRedRows);
             if (nb[i] >= maxb)
                 continue;
             double load = double(t.nv) / nb[i];
@@ -603,9 +603,9 @@ int plan_persistent(cloth_ctx *ctx, Batch *b)
     for (int i = 0; i < n; i++)
     {
         const Tables &t = b->members[i]->tab;
-        // 128-row aligned ranges keep the reduction tiles of an instance the
+        // ranges aligned to the reduction units keep an instance's sums the
         // same whatever the team size
-        const int chunk = ((t.nv + nb[i] - 1) / nb[i] + kTile - 1) / kTile * kTile;
+        const int chunk = ((t.nv + nb[i] - 1) / nb[i] + kRedRows - 1) / kRedRows * kRedRows;
         if (chunk > kMaxBlockRows)
             return CLOTH_OK;
         int rank = 0;
@@ -678,7 +678,7 @@ int build_graph(Batch *b, bool full, cudaGraphExec_t *exec)
     cudaGraph_t g = nullptr;
     CK(cudaGraphCreate(&g, 0));
     int rc = CLOTH_OK;
-    cudaGraphConditionalHandle hnd;
+    cudaGraphConditionalHandle hnd = 0;
     cudaGraphNode_t last = nullptr, n = nullptr;
     int one = 1, zero = 0;
     int ninst = int(b->members.size());
@@ -698,8 +698,9 @@ int build_graph(Batch *b, bool full, cudaGraphExec_t *exec)
                         f == (void *)k_cond ? 1 : kTile, args);
         last = n;
     };
-    if (cudaGraphConditionalHandleCreate(&hnd, g, 1, cudaGraphCondAssignDefault) !=
-        cudaSuccess)
+    if (!b->persist_ok &&
+        cudaGraphConditionalHandleCreate(&hnd, g, 1, cudaGraphCondAssignDefault) !=
+            cudaSuccess)
     {
         cudaGraphDestroy(g);
         return fail(CLOTH_ERR_CUDA, "cudaGraphConditionalHandleCreate failed");

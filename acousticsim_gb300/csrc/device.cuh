@@ -116,7 +116,8 @@ struct TeamBlock
     int pad;
 };
 
-constexpr int kPBlock = 512;                 // threads per persistent block
+constexpr int kPBlock = 1024;                // threads per persistent block
+constexpr int kRedRows = 256;                // rows per reduction unit (team ranges align to it)
 constexpr int kMaxBlockRows = 16384;         // rows one persistent block may own
 constexpr unsigned kSpinLimit = 1u << 25;    // bounded barrier wait (~seconds)
 

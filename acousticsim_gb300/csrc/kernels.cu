@@ -41,10 +41,18 @@ __device__ __forceinline__ float4 f4(float3 v, float w = 0.f)
 {
     return make_float4(v.x, v.y, v.z, w);
 }
-__device__ __forceinline__ double ddot(float3 a, float3 b)
+// Row-level products stay in FP32; sums from 32 rows upward are FP64 (GB300's
+// FP64 pipe is narrow, so FP64 work is kept per warp, not per row).
+__device__ __forceinline__ float fdot(float3 a, float3 b)
 {
-    return double(a.x) * double(b.x) + double(a.y) * double(b.y) +
-           double(a.z) * double(b.z);
+    return fmaf(a.z, b.z, fmaf(a.y, b.y, a.x * b.x));
+}
+__device__ __forceinline__ float warp_sum(float v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+        v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
 }
 // sum of squares in component order, as tCudaMatrix::norm (CudaMatrix.h:314-320)
 __device__ __forceinline__ float norm3(float3 a)
@@ -95,9 +103,38 @@ __device__ __forceinline__ void sym_inverse(const float *a, float *m)
     m[5] = c22 * inv;
 }
 
-// Sum N doubles over the block; thread 0 gets the totals. Fixed order.
+// Sum N values over the block (FP32 within a warp, FP64 across warps);
+// thread 0 gets the totals. Fixed order.
 template <int N>
-__device__ __forceinline__ void block_sum(double (&v)[N], double (*sh)[kTile / 32])
+__device__ __forceinline__ void block_sum(const float (&vf)[N], double (&v)[N],
+                                          double (*sh)[kTile / 32])
+{
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    float t[N];
+#pragma unroll
+    for (int k = 0; k < N; k++)
+        t[k] = warp_sum(vf[k]);
+    if (l == 0)
+#pragma unroll
+        for (int k = 0; k < N; k++)
+            sh[k][w] = double(t[k]);
+    __syncthreads();
+    if (threadIdx.x == 0)
+#pragma unroll
+        for (int k = 0; k < N; k++)
+        {
+            double s = sh[k][0];
+#pragma unroll
+            for (int j = 1; j < kTile / 32; j++)
+                s += sh[k][j];
+            v[k] = s;
+        }
+    __syncthreads();
+}
+
+// FP64 block sum (last-tile stage only); thread 0 gets the totals.
+template <int N>
+__device__ __forceinline__ void block_sum_d(double (&v)[N], double (*sh)[kTile / 32])
 {
 #pragma unroll
     for (int k = 0; k < N; k++)
@@ -127,11 +164,12 @@ __device__ __forceinline__ void block_sum(double (&v)[N], double (*sh)[kTile / 3
 // last tile. When it is, every thread of the block returns true and totals
 // holds the instance sums (summed in tile order, deterministic).
 template <int N>
-__device__ bool tile_reduce(const InstDesc &d, int tile_idx, double (&v)[N],
+__device__ bool tile_reduce(const InstDesc &d, int tile_idx, const float (&vf)[N],
                             double (&totals)[N], double (*sh)[kTile / 32],
                             int *flag)
 {
-    block_sum<N>(v, sh);
+    double v[N];
+    block_sum<N>(vf, v, sh);
     const int nt = d.ntile_rows;
     if (threadIdx.x == 0)
     {
@@ -155,7 +193,7 @@ __device__ bool tile_reduce(const InstDesc &d, int tile_idx, double (&v)[N],
 #pragma unroll
         for (int k = 0; k < N; k++)
             s[k] += __ldcg(&d.part[k * nt + i]);
-    block_sum<N>(s, sh);
+    block_sum_d<N>(s, sh);
 #pragma unroll
     for (int k = 0; k < N; k++)
         totals[k] = s[k];
@@ -334,7 +372,7 @@ __global__ void __launch_bounds__(kTile) k_row(InstDesc *const *descs,
         const Tile tl = tiles[ti];
         const InstDesc &d = *descs[tl.inst];
         const int row = tl.start + threadIdx.x;
-        double part[3] = {0.0, 0.0, 0.0};
+        float part[3] = {0.f, 0.f, 0.f};
         if (row < d.nv)
         {
             const int info = d.rowinfo[row];
@@ -422,9 +460,9 @@ __global__ void __launch_bounds__(kTile) k_row(InstDesc *const *descs,
             d.z[row] = f4(z);
             d.M0[row] = make_float4(M[0], M[1], M[2], M[3]);
             d.M1[row] = make_float2(M[4], M[5]);
-            part[0] = ddot(r, z);
-            part[1] = ddot(r, r);
-            part[2] = ddot(b, b);
+            part[0] = fdot(r, z);
+            part[1] = fdot(r, r);
+            part[2] = fdot(b, b);
         }
         double tot[3];
         if (tile_reduce<3>(d, tl.start / kTile, part, tot, sh, &flag) &&
@@ -488,7 +526,7 @@ __global__ void __launch_bounds__(kTile) k_spmv(InstDesc *const *descs,
         const float4 *pold = (it & 1) ? d.p1 : d.p0;
         float4 *pnew = (it & 1) ? d.p0 : d.p1;
         const int row = tl.start + threadIdx.x;
-        double part[1] = {0.0};
+        float part[1] = {0.f};
         if (row < d.nv)
         {
             const int len = d.rowinfo[row] & 255;
@@ -515,7 +553,7 @@ __global__ void __launch_bounds__(kTile) k_spmv(InstDesc *const *descs,
                 q = q + symv(A, pc);
             }
             d.q[row] = f4(q);
-            part[0] = ddot(pv, q);
+            part[0] = fdot(pv, q);
         }
         double tot[1];
         if (tile_reduce<1>(d, tl.start / kTile, part, tot, sh, &flag) &&
@@ -563,7 +601,7 @@ __global__ void __launch_bounds__(kTile) k_update(InstDesc *const *descs,
         const float alpha = float(stp->alpha);
         const float4 *pnew = (it & 1) ? d.p0 : d.p1;
         const int row = tl.start + threadIdx.x;
-        double part[2] = {0.0, 0.0};
+        float part[2] = {0.f, 0.f};
         if (row < d.nv)
         {
             const float3 p = xyz(pnew[row]);
@@ -580,8 +618,8 @@ __global__ void __launch_bounds__(kTile) k_update(InstDesc *const *descs,
             d.dx[row] = f4(x);
             d.r[row] = f4(r);
             d.z[row] = f4(z);
-            part[0] = ddot(r, z);
-            part[1] = ddot(r, r);
+            part[0] = fdot(r, z);
+            part[1] = fdot(r, r);
         }
         double tot[2];
         if (tile_reduce<2>(d, tl.start / kTile, part, tot, sh, &flag) &&
@@ -634,33 +672,6 @@ __global__ void __launch_bounds__(kTile) k_update(InstDesc *const *descs,
 // without a third synchronisation.  Data written by other blocks inside the
 // kernel (z, p, partials) is read through L2 (ld.global.cg); A is read-only.
 namespace {
-
-// All threads of the block get the block sums of v[0..N) (fixed order).
-template <int N>
-__device__ __forceinline__ void block_allreduce(double (&v)[N], double *sh)
-{
-    constexpr int NW = kPBlock / 32;
-    __syncthreads();
-#pragma unroll
-    for (int k = 0; k < N; k++)
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1)
-            v[k] += __shfl_xor_sync(0xffffffffu, v[k], o);
-    if ((threadIdx.x & 31) == 0)
-#pragma unroll
-        for (int k = 0; k < N; k++)
-            sh[k * NW + (threadIdx.x >> 5)] = v[k];
-    __syncthreads();
-#pragma unroll
-    for (int k = 0; k < N; k++)
-    {
-        double t = sh[k * NW];
-#pragma unroll
-        for (int j = 1; j < NW; j++)
-            t += sh[k * NW + j];
-        v[k] = t;
-    }
-}
 
 // Barrier of the nblk blocks of one team. Returns false when the bounded
 // wait gave up (then the team's error flag is set and the solve stops).
@@ -715,40 +726,73 @@ __global__ void __launch_bounds__(kPBlock, 1)
     k_pcg_persistent(InstDesc *const *descs, const TeamBlock *work)
 {
     constexpr int NW = kPBlock / 32;
+    constexpr int CPU = kRedRows / 32; // 32-row chunks per reduction unit
     extern __shared__ float4 sp[];
-    __shared__ double red[3 * NW];
-    // per-32-row chunk sums of this block (team ranges are 128-row aligned
-    // and at most kMaxBlockRows long)
+    __shared__ InstDesc d;
+    __shared__ double bc[2];
     __shared__ double csum[2][kMaxBlockRows / 32];
     const TeamBlock w = work[blockIdx.x];
     if (w.inst < 0)
         return;
-    const InstDesc d = *descs[w.inst];
+    if (threadIdx.x == 0)
+        d = *descs[w.inst];
+    __syncthreads();
     InstState *st = d.st;
     if (!__ldcg(&st->active))
         return;
-    const int nt = d.ntile_rows;
+    const int nt = d.ntile_rows;                        // stride of the partial arrays
+    const int nu = (d.nv + kRedRows - 1) / kRedRows;    // reduction units of the instance
     double rho = __ldcg(&st->rho);
     double beta = 0.0, alpha = 0.0, pq = 0.0, rr = __ldcg(&st->rr);
     int it = 0, status = 0;
     const bool staged = w.halo0 >= 0;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int nch = (w.row1 - w.row0 + 31) / 32;
-    const int ntl = (w.row1 - w.row0 + kTile - 1) / kTile;
-    const int tile0 = w.row0 / kTile;
-    // Tile partials (fixed order over the tile's four 32-row chunks) go to
-    // d.part[k*nt + tile]; the team sums them over all the instance's tiles in
-    // a fixed thread assignment, independent of the team's size.
+    const int nun = (w.row1 - w.row0 + kRedRows - 1) / kRedRows;
+    const int unit0 = w.row0 / kRedRows;
+    // Unit partials: fixed-order FP64 sums of the unit's 32-row chunk sums,
+    // written to d.part[q*nt + unit]; the units are the same whatever the
+    // team size, so an instance's sums do not depend on its neighbours.
     auto publish = [&](int nq) {
         __syncthreads();
-        for (int t = tid; t < ntl; t += kPBlock)
-            for (int k = 0; k < nq; k++)
+        for (int u = tid; u < nun; u += kPBlock)
+            for (int q = 0; q < nq; q++)
             {
                 double v = 0.0;
-                for (int c = 4 * t; c < min(4 * t + 4, nch); c++)
-                    v += csum[k][c];
-                d.part[k * nt + tile0 + t] = v;
+                for (int c = CPU * u; c < min(CPU * u + CPU, nch); c++)
+                    v += csum[q][c];
+                d.part[q * nt + unit0 + u] = v;
             }
+    };
+    // Team total of nq quantities: warp 0 sums the nu unit partials (FP64,
+    // fixed lane assignment and tree), the block reads it from shared memory.
+    auto team_total = [&](int nq, double *out) {
+        if (warp == 0)
+        {
+            double s0 = 0.0, s1 = 0.0;
+            for (int k = lane; k < nu; k += 32)
+            {
+                s0 += __ldcg(d.part + k);
+                if (nq > 1)
+                    s1 += __ldcg(d.part + nt + k);
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1)
+            {
+                s0 += __shfl_xor_sync(0xffffffffu, s0, o);
+                if (nq > 1)
+                    s1 += __shfl_xor_sync(0xffffffffu, s1, o);
+            }
+            if (lane == 0)
+            {
+                bc[0] = s0;
+                bc[1] = s1;
+            }
+        }
+        __syncthreads();
+        out[0] = bc[0];
+        if (nq > 1)
+            out[1] = bc[1];
     };
     for (;;)
     {
@@ -778,7 +822,7 @@ __global__ void __launch_bounds__(kPBlock, 1)
         for (int ch = warp; ch < nch; ch += NW)
         {
             const int row = w.row0 + ch * 32 + lane;
-            double part = 0.0;
+            float part = 0.f;
             if (row < w.row1)
             {
                 float3 pv;
@@ -824,13 +868,11 @@ __global__ void __launch_bounds__(kPBlock, 1)
                     q = q + symv(A, pc);
                 }
                 d.q[row] = f4(q);
-                part = ddot(pv, q);
+                part = fdot(pv, q);
             }
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1)
-                part += __shfl_xor_sync(0xffffffffu, part, o);
+            part = warp_sum(part);
             if (lane == 0)
-                csum[0][ch] = part;
+                csum[0][ch] = double(part);
         }
         publish(1);
         if (!team_barrier(st, w.nblk))
@@ -838,13 +880,7 @@ __global__ void __launch_bounds__(kPBlock, 1)
             status = 9; // CLOTH_ERR_TIMEOUT
             break;
         }
-        {
-            double t[1] = {0.0};
-            for (int k = tid; k < nt; k += kPBlock)
-                t[0] += __ldcg(d.part + k);
-            block_allreduce<1>(t, red);
-            pq = t[0];
-        }
+        team_total(1, &pq);
         if (!isfinite(pq))
         {
             status = 6;
@@ -861,7 +897,7 @@ __global__ void __launch_bounds__(kPBlock, 1)
         for (int ch = warp; ch < nch; ch += NW)
         {
             const int row = w.row0 + ch * 32 + lane;
-            double pr = 0.0, prr = 0.0;
+            float pr = 0.f, prr = 0.f;
             if (row < w.row1)
             {
                 const float3 p = staged ? xyz(sp[row - w.halo0]) : xyz(pnew[row]);
@@ -877,19 +913,15 @@ __global__ void __launch_bounds__(kPBlock, 1)
                 d.dx[row] = f4(x);
                 d.r[row] = f4(r);
                 d.z[row] = f4(z);
-                pr = ddot(r, z);
-                prr = ddot(r, r);
+                pr = fdot(r, z);
+                prr = fdot(r, r);
             }
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1)
-            {
-                pr += __shfl_xor_sync(0xffffffffu, pr, o);
-                prr += __shfl_xor_sync(0xffffffffu, prr, o);
-            }
+            pr = warp_sum(pr);
+            prr = warp_sum(prr);
             if (lane == 0)
             {
-                csum[0][ch] = pr;
-                csum[1][ch] = prr;
+                csum[0][ch] = double(pr);
+                csum[1][ch] = double(prr);
             }
         }
         publish(2);
@@ -898,13 +930,8 @@ __global__ void __launch_bounds__(kPBlock, 1)
             status = 9;
             break;
         }
-        double t[2] = {0.0, 0.0};
-        for (int k = tid; k < nt; k += kPBlock)
-        {
-            t[0] += __ldcg(d.part + k);
-            t[1] += __ldcg(d.part + nt + k);
-        }
-        block_allreduce<2>(t, red);
+        double t[2];
+        team_total(2, t);
         const double rho_new = t[0];
         rr = t[1];
         beta = (rho == 0.0) ? 0.0 : rho_new / rho;
