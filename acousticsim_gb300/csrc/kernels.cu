@@ -20,6 +20,8 @@
 // Reference kernels: src/sim/cloth/BaraffClothGpu.cu, src/sim/cloth/gpu_solvers/PCGSolver.cu.
 #include "device.cuh"
 
+#include <type_traits>
+
 namespace cloth {
 
 namespace {
@@ -729,7 +731,8 @@ __global__ void __launch_bounds__(kPBlock, 1)
     constexpr int CPU = kRedRows / 32; // 32-row chunks per reduction unit
     extern __shared__ float4 sp[];
     __shared__ InstDesc d;
-    __shared__ double bc[2];
+    __shared__ double bc_alpha, bc_beta;
+    __shared__ int bc_stop;
     __shared__ double csum[2][kMaxBlockRows / 32];
     const TeamBlock w = work[blockIdx.x];
     if (w.inst < 0)
@@ -766,33 +769,38 @@ __global__ void __launch_bounds__(kPBlock, 1)
     };
     // Team total of nq quantities: warp 0 sums the nu unit partials (FP64,
     // fixed lane assignment and tree), the block reads it from shared memory.
-    auto team_total = [&](int nq, double *out) {
+    // The caller's warp 0 then turns the totals into the PCG scalars (one
+    // thread), which the block reads back from shared memory.
+    auto team_total = [&](auto nq_tag, double *out) {
+        constexpr int NQ = decltype(nq_tag)::value;
         if (warp == 0)
         {
-            double s0 = 0.0, s1 = 0.0;
-            for (int k = lane; k < nu; k += 32)
-            {
-                s0 += __ldcg(d.part + k);
-                if (nq > 1)
-                    s1 += __ldcg(d.part + nt + k);
-            }
+            double a[NQ][2];
 #pragma unroll
-            for (int o = 16; o > 0; o >>= 1)
+            for (int q = 0; q < NQ; q++)
+                a[q][0] = a[q][1] = 0.0;
+            int k = lane;
+            for (; k + 32 < nu; k += 64)
+#pragma unroll
+                for (int q = 0; q < NQ; q++)
+                {
+                    a[q][0] += __ldcg(d.part + q * nt + k);
+                    a[q][1] += __ldcg(d.part + q * nt + k + 32);
+                }
+            if (k < nu)
+#pragma unroll
+                for (int q = 0; q < NQ; q++)
+                    a[q][0] += __ldcg(d.part + q * nt + k);
+#pragma unroll
+            for (int q = 0; q < NQ; q++)
             {
-                s0 += __shfl_xor_sync(0xffffffffu, s0, o);
-                if (nq > 1)
-                    s1 += __shfl_xor_sync(0xffffffffu, s1, o);
-            }
-            if (lane == 0)
-            {
-                bc[0] = s0;
-                bc[1] = s1;
+                double v = a[q][0] + a[q][1];
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1)
+                    v += __shfl_xor_sync(0xffffffffu, v, o);
+                out[q] = v;
             }
         }
-        __syncthreads();
-        out[0] = bc[0];
-        if (nq > 1)
-            out[1] = bc[1];
     };
     for (;;)
     {
@@ -842,30 +850,47 @@ __global__ void __launch_bounds__(kPBlock, 1)
                 pnew[row] = f4(pv);
                 const int len = __ldg(d.rowinfo + row) & 255;
                 float3 q = make_float3(0, 0, 0);
-                for (int s = 0; s < len; s++)
+                // four slots at a time: their loads are all in flight together
+                for (int s0 = 0; s0 < len; s0 += 4)
                 {
-                    const size_t o = size_t(s) * d.stride + row;
-                    const int c = __ldg(d.col + o);
-                    const float4 a0 = __ldg(d.A0 + o);
-                    const float2 a1 = __ldg(d.A1 + o);
-                    const float A[6] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y};
-                    float3 pc;
-                    if (staged)
-                        pc = xyz(sp[c - w.halo0]);
-                    else if (c == row)
-                        pc = pv;
-                    else
-                    {
-                        const float4 zz = ldcg4(d.z + c);
-                        pc = xyz(zz);
-                        if (!first)
+                    int cc[4];
+                    float4 a0[4];
+                    float2 a1[4];
+#pragma unroll
+                    for (int k = 0; k < 4; k++)
+                        if (s0 + k < len)
                         {
-                            const float4 po = ldcg4(pold + c);
-                            pc = make_float3(fmaf(bf, po.x, zz.x), fmaf(bf, po.y, zz.y),
-                                             fmaf(bf, po.z, zz.z));
+                            const size_t o = size_t(s0 + k) * d.stride + row;
+                            cc[k] = __ldg(d.col + o);
+                            a0[k] = __ldg(d.A0 + o);
+                            a1[k] = __ldg(d.A1 + o);
                         }
-                    }
-                    q = q + symv(A, pc);
+#pragma unroll
+                    for (int k = 0; k < 4; k++)
+                        if (s0 + k < len)
+                        {
+                            const int c = cc[k];
+                            const float A[6] = {a0[k].x, a0[k].y, a0[k].z, a0[k].w,
+                                                a1[k].x, a1[k].y};
+                            float3 pc;
+                            if (staged)
+                                pc = xyz(sp[c - w.halo0]);
+                            else if (c == row)
+                                pc = pv;
+                            else
+                            {
+                                const float4 zz = ldcg4(d.z + c);
+                                pc = xyz(zz);
+                                if (!first)
+                                {
+                                    const float4 po = ldcg4(pold + c);
+                                    pc = make_float3(fmaf(bf, po.x, zz.x),
+                                                     fmaf(bf, po.y, zz.y),
+                                                     fmaf(bf, po.z, zz.z));
+                                }
+                            }
+                            q = q + symv(A, pc);
+                        }
                 }
                 d.q[row] = f4(q);
                 part = fdot(pv, q);
@@ -880,18 +905,30 @@ __global__ void __launch_bounds__(kPBlock, 1)
             status = 9; // CLOTH_ERR_TIMEOUT
             break;
         }
-        team_total(1, &pq);
-        if (!isfinite(pq))
         {
-            status = 6;
-            break;
+            double t1[1];
+            team_total(std::integral_constant<int, 1>(), t1);
+            if (tid == 0)
+            {
+                pq = t1[0];
+                int stop = 0;
+                if (!isfinite(pq))
+                    stop = 6;
+                else if (pq == 0.0)
+                    stop = 7;
+                else
+                    alpha = rho / pq;
+                bc_alpha = alpha;
+                bc_stop = stop;
+            }
+            __syncthreads();
+            if (bc_stop)
+            {
+                status = bc_stop;
+                break;
+            }
+            alpha = bc_alpha;
         }
-        if (pq == 0.0)
-        {
-            status = 7;
-            break;
-        }
-        alpha = rho / pq;
         const float af = float(alpha);
         // ---- dx += alpha p, r -= alpha q, z = M^-1 r; r.z and r.r per chunk
         for (int ch = warp; ch < nch; ch += NW)
@@ -930,25 +967,38 @@ __global__ void __launch_bounds__(kPBlock, 1)
             status = 9;
             break;
         }
-        double t[2];
-        team_total(2, t);
-        const double rho_new = t[0];
-        rr = t[1];
-        beta = (rho == 0.0) ? 0.0 : rho_new / rho;
-        rho = rho_new;
-        it++;
-        if (!isfinite(rho_new) || !isfinite(rr))
         {
-            status = 6;
-            break;
-        }
-        const bool check = ((it - 1) % d.check_every) == 0 || it >= d.max_iters;
-        if (check && test_converged(d, *st, rr))
-            break;
-        if (it >= d.max_iters)
-        {
-            status = 8;
-            break;
+            double t2[2];
+            team_total(std::integral_constant<int, 2>(), t2);
+            it++;
+            if (tid == 0)
+            {
+                const double rho_new = t2[0];
+                rr = t2[1];
+                beta = (rho == 0.0) ? 0.0 : rho_new / rho;
+                rho = rho_new;
+                int stop = 0; // 0 go on, 1 converged, else a status code
+                if (!isfinite(rho_new) || !isfinite(rr))
+                    stop = 6;
+                else
+                {
+                    const bool check = ((it - 1) % d.check_every) == 0 || it >= d.max_iters;
+                    if (check && test_converged(d, *st, rr))
+                        stop = 1;
+                    else if (it >= d.max_iters)
+                        stop = 8;
+                }
+                bc_beta = beta;
+                bc_stop = stop;
+            }
+            __syncthreads();
+            beta = bc_beta;
+            const int stop = bc_stop;
+            if (stop)
+            {
+                status = (stop == 1) ? 0 : stop;
+                break;
+            }
         }
     }
     if (w.rank == 0 && tid == 0)
