@@ -25,7 +25,10 @@ __global__ void k_update(InstDesc *const *descs, const Tile *tiles, BatchCtl *ct
 __global__ void k_advance(InstDesc *const *descs, const Tile *tiles,
                           const BatchCtl *ctl);
 __global__ void k_sync_x32(InstDesc *d);
-__global__ void k_pcg_persistent(InstDesc *const *descs, const TeamBlock *work);
+__global__ void k_pcg_persistent_sm(InstDesc *const *descs, const TeamBlock *work,
+                                    int halo_cap, int rows_cap);
+__global__ void k_pcg_persistent_gm(InstDesc *const *descs, const TeamBlock *work,
+                                    int halo_cap, int rows_cap);
 } // namespace cloth
 
 using namespace cloth;
@@ -133,8 +136,10 @@ struct Batch
     int grid_tri = 1, grid_row = 1, grid_spmv = 1, grid_update = 1;
     // persistent solver plan
     bool persist_ok = false;
+    bool persist_sm = false; // own-row state in shared memory
     TeamBlock *d_work = nullptr;
     int grid_persist = 0;
+    int halo_cap = 0, rows_cap = 0;
     size_t smem_persist = 0;
     cudaGraphExec_t step_exec = nullptr;
     cudaGraphExec_t solve_exec = nullptr;
@@ -534,9 +539,11 @@ int plan_persistent(cloth_ctx *ctx, Batch *b)
     const int cap_entries = int(smem_cap_bytes / sizeof(float4));
     // occupancy at the largest staging size we may request
     int occ = 0;
-    if (cudaFuncSetAttribute(k_pcg_persistent, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    if (cudaFuncSetAttribute(k_pcg_persistent_sm, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              int(smem_cap_bytes)) != cudaSuccess ||
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_pcg_persistent, kPBlock,
+        cudaFuncSetAttribute(k_pcg_persistent_gm, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             int(smem_cap_bytes)) != cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_pcg_persistent_gm, kPBlock,
                                                       smem_cap_bytes) != cudaSuccess ||
         occ <= 0)
     {
@@ -599,7 +606,7 @@ int plan_persistent(cloth_ctx *ctx, Batch *b)
         used--;
     }
     std::vector<TeamBlock> work;
-    int max_entries = 0;
+    int max_entries = 0, max_rows = 0;
     for (int i = 0; i < n; i++)
     {
         const Tables &t = b->members[i]->tab;
@@ -631,6 +638,7 @@ int plan_persistent(cloth_ctx *ctx, Batch *b)
         for (auto &w : team)
         {
             w.nblk = int(team.size());
+            max_rows = std::max(max_rows, w.row1 - w.row0);
             if (w.halo1 - w.halo0 > cap_entries)
                 w.halo0 = w.halo1 = -1;
             else
@@ -640,10 +648,17 @@ int plan_persistent(cloth_ctx *ctx, Batch *b)
     }
     while (int(work.size()) < G)
         work.push_back(TeamBlock{-1, 0, 0, 0, 0, -1, -1, 0});
-    b->smem_persist = size_t(max_entries) * sizeof(float4);
+    // own-row state (dx, r, q, M^-1: 72 bytes per row) in shared memory when
+    // it fits next to the staged p
+    b->halo_cap = max_entries;
+    b->rows_cap = max_rows;
+    const size_t sm_bytes = size_t(max_entries) * sizeof(float4) + size_t(max_rows) * 72;
+    b->persist_sm = sm_bytes <= smem_cap_bytes;
+    b->smem_persist = b->persist_sm ? sm_bytes : size_t(max_entries) * sizeof(float4);
     int occ2 = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ2, k_pcg_persistent, kPBlock,
-                                                      b->smem_persist) != cudaSuccess ||
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+            &occ2, b->persist_sm ? k_pcg_persistent_sm : k_pcg_persistent_gm, kPBlock,
+            b->smem_persist) != cudaSuccess ||
         occ2 * ctx->num_sms < int(work.size()))
     {
         cudaGetLastError();
@@ -723,12 +738,13 @@ int build_graph(Batch *b, bool full, cudaGraphExec_t *exec)
     }
     if (b->persist_ok)
     {
-        void *a_per[] = {&b->d_descs, &b->d_work};
+        void *a_per[] = {&b->d_descs, &b->d_work, &b->halo_cap, &b->rows_cap};
         if (rc == CLOTH_OK)
         {
             cudaKernelNodeParams p;
             std::memset(&p, 0, sizeof(p));
-            p.func = (void *)k_pcg_persistent;
+            p.func = b->persist_sm ? (void *)k_pcg_persistent_sm
+                                   : (void *)k_pcg_persistent_gm;
             p.gridDim = dim3(b->grid_persist);
             p.blockDim = dim3(kPBlock);
             p.sharedMemBytes = unsigned(b->smem_persist);
@@ -809,9 +825,11 @@ int launch_persistent(Batch *b)
 {
     cloth_ctx *ctx = b->ctx;
     PhaseTimer t(ctx, PH_SPMV);
-    void *args[] = {&b->d_descs, &b->d_work};
-    CK(cudaLaunchCooperativeKernel((void *)k_pcg_persistent, dim3(b->grid_persist),
-                                   dim3(kPBlock), args, b->smem_persist, ctx->stream));
+    void *args[] = {&b->d_descs, &b->d_work, &b->halo_cap, &b->rows_cap};
+    CK(cudaLaunchCooperativeKernel(b->persist_sm ? (void *)k_pcg_persistent_sm
+                                                 : (void *)k_pcg_persistent_gm,
+                                   dim3(b->grid_persist), dim3(kPBlock), args,
+                                   b->smem_persist, ctx->stream));
     return CLOTH_OK;
 }
 

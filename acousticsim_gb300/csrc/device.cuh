@@ -47,6 +47,11 @@ struct InstState
     unsigned bar_gen;
     int bar_err;
     int pad;
+    // exact fixed-point team sums of the persistent solver, triple-buffered by
+    // iteration: [buffer][quantity: p.q, r.z, r.r][limb: units of 2^32, units]
+    unsigned long long acc[3][3][2];
+    float acc_chk[3][3];  // FP32 magnitude check of the same sums
+    float pad2[3];
 };
 
 struct InstDesc
@@ -116,8 +121,13 @@ struct TeamBlock
     int pad;
 };
 
+// Fixed-point scale: sums are carried as round(v * 2^s) with s chosen from
+// the previous value of the same quantity so that it maps to about 2^kFxTop.
+constexpr int kFxTop = 70;
+
 constexpr int kPBlock = 1024;                // threads per persistent block
-constexpr int kRedRows = 256;                // rows per reduction unit (team ranges align to it)
+constexpr int kRedRows = 32;                 // team ranges align to 32-row chunks (the FP32 warp sums)
+constexpr int kSlotUnroll = 3;               // ELL slots whose loads are issued together
 constexpr int kMaxBlockRows = 16384;         // rows one persistent block may own
 constexpr unsigned kSpinLimit = 1u << 25;    // bounded barrier wait (~seconds)
 

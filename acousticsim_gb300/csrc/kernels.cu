@@ -483,6 +483,13 @@ __global__ void __launch_bounds__(kTile) k_row(InstDesc *const *descs,
             st.status = 0;
             st.bar_count = 0u;
             st.bar_err = 0;
+            for (int bq = 0; bq < 3; bq++)
+                for (int q = 0; q < 3; q++)
+                {
+                    st.acc[bq][q][0] = 0ull;
+                    st.acc[bq][q][1] = 0ull;
+                    st.acc_chk[bq][q] = 0.f;
+                }
             if (!isfinite(tot[0]) || !isfinite(tot[1]) || !isfinite(tot[2]))
             {
                 st.status = 6; // CLOTH_ERR_NAN
@@ -724,16 +731,110 @@ __device__ __forceinline__ float4 ldcg4(const float4 *p) { return __ldcg(p); }
 
 } // namespace
 
-__global__ void __launch_bounds__(kPBlock, 1)
-    k_pcg_persistent(InstDesc *const *descs, const TeamBlock *work)
+namespace {
+
+// round(v * 2^s) as a signed 128-bit integer, returned as H * 2^32 + L with
+// 0 <= L < 2^32 (integer operations only).  Exact addition of these limbs
+// makes a team sum independent of how the rows are split over blocks.
+__device__ __forceinline__ void fx_split(float v, int s, long long &H,
+                                         unsigned long long &L)
+{
+    const unsigned bits = __float_as_uint(v);
+    const int e = int((bits >> 23) & 0xffu);
+    H = 0;
+    L = 0;
+    if (e == 0 || e == 255)
+        return; // zero, subnormal (below any scale in use) or Inf/NaN (check sum)
+    const unsigned long long m = (bits & 0x7fffffu) | 0x800000u;
+    const int sh = e - 150 + s; // |v| = m * 2^(e - 150)
+    unsigned long long fh = 0ull, fl = 0ull;
+    if (sh >= 104)
+    {
+        fh = 0x3fffffffffffffffull; // saturate; the check sum flags it
+        fl = ~0ull;
+    }
+    else if (sh >= 64)
+        fh = m << (sh - 64);
+    else if (sh > 0)
+    {
+        fl = m << sh;
+        fh = m >> (64 - sh);
+    }
+    else if (sh == 0)
+        fl = m;
+    else if (sh > -25)
+        fl = (m + (1ull << (-sh - 1))) >> (-sh);
+    if (bits & 0x80000000u)
+    {
+        fl = ~fl + 1ull;
+        fh = ~fh + (fl == 0ull ? 1ull : 0ull);
+    }
+    L = fl & 0xffffffffull;
+    H = (long long)((fh << 32) | (fl >> 32));
+}
+
+// Scale exponent for an estimate of a sum (from the double's exponent bits).
+__device__ __forceinline__ int fx_scale(double est)
+{
+    const long long b = __double_as_longlong(est);
+    const int e = int((b >> 52) & 0x7ff);
+    if (e == 0 || e == 0x7ff)
+        return 100;
+    const int s = kFxTop - (e - 1023);
+    return max(-900, min(900, s));
+}
+
+__device__ __forceinline__ double fx_value(unsigned long long H, unsigned long long L,
+                                           int s)
+{
+    return ldexp(double((long long)H), 32 - s) + ldexp(double(L), -s);
+}
+
+// Per-warp fixed-point accumulator of NQ chunk sums (held by lane 0).
+template <int NQ> struct WarpFx
+{
+    long long H[NQ];
+    unsigned long long L[NQ];
+    float chk[NQ];
+    __device__ __forceinline__ void clear()
+    {
+#pragma unroll
+        for (int q = 0; q < NQ; q++)
+        {
+            H[q] = 0;
+            L[q] = 0ull;
+            chk[q] = 0.f;
+        }
+    }
+    __device__ __forceinline__ void add(int q, float v, int s)
+    {
+        long long h;
+        unsigned long long l;
+        fx_split(v, s, h, l);
+        H[q] += h;
+        L[q] += l;
+        chk[q] += v;
+    }
+};
+
+} // namespace
+
+// State of the block's own rows lives in shared memory (SM = true) or in
+// global memory (SM = false, for row ranges too long for shared memory).
+template <bool SM>
+__device__ __forceinline__ void pcg_persistent_body(InstDesc *const *descs,
+                                                    const TeamBlock *work, int halo_cap,
+                                                    int rows_cap)
 {
     constexpr int NW = kPBlock / 32;
-    constexpr int CPU = kRedRows / 32; // 32-row chunks per reduction unit
-    extern __shared__ float4 sp[];
+    extern __shared__ float4 sm_dyn[];
     __shared__ InstDesc d;
-    __shared__ double bc_alpha, bc_beta;
-    __shared__ int bc_stop;
-    __shared__ double csum[2][kMaxBlockRows / 32];
+    __shared__ unsigned long long blk_acc[2][2];
+    __shared__ float blk_chk[2];
+    // FP64 PCG scalars: owned by thread 0, the block reads the FP32 copies
+    __shared__ double s_rho, s_beta, s_alpha, s_pq, s_rr;
+    __shared__ float bc_af, bc_bf;
+    __shared__ int bc_stop, bc_s[3];
     const TeamBlock w = work[blockIdx.x];
     if (w.inst < 0)
         return;
@@ -743,74 +844,102 @@ __global__ void __launch_bounds__(kPBlock, 1)
     InstState *st = d.st;
     if (!__ldcg(&st->active))
         return;
-    const int nt = d.ntile_rows;                        // stride of the partial arrays
-    const int nu = (d.nv + kRedRows - 1) / kRedRows;    // reduction units of the instance
-    double rho = __ldcg(&st->rho);
-    double beta = 0.0, alpha = 0.0, pq = 0.0, rr = __ldcg(&st->rr);
-    int it = 0, status = 0;
-    const bool staged = w.halo0 >= 0;
+    // dynamic shared memory: staged p, then the own-row state (SM only)
+    float4 *sp = sm_dyn;
+    float4 *sdx = sp + halo_cap;
+    float4 *sr = sdx + rows_cap;
+    float4 *sq = sr + rows_cap;
+    float4 *sm0 = sq + rows_cap;
+    float2 *sm1 = reinterpret_cast<float2 *>(sm0 + rows_cap);
+
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const int nch = (w.row1 - w.row0 + 31) / 32;
-    const int nun = (w.row1 - w.row0 + kRedRows - 1) / kRedRows;
-    const int unit0 = w.row0 / kRedRows;
-    // Unit partials: fixed-order FP64 sums of the unit's 32-row chunk sums,
-    // written to d.part[q*nt + unit]; the units are the same whatever the
-    // team size, so an instance's sums do not depend on its neighbours.
-    auto publish = [&](int nq) {
+    const int nrow = w.row1 - w.row0;
+    const int nch = (nrow + 31) / 32;
+    const bool staged = w.halo0 >= 0;
+    if (SM)
+        for (int i = tid; i < nrow; i += kPBlock)
+        {
+            const int row = w.row0 + i;
+            sdx[i] = d.dx[row];
+            sr[i] = d.r[row];
+            sm0[i] = d.M0[row];
+            sm1[i] = d.M1[row];
+        }
+    if (tid == 0)
+    {
+        s_rho = __ldcg(&st->rho);
+        s_rr = __ldcg(&st->rr);
+        s_pq = s_rho;
+        s_beta = 0.0;
+        s_alpha = 0.0;
+        bc_bf = 0.f;
+    }
+    int it = 0, status = 0;
+
+    // Team sum of NQ quantities (q0.. in the accumulator): every warp's
+    // fixed-point partials go to the block (shared atomics), the block's to
+    // the team buffer (one global atomic per limb), then the team barrier.
+    // Returns false when the barrier wait gave up.
+    auto team_sum = [&](auto &wfx, int nq, int q0, int bq) -> bool {
+        if (tid < 4)
+            reinterpret_cast<unsigned long long *>(blk_acc)[tid] = 0ull;
+        if (tid < 2)
+            blk_chk[tid] = 0.f;
         __syncthreads();
-        for (int u = tid; u < nun; u += kPBlock)
+        if (lane == 0)
             for (int q = 0; q < nq; q++)
             {
-                double v = 0.0;
-                for (int c = CPU * u; c < min(CPU * u + CPU, nch); c++)
-                    v += csum[q][c];
-                d.part[q * nt + unit0 + u] = v;
+                atomicAdd(&blk_acc[q][0], (unsigned long long)wfx.H[q]);
+                atomicAdd(&blk_acc[q][1], wfx.L[q]);
+                atomicAdd(&blk_chk[q], wfx.chk[q]);
             }
-    };
-    // Team total of nq quantities: warp 0 sums the nu unit partials (FP64,
-    // fixed lane assignment and tree), the block reads it from shared memory.
-    // The caller's warp 0 then turns the totals into the PCG scalars (one
-    // thread), which the block reads back from shared memory.
-    auto team_total = [&](auto nq_tag, double *out) {
-        constexpr int NQ = decltype(nq_tag)::value;
-        if (warp == 0)
+        __syncthreads();
+        if (tid < nq)
         {
-            double a[NQ][2];
-#pragma unroll
-            for (int q = 0; q < NQ; q++)
-                a[q][0] = a[q][1] = 0.0;
-            int k = lane;
-            for (; k + 32 < nu; k += 64)
-#pragma unroll
-                for (int q = 0; q < NQ; q++)
-                {
-                    a[q][0] += __ldcg(d.part + q * nt + k);
-                    a[q][1] += __ldcg(d.part + q * nt + k + 32);
-                }
-            if (k < nu)
-#pragma unroll
-                for (int q = 0; q < NQ; q++)
-                    a[q][0] += __ldcg(d.part + q * nt + k);
-#pragma unroll
-            for (int q = 0; q < NQ; q++)
-            {
-                double v = a[q][0] + a[q][1];
-#pragma unroll
-                for (int o = 16; o > 0; o >>= 1)
-                    v += __shfl_xor_sync(0xffffffffu, v, o);
-                out[q] = v;
-            }
+            atomicAdd(&st->acc[bq][q0 + tid][0], blk_acc[tid][0]);
+            atomicAdd(&st->acc[bq][q0 + tid][1], blk_acc[tid][1]);
+            atomicAdd(&st->acc_chk[bq][q0 + tid], blk_chk[tid]);
         }
+        return team_barrier(st, w.nblk);
     };
+    // Reads a team sum after the barrier; flags a fixed-point overflow when it
+    // disagrees with the FP32 magnitude check.
+    auto team_value = [&](int q, int bq, int s, int *bad) -> double {
+        const double v = fx_value(__ldcg(&st->acc[bq][q][0]), __ldcg(&st->acc[bq][q][1]), s);
+        const float chk = __ldcg(&st->acc_chk[bq][q]);
+        if (!isfinite(chk) || fabs(v - double(chk)) > 1e-3 * fabs(double(chk)) + 1e-30)
+            *bad = 1;
+        return v;
+    };
+
     for (;;)
     {
+        const int bq = it % 3;
         const float4 *pold = (it & 1) ? d.p1 : d.p0;
         float4 *pnew = (it & 1) ? d.p0 : d.p1;
-        const float bf = float(beta);
-        const bool first = (beta == 0.0);
+        __syncthreads();
+        const float bf = bc_bf;
+        const bool first = (bf == 0.f);
+        if (tid == 0)
+        {
+            // scales of this iteration, identical in every block of the team
+            bc_s[0] = fx_scale(s_pq);
+            bc_s[1] = fx_scale(s_rho);
+            bc_s[2] = fx_scale(s_rr);
+            if (w.rank == 0)
+            {
+                // the buffer of iteration it+1 was last read in iteration it-2
+                const int nb = (it + 1) % 3;
+                for (int q = 0; q < 3; q++)
+                {
+                    st->acc[nb][q][0] = 0ull;
+                    st->acc[nb][q][1] = 0ull;
+                    st->acc_chk[nb][q] = 0.f;
+                }
+            }
+        }
         // ---- p = z + beta p_old over the staged range
         if (staged)
-        {
             for (int i = tid; i < w.halo1 - w.halo0; i += kPBlock)
             {
                 const int c = w.halo0 + i;
@@ -824,14 +953,17 @@ __global__ void __launch_bounds__(kPBlock, 1)
                 }
                 sp[i] = pn;
             }
-            __syncthreads();
-        }
-        // ---- q = A p on own rows, p.q per 32-row chunk
+        __syncthreads();
+        const int s0q = bc_s[0], s1q = bc_s[1], s2q = bc_s[2];
+        // ---- q = A p on own rows; p.q per 32-row chunk
+        WarpFx<1> f1;
+        f1.clear();
         for (int ch = warp; ch < nch; ch += NW)
         {
-            const int row = w.row0 + ch * 32 + lane;
+            const int li = ch * 32 + lane;
+            const int row = w.row0 + li;
             float part = 0.f;
-            if (row < w.row1)
+            if (li < nrow)
             {
                 float3 pv;
                 if (staged)
@@ -850,14 +982,14 @@ __global__ void __launch_bounds__(kPBlock, 1)
                 pnew[row] = f4(pv);
                 const int len = __ldg(d.rowinfo + row) & 255;
                 float3 q = make_float3(0, 0, 0);
-                // four slots at a time: their loads are all in flight together
-                for (int s0 = 0; s0 < len; s0 += 4)
+                // kSlotUnroll slots at a time: their loads are all in flight together
+                for (int s0 = 0; s0 < len; s0 += kSlotUnroll)
                 {
-                    int cc[4];
-                    float4 a0[4];
-                    float2 a1[4];
+                    int cc[kSlotUnroll];
+                    float4 a0[kSlotUnroll];
+                    float2 a1[kSlotUnroll];
 #pragma unroll
-                    for (int k = 0; k < 4; k++)
+                    for (int k = 0; k < kSlotUnroll; k++)
                         if (s0 + k < len)
                         {
                             const size_t o = size_t(s0 + k) * d.stride + row;
@@ -866,7 +998,7 @@ __global__ void __launch_bounds__(kPBlock, 1)
                             a1[k] = __ldg(d.A1 + o);
                         }
 #pragma unroll
-                    for (int k = 0; k < 4; k++)
+                    for (int k = 0; k < kSlotUnroll; k++)
                         if (s0 + k < len)
                         {
                             const int c = cc[k];
@@ -892,63 +1024,85 @@ __global__ void __launch_bounds__(kPBlock, 1)
                             q = q + symv(A, pc);
                         }
                 }
-                d.q[row] = f4(q);
+                if (SM)
+                    sq[li] = f4(q);
+                else
+                    d.q[row] = f4(q);
                 part = fdot(pv, q);
             }
             part = warp_sum(part);
             if (lane == 0)
-                csum[0][ch] = double(part);
+                f1.add(0, part, s0q);
         }
-        publish(1);
-        if (!team_barrier(st, w.nblk))
+        if (!team_sum(f1, 1, 0, bq))
         {
             status = 9; // CLOTH_ERR_TIMEOUT
             break;
         }
+        if (tid == 0)
         {
-            double t1[1];
-            team_total(std::integral_constant<int, 1>(), t1);
-            if (tid == 0)
-            {
-                pq = t1[0];
-                int stop = 0;
-                if (!isfinite(pq))
-                    stop = 6;
-                else if (pq == 0.0)
-                    stop = 7;
-                else
-                    alpha = rho / pq;
-                bc_alpha = alpha;
-                bc_stop = stop;
-            }
-            __syncthreads();
-            if (bc_stop)
-            {
-                status = bc_stop;
-                break;
-            }
-            alpha = bc_alpha;
+            int bad = 0;
+            const double pq = team_value(0, bq, s0q, &bad);
+            s_pq = pq;
+            int stop = 0;
+            if (bad || !isfinite(pq))
+                stop = 6;
+            else if (pq == 0.0)
+                stop = 7;
+            else
+                s_alpha = s_rho / pq;
+            bc_af = float(s_alpha);
+            bc_stop = stop;
         }
-        const float af = float(alpha);
+        __syncthreads();
+        if (bc_stop)
+        {
+            status = bc_stop;
+            break;
+        }
+        const float af = bc_af;
         // ---- dx += alpha p, r -= alpha q, z = M^-1 r; r.z and r.r per chunk
+        WarpFx<2> f2;
+        f2.clear();
         for (int ch = warp; ch < nch; ch += NW)
         {
-            const int row = w.row0 + ch * 32 + lane;
+            const int li = ch * 32 + lane;
+            const int row = w.row0 + li;
             float pr = 0.f, prr = 0.f;
-            if (row < w.row1)
+            if (li < nrow)
             {
                 const float3 p = staged ? xyz(sp[row - w.halo0]) : xyz(pnew[row]);
-                const float3 qv = xyz(d.q[row]);
-                float3 x = xyz(d.dx[row]);
-                float3 r = xyz(d.r[row]);
+                const float3 qv = SM ? xyz(sq[li]) : xyz(d.q[row]);
+                float3 x = SM ? xyz(sdx[li]) : xyz(d.dx[row]);
+                float3 r = SM ? xyz(sr[li]) : xyz(d.r[row]);
                 x = make_float3(fmaf(af, p.x, x.x), fmaf(af, p.y, x.y), fmaf(af, p.z, x.z));
                 r = make_float3(fmaf(-af, qv.x, r.x), fmaf(-af, qv.y, r.y),
                                 fmaf(-af, qv.z, r.z));
                 float M[6];
-                load_sym(d.M0, d.M1, row, M);
+                if (SM)
+                {
+                    const float4 u = sm0[li];
+                    const float2 v = sm1[li];
+                    M[0] = u.x;
+                    M[1] = u.y;
+                    M[2] = u.z;
+                    M[3] = u.w;
+                    M[4] = v.x;
+                    M[5] = v.y;
+                }
+                else
+                    load_sym(d.M0, d.M1, row, M);
                 const float3 z = symv(M, r);
-                d.dx[row] = f4(x);
-                d.r[row] = f4(r);
+                if (SM)
+                {
+                    sdx[li] = f4(x);
+                    sr[li] = f4(r);
+                }
+                else
+                {
+                    d.dx[row] = f4(x);
+                    d.r[row] = f4(r);
+                }
                 d.z[row] = f4(z);
                 pr = fdot(r, z);
                 prr = fdot(r, r);
@@ -957,61 +1111,81 @@ __global__ void __launch_bounds__(kPBlock, 1)
             prr = warp_sum(prr);
             if (lane == 0)
             {
-                csum[0][ch] = double(pr);
-                csum[1][ch] = double(prr);
+                f2.add(0, pr, s1q);
+                f2.add(1, prr, s2q);
             }
         }
-        publish(2);
-        if (!team_barrier(st, w.nblk))
+        if (!team_sum(f2, 2, 1, bq))
         {
             status = 9;
             break;
         }
+        it++;
+        if (tid == 0)
         {
-            double t2[2];
-            team_total(std::integral_constant<int, 2>(), t2);
-            it++;
-            if (tid == 0)
+            int bad = 0;
+            const double rho_new = team_value(1, bq, s1q, &bad);
+            const double rr = team_value(2, bq, s2q, &bad);
+            s_beta = (s_rho == 0.0) ? 0.0 : rho_new / s_rho;
+            s_rho = rho_new;
+            s_rr = rr;
+            int stop = 0; // 0 go on, 1 converged, else a status code
+            if (bad || !isfinite(rho_new) || !isfinite(rr))
+                stop = 6;
+            else
             {
-                const double rho_new = t2[0];
-                rr = t2[1];
-                beta = (rho == 0.0) ? 0.0 : rho_new / rho;
-                rho = rho_new;
-                int stop = 0; // 0 go on, 1 converged, else a status code
-                if (!isfinite(rho_new) || !isfinite(rr))
-                    stop = 6;
-                else
-                {
-                    const bool check = ((it - 1) % d.check_every) == 0 || it >= d.max_iters;
-                    if (check && test_converged(d, *st, rr))
-                        stop = 1;
-                    else if (it >= d.max_iters)
-                        stop = 8;
-                }
-                bc_beta = beta;
-                bc_stop = stop;
+                const bool check = ((it - 1) % d.check_every) == 0 || it >= d.max_iters;
+                if (check && test_converged(d, *st, rr))
+                    stop = 1;
+                else if (it >= d.max_iters)
+                    stop = 8;
             }
-            __syncthreads();
-            beta = bc_beta;
-            const int stop = bc_stop;
-            if (stop)
-            {
-                status = (stop == 1) ? 0 : stop;
-                break;
-            }
+            bc_bf = float(s_beta);
+            bc_stop = stop;
+        }
+        __syncthreads();
+        const int stop = bc_stop;
+        if (stop)
+        {
+            status = (stop == 1) ? 0 : stop;
+            break;
+        }
+    }
+    if (SM)
+    {
+        __syncthreads();
+        for (int i = tid; i < nrow; i += kPBlock)
+        {
+            const int row = w.row0 + i;
+            d.dx[row] = sdx[i];
+            d.r[row] = sr[i];
         }
     }
     if (w.rank == 0 && tid == 0)
     {
         st->iter = it;
         st->status = status;
-        st->rho = rho;
-        st->rr = rr;
-        st->pq = pq;
-        st->alpha = alpha;
-        st->beta = beta;
+        st->rho = s_rho;
+        st->rr = s_rr;
+        st->pq = s_pq;
+        st->alpha = s_alpha;
+        st->beta = s_beta;
         st->active = 0;
     }
+}
+
+__global__ void __launch_bounds__(kPBlock, 1)
+    k_pcg_persistent_sm(InstDesc *const *descs, const TeamBlock *work, int halo_cap,
+                        int rows_cap)
+{
+    pcg_persistent_body<true>(descs, work, halo_cap, rows_cap);
+}
+
+__global__ void __launch_bounds__(kPBlock, 1)
+    k_pcg_persistent_gm(InstDesc *const *descs, const TeamBlock *work, int halo_cap,
+                        int rows_cap)
+{
+    pcg_persistent_body<false>(descs, work, halo_cap, rows_cap);
 }
 
 // ------------------------------------------------------------------ advance
