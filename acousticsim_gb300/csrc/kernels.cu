@@ -729,6 +729,37 @@ __device__ __forceinline__ bool team_barrier(InstState *st, int nblk)
 
 __device__ __forceinline__ float4 ldcg4(const float4 *p) { return __ldcg(p); }
 
+// Loads of the matrix carry an L2 evict_last policy: A is re-read every PCG
+// iteration and should outlive the streamed vectors in L2.
+__device__ __forceinline__ unsigned long long l2_keep_policy()
+{
+    unsigned long long p;
+    asm("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
+    return p;
+}
+__device__ __forceinline__ float4 ld_keep(const float4 *ptr, unsigned long long pol)
+{
+    float4 v;
+    asm("ld.global.nc.L2::cache_hint.v4.f32 {%0, %1, %2, %3}, [%4], %5;"
+        : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
+        : "l"(ptr), "l"(pol));
+    return v;
+}
+__device__ __forceinline__ float2 ld_keep(const float2 *ptr, unsigned long long pol)
+{
+    float2 v;
+    asm("ld.global.nc.L2::cache_hint.v2.f32 {%0, %1}, [%2], %3;"
+        : "=f"(v.x), "=f"(v.y)
+        : "l"(ptr), "l"(pol));
+    return v;
+}
+__device__ __forceinline__ int ld_keep(const int *ptr, unsigned long long pol)
+{
+    int v;
+    asm("ld.global.nc.L2::cache_hint.b32 %0, [%1], %2;" : "=r"(v) : "l"(ptr), "l"(pol));
+    return v;
+}
+
 } // namespace
 
 namespace {
@@ -853,6 +884,7 @@ __device__ __forceinline__ void pcg_persistent_body(InstDesc *const *descs,
     float2 *sm1 = reinterpret_cast<float2 *>(sm0 + rows_cap);
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const unsigned long long keep = l2_keep_policy();
     const int nrow = w.row1 - w.row0;
     const int nch = (nrow + 31) / 32;
     const bool staged = w.halo0 >= 0;
@@ -980,7 +1012,7 @@ __device__ __forceinline__ void pcg_persistent_body(InstDesc *const *descs,
                     }
                 }
                 pnew[row] = f4(pv);
-                const int len = __ldg(d.rowinfo + row) & 255;
+                const int len = ld_keep(d.rowinfo + row, keep) & 255;
                 float3 q = make_float3(0, 0, 0);
                 // kSlotUnroll slots at a time: their loads are all in flight together
                 for (int s0 = 0; s0 < len; s0 += kSlotUnroll)
@@ -993,9 +1025,9 @@ __device__ __forceinline__ void pcg_persistent_body(InstDesc *const *descs,
                         if (s0 + k < len)
                         {
                             const size_t o = size_t(s0 + k) * d.stride + row;
-                            cc[k] = __ldg(d.col + o);
-                            a0[k] = __ldg(d.A0 + o);
-                            a1[k] = __ldg(d.A1 + o);
+                            cc[k] = ld_keep(d.col + o, keep);
+                            a0[k] = ld_keep(d.A0 + o, keep);
+                            a1[k] = ld_keep(d.A1 + o, keep);
                         }
 #pragma unroll
                     for (int k = 0; k < kSlotUnroll; k++)
