@@ -682,26 +682,25 @@ __global__ void __launch_bounds__(kTile) k_update(InstDesc *const *descs,
 // kernel (z, p, partials) is read through L2 (ld.global.cg); A is read-only.
 namespace {
 
-// Barrier of the nblk blocks of one team. Returns false when the bounded
-// wait gave up (then the team's error flag is set and the solve stops).
+// Barrier of the nblk blocks of one team (the cooperative-groups grid-sync
+// pattern: one thread per block fences, arrives and waits; the CTA barriers
+// around it carry the block's other writes). Returns false when the bounded
+// wait gave up; the team's error flag is set then and the solve stops.
 __device__ __forceinline__ bool team_barrier(InstState *st, int nblk)
 {
     __shared__ int ok;
-    // every thread's global writes (vectors, partials) are made visible
-    // device-wide before the block arrives
-    __threadfence();
     __syncthreads();
     if (threadIdx.x == 0)
     {
         ok = 1;
         if (nblk > 1)
         {
-            __threadfence();
             volatile unsigned *gen = &st->bar_gen;
             const unsigned g = *gen;
+            __threadfence();
             if (atomicAdd(&st->bar_count, 1u) == unsigned(nblk - 1))
             {
-                atomicExch(&st->bar_count, 0u);
+                st->bar_count = 0u;
                 __threadfence();
                 atomicAdd(&st->bar_gen, 1u);
             }
@@ -713,14 +712,13 @@ __device__ __forceinline__ bool team_barrier(InstState *st, int nblk)
                     if (++n > kSpinLimit)
                     {
                         atomicExch(&st->bar_err, 1);
+                        ok = 0;
                         break;
                     }
-                    __nanosleep(64);
+                    __nanosleep(32);
                 }
             }
             __threadfence();
-            if (*(volatile int *)&st->bar_err)
-                ok = 0;
         }
     }
     __syncthreads();
@@ -815,10 +813,16 @@ __device__ __forceinline__ int fx_scale(double est)
     return max(-900, min(900, s));
 }
 
+// 2^e for |e| < 1000, built from the exponent field
+__device__ __forceinline__ double pow2(int e)
+{
+    return __longlong_as_double((long long)(1023 + e) << 52);
+}
+
 __device__ __forceinline__ double fx_value(unsigned long long H, unsigned long long L,
                                            int s)
 {
-    return ldexp(double((long long)H), 32 - s) + ldexp(double(L), -s);
+    return double((long long)H) * pow2(32 - s) + double(L) * pow2(-s);
 }
 
 // Per-warp fixed-point accumulator of NQ chunk sums (held by lane 0).
@@ -860,8 +864,8 @@ __device__ __forceinline__ void pcg_persistent_body(InstDesc *const *descs,
     constexpr int NW = kPBlock / 32;
     extern __shared__ float4 sm_dyn[];
     __shared__ InstDesc d;
-    __shared__ unsigned long long blk_acc[2][2];
-    __shared__ float blk_chk[2];
+    __shared__ unsigned long long wsum_h[2][kPBlock / 32], wsum_l[2][kPBlock / 32];
+    __shared__ float wsum_c[2][kPBlock / 32];
     // FP64 PCG scalars: owned by thread 0, the block reads the FP32 copies
     __shared__ double s_rho, s_beta, s_alpha, s_pq, s_rr;
     __shared__ float bc_af, bc_bf;
@@ -908,30 +912,34 @@ __device__ __forceinline__ void pcg_persistent_body(InstDesc *const *descs,
     }
     int it = 0, status = 0;
 
-    // Team sum of NQ quantities (q0.. in the accumulator): every warp's
-    // fixed-point partials go to the block (shared atomics), the block's to
-    // the team buffer (one global atomic per limb), then the team barrier.
-    // Returns false when the barrier wait gave up.
+    // Team sum of NQ quantities (q0.. in the accumulator): lane 0 of every
+    // warp leaves its fixed-point partials in shared memory, thread 0 folds
+    // them (exact integer adds) and sends one reduction per limb to the team
+    // buffer, then the team barrier. Returns false when the barrier gave up.
     auto team_sum = [&](auto &wfx, int nq, int q0, int bq) -> bool {
-        if (tid < 4)
-            reinterpret_cast<unsigned long long *>(blk_acc)[tid] = 0ull;
-        if (tid < 2)
-            blk_chk[tid] = 0.f;
-        __syncthreads();
         if (lane == 0)
             for (int q = 0; q < nq; q++)
             {
-                atomicAdd(&blk_acc[q][0], (unsigned long long)wfx.H[q]);
-                atomicAdd(&blk_acc[q][1], wfx.L[q]);
-                atomicAdd(&blk_chk[q], wfx.chk[q]);
+                wsum_h[q][warp] = (unsigned long long)wfx.H[q];
+                wsum_l[q][warp] = wfx.L[q];
+                wsum_c[q][warp] = wfx.chk[q];
             }
         __syncthreads();
-        if (tid < nq)
-        {
-            atomicAdd(&st->acc[bq][q0 + tid][0], blk_acc[tid][0]);
-            atomicAdd(&st->acc[bq][q0 + tid][1], blk_acc[tid][1]);
-            atomicAdd(&st->acc_chk[bq][q0 + tid], blk_chk[tid]);
-        }
+        if (tid == 0)
+            for (int q = 0; q < nq; q++)
+            {
+                unsigned long long h = 0ull, l = 0ull;
+                float c = 0.f;
+                for (int j = 0; j < NW; j++)
+                {
+                    h += wsum_h[q][j];
+                    l += wsum_l[q][j];
+                    c += wsum_c[q][j];
+                }
+                atomicAdd(&st->acc[bq][q0 + q][0], h);
+                atomicAdd(&st->acc[bq][q0 + q][1], l);
+                atomicAdd(&st->acc_chk[bq][q0 + q], c);
+            }
         return team_barrier(st, w.nblk);
     };
     // Reads a team sum after the barrier; flags a fixed-point overflow when it
