@@ -682,10 +682,28 @@ __global__ void __launch_bounds__(kTile) k_update(InstDesc *const *descs,
 // kernel (z, p, partials) is read through L2 (ld.global.cg); A is read-only.
 namespace {
 
-// Barrier of the nblk blocks of one team (the cooperative-groups grid-sync
-// pattern: one thread per block fences, arrives and waits; the CTA barriers
-// around it carry the block's other writes). Returns false when the bounded
-// wait gave up; the team's error flag is set then and the solve stops.
+// Barrier of the nblk blocks of one team: one thread per block arrives with
+// an acquire-release atomic (its release covers the writes the block's CTA
+// barrier ordered before it) and polls the generation word with acquire
+// loads. Returns false when the bounded wait gave up; the team's error flag
+// is set then and the solve stops.
+__device__ __forceinline__ unsigned atom_add_acq_rel(unsigned *a, unsigned v)
+{
+    unsigned old;
+    asm volatile("atom.add.acq_rel.gpu.u32 %0, [%1], %2;" : "=r"(old) : "l"(a), "r"(v) : "memory");
+    return old;
+}
+__device__ __forceinline__ void red_add_release(unsigned *a, unsigned v)
+{
+    asm volatile("red.add.release.gpu.u32 [%0], %1;" ::"l"(a), "r"(v) : "memory");
+}
+__device__ __forceinline__ unsigned ld_acquire(const unsigned *a)
+{
+    unsigned v;
+    asm volatile("ld.acquire.gpu.u32 %0, [%1];" : "=r"(v) : "l"(a) : "memory");
+    return v;
+}
+
 __device__ __forceinline__ bool team_barrier(InstState *st, int nblk)
 {
     __shared__ int ok;
@@ -695,19 +713,16 @@ __device__ __forceinline__ bool team_barrier(InstState *st, int nblk)
         ok = 1;
         if (nblk > 1)
         {
-            volatile unsigned *gen = &st->bar_gen;
-            const unsigned g = *gen;
-            __threadfence();
-            if (atomicAdd(&st->bar_count, 1u) == unsigned(nblk - 1))
+            const unsigned g = ld_acquire(&st->bar_gen);
+            if (atom_add_acq_rel(&st->bar_count, 1u) == unsigned(nblk - 1))
             {
                 st->bar_count = 0u;
-                __threadfence();
-                atomicAdd(&st->bar_gen, 1u);
+                red_add_release(&st->bar_gen, 1u);
             }
             else
             {
                 unsigned n = 0;
-                while (*gen == g)
+                while (ld_acquire(&st->bar_gen) == g)
                 {
                     if (++n > kSpinLimit)
                     {
@@ -715,10 +730,10 @@ __device__ __forceinline__ bool team_barrier(InstState *st, int nblk)
                         ok = 0;
                         break;
                     }
-                    __nanosleep(32);
+                    if (n > 256)
+                        __nanosleep(32);
                 }
             }
-            __threadfence();
         }
     }
     __syncthreads();
