@@ -108,6 +108,9 @@ SIGNATURES = {
     "cloth_export_tables": (C.c_int, [P, PI, PF, PF, PF, PI]),
     "cloth_batch_step": (C.c_int, [P, C.POINTER(P), C.c_int, C.c_double,
                                    C.POINTER(SolveParams), C.POINTER(SolveStats)]),
+    "cloth_pcg_solve_ell32_noalloc": (C.c_int, [C.c_int, P, P, P, P, P, C.c_int,
+                                                C.POINTER(SolveParams), C.POINTER(SolveStats),
+                                                P]),
 }
 
 

@@ -988,6 +988,11 @@ bool valid_params(const cloth_solve_params *p)
 
 } // namespace
 
+namespace cloth {
+// Lets other translation units of the library report through cloth_last_error().
+void set_last_error(const std::string &msg) { g_err = msg; }
+} // namespace cloth
+
 // ====================================================================== ABI
 extern "C" {
 

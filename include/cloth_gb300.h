@@ -235,6 +235,30 @@ int cloth_export_tables(const cloth_t *cloth, int *stencil, float *coef,
 int cloth_batch_step(cloth_ctx *ctx, cloth_t *const *cloths, int n, double dt,
                      const cloth_solve_params *params, cloth_solve_stats *stats);
 
+/* ---------------------------------------------------------------- no allocation */
+/* Allocation-free PCG solve. No counterpart in the reference: this entry point
+ * exists for callers that cannot allocate device memory when they solve - a
+ * render or physics loop that must not stall on cudaMalloc or fail for lack of
+ * memory in the middle of a frame, or a host whose device memory belongs to
+ * another allocator or budget. It solves A x = b (block-Jacobi PCG, FP32
+ * vectors, FP64 reductions) on a system the caller has assembled in the
+ * reference's layout: ell_dev nv*32 vertex ids (-1 padded, sorted, as
+ * mELLVidToGlobalVid), A_dev nv*32 3x3 blocks of 9 floats, column-major
+ * (tCudaMatrix3f), b_dev and x_dev nv*3 floats; x_dev is the start and the
+ * result. Rows and columns of the fixed_dev vertices are left out, and their
+ * x entries are set to zero. All pointers are device pointers on the current
+ * device; the work runs on `stream` (a cudaStream_t, NULL = default stream).
+ * Nothing is allocated: the solver's scratch (4 MiB) is a static array that
+ * every GPU loading this library holds until the process exits, which limits
+ * nv to 32768; larger systems are rejected with CLOTH_ERR_INVALID. The first
+ * call on a device looks up that array's device address, so make it before
+ * any stream capture. Every call reuses the same array: calls that may
+ * overlap on the GPU race and must be serialised by the caller. */
+int cloth_pcg_solve_ell32_noalloc(int nv, const int *ell_dev, const float *A_dev,
+                                  const float *b_dev, float *x_dev, const int *fixed_dev,
+                                  int nfixed, const cloth_solve_params *params,
+                                  cloth_solve_stats *stats, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
