@@ -392,13 +392,39 @@ def run_ours(args, rank, world, local, pg):
     ctx.close()
 
 
+def run_profile_case(args):
+    """Small case for ncu: one step of the 512x512 workload with the PCG capped
+    at --profile-iters iterations, kernels launched from the host."""
+    from acousticsim_gb300 import BaraffClothGpu, ClothContext, params
+    from acousticsim_gb300 import build as b
+    b.build_all()
+    ctx = ClothContext(0)
+    if args.solver:
+        ctx.set_solver(args.solver)
+    cloth = BaraffClothGpu(ctx, workload_conf())
+    x0, xp0 = initial_state(cloth.GetInitPos(), 1234)
+    cloth.SetPos(x0)
+    cloth.SetPrePos(xp0)
+    ctx.set_profiling(True)
+    st = cloth.UpdatePos(0.0, params(max_iters=args.profile_iters, rel_tol=1e-12))
+    print(json.dumps({"profile_case": st, "phases": ctx.profile()}))
+    cloth.close()
+    ctx.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--profile-iters", type=int, default=0,
+                    help="run only the small ncu case: one step, PCG capped at N iterations")
+    ap.add_argument("--solver", choices=["persistent", "graph_loop"], default=None)
     args = ap.parse_args()
+    if args.profile_iters > 0:
+        run_profile_case(args)
+        return
     rank, world, local, pg = dist_init(args.gpus)
     if args.impl == "reference":
         run_reference(args, rank, world, pg)
