@@ -22,7 +22,7 @@ PHASE_NAMES = ["pins", "tri_assemble", "row_assemble", "spmv_dot", "update_dot",
 ELL_REF_WIDTH = 32
 SOLVER_PERSISTENT = 0
 SOLVER_GRAPH_LOOP = 1
-SOLVER_NAMES = {0: "persistent", 1: "graph_loop"}
+SOLVER_NAMES = {0: "persistent", 1: "graph_loop", -1: "plain"}
 
 
 class GridDesc(C.Structure):
@@ -106,6 +106,7 @@ SIGNATURES = {
     "cloth_export_system": (C.c_int, [P, PI, PF, PF, PF, PF]),
     "cloth_export_triangles": (C.c_int, [P, PF, PF]),
     "cloth_export_tables": (C.c_int, [P, PI, PF, PF, PF, PI]),
+    "cloth_step_plain": (C.c_int, [P, C.c_double, C.POINTER(SolveParams), C.POINTER(SolveStats)]),
     "cloth_batch_step": (C.c_int, [P, C.POINTER(P), C.c_int, C.c_double,
                                    C.POINTER(SolveParams), C.POINTER(SolveStats)]),
     "cloth_pcg_solve_ell32_noalloc": (C.c_int, [C.c_int, P, P, P, P, P, C.c_int,

@@ -246,6 +246,13 @@ class BaraffClothGpu:
 
     Update = UpdatePos
 
+    def UpdatePosPlain(self, dt: float = 0.0, params: N.SolveParams | None = None) -> dict:
+        """One step through the reference-structured baseline (cloth_step_plain)."""
+        st = N.SolveStats()
+        N.call("cloth_step_plain", self._h, float(dt),
+               C.byref(params) if params is not None else None, C.byref(st))
+        return st.as_dict()
+
     def step_async(self, dt: float = 0.0, params: N.SolveParams | None = None) -> None:
         N.call("cloth_step", self._h, float(dt), C.byref(params) if params is not None else None,
                None)

@@ -25,6 +25,22 @@ __global__ void k_update(InstDesc *const *descs, const Tile *tiles, BatchCtl *ct
 __global__ void k_advance(InstDesc *const *descs, const Tile *tiles,
                           const BatchCtl *ctl);
 __global__ void k_sync_x32(InstDesc *d);
+struct PlainState;
+struct PlainInit
+{
+    int nv, nt;
+    const int *ell_host;
+    const float *kb_scalar_host;
+    const float *mass_host, *grav_host;
+    const int4 *tri_dev;
+    const float4 *coef_dev;
+};
+int plain_create(const PlainInit &in, PlainState **out);
+void plain_free(PlainState *p);
+size_t plain_bytes(const PlainState *p);
+int plain_step(PlainState *p, double *x, double *xp, const int *pins, const float *pin_tgt,
+               int npins, float dt, float kw, float kwe, float kb, int fix_fv, float ra,
+               float rb, const cloth_solve_params *prm, cloth_solve_stats *stats);
 __global__ void k_pcg_persistent_sm(InstDesc *const *descs, const TeamBlock *work,
                                     int halo_cap, int rows_cap);
 __global__ void k_pcg_persistent_gm(InstDesc *const *descs, const TeamBlock *work,
@@ -119,6 +135,15 @@ struct cloth_s
     bool assembled = false;
     double dt_set = -1.0;
     std::unique_ptr<Batch> self;
+    // plain (reference-structured) path: host positions and its device state
+    cloth::PlainState *plain = nullptr;
+    std::vector<double> plain_x, plain_xp;
+    bool plain_host_valid = false;
+    ~cloth_s()
+    {
+        if (plain)
+            cloth::plain_free(plain);
+    }
 };
 
 namespace {
@@ -945,6 +970,8 @@ int run_step(Batch *b, double dt, const cloth_solve_params *params,
              cloth_solve_stats *stats)
 {
     cloth_ctx *ctx = b->ctx;
+    for (auto *c : b->members)
+        c->plain_host_valid = false;
     int rc = prepare(b->members, dt, params);
     if (rc != CLOTH_OK)
         return rc;
@@ -1449,6 +1476,7 @@ static int set_state(cloth_t *c, const double *x, int nv, bool pre)
         k_sync_x32<<<std::min(1024, (nv + 255) / 256), 256, 0, s>>>(c->d_desc);
     CK(cudaGetLastError());
     c->assembled = false;
+    c->plain_host_valid = false;
     return CLOTH_OK;
 }
 
@@ -1761,6 +1789,76 @@ int cloth_export_tables(const cloth_t *c, int *stencil, float *coef, float *area
             mass[v] = float(t.mass[v]);
     if (tri_slot)
         std::memcpy(tri_slot, t.tri_slot.data(), t.tri_slot.size() * sizeof(int));
+    return CLOTH_OK;
+}
+
+int cloth_step_plain(cloth_t *c, double dt, const cloth_solve_params *params,
+                     cloth_solve_stats *stats)
+{
+    if (!c || !valid_params(params) || (params && params->max_iters > 100000))
+        return fail(CLOTH_ERR_INVALID, "cloth_step_plain: bad argument");
+    std::lock_guard<std::recursive_mutex> lk(c->ctx->mu);
+    CK(cudaSetDevice(c->ctx->device));
+    CK(cudaStreamSynchronize(c->ctx->stream));
+    const Tables &t = c->tab;
+    const int n = t.nv, R = CLOTH_ELL_REF_WIDTH;
+    if (!c->plain)
+    {
+        std::vector<int> ell(size_t(n) * R, -1);
+        std::vector<float> kb(size_t(n) * R, 0.f), mass(n), grav(n);
+        for (int v = 0; v < n; v++)
+        {
+            for (int s = 0; s < t.rowptr[v + 1] - t.rowptr[v]; s++)
+            {
+                ell[size_t(v) * R + s] = t.cols[size_t(t.rowptr[v]) + s];
+                kb[size_t(v) * R + s] = t.kbend[size_t(t.rowptr[v]) + s];
+            }
+            mass[v] = float(t.mass[v]);
+            grav[v] = float(c->mat.gravity * t.mass[v]);
+        }
+        PlainInit in{n, t.nt, ell.data(), kb.data(), mass.data(), grav.data(), c->h.tri, c->h.tcoef};
+        int rc = plain_create(in, &c->plain);
+        if (rc != CLOTH_OK)
+            return rc;
+        c->ctx->bytes += plain_bytes(c->plain);
+    }
+    if (!c->plain_host_valid)
+    {
+        c->plain_x.resize(size_t(n) * 3);
+        c->plain_xp.resize(size_t(n) * 3);
+        CK(cudaMemcpy(c->plain_x.data(), c->h.x64, c->plain_x.size() * 8, cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(c->plain_xp.data(), c->h.xp64, c->plain_xp.size() * 8, cudaMemcpyDeviceToHost));
+        c->plain_host_valid = true;
+    }
+    std::vector<int> pins(c->static_pins);
+    std::vector<float> tgt;
+    for (int v : c->static_pins)
+        for (int k = 0; k < 4; k++)
+            tgt.push_back(k < 3 ? float(c->mesh.pos[size_t(v) * 3 + k]) : 0.f);
+    if (c->drag_vid >= 0)
+    {
+        pins.push_back(c->drag_vid);
+        for (int k = 0; k < 4; k++)
+            tgt.push_back(k < 3 ? c->drag_tgt[k] : 0.f);
+    }
+    if (!(dt > 0))
+        dt = c->mat.default_timestep;
+    int rc = plain_step(c->plain, c->plain_x.data(), c->plain_xp.data(), pins.data(), tgt.data(),
+                        int(pins.size()), float(dt), c->mat.stretch_k[0], c->mat.stretch_k[1],
+                        c->mat.stretch_k[2], c->mat.fix_fv_norm, c->mat.rayleigh_a,
+                        c->mat.rayleigh_b, params, stats);
+    if (rc != CLOTH_OK)
+        return rc;
+    // keep the library's device state in step, so GetPos and the fast path see it
+    CK(cudaMemcpy(c->h.x64, c->plain_x.data(), c->plain_x.size() * 8, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(c->h.xp64, c->plain_xp.data(), c->plain_xp.size() * 8, cudaMemcpyHostToDevice));
+    k_sync_x32<<<std::min(1024, (n + 255) / 256), 256, 0, c->ctx->stream>>>(c->d_desc);
+    CK(cudaGetLastError());
+    if (c->drag_vid >= 0)
+    {
+        c->drag_vid = -1;
+        c->pins_dirty = true;
+    }
     return CLOTH_OK;
 }
 

@@ -226,6 +226,19 @@ int cloth_export_triangles(cloth_t *cloth, float *fint, float *hess);
 int cloth_export_tables(const cloth_t *cloth, int *stencil, float *coef,
                         float *area, float *mass, int *tri_slot);
 
+/* The reference GPU path's structure, re-expressed, as the comparison
+ * baseline ("plain GPU PCG"): cBaraffClothGpu::UpdatePos
+ * (BaraffClothGpu.cpp:152-265) with its host round trips (pins snapped and
+ * positions kept in double on the host, float copies uploaded, dx downloaded
+ * and added on the host), its assembly kernels (float atomics, 32-wide slot
+ * search, BaraffClothGpu.cu:111-483) and PCGSolver::Solve (PCGSolver.cu:332-481:
+ * four launches per iteration, float single-address atomic dot products, the
+ * residual downloaded and its norm taken on the host every check_every-th
+ * iteration). params NULL = the reference's settings (100 iterations,
+ * ||r|| < 1e-10 absolute, checked every 10). The cloth's state is updated. */
+int cloth_step_plain(cloth_t *cloth, double dt, const cloth_solve_params *params,
+                     cloth_solve_stats *stats);
+
 /* ---------------------------------------------------------------- batch */
 /* Many cloths of uneven sizes stepped together: one launch per phase covers
  * every instance (a packed tile list over all of them), each instance keeps its

@@ -279,3 +279,44 @@ def test_status_codes(ctx):
     st = c.UpdatePos(0.0, params(max_iters=50, rel_tol=1e-6))
     assert st["status"] == "NAN"
     c.close()
+
+
+def test_plain_baseline_matches_fast_path(ctx, orc):
+    """The reference-structured baseline (cloth_step_plain) and the fast path
+    solve the same step; with the same relative tolerance their displacements
+    agree, and both agree with the FP64 oracle."""
+    from acousticsim_gb300 import params
+    p = params(max_iters=20000, rel_tol=1e-6, check_every=10)
+    conf = _grid_conf(40)
+    a, b = make(ctx, conf), make(ctx, conf)
+    x, xp = _perturbed(a, 21, 2e-3)
+    for c in (a, b):
+        c.SetPos(x)
+        c.SetPrePos(xp)
+    sa = a.UpdatePos(0.0, p)
+    sb = b.UpdatePosPlain(0.0, p)
+    assert sa["status"] == "OK" and sb["status"] == "OK", (sa, sb)
+    assert sb["solver"] == "plain"
+    oc = orc.OracleCloth(a.mesh, conf, a.GetConstraintStaticVertices())
+    oc.x, oc.xpre = x.copy(), xp.copy()
+    oc.step(rel_tol=1e-12)
+    da, db, do = a.GetPos() - x, b.GetPos() - x, oc.x - x
+    print("fast vs oracle", rel(da, do), "plain vs oracle", rel(db, do), "iters", sa["iters"], sb["iters"])
+    assert rel(da, do) < 1e-3 and rel(db, do) < 1e-3
+    assert np.array_equal(b.GetPrePos(), a.GetPrePos())
+    a.close()
+    b.close()
+
+
+def test_plain_reference_schedule(ctx):
+    """Default plain settings are the reference's: at most 100 iterations,
+    absolute 1e-10 tested after iterations 1, 11, 21, ..."""
+    conf = _grid_conf(24)
+    c = make(ctx, conf)
+    x, xp = _perturbed(c, 4, 2e-3)
+    c.SetPos(x)
+    c.SetPrePos(xp)
+    for _ in range(2):
+        st = c.UpdatePosPlain()
+        assert st["iters"] in [1 + 10 * k for k in range(10)] + [100], st
+    c.close()
