@@ -392,6 +392,102 @@ def run_ours(args, rank, world, local, pg):
     ctx.close()
 
 
+# ---------------------------------------------------------------- batched
+def batch_confs(count=256, seed=7, dt=DT):
+    """Batched workload: sides log-uniform in [16, 128] vertices, stretch
+    stiffness log-uniform in [1e2, 1e4] (shear a tenth of it), the top edge
+    pinned, the same density, bending, damping and perturbation as the
+    single-cloth workload."""
+    rng = np.random.default_rng(seed)
+    sides = np.rint(np.exp(rng.uniform(np.log(16), np.log(128), count))).astype(int)
+    ks = np.exp(rng.uniform(np.log(1e2), np.log(1e4), count))
+    out = []
+    for n, k in zip(sides, ks):
+        c = workload_conf(int(n), dt)
+        c["cloth_stretch_stiffness"] = [float(k), float(k), float(k) / 10]
+        c.pop("constraints")
+        out.append((int(n), c))
+    return out
+
+
+def make_batch(ctx, confs, seed=11):
+    from acousticsim_gb300 import BaraffClothGpu
+    cloths, states = [], []
+    for i, (n, conf) in enumerate(confs):
+        c = BaraffClothGpu(ctx, conf)
+        c.AddConstraintStaticVertices([k * n + (n - 1) for k in range(n)])  # top edge
+        x, xp = initial_state(c.GetInitPos(), seed + i)
+        c.SetPos(x)
+        c.SetPrePos(xp)
+        cloths.append(c)
+        states.append((x, xp))
+    return cloths, states
+
+
+def run_batch(args):
+    """256 cloths stepped together vs one at a time (fast path and the plain
+    reference-structured path). Metric: solves/s (cloth steps per second)."""
+    import torch
+    from acousticsim_gb300 import ClothContext, params
+    from acousticsim_gb300 import build as b
+    b.build_all()
+    ctx = ClothContext(0)
+    confs = batch_confs(args.batch_count)
+    p = params(max_iters=MAX_ITERS, rel_tol=REL_TOL)
+    pplain = params(max_iters=100000, rel_tol=REL_TOL, check_every=10)
+    res = {}
+    for solver in ("persistent", "graph_loop"):
+        ctx.set_solver(solver)
+        cloths, _ = make_batch(ctx, confs)
+        for _ in range(args.warmup):
+            ctx.batch_step(cloths, 0.0, p)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        iters = []
+        for _ in range(args.steps):
+            st = ctx.batch_step(cloths, 0.0, p)
+            assert all(s["status"] == "OK" for s in st), st
+            iters.append(max(s["iters"] for s in st))
+        dt_ = time.perf_counter() - t0
+        res[f"batched_{solver}"] = {"solves_per_s": len(cloths) * args.steps / dt_,
+                                    "ms_per_batch_step": 1e3 * dt_ / args.steps,
+                                    "max_iters_per_step": iters, "solver_used": st[0]["solver"]}
+        for c in cloths:
+            c.close()
+    ctx.set_solver("persistent")
+    # one instance per launch: our own fast path, then the plain path, on a
+    # bounded sample of the cloths
+    cloths, _ = make_batch(ctx, confs)
+    sample = cloths[: args.batch_sample]
+    for c in sample:
+        c.UpdatePos(0.0, p)
+    t0 = time.perf_counter()
+    for c in sample:
+        c.UpdatePos(0.0, p)
+    dt_ = time.perf_counter() - t0
+    res["one_at_a_time_fast"] = {"solves_per_s": len(sample) / dt_, "sample": len(sample)}
+    for c in sample:
+        c.UpdatePosPlain(0.0, pplain)
+    t0 = time.perf_counter()
+    for c in sample:
+        st = c.UpdatePosPlain(0.0, pplain)
+    dt_ = time.perf_counter() - t0
+    res["one_at_a_time_plain"] = {"solves_per_s": len(sample) / dt_, "sample": len(sample)}
+    best = max(res["batched_persistent"]["solves_per_s"], res["batched_graph_loop"]["solves_per_s"])
+    line = {"metric": "batched solves/s, 256 cloths 16..128 per side @1e-6 rel residual",
+            "value": best, "unit": "solves/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "higher_is_better": True, "dtype": "f32 (FP64 PCG reductions)",
+            "data": "synthetic", "config": {"workload": f"{len(confs)} cloths, sides log-U[16,128], "
+                                                        "K log-U[1e2,1e4], top edge pinned, dt=2ms"},
+            "results": res,
+            "speedup_vs_plain": best / res["one_at_a_time_plain"]["solves_per_s"],
+            "speedup_vs_one_at_a_time_fast": best / res["one_at_a_time_fast"]["solves_per_s"]}
+    print(json.dumps(line), flush=True)
+    for c in cloths:
+        c.close()
+    ctx.close()
+
+
 def run_profile_case(args):
     """Small case for ncu: one step of the 512x512 workload with the PCG capped
     at --profile-iters iterations, kernels launched from the host."""
@@ -421,9 +517,17 @@ def main():
     ap.add_argument("--profile-iters", type=int, default=0,
                     help="run only the small ncu case: one step, PCG capped at N iterations")
     ap.add_argument("--solver", choices=["persistent", "graph_loop"], default=None)
+    ap.add_argument("--mode", choices=["step", "batch"], default="step",
+                    help="step: the 512x512 single-cloth headline; batch: 256 mixed cloths")
+    ap.add_argument("--batch-count", type=int, default=256)
+    ap.add_argument("--batch-sample", type=int, default=32,
+                    help="cloths timed one at a time for the unbatched comparisons")
     args = ap.parse_args()
     if args.profile_iters > 0:
         run_profile_case(args)
+        return
+    if args.mode == "batch":
+        run_batch(args)
         return
     rank, world, local, pg = dist_init(args.gpus)
     if args.impl == "reference":
