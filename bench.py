@@ -384,6 +384,7 @@ def run_ours(args, rank, world, local, pg):
                 "data": "synthetic (seeded perturbation of the flat 512x512 cloth)",
                 "config": config_block({"parallelism": f"replicas x{world}",
                                         "pcg_iters_per_step": iters,
+                                        "step_ms": [round(v, 3) for v in step_ms],
                                         "wall_s_timed_region": wall}),
                 "e2e": e2e, "gpu_launches": launches, "clocks": clk,
                 "roofline": roof, "cpu_baseline": cpu}
