@@ -167,14 +167,15 @@ def measured_peaks() -> dict:
     return {"hbm_gbs": 6800.0, "source": "fallback"}
 
 
-def ncu_traffic(kernel: str) -> float | None:
-    """DRAM bytes per launch of `kernel` from the committed ncu summary, if any."""
+def ncu_traffic(kernel: str, iterations: float) -> float | None:
+    """DRAM bytes (read + write) per launch of `kernel`: the committed ncu
+    capture's bytes per PCG iteration times the iterations of an average launch."""
     p = ROOT / "profiles" / "ncu_traffic.json"
     if not p.exists():
         return None
     d = json.loads(p.read_text())
-    v = d.get(kernel, {}).get("dram_bytes_per_launch_full_workload")
-    return float(v) if v is not None else None
+    v = d.get(kernel, {}).get("dram_bytes_per_iteration")
+    return float(v) * iterations if v is not None else None
 
 
 def algorithmic_bytes(nv: int, nnzb: int) -> dict:
@@ -358,7 +359,9 @@ def run_ours(args, rank, world, local, pg):
     roof = {"bound": "hbm", "kernel": kname,
             "achieved": achieved, "peak": peak["hbm_gbs"], "unit": "GB/s",
             "frac": achieved / peak["hbm_gbs"], "peak_source": f"{peak['source']} hbm_gbs",
-            "traffic": ncu_traffic("k_pcg_persistent" if solver == "persistent" else "k_spmv"),
+            "traffic": ncu_traffic("k_pcg_persistent_sm", float(np.mean(prof_iters)))
+            if solver == "persistent" else None,
+            "traffic_source": "profiles/ncu_traffic.json (ncu capture, 20 iterations of this workload, scaled by iterations)",
             "algorithmic_bytes_per_launch": bytes_launch,
             "algorithmic_bytes_per_iteration": alg["iteration"],
             "avg_launch_ms": launch_ms,
