@@ -59,6 +59,35 @@ class SolveStats(C.Structure):
                 "solver": SOLVER_NAMES.get(self.solver, str(self.solver))}
 
 
+class ServerConfig(C.Structure):
+    _fields_ = [("budget_bytes", C.c_size_t), ("max_inflight", C.c_int),
+                ("chunk_iters", C.c_int)]
+
+
+class ServerResult(C.Structure):
+    _fields_ = [("tag", C.c_longlong), ("cloth", C.c_int), ("status", C.c_int),
+                ("iters", C.c_int), ("pad", C.c_int), ("rel_residual", C.c_double),
+                ("t_arrival", C.c_double), ("t_admit", C.c_double), ("t_done", C.c_double)]
+
+    def as_dict(self) -> dict:
+        return {"tag": self.tag, "cloth": self.cloth,
+                "status": STATUS_NAMES.get(self.status, str(self.status)), "iters": self.iters,
+                "rel_residual": self.rel_residual, "t_arrival": self.t_arrival,
+                "t_admit": self.t_admit, "t_done": self.t_done}
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("submitted", C.c_longlong), ("completed", C.c_longlong),
+                ("chunks", C.c_longlong), ("admitted_waits", C.c_longlong),
+                ("max_inflight_seen", C.c_int), ("registered", C.c_int),
+                ("resident_bytes", C.c_size_t), ("pool_bytes", C.c_size_t),
+                ("pool_peak_bytes", C.c_size_t), ("own_bytes", C.c_size_t),
+                ("max_request_bytes", C.c_size_t)]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 P = C.c_void_p
 PI = C.POINTER(C.c_int)
 PF = C.POINTER(C.c_float)
@@ -84,6 +113,8 @@ SIGNATURES = {
     "cloth_create": (C.c_int, [P, C.POINTER(MeshDesc), C.POINTER(Material), C.POINTER(P)]),
     "cloth_destroy": (C.c_int, [P]),
     "cloth_num_vertices": (C.c_int, [P, PI, PI, PI]),
+    "cloth_matrix_info": (C.c_int, [P, C.POINTER(C.c_longlong), PI, C.POINTER(C.c_size_t),
+                                    C.POINTER(C.c_size_t)]),
     "cloth_set_material": (C.c_int, [P, C.POINTER(Material)]),
     "cloth_find_vertices_from_uv": (C.c_int, [P, PF, C.c_int, PI]),
     "cloth_add_static_vertices": (C.c_int, [P, PI, C.c_int]),
@@ -112,6 +143,15 @@ SIGNATURES = {
     "cloth_pcg_solve_ell32_noalloc": (C.c_int, [C.c_int, P, P, P, P, P, C.c_int,
                                                 C.POINTER(SolveParams), C.POINTER(SolveStats),
                                                 P]),
+    "cloth_server_now": (C.c_double, []),
+    "cloth_server_create": (C.c_int, [P, C.POINTER(ServerConfig), C.POINTER(P)]),
+    "cloth_server_add": (C.c_int, [P, P, C.c_double, C.POINTER(SolveParams), PI]),
+    "cloth_server_start": (C.c_int, [P]),
+    "cloth_server_submit": (C.c_int, [P, C.c_int, C.c_longlong, C.c_double]),
+    "cloth_server_poll": (C.c_int, [P, C.POINTER(ServerResult), C.c_int, PI, C.c_double]),
+    "cloth_server_drain": (C.c_int, [P, C.c_double]),
+    "cloth_server_get_stats": (C.c_int, [P, C.POINTER(ServerStats)]),
+    "cloth_server_destroy": (C.c_int, [P]),
 }
 
 

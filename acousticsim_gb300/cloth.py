@@ -22,6 +22,7 @@ class ClothContext:
         import weakref
         self._h = C.c_void_p()
         self._cloths = weakref.WeakSet()
+        self._servers = weakref.WeakSet()
         N.call("cloth_ctx_create", int(device), C.byref(self._h))
 
     @property
@@ -68,8 +69,8 @@ class ClothContext:
         return [s.as_dict() for s in st] if stats else None
 
     def close(self) -> None:
-        # the context frees every cloth it holds; their handles die with it
-        for c in list(self._cloths):
+        # the context frees every server and cloth it holds; their handles die with it
+        for c in list(self._cloths) + list(self._servers):
             c._h = C.c_void_p()
         if self._h:
             N.load().cloth_ctx_destroy(self._h)
@@ -227,6 +228,16 @@ class BaraffClothGpu:
     def GetInitPos(self) -> np.ndarray:
         return np.asarray(self.mesh["pos"], np.float64).reshape(-1).copy()
 
+    def matrix_info(self) -> dict:
+        nnzb = C.c_longlong()
+        w = C.c_int()
+        rb = C.c_size_t()
+        sb = C.c_size_t()
+        N.call("cloth_matrix_info", self._h, C.byref(nnzb), C.byref(w), C.byref(rb),
+               C.byref(sb))
+        return {"nnzb": nnzb.value, "width": w.value, "resident_bytes": rb.value,
+                "solve_bytes": sb.value}
+
     def GetNumOfVertices(self) -> int:
         return self.nv
 
@@ -319,9 +330,70 @@ class BaraffClothGpu:
         return {"stencil": st, "coef": coef, "area": area, "mass": mass, "tri_slot": ts}
 
     def close(self) -> None:
-        if self._h:
-            N.load().cloth_destroy(self._h)
+        # a cloth held by a server stays alive until the server (or the context) goes
+        if self._h and N.load().cloth_destroy(self._h) == N.CLOTH_OK:
             self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class ClothServer:
+    """Request server with continuous batching (cloth_server_*).
+
+    Register cloths with `add`, then `start`; `submit(index, tag, t_arrival)`
+    queues one step of a cloth, `poll` returns completed requests as dicts
+    with the arrival, admission and completion times on the `now()` clock."""
+
+    def __init__(self, ctx: ClothContext, budget_bytes: int, max_inflight: int = 0,
+                 chunk_iters: int = 16):
+        self._h = C.c_void_p()
+        self.ctx = ctx
+        self._held = []
+        cfg = N.ServerConfig(int(budget_bytes), int(max_inflight), int(chunk_iters))
+        N.call("cloth_server_create", ctx.handle, C.byref(cfg), C.byref(self._h))
+        ctx._servers.add(self)
+
+    @staticmethod
+    def now() -> float:
+        return float(N.load().cloth_server_now())
+
+    def add(self, cloth: BaraffClothGpu, dt: float = 0.0,
+            params: N.SolveParams | None = None) -> int:
+        idx = C.c_int()
+        N.call("cloth_server_add", self._h, cloth.handle, float(dt),
+               C.byref(params) if params is not None else None, C.byref(idx))
+        self._held.append(cloth)
+        return idx.value
+
+    def start(self) -> None:
+        N.call("cloth_server_start", self._h)
+
+    def submit(self, index: int, tag: int, t_arrival: float = -1.0) -> None:
+        N.call("cloth_server_submit", self._h, int(index), int(tag), float(t_arrival))
+
+    def poll(self, cap: int = 4096, wait_s: float = 0.0) -> list[dict]:
+        out = (N.ServerResult * cap)()
+        n = C.c_int()
+        N.call("cloth_server_poll", self._h, out, int(cap), C.byref(n), float(wait_s))
+        return [out[k].as_dict() for k in range(n.value)]
+
+    def drain(self, wait_s: float = -1.0) -> None:
+        N.call("cloth_server_drain", self._h, float(wait_s))
+
+    def stats(self) -> dict:
+        st = N.ServerStats()
+        N.call("cloth_server_get_stats", self._h, C.byref(st))
+        return st.as_dict()
+
+    def close(self) -> None:
+        if self._h:
+            N.load().cloth_server_destroy(self._h)
+            self._h = C.c_void_p()
+        self._held = []
 
     def __del__(self):
         try:

@@ -1,53 +1,14 @@
 // C ABI of the GB300 implicit cloth step: contexts, cloth instances, the
 // step driver (one CUDA graph per launch set, PCG as a device-side while loop),
 // batches and exports.  Declarations and reference mapping: include/cloth_gb300.h.
-#include "../../include/cloth_gb300.h"
-#include "device.cuh"
-#include "topology.h"
+#include "internal.h"
 
 #include <algorithm>
 #include <cmath>
-#include <cstring>
-#include <memory>
-#include <mutex>
-#include <string>
-#include <vector>
-
-namespace cloth {
-__global__ void k_pins(InstDesc *const *descs, const int *inst_list, int ninst);
-__global__ void k_tri(InstDesc *const *descs, const Tile *tiles, const BatchCtl *ctl);
-__global__ void k_row(InstDesc *const *descs, const Tile *tiles, BatchCtl *ctl);
-__global__ void k_cond(const BatchCtl *ctl, cudaGraphConditionalHandle h);
-__global__ void k_spmv(InstDesc *const *descs, const Tile *tiles, BatchCtl *ctl,
-                       int use_cond, cudaGraphConditionalHandle h);
-__global__ void k_update(InstDesc *const *descs, const Tile *tiles, BatchCtl *ctl,
-                         int use_cond, cudaGraphConditionalHandle h);
-__global__ void k_advance(InstDesc *const *descs, const Tile *tiles,
-                          const BatchCtl *ctl);
-__global__ void k_sync_x32(InstDesc *d);
-struct PlainState;
-struct PlainInit
-{
-    int nv, nt;
-    const int *ell_host;
-    const float *kb_scalar_host;
-    const float *mass_host, *grav_host;
-    const int4 *tri_dev;
-    const float4 *coef_dev;
-};
-int plain_create(const PlainInit &in, PlainState **out);
-void plain_free(PlainState *p);
-size_t plain_bytes(const PlainState *p);
-int plain_step(PlainState *p, double *x, double *xp, const int *pins, const float *pin_tgt,
-               int npins, float dt, float kw, float kwe, float kb, int fix_fv, float ra,
-               float rb, const cloth_solve_params *prm, cloth_solve_stats *stats);
-__global__ void k_pcg_persistent_sm(InstDesc *const *descs, const TeamBlock *work,
-                                    int halo_cap, int rows_cap);
-__global__ void k_pcg_persistent_gm(InstDesc *const *descs, const TeamBlock *work,
-                                    int halo_cap, int rows_cap);
-} // namespace cloth
 
 using namespace cloth;
+using namespace cloth::detail;
+
 
 namespace {
 
@@ -68,20 +29,6 @@ int fail(int code, const std::string &msg)
                         std::string(#call) + ": " + cudaGetErrorString(e_));   \
     } while (0)
 
-size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
-
-// Sub-allocations of one cudaMalloc, 256-byte aligned.
-struct Layout
-{
-    size_t off = 0;
-    template <class T> size_t take(size_t n)
-    {
-        size_t o = off;
-        off = align_up(off + n * sizeof(T), 256);
-        return o;
-    }
-};
-
 enum Phase
 {
     PH_PINS = 0,
@@ -92,61 +39,18 @@ enum Phase
     PH_ADVANCE
 };
 
-struct Batch;
-
 } // namespace
 
-struct cloth_ctx_s
-{
-    int device = 0;
-    cudaStream_t stream = nullptr;
-    std::recursive_mutex mu;
-    int num_sms = 0;
-    int occ_tri = 1, occ_row = 1, occ_spmv = 1, occ_update = 1;
-    int max_smem_optin = 0;
-    int solver = 0; // 0: persistent cooperative PCG when the set fits, 1: graph loop
-    bool prof = false;
-    double prof_ms[CLOTH_NUM_PHASES] = {};
-    long long prof_n[CLOTH_NUM_PHASES] = {};
-    std::vector<cudaEvent_t> ev_pool;
-    std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> ev_pending;
-    size_t bytes = 0;
-    std::vector<cloth_s *> cloths;
-    std::unique_ptr<Batch> last_batch;
-};
+cloth_ctx_s::~cloth_ctx_s() = default;
 
-struct cloth_s
+cloth_s::~cloth_s()
 {
-    cloth_ctx *ctx = nullptr;
-    Mesh mesh;
-    Tables tab;
-    Material mat;
-    std::vector<int> static_pins;
-    int drag_vid = -1;
-    float drag_tgt[3] = {0, 0, 0};
-    bool pins_dirty = true;
-    int npins_uploaded = 0;
-    char *arena = nullptr;
-    size_t arena_bytes = 0;
-    InstDesc h;               // host copy of the descriptor
-    InstDesc *d_desc = nullptr;
-    InstState *d_state = nullptr;
-    bool desc_dirty = true;
-    bool assembled = false;
-    double dt_set = -1.0;
-    std::unique_ptr<Batch> self;
-    // plain (reference-structured) path: host positions and its device state
-    cloth::PlainState *plain = nullptr;
-    std::vector<double> plain_x, plain_xp;
-    bool plain_host_valid = false;
-    ~cloth_s()
-    {
-        if (plain)
-            cloth::plain_free(plain);
-    }
-};
+    if (plain)
+        cloth::plain_free(plain);
+}
 
-namespace {
+namespace cloth {
+namespace detail {
 
 struct Batch
 {
@@ -180,6 +84,11 @@ struct Batch
             cudaFree(d_work);
     }
 };
+
+} // namespace detail
+} // namespace cloth
+
+namespace {
 
 cloth_solve_params default_params()
 {
@@ -255,24 +164,45 @@ int upload_tables(cloth_s *c)
     const int S = int(align_up(size_t(n), 32));
     const int ntr = (n + kTile - 1) / kTile, ntt = (T + kTile - 1) / kTile;
     const size_t WS = size_t(W) * S;
+    // planes of the stored (diagonal + upper) blocks and of the lower slots
+    int Wu = 1, Wl = 0;
+    for (int v = 0; v < n; v++)
+    {
+        const int len = t.rowptr[v + 1] - t.rowptr[v];
+        Wu = std::max(Wu, len - t.diag_slot[v]);
+        Wl = std::max(Wl, t.diag_slot[v]);
+    }
+    const size_t WuS = size_t(Wu) * S, WlS = size_t(std::max(Wl, 1)) * S;
+    c->width_up = Wu;
     Layout L;
     size_t o_tri = L.take<int4>(T), o_tcoef = L.take<float4>(3 * size_t(T)),
            o_tdest = L.take<int4>(3 * size_t(T));
-    size_t o_col = L.take<int>(WS), o_hsrc = L.take<uint32_t>(WS),
-           o_kb = L.take<float>(WS), o_A0 = L.take<float4>(WS),
-           o_A1 = L.take<float2>(WS);
+    size_t o_col = L.take<int>(WS), o_hsrc = L.take<uint32_t>(WS), o_kb = L.take<float>(WS),
+           o_lidx = L.take<uint32_t>(WlS);
     size_t o_rowinfo = L.take<int>(n), o_fptr = L.take<int>(n + 1),
            o_mass = L.take<float>(n), o_grav = L.take<float>(n);
     size_t o_pv = L.take<int>(n + 1), o_pt = L.take<float4>(n + 1);
-    size_t o_hrec = L.take<HRec>(9 * size_t(T)), o_frec = L.take<float4>(3 * size_t(T));
-    size_t o_M0 = L.take<float4>(n), o_M1 = L.take<float2>(n), o_b = L.take<float4>(n);
     size_t o_x64 = L.take<double>(3 * size_t(n)), o_xp64 = L.take<double>(3 * size_t(n));
-    size_t o_x32 = L.take<float4>(n), o_dx = L.take<float4>(n), o_r = L.take<float4>(n),
-           o_z = L.take<float4>(n), o_p0 = L.take<float4>(n), o_p1 = L.take<float4>(n),
-           o_q = L.take<float4>(n);
-    size_t o_part = L.take<double>(3 * size_t(ntr));
+    size_t o_x32 = L.take<float4>(n), o_dx = L.take<float4>(n);
     size_t o_st = L.take<InstState>(1), o_desc = L.take<InstDesc>(1);
     const size_t bytes = L.off;
+    // per-solve work arrays, a separate allocation (a server hands these out)
+    Layout W2;
+    ScratchLayout &sl = c->sl;
+    sl.hrec = W2.take<HRec>(9 * size_t(T));
+    sl.frec = W2.take<float4>(3 * size_t(T));
+    sl.A0 = W2.take<float4>(WuS);
+    sl.A1 = W2.take<float2>(WuS);
+    sl.M0 = W2.take<float4>(n);
+    sl.M1 = W2.take<float2>(n);
+    sl.b = W2.take<float4>(n);
+    sl.r = W2.take<float4>(n);
+    sl.z = W2.take<float4>(n);
+    sl.p0 = W2.take<float4>(n);
+    sl.p1 = W2.take<float4>(n);
+    sl.q = W2.take<float4>(n);
+    sl.part = W2.take<double>(3 * size_t(ntr));
+    sl.bytes = W2.off;
 
     char *base = nullptr;
     if (cudaMalloc(&base, bytes) != cudaSuccess)
@@ -283,8 +213,17 @@ int upload_tables(cloth_s *c)
     }
     c->arena = base;
     c->arena_bytes = bytes;
+    if (cudaMalloc(&c->scratch, sl.bytes) != cudaSuccess)
+    {
+        cudaGetLastError();
+        c->scratch = nullptr;
+        return fail(CLOTH_ERR_OOM, "cloth_create: device allocation of " +
+                                       std::to_string(sl.bytes) + " bytes failed");
+    }
+    c->scratch_bytes = sl.bytes;
     cudaStream_t s = c->ctx->stream;
     CK(cudaMemsetAsync(base, 0, bytes, s));
+    CK(cudaMemsetAsync(c->scratch, 0, sl.bytes, s));
 
     // host staging in device layout
     std::vector<int4> tri(T);
@@ -307,7 +246,7 @@ int upload_tables(cloth_s *c)
         tdest[3 * i + 2] = make_int4(hd[8], fd[0], fd[1], fd[2]);
     }
     std::vector<int> col(WS, 0), rowinfo(n);
-    std::vector<uint32_t> hsrc(WS, 0u);
+    std::vector<uint32_t> hsrc(WS, 0u), lidx(WlS, 0u);
     std::vector<float> kb(WS, 0.f), mass(n), grav(n);
     for (int v = 0; v < n; v++)
     {
@@ -320,6 +259,14 @@ int upload_tables(cloth_s *c)
             col[o] = t.cols[k];
             hsrc[o] = (uint32_t(t.h_start[k]) << 5) | uint32_t(t.h_count[k]);
             kb[o] = t.kbend[k];
+            if (sl < t.diag_slot[v])
+            {
+                // transposed block: row cols[k], the slot holding column v
+                const int cr = t.cols[k];
+                const int *b0 = &t.cols[t.rowptr[cr]], *b1 = &t.cols[t.rowptr[cr + 1]];
+                const int s2 = int(std::lower_bound(b0, b1, v) - b0);
+                lidx[o] = uint32_t(size_t(s2 - t.diag_slot[cr]) * S + size_t(cr));
+            }
         }
         mass[v] = float(t.mass[v]);
         grav[v] = float(c->mat.gravity * t.mass[v]);
@@ -341,6 +288,8 @@ int upload_tables(cloth_s *c)
     CK(cudaMemcpyAsync(base + o_hsrc, hsrc.data(), WS * sizeof(uint32_t),
                        cudaMemcpyHostToDevice, s));
     CK(cudaMemcpyAsync(base + o_kb, kb.data(), WS * sizeof(float),
+                       cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(base + o_lidx, lidx.data(), WlS * sizeof(uint32_t),
                        cudaMemcpyHostToDevice, s));
     CK(cudaMemcpyAsync(base + o_rowinfo, rowinfo.data(), n * sizeof(int),
                        cudaMemcpyHostToDevice, s));
@@ -371,6 +320,7 @@ int upload_tables(cloth_s *c)
     h.col = reinterpret_cast<const int *>(base + o_col);
     h.hsrc = reinterpret_cast<const uint32_t *>(base + o_hsrc);
     h.kb = reinterpret_cast<const float *>(base + o_kb);
+    h.lidx = reinterpret_cast<const uint32_t *>(base + o_lidx);
     h.rowinfo = reinterpret_cast<const int *>(base + o_rowinfo);
     h.fptr = reinterpret_cast<const int *>(base + o_fptr);
     h.mass = reinterpret_cast<const float *>(base + o_mass);
@@ -378,29 +328,83 @@ int upload_tables(cloth_s *c)
     h.pin_vid = reinterpret_cast<const int *>(base + o_pv);
     h.pin_tgt = reinterpret_cast<const float4 *>(base + o_pt);
     h.npins = 0;
-    h.hrec = reinterpret_cast<HRec *>(base + o_hrec);
-    h.frec = reinterpret_cast<float4 *>(base + o_frec);
-    h.A0 = reinterpret_cast<float4 *>(base + o_A0);
-    h.A1 = reinterpret_cast<float2 *>(base + o_A1);
-    h.M0 = reinterpret_cast<float4 *>(base + o_M0);
-    h.M1 = reinterpret_cast<float2 *>(base + o_M1);
-    h.b = reinterpret_cast<float4 *>(base + o_b);
     h.x64 = reinterpret_cast<double *>(base + o_x64);
     h.xp64 = reinterpret_cast<double *>(base + o_xp64);
     h.x32 = reinterpret_cast<float4 *>(base + o_x32);
     h.dx = reinterpret_cast<float4 *>(base + o_dx);
-    h.r = reinterpret_cast<float4 *>(base + o_r);
-    h.z = reinterpret_cast<float4 *>(base + o_z);
-    h.p0 = reinterpret_cast<float4 *>(base + o_p0);
-    h.p1 = reinterpret_cast<float4 *>(base + o_p1);
-    h.q = reinterpret_cast<float4 *>(base + o_q);
-    h.part = reinterpret_cast<double *>(base + o_part);
+    bind_scratch(c, h, c->scratch);
     h.st = reinterpret_cast<InstState *>(base + o_st);
     c->d_state = h.st;
     c->d_desc = reinterpret_cast<InstDesc *>(base + o_desc);
     CK(cudaStreamSynchronize(s));
     return CLOTH_OK;
 }
+
+} // namespace
+
+void cloth::detail::bind_scratch(const cloth_s *c, InstDesc &h, char *base)
+{
+    const ScratchLayout &sl = c->sl;
+    auto at = [&](size_t o) { return base ? base + o : nullptr; };
+    h.hrec = reinterpret_cast<HRec *>(at(sl.hrec));
+    h.frec = reinterpret_cast<float4 *>(at(sl.frec));
+    h.A0 = reinterpret_cast<float4 *>(at(sl.A0));
+    h.A1 = reinterpret_cast<float2 *>(at(sl.A1));
+    h.M0 = reinterpret_cast<float4 *>(at(sl.M0));
+    h.M1 = reinterpret_cast<float2 *>(at(sl.M1));
+    h.b = reinterpret_cast<float4 *>(at(sl.b));
+    h.r = reinterpret_cast<float4 *>(at(sl.r));
+    h.z = reinterpret_cast<float4 *>(at(sl.z));
+    h.p0 = reinterpret_cast<float4 *>(at(sl.p0));
+    h.p1 = reinterpret_cast<float4 *>(at(sl.p1));
+    h.q = reinterpret_cast<float4 *>(at(sl.q));
+    h.part = reinterpret_cast<double *>(at(sl.part));
+}
+
+int cloth::detail::alloc_own_scratch(cloth_s *c)
+{
+    if (c->scratch)
+        return CLOTH_OK;
+    if (cudaMalloc(&c->scratch, c->sl.bytes) != cudaSuccess)
+    {
+        cudaGetLastError();
+        c->scratch = nullptr;
+        return fail(CLOTH_ERR_OOM, "device allocation of " + std::to_string(c->sl.bytes) +
+                                       " bytes failed");
+    }
+    c->scratch_bytes = c->sl.bytes;
+    c->ctx->bytes += c->scratch_bytes;
+    CK(cudaMemsetAsync(c->scratch, 0, c->sl.bytes, c->ctx->stream));
+    bind_scratch(c, c->h, c->scratch);
+    c->desc_dirty = true;
+    c->assembled = false;
+    return sync_desc(c);
+}
+
+void cloth::detail::free_own_scratch(cloth_s *c)
+{
+    if (!c->scratch)
+        return;
+    cudaStreamSynchronize(c->ctx->stream);
+    c->self.reset();
+    cloth_ctx *ctx = c->ctx;
+    if (ctx->last_batch)
+        for (auto *m : ctx->last_batch->members)
+            if (m == c)
+            {
+                ctx->last_batch.reset();
+                break;
+            }
+    cudaFree(c->scratch);
+    c->scratch = nullptr;
+    c->ctx->bytes -= c->scratch_bytes;
+    c->scratch_bytes = 0;
+    bind_scratch(c, c->h, nullptr);
+    c->desc_dirty = true;
+    c->assembled = false;
+}
+
+namespace {
 
 void set_material_fields(cloth_s *c)
 {
@@ -411,7 +415,9 @@ void set_material_fields(cloth_s *c)
     c->desc_dirty = true;
 }
 
-void set_params(cloth_s *c, const cloth_solve_params *p)
+} // namespace
+
+void cloth::detail::set_params(cloth_s *c, const cloth_solve_params *p)
 {
     cloth_solve_params q = p ? *p : default_params();
     InstDesc &h = c->h;
@@ -432,7 +438,11 @@ void set_params(cloth_s *c, const cloth_solve_params *p)
     }
 }
 
-void set_dt(cloth_s *c, double dt)
+namespace {
+
+} // namespace
+
+void cloth::detail::set_dt(cloth_s *c, double dt)
 {
     if (!(dt > 0))
         dt = c->mat.default_timestep;
@@ -448,8 +458,12 @@ void set_dt(cloth_s *c, double dt)
     c->desc_dirty = true;
 }
 
+namespace {
+
 // Static points plus the drag point of this step; targets are float.
-int sync_pins(cloth_s *c)
+} // namespace
+
+int cloth::detail::sync_pins(cloth_s *c)
 {
     if (!c->pins_dirty)
         return CLOTH_OK;
@@ -486,7 +500,11 @@ int sync_pins(cloth_s *c)
     return CLOTH_OK;
 }
 
-int sync_desc(cloth_s *c)
+namespace {
+
+} // namespace
+
+int cloth::detail::sync_desc(cloth_s *c)
 {
     if (!c->desc_dirty)
         return CLOTH_OK;
@@ -495,12 +513,18 @@ int sync_desc(cloth_s *c)
     return CLOTH_OK;
 }
 
+namespace {
+
 // ------------------------------------------------------------ batches
 int plan_persistent(cloth_ctx *ctx, Batch *b);
 
 int make_batch(cloth_ctx *ctx, const std::vector<cloth_s *> &members,
                std::unique_ptr<Batch> &out)
 {
+    for (auto *c : members)
+        if (!c->scratch)
+            return fail(CLOTH_ERR_STATE, "the cloth is held by a server; step it through "
+                                         "the server");
     auto b = std::make_unique<Batch>();
     b->ctx = ctx;
     b->members = members;
@@ -723,13 +747,16 @@ int build_graph(Batch *b, bool full, cudaGraphExec_t *exec)
     int one = 1, zero = 0;
     int ninst = int(b->members.size());
     int gpins = std::max(1, std::min(ninst, 1024));
-    void *a_pins[] = {&b->d_descs, &b->d_inst, &ninst};
+    const int *no_count = nullptr;
+    int all_rows = 0;
+    void *a_pins[] = {&b->d_descs, &b->d_inst, &ninst, &no_count};
     void *a_tri[] = {&b->d_descs, &b->d_tt, &b->d_ctl};
     void *a_row[] = {&b->d_descs, &b->d_rt, &b->d_ctl};
     void *a_cond[] = {&b->d_ctl, &hnd};
     void *a_spmv[] = {&b->d_descs, &b->d_rt, &b->d_ctl, &one, &hnd};
-    void *a_upd[] = {&b->d_descs, &b->d_rt, &b->d_ctl, &one, &hnd};
-    void *a_adv[] = {&b->d_descs, &b->d_rt, &b->d_ctl};
+    int *no_left = nullptr;
+    void *a_upd[] = {&b->d_descs, &b->d_rt, &b->d_ctl, &one, &hnd, &no_left};
+    void *a_adv[] = {&b->d_descs, &b->d_rt, &b->d_ctl, &all_rows};
     (void)zero;
     auto chain = [&](void *f, int grid, void **args) {
         if (rc != CLOTH_OK)
@@ -832,7 +859,7 @@ int launch_assemble(Batch *b)
     {
         PhaseTimer t(ctx, PH_PINS);
         k_pins<<<std::max(1, std::min(ninst, 1024)), kTile, 0, s>>>(b->d_descs,
-                                                                  b->d_inst, ninst);
+                                                                  b->d_inst, ninst, nullptr);
     }
     {
         PhaseTimer t(ctx, PH_TRI);
@@ -881,7 +908,7 @@ int launch_solve_host(Batch *b, int max_iters)
             {
                 PhaseTimer t(ctx, PH_UPDATE);
                 k_update<<<b->grid_update, kTile, 0, s>>>(b->d_descs, b->d_rt,
-                                                           b->d_ctl, 0, none);
+                                                           b->d_ctl, 0, none, nullptr);
             }
         }
         if (cudaMemcpyAsync(h_active, &b->d_ctl->n_active, sizeof(int),
@@ -901,7 +928,7 @@ int launch_solve_host(Batch *b, int max_iters)
 int launch_advance(Batch *b)
 {
     PhaseTimer t(b->ctx, PH_ADVANCE);
-    k_advance<<<b->grid_row, kTile, 0, b->ctx->stream>>>(b->d_descs, b->d_rt, b->d_ctl);
+    k_advance<<<b->grid_row, kTile, 0, b->ctx->stream>>>(b->d_descs, b->d_rt, b->d_ctl, 0);
     CK(cudaGetLastError());
     return CLOTH_OK;
 }
@@ -1079,6 +1106,11 @@ int cloth_ctx_destroy(cloth_ctx *ctx)
 {
     if (!ctx)
         return CLOTH_OK;
+    // servers first, without the context lock: their worker threads take it
+    cudaSetDevice(ctx->device);
+    for (auto *sv : std::vector<cloth_server_s *>(ctx->servers))
+        server_teardown(sv);
+    ctx->servers.clear();
     {
         std::lock_guard<std::recursive_mutex> lk(ctx->mu);
         cudaSetDevice(ctx->device);
@@ -1089,6 +1121,8 @@ int cloth_ctx_destroy(cloth_ctx *ctx)
             c->self.reset();
             if (c->arena)
                 cudaFree(c->arena);
+            if (c->scratch)
+                cudaFree(c->scratch);
             delete c;
         }
         ctx->cloths.clear();
@@ -1305,8 +1339,6 @@ int cloth_create(cloth_ctx *ctx, const cloth_mesh_desc *mesh,
         return fail(CLOTH_ERR_INVALID, "cloth_create: bad mesh description");
     if (!(mat->density > 0) || !(mat->default_timestep > 0))
         return fail(CLOTH_ERR_INVALID, "cloth_create: density and timestep must be > 0");
-    std::lock_guard<std::recursive_mutex> lk(ctx->mu);
-    CK(cudaSetDevice(ctx->device));
     auto c = std::make_unique<cloth_s>();
     c->ctx = ctx;
     Mesh &m = c->mesh;
@@ -1315,13 +1347,18 @@ int cloth_create(cloth_ctx *ctx, const cloth_mesh_desc *mesh,
         return fail(CLOTH_ERR_MESH, err);
     Material &mt = c->mat;
     copy_material(mat, mt);
+    // host tables outside the context lock: threads may create cloths in parallel
     if (!build_tables(m, mt, c->tab, err))
         return fail(CLOTH_ERR_MESH, err);
+    std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+    CK(cudaSetDevice(ctx->device));
     int rc = upload_tables(c.get());
     if (rc != CLOTH_OK)
     {
         if (c->arena)
             cudaFree(c->arena);
+        if (c->scratch)
+            cudaFree(c->scratch);
         return rc;
     }
     set_material_fields(c.get());
@@ -1331,9 +1368,10 @@ int cloth_create(cloth_ctx *ctx, const cloth_mesh_desc *mesh,
     if (rc != CLOTH_OK)
     {
         cudaFree(c->arena);
+        cudaFree(c->scratch);
         return rc;
     }
-    ctx->bytes += c->arena_bytes;
+    ctx->bytes += c->arena_bytes + c->scratch_bytes;
     ctx->cloths.push_back(c.get());
     *out = c.release();
     return CLOTH_OK;
@@ -1345,6 +1383,9 @@ int cloth_destroy(cloth_t *c)
         return CLOTH_OK;
     cloth_ctx *ctx = c->ctx;
     std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+    if (c->server)
+        return fail(CLOTH_ERR_STATE, "cloth_destroy: the cloth is held by a server "
+                                     "(destroy the server first)");
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
     if (ctx->last_batch)
@@ -1357,10 +1398,28 @@ int cloth_destroy(cloth_t *c)
     c->self.reset();
     if (c->arena)
         cudaFree(c->arena);
-    ctx->bytes -= c->arena_bytes;
+    if (c->scratch)
+        cudaFree(c->scratch);
+    ctx->bytes -= c->arena_bytes + c->scratch_bytes;
     ctx->cloths.erase(std::remove(ctx->cloths.begin(), ctx->cloths.end(), c),
                       ctx->cloths.end());
     delete c;
+    return CLOTH_OK;
+}
+
+int cloth_matrix_info(const cloth_t *c, long long *nnzb, int *width, size_t *resident_bytes,
+                      size_t *solve_bytes)
+{
+    if (!c)
+        return fail(CLOTH_ERR_INVALID, "cloth is NULL");
+    if (nnzb)
+        *nnzb = (long long)c->tab.cols.size();
+    if (width)
+        *width = c->tab.width;
+    if (resident_bytes)
+        *resident_bytes = c->arena_bytes;
+    if (solve_bytes)
+        *solve_bytes = c->sl.bytes;
     return CLOTH_OK;
 }
 
@@ -1468,6 +1527,8 @@ static int set_state(cloth_t *c, const double *x, int nv, bool pre)
     if (!c || !x || nv != c->mesh.nv)
         return fail(CLOTH_ERR_INVALID, "set_pos: bad argument");
     std::lock_guard<std::recursive_mutex> lk(c->ctx->mu);
+    if (c->server && server_busy(c->server, c))
+        return fail(CLOTH_ERR_STATE, "set_pos: the cloth has server requests in flight");
     CK(cudaSetDevice(c->ctx->device));
     cudaStream_t s = c->ctx->stream;
     CK(cudaMemcpyAsync(pre ? c->h.xp64 : c->h.x64, x, size_t(nv) * 3 * sizeof(double),
@@ -1488,6 +1549,8 @@ static int get_state(cloth_t *c, double *x, int nv, bool pre)
     if (!c || !x || nv != c->mesh.nv)
         return fail(CLOTH_ERR_INVALID, "get_pos: bad argument");
     std::lock_guard<std::recursive_mutex> lk(c->ctx->mu);
+    if (c->server && server_busy(c->server, c))
+        return fail(CLOTH_ERR_STATE, "get_pos: the cloth has server requests in flight");
     CK(cudaSetDevice(c->ctx->device));
     cudaStream_t s = c->ctx->stream;
     CK(cudaMemcpyAsync(x, pre ? c->h.xp64 : c->h.x64, size_t(nv) * 3 * sizeof(double),
@@ -1659,6 +1722,8 @@ int cloth_export_system(cloth_t *c, int *ell, float *A, float *b, float *fint,
     if (!c)
         return fail(CLOTH_ERR_INVALID, "cloth is NULL");
     std::lock_guard<std::recursive_mutex> lk(c->ctx->mu);
+    if (!c->scratch)
+        return fail(CLOTH_ERR_STATE, "export: the cloth is held by a server");
     CK(cudaSetDevice(c->ctx->device));
     CK(cudaStreamSynchronize(c->ctx->stream));
     const Tables &t = c->tab;
@@ -1673,15 +1738,28 @@ int cloth_export_system(cloth_t *c, int *ell, float *A, float *b, float *fint,
             }
     if (A)
     {
-        std::vector<float4> a0(WS);
-        std::vector<float2> a1(WS);
-        CK(cudaMemcpy(a0.data(), c->h.A0, WS * sizeof(float4), cudaMemcpyDeviceToHost));
-        CK(cudaMemcpy(a1.data(), c->h.A1, WS * sizeof(float2), cudaMemcpyDeviceToHost));
+        // stored diagonal + upper blocks; a lower block is its transposed
+        // upper block (the same symmetric 6 floats)
+        const size_t WuS = size_t(c->width_up) * S;
+        std::vector<float4> a0(WuS);
+        std::vector<float2> a1(WuS);
+        CK(cudaMemcpy(a0.data(), c->h.A0, WuS * sizeof(float4), cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(a1.data(), c->h.A1, WuS * sizeof(float2), cudaMemcpyDeviceToHost));
         std::fill(A, A + size_t(n) * R * 9, 0.f);
         for (int v = 0; v < n; v++)
             for (int s = 0; s < t.rowptr[v + 1] - t.rowptr[v]; s++)
             {
-                size_t o = size_t(s) * S + v;
+                const int ds = t.diag_slot[v];
+                size_t o;
+                if (s >= ds)
+                    o = size_t(s - ds) * S + v;
+                else
+                {
+                    const int cr = t.cols[size_t(t.rowptr[v]) + s];
+                    const int *b0 = &t.cols[t.rowptr[cr]], *b1 = &t.cols[t.rowptr[cr + 1]];
+                    const int s2 = int(std::lower_bound(b0, b1, v) - b0);
+                    o = size_t(s2 - t.diag_slot[cr]) * S + size_t(cr);
+                }
                 float e[6] = {a0[o].x, a0[o].y, a0[o].z, a0[o].w, a1[o].x, a1[o].y};
                 float full[9] = {e[0], e[1], e[2], e[1], e[3], e[4], e[2], e[4], e[5]};
                 std::memcpy(A + (size_t(v) * R + s) * 9, full, sizeof(full));
@@ -1739,6 +1817,8 @@ int cloth_export_triangles(cloth_t *c, float *fint, float *hess)
     if (!c)
         return fail(CLOTH_ERR_INVALID, "cloth is NULL");
     std::lock_guard<std::recursive_mutex> lk(c->ctx->mu);
+    if (!c->scratch)
+        return fail(CLOTH_ERR_STATE, "export: the cloth is held by a server");
     CK(cudaSetDevice(c->ctx->device));
     CK(cudaStreamSynchronize(c->ctx->stream));
     const Tables &t = c->tab;

@@ -11,6 +11,14 @@
 // each plane.  A 3x3 block is symmetric (stretch, shear, bending, mass and the
 // Rayleigh terms all are), so it is stored as 6 floats:
 //   A0 = (a00, a01, a02, a11)  as float4,   A1 = (a12, a22) as float2.
+// The matrix is block-symmetric bit for bit (block (i,j) and block (j,i) sum
+// the same triangle records in the same order, the bending scalars are
+// symmetric, the pin projection zeroes both), so only the diagonal and upper
+// blocks (column >= row) are stored: row i's slots are sorted by column, the
+// first diag_slot(i) of them are lower, and upper slot s lives in plane
+// s - diag_slot(i).  A lower slot keeps its column and the plane index of its
+// transposed block (lidx); the SpMV fetches that block, which another row of
+// the same launch has just streamed, from L2.
 #pragma once
 #include <cstdint>
 #include <cuda_runtime.h>
@@ -46,7 +54,7 @@ struct InstState
     unsigned bar_count;
     unsigned bar_gen;
     int bar_err;
-    int pad;
+    int open;       // step assembled and not yet advanced (request server)
     // exact fixed-point team sums of the persistent solver, triple-buffered by
     // iteration: [buffer][quantity: p.q, r.z, r.r][limb: units of 2^32, units]
     unsigned long long acc[3][3][2];
@@ -74,6 +82,7 @@ struct InstDesc
     const int4 *tdest;    // 3 per triangle: h_dest[9], f_dest[3]
     // rows
     const int *col;       // [slot][stride] column (vertex) ids
+    const uint32_t *lidx; // [slot][stride], lower slots: index of the transposed block in A0/A1
     const uint32_t *hsrc; // [slot][stride] first record << 5 | record count
     const float *kb;      // [slot][stride] bending scalar (+K_b)
     const int *rowinfo;   // len | diag_slot << 8
@@ -88,7 +97,7 @@ struct InstDesc
     HRec *hrec;
     float4 *frec;
     // assembled system
-    float4 *A0;
+    float4 *A0;          // [slot - diag_slot][stride]: diagonal and upper blocks
     float2 *A1;
     float4 *M0; // block-Jacobi inverse, symmetric: (00 01 02 11)
     float2 *M1; // (12 22)

@@ -1,0 +1,162 @@
+// Host-side objects shared by the translation units of the library: the
+// context, the cloth instance with its device memory, and the helpers the
+// step driver (cloth_api.cu) and the request server (server.cu) both use.
+// Not part of the C ABI.
+#pragma once
+#include "../../include/cloth_gb300.h"
+#include "device.cuh"
+#include "topology.h"
+
+#include <cstring>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <utility>
+#include <vector>
+
+namespace cloth {
+
+// ---------------------------------------------------------------- kernels
+__global__ void k_pins(InstDesc *const *descs, const int *inst_list, int ninst,
+                       const int *ninst_dev);
+__global__ void k_tri(InstDesc *const *descs, const Tile *tiles, const BatchCtl *ctl);
+__global__ void k_row(InstDesc *const *descs, const Tile *tiles, BatchCtl *ctl);
+__global__ void k_cond(const BatchCtl *ctl, cudaGraphConditionalHandle h);
+__global__ void k_spmv(InstDesc *const *descs, const Tile *tiles, BatchCtl *ctl,
+                       int use_cond, cudaGraphConditionalHandle h);
+__global__ void k_update(InstDesc *const *descs, const Tile *tiles, BatchCtl *ctl,
+                         int use_cond, cudaGraphConditionalHandle h, int *iters_left);
+__global__ void k_advance(InstDesc *const *descs, const Tile *tiles,
+                          const BatchCtl *ctl, int finished_only);
+__global__ void k_sync_x32(InstDesc *d);
+__global__ void k_pcg_persistent_sm(InstDesc *const *descs, const TeamBlock *work,
+                                    int halo_cap, int rows_cap);
+__global__ void k_pcg_persistent_gm(InstDesc *const *descs, const TeamBlock *work,
+                                    int halo_cap, int rows_cap);
+
+// ---------------------------------------------------------------- plain path
+struct PlainState;
+struct PlainInit
+{
+    int nv, nt;
+    const int *ell_host;
+    const float *kb_scalar_host;
+    const float *mass_host, *grav_host;
+    const int4 *tri_dev;
+    const float4 *coef_dev;
+};
+int plain_create(const PlainInit &in, PlainState **out);
+void plain_free(PlainState *p);
+size_t plain_bytes(const PlainState *p);
+int plain_step(PlainState *p, double *x, double *xp, const int *pins, const float *pin_tgt,
+               int npins, float dt, float kw, float kwe, float kb, int fix_fv, float ra,
+               float rb, const cloth_solve_params *prm, cloth_solve_stats *stats);
+
+void set_last_error(const std::string &msg);
+
+inline size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+// Sub-allocations of one device allocation, 256-byte aligned.
+struct Layout
+{
+    size_t off = 0;
+    template <class T> size_t take(size_t n)
+    {
+        size_t o = off;
+        off = align_up(off + n * sizeof(T), 256);
+        return o;
+    }
+};
+
+// Offsets of the per-solve work arrays inside one scratch allocation: the
+// triangle records, the assembled system and preconditioner, and the PCG
+// vectors.  Everything else of a cloth (mesh tables, ELL map, positions, the
+// warm-start dx, pins, PCG scalars) is resident state.
+struct ScratchLayout
+{
+    size_t hrec = 0, frec = 0, A0 = 0, A1 = 0, M0 = 0, M1 = 0, b = 0;
+    size_t r = 0, z = 0, p0 = 0, p1 = 0, q = 0, part = 0;
+    size_t bytes = 0;
+};
+
+namespace detail {
+struct Batch;
+}
+
+} // namespace cloth
+
+struct cloth_server_s;
+
+struct cloth_ctx_s
+{
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    std::recursive_mutex mu;
+    int num_sms = 0;
+    int occ_tri = 1, occ_row = 1, occ_spmv = 1, occ_update = 1;
+    int max_smem_optin = 0;
+    int solver = 0; // 0: persistent cooperative PCG when the set fits, 1: graph loop
+    bool prof = false;
+    double prof_ms[CLOTH_NUM_PHASES] = {};
+    long long prof_n[CLOTH_NUM_PHASES] = {};
+    std::vector<cudaEvent_t> ev_pool;
+    std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> ev_pending;
+    size_t bytes = 0;
+    std::vector<cloth_s *> cloths;
+    std::vector<cloth_server_s *> servers;
+    std::unique_ptr<cloth::detail::Batch> last_batch;
+    ~cloth_ctx_s();
+};
+
+struct cloth_s
+{
+    cloth_ctx *ctx = nullptr;
+    cloth::Mesh mesh;
+    cloth::Tables tab;
+    cloth::Material mat;
+    std::vector<int> static_pins;
+    int drag_vid = -1;
+    float drag_tgt[3] = {0, 0, 0};
+    bool pins_dirty = true;
+    int npins_uploaded = 0;
+    char *arena = nullptr;    // resident state
+    size_t arena_bytes = 0;
+    char *scratch = nullptr;  // own per-solve work arrays; null while a server holds the cloth
+    size_t scratch_bytes = 0;
+    cloth::ScratchLayout sl;
+    int width_up = 1;         // planes of the stored (diagonal + upper) blocks
+    cloth_server_s *server = nullptr;
+    cloth::InstDesc h;        // host copy of the descriptor
+    cloth::InstDesc *d_desc = nullptr;
+    cloth::InstState *d_state = nullptr;
+    bool desc_dirty = true;
+    bool assembled = false;
+    double dt_set = -1.0;
+    std::unique_ptr<cloth::detail::Batch> self;
+    // plain (reference-structured) path: host positions and its device state
+    cloth::PlainState *plain = nullptr;
+    std::vector<double> plain_x, plain_xp;
+    bool plain_host_valid = false;
+    ~cloth_s();
+};
+
+namespace cloth {
+namespace detail {
+
+// Points the scratch fields of h at base (null: clears them).
+void bind_scratch(const cloth_s *c, InstDesc &h, char *base);
+// Own scratch of a cloth: allocate (and bind, upload the descriptor) / free.
+int alloc_own_scratch(cloth_s *c);
+void free_own_scratch(cloth_s *c);
+// Parameters, time step and pins of the next step, as the step driver sets them.
+void set_params(cloth_s *c, const cloth_solve_params *p);
+void set_dt(cloth_s *c, double dt);
+int sync_pins(cloth_s *c);
+int sync_desc(cloth_s *c);
+// A server's view of one of its cloths: true while requests are queued or running.
+bool server_busy(const cloth_server_s *s, const cloth_s *c);
+// Detach every cloth of a server and free it (context teardown).
+void server_teardown(cloth_server_s *s);
+
+} // namespace detail
+} // namespace cloth

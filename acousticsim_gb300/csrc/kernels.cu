@@ -280,8 +280,11 @@ __device__ __forceinline__ void stretch_component(
 // ------------------------------------------------------------------ pins
 // UpdateConstraintVertexPos (BaraffClothGpu.cpp:411-436): pinned vertices are
 // put at their target in x and x_pre; x32.w marks them for the row pass.
-__global__ void k_pins(InstDesc *const *descs, const int *inst_list, int ninst)
+__global__ void k_pins(InstDesc *const *descs, const int *inst_list, int ninst,
+                       const int *ninst_dev)
 {
+    if (ninst_dev)
+        ninst = *ninst_dev;
     for (int i = blockIdx.x; i < ninst; i += gridDim.x)
     {
         const InstDesc &d = *descs[inst_list[i]];
@@ -433,8 +436,14 @@ __global__ void __launch_bounds__(kTile) k_row(InstDesc *const *descs,
                     for (int k = 0; k < 6; k++)
                         A[k] = 0.f;
                 }
-                d.A0[o] = make_float4(A[0], A[1], A[2], A[3]);
-                d.A1[o] = make_float2(A[4], A[5]);
+                if (s >= ds)
+                {
+                    // stored: diagonal and upper blocks (the lower ones are
+                    // the same values, held by the transposed position)
+                    const size_t ou = size_t(s - ds) * d.stride + row;
+                    d.A0[ou] = make_float4(A[0], A[1], A[2], A[3]);
+                    d.A1[ou] = make_float2(A[4], A[5]);
+                }
                 if (d.warm_start && !zero && !fixv)
                     acc = acc + symv(A, xyz(d.dx[c]));
             }
@@ -483,6 +492,7 @@ __global__ void __launch_bounds__(kTile) k_row(InstDesc *const *descs,
             st.status = 0;
             st.bar_count = 0u;
             st.bar_err = 0;
+            st.open = 1;
             for (int bq = 0; bq < 3; bq++)
                 for (int q = 0; q < 3; q++)
                 {
@@ -538,7 +548,8 @@ __global__ void __launch_bounds__(kTile) k_spmv(InstDesc *const *descs,
         float part[1] = {0.f};
         if (row < d.nv)
         {
-            const int len = d.rowinfo[row] & 255;
+            const int info = d.rowinfo[row];
+            const int len = info & 255, ds = (info >> 8) & 255;
             float3 pv = xyz(d.z[row]);
             if (beta != 0.f)
                 pv = pv + beta * xyz(pold[row]);
@@ -548,8 +559,9 @@ __global__ void __launch_bounds__(kTile) k_spmv(InstDesc *const *descs,
             {
                 const size_t o = size_t(s) * d.stride + row;
                 const int c = d.col[o];
+                const size_t oa = s < ds ? size_t(d.lidx[o]) : size_t(s - ds) * d.stride + row;
                 float A[6];
-                load_sym(d.A0, d.A1, o, A);
+                load_sym(d.A0, d.A1, oa, A);
                 float3 pc;
                 if (c == row)
                     pc = pv;
@@ -594,10 +606,20 @@ __global__ void __launch_bounds__(kTile) k_spmv(InstDesc *const *descs,
 __global__ void __launch_bounds__(kTile) k_update(InstDesc *const *descs,
                                                   const Tile *tiles,
                                                   BatchCtl *ctl, int use_cond,
-                                                  cudaGraphConditionalHandle h)
+                                                  cudaGraphConditionalHandle h,
+                                                  int *iters_left)
 {
     __shared__ double sh[2][kTile / 32];
     __shared__ int flag;
+    // chunked loops (the request server): the last iteration of a chunk ends
+    // the while loop; the condition is read after the body completes
+    if (iters_left && blockIdx.x == 0 && threadIdx.x == 0)
+    {
+        const int left = *iters_left - 1;
+        *iters_left = left;
+        if (use_cond && left <= 0)
+            cudaGraphSetConditional(h, 0u);
+    }
     const int ntiles = ctl->n_tiles_rows;
     for (int ti = blockIdx.x; ti < ntiles; ti += gridDim.x)
     {
@@ -1035,9 +1057,14 @@ __device__ __forceinline__ void pcg_persistent_body(InstDesc *const *descs,
                     }
                 }
                 pnew[row] = f4(pv);
-                const int len = ld_keep(d.rowinfo + row, keep) & 255;
+                const int info = ld_keep(d.rowinfo + row, keep);
+                const int len = info & 255, ds = (info >> 8) & 255;
                 float3 q = make_float3(0, 0, 0);
-                // kSlotUnroll slots at a time: their loads are all in flight together
+                // Slots in column order: a lower slot (s < ds) fetches its block
+                // at the transposed position, the diagonal and upper ones are
+                // stored in plane s - ds. kSlotUnroll slots at a time: their
+                // loads are all in flight together.
+                const uint32_t *lix = d.lidx + row;
                 for (int s0 = 0; s0 < len; s0 += kSlotUnroll)
                 {
                     int cc[kSlotUnroll];
@@ -1047,10 +1074,14 @@ __device__ __forceinline__ void pcg_persistent_body(InstDesc *const *descs,
                     for (int k = 0; k < kSlotUnroll; k++)
                         if (s0 + k < len)
                         {
-                            const size_t o = size_t(s0 + k) * d.stride + row;
-                            cc[k] = ld_keep(d.col + o, keep);
-                            a0[k] = ld_keep(d.A0 + o, keep);
-                            a1[k] = ld_keep(d.A1 + o, keep);
+                            const int sl = s0 + k;
+                            const uint32_t o = uint32_t(sl) * uint32_t(d.stride);
+                            cc[k] = ld_keep(d.col + row + o, keep);
+                            const uint32_t oa =
+                                sl < ds ? uint32_t(ld_keep(reinterpret_cast<const int *>(lix + o), keep))
+                                        : uint32_t(sl - ds) * uint32_t(d.stride) + uint32_t(row);
+                            a0[k] = ld_keep(d.A0 + oa, keep);
+                            a1[k] = ld_keep(d.A1 + oa, keep);
                         }
 #pragma unroll
                     for (int k = 0; k < kSlotUnroll; k++)
@@ -1246,13 +1277,18 @@ __global__ void __launch_bounds__(kPBlock, 1)
 // ------------------------------------------------------------------ advance
 __global__ void __launch_bounds__(kTile) k_advance(InstDesc *const *descs,
                                                    const Tile *tiles,
-                                                   const BatchCtl *ctl)
+                                                   const BatchCtl *ctl,
+                                                   int finished_only)
 {
     const int ntiles = ctl->n_tiles_rows;
     for (int ti = blockIdx.x; ti < ntiles; ti += gridDim.x)
     {
         const Tile tl = tiles[ti];
         const InstDesc &d = *descs[tl.inst];
+        // finished_only: instances whose solve ended and whose step is still
+        // open (the request server's tile list holds running ones too)
+        if (finished_only && (d.st->active || !d.st->open))
+            continue;
         const int row = tl.start + threadIdx.x;
         if (row >= d.nv)
             continue;

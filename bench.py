@@ -179,16 +179,29 @@ def ncu_traffic(kernel: str, iterations: float) -> float | None:
 
 
 def algorithmic_bytes(nv: int, nnzb: int) -> dict:
-    """Unique bytes one PCG iteration must move (FP32 6-float symmetric blocks,
-    int32 columns, float4 vectors):
-      SpMV phase   : 24*nnzb (A) + 4*nnzb (cols) + 4*nv (row info)
-                     + 16*nv (z) + 16*nv (p_old) + 16*nv (p write) + 16*nv (q write)
+    """Unique bytes one PCG iteration must move. The matrix is stored as its
+    diagonal and upper blocks (FP32, 6 floats per symmetric block); a lower
+    slot holds its column and the index of the transposed block:
+      SpMV phase   : 24*nnzb_up (A) + 4*nnzb (cols) + 4*nnzb_lo (transposed index)
+                     + 4*nv (row info) + 16*nv (z) + 16*nv (p_old)
+                     + 16*nv (p write) + 16*nv (q write)
       update phase : 16*nv (q) + 16*nv (dx) + 16*nv (r) + 24*nv (M^-1 read)
                      + 48*nv (dx, r, z write)   [p comes from shared memory]
+    with nnzb_up = (nnzb + nv) / 2 and nnzb_lo = (nnzb - nv) / 2.
     """
-    spmv = 28 * nnzb + 68 * nv
+    up, lo = (nnzb + nv) // 2, (nnzb - nv) // 2
+    spmv = 24 * up + 4 * nnzb + 4 * lo + 68 * nv
     update = 120 * nv
-    return {"spmv_dot": spmv, "update_dot": update, "iteration": spmv + update}
+    return {"spmv_dot": spmv, "update_dot": update, "iteration": spmv + update,
+            "matrix": 24 * up + 4 * nnzb + 4 * lo}
+
+
+def graph_loop_bytes(nv: int, nnzb: int) -> int:
+    """Unique bytes of one iteration of the two-kernel loop (k_spmv, k_update),
+    the batched and served solver: the matrix as above, k_spmv 68*nv (row info,
+    z, p_old, p and q writes), k_update 136*nv (p, q, dx, r, M^-1 reads; dx, r,
+    z writes)."""
+    return algorithmic_bytes(nv, nnzb)["matrix"] + 204 * nv
 
 
 def count_nnzb(n_side: int) -> int:
@@ -492,6 +505,190 @@ def run_batch(args):
     ctx.close()
 
 
+# ---------------------------------------------------------------- served
+def serve_workload(count=512, requests=20000, rate=2000.0, seed=21, material="base",
+                   pins="corners"):
+    """Served workload: `count` resident cloths with sides log-uniform in
+    [16, 256] vertices (16^2 .. 256^2 vertices) and a Poisson stream of
+    single-step requests (rate per second), each for a cloth drawn uniformly.
+    material "base": the single-cloth materials (stretch 1e3, shear 1e2);
+    "mixed": stretch log-uniform in [1e2, 1e4] as the batched workload.
+    pins "corners": the two top corners (the single-cloth setup); "edge": the
+    top edge (the batched setup)."""
+    rng = np.random.default_rng(seed)
+    sides = np.rint(np.exp(rng.uniform(np.log(16), np.log(256), count))).astype(int)
+    ks = np.exp(rng.uniform(np.log(1e2), np.log(1e4), count))
+    confs = []
+    for n, k in zip(sides, ks):
+        c = workload_conf(int(n))
+        if material == "mixed":
+            c["cloth_stretch_stiffness"] = [float(k), float(k), float(k) / 10]
+        if pins == "edge":
+            c.pop("constraints")
+        confs.append((int(n), c))
+    gaps = rng.exponential(1.0 / rate, requests)
+    arrivals = np.cumsum(gaps) - gaps[0]
+    which = rng.integers(0, count, requests)
+    return confs, arrivals, which
+
+
+def make_cloths_parallel(ctx, confs, seed=31, threads=8):
+    """Cloths with their pins (the configuration's static points, else the top
+    edge) and the seeded perturbation, created by a thread pool (host tables
+    are built outside the context lock)."""
+    from concurrent.futures import ThreadPoolExecutor
+    from acousticsim_gb300 import BaraffClothGpu
+
+    def one(i):
+        n, conf = confs[i]
+        c = BaraffClothGpu(ctx, conf)
+        if "constraints" not in conf:
+            c.AddConstraintStaticVertices([k * n + (n - 1) for k in range(n)])
+        x, xp = initial_state(c.GetInitPos(), seed + i)
+        c.SetPos(x)
+        c.SetPrePos(xp)
+        return c
+
+    with ThreadPoolExecutor(threads) as ex:
+        return list(ex.map(one, range(len(confs))))
+
+
+def latency_summary(lat_s) -> dict:
+    a = np.sort(np.asarray(lat_s, np.float64)) * 1e3
+    return {"p50_ms": float(np.percentile(a, 50)), "p90_ms": float(np.percentile(a, 90)),
+            "p99_ms": float(np.percentile(a, 99)), "max_ms": float(a[-1]),
+            "mean_ms": float(a.mean())}
+
+
+def replay_one_at_a_time(step, arrivals, which, now):
+    """FIFO, one request per launch: wait for the arrival, step, next."""
+    lat, t0 = [], now() + 0.05
+    for a, i in zip(arrivals, which):
+        t_arr = t0 + a
+        while now() < t_arr:
+            time.sleep(max(0.0, min(1e-3, t_arr - now())))
+        step(int(i))
+        lat.append(now() - t_arr)
+    t_end = now()
+    return lat, (t_end - t0 - 0.0)
+
+
+def run_serve(args):
+    """Poisson stream of single-step requests against resident cloths through
+    the continuous-batching server, against one launch per request (the plain
+    reference-structured PCG, and this library's own solver) on a prefix of
+    the same stream."""
+    import torch
+    from acousticsim_gb300 import ClothContext, ClothServer, params
+    from acousticsim_gb300 import build as b
+    b.build_all()
+    ctx = ClothContext(0)
+    confs, arrivals, which = serve_workload(args.serve_cloths, args.serve_requests,
+                                            args.serve_rate, material=args.serve_material,
+                                            pins=args.serve_pins)
+    p = params(max_iters=MAX_ITERS, rel_tol=REL_TOL)
+    now = ClothServer.now
+    t_build = time.perf_counter()
+    cloths = make_cloths_parallel(ctx, confs)
+    t_build = time.perf_counter() - t_build
+    budget = int(args.serve_budget_gb * (1 << 30))
+    srv = ClothServer(ctx, budget, args.serve_max_inflight, args.serve_chunk)
+    it_bytes = []
+    for c in cloths:
+        mi = c.matrix_info()
+        it_bytes.append(graph_loop_bytes(c.nv, mi["nnzb"]))
+        srv.add(c, 0.0, p)
+    srv.start()
+    clocks = ClockSampler(0)
+    # warm-up: a few requests, not timed
+    for i in range(min(8, len(cloths))):
+        srv.submit(i, -1 - i)
+    srv.drain(600.0)
+    srv.poll(cap=64)
+    clocks.start()
+    t0 = now() + 0.05
+    for tag, (a, i) in enumerate(zip(arrivals, which)):
+        t_arr = t0 + a
+        while True:
+            d = t_arr - now()
+            if d <= 0:
+                break
+            if d > 2e-3:
+                time.sleep(d - 1e-3)
+        srv.submit(int(i), tag, t_arr)
+    srv.drain(3600.0)
+    clk = clocks.stop()
+    res = srv.poll(cap=len(arrivals) + 64)
+    stats = srv.stats()
+    assert len(res) == len(arrivals), (len(res), stats)
+    bad = [r for r in res if r["status"] != "OK"]
+    lat = [r["t_done"] - r["t_arrival"] for r in res]
+    t_last = max(r["t_done"] for r in res)
+    served = len(res) / (t_last - t0)
+    iters = np.array([r["iters"] for r in res])
+    queue = [r["t_admit"] - r["t_arrival"] for r in res]
+    moved = float(sum(r["iters"] * it_bytes[r["cloth"]] for r in res))
+    row_iters = float(sum(r["iters"] * cloths[r["cloth"]].nv for r in res))
+    span = t_last - t0
+    srv.close()
+    # one launch per request, on a prefix of the same stream (fresh cloths)
+    pref = args.serve_sample
+    arr_p, which_p = arrivals[:pref], which[:pref]
+    need = sorted(set(int(i) for i in which_p))
+    base = {}
+    for name in ("plain", "fast"):
+        sub = make_cloths_parallel(ctx, [confs[i] for i in need])
+        by = dict(zip(need, sub))
+        pp = params(max_iters=100000, rel_tol=REL_TOL, check_every=10) if name == "plain" else p
+
+        def step(i, by=by, name=name, pp=pp):
+            st = (by[i].UpdatePosPlain(0.0, pp) if name == "plain" else by[i].UpdatePos(0.0, pp))
+            assert st["status"] == "OK", st
+        lat_b, span_b = replay_one_at_a_time(step, arr_p, which_p, now)
+        base[name] = {"solves_per_s": pref / span_b, "requests": pref,
+                      **latency_summary(lat_b)}
+        for c in sub:
+            c.close()
+    line = {
+        "metric": "served solves/s (continuous batching) @1e-6 rel residual",
+        "value": served, "unit": "solves/s", "n_gpus": 1, "higher_is_better": True,
+        "dtype": "f32 (FP64 PCG reductions)", "data": "synthetic",
+        "config": {"workload": f"{len(confs)} resident cloths, sides log-U[16,256], "
+                               + ("K log-U[1e2,1e4]" if args.serve_material == "mixed"
+                                  else "stretch 1e3 shear 1e2")
+                               + (", top edge pinned" if args.serve_pins == "edge"
+                                  else ", top corners pinned")
+                               + f", dt=2ms; Poisson {args.serve_rate:g} req/s, "
+                                 f"{len(arrivals)} requests",
+                   "budget_gb": args.serve_budget_gb, "chunk_iters": args.serve_chunk,
+                   "max_inflight": args.serve_max_inflight,
+                   "vertices_total": int(sum(n * n for n, _ in confs))},
+        "latency": latency_summary(lat),
+        "queue_wait": latency_summary(queue),
+        "failed_requests": len(bad),
+        "pcg_iters": {"mean": float(iters.mean()), "p50": float(np.median(iters)),
+                      "max": int(iters.max())},
+        "work": {"row_iterations_per_s": row_iters / span,
+                 "algorithmic_gb_per_solve": moved / len(res) / 1e9,
+                 "achieved_gbs": moved / span / 1e9,
+                 "hbm_peak_gbs": measured_peaks()["hbm_gbs"],
+                 "frac": moved / span / 1e9 / measured_peaks()["hbm_gbs"],
+                 "capacity_at_peak_solves_per_s":
+                     measured_peaks()["hbm_gbs"] * 1e9 / (moved / len(res)),
+                 "note": "PCG iteration bytes of the two-kernel loop (graph_loop_bytes) "
+                         "summed over the served requests, over the served span"},
+        "server": stats, "cloth_build_s": t_build, "clocks": clk,
+        "one_launch_per_request": base,
+        "speedup_vs_plain": served / base["plain"]["solves_per_s"],
+        "speedup_vs_one_at_a_time_fast": served / base["fast"]["solves_per_s"],
+    }
+    print(json.dumps(line), flush=True)
+    for c in cloths:
+        c.close()
+    ctx.close()
+    del torch
+
+
 def run_profile_case(args):
     """Small case for ncu: one step of the 512x512 workload with the PCG capped
     at --profile-iters iterations, kernels launched from the host."""
@@ -521,8 +718,19 @@ def main():
     ap.add_argument("--profile-iters", type=int, default=0,
                     help="run only the small ncu case: one step, PCG capped at N iterations")
     ap.add_argument("--solver", choices=["persistent", "graph_loop"], default=None)
-    ap.add_argument("--mode", choices=["step", "batch"], default="step",
-                    help="step: the 512x512 single-cloth headline; batch: 256 mixed cloths")
+    ap.add_argument("--mode", choices=["step", "batch", "serve"], default="step",
+                    help="step: the 512x512 single-cloth headline; batch: 256 mixed cloths; "
+                         "serve: Poisson request stream through the continuous-batching server")
+    ap.add_argument("--serve-cloths", type=int, default=512)
+    ap.add_argument("--serve-requests", type=int, default=20000)
+    ap.add_argument("--serve-rate", type=float, default=2000.0)
+    ap.add_argument("--serve-budget-gb", type=float, default=40.0)
+    ap.add_argument("--serve-chunk", type=int, default=16)
+    ap.add_argument("--serve-max-inflight", type=int, default=0)
+    ap.add_argument("--serve-material", choices=["base", "mixed"], default="base")
+    ap.add_argument("--serve-pins", choices=["corners", "edge"], default="corners")
+    ap.add_argument("--serve-sample", type=int, default=300,
+                    help="prefix of the stream replayed one request per launch")
     ap.add_argument("--batch-count", type=int, default=256)
     ap.add_argument("--batch-sample", type=int, default=32,
                     help="cloths timed one at a time for the unbatched comparisons")
@@ -532,6 +740,9 @@ def main():
         return
     if args.mode == "batch":
         run_batch(args)
+        return
+    if args.mode == "serve":
+        run_serve(args)
         return
     rank, world, local, pg = dist_init(args.gpus)
     if args.impl == "reference":

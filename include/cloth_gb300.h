@@ -154,6 +154,11 @@ int cloth_create(cloth_ctx *ctx, const cloth_mesh_desc *mesh,
                  const cloth_material *mat, cloth_t **out);
 int cloth_destroy(cloth_t *cloth);
 int cloth_num_vertices(const cloth_t *cloth, int *nv, int *nt, int *ne);
+/* Sparsity of the system matrix: nonzero 3x3 blocks (all of them, as the
+ * reference's ELL holds them), the widest row, and the bytes of device memory
+ * the cloth holds resident and per solve. */
+int cloth_matrix_info(const cloth_t *cloth, long long *nnzb, int *width,
+                      size_t *resident_bytes, size_t *solve_bytes);
 /* Changes stretch/bending stiffness and damping (the reference's ImGui sliders,
  * BaraffClothGpu.cpp:282-291, and UpdateBendingMatrix). */
 int cloth_set_material(cloth_t *cloth, const cloth_material *mat);
@@ -247,6 +252,85 @@ int cloth_step_plain(cloth_t *cloth, double dt, const cloth_solve_params *params
  * Each instance's result is bit-identical to stepping it alone. */
 int cloth_batch_step(cloth_ctx *ctx, cloth_t *const *cloths, int n, double dt,
                      const cloth_solve_params *params, cloth_solve_stats *stats);
+
+/* ---------------------------------------------------------------- serving */
+/* Request server with continuous batching. The reference steps one cloth per
+ * call on the host thread (cBaseCloth::Update -> UpdatePos,
+ * src/sim/cloth/BaseCloth.cpp, src/sim/cloth/BaraffClothGpu.cpp:203-262);
+ * this is the batch/serve variant over handle arrays.
+ *
+ * Registered cloths stay resident (mesh tables, ELL map, positions, the
+ * warm-start dx, pins); a step request needs per-solve work memory (triangle
+ * records, the assembled system, PCG vectors: about 1.1 KB per vertex) that
+ * the server hands out from one pool. The pool is the device-memory budget
+ * minus the resident bytes of the registered cloths and the server's own
+ * buffers. A worker thread runs the device in chunks of chunk_iters PCG
+ * iterations; between chunks it admits ready requests in arrival order while
+ * a slot (max_inflight) and pool memory are free, so their assembly and PCG
+ * run on the GPU beside requests already iterating, and it retires requests
+ * whose solve ended (the position update runs on the device). Requests for
+ * one cloth run one after another, in submission order. Every request's
+ * arithmetic is per instance and fixed-order, so its result is bit-identical
+ * to stepping that cloth alone with the graph-loop solver. */
+typedef struct cloth_server_s cloth_server;
+
+typedef struct {
+    size_t budget_bytes;   /* device bytes the server may hold (resident + pool + own) */
+    int max_inflight;      /* requests on the GPU at once (<= 0: no limit but memory) */
+    int chunk_iters;       /* PCG iterations per chunk between admissions (> 0) */
+} cloth_server_config;
+
+typedef struct {
+    long long tag;         /* caller's tag from cloth_server_submit */
+    int cloth;             /* index from cloth_server_add */
+    int status;            /* CLOTH_OK or the solve's per-instance status */
+    int iters;             /* PCG iterations of this step */
+    int pad;
+    double rel_residual;   /* ||r|| / ||b|| at exit (FP64 recurrence) */
+    double t_arrival;      /* cloth_server_now() clock, seconds */
+    double t_admit;        /* when the request joined a chunk */
+    double t_done;         /* when the worker saw the step finished */
+} cloth_server_result;
+
+typedef struct {
+    long long submitted, completed, chunks;
+    long long admitted_waits;   /* admissions deferred for lack of pool memory or slots */
+    int max_inflight_seen;
+    int registered;
+    size_t resident_bytes;      /* registered cloths' resident state */
+    size_t pool_bytes;          /* per-solve pool */
+    size_t pool_peak_bytes;     /* largest pool use seen */
+    size_t own_bytes;           /* the server's lists and descriptors */
+    size_t max_request_bytes;   /* work memory of the largest registered cloth's request */
+} cloth_server_stats;
+
+/* Monotonic clock of the server (seconds), for arrival times. */
+double cloth_server_now(void);
+int cloth_server_create(cloth_ctx *ctx, const cloth_server_config *cfg, cloth_server **out);
+/* Register a cloth (same ctx) with the dt and solve parameters its requests
+ * use (dt <= 0: the material's default timestep; params NULL: defaults). The
+ * cloth's own work memory is released; until the server is destroyed the
+ * cloth is stepped only through the server (get/set_pos work while it has no
+ * request queued or running). CLOTH_ERR_BUDGET when its resident bytes do not
+ * fit the budget. Only before cloth_server_start. */
+int cloth_server_add(cloth_server *srv, cloth_t *cloth, double dt,
+                     const cloth_solve_params *params, int *index);
+/* Allocate the pool (CLOTH_ERR_BUDGET when the largest registered cloth's
+ * work memory does not fit) and start the worker thread. */
+int cloth_server_start(cloth_server *srv);
+/* Queue one step of cloth `index`. t_arrival < 0: now. Thread-safe. */
+int cloth_server_submit(cloth_server *srv, int index, long long tag, double t_arrival);
+/* Completed requests, oldest first: waits up to wait_s seconds for at least
+ * one, returns at most cap in out and their count in *n. Thread-safe. */
+int cloth_server_poll(cloth_server *srv, cloth_server_result *out, int cap, int *n,
+                      double wait_s);
+/* Wait until every submitted request has completed (wait_s < 0: no limit);
+ * CLOTH_ERR_TIMEOUT when the time ran out. */
+int cloth_server_drain(cloth_server *srv, double wait_s);
+int cloth_server_get_stats(cloth_server *srv, cloth_server_stats *stats);
+/* Stop the worker (requests still queued are dropped), hand every cloth its
+ * own work memory back and free the server. */
+int cloth_server_destroy(cloth_server *srv);
 
 /* ---------------------------------------------------------------- no allocation */
 /* Allocation-free PCG solve. No counterpart in the reference: this entry point
