@@ -22,7 +22,8 @@ PHASE_NAMES = ["pins", "tri_assemble", "row_assemble", "spmv_dot", "update_dot",
 ELL_REF_WIDTH = 32
 SOLVER_PERSISTENT = 0
 SOLVER_GRAPH_LOOP = 1
-SOLVER_NAMES = {0: "persistent", 1: "graph_loop", -1: "plain"}
+SOLVER_FP64 = 2
+SOLVER_NAMES = {0: "persistent", 1: "graph_loop", 2: "fp64", -1: "plain"}
 
 
 class GridDesc(C.Structure):
@@ -57,6 +58,22 @@ class SolveStats(C.Structure):
                 "res_norm": self.res_norm, "rhs_norm": self.rhs_norm,
                 "rel_residual": self.rel_residual,
                 "solver": SOLVER_NAMES.get(self.solver, str(self.solver))}
+
+
+class RefineStats(C.Structure):
+    _fields_ = [("outer", C.c_int), ("inner_iters", C.c_int), ("status", C.c_int),
+                ("solver", C.c_int), ("initial_rel_residual", C.c_double),
+                ("rel_residual", C.c_double), ("last_inner_rel_residual", C.c_double),
+                ("rejected", C.c_int), ("pad", C.c_int)]
+
+    def as_dict(self) -> dict:
+        return {"outer": self.outer, "inner_iters": self.inner_iters,
+                "status": STATUS_NAMES.get(self.status, str(self.status)),
+                "solver": SOLVER_NAMES.get(self.solver, str(self.solver)),
+                "initial_rel_residual": self.initial_rel_residual,
+                "rel_residual": self.rel_residual,
+                "last_inner_rel_residual": self.last_inner_rel_residual,
+                "rejected": self.rejected}
 
 
 class ServerConfig(C.Structure):
@@ -143,6 +160,10 @@ SIGNATURES = {
     "cloth_pcg_solve_ell32_noalloc": (C.c_int, [C.c_int, P, P, P, P, P, C.c_int,
                                                 C.POINTER(SolveParams), C.POINTER(SolveStats),
                                                 P]),
+    "cloth_residual_fp64": (C.c_int, [P, PD]),
+    "cloth_solve_refined": (C.c_int, [P, C.POINTER(SolveParams), C.c_double, C.c_int,
+                                      C.POINTER(RefineStats)]),
+    "cloth_solve_fp64": (C.c_int, [P, C.POINTER(SolveParams), C.POINTER(SolveStats)]),
     "cloth_server_now": (C.c_double, []),
     "cloth_server_create": (C.c_int, [P, C.POINTER(ServerConfig), C.POINTER(P)]),
     "cloth_server_add": (C.c_int, [P, P, C.c_double, C.POINTER(SolveParams), PI]),

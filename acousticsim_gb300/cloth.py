@@ -287,6 +287,26 @@ class BaraffClothGpu:
                C.byref(st))
         return st.as_dict()
 
+    def solve_refined(self, inner: N.SolveParams, rel_tol: float = 1e-8,
+                      max_outer: int = 20) -> dict:
+        """FP32 PCG corrections inside an FP64 residual loop (after assemble)."""
+        st = N.RefineStats()
+        N.call("cloth_solve_refined", self._h, C.byref(inner), float(rel_tol), int(max_outer),
+               C.byref(st))
+        return st.as_dict()
+
+    def solve_fp64(self, params: N.SolveParams) -> dict:
+        """All-FP64 block-Jacobi PCG from zero (after assemble)."""
+        st = N.SolveStats()
+        N.call("cloth_solve_fp64", self._h, C.byref(params), C.byref(st))
+        return st.as_dict()
+
+    def residual_fp64(self) -> float:
+        """||b - A dx|| / ||b|| in FP64 for the current dx."""
+        v = C.c_double()
+        N.call("cloth_residual_fp64", self._h, C.byref(v))
+        return float(v.value)
+
     def advance(self) -> None:
         N.call("cloth_advance", self._h)
 

@@ -990,6 +990,7 @@ void end_step(const std::vector<cloth_s *> &members)
             c->pins_dirty = true;
         }
         c->assembled = false;
+        c->dx64_valid = false;
     }
 }
 
@@ -1033,6 +1034,39 @@ Batch *self_batch(cloth_s *c, int *rc)
         *rc = make_batch(c->ctx, {c}, c->self);
     return c->self.get();
 }
+
+} // namespace
+
+int cloth::detail::inner_solve(cloth_s *c, const double *rhs64, const cloth_solve_params *p,
+                               cloth_solve_stats *stats)
+{
+    int rc;
+    Batch *b = self_batch(c, &rc);
+    if (rc != CLOTH_OK)
+        return rc;
+    set_params(c, p);
+    rc = sync_desc(c);
+    if (rc != CLOTH_OK)
+        return rc;
+    cudaStream_t s = c->ctx->stream;
+    CK(cudaMemsetAsync(&b->d_ctl->n_active, 0, sizeof(int), s));
+    k_ir_start<<<b->grid_row, kTile, 0, s>>>(b->d_descs, b->d_rt, b->d_ctl, rhs64);
+    CK(cudaGetLastError());
+    if (c->ctx->prof)
+        rc = launch_solve_host(b, c->h.max_iters);
+    else
+    {
+        if (!b->solve_exec)
+            rc = build_graph(b, false, &b->solve_exec);
+        if (rc == CLOTH_OK && cudaGraphLaunch(b->solve_exec, s) != cudaSuccess)
+            rc = fail(CLOTH_ERR_CUDA, "cudaGraphLaunch failed");
+    }
+    if (rc != CLOTH_OK)
+        return rc;
+    return read_stats(b, stats);
+}
+
+namespace {
 
 bool valid_params(const cloth_solve_params *p)
 {
@@ -1119,6 +1153,7 @@ int cloth_ctx_destroy(cloth_ctx *ctx)
         for (auto *c : std::vector<cloth_s *>(ctx->cloths))
         {
             c->self.reset();
+            f64_free(c);
             if (c->arena)
                 cudaFree(c->arena);
             if (c->scratch)
@@ -1396,6 +1431,7 @@ int cloth_destroy(cloth_t *c)
                 break;
             }
     c->self.reset();
+    f64_free(c);
     if (c->arena)
         cudaFree(c->arena);
     if (c->scratch)
@@ -1627,7 +1663,11 @@ int cloth_assemble(cloth_t *c, double dt)
     if (rc == CLOTH_OK)
         rc = launch_assemble(b);
     if (rc == CLOTH_OK)
+    {
         c->assembled = true;
+        c->dx64_valid = false;
+        c->pcg_stale = false;
+    }
     return rc;
 }
 
@@ -1638,6 +1678,9 @@ int cloth_solve(cloth_t *c, const cloth_solve_params *params, cloth_solve_stats 
     std::lock_guard<std::recursive_mutex> lk(c->ctx->mu);
     if (!c->assembled)
         return fail(CLOTH_ERR_STATE, "cloth_solve: call cloth_assemble first");
+    if (c->pcg_stale)
+        return fail(CLOTH_ERR_STATE, "cloth_solve: a refined or FP64 solve replaced the PCG "
+                                     "start; call cloth_assemble again");
     CK(cudaSetDevice(c->ctx->device));
     int rc;
     Batch *b = self_batch(c, &rc);
@@ -1649,6 +1692,7 @@ int cloth_solve(cloth_t *c, const cloth_solve_params *params, cloth_solve_stats 
     rc = sync_desc(c);
     if (rc != CLOTH_OK)
         return rc;
+    c->dx64_valid = false;
     if (c->ctx->prof)
         rc = launch_solve_host(b, c->h.max_iters);
     else
@@ -1673,7 +1717,8 @@ int cloth_advance(cloth_t *c)
     Batch *b = self_batch(c, &rc);
     if (rc != CLOTH_OK)
         return rc;
-    rc = launch_advance(b);
+    // the FP64 result of a refined or FP64 solve, else the FP32 dx
+    rc = c->dx64_valid ? f64_advance(c) : launch_advance(b);
     end_step({c});
     return rc;
 }
@@ -1704,6 +1749,8 @@ int cloth_get_dx(cloth_t *c, double *dx, int nv)
         return fail(CLOTH_ERR_INVALID, "bad argument");
     std::lock_guard<std::recursive_mutex> lk(c->ctx->mu);
     CK(cudaSetDevice(c->ctx->device));
+    if (c->dx64_valid)
+        return f64_get_dx(c, dx, nv);
     std::vector<float4> v(nv);
     CK(cudaStreamSynchronize(c->ctx->stream));
     CK(cudaMemcpy(v.data(), c->h.dx, size_t(nv) * sizeof(float4), cudaMemcpyDeviceToHost));

@@ -29,6 +29,8 @@ __global__ void k_update(InstDesc *const *descs, const Tile *tiles, BatchCtl *ct
 __global__ void k_advance(InstDesc *const *descs, const Tile *tiles,
                           const BatchCtl *ctl, int finished_only);
 __global__ void k_sync_x32(InstDesc *d);
+__global__ void k_ir_start(InstDesc *const *descs, const Tile *tiles, BatchCtl *ctl,
+                           const double *rhs64);
 __global__ void k_pcg_persistent_sm(InstDesc *const *descs, const TeamBlock *work,
                                     int halo_cap, int rows_cap);
 __global__ void k_pcg_persistent_gm(InstDesc *const *descs, const TeamBlock *work,
@@ -86,6 +88,7 @@ struct Batch;
 } // namespace cloth
 
 struct cloth_server_s;
+struct cloth_f64_s;
 
 struct cloth_ctx_s
 {
@@ -126,6 +129,9 @@ struct cloth_s
     cloth::ScratchLayout sl;
     int width_up = 1;         // planes of the stored (diagonal + upper) blocks
     cloth_server_s *server = nullptr;
+    cloth_f64_s *f64 = nullptr; // FP64 work arrays (refinement, FP64 PCG), on first use
+    bool dx64_valid = false;    // the last solve left an FP64 dx (refined or FP64 PCG)
+    bool pcg_stale = false;     // the FP32 PCG start of the assembly was overwritten
     cloth::InstDesc h;        // host copy of the descriptor
     cloth::InstDesc *d_desc = nullptr;
     cloth::InstState *d_state = nullptr;
@@ -153,6 +159,14 @@ void set_params(cloth_s *c, const cloth_solve_params *p);
 void set_dt(cloth_s *c, double dt);
 int sync_pins(cloth_s *c);
 int sync_desc(cloth_s *c);
+// FP32 PCG solve of A e = float(rhs64) from e = 0 on the cloth's own launch set
+// (the correction step of iterative refinement); e is left in dx.
+int inner_solve(cloth_s *c, const double *rhs64, const cloth_solve_params *p,
+                cloth_solve_stats *stats);
+// FP64 result handling (precision.cu)
+void f64_free(cloth_s *c);
+int f64_advance(cloth_s *c);
+int f64_get_dx(cloth_s *c, double *dx, int nv);
 // A server's view of one of its cloths: true while requests are queued or running.
 bool server_busy(const cloth_server_s *s, const cloth_s *c);
 // Detach every cloth of a server and free it (context teardown).

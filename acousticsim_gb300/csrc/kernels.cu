@@ -213,6 +213,49 @@ __device__ __forceinline__ bool test_converged(const InstDesc &d,
     return ok;
 }
 
+// PCG start bookkeeping of one instance (thread 0 of its last tile): FP64
+// scalars from the start sums tot = (r.z, r.r, b.b), counters, the team
+// barrier and team-sum buffers of the persistent solver, the active flag.
+__device__ __forceinline__ void begin_solve(const InstDesc &d, const double (&tot)[3],
+                                            BatchCtl *ctl)
+{
+    InstState &st = *d.st;
+    st.ticket = 0u;
+    st.rho = tot[0];
+    st.rr = tot[1];
+    st.rr0 = tot[1];
+    st.bb = tot[2];
+    st.beta = 0.0;
+    st.alpha = 0.0;
+    st.pq = 0.0;
+    st.iter = 0;
+    st.status = 0;
+    st.bar_count = 0u;
+    st.bar_err = 0;
+    st.open = 1;
+    for (int bq = 0; bq < 3; bq++)
+        for (int q = 0; q < 3; q++)
+        {
+            st.acc[bq][q][0] = 0ull;
+            st.acc[bq][q][1] = 0ull;
+            st.acc_chk[bq][q] = 0.f;
+        }
+    if (!isfinite(tot[0]) || !isfinite(tot[1]) || !isfinite(tot[2]))
+    {
+        st.status = 6; // CLOTH_ERR_NAN
+        st.active = 0;
+    }
+    else if (d.max_iters <= 0 || test_converged(d, st, tot[1]))
+    {
+        st.active = 0;
+    }
+    else
+    {
+        st.active = 1;
+        atomicAdd(&ctl->n_active, 1);
+    }
+}
+
 // An instance leaves the loop: the thread that retires the last active one
 // clears the graph's while condition.
 __device__ __forceinline__ void retire(BatchCtl *ctl, bool use_cond,
@@ -478,43 +521,47 @@ __global__ void __launch_bounds__(kTile) k_row(InstDesc *const *descs,
         double tot[3];
         if (tile_reduce<3>(d, tl.start / kTile, part, tot, sh, &flag) &&
             threadIdx.x == 0)
+            begin_solve(d, tot, ctl);
+    }
+}
+
+// PCG start of an iterative-refinement correction: the system is the
+// assembled A with right-hand side float(rhs64) (zero on pinned rows), from
+// dx = 0.  Same bookkeeping as the start k_row makes.
+__global__ void __launch_bounds__(kTile) k_ir_start(InstDesc *const *descs,
+                                                    const Tile *tiles, BatchCtl *ctl,
+                                                    const double *rhs64)
+{
+    __shared__ double sh[3][kTile / 32];
+    __shared__ int flag;
+    const int ntiles = ctl->n_tiles_rows;
+    for (int ti = blockIdx.x; ti < ntiles; ti += gridDim.x)
+    {
+        const Tile tl = tiles[ti];
+        const InstDesc &d = *descs[tl.inst];
+        const int row = tl.start + threadIdx.x;
+        float part[3] = {0.f, 0.f, 0.f};
+        if (row < d.nv)
         {
-            InstState &st = *d.st;
-            st.ticket = 0u;
-            st.rho = tot[0];
-            st.rr = tot[1];
-            st.rr0 = tot[1];
-            st.bb = tot[2];
-            st.beta = 0.0;
-            st.alpha = 0.0;
-            st.pq = 0.0;
-            st.iter = 0;
-            st.status = 0;
-            st.bar_count = 0u;
-            st.bar_err = 0;
-            st.open = 1;
-            for (int bq = 0; bq < 3; bq++)
-                for (int q = 0; q < 3; q++)
-                {
-                    st.acc[bq][q][0] = 0ull;
-                    st.acc[bq][q][1] = 0ull;
-                    st.acc_chk[bq][q] = 0.f;
-                }
-            if (!isfinite(tot[0]) || !isfinite(tot[1]) || !isfinite(tot[2]))
-            {
-                st.status = 6; // CLOTH_ERR_NAN
-                st.active = 0;
-            }
-            else if (d.max_iters <= 0 || test_converged(d, st, tot[1]))
-            {
-                st.active = 0;
-            }
-            else
-            {
-                st.active = 1;
-                atomicAdd(&ctl->n_active, 1);
-            }
+            const bool fixv = d.x32[row].w != 0.f;
+            float3 r = make_float3(float(rhs64[3 * row + 0]), float(rhs64[3 * row + 1]),
+                                   float(rhs64[3 * row + 2]));
+            if (fixv)
+                r = make_float3(0, 0, 0);
+            float M[6];
+            load_sym(d.M0, d.M1, row, M);
+            const float3 z = symv(M, r);
+            d.dx[row] = make_float4(0, 0, 0, 0);
+            d.r[row] = f4(r);
+            d.z[row] = f4(z);
+            part[0] = fdot(r, z);
+            part[1] = fdot(r, r);
+            part[2] = part[1];
         }
+        double tot[3];
+        if (tile_reduce<3>(d, tl.start / kTile, part, tot, sh, &flag) &&
+            threadIdx.x == 0)
+            begin_solve(d, tot, ctl);
     }
 }
 
@@ -592,7 +639,8 @@ __global__ void __launch_bounds__(kTile) k_spmv(InstDesc *const *descs,
             else if (tot[0] == 0.0)
             {
                 // PCGSolver.cu:259-263 clamps alpha to zero; nothing moves
-                // afterwards, so the loop ends here.
+                // afterwards, so the loop ends here. (p.Ap < 0 goes on with a
+                // negative alpha, as the reference does.)
                 st.status = 7;
                 st.active = 0;
                 retire(ctl, use_cond, h);

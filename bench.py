@@ -689,6 +689,118 @@ def run_serve(args):
     del torch
 
 
+# ---------------------------------------------------------------- precision stress
+def precision_conf(n: int, k_stretch: float = 1e4, k_bend: float = 1e-3) -> dict:
+    """Ill-conditioned step: stretch k_stretch (shear a tenth) over bending
+    k_bend, a stiffness ratio of 1e7 by default, dt = 10 ms; the single-cloth
+    setup otherwise."""
+    c = workload_conf(n, dt=1e-2)
+    c["cloth_stretch_stiffness"] = [k_stretch, k_stretch, k_stretch / 10]
+    c["cloth_bending_stiffness"] = [k_bend, k_bend]
+    return c
+
+
+def sparse_direct(sysd):
+    """FP64 sparse LU (SuperLU, minimum-degree ordering) of an exported system."""
+    import scipy.sparse as sp
+    import scipy.sparse.linalg as spl
+    ell, A = sysd["ell"], sysd["A"].astype(np.float64)
+    nv, W = ell.shape
+    rows, cols, vals = [], [], []
+    for s in range(W):
+        m = ell[:, s] >= 0
+        v = np.nonzero(m)[0]
+        cc = ell[m, s]
+        for a in range(3):
+            for b in range(3):
+                rows.append(3 * v + a)
+                cols.append(3 * cc + b)
+                vals.append(A[m, s, a, b])
+    M = sp.csc_matrix((np.concatenate(vals), (np.concatenate(rows), np.concatenate(cols))),
+                      shape=(3 * nv, 3 * nv))
+    b = sysd["b"].astype(np.float64).reshape(-1)
+    return spl.splu(M, permc_spec="MMD_AT_PLUS_A").solve(b)
+
+
+def precision_case(ctx, n, inner_tol, tol, ref_tol, direct: bool, fp32_cap: int,
+                   k_stretch=1e4, k_bend=1e-3):
+    """One assembled ill-conditioned system of an n x n cloth solved four ways:
+    FP32 PCG alone, FP32 PCG inside FP64 iterative refinement, all-FP64 PCG,
+    and a reference: a sparse direct solve in FP64 on the host (direct=True)
+    or the FP64 PCG run to ref_tol (ref_tol > 0)."""
+    from acousticsim_gb300 import BaraffClothGpu, params
+    cloth = BaraffClothGpu(ctx, precision_conf(n, k_stretch, k_bend))
+    x0, xp0 = initial_state(cloth.GetInitPos(), 77, dt=1e-2)
+    cloth.SetPos(x0)
+    cloth.SetPrePos(xp0)
+    cloth.assemble(1e-2)
+    rel = lambda a, b: float(np.linalg.norm(a - b) / np.linalg.norm(b))
+    out = {"grid": n, "vertices": n * n, "stretch": k_stretch, "bending": k_bend}
+    t = time.perf_counter()
+    st = cloth.solve(params(max_iters=fp32_cap, rel_tol=tol))
+    out["fp32_pcg"] = {"seconds": time.perf_counter() - t, "iters": st["iters"],
+                       "status": st["status"], "solver": st["solver"],
+                       "recurrence_rel_residual": st["rel_residual"],
+                       "fp64_rel_residual": cloth.residual_fp64()}
+    t = time.perf_counter()
+    st = cloth.solve_refined(params(max_iters=200000, rel_tol=inner_tol), tol, 40)
+    out["refined"] = {"seconds": time.perf_counter() - t, **st,
+                      "inner_rel_tol": inner_tol}
+    dx_ir = cloth.get_dx()
+    t = time.perf_counter()
+    st = cloth.solve_fp64(params(max_iters=200000, rel_tol=tol))
+    out["fp64_pcg"] = {"seconds": time.perf_counter() - t, "iters": st["iters"],
+                       "status": st["status"], "fp64_rel_residual": cloth.residual_fp64()}
+    dx_64 = cloth.get_dx()
+    out["refined_vs_fp64_pcg"] = rel(dx_ir, dx_64)
+    if direct:
+        t = time.perf_counter()
+        # the exported system is the assembled one; the PCG state does not matter
+        cloth.assemble(1e-2)
+        x_d = sparse_direct(cloth.export_system())
+        out["direct"] = {"seconds_host": time.perf_counter() - t,
+                         "refined_error": rel(dx_ir, x_d), "fp64_pcg_error": rel(dx_64, x_d)}
+    elif ref_tol > 0:
+        t = time.perf_counter()
+        st = cloth.solve_fp64(params(max_iters=300000, rel_tol=ref_tol))
+        x_ref = cloth.get_dx()
+        out["fp64_reference"] = {"rel_tol": ref_tol, "iters": st["iters"],
+                                 "seconds": time.perf_counter() - t,
+                                 "refined_error": rel(dx_ir, x_ref),
+                                 "fp64_pcg_error": rel(dx_64, x_ref)}
+    cloth.close()
+    return out
+
+
+def run_precision(args):
+    """Precision stress (1024x1024, stiffness ratio 1e7, dt = 10 ms): FP32 PCG
+    inside FP64 iterative refinement to 1e-8 against all-FP64 PCG, with
+    errors against a high-accuracy FP64 solution at full size and against a
+    sparse direct solve at --prec-direct-side."""
+    from acousticsim_gb300 import ClothContext
+    from acousticsim_gb300 import build as b
+    b.build_all()
+    ctx = ClothContext(0)
+    big = precision_case(ctx, args.prec_side, args.prec_inner_tol, 1e-8, 1e-12, False,
+                         args.prec_fp32_cap)
+    # the same ratio with the single-cloth stretch stiffness (1e3 / 1e-4): a
+    # ten times better conditioned system
+    milder = precision_case(ctx, args.prec_side, args.prec_inner_tol, 1e-8, 0.0, False,
+                            args.prec_fp32_cap, k_stretch=1e3, k_bend=1e-4)
+    small = precision_case(ctx, args.prec_direct_side, args.prec_inner_tol, 1e-8, 0.0,
+                           True, args.prec_fp32_cap)
+    line = {"metric": f"precision stress: seconds to 1e-8 FP64 residual, {args.prec_side}^2, "
+                      "stiffness ratio 1e7, dt 10 ms (refined FP32 PCG)",
+            "value": big["refined"]["seconds"], "unit": "s", "n_gpus": 1,
+            "higher_is_better": False, "dtype": "f32 PCG inside f64 refinement",
+            "data": "synthetic (seeded perturbation)",
+            "refined_reached_tol": big["refined"]["status"] == "OK",
+            "speedup_vs_fp64_pcg": big["fp64_pcg"]["seconds"] / big["refined"]["seconds"],
+            "full_size": big, "full_size_stretch_1e3": milder, "direct_check": small}
+    print(json.dumps(line), flush=True)
+    ctx.close()
+
+
 def run_profile_case(args):
     """Small case for ncu: one step of the 512x512 workload with the PCG capped
     at --profile-iters iterations, kernels launched from the host."""
@@ -718,7 +830,7 @@ def main():
     ap.add_argument("--profile-iters", type=int, default=0,
                     help="run only the small ncu case: one step, PCG capped at N iterations")
     ap.add_argument("--solver", choices=["persistent", "graph_loop"], default=None)
-    ap.add_argument("--mode", choices=["step", "batch", "serve"], default="step",
+    ap.add_argument("--mode", choices=["step", "batch", "serve", "precision"], default="step",
                     help="step: the 512x512 single-cloth headline; batch: 256 mixed cloths; "
                          "serve: Poisson request stream through the continuous-batching server")
     ap.add_argument("--serve-cloths", type=int, default=512)
@@ -727,6 +839,10 @@ def main():
     ap.add_argument("--serve-budget-gb", type=float, default=40.0)
     ap.add_argument("--serve-chunk", type=int, default=16)
     ap.add_argument("--serve-max-inflight", type=int, default=0)
+    ap.add_argument("--prec-side", type=int, default=1024)
+    ap.add_argument("--prec-direct-side", type=int, default=256)
+    ap.add_argument("--prec-inner-tol", type=float, default=1e-4)
+    ap.add_argument("--prec-fp32-cap", type=int, default=100000)
     ap.add_argument("--serve-material", choices=["base", "mixed"], default="base")
     ap.add_argument("--serve-pins", choices=["corners", "edge"], default="corners")
     ap.add_argument("--serve-sample", type=int, default=300,
@@ -743,6 +859,9 @@ def main():
         return
     if args.mode == "serve":
         run_serve(args)
+        return
+    if args.mode == "precision":
+        run_precision(args)
         return
     rank, world, local, pg = dist_init(args.gpus)
     if args.impl == "reference":

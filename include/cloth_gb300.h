@@ -103,6 +103,7 @@ typedef struct {
  * iteration inside a CUDA-graph while loop with a device-side condition. */
 #define CLOTH_SOLVER_PERSISTENT 0
 #define CLOTH_SOLVER_GRAPH_LOOP 1
+#define CLOTH_SOLVER_FP64 2       /* cloth_solve_fp64 */
 
 /* ---------------------------------------------------------------- library */
 int cloth_abi_version(void);
@@ -242,6 +243,41 @@ int cloth_export_tables(const cloth_t *cloth, int *stencil, float *coef,
  * iteration). params NULL = the reference's settings (100 iterations,
  * ||r|| < 1e-10 absolute, checked every 10). The cloth's state is updated. */
 int cloth_step_plain(cloth_t *cloth, double dt, const cloth_solve_params *params,
+                     cloth_solve_stats *stats);
+
+/* ---------------------------------------------------------------- precision */
+/* FP64 checks and solvers on the assembled system (after cloth_assemble). The
+ * system is the assembled one: FP32 blocks and right-hand side, exact in FP64.
+ * The reference solves it in FP32 only (PCGSolver::Solve,
+ * src/sim/cloth/gpu_solvers/PCGSolver.cu:332-481); its FP64 counterparts are
+ * the CPU path's Eigen solvers (src/utils/SparseUtil.h). */
+typedef struct {
+    int outer;                     /* refinement steps (FP32 corrections) */
+    int inner_iters;               /* FP32 PCG iterations over all corrections */
+    int status;                    /* CLOTH_OK: reached rel_tol; MAXITER; NAN; BREAKDOWN */
+    int solver;                    /* driver of the FP32 corrections */
+    double initial_rel_residual;   /* ||b|| relative residual of dx = 0 (= 1) */
+    double rel_residual;           /* final ||b - A dx|| / ||b||, FP64 */
+    double last_inner_rel_residual;
+    int rejected;                  /* corrections undone (failed, or raised the residual) */
+    int pad;
+} cloth_refine_stats;
+
+/* ||b - A dx|| / ||b|| with the residual formed in FP64 (dx: the FP64 result
+ * of the last refined or FP64 solve, else the FP32 dx). */
+int cloth_residual_fp64(cloth_t *cloth, double *rel_residual);
+/* Mixed-precision iterative refinement: dx = 0; repeat r = b - A dx in FP64;
+ * stop when ||r|| <= rel_tol ||b||; solve A e = float(r) with the FP32 PCG
+ * (inner: its iteration cap and relative tolerance); dx += e in FP64. At most
+ * max_outer corrections. A correction whose FP32 solve fails (NaN, p.Ap = 0)
+ * or that does not lower the FP64 residual is undone and retried with half
+ * the inner iterations. The FP64 dx is what cloth_get_dx and cloth_advance
+ * use afterwards. */
+int cloth_solve_refined(cloth_t *cloth, const cloth_solve_params *inner, double rel_tol,
+                        int max_outer, cloth_refine_stats *stats);
+/* All-FP64 block-Jacobi PCG (FP64 vectors, FP64 inverse diagonal blocks, FP64
+ * reductions) from dx = 0, for comparison; recurrence residual in stats. */
+int cloth_solve_fp64(cloth_t *cloth, const cloth_solve_params *params,
                      cloth_solve_stats *stats);
 
 /* ---------------------------------------------------------------- batch */
