@@ -123,6 +123,10 @@ SIGNATURES = {
     "cloth_ctx_reset_profile": (C.c_int, [P]),
     "cloth_ctx_set_solver": (C.c_int, [P, C.c_int]),
     "cloth_ctx_device_bytes": (C.c_int, [P, C.POINTER(C.c_size_t)]),
+    "cloth_ctx_set_kernel_variant": (C.c_int, [P, C.c_int, C.c_int, C.c_int, C.c_int,
+                                               C.c_int, C.c_int]),
+    "cloth_ctx_get_kernel_variant": (C.c_int, [P, PI, PI, PI, PI, PI, PI]),
+    "cloth_ctx_get_tuning_times": (C.c_int, [P, PF, C.c_int, PF, C.c_int]),
     "cloth_ctx_get_stream": (C.c_int, [P, C.POINTER(P)]),
     "cloth_grid_build": (C.c_int, [C.POINTER(GridDesc), PI, PI, PI, PD, PF, PI, PI]),
     "cloth_host_tables": (C.c_int, [C.POINTER(MeshDesc), C.POINTER(Material), PI, PI, PI, PI, PF,

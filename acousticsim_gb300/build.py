@@ -28,8 +28,11 @@ ORACLE_LIB = ORACLE_DIR / "libcloth_oracle.so"
 INCLUDE = ROOT / "include"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+# --fmad=false: no implicit multiply-add contraction in device code, so a
+# result does not depend on how the compiler shaped a kernel variant (fused
+# multiply-adds are written out as fmaf where they are wanted)
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC",
-              "-Xcompiler", "-ffp-contract=off", "--expt-relaxed-constexpr"]
+              "-Xcompiler", "-ffp-contract=off", "--fmad=false", "--expt-relaxed-constexpr"]
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall"]
 
 

@@ -49,6 +49,30 @@ class ClothContext:
         code = {"persistent": N.SOLVER_PERSISTENT, "graph_loop": N.SOLVER_GRAPH_LOOP}[solver]
         N.call("cloth_ctx_set_solver", self._h, code)
 
+    SPMV_VARIANTS = [(1, 1, 1), (1, 2, 1), (1, 3, 1), (2, 1, 1), (2, 2, 1), (4, 1, 1),
+                     (1, 1, 4), (1, 2, 4), (2, 1, 4), (2, 2, 4), (4, 1, 4), (2, 1, 8)]
+    UPDATE_VARIANTS = [(1, 1), (2, 1), (4, 1), (1, 4), (2, 4), (1, 8), (2, 8)]
+
+    def set_kernel_variant(self, spmv=(1, 3, 1), update=(1, 1), autotune: bool = False) -> None:
+        """Graph-loop kernels: spmv = (rows per thread, slot unroll, tiles per block),
+        update = (rows per thread, tiles per block)."""
+        N.call("cloth_ctx_set_kernel_variant", self._h, *map(int, spmv), *map(int, update),
+               int(bool(autotune)))
+
+    def kernel_variant(self) -> dict:
+        v = [C.c_int() for _ in range(6)]
+        N.call("cloth_ctx_get_kernel_variant", self._h, *[C.byref(x) for x in v])
+        return {"spmv": tuple(x.value for x in v[:3]), "update": (v[3].value, v[4].value),
+                "autotune": bool(v[5].value)}
+
+    def tuning_times(self) -> dict:
+        """Per-variant kernel times (ms) of the last autotuning."""
+        a = (C.c_float * len(self.SPMV_VARIANTS))()
+        b = (C.c_float * len(self.UPDATE_VARIANTS))()
+        N.call("cloth_ctx_get_tuning_times", self._h, a, len(a), b, len(b))
+        return {"spmv": {"R%dU%dT%d" % v: a[i] for i, v in enumerate(self.SPMV_VARIANTS)},
+                "update": {"R%dT%d" % v: b[i] for i, v in enumerate(self.UPDATE_VARIANTS)}}
+
     def stream_ptr(self) -> int:
         s = C.c_void_p()
         N.call("cloth_ctx_get_stream", self._h, C.byref(s))

@@ -62,7 +62,24 @@ struct Batch
     Tile *d_rt = nullptr, *d_tt = nullptr;
     BatchCtl *d_ctl = nullptr;
     int n_rt = 0, n_tt = 0;
-    int grid_tri = 1, grid_row = 1, grid_spmv = 1, grid_update = 1;
+    int grid_tri = 1, grid_row = 1;
+    // graph-loop kernel variants (autotuned on the first step) and their grids
+    int spmv_v = kDefaultSpmvVariant, upd_v = kDefaultUpdateVariant;
+    bool tuned = false;
+    int grid_spmv = 1, grid_update = 1;
+    void set_variants(int sv, int uv)
+    {
+        spmv_v = sv;
+        upd_v = uv;
+        grid_spmv = grid_for(kSpmvVariants[sv], ctx->occ_spmv[sv]);
+        grid_update = grid_for(kUpdateVariants[uv], ctx->occ_update[uv]);
+    }
+    // one block per group of TPB tiles while that fits in a few waves
+    int grid_for(const GraphLoopVariant &v, int occ) const
+    {
+        const int groups = (n_rt + v.tiles_per_block - 1) / v.tiles_per_block;
+        return std::max(1, std::min(groups, ctx->num_sms * occ * 8));
+    }
     // persistent solver plan
     bool persist_ok = false;
     bool persist_sm = false; // own-row state in shared memory
@@ -178,7 +195,7 @@ int upload_tables(cloth_s *c)
     size_t o_tri = L.take<int4>(T), o_tcoef = L.take<float4>(3 * size_t(T)),
            o_tdest = L.take<int4>(3 * size_t(T));
     size_t o_col = L.take<int>(WS), o_hsrc = L.take<uint32_t>(WS), o_kb = L.take<float>(WS),
-           o_lidx = L.take<uint32_t>(WlS);
+           o_lidx = L.take<uint32_t>(WlS), o_colu = L.take<int>(WuS);
     size_t o_rowinfo = L.take<int>(n), o_fptr = L.take<int>(n + 1),
            o_mass = L.take<float>(n), o_grav = L.take<float>(n);
     size_t o_pv = L.take<int>(n + 1), o_pt = L.take<float4>(n + 1);
@@ -245,7 +262,7 @@ int upload_tables(cloth_s *c)
         tdest[3 * i + 1] = make_int4(hd[4], hd[5], hd[6], hd[7]);
         tdest[3 * i + 2] = make_int4(hd[8], fd[0], fd[1], fd[2]);
     }
-    std::vector<int> col(WS, 0), rowinfo(n);
+    std::vector<int> col(WS, 0), colu(WuS, 0), rowinfo(n);
     std::vector<uint32_t> hsrc(WS, 0u), lidx(WlS, 0u);
     std::vector<float> kb(WS, 0.f), mass(n), grav(n);
     for (int v = 0; v < n; v++)
@@ -259,6 +276,8 @@ int upload_tables(cloth_s *c)
             col[o] = t.cols[k];
             hsrc[o] = (uint32_t(t.h_start[k]) << 5) | uint32_t(t.h_count[k]);
             kb[o] = t.kbend[k];
+            if (sl >= t.diag_slot[v])
+                colu[size_t(sl - t.diag_slot[v]) * S + v] = t.cols[k];
             if (sl < t.diag_slot[v])
             {
                 // transposed block: row cols[k], the slot holding column v
@@ -291,6 +310,8 @@ int upload_tables(cloth_s *c)
                        cudaMemcpyHostToDevice, s));
     CK(cudaMemcpyAsync(base + o_lidx, lidx.data(), WlS * sizeof(uint32_t),
                        cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(base + o_colu, colu.data(), WuS * sizeof(int),
+                       cudaMemcpyHostToDevice, s));
     CK(cudaMemcpyAsync(base + o_rowinfo, rowinfo.data(), n * sizeof(int),
                        cudaMemcpyHostToDevice, s));
     CK(cudaMemcpyAsync(base + o_fptr, t.f_rowptr.data(), (n + 1) * sizeof(int),
@@ -312,6 +333,8 @@ int upload_tables(cloth_s *c)
     h.nt = T;
     h.width = W;
     h.stride = S;
+    h.width_lo = Wl;
+    h.width_up = Wu;
     h.ntile_rows = ntr;
     h.ntile_tris = ntt;
     h.tri = reinterpret_cast<const int4 *>(base + o_tri);
@@ -321,6 +344,7 @@ int upload_tables(cloth_s *c)
     h.hsrc = reinterpret_cast<const uint32_t *>(base + o_hsrc);
     h.kb = reinterpret_cast<const float *>(base + o_kb);
     h.lidx = reinterpret_cast<const uint32_t *>(base + o_lidx);
+    h.colu = reinterpret_cast<const int *>(base + o_colu);
     h.rowinfo = reinterpret_cast<const int *>(base + o_rowinfo);
     h.fptr = reinterpret_cast<const int *>(base + o_fptr);
     h.mass = reinterpret_cast<const float *>(base + o_mass);
@@ -565,8 +589,7 @@ int make_batch(cloth_ctx *ctx, const std::vector<cloth_s *> &members,
     auto cap = [&](int occ) { return std::max(1, ctx->num_sms * occ * 8); };
     b->grid_tri = std::max(1, std::min(b->n_tt, cap(ctx->occ_tri)));
     b->grid_row = std::max(1, std::min(b->n_rt, cap(ctx->occ_row)));
-    b->grid_spmv = std::max(1, std::min(b->n_rt, cap(ctx->occ_spmv)));
-    b->grid_update = std::max(1, std::min(b->n_rt, cap(ctx->occ_update)));
+    b->set_variants(ctx->tune_spmv, ctx->tune_update);
     int rc = plan_persistent(ctx, b.get());
     if (rc != CLOTH_OK)
         return rc;
@@ -831,11 +854,13 @@ int build_graph(Batch *b, bool full, cudaGraphExec_t *exec)
         {
             cudaGraph_t body = cp.conditional.phGraph_out[0];
             cudaGraphNode_t k1, k2;
-            rc = add_kernel(body, &k1, nullptr, 0, (void *)k_spmv, b->grid_spmv,
-                            kTile, a_spmv);
+            const GraphLoopVariant &sv = kSpmvVariants[b->spmv_v];
+            const GraphLoopVariant &uv = kUpdateVariants[b->upd_v];
+            rc = add_kernel(body, &k1, nullptr, 0, const_cast<void *>(sv.func), b->grid_spmv,
+                            kTile / sv.rows_per_thread, a_spmv);
             if (rc == CLOTH_OK)
-                rc = add_kernel(body, &k2, &k1, 1, (void *)k_update,
-                                b->grid_update, kTile, a_upd);
+                rc = add_kernel(body, &k2, &k1, 1, const_cast<void *>(uv.func),
+                                b->grid_update, kTile / uv.rows_per_thread, a_upd);
             last = cn;
         }
     }
@@ -892,6 +917,12 @@ int launch_solve_host(Batch *b, int max_iters)
     if (b->persist_ok)
         return launch_persistent(b);
     cudaGraphConditionalHandle none = 0;
+    int zero = 0;
+    int *no_left = nullptr;
+    void *a_spmv[] = {&b->d_descs, &b->d_rt, &b->d_ctl, &zero, &none};
+    void *a_upd[] = {&b->d_descs, &b->d_rt, &b->d_ctl, &zero, &none, &no_left};
+    const GraphLoopVariant &sv = kSpmvVariants[b->spmv_v];
+    const GraphLoopVariant &uv = kUpdateVariants[b->upd_v];
     int *h_active = nullptr;
     CK(cudaMallocHost(&h_active, sizeof(int)));
     int rc = CLOTH_OK;
@@ -902,13 +933,13 @@ int launch_solve_host(Batch *b, int max_iters)
         {
             {
                 PhaseTimer t(ctx, PH_SPMV);
-                k_spmv<<<b->grid_spmv, kTile, 0, s>>>(b->d_descs, b->d_rt, b->d_ctl,
-                                                       0, none);
+                cudaLaunchKernel(sv.func, dim3(b->grid_spmv), dim3(kTile / sv.rows_per_thread),
+                                 a_spmv, 0, s);
             }
             {
                 PhaseTimer t(ctx, PH_UPDATE);
-                k_update<<<b->grid_update, kTile, 0, s>>>(b->d_descs, b->d_rt,
-                                                           b->d_ctl, 0, none, nullptr);
+                cudaLaunchKernel(uv.func, dim3(b->grid_update),
+                                 dim3(kTile / uv.rows_per_thread), a_upd, 0, s);
             }
         }
         if (cudaMemcpyAsync(h_active, &b->d_ctl->n_active, sizeof(int),
@@ -994,6 +1025,110 @@ void end_step(const std::vector<cloth_s *> &members)
     }
 }
 
+// Autotuner of the graph-loop kernels: right after the assembly of a launch
+// set's first step (PCG at iteration 0) every SpMV variant is timed on the
+// real data - at iteration 0 the SpMV is idempotent (p = z, q = A z, alpha) -
+// and every update variant is timed from a snapshot of the state it changes
+// (dx, r, z, the instance scalars, the active count), restored after each
+// run. All variants compute bit-identical results, so the choice only moves
+// the time. The fastest pair is kept for the launch set and becomes the
+// context's default (the request server builds its chunks with it).
+int autotune_graph_loop(Batch *b)
+{
+    cloth_ctx *ctx = b->ctx;
+    cudaStream_t s = ctx->stream;
+    const int ninst = int(b->members.size());
+    float4 *rows = nullptr;
+    InstState *sts = nullptr;
+    BatchCtl *ctl_buf = nullptr;
+    CK(cudaMalloc(&rows, size_t(b->n_rt) * kTile * 3 * sizeof(float4)));
+    CK(cudaMalloc(&sts, size_t(ninst) * sizeof(InstState)));
+    CK(cudaMalloc(&ctl_buf, sizeof(BatchCtl)));
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaGraphConditionalHandle none = 0;
+    int zero = 0;
+    int *no_left = nullptr;
+    void *a_spmv[] = {&b->d_descs, &b->d_rt, &b->d_ctl, &zero, &none};
+    void *a_upd[] = {&b->d_descs, &b->d_rt, &b->d_ctl, &zero, &none, &no_left};
+    const int gsnap = std::max(1, std::min(b->n_rt, ctx->num_sms * 16));
+    auto snap = [&](int restore) {
+        k_snap_rows<<<gsnap, kTile, 0, s>>>(b->d_descs, b->d_rt, b->d_ctl, rows, restore);
+        k_snap_state<<<std::max(1, std::min(ninst, 1024)), 64, 0, s>>>(
+            b->d_descs, b->d_inst, ninst, sts, b->d_ctl, ctl_buf, restore);
+    };
+    auto time_launch = [&](const GraphLoopVariant &v, int grid, void **args) -> float {
+        cudaEventRecord(e0, s);
+        cudaLaunchKernel(v.func, dim3(grid), dim3(kTile / v.rows_per_thread), args, 0, s);
+        cudaEventRecord(e1, s);
+        cudaEventSynchronize(e1);
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        return ms;
+    };
+    auto grid_of = [&](const GraphLoopVariant &v, int occ) { return b->grid_for(v, occ); };
+    int best_s = b->spmv_v, best_u = b->upd_v;
+    float t_best = 1e30f;
+    ctx->tune_ms_spmv.assign(kNumSpmvVariants, 0.f);
+    ctx->tune_ms_update.assign(kNumUpdateVariants, 0.f);
+    for (int v = 0; v < kNumSpmvVariants; v++)
+    {
+        const int g = grid_of(kSpmvVariants[v], ctx->occ_spmv[v]);
+        float t = 1e30f;
+        for (int rep = 0; rep < 4; rep++)
+        {
+            const float ms = time_launch(kSpmvVariants[v], g, a_spmv);
+            if (rep > 0)
+                t = std::min(t, ms);
+        }
+        ctx->tune_ms_spmv[v] = t;
+        if (t < t_best)
+        {
+            t_best = t;
+            best_s = v;
+        }
+    }
+    // leave the state of iteration 0 with alpha set, as the loop expects it
+    cudaLaunchKernel(kSpmvVariants[best_s].func,
+                     dim3(grid_of(kSpmvVariants[best_s], ctx->occ_spmv[best_s])),
+                     dim3(kTile / kSpmvVariants[best_s].rows_per_thread), a_spmv, 0, s);
+    snap(0);
+    t_best = 1e30f;
+    for (int v = 0; v < kNumUpdateVariants; v++)
+    {
+        const int g = grid_of(kUpdateVariants[v], ctx->occ_update[v]);
+        float t = 1e30f;
+        for (int rep = 0; rep < 4; rep++)
+        {
+            snap(1);
+            const float ms = time_launch(kUpdateVariants[v], g, a_upd);
+            if (rep > 0)
+                t = std::min(t, ms);
+        }
+        ctx->tune_ms_update[v] = t;
+        if (t < t_best)
+        {
+            t_best = t;
+            best_u = v;
+        }
+    }
+    snap(1);
+    cudaError_t err = cudaStreamSynchronize(s);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(rows);
+    cudaFree(sts);
+    cudaFree(ctl_buf);
+    if (err != cudaSuccess)
+        return fail(CLOTH_ERR_CUDA, std::string("autotune: ") + cudaGetErrorString(err));
+    b->set_variants(best_s, best_u);
+    b->tuned = true;
+    ctx->tune_spmv = best_s;
+    ctx->tune_update = best_u;
+    return CLOTH_OK;
+}
+
 int run_step(Batch *b, double dt, const cloth_solve_params *params,
              cloth_solve_stats *stats)
 {
@@ -1008,6 +1143,20 @@ int run_step(Batch *b, double dt, const cloth_solve_params *params,
         rc = launch_assemble(b);
         if (rc == CLOTH_OK)
             rc = launch_solve_host(b, max_iters_of(b));
+        if (rc == CLOTH_OK)
+            rc = launch_advance(b);
+    }
+    else if (!b->persist_ok && !b->tuned && ctx->autotune)
+    {
+        // first step of a graph-loop launch set: assemble, tune on the real
+        // system, then solve and advance with the chosen kernels
+        rc = launch_assemble(b);
+        if (rc == CLOTH_OK)
+            rc = autotune_graph_loop(b);
+        if (rc == CLOTH_OK && !b->solve_exec)
+            rc = build_graph(b, false, &b->solve_exec);
+        if (rc == CLOTH_OK && cudaGraphLaunch(b->solve_exec, ctx->stream) != cudaSuccess)
+            rc = fail(CLOTH_ERR_CUDA, "cudaGraphLaunch failed");
         if (rc == CLOTH_OK)
             rc = launch_advance(b);
     }
@@ -1130,8 +1279,16 @@ int cloth_ctx_create(int device, cloth_ctx **out)
                               device));
     CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c->occ_tri, k_tri, kTile, 0));
     CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c->occ_row, k_row, kTile, 0));
-    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c->occ_spmv, k_spmv, kTile, 0));
-    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c->occ_update, k_update, kTile, 0));
+    c->occ_spmv.assign(kNumSpmvVariants, 1);
+    c->occ_update.assign(kNumUpdateVariants, 1);
+    for (int v = 0; v < kNumSpmvVariants; v++)
+        CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+            &c->occ_spmv[v], kSpmvVariants[v].func, kTile / kSpmvVariants[v].rows_per_thread,
+            0));
+    for (int v = 0; v < kNumUpdateVariants; v++)
+        CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+            &c->occ_update[v], kUpdateVariants[v].func,
+            kTile / kUpdateVariants[v].rows_per_thread, 0));
     *out = c.release();
     return CLOTH_OK;
 }
@@ -1233,6 +1390,66 @@ int cloth_ctx_set_solver(cloth_ctx *ctx, int solver)
     ctx->last_batch.reset();
     for (auto *c : ctx->cloths)
         c->self.reset();
+    return CLOTH_OK;
+}
+
+int cloth_ctx_set_kernel_variant(cloth_ctx *ctx, int spmv_r, int spmv_u, int spmv_tpb,
+                                 int upd_r, int upd_tpb, int autotune)
+{
+    if (!ctx)
+        return fail(CLOTH_ERR_INVALID, "cloth_ctx_set_kernel_variant: NULL context");
+    int sv = -1, uv = -1;
+    for (int v = 0; v < kNumSpmvVariants; v++)
+        if (kSpmvVariants[v].rows_per_thread == spmv_r && kSpmvVariants[v].slot_unroll == spmv_u &&
+            kSpmvVariants[v].tiles_per_block == spmv_tpb)
+            sv = v;
+    for (int v = 0; v < kNumUpdateVariants; v++)
+        if (kUpdateVariants[v].rows_per_thread == upd_r &&
+            kUpdateVariants[v].tiles_per_block == upd_tpb)
+            uv = v;
+    if (sv < 0 || uv < 0)
+        return fail(CLOTH_ERR_INVALID, "cloth_ctx_set_kernel_variant: no such variant");
+    std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+    ctx->tune_spmv = sv;
+    ctx->tune_update = uv;
+    ctx->autotune = autotune != 0;
+    ctx->last_batch.reset();
+    for (auto *c : ctx->cloths)
+        c->self.reset();
+    return CLOTH_OK;
+}
+
+int cloth_ctx_get_kernel_variant(cloth_ctx *ctx, int *spmv_r, int *spmv_u, int *spmv_tpb,
+                                 int *upd_r, int *upd_tpb, int *autotune)
+{
+    if (!ctx)
+        return fail(CLOTH_ERR_INVALID, "cloth_ctx_get_kernel_variant: NULL context");
+    std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+    if (spmv_r)
+        *spmv_r = kSpmvVariants[ctx->tune_spmv].rows_per_thread;
+    if (spmv_u)
+        *spmv_u = kSpmvVariants[ctx->tune_spmv].slot_unroll;
+    if (spmv_tpb)
+        *spmv_tpb = kSpmvVariants[ctx->tune_spmv].tiles_per_block;
+    if (upd_r)
+        *upd_r = kUpdateVariants[ctx->tune_update].rows_per_thread;
+    if (upd_tpb)
+        *upd_tpb = kUpdateVariants[ctx->tune_update].tiles_per_block;
+    if (autotune)
+        *autotune = ctx->autotune ? 1 : 0;
+    return CLOTH_OK;
+}
+
+int cloth_ctx_get_tuning_times(cloth_ctx *ctx, float *spmv_ms, int n_spmv, float *update_ms,
+                               int n_update)
+{
+    if (!ctx)
+        return fail(CLOTH_ERR_INVALID, "cloth_ctx_get_tuning_times: NULL context");
+    std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+    for (int v = 0; v < n_spmv && spmv_ms; v++)
+        spmv_ms[v] = v < int(ctx->tune_ms_spmv.size()) ? ctx->tune_ms_spmv[v] : 0.f;
+    for (int v = 0; v < n_update && update_ms; v++)
+        update_ms[v] = v < int(ctx->tune_ms_update.size()) ? ctx->tune_ms_update[v] : 0.f;
     return CLOTH_OK;
 }
 

@@ -16,9 +16,13 @@
 // symmetric, the pin projection zeroes both), so only the diagonal and upper
 // blocks (column >= row) are stored: row i's slots are sorted by column, the
 // first diag_slot(i) of them are lower, and upper slot s lives in plane
-// s - diag_slot(i).  A lower slot keeps its column and the plane index of its
-// transposed block (lidx); the SpMV fetches that block, which another row of
-// the same launch has just streamed, from L2.
+// u = s - diag_slot(i) (u = 0: the diagonal block).  A lower slot keeps its
+// column and the plane index of its transposed block (lidx); the SpMV fetches
+// that block, which another row of the same launch has just streamed, from
+// L2.  The SpMV walks the lower slots by s and the upper ones by u, with the
+// upper columns in planes of their own (colu), so that at every step the 32
+// rows of a warp read one plane of each array: coalesced, whatever the rows'
+// diag_slot.
 #pragma once
 #include <cstdint>
 #include <cuda_runtime.h>
@@ -65,6 +69,7 @@ struct InstState
 struct InstDesc
 {
     int nv, nt, width, stride;   // stride: padded row count of slot-major planes
+    int width_lo, width_up;      // planes of lower slots (lidx) and of stored blocks
     int ntile_rows, ntile_tris;
     int warm_start;
     int fix_fv_norm;
@@ -83,6 +88,7 @@ struct InstDesc
     // rows
     const int *col;       // [slot][stride] column (vertex) ids
     const uint32_t *lidx; // [slot][stride], lower slots: index of the transposed block in A0/A1
+    const int *colu;      // [slot - diag_slot][stride]: columns of the upper slots
     const uint32_t *hsrc; // [slot][stride] first record << 5 | record count
     const float *kb;      // [slot][stride] bending scalar (+K_b)
     const int *rowinfo;   // len | diag_slot << 8
@@ -136,9 +142,20 @@ constexpr int kFxTop = 70;
 
 constexpr int kPBlock = 1024;                // threads per persistent block
 constexpr int kRedRows = 32;                 // team ranges align to 32-row chunks (the FP32 warp sums)
-constexpr int kSlotUnroll = 3;               // ELL slots whose loads are issued together
+constexpr int kSlotUnroll = 2;               // ELL slots whose loads are issued together
 constexpr int kMaxBlockRows = 16384;         // rows one persistent block may own
 constexpr unsigned kSpinLimit = 1u << 25;    // bounded barrier wait (~seconds)
+
+// One variant of a graph-loop kernel: R rows per thread (blocks of kTile / R
+// threads), U ELL slots whose loads are issued together (SpMV only), TPB
+// consecutive tiles taken by a block at a time.
+struct GraphLoopVariant
+{
+    int rows_per_thread;
+    int slot_unroll;
+    int tiles_per_block;
+    const void *func;
+};
 
 // Batch-wide control words (one per launch set).
 struct BatchCtl

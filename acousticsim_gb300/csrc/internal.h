@@ -22,10 +22,19 @@ __global__ void k_pins(InstDesc *const *descs, const int *inst_list, int ninst,
 __global__ void k_tri(InstDesc *const *descs, const Tile *tiles, const BatchCtl *ctl);
 __global__ void k_row(InstDesc *const *descs, const Tile *tiles, BatchCtl *ctl);
 __global__ void k_cond(const BatchCtl *ctl, cudaGraphConditionalHandle h);
-__global__ void k_spmv(InstDesc *const *descs, const Tile *tiles, BatchCtl *ctl,
-                       int use_cond, cudaGraphConditionalHandle h);
-__global__ void k_update(InstDesc *const *descs, const Tile *tiles, BatchCtl *ctl,
-                         int use_cond, cudaGraphConditionalHandle h, int *iters_left);
+// graph-loop kernel variants (k_spmv_t<R, U>, k_update_t<R>); arguments:
+//   spmv  (descs, tiles, ctl, use_cond, handle)
+//   update(descs, tiles, ctl, use_cond, handle, iters_left)
+extern const GraphLoopVariant kSpmvVariants[];
+extern const GraphLoopVariant kUpdateVariants[];
+extern const int kNumSpmvVariants;
+extern const int kNumUpdateVariants;
+constexpr int kDefaultSpmvVariant = 3;   // R = 2, U = 1, TPB = 1 until a tuner says otherwise
+constexpr int kDefaultUpdateVariant = 1; // R = 2, TPB = 1
+__global__ void k_snap_rows(InstDesc *const *descs, const Tile *tiles, const BatchCtl *ctl,
+                            float4 *buf, int restore);
+__global__ void k_snap_state(InstDesc *const *descs, const int *inst, int ninst,
+                             InstState *buf, BatchCtl *ctl, BatchCtl *ctl_buf, int restore);
 __global__ void k_advance(InstDesc *const *descs, const Tile *tiles,
                           const BatchCtl *ctl, int finished_only);
 __global__ void k_sync_x32(InstDesc *d);
@@ -96,7 +105,11 @@ struct cloth_ctx_s
     cudaStream_t stream = nullptr;
     std::recursive_mutex mu;
     int num_sms = 0;
-    int occ_tri = 1, occ_row = 1, occ_spmv = 1, occ_update = 1;
+    int occ_tri = 1, occ_row = 1;
+    std::vector<int> occ_spmv, occ_update; // resident blocks per SM of each variant
+    bool autotune = true;                  // tune graph-loop batches on their first step
+    int tune_spmv = cloth::kDefaultSpmvVariant, tune_update = cloth::kDefaultUpdateVariant;
+    std::vector<float> tune_ms_spmv, tune_ms_update; // the last tuning's timings
     int max_smem_optin = 0;
     int solver = 0; // 0: persistent cooperative PCG when the set fits, 1: graph loop
     bool prof = false;

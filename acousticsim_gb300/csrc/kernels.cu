@@ -65,11 +65,13 @@ __device__ __forceinline__ float norm3(float3 a)
     return sqrtf(s);
 }
 // symmetric 3x3 (00 01 02 11 12 22) times vector
+// (explicit fused multiply-adds: device code is built without implicit
+// contraction, so every kernel variant rounds the same way)
 __device__ __forceinline__ float3 symv(const float *s, float3 v)
 {
-    return make_float3(s[0] * v.x + s[1] * v.y + s[2] * v.z,
-                       s[1] * v.x + s[3] * v.y + s[4] * v.z,
-                       s[2] * v.x + s[4] * v.y + s[5] * v.z);
+    return make_float3(fmaf(s[2], v.z, fmaf(s[1], v.y, s[0] * v.x)),
+                       fmaf(s[4], v.z, fmaf(s[3], v.y, s[1] * v.x)),
+                       fmaf(s[5], v.z, fmaf(s[4], v.y, s[2] * v.x)));
 }
 __device__ __forceinline__ void load_sym(const float4 *a0, const float2 *a1,
                                          size_t o, float *s)
@@ -572,91 +574,378 @@ __global__ void k_cond(const BatchCtl *ctl, cudaGraphConditionalHandle h)
 }
 
 // ------------------------------------------------------------------ PCG
-__global__ void __launch_bounds__(kTile) k_spmv(InstDesc *const *descs,
-                                                const Tile *tiles,
-                                                BatchCtl *ctl, int use_cond,
-                                                cudaGraphConditionalHandle h)
+// The graph-loop kernels come in variants: R rows per thread (blocks of
+// kTile / R threads; thread t of a tile owns rows t, t + kTile/R, ...) and U
+// ELL slots whose loads are issued together.  Every variant reproduces the
+// arithmetic and the summation order of R = 1 exactly - the per-row work is
+// the same code, and the tile sums go through 32-row groups summed in group
+// order, whichever thread held the group - so the variant an autotuner picks
+// does not change any result.
+namespace {
+
+// Tile sum of N values per row, rows held R per thread: FP32 butterfly per
+// 32-row group, FP64 over the groups in order (block_sum for R = 1).
+template <int R, int N>
+__device__ __forceinline__ void group_sum(const float (&vf)[R][N], double (&v)[N],
+                                          double (*sh)[kTile / 32])
 {
-    __shared__ double sh[1][kTile / 32];
-    __shared__ int flag;
-    const int ntiles = ctl->n_tiles_rows;
-    for (int ti = blockIdx.x; ti < ntiles; ti += gridDim.x)
+    constexpr int WPB = kTile / R / 32; // warps per block
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+#pragma unroll
+    for (int r = 0; r < R; r++)
+#pragma unroll
+        for (int k = 0; k < N; k++)
+        {
+            const float t = warp_sum(vf[r][k]);
+            if (l == 0)
+                sh[k][r * WPB + w] = double(t);
+        }
+    __syncthreads();
+    if (threadIdx.x == 0)
+#pragma unroll
+        for (int k = 0; k < N; k++)
+        {
+            double s = sh[k][0];
+#pragma unroll
+            for (int j = 1; j < kTile / 32; j++)
+                s += sh[k][j];
+            v[k] = s;
+        }
+    __syncthreads();
+}
+
+// FP64 counterpart over virtual threads v = r * (kTile/R) + t (block_sum_d for R = 1).
+template <int R, int N>
+__device__ __forceinline__ void group_sum_d(double (&vv)[R][N], double (&v)[N],
+                                            double (*sh)[kTile / 32])
+{
+    constexpr int WPB = kTile / R / 32;
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+#pragma unroll
+    for (int r = 0; r < R; r++)
+#pragma unroll
+        for (int k = 0; k < N; k++)
+        {
+            double x = vv[r][k];
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1)
+                x += __shfl_down_sync(0xffffffffu, x, o);
+            if (l == 0)
+                sh[k][r * WPB + w] = x;
+        }
+    __syncthreads();
+    if (threadIdx.x == 0)
+#pragma unroll
+        for (int k = 0; k < N; k++)
+        {
+            double s = sh[k][0];
+#pragma unroll
+            for (int j = 1; j < kTile / 32; j++)
+                s += sh[k][j];
+            v[k] = s;
+        }
+    __syncthreads();
+}
+
+// tile_reduce for R rows per thread (same order as tile_reduce); the
+// instance's partials, tile count and state come from the caller's header.
+template <int R, int N>
+__device__ bool tile_reduce_r(double *part, int nt, InstState *st, int tile_idx,
+                              const float (&vf)[R][N], double (&totals)[N],
+                              double (*sh)[kTile / 32], int *flag)
+{
+    constexpr int T = kTile / R;
+    double v[N];
+    group_sum<R, N>(vf, v, sh);
+    if (threadIdx.x == 0)
     {
-        const Tile tl = tiles[ti];
-        const InstDesc &d = *descs[tl.inst];
-        InstState *stp = d.st;
-        if (!stp->active)
-            continue;
-        const int it = stp->iter;
-        const float beta = float(stp->beta);
-        const float4 *pold = (it & 1) ? d.p1 : d.p0;
-        float4 *pnew = (it & 1) ? d.p0 : d.p1;
-        const int row = tl.start + threadIdx.x;
-        float part[1] = {0.f};
-        if (row < d.nv)
+#pragma unroll
+        for (int k = 0; k < N; k++)
+            part[k * nt + tile_idx] = v[k];
+        __threadfence();
+        unsigned prev = atomicAdd(&st->ticket, 1u);
+        *flag = (prev == unsigned(nt - 1));
+    }
+    __syncthreads();
+    if (!*flag)
+        return false;
+    __threadfence();
+    double s[R][N];
+#pragma unroll
+    for (int r = 0; r < R; r++)
+    {
+#pragma unroll
+        for (int k = 0; k < N; k++)
+            s[r][k] = 0.0;
+        for (int i = r * T + threadIdx.x; i < nt; i += kTile)
+#pragma unroll
+            for (int k = 0; k < N; k++)
+                s[r][k] += __ldcg(&part[k * nt + i]);
+    }
+    group_sum_d<R, N>(s, totals, sh);
+    return true;
+}
+
+// Read-only load of a pointer field (the descriptor is constant during a kernel).
+template <class T> __device__ __forceinline__ T *ldg_ptr(T *const *addr)
+{
+    return reinterpret_cast<T *>(
+        __ldg(reinterpret_cast<const unsigned long long *>(addr)));
+}
+
+// What the SpMV kernel needs of one instance, loaded once per run of
+// consecutive tiles of that instance (descriptor fields are read-only during
+// the kernel; the scalars are the ones the previous kernel left).
+struct SpmvHdr
+{
+    int inst, nv, stride, nt, active, wl;
+    float beta;
+    const int *rowinfo, *col, *colu;
+    const uint32_t *lidx;
+    const float4 *A0;
+    const float2 *A1;
+    const float4 *z, *pold;
+    float4 *pnew, *q;
+    double *part;
+    InstState *st;
+};
+
+__device__ __forceinline__ void load_hdr(SpmvHdr &h, InstDesc *const *descs, int inst)
+{
+    const InstDesc *dp = descs[inst];
+    InstState *st = ldg_ptr(&dp->st);
+    h.inst = inst;
+    h.active = st->active;
+    const int it = st->iter;
+    h.beta = float(st->beta);
+    h.nv = __ldg(&dp->nv);
+    h.stride = __ldg(&dp->stride);
+    h.wl = __ldg(&dp->width_lo);
+    h.nt = __ldg(&dp->ntile_rows);
+    h.rowinfo = ldg_ptr(&dp->rowinfo);
+    h.col = ldg_ptr(&dp->col);
+    h.lidx = ldg_ptr(&dp->lidx);
+    h.colu = ldg_ptr(&dp->colu);
+    h.A0 = ldg_ptr(reinterpret_cast<float4 *const *>(&dp->A0));
+    h.A1 = ldg_ptr(reinterpret_cast<float2 *const *>(&dp->A1));
+    h.z = ldg_ptr(reinterpret_cast<float4 *const *>(&dp->z));
+    float4 *p0 = ldg_ptr(&dp->p0), *p1 = ldg_ptr(&dp->p1);
+    h.pold = (it & 1) ? p1 : p0;
+    h.pnew = (it & 1) ? p0 : p1;
+    h.q = ldg_ptr(&dp->q);
+    h.part = ldg_ptr(&dp->part);
+    h.st = st;
+}
+
+// R rows of q = A p (rows row0 + r * T) with p = z + beta p_old recomputed
+// at the gathered columns; writes p_new and q, leaves p.q per row in pq.
+// Slots in column order: the lower ones by s (block at the transposed
+// position), then the diagonal and upper ones by plane u. Step k covers lower
+// plane k for k < wl and upper plane k - wl after (wl, the instance's lower
+// plane count, is uniform), so every load instruction of a warp reads one
+// plane; at each step the loads of all R rows and U steps are in flight
+// together.
+template <int R, int U, int T>
+__device__ __forceinline__ void spmv_rows(const SpmvHdr &d, int row0, float (&pq)[R][1])
+{
+    const float beta = d.beta;
+    const int wl = d.wl;
+    int len[R], ds[R], kend[R];
+    float3 pv[R], q[R];
+    bool ok[R];
+    int kmax = 0;
+#pragma unroll
+    for (int r = 0; r < R; r++)
+    {
+        const int row = row0 + r * T;
+        ok[r] = row < d.nv;
+        len[r] = ds[r] = 0;
+        pv[r] = q[r] = make_float3(0, 0, 0);
+        if (ok[r])
         {
             const int info = d.rowinfo[row];
-            const int len = info & 255, ds = (info >> 8) & 255;
-            float3 pv = xyz(d.z[row]);
+            len[r] = info & 255;
+            ds[r] = (info >> 8) & 255;
+            pv[r] = xyz(d.z[row]);
             if (beta != 0.f)
-                pv = pv + beta * xyz(pold[row]);
-            pnew[row] = f4(pv);
-            float3 q = make_float3(0, 0, 0);
-            for (int s = 0; s < len; s++)
-            {
-                const size_t o = size_t(s) * d.stride + row;
-                const int c = d.col[o];
-                const size_t oa = s < ds ? size_t(d.lidx[o]) : size_t(s - ds) * d.stride + row;
-                float A[6];
-                load_sym(d.A0, d.A1, oa, A);
-                float3 pc;
-                if (c == row)
-                    pc = pv;
-                else
-                {
-                    pc = xyz(d.z[c]);
-                    if (beta != 0.f)
-                        pc = pc + beta * xyz(pold[c]);
-                }
-                q = q + symv(A, pc);
-            }
-            d.q[row] = f4(q);
-            part[0] = fdot(pv, q);
+                pv[r] = pv[r] + beta * xyz(d.pold[row]);
+            d.pnew[row] = f4(pv[r]);
         }
-        double tot[1];
-        if (tile_reduce<1>(d, tl.start / kTile, part, tot, sh, &flag) &&
-            threadIdx.x == 0)
+        kend[r] = wl + (len[r] - ds[r]);
+        kmax = max(kmax, ok[r] ? kend[r] : 0);
+    }
+    for (int k0 = 0; k0 < kmax; k0 += U)
+    {
+        int cc[R][U];
+        float4 a0[R][U];
+        float2 a1[R][U];
+        bool on[R][U];
+#pragma unroll
+        for (int k = 0; k < U; k++)
         {
-            InstState &st = *stp;
-            st.ticket = 0u;
-            st.pq = tot[0];
-            if (!isfinite(tot[0]))
+            const int kk = k0 + k;
+            const bool lower = kk < wl;
+#pragma unroll
+            for (int r = 0; r < R; r++)
             {
-                st.status = 6;
-                st.active = 0;
-                retire(ctl, use_cond, h);
+                const int row = row0 + r * T;
+                on[r][k] = ok[r] && (lower ? kk < ds[r] : kk < kend[r]);
+                if (on[r][k])
+                {
+                    const size_t o = size_t(lower ? kk : kk - wl) * d.stride + row;
+                    cc[r][k] = lower ? d.col[o] : d.colu[o];
+                    const size_t oa = lower ? size_t(d.lidx[o]) : o;
+                    a0[r][k] = d.A0[oa];
+                    a1[r][k] = d.A1[oa];
+                }
             }
-            else if (tot[0] == 0.0)
-            {
-                // PCGSolver.cu:259-263 clamps alpha to zero; nothing moves
-                // afterwards, so the loop ends here. (p.Ap < 0 goes on with a
-                // negative alpha, as the reference does.)
-                st.status = 7;
-                st.active = 0;
-                retire(ctl, use_cond, h);
-            }
-            else
-                st.alpha = st.rho / tot[0];
+        }
+#pragma unroll
+        for (int k = 0; k < U; k++)
+#pragma unroll
+            for (int r = 0; r < R; r++)
+                if (on[r][k])
+                {
+                    const int row = row0 + r * T;
+                    const int c = cc[r][k];
+                    const float A[6] = {a0[r][k].x, a0[r][k].y, a0[r][k].z, a0[r][k].w,
+                                        a1[r][k].x, a1[r][k].y};
+                    float3 pc;
+                    if (c == row)
+                        pc = pv[r];
+                    else
+                    {
+                        pc = xyz(d.z[c]);
+                        if (beta != 0.f)
+                            pc = pc + beta * xyz(d.pold[c]);
+                    }
+                    q[r] = q[r] + symv(A, pc);
+                }
+    }
+#pragma unroll
+    for (int r = 0; r < R; r++)
+    {
+        pq[r][0] = 0.f;
+        if (ok[r])
+        {
+            d.q[row0 + r * T] = f4(q[r]);
+            pq[r][0] = fdot(pv[r], q[r]);
         }
     }
 }
 
-__global__ void __launch_bounds__(kTile) k_update(InstDesc *const *descs,
-                                                  const Tile *tiles,
-                                                  BatchCtl *ctl, int use_cond,
-                                                  cudaGraphConditionalHandle h,
-                                                  int *iters_left)
+struct UpdHdr
 {
+    int inst, nv, nt, active, iter, max_iters, check_every;
+    float alpha;
+    double rel_tol2, abs_tol2;
+    const float4 *pnew, *q;
+    float4 *dx, *r, *z;
+    const float4 *M0;
+    const float2 *M1;
+    double *part;
+    InstState *st;
+};
+
+__device__ __forceinline__ void load_hdr(UpdHdr &h, InstDesc *const *descs, int inst)
+{
+    const InstDesc *dp = descs[inst];
+    InstState *st = ldg_ptr(&dp->st);
+    h.inst = inst;
+    h.active = st->active;
+    h.iter = st->iter;
+    h.alpha = float(st->alpha);
+    h.nv = __ldg(&dp->nv);
+    h.nt = __ldg(&dp->ntile_rows);
+    h.max_iters = __ldg(&dp->max_iters);
+    h.check_every = __ldg(&dp->check_every);
+    h.rel_tol2 = __ldg(&dp->rel_tol2);
+    h.abs_tol2 = __ldg(&dp->abs_tol2);
+    float4 *p0 = ldg_ptr(&dp->p0), *p1 = ldg_ptr(&dp->p1);
+    h.pnew = (h.iter & 1) ? p0 : p1;
+    h.q = ldg_ptr(&dp->q);
+    h.dx = ldg_ptr(&dp->dx);
+    h.r = ldg_ptr(&dp->r);
+    h.z = ldg_ptr(&dp->z);
+    h.M0 = ldg_ptr(reinterpret_cast<float4 *const *>(&dp->M0));
+    h.M1 = ldg_ptr(reinterpret_cast<float2 *const *>(&dp->M1));
+    h.part = ldg_ptr(&dp->part);
+    h.st = st;
+}
+
+} // namespace
+
+// Blocks take TPB consecutive tile-list entries at a time (grid-stride over
+// those groups); the instance header is reloaded only when the instance
+// changes, so its dependent loads are paid once per run of tiles.
+template <int R, int U, int TPB>
+__global__ void __launch_bounds__(kTile / R) k_spmv_t(InstDesc *const *descs,
+                                                      const Tile *tiles, BatchCtl *ctl,
+                                                      int use_cond,
+                                                      cudaGraphConditionalHandle h)
+{
+    constexpr int T = kTile / R;
+    __shared__ double sh[1][kTile / 32];
+    __shared__ int flag;
+    __shared__ SpmvHdr d; // the current instance's header (thread 0 loads it)
+    const int ntiles = ctl->n_tiles_rows;
+    int cur = -1;
+    for (int t0 = blockIdx.x * TPB; t0 < ntiles; t0 += gridDim.x * TPB)
+    {
+        const int t1 = min(t0 + TPB, ntiles);
+        for (int ti = t0; ti < t1; ti++)
+        {
+            const Tile tl = tiles[ti];
+            if (tl.inst != cur)
+            {
+                __syncthreads();
+                if (threadIdx.x == 0)
+                    load_hdr(d, descs, tl.inst);
+                __syncthreads();
+                cur = tl.inst;
+            }
+            if (!d.active)
+                continue;
+            float part[R][1];
+            spmv_rows<R, U, T>(d, tl.start + threadIdx.x, part);
+            double tot[1];
+            if (tile_reduce_r<R, 1>(d.part, d.nt, d.st, tl.start / kTile, part, tot, sh,
+                                    &flag) &&
+                threadIdx.x == 0)
+            {
+                InstState &st = *d.st;
+                st.ticket = 0u;
+                st.pq = tot[0];
+                if (!isfinite(tot[0]))
+                {
+                    st.status = 6;
+                    st.active = 0;
+                    retire(ctl, use_cond, h);
+                }
+                else if (tot[0] == 0.0)
+                {
+                    // PCGSolver.cu:259-263 clamps alpha to zero; nothing moves
+                    // afterwards, so the loop ends here. (p.Ap < 0 goes on with a
+                    // negative alpha, as the reference does.)
+                    st.status = 7;
+                    st.active = 0;
+                    retire(ctl, use_cond, h);
+                }
+                else
+                    st.alpha = st.rho / tot[0];
+            }
+        }
+    }
+}
+
+template <int R, int TPB>
+__global__ void __launch_bounds__(kTile / R) k_update_t(InstDesc *const *descs,
+                                                        const Tile *tiles, BatchCtl *ctl,
+                                                        int use_cond,
+                                                        cudaGraphConditionalHandle h,
+                                                        int *iters_left)
+{
+    constexpr int T = kTile / R;
     __shared__ double sh[2][kTile / 32];
     __shared__ int flag;
     // chunked loops (the request server): the last iteration of a chunk ends
@@ -668,77 +957,169 @@ __global__ void __launch_bounds__(kTile) k_update(InstDesc *const *descs,
         if (use_cond && left <= 0)
             cudaGraphSetConditional(h, 0u);
     }
+    __shared__ UpdHdr d; // the current instance's header (thread 0 loads it)
+    const int ntiles = ctl->n_tiles_rows;
+    int cur = -1;
+    for (int t0 = blockIdx.x * TPB; t0 < ntiles; t0 += gridDim.x * TPB)
+    {
+        const int t1 = min(t0 + TPB, ntiles);
+        for (int ti = t0; ti < t1; ti++)
+        {
+            const Tile tl = tiles[ti];
+            if (tl.inst != cur)
+            {
+                __syncthreads();
+                if (threadIdx.x == 0)
+                    load_hdr(d, descs, tl.inst);
+                __syncthreads();
+                cur = tl.inst;
+            }
+            if (!d.active)
+                continue;
+            const float alpha = d.alpha;
+            float part[R][2];
+#pragma unroll
+            for (int r = 0; r < R; r++)
+            {
+                const int row = tl.start + r * T + threadIdx.x;
+                part[r][0] = part[r][1] = 0.f;
+                if (row < d.nv)
+                {
+                    const float3 p = xyz(d.pnew[row]);
+                    const float3 qv = xyz(d.q[row]);
+                    float3 x = xyz(d.dx[row]);
+                    float3 rr = xyz(d.r[row]);
+                    x = make_float3(fmaf(alpha, p.x, x.x), fmaf(alpha, p.y, x.y),
+                                    fmaf(alpha, p.z, x.z));
+                    rr = make_float3(fmaf(-alpha, qv.x, rr.x), fmaf(-alpha, qv.y, rr.y),
+                                     fmaf(-alpha, qv.z, rr.z));
+                    float M[6];
+                    load_sym(d.M0, d.M1, row, M);
+                    const float3 z = symv(M, rr);
+                    d.dx[row] = f4(x);
+                    d.r[row] = f4(rr);
+                    d.z[row] = f4(z);
+                    part[r][0] = fdot(rr, z);
+                    part[r][1] = fdot(rr, rr);
+                }
+            }
+            double tot[2];
+            if (tile_reduce_r<R, 2>(d.part, d.nt, d.st, tl.start / kTile, part, tot, sh,
+                                    &flag) &&
+                threadIdx.x == 0)
+            {
+                InstState &st = *d.st;
+                st.ticket = 0u;
+                const double rho_new = tot[0];
+                st.beta = (st.rho == 0.0) ? 0.0 : rho_new / st.rho;
+                st.rho = rho_new;
+                st.rr = tot[1];
+                st.iter = d.iter + 1;
+                const int n = st.iter;
+                bool stop = false;
+                if (!isfinite(tot[0]) || !isfinite(tot[1]))
+                {
+                    st.status = 6;
+                    stop = true;
+                }
+                else
+                {
+                    const bool check = ((n - 1) % d.check_every) == 0 || n >= d.max_iters;
+                    const bool conv = (d.rel_tol2 > 0.0 && tot[1] <= d.rel_tol2 * st.bb) ||
+                                      (d.abs_tol2 > 0.0 && tot[1] <= d.abs_tol2);
+                    if (check && conv)
+                    {
+                        st.status = 0;
+                        stop = true;
+                    }
+                    else if (n >= d.max_iters)
+                    {
+                        st.status = 8; // CLOTH_ERR_MAXITER
+                        stop = true;
+                    }
+                }
+                if (stop)
+                {
+                    st.active = 0;
+                    retire(ctl, use_cond, h);
+                }
+            }
+        }
+    }
+}
+
+// Variant table of the graph-loop kernels (the autotuner's search space).
+extern const GraphLoopVariant kSpmvVariants[] = {
+    {1, 1, 1, (const void *)k_spmv_t<1, 1, 1>}, {1, 2, 1, (const void *)k_spmv_t<1, 2, 1>},
+    {1, 3, 1, (const void *)k_spmv_t<1, 3, 1>}, {2, 1, 1, (const void *)k_spmv_t<2, 1, 1>},
+    {2, 2, 1, (const void *)k_spmv_t<2, 2, 1>}, {4, 1, 1, (const void *)k_spmv_t<4, 1, 1>},
+    {1, 1, 4, (const void *)k_spmv_t<1, 1, 4>}, {1, 2, 4, (const void *)k_spmv_t<1, 2, 4>},
+    {2, 1, 4, (const void *)k_spmv_t<2, 1, 4>}, {2, 2, 4, (const void *)k_spmv_t<2, 2, 4>},
+    {4, 1, 4, (const void *)k_spmv_t<4, 1, 4>}, {2, 1, 8, (const void *)k_spmv_t<2, 1, 8>},
+};
+extern const GraphLoopVariant kUpdateVariants[] = {
+    {1, 0, 1, (const void *)k_update_t<1, 1>}, {2, 0, 1, (const void *)k_update_t<2, 1>},
+    {4, 0, 1, (const void *)k_update_t<4, 1>}, {1, 0, 4, (const void *)k_update_t<1, 4>},
+    {2, 0, 4, (const void *)k_update_t<2, 4>}, {1, 0, 8, (const void *)k_update_t<1, 8>},
+    {2, 0, 8, (const void *)k_update_t<2, 8>},
+};
+extern const int kNumSpmvVariants = 12;
+extern const int kNumUpdateVariants = 7;
+static_assert(sizeof(kSpmvVariants) / sizeof(kSpmvVariants[0]) == 12, "variant count");
+static_assert(sizeof(kUpdateVariants) / sizeof(kUpdateVariants[0]) == 7, "variant count");
+
+// Copies of the PCG state the autotuner disturbs (dx, r, z per row, the
+// instance scalars), so that timing k_update candidates leaves no trace.
+__global__ void __launch_bounds__(kTile) k_snap_rows(InstDesc *const *descs, const Tile *tiles,
+                                                     const BatchCtl *ctl, float4 *buf,
+                                                     int restore)
+{
     const int ntiles = ctl->n_tiles_rows;
     for (int ti = blockIdx.x; ti < ntiles; ti += gridDim.x)
     {
         const Tile tl = tiles[ti];
         const InstDesc &d = *descs[tl.inst];
-        InstState *stp = d.st;
-        if (!stp->active)
-            continue;
-        const int it = stp->iter;
-        const float alpha = float(stp->alpha);
-        const float4 *pnew = (it & 1) ? d.p0 : d.p1;
         const int row = tl.start + threadIdx.x;
-        float part[2] = {0.f, 0.f};
-        if (row < d.nv)
+        if (row >= d.nv)
+            continue;
+        float4 *b = buf + 3 * (size_t(ti) * kTile + threadIdx.x);
+        if (restore)
         {
-            const float3 p = xyz(pnew[row]);
-            const float3 qv = xyz(d.q[row]);
-            float3 x = xyz(d.dx[row]);
-            float3 r = xyz(d.r[row]);
-            x = make_float3(fmaf(alpha, p.x, x.x), fmaf(alpha, p.y, x.y),
-                            fmaf(alpha, p.z, x.z));
-            r = make_float3(fmaf(-alpha, qv.x, r.x), fmaf(-alpha, qv.y, r.y),
-                            fmaf(-alpha, qv.z, r.z));
-            float M[6];
-            load_sym(d.M0, d.M1, row, M);
-            const float3 z = symv(M, r);
-            d.dx[row] = f4(x);
-            d.r[row] = f4(r);
-            d.z[row] = f4(z);
-            part[0] = fdot(r, z);
-            part[1] = fdot(r, r);
+            d.dx[row] = b[0];
+            d.r[row] = b[1];
+            d.z[row] = b[2];
         }
-        double tot[2];
-        if (tile_reduce<2>(d, tl.start / kTile, part, tot, sh, &flag) &&
-            threadIdx.x == 0)
+        else
         {
-            InstState &st = *stp;
-            st.ticket = 0u;
-            const double rho_new = tot[0];
-            st.beta = (st.rho == 0.0) ? 0.0 : rho_new / st.rho;
-            st.rho = rho_new;
-            st.rr = tot[1];
-            st.iter = it + 1;
-            const int n = st.iter;
-            bool stop = false;
-            if (!isfinite(tot[0]) || !isfinite(tot[1]))
-            {
-                st.status = 6;
-                stop = true;
-            }
+            b[0] = d.dx[row];
+            b[1] = d.r[row];
+            b[2] = d.z[row];
+        }
+    }
+}
+
+__global__ void k_snap_state(InstDesc *const *descs, const int *inst, int ninst,
+                             InstState *buf, BatchCtl *ctl, BatchCtl *ctl_buf, int restore)
+{
+    constexpr int W = int(sizeof(InstState) / sizeof(unsigned));
+    for (int i = blockIdx.x; i < ninst; i += gridDim.x)
+    {
+        unsigned *a = reinterpret_cast<unsigned *>(descs[inst[i]]->st);
+        unsigned *b = reinterpret_cast<unsigned *>(buf + i);
+        for (int k = threadIdx.x; k < W; k += blockDim.x)
+        {
+            if (restore)
+                a[k] = b[k];
             else
-            {
-                const bool check =
-                    ((n - 1) % d.check_every) == 0 || n >= d.max_iters;
-                if (check && test_converged(d, st, tot[1]))
-                {
-                    st.status = 0;
-                    stop = true;
-                }
-                else if (n >= d.max_iters)
-                {
-                    st.status = 8; // CLOTH_ERR_MAXITER
-                    stop = true;
-                }
-            }
-            if (stop)
-            {
-                st.active = 0;
-                retire(ctl, use_cond, h);
-            }
+                b[k] = a[k];
         }
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0)
+    {
+        if (restore)
+            *ctl = *ctl_buf;
+        else
+            *ctl_buf = *ctl;
     }
 }
 
@@ -1108,32 +1489,41 @@ __device__ __forceinline__ void pcg_persistent_body(InstDesc *const *descs,
                 const int info = ld_keep(d.rowinfo + row, keep);
                 const int len = info & 255, ds = (info >> 8) & 255;
                 float3 q = make_float3(0, 0, 0);
-                // Slots in column order: a lower slot (s < ds) fetches its block
-                // at the transposed position, the diagonal and upper ones are
-                // stored in plane s - ds. kSlotUnroll slots at a time: their
-                // loads are all in flight together.
-                const uint32_t *lix = d.lidx + row;
-                for (int s0 = 0; s0 < len; s0 += kSlotUnroll)
+                // Slots in column order: the lower ones by s (block at the
+                // transposed position), then the diagonal and upper ones by
+                // plane u. Step k covers lower plane k for k < wl and upper
+                // plane k - wl after, so every load instruction of a warp reads
+                // one plane (wl, the instance's lower plane count, is uniform).
+                // kSlotUnroll steps' loads are in flight together.
+                const int wl = d.width_lo, kend = wl + (len - ds);
+                for (int k0 = 0; k0 < kend; k0 += kSlotUnroll)
                 {
                     int cc[kSlotUnroll];
                     float4 a0[kSlotUnroll];
                     float2 a1[kSlotUnroll];
+                    bool on[kSlotUnroll];
 #pragma unroll
                     for (int k = 0; k < kSlotUnroll; k++)
-                        if (s0 + k < len)
+                    {
+                        const int kk = k0 + k;
+                        const bool lower = kk < wl;
+                        on[k] = lower ? kk < ds : kk < kend;
+                        if (on[k])
                         {
-                            const int sl = s0 + k;
-                            const uint32_t o = uint32_t(sl) * uint32_t(d.stride);
-                            cc[k] = ld_keep(d.col + row + o, keep);
+                            const uint32_t o = uint32_t(lower ? kk : kk - wl) * uint32_t(d.stride) +
+                                               uint32_t(row);
+                            cc[k] = ld_keep(lower ? d.col + o : d.colu + o, keep);
                             const uint32_t oa =
-                                sl < ds ? uint32_t(ld_keep(reinterpret_cast<const int *>(lix + o), keep))
-                                        : uint32_t(sl - ds) * uint32_t(d.stride) + uint32_t(row);
+                                lower ? uint32_t(ld_keep(reinterpret_cast<const int *>(d.lidx) + o,
+                                                         keep))
+                                      : o;
                             a0[k] = ld_keep(d.A0 + oa, keep);
                             a1[k] = ld_keep(d.A1 + oa, keep);
                         }
+                    }
 #pragma unroll
                     for (int k = 0; k < kSlotUnroll; k++)
-                        if (s0 + k < len)
+                        if (on[k])
                         {
                             const int c = cc[k];
                             const float A[6] = {a0[k].x, a0[k].y, a0[k].z, a0[k].w,

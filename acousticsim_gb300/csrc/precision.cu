@@ -127,8 +127,9 @@ __device__ __forceinline__ void load_block64(const InstDesc &d, size_t o, double
     a[5] = w.y;
 }
 
-// y = A v on one row in FP64 (slots in column order; lower slots read the
-// transposed block). v: nv*3 doubles, or the FP32 dx when v64 is null.
+// y = A v on one row in FP64, slots in column order: the lower ones (block at
+// the transposed position), then the diagonal and upper ones. v: nv*3
+// doubles, or the FP32 dx when v64 is null.
 __device__ __forceinline__ void row_mul64(const InstDesc &d, int row, const double *v64,
                                           double *y)
 {
@@ -137,9 +138,10 @@ __device__ __forceinline__ void row_mul64(const InstDesc &d, int row, const doub
     y[0] = y[1] = y[2] = 0.0;
     for (int s = 0; s < len; s++)
     {
-        const size_t o = size_t(s) * d.stride + row;
-        const int c = d.col[o];
-        const size_t oa = s < ds ? size_t(d.lidx[o]) : size_t(s - ds) * d.stride + row;
+        const bool lower = s < ds;
+        const size_t o = lower ? size_t(s) * d.stride + row : size_t(s - ds) * d.stride + row;
+        const int c = lower ? d.col[o] : d.colu[o];
+        const size_t oa = lower ? size_t(d.lidx[o]) : o;
         double a[6];
         load_block64(d, oa, a);
         double x0, x1, x2;

@@ -318,8 +318,10 @@ int build_chunk_graph(cloth_server_s *s)
     const int n = int(s->cl.size());
     const int one_wave_tri = ctx->num_sms * std::max(1, ctx->occ_tri);
     const int one_wave_row = ctx->num_sms * std::max(1, ctx->occ_row);
-    const int one_wave_spmv = ctx->num_sms * std::max(1, ctx->occ_spmv);
-    const int one_wave_upd = ctx->num_sms * std::max(1, ctx->occ_update);
+    const GraphLoopVariant &sv = kSpmvVariants[ctx->tune_spmv];
+    const GraphLoopVariant &uv = kUpdateVariants[ctx->tune_update];
+    const int one_wave_spmv = ctx->num_sms * std::max(1, ctx->occ_spmv[ctx->tune_spmv]);
+    const int one_wave_upd = ctx->num_sms * std::max(1, ctx->occ_update[ctx->tune_update]);
     cudaGraph_t g = nullptr;
     SCK(cudaGraphCreate(&g, 0));
     cudaGraphConditionalHandle hnd = 0;
@@ -367,9 +369,11 @@ int build_chunk_graph(cloth_server_s *s)
         {
             cudaGraph_t body = cp.conditional.phGraph_out[0];
             cudaGraphNode_t bl = nullptr, bn = nullptr;
-            rc = add_node(body, &bn, &bl, (void *)k_spmv, one_wave_spmv, kTile, a_spmv);
+            rc = add_node(body, &bn, &bl, const_cast<void *>(sv.func), one_wave_spmv,
+                          kTile / sv.rows_per_thread, a_spmv);
             if (rc == CLOTH_OK)
-                rc = add_node(body, &bn, &bl, (void *)k_update, one_wave_upd, kTile, a_upd);
+                rc = add_node(body, &bn, &bl, const_cast<void *>(uv.func), one_wave_upd,
+                              kTile / uv.rows_per_thread, a_upd);
             last = cn;
         }
     }

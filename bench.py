@@ -801,12 +801,55 @@ def run_precision(args):
     ctx.close()
 
 
+def run_profile_batch(args):
+    """The batched workload (256 cloths, graph-loop kernels launched from the
+    host) for --profile-iters PCG iterations: per-kernel CUDA-event times and
+    the bytes each k_spmv / k_update launch must move, i.e. the achieved
+    bandwidth of the SpMV kernel on a working set far larger than L2."""
+    from acousticsim_gb300 import ClothContext, params
+    from acousticsim_gb300 import build as b
+    b.build_all()
+    ctx = ClothContext(0)
+    ctx.set_solver("graph_loop")
+    confs = batch_confs(args.batch_count)
+    cloths, _ = make_batch(ctx, confs)
+    spmv_b = upd_b = 0
+    for c in cloths:
+        mi = c.matrix_info()
+        spmv_b += algorithmic_bytes(c.nv, mi["nnzb"])["matrix"] + 68 * c.nv
+        upd_b += 136 * c.nv
+    p = params(max_iters=args.profile_iters, rel_tol=1e-12)
+    ctx.batch_step(cloths, 0.0, p)  # first step: the autotuner picks the kernel variants
+    tuned = {"variant": ctx.kernel_variant(), "times_ms": ctx.tuning_times()}
+    ctx.set_profiling(True)
+    ctx.reset_profile()
+    st = ctx.batch_step(cloths, 0.0, p)
+    ph = ctx.profile()
+    peak = measured_peaks()["hbm_gbs"]
+    out = {"profile_batch": {"cloths": len(cloths), "rows": int(sum(c.nv for c in cloths)),
+                             "iters": max(s["iters"] for s in st)}, "phases": ph,
+           "autotune": tuned}
+    for name, nbytes in (("spmv_dot", spmv_b), ("update_dot", upd_b)):
+        n = ph[name]["launches"]
+        if n:
+            us = 1e3 * ph[name]["ms"] / n
+            out[name] = {"us_per_launch": us, "bytes_per_launch": nbytes,
+                         "gbs": nbytes / us / 1e3, "frac_of_hbm_peak": nbytes / us / 1e3 / peak}
+    print(json.dumps(out))
+    for c in cloths:
+        c.close()
+    ctx.close()
+
+
 def run_profile_case(args):
     """Small case for ncu: one step of the 512x512 workload with the PCG capped
     at --profile-iters iterations, kernels launched from the host."""
     from acousticsim_gb300 import BaraffClothGpu, ClothContext, params
     from acousticsim_gb300 import build as b
     b.build_all()
+    if args.mode == "batch":
+        run_profile_batch(args)
+        return
     ctx = ClothContext(0)
     if args.solver:
         ctx.set_solver(args.solver)

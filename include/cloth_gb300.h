@@ -124,6 +124,27 @@ int cloth_ctx_get_profile(cloth_ctx *ctx, double *ms_total, long long *launches)
 int cloth_ctx_reset_profile(cloth_ctx *ctx);
 /* Preferred PCG driver for launch sets built after the call. */
 int cloth_ctx_set_solver(cloth_ctx *ctx, int solver);
+/* Graph-loop kernel variants (the batched and served PCG): rows per thread R
+ * of the SpMV and update kernels, the SpMV's slot unroll U and the tiles a
+ * block takes at a time (TPB). With autotune on (the default) every graph-loop
+ * launch set times all variants on its first step and keeps the fastest; the
+ * choice becomes the context's default, which the request server uses. Every
+ * variant computes bit-identical results. Variants (SpMV R,U,TPB): 1,1,1
+ * 1,2,1 1,3,1 2,1,1 2,2,1 4,1,1 1,1,4 1,2,4 2,1,4 2,2,4 4,1,4 2,1,8;
+ * (update R,TPB): 1,1 2,1 4,1 1,4 2,4 1,8 2,8. Others: CLOTH_ERR_INVALID.
+ * Applies to launch sets built afterwards. */
+int cloth_ctx_set_kernel_variant(cloth_ctx *ctx, int spmv_rows_per_thread,
+                                 int spmv_slot_unroll, int spmv_tiles_per_block,
+                                 int update_rows_per_thread, int update_tiles_per_block,
+                                 int autotune);
+int cloth_ctx_get_kernel_variant(cloth_ctx *ctx, int *spmv_rows_per_thread,
+                                 int *spmv_slot_unroll, int *spmv_tiles_per_block,
+                                 int *update_rows_per_thread, int *update_tiles_per_block,
+                                 int *autotune);
+/* Kernel times (ms, best of three) of the last tuning, per variant in the
+ * order listed above. Zero when nothing was tuned. */
+int cloth_ctx_get_tuning_times(cloth_ctx *ctx, float *spmv_ms, int n_spmv, float *update_ms,
+                               int n_update);
 /* Device bytes held by all cloths of the context. */
 int cloth_ctx_device_bytes(cloth_ctx *ctx, size_t *bytes);
 /* The context's cudaStream_t, so callers can order their own work and CUDA

@@ -193,6 +193,55 @@ def test_batch_equals_alone_bit_exact(ctx, solver):
         c.close()
 
 
+def test_kernel_variants_bit_identical(ctx):
+    """Every graph-loop kernel variant (rows per thread, slot unroll) and the
+    autotuned choice give bit-identical trajectories on a mixed batch."""
+    from acousticsim_gb300 import params
+    p = params(max_iters=5000, rel_tol=1e-6)
+    sizes = [12, 40, 23, 33]
+    confs = [_grid_conf(n, 2e-3, ks=(10 ** (2 + k % 2), 10 ** (2 + k % 2), 10 ** (1 + k % 2)))
+             for k, n in enumerate(sizes)]
+
+    def run(variant, autotune=False):
+        ctx.set_solver("graph_loop")
+        ctx.set_kernel_variant(variant[0], variant[1], autotune=autotune)
+        cl = []
+        for k, conf in enumerate(confs):
+            c = make(ctx, conf)
+            x, xp = _perturbed(c, 300 + k, 2e-3)
+            c.SetPos(x)
+            c.SetPrePos(xp)
+            cl.append(c)
+        its = []
+        for _ in range(2):
+            st = ctx.batch_step(cl, 0.0, p)
+            assert all(s["status"] == "OK" and s["solver"] == "graph_loop" for s in st), st
+            its.append([s["iters"] for s in st])
+        out = ([c.GetPos() for c in cl], its, ctx.kernel_variant())
+        for c in cl:
+            c.close()
+        return out
+
+    from acousticsim_gb300 import ClothContext
+    ref = run(((1, 1, 1), (1, 1)))
+    sv, uv = ClothContext.SPMV_VARIANTS, ClothContext.UPDATE_VARIANTS
+    variants = [(sv[k], uv[k % len(uv)]) for k in range(1, len(sv))]
+    for v in variants:
+        got = run(v)
+        assert got[1] == ref[1], (v, got[1], ref[1])
+        for a, b in zip(got[0], ref[0]):
+            assert np.array_equal(a, b), v
+    tuned = run(((1, 1, 1), (1, 1)), autotune=True)
+    assert tuned[1] == ref[1]
+    for a, b in zip(tuned[0], ref[0]):
+        assert np.array_equal(a, b)
+    print("autotuned:", tuned[2])
+    ctx.set_kernel_variant((1, 3, 1), (1, 1), autotune=True)
+    ctx.set_solver("persistent")
+    with pytest.raises(Exception):
+        ctx.set_kernel_variant((3, 1, 1), (1, 1))
+
+
 def test_solvers_agree(ctx):
     """Persistent and graph-loop drivers run the same recurrence; only the
     order of the FP64 reductions differs."""
