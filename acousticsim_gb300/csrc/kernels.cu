@@ -164,6 +164,33 @@ __device__ __forceinline__ void block_sum_d(double (&v)[N], double (*sh)[kTile /
     __syncthreads();
 }
 
+// s[k] += part[k * nt + i] for i = v, v + kTile, v + 2 kTile, ... in that
+// order; eight loads in flight at a time (the additions keep their order).
+template <int N>
+__device__ __forceinline__ void sum_strided(const double *part, int nt, int v,
+                                            double (&s)[N])
+{
+    constexpr int B = 8;
+    for (int i0 = v; i0 < nt; i0 += B * kTile)
+    {
+        double x[B][N];
+#pragma unroll
+        for (int j = 0; j < B; j++)
+        {
+            const int i = i0 + j * kTile;
+#pragma unroll
+            for (int k = 0; k < N; k++)
+                x[j][k] = i < nt ? __ldcg(&part[k * nt + i]) : 0.0;
+        }
+#pragma unroll
+        for (int j = 0; j < B; j++)
+            if (i0 + j * kTile < nt)
+#pragma unroll
+                for (int k = 0; k < N; k++)
+                    s[k] += x[j][k];
+    }
+}
+
 // Publish this tile's N partials and find out whether it is the instance's
 // last tile. When it is, every thread of the block returns true and totals
 // holds the instance sums (summed in tile order, deterministic).
@@ -193,10 +220,7 @@ __device__ bool tile_reduce(const InstDesc &d, int tile_idx, const float (&vf)[N
     for (int k = 0; k < N; k++)
         s[k] = 0.0;
     // fixed thread -> tile assignment, then a fixed-order block sum
-    for (int i = threadIdx.x; i < nt; i += kTile)
-#pragma unroll
-        for (int k = 0; k < N; k++)
-            s[k] += __ldcg(&d.part[k * nt + i]);
+    sum_strided<N>(d.part, nt, threadIdx.x, s);
     block_sum_d<N>(s, sh);
 #pragma unroll
     for (int k = 0; k < N; k++)
@@ -677,10 +701,7 @@ __device__ bool tile_reduce_r(double *part, int nt, InstState *st, int tile_idx,
 #pragma unroll
         for (int k = 0; k < N; k++)
             s[r][k] = 0.0;
-        for (int i = r * T + threadIdx.x; i < nt; i += kTile)
-#pragma unroll
-            for (int k = 0; k < N; k++)
-                s[r][k] += __ldcg(&part[k * nt + i]);
+        sum_strided<N>(part, nt, r * T + threadIdx.x, s[r]);
     }
     group_sum_d<R, N>(s, totals, sh);
     return true;

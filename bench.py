@@ -853,13 +853,26 @@ def run_profile_case(args):
     ctx = ClothContext(0)
     if args.solver:
         ctx.set_solver(args.solver)
-    cloth = BaraffClothGpu(ctx, workload_conf())
+    cloth = BaraffClothGpu(ctx, workload_conf(args.profile_side))
     x0, xp0 = initial_state(cloth.GetInitPos(), 1234)
     cloth.SetPos(x0)
     cloth.SetPrePos(xp0)
     ctx.set_profiling(True)
     st = cloth.UpdatePos(0.0, params(max_iters=args.profile_iters, rel_tol=1e-12))
-    print(json.dumps({"profile_case": st, "phases": ctx.profile()}))
+    ph = ctx.profile()
+    out = {"profile_case": st, "phases": ph, "grid": args.profile_side}
+    mi = cloth.matrix_info()
+    ab = algorithmic_bytes(cloth.nv, mi["nnzb"])
+    if st["solver"] == "graph_loop":
+        peak = measured_peaks()["hbm_gbs"]
+        for name, nbytes in (("spmv_dot", ab["matrix"] + 68 * cloth.nv),
+                             ("update_dot", 136 * cloth.nv)):
+            n = ph[name]["launches"]
+            if n:
+                us = 1e3 * ph[name]["ms"] / n
+                out[name] = {"us_per_launch": us, "bytes_per_launch": nbytes,
+                             "gbs": nbytes / us / 1e3, "frac_of_hbm_peak": nbytes / us / 1e3 / peak}
+    print(json.dumps(out))
     cloth.close()
     ctx.close()
 
@@ -873,6 +886,8 @@ def main():
     ap.add_argument("--profile-iters", type=int, default=0,
                     help="run only the small ncu case: one step, PCG capped at N iterations")
     ap.add_argument("--solver", choices=["persistent", "graph_loop"], default=None)
+    ap.add_argument("--profile-side", type=int, default=N_SIDE,
+                    help="grid side of the single-cloth ncu case")
     ap.add_argument("--mode", choices=["step", "batch", "serve", "precision"], default="step",
                     help="step: the 512x512 single-cloth headline; batch: 256 mixed cloths; "
                          "serve: Poisson request stream through the continuous-batching server")
