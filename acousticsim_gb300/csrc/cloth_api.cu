@@ -67,18 +67,22 @@ struct Batch
     int spmv_v = kDefaultSpmvVariant, upd_v = kDefaultUpdateVariant;
     bool tuned = false;
     int grid_spmv = 1, grid_update = 1;
-    void set_variants(int sv, int uv)
+    int spmv_waves = 8, upd_waves = 8;
+    void set_variants(int sv, int uv, int sw = 8, int uw = 8)
     {
         spmv_v = sv;
         upd_v = uv;
-        grid_spmv = grid_for(kSpmvVariants[sv], ctx->occ_spmv[sv]);
-        grid_update = grid_for(kUpdateVariants[uv], ctx->occ_update[uv]);
+        spmv_waves = sw;
+        upd_waves = uw;
+        grid_spmv = grid_for(kSpmvVariants[sv], ctx->occ_spmv[sv], sw);
+        grid_update = grid_for(kUpdateVariants[uv], ctx->occ_update[uv], uw);
     }
-    // one block per group of TPB tiles while that fits in a few waves
-    int grid_for(const GraphLoopVariant &v, int occ) const
+    // one block per group of TPB tiles, at most `waves` full waves of resident
+    // blocks (fewer waves: each block walks more tiles, grid-stride)
+    int grid_for(const GraphLoopVariant &v, int occ, int waves = 8) const
     {
         const int groups = (n_rt + v.tiles_per_block - 1) / v.tiles_per_block;
-        return std::max(1, std::min(groups, ctx->num_sms * occ * 8));
+        return std::max(1, std::min(groups, ctx->num_sms * occ * waves));
     }
     // persistent solver plan
     bool persist_ok = false;
@@ -561,9 +565,9 @@ int make_batch(cloth_ctx *ctx, const std::vector<cloth_s *> &members,
         descs.push_back(c->d_desc);
         inst.push_back(int(i));
         for (int s = 0; s < c->tab.nv; s += kTile)
-            rt.push_back(Tile{int(i), s});
+            rt.push_back(Tile{int(i), s, c->d_desc, c->d_state});
         for (int s = 0; s < c->tab.nt; s += kTile)
-            tt.push_back(Tile{int(i), s});
+            tt.push_back(Tile{int(i), s, c->d_desc, c->d_state});
     }
     b->n_rt = int(rt.size());
     b->n_tt = int(tt.size());
@@ -1067,51 +1071,64 @@ int autotune_graph_loop(Batch *b)
         cudaEventElapsedTime(&ms, e0, e1);
         return ms;
     };
-    auto grid_of = [&](const GraphLoopVariant &v, int occ) { return b->grid_for(v, occ); };
+    const int kWaves[2] = {1, 8};
     int best_s = b->spmv_v, best_u = b->upd_v;
     float t_best = 1e30f;
     ctx->tune_ms_spmv.assign(kNumSpmvVariants, 0.f);
     ctx->tune_ms_update.assign(kNumUpdateVariants, 0.f);
+    int best_sw = 8, best_uw = 8;
     for (int v = 0; v < kNumSpmvVariants; v++)
     {
-        const int g = grid_of(kSpmvVariants[v], ctx->occ_spmv[v]);
-        float t = 1e30f;
-        for (int rep = 0; rep < 4; rep++)
+        float tv = 1e30f;
+        for (int wv : kWaves)
         {
-            const float ms = time_launch(kSpmvVariants[v], g, a_spmv);
-            if (rep > 0)
-                t = std::min(t, ms);
+            const int g = b->grid_for(kSpmvVariants[v], ctx->occ_spmv[v], wv);
+            float t = 1e30f;
+            for (int rep = 0; rep < 4; rep++)
+            {
+                const float ms = time_launch(kSpmvVariants[v], g, a_spmv);
+                if (rep > 0)
+                    t = std::min(t, ms);
+            }
+            tv = std::min(tv, t);
+            if (t < t_best)
+            {
+                t_best = t;
+                best_s = v;
+                best_sw = wv;
+            }
         }
-        ctx->tune_ms_spmv[v] = t;
-        if (t < t_best)
-        {
-            t_best = t;
-            best_s = v;
-        }
+        ctx->tune_ms_spmv[v] = tv;
     }
     // leave the state of iteration 0 with alpha set, as the loop expects it
     cudaLaunchKernel(kSpmvVariants[best_s].func,
-                     dim3(grid_of(kSpmvVariants[best_s], ctx->occ_spmv[best_s])),
+                     dim3(b->grid_for(kSpmvVariants[best_s], ctx->occ_spmv[best_s], best_sw)),
                      dim3(kTile / kSpmvVariants[best_s].rows_per_thread), a_spmv, 0, s);
     snap(0);
     t_best = 1e30f;
     for (int v = 0; v < kNumUpdateVariants; v++)
     {
-        const int g = grid_of(kUpdateVariants[v], ctx->occ_update[v]);
-        float t = 1e30f;
-        for (int rep = 0; rep < 4; rep++)
+        float tv = 1e30f;
+        for (int wv : kWaves)
         {
-            snap(1);
-            const float ms = time_launch(kUpdateVariants[v], g, a_upd);
-            if (rep > 0)
-                t = std::min(t, ms);
+            const int g = b->grid_for(kUpdateVariants[v], ctx->occ_update[v], wv);
+            float t = 1e30f;
+            for (int rep = 0; rep < 4; rep++)
+            {
+                snap(1);
+                const float ms = time_launch(kUpdateVariants[v], g, a_upd);
+                if (rep > 0)
+                    t = std::min(t, ms);
+            }
+            tv = std::min(tv, t);
+            if (t < t_best)
+            {
+                t_best = t;
+                best_u = v;
+                best_uw = wv;
+            }
         }
-        ctx->tune_ms_update[v] = t;
-        if (t < t_best)
-        {
-            t_best = t;
-            best_u = v;
-        }
+        ctx->tune_ms_update[v] = tv;
     }
     snap(1);
     cudaError_t err = cudaStreamSynchronize(s);
@@ -1122,7 +1139,7 @@ int autotune_graph_loop(Batch *b)
     cudaFree(ctl_buf);
     if (err != cudaSuccess)
         return fail(CLOTH_ERR_CUDA, std::string("autotune: ") + cudaGetErrorString(err));
-    b->set_variants(best_s, best_u);
+    b->set_variants(best_s, best_u, best_sw, best_uw);
     b->tuned = true;
     ctx->tune_spmv = best_s;
     ctx->tune_update = best_u;

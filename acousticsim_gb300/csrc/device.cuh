@@ -116,10 +116,15 @@ struct InstDesc
     InstState *st;
 };
 
+// A tile carries its instance's descriptor and state addresses, so the PCG
+// kernels reach both with one dependent load instead of walking the
+// descriptor table and then the descriptor.
 struct Tile
 {
     int inst;
     int start;
+    InstDesc *d;
+    InstState *st;
 };
 
 // One block of the persistent PCG grid: a contiguous row range of one

@@ -731,10 +731,11 @@ struct SpmvHdr
     InstState *st;
 };
 
-__device__ __forceinline__ void load_hdr(SpmvHdr &h, InstDesc *const *descs, int inst)
+__device__ __forceinline__ void load_hdr(SpmvHdr &h, const Tile &tl)
 {
-    const InstDesc *dp = descs[inst];
-    InstState *st = ldg_ptr(&dp->st);
+    const InstDesc *dp = tl.d;
+    const int inst = tl.inst;
+    InstState *st = tl.st;
     h.inst = inst;
     h.active = st->active;
     const int it = st->iter;
@@ -868,10 +869,11 @@ struct UpdHdr
     InstState *st;
 };
 
-__device__ __forceinline__ void load_hdr(UpdHdr &h, InstDesc *const *descs, int inst)
+__device__ __forceinline__ void load_hdr(UpdHdr &h, const Tile &tl)
 {
-    const InstDesc *dp = descs[inst];
-    InstState *st = ldg_ptr(&dp->st);
+    const InstDesc *dp = tl.d;
+    const int inst = tl.inst;
+    InstState *st = tl.st;
     h.inst = inst;
     h.active = st->active;
     h.iter = st->iter;
@@ -921,7 +923,7 @@ __global__ void __launch_bounds__(kTile / R) k_spmv_t(InstDesc *const *descs,
             {
                 __syncthreads();
                 if (threadIdx.x == 0)
-                    load_hdr(d, descs, tl.inst);
+                    load_hdr(d, tl);
                 __syncthreads();
                 cur = tl.inst;
             }
@@ -991,7 +993,7 @@ __global__ void __launch_bounds__(kTile / R) k_update_t(InstDesc *const *descs,
             {
                 __syncthreads();
                 if (threadIdx.x == 0)
-                    load_hdr(d, descs, tl.inst);
+                    load_hdr(d, tl);
                 __syncthreads();
                 cur = tl.inst;
             }

@@ -462,9 +462,9 @@ int launch_chunk(cloth_server_s *s, Stage &sg, long long chunk_no, bool *launche
             sg.new_ids[n_admit] = id;
             n_admit++;
             for (int k = 0; k < cr.ntt; k++)
-                sg.new_tt[n_new_tt++] = Tile{id, k * kTile};
+                sg.new_tt[n_new_tt++] = Tile{id, k * kTile, s->d_table + id, cr.c->d_state};
             for (int k = 0; k < cr.ntr; k++)
-                sg.new_rt[n_new_rt++] = Tile{id, k * kTile};
+                sg.new_rt[n_new_rt++] = Tile{id, k * kTile, s->d_table + id, cr.c->d_state};
             s->inflight.push_back(id);
         }
         s->max_inflight_seen = std::max(s->max_inflight_seen, int(s->inflight.size()));
@@ -473,7 +473,8 @@ int launch_chunk(cloth_server_s *s, Stage &sg, long long chunk_no, bool *launche
             const int id = s->inflight[i];
             sg.inflight[i] = id;
             for (int k = 0; k < s->cl[id].ntr; k++)
-                sg.act_rt[n_act_rt++] = Tile{id, k * kTile};
+                sg.act_rt[n_act_rt++] =
+                    Tile{id, k * kTile, s->d_table + id, s->cl[id].c->d_state};
         }
         sg.n_inflight = int(s->inflight.size());
     }
