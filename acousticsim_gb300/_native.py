@@ -23,7 +23,9 @@ ELL_REF_WIDTH = 32
 SOLVER_PERSISTENT = 0
 SOLVER_GRAPH_LOOP = 1
 SOLVER_FP64 = 2
-SOLVER_NAMES = {0: "persistent", 1: "graph_loop", 2: "fp64", -1: "plain"}
+SOLVER_PERSISTENT_1B = 3
+SOLVER_PERSISTENT_2B = 4
+SOLVER_NAMES = {0: "persistent", 1: "graph_loop", 2: "fp64", 3: "persistent_1b", -1: "plain"}
 
 
 class GridDesc(C.Structure):

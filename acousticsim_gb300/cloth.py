@@ -45,8 +45,13 @@ class ClothContext:
         return {N.PHASE_NAMES[k]: {"ms": ms[k], "launches": n[k]} for k in range(N.NUM_PHASES)}
 
     def set_solver(self, solver: str) -> None:
-        """'persistent' (default; falls back when the set does not fit) or 'graph_loop'."""
-        code = {"persistent": N.SOLVER_PERSISTENT, "graph_loop": N.SOLVER_GRAPH_LOOP}[solver]
+        """'persistent' (default: one cooperative launch; falls back to the graph
+        loop when the set does not fit), 'persistent_1b' (single-barrier
+        iterations where every block's halo is staged), 'persistent_2b' (the
+        two-barrier persistent kernel only) or 'graph_loop'."""
+        code = {"persistent": N.SOLVER_PERSISTENT, "graph_loop": N.SOLVER_GRAPH_LOOP,
+                "persistent_1b": N.SOLVER_PERSISTENT_1B,
+                "persistent_2b": N.SOLVER_PERSISTENT_2B}[solver]
         N.call("cloth_ctx_set_solver", self._h, code)
 
     SPMV_VARIANTS = [(1, 1, 1), (1, 2, 1), (1, 3, 1), (2, 1, 1), (2, 2, 1), (4, 1, 1),

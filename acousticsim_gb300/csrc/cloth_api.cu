@@ -87,6 +87,7 @@ struct Batch
     // persistent solver plan
     bool persist_ok = false;
     bool persist_sm = false; // own-row state in shared memory
+    bool persist_1b = false; // single-barrier variant (shared memory, every halo staged)
     TeamBlock *d_work = nullptr;
     int grid_persist = 0;
     int halo_cap = 0, rows_cap = 0;
@@ -222,6 +223,7 @@ int upload_tables(cloth_s *c)
     sl.p0 = W2.take<float4>(n);
     sl.p1 = W2.take<float4>(n);
     sl.q = W2.take<float4>(n);
+    sl.w1 = W2.take<float4>(n);
     sl.part = W2.take<double>(3 * size_t(ntr));
     sl.bytes = W2.off;
 
@@ -386,6 +388,7 @@ void cloth::detail::bind_scratch(const cloth_s *c, InstDesc &h, char *base)
     h.p0 = reinterpret_cast<float4 *>(at(sl.p0));
     h.p1 = reinterpret_cast<float4 *>(at(sl.p1));
     h.q = reinterpret_cast<float4 *>(at(sl.q));
+    h.w1 = reinterpret_cast<float4 *>(at(sl.w1));
     h.part = reinterpret_cast<double *>(at(sl.part));
 }
 
@@ -607,7 +610,9 @@ int make_batch(cloth_ctx *ctx, const std::vector<cloth_s *> &members,
 int plan_persistent(cloth_ctx *ctx, Batch *b)
 {
     b->persist_ok = false;
-    if (ctx->solver != 0)
+    b->persist_1b = false;
+    if (ctx->solver != CLOTH_SOLVER_PERSISTENT && ctx->solver != CLOTH_SOLVER_PERSISTENT_1B &&
+        ctx->solver != CLOTH_SOLVER_PERSISTENT_2B)
         return CLOTH_OK;
     const size_t smem_cap_bytes =
         std::min<size_t>(size_t(std::max(ctx->max_smem_optin, 48 * 1024)) - 4096,
@@ -618,6 +623,8 @@ int plan_persistent(cloth_ctx *ctx, Batch *b)
     if (cudaFuncSetAttribute(k_pcg_persistent_sm, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              int(smem_cap_bytes)) != cudaSuccess ||
         cudaFuncSetAttribute(k_pcg_persistent_gm, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             int(smem_cap_bytes)) != cudaSuccess ||
+        cudaFuncSetAttribute(k_pcg1_persistent, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              int(smem_cap_bytes)) != cudaSuccess ||
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_pcg_persistent_gm, kPBlock,
                                                       smem_cap_bytes) != cudaSuccess ||
@@ -683,6 +690,7 @@ int plan_persistent(cloth_ctx *ctx, Batch *b)
     }
     std::vector<TeamBlock> work;
     int max_entries = 0, max_rows = 0;
+    bool all_staged = true;
     for (int i = 0; i < n; i++)
     {
         const Tables &t = b->members[i]->tab;
@@ -716,7 +724,10 @@ int plan_persistent(cloth_ctx *ctx, Batch *b)
             w.nblk = int(team.size());
             max_rows = std::max(max_rows, w.row1 - w.row0);
             if (w.halo1 - w.halo0 > cap_entries)
+            {
                 w.halo0 = w.halo1 = -1;
+                all_staged = false;
+            }
             else
                 max_entries = std::max(max_entries, w.halo1 - w.halo0);
             work.push_back(w);
@@ -731,10 +742,15 @@ int plan_persistent(cloth_ctx *ctx, Batch *b)
     const size_t sm_bytes = size_t(max_entries) * sizeof(float4) + size_t(max_rows) * 72;
     b->persist_sm = sm_bytes <= smem_cap_bytes;
     b->smem_persist = b->persist_sm ? sm_bytes : size_t(max_entries) * sizeof(float4);
+    // the single-barrier variant keeps dx, p and M^-1 per own row (56 bytes)
+    // next to u over the halo: it fits wherever the two-barrier one does
+    b->persist_1b = b->persist_sm && all_staged && ctx->solver == CLOTH_SOLVER_PERSISTENT_1B;
     int occ2 = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-            &occ2, b->persist_sm ? k_pcg_persistent_sm : k_pcg_persistent_gm, kPBlock,
-            b->smem_persist) != cudaSuccess ||
+            &occ2,
+            b->persist_1b ? k_pcg1_persistent
+                          : (b->persist_sm ? k_pcg_persistent_sm : k_pcg_persistent_gm),
+            kPBlock, b->smem_persist) != cudaSuccess ||
         occ2 * ctx->num_sms < int(work.size()))
     {
         cudaGetLastError();
@@ -822,8 +838,9 @@ int build_graph(Batch *b, bool full, cudaGraphExec_t *exec)
         {
             cudaKernelNodeParams p;
             std::memset(&p, 0, sizeof(p));
-            p.func = b->persist_sm ? (void *)k_pcg_persistent_sm
-                                   : (void *)k_pcg_persistent_gm;
+            p.func = b->persist_1b   ? (void *)k_pcg1_persistent
+                     : b->persist_sm ? (void *)k_pcg_persistent_sm
+                                     : (void *)k_pcg_persistent_gm;
             p.gridDim = dim3(b->grid_persist);
             p.blockDim = dim3(kPBlock);
             p.sharedMemBytes = unsigned(b->smem_persist);
@@ -907,8 +924,9 @@ int launch_persistent(Batch *b)
     cloth_ctx *ctx = b->ctx;
     PhaseTimer t(ctx, PH_SPMV);
     void *args[] = {&b->d_descs, &b->d_work, &b->halo_cap, &b->rows_cap};
-    CK(cudaLaunchCooperativeKernel(b->persist_sm ? (void *)k_pcg_persistent_sm
-                                                 : (void *)k_pcg_persistent_gm,
+    CK(cudaLaunchCooperativeKernel(b->persist_1b   ? (void *)k_pcg1_persistent
+                                   : b->persist_sm ? (void *)k_pcg_persistent_sm
+                                                   : (void *)k_pcg_persistent_gm,
                                    dim3(b->grid_persist), dim3(kPBlock), args,
                                    b->smem_persist, ctx->stream));
     return CLOTH_OK;
@@ -983,7 +1001,9 @@ int read_stats(Batch *b, cloth_solve_stats *stats)
         o.res_norm = std::sqrt(std::max(0.0, st.rr));
         o.rhs_norm = std::sqrt(std::max(0.0, st.bb));
         o.rel_residual = o.rhs_norm > 0 ? o.res_norm / o.rhs_norm : o.res_norm;
-        o.solver = b->persist_ok ? CLOTH_SOLVER_PERSISTENT : CLOTH_SOLVER_GRAPH_LOOP;
+        o.solver = !b->persist_ok  ? CLOTH_SOLVER_GRAPH_LOOP
+                   : b->persist_1b ? CLOTH_SOLVER_PERSISTENT_1B
+                                   : CLOTH_SOLVER_PERSISTENT;
     }
     return CLOTH_OK;
 }
@@ -1399,7 +1419,8 @@ int cloth_ctx_reset_profile(cloth_ctx *ctx)
 
 int cloth_ctx_set_solver(cloth_ctx *ctx, int solver)
 {
-    if (!ctx || (solver != CLOTH_SOLVER_PERSISTENT && solver != CLOTH_SOLVER_GRAPH_LOOP))
+    if (!ctx || (solver != CLOTH_SOLVER_PERSISTENT && solver != CLOTH_SOLVER_GRAPH_LOOP &&
+                 solver != CLOTH_SOLVER_PERSISTENT_1B && solver != CLOTH_SOLVER_PERSISTENT_2B))
         return fail(CLOTH_ERR_INVALID, "cloth_ctx_set_solver: bad argument");
     std::lock_guard<std::recursive_mutex> lk(ctx->mu);
     cudaStreamSynchronize(ctx->stream);
@@ -1972,8 +1993,9 @@ int cloth_get_stats(cloth_t *c, cloth_solve_stats *stats)
     stats->rhs_norm = std::sqrt(std::max(0.0, st.bb));
     stats->rel_residual = stats->rhs_norm > 0 ? stats->res_norm / stats->rhs_norm
                                               : stats->res_norm;
-    stats->solver = (c->self && c->self->persist_ok) ? CLOTH_SOLVER_PERSISTENT
-                                                     : CLOTH_SOLVER_GRAPH_LOOP;
+    stats->solver = !(c->self && c->self->persist_ok) ? CLOTH_SOLVER_GRAPH_LOOP
+                    : c->self->persist_1b             ? CLOTH_SOLVER_PERSISTENT_1B
+                                                      : CLOTH_SOLVER_PERSISTENT;
     return CLOTH_OK;
 }
 

@@ -112,6 +112,7 @@ struct InstDesc
     double *x64, *xp64;  // nv*3
     float4 *x32;         // float copy of x; .w = 1 on pinned vertices
     float4 *dx, *r, *z, *p0, *p1, *q;
+    float4 *w1;          // second buffer of w (single-barrier persistent PCG)
     double *part;        // 3 * ntile_rows reduction partials
     InstState *st;
 };

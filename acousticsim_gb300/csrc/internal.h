@@ -44,6 +44,8 @@ __global__ void k_pcg_persistent_sm(InstDesc *const *descs, const TeamBlock *wor
                                     int halo_cap, int rows_cap);
 __global__ void k_pcg_persistent_gm(InstDesc *const *descs, const TeamBlock *work,
                                     int halo_cap, int rows_cap);
+__global__ void k_pcg1_persistent(InstDesc *const *descs, const TeamBlock *work, int halo_cap,
+                                  int rows_cap);
 
 // ---------------------------------------------------------------- plain path
 struct PlainState;
@@ -86,7 +88,7 @@ struct Layout
 struct ScratchLayout
 {
     size_t hrec = 0, frec = 0, A0 = 0, A1 = 0, M0 = 0, M1 = 0, b = 0;
-    size_t r = 0, z = 0, p0 = 0, p1 = 0, q = 0, part = 0;
+    size_t r = 0, z = 0, p0 = 0, p1 = 0, q = 0, w1 = 0, part = 0;
     size_t bytes = 0;
 };
 

@@ -1735,6 +1735,370 @@ __global__ void __launch_bounds__(kPBlock, 1)
     pcg_persistent_body<false>(descs, work, halo_cap, rows_cap);
 }
 
+// ------------------------------------------------------------------ single-barrier persistent PCG
+// The same block-Jacobi PCG in the Chronopoulos-Gear arrangement: with
+// u = M^-1 r and w = A u, the scalars come from gamma = r.u, delta = w.u
+// and r.r, all three summed at ONE team barrier per iteration:
+//   beta = gamma / gamma_prev,  alpha = gamma / (delta - beta gamma / alpha_prev)
+//   p = u + beta p,  s = w + beta s,  dx += alpha p,  r -= alpha s,
+//   u = M^-1 r,  w = A u.
+// The SpMV needs u over the block's halo.  A block recomputes u for the halo
+// rows it does not own from the previous iteration's r, w and s, which their
+// owners wrote to global memory before the barrier (two buffers each,
+// alternating by iteration, so no row is overwritten while another block may
+// still read it), with the same code the owners run, so the values agree bit
+// for bit.  Requires the shared-memory plan with every block's halo staged.
+// Team sums are the exact fixed-point sums of the two-barrier solver, so an
+// instance's result does not depend on the launch set.
+namespace {
+
+// r_new = r - alpha (w + beta s) and s_new = w + beta s (s absent at the
+// first iteration); the owner and every block staging the row run this.
+__device__ __forceinline__ float3 cg1_residual(float3 r, float3 w, float3 s, float af,
+                                               float bf, bool first, float3 &s_new)
+{
+    s_new = first ? w
+                  : make_float3(fmaf(bf, s.x, w.x), fmaf(bf, s.y, w.y), fmaf(bf, s.z, w.z));
+    return make_float3(fmaf(-af, s_new.x, r.x), fmaf(-af, s_new.y, r.y),
+                       fmaf(-af, s_new.z, r.z));
+}
+
+} // namespace
+
+__global__ void __launch_bounds__(kPBlock, 1)
+    k_pcg1_persistent(InstDesc *const *descs, const TeamBlock *work, int halo_cap,
+                      int rows_cap)
+{
+    constexpr int NW = kPBlock / 32;
+    extern __shared__ float4 sm_dyn[];
+    __shared__ InstDesc d;
+    __shared__ unsigned long long wsum_h[3][NW], wsum_l[3][NW];
+    __shared__ float wsum_c[3][NW];
+    // FP64 scalars: owned by thread 0, the block reads the FP32 copies
+    __shared__ double s_gam, s_del, s_rr, s_alpha, s_beta;
+    __shared__ float bc_af, bc_bf;
+    __shared__ int bc_stop, bc_s[3];
+    const TeamBlock w = work[blockIdx.x];
+    if (w.inst < 0)
+        return;
+    if (threadIdx.x == 0)
+        d = *descs[w.inst];
+    __syncthreads();
+    InstState *st = d.st;
+    if (!__ldcg(&st->active))
+        return;
+    // dynamic shared memory: u over the halo, then own rows' dx, p, M^-1
+    float4 *su = sm_dyn;
+    float4 *sx = su + halo_cap;
+    float4 *sp = sx + rows_cap;
+    float4 *sm0 = sp + rows_cap;
+    float2 *sm1 = reinterpret_cast<float2 *>(sm0 + rows_cap);
+    float4 *const rb[2] = {d.r, d.z};
+    float4 *const sb[2] = {d.p0, d.p1};
+    float4 *const wb[2] = {d.q, d.w1};
+
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const unsigned long long keep = l2_keep_policy();
+    const int nrow = w.row1 - w.row0;
+    const int nch = (nrow + 31) / 32;
+    const int h0 = w.halo0, nh = w.halo1 - w.halo0;
+    for (int i = tid; i < nrow; i += kPBlock)
+    {
+        const int row = w.row0 + i;
+        sx[i] = d.dx[row];
+        sm0[i] = d.M0[row];
+        sm1[i] = d.M1[row];
+    }
+    // u0 = z0 of the assembly over the halo
+    for (int i = tid; i < nh; i += kPBlock)
+        su[i] = ldcg4(d.z + h0 + i);
+    if (tid == 0)
+    {
+        s_gam = __ldcg(&st->rho);
+        s_rr = __ldcg(&st->rr);
+        s_del = s_gam; // scale estimate for the first delta
+        s_alpha = 0.0;
+        s_beta = 0.0;
+        bc_s[0] = fx_scale(s_gam);
+        bc_s[1] = fx_scale(s_del);
+        bc_s[2] = fx_scale(s_rr);
+    }
+    // (the three sum buffers start at zero: the PCG start cleared them)
+    __syncthreads();
+
+    auto team_sum = [&](WarpFx<3> &wfx, int bq) -> bool {
+        if (lane == 0)
+            for (int q = 0; q < 3; q++)
+            {
+                wsum_h[q][warp] = (unsigned long long)wfx.H[q];
+                wsum_l[q][warp] = wfx.L[q];
+                wsum_c[q][warp] = wfx.chk[q];
+            }
+        __syncthreads();
+        if (tid == 0)
+            for (int q = 0; q < 3; q++)
+            {
+                unsigned long long hh = 0ull, ll = 0ull;
+                float c = 0.f;
+                for (int j = 0; j < NW; j++)
+                {
+                    hh += wsum_h[q][j];
+                    ll += wsum_l[q][j];
+                    c += wsum_c[q][j];
+                }
+                atomicAdd(&st->acc[bq][q][0], hh);
+                atomicAdd(&st->acc[bq][q][1], ll);
+                atomicAdd(&st->acc_chk[bq][q], c);
+            }
+        return team_barrier(st, w.nblk);
+    };
+    auto team_value = [&](int q, int bq, int s, int *bad) -> double {
+        const double v = fx_value(__ldcg(&st->acc[bq][q][0]), __ldcg(&st->acc[bq][q][1]), s);
+        const float chk = __ldcg(&st->acc_chk[bq][q]);
+        if (!isfinite(chk) || fabs(v - double(chk)) > 1e-3 * fabs(double(chk)) + 1e-30)
+            *bad = 1;
+        return v;
+    };
+    // w = A u on an own row from the staged u; writes wbuf, returns w.u
+    auto spmv_row = [&](int row, float3 uv, float4 *wbuf) -> float {
+        const int info = ld_keep(d.rowinfo + row, keep);
+        const int len = info & 255, ds = (info >> 8) & 255;
+        const int wl = d.width_lo, kend = wl + (len - ds);
+        float3 q = make_float3(0, 0, 0);
+        for (int k0 = 0; k0 < kend; k0 += kSlotUnroll)
+        {
+            int cc[kSlotUnroll];
+            float4 a0[kSlotUnroll];
+            float2 a1[kSlotUnroll];
+            bool on[kSlotUnroll];
+#pragma unroll
+            for (int k = 0; k < kSlotUnroll; k++)
+            {
+                const int kk = k0 + k;
+                const bool lower = kk < wl;
+                on[k] = lower ? kk < ds : kk < kend;
+                if (on[k])
+                {
+                    const uint32_t o =
+                        uint32_t(lower ? kk : kk - wl) * uint32_t(d.stride) + uint32_t(row);
+                    cc[k] = ld_keep(lower ? d.col + o : d.colu + o, keep);
+                    const uint32_t oa =
+                        lower ? uint32_t(ld_keep(reinterpret_cast<const int *>(d.lidx) + o, keep))
+                              : o;
+                    a0[k] = ld_keep(d.A0 + oa, keep);
+                    a1[k] = ld_keep(d.A1 + oa, keep);
+                }
+            }
+#pragma unroll
+            for (int k = 0; k < kSlotUnroll; k++)
+                if (on[k])
+                {
+                    const float A[6] = {a0[k].x, a0[k].y, a0[k].z, a0[k].w, a1[k].x, a1[k].y};
+                    q = q + symv(A, xyz(su[cc[k] - h0]));
+                }
+        }
+        wbuf[row] = f4(q);
+        return fdot(q, uv);
+    };
+
+    int it = 0, status = 0, bq = 1;
+    // ---- setup: w0 = A u0; gamma0 = r0.u0, delta0 = w0.u0, r0.r0
+    {
+        const int s0q = bc_s[0], s1q = bc_s[1], s2q = bc_s[2];
+        WarpFx<3> f;
+        f.clear();
+        for (int ch = warp; ch < nch; ch += NW)
+        {
+            const int li = ch * 32 + lane;
+            const int row = w.row0 + li;
+            float pg = 0.f, pd = 0.f, pr = 0.f;
+            if (li < nrow)
+            {
+                const float3 uv = xyz(su[row - h0]);
+                const float3 rv = xyz(ldcg4(rb[0] + row));
+                pd = spmv_row(row, uv, wb[0]);
+                pg = fdot(rv, uv);
+                pr = fdot(rv, rv);
+            }
+            pg = warp_sum(pg);
+            pd = warp_sum(pd);
+            pr = warp_sum(pr);
+            if (lane == 0)
+            {
+                f.add(0, pg, s0q);
+                f.add(1, pd, s1q);
+                f.add(2, pr, s2q);
+            }
+        }
+        if (!team_sum(f, bq))
+            status = 9;
+    }
+    while (status == 0)
+    {
+        // ---- scalars from the sums of this iteration
+        if (tid == 0)
+        {
+            int bad = 0;
+            const double gam = team_value(0, bq, bc_s[0], &bad);
+            const double del = team_value(1, bq, bc_s[1], &bad);
+            const double rr = team_value(2, bq, bc_s[2], &bad);
+            int stop = 0; // 0 go on, 1 converged, else a status code
+            double beta = 0.0, alpha = s_alpha;
+            if (bad || !isfinite(gam) || !isfinite(del) || !isfinite(rr))
+                stop = 6;
+            else if (it > 0)
+            {
+                const bool check = ((it - 1) % d.check_every) == 0 || it >= d.max_iters;
+                if (check && test_converged(d, *st, rr))
+                    stop = 1;
+                else if (it >= d.max_iters)
+                    stop = 8;
+            }
+            if (!stop)
+            {
+                beta = (it == 0 || s_gam == 0.0) ? 0.0 : gam / s_gam;
+                const double den = (it == 0) ? del : del - beta * gam / s_alpha;
+                if (den == 0.0)
+                    stop = 7;
+                else
+                    alpha = gam / den;
+            }
+            s_gam = gam;
+            s_del = del;
+            s_rr = rr;
+            s_beta = beta;
+            s_alpha = alpha;
+            bc_af = float(alpha);
+            bc_bf = float(beta);
+            bc_stop = stop;
+            bc_s[0] = fx_scale(gam);
+            bc_s[1] = fx_scale(del);
+            bc_s[2] = fx_scale(rr);
+            if (w.rank == 0)
+            {
+                // the buffer of the next sums was last read two iterations ago
+                const int nb = (bq + 1) % 3;
+                for (int q = 0; q < 3; q++)
+                {
+                    st->acc[nb][q][0] = 0ull;
+                    st->acc[nb][q][1] = 0ull;
+                    st->acc_chk[nb][q] = 0.f;
+                }
+            }
+        }
+        __syncthreads();
+        if (bc_stop)
+        {
+            status = (bc_stop == 1) ? 0 : bc_stop;
+            break;
+        }
+        const float af = bc_af, bf = bc_bf;
+        const bool first = (it == 0);
+        const int cur = it & 1, nxt = cur ^ 1;
+        const int s0q = bc_s[0], s1q = bc_s[1], s2q = bc_s[2];
+        WarpFx<3> f;
+        f.clear();
+        // ---- own rows: p, s, dx, r, u; gamma and r.r of the new r
+        for (int ch = warp; ch < nch; ch += NW)
+        {
+            const int li = ch * 32 + lane;
+            const int row = w.row0 + li;
+            float pg = 0.f, pr = 0.f;
+            if (li < nrow)
+            {
+                const float3 uv = xyz(su[row - h0]);
+                const float3 wv = xyz(ldcg4(wb[cur] + row));
+                const float3 sv = first ? make_float3(0, 0, 0) : xyz(ldcg4(sb[cur] + row));
+                const float3 rv = xyz(ldcg4(rb[cur] + row));
+                float3 pv = uv;
+                if (!first)
+                {
+                    const float3 po = xyz(sp[li]);
+                    pv = make_float3(fmaf(bf, po.x, uv.x), fmaf(bf, po.y, uv.y),
+                                     fmaf(bf, po.z, uv.z));
+                }
+                float3 s_new;
+                const float3 r_new = cg1_residual(rv, wv, sv, af, bf, first, s_new);
+                float3 x = xyz(sx[li]);
+                x = make_float3(fmaf(af, pv.x, x.x), fmaf(af, pv.y, x.y), fmaf(af, pv.z, x.z));
+                const float4 m0 = sm0[li];
+                const float2 m1 = sm1[li];
+                const float M[6] = {m0.x, m0.y, m0.z, m0.w, m1.x, m1.y};
+                const float3 u_new = symv(M, r_new);
+                sp[li] = f4(pv);
+                sx[li] = f4(x);
+                sb[nxt][row] = f4(s_new);
+                rb[nxt][row] = f4(r_new);
+                su[row - h0] = f4(u_new);
+                pg = fdot(r_new, u_new);
+                pr = fdot(r_new, r_new);
+            }
+            pg = warp_sum(pg);
+            pr = warp_sum(pr);
+            if (lane == 0)
+            {
+                f.add(0, pg, s0q);
+                f.add(2, pr, s2q);
+            }
+        }
+        // ---- halo rows owned by other blocks: the same u from their r, w, s
+        for (int i = tid; i < nh; i += kPBlock)
+        {
+            const int row = h0 + i;
+            if (row >= w.row0 && row < w.row1)
+                continue;
+            const float3 wv = xyz(ldcg4(wb[cur] + row));
+            const float3 sv = first ? make_float3(0, 0, 0) : xyz(ldcg4(sb[cur] + row));
+            const float3 rv = xyz(ldcg4(rb[cur] + row));
+            float3 s_new;
+            const float3 r_new = cg1_residual(rv, wv, sv, af, bf, first, s_new);
+            float M[6];
+            load_sym(d.M0, d.M1, row, M);
+            su[i] = f4(symv(M, r_new));
+        }
+        __syncthreads();
+        // ---- w = A u on own rows; delta = w.u
+        for (int ch = warp; ch < nch; ch += NW)
+        {
+            const int li = ch * 32 + lane;
+            const int row = w.row0 + li;
+            float pd = 0.f;
+            if (li < nrow)
+                pd = spmv_row(row, xyz(su[row - h0]), wb[nxt]);
+            pd = warp_sum(pd);
+            if (lane == 0)
+                f.add(1, pd, s1q);
+        }
+        bq = (bq + 1) % 3;
+        it++;
+        if (!team_sum(f, bq))
+        {
+            status = 9; // CLOTH_ERR_TIMEOUT
+            break;
+        }
+    }
+    // ---- own rows back to the standard buffers: dx, and r into d.r
+    __syncthreads();
+    for (int i = tid; i < nrow; i += kPBlock)
+    {
+        const int row = w.row0 + i;
+        d.dx[row] = sx[i];
+        if (it & 1)
+            d.r[row] = ldcg4(rb[1] + row);
+    }
+    if (w.rank == 0 && tid == 0)
+    {
+        st->iter = it;
+        st->status = status;
+        st->rho = s_gam;
+        st->rr = s_rr;
+        st->pq = s_del;
+        st->alpha = s_alpha;
+        st->beta = s_beta;
+        st->active = 0;
+    }
+}
+
 // ------------------------------------------------------------------ advance
 __global__ void __launch_bounds__(kTile) k_advance(InstDesc *const *descs,
                                                    const Tile *tiles,

@@ -196,6 +196,14 @@ def algorithmic_bytes(nv: int, nnzb: int) -> dict:
             "matrix": 24 * up + 4 * nnzb + 4 * lo}
 
 
+def single_barrier_bytes(nv: int, nnzb: int) -> int:
+    """Unique bytes of one iteration of the single-barrier persistent PCG:
+    the matrix as above, 4*nv row info, 16*nv w written, 80*nv for w, s, r read
+    and s, r written (dx, p, u and M^-1 of a block's own rows stay in shared
+    memory; the halo's r, w, s are the owners' values, read again from L2)."""
+    return algorithmic_bytes(nv, nnzb)["matrix"] + 100 * nv
+
+
 def graph_loop_bytes(nv: int, nnzb: int) -> int:
     """Unique bytes of one iteration of the two-kernel loop (k_spmv, k_update),
     the batched and served solver: the matrix as above, k_spmv 68*nv (row info,
@@ -278,6 +286,8 @@ def run_ours(args, rank, world, local, pg):
     b.build_all()
     torch.cuda.set_device(local)
     ctx = ClothContext(local)
+    if args.solver:
+        ctx.set_solver(args.solver)
     stream = torch.cuda.ExternalStream(ctx.stream_ptr(), device=torch.device("cuda", local))
     conf = workload_conf()
     cloth = BaraffClothGpu(ctx, conf)
@@ -318,7 +328,7 @@ def run_ours(args, rank, world, local, pg):
     t_max = max_over_ranks(pg, sum(step_ms) / 1e3)
     steps_total = sum_over_ranks(pg, float(args.steps))
     value = steps_total / t_max if t_max > 0 else 0.0
-    per_step = 5 if st["solver"] == "persistent" else None
+    per_step = 5 if st["solver"].startswith("persistent") else None
     launches = sum(per_step if per_step else 5 + 2 * i for i in iters)
 
     # ---- e2e: the same steps through the C ABI with host buffers, pinned
@@ -358,12 +368,17 @@ def run_ours(args, rank, world, local, pg):
     shares = {k: round(v["ms"] / total_ms, 4) if total_ms else None for k, v in prof.items()}
     solver = st["solver"]
     sp = prof["spmv_dot"]
-    if solver == "persistent":
+    per_iter = alg["iteration"]
+    if solver == "persistent_1b":
+        per_iter = single_barrier_bytes(nv, nnzb)
+    if solver.startswith("persistent"):
         # one launch per step runs all iterations: bytes per launch = iterations x
         # bytes per iteration
         launch_ms = sp["ms"] / max(1, sp["launches"])
-        bytes_launch = alg["iteration"] * float(np.mean(prof_iters))
-        kname = "k_pcg_persistent (all PCG iterations of the step in one cooperative launch)"
+        bytes_launch = per_iter * float(np.mean(prof_iters))
+        kname = ("k_pcg1_persistent (single-barrier PCG, all iterations of the step in one "
+                 "cooperative launch)" if solver == "persistent_1b" else
+                 "k_pcg_persistent_sm (all PCG iterations of the step in one cooperative launch)")
     else:
         launch_ms = sp["ms"] / max(1, sp["launches"])
         bytes_launch = alg["spmv_dot"]
@@ -372,11 +387,12 @@ def run_ours(args, rank, world, local, pg):
     roof = {"bound": "hbm", "kernel": kname,
             "achieved": achieved, "peak": peak["hbm_gbs"], "unit": "GB/s",
             "frac": achieved / peak["hbm_gbs"], "peak_source": f"{peak['source']} hbm_gbs",
-            "traffic": ncu_traffic("k_pcg_persistent_sm", float(np.mean(prof_iters)))
-            if solver == "persistent" else None,
+            "traffic": ncu_traffic("k_pcg1_persistent" if solver == "persistent_1b"
+                                   else "k_pcg_persistent_sm", float(np.mean(prof_iters)))
+            if solver.startswith("persistent") else None,
             "traffic_source": "profiles/ncu_traffic.json (ncu capture, 20 iterations of this workload, scaled by iterations)",
             "algorithmic_bytes_per_launch": bytes_launch,
-            "algorithmic_bytes_per_iteration": alg["iteration"],
+            "algorithmic_bytes_per_iteration": per_iter,
             "avg_launch_ms": launch_ms,
             "us_per_pcg_iteration": 1e3 * sp["ms"] / max(1, sum(prof_iters)),
             "phase_share": shares, "solver": solver, "nnzb": nnzb}
@@ -889,7 +905,8 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--profile-iters", type=int, default=0,
                     help="run only the small ncu case: one step, PCG capped at N iterations")
-    ap.add_argument("--solver", choices=["persistent", "graph_loop"], default=None)
+    ap.add_argument("--solver", choices=["persistent", "persistent_1b", "persistent_2b",
+                                         "graph_loop"], default=None)
     ap.add_argument("--profile-side", type=int, default=N_SIDE,
                     help="grid side of the single-cloth ncu case")
     ap.add_argument("--mode", choices=["step", "batch", "serve", "precision"], default="step",

@@ -104,6 +104,12 @@ typedef struct {
 #define CLOTH_SOLVER_PERSISTENT 0
 #define CLOTH_SOLVER_GRAPH_LOOP 1
 #define CLOTH_SOLVER_FP64 2       /* cloth_solve_fp64 */
+/* PERSISTENT_1B: the persistent launch with one team barrier per iteration
+ * (the same PCG in the Chronopoulos-Gear arrangement: r.u, w.u and r.r summed
+ * together), used where every block's halo fits in shared memory; stats report
+ * which one ran. PERSISTENT_2B: only the two-barrier persistent kernel. */
+#define CLOTH_SOLVER_PERSISTENT_1B 3
+#define CLOTH_SOLVER_PERSISTENT_2B 4
 
 /* ---------------------------------------------------------------- library */
 int cloth_abi_version(void);

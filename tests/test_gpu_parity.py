@@ -69,7 +69,7 @@ def test_assembly_matches_reference(ctx, case):
     c.close()
 
 
-SOLVERS = ["persistent", "graph_loop"]
+SOLVERS = ["persistent", "persistent_1b", "graph_loop"]
 
 
 @pytest.fixture(params=SOLVERS)
@@ -249,7 +249,7 @@ def test_solvers_agree(ctx):
     p = params(max_iters=5000, rel_tol=1e-6)
     conf = _grid_conf(64)
     out = {}
-    for sv in ("persistent", "graph_loop"):
+    for sv in ("persistent", "persistent_1b", "graph_loop"):
         ctx.set_solver(sv)
         c = make(ctx, conf)
         x, xp = _perturbed(c, 11, 2e-3)
@@ -260,15 +260,18 @@ def test_solvers_agree(ctx):
         out[sv] = (c.GetPos() - x, st["iters"])
         c.close()
     ctx.set_solver("persistent")
-    assert abs(out["persistent"][1] - out["graph_loop"][1]) <= 2
-    assert rel(out["persistent"][0], out["graph_loop"][0]) < 1e-4
+    for sv in ("persistent", "persistent_1b"):
+        assert abs(out[sv][1] - out["graph_loop"][1]) <= 2, (sv, out[sv][1], out["graph_loop"][1])
+        assert rel(out[sv][0], out["graph_loop"][0]) < 1e-4
 
 
-def test_persistent_many_instances(ctx):
+@pytest.mark.parametrize("psolver", ["persistent", "persistent_1b"])
+def test_persistent_many_instances(ctx, psolver):
     """A set with more instances than one block each still solves (teams of
     one block need no grid barrier; large ones span many blocks)."""
     from acousticsim_gb300 import params
     p = params(max_iters=5000, rel_tol=1e-6)
+    ctx.set_solver(psolver)
     cl = []
     for k, n in enumerate([16, 16, 130, 20, 64]):
         c = make(ctx, _grid_conf(n))
@@ -277,7 +280,8 @@ def test_persistent_many_instances(ctx):
         c.SetPrePos(xp)
         cl.append(c)
     stats = ctx.batch_step(cl, 0.0, p)
-    assert all(s["status"] == "OK" and s["solver"] == "persistent" for s in stats), stats
+    ctx.set_solver("persistent")
+    assert all(s["status"] == "OK" and s["solver"] == psolver for s in stats), stats
     for c in cl:
         c.close()
 
