@@ -744,7 +744,7 @@ int cloth_solve_refined(cloth_t *c, const cloth_solve_params *inner, double rel_
             out.status = CLOTH_OK;
             break;
         }
-        if (out.outer >= max_outer || out.rejected > 12)
+        if (out.outer >= max_outer || out.rejected > 6)
             break;
         // FP32 correction: A e = float(r), then dx64 += e
         if (restored)
