@@ -735,11 +735,11 @@ int plan_persistent(cloth_ctx *ctx, Batch *b)
     }
     while (int(work.size()) < G)
         work.push_back(TeamBlock{-1, 0, 0, 0, 0, -1, -1, 0});
-    // own-row state (dx, r, q, M^-1: 72 bytes per row) in shared memory when
-    // it fits next to the staged p
+    // own-row state (dx, r, q, z, M^-1: 88 bytes per row) in shared memory
+    // when it fits next to the staged p
     b->halo_cap = max_entries;
     b->rows_cap = max_rows;
-    const size_t sm_bytes = size_t(max_entries) * sizeof(float4) + size_t(max_rows) * 72;
+    const size_t sm_bytes = size_t(max_entries) * sizeof(float4) + size_t(max_rows) * 88;
     b->persist_sm = sm_bytes <= smem_cap_bytes;
     b->smem_persist = b->persist_sm ? sm_bytes : size_t(max_entries) * sizeof(float4);
     // the single-barrier variant keeps dx, p and M^-1 per own row (56 bytes)
