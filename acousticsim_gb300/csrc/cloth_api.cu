@@ -735,11 +735,13 @@ int plan_persistent(cloth_ctx *ctx, Batch *b)
     }
     while (int(work.size()) < G)
         work.push_back(TeamBlock{-1, 0, 0, 0, 0, -1, -1, 0});
-    // own-row state (dx, r, q, z, M^-1: 88 bytes per row) in shared memory
-    // when it fits next to the staged p
+    // own-row state (dx, r, q, M^-1: 72 bytes per row) in shared memory when
+    // it fits next to the staged p.  (Keeping z there as well was measured
+    // slower: at 512^2 it pushes the block past the 196 KB shared-memory
+    // carve-out, and the L1 left for the matrix and gathers halves.)
     b->halo_cap = max_entries;
     b->rows_cap = max_rows;
-    const size_t sm_bytes = size_t(max_entries) * sizeof(float4) + size_t(max_rows) * 88;
+    const size_t sm_bytes = size_t(max_entries) * sizeof(float4) + size_t(max_rows) * 72;
     b->persist_sm = sm_bytes <= smem_cap_bytes;
     b->smem_persist = b->persist_sm ? sm_bytes : size_t(max_entries) * sizeof(float4);
     // the single-barrier variant keeps dx, p and M^-1 per own row (56 bytes)

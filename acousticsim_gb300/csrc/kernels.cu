@@ -1373,8 +1373,7 @@ __device__ __forceinline__ void pcg_persistent_body(InstDesc *const *descs,
     float4 *sdx = sp + halo_cap;
     float4 *sr = sdx + rows_cap;
     float4 *sq = sr + rows_cap;
-    float4 *sz = sq + rows_cap; // own rows' z (the staged p of own rows needs no global read)
-    float4 *sm0 = sz + rows_cap;
+    float4 *sm0 = sq + rows_cap;
     float2 *sm1 = reinterpret_cast<float2 *>(sm0 + rows_cap);
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -1388,7 +1387,6 @@ __device__ __forceinline__ void pcg_persistent_body(InstDesc *const *descs,
             const int row = w.row0 + i;
             sdx[i] = d.dx[row];
             sr[i] = d.r[row];
-            sz[i] = d.z[row];
             sm0[i] = d.M0[row];
             sm1[i] = d.M1[row];
         }
@@ -1480,21 +1478,6 @@ __device__ __forceinline__ void pcg_persistent_body(InstDesc *const *descs,
             for (int i = tid; i < w.halo1 - w.halo0; i += kPBlock)
             {
                 const int c = w.halo0 + i;
-                if (SM && c >= w.row0 && c < w.row1)
-                {
-                    // own row: z from shared memory, p_old is this slot's
-                    // previous value (the p this block staged and wrote)
-                    float4 pn = sz[c - w.row0];
-                    if (!first)
-                    {
-                        const float4 po = sp[i];
-                        pn.x = fmaf(bf, po.x, pn.x);
-                        pn.y = fmaf(bf, po.y, pn.y);
-                        pn.z = fmaf(bf, po.z, pn.z);
-                    }
-                    sp[i] = pn;
-                    continue;
-                }
                 float4 pn = ldcg4(d.z + c);
                 if (!first)
                 {
@@ -1674,8 +1657,6 @@ __device__ __forceinline__ void pcg_persistent_body(InstDesc *const *descs,
                     d.r[row] = f4(r);
                 }
                 d.z[row] = f4(z);
-                if (SM)
-                    sz[li] = f4(z);
                 pr = fdot(r, z);
                 prr = fdot(r, r);
             }
