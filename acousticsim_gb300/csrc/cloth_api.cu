@@ -741,7 +741,8 @@ int plan_persistent(cloth_ctx *ctx, Batch *b)
     // carve-out, and the L1 left for the matrix and gathers halves.)
     b->halo_cap = max_entries;
     b->rows_cap = max_rows;
-    const size_t sm_bytes = size_t(max_entries) * sizeof(float4) + size_t(max_rows) * 72;
+    const size_t sm_bytes = size_t(max_entries) * sizeof(float4) +
+                            size_t(max_rows) * (kPersistMShared ? 72 : 48);
     b->persist_sm = sm_bytes <= smem_cap_bytes;
     b->smem_persist = b->persist_sm ? sm_bytes : size_t(max_entries) * sizeof(float4);
     // the single-barrier variant keeps dx, p and M^-1 per own row (56 bytes)

@@ -1387,8 +1387,11 @@ __device__ __forceinline__ void pcg_persistent_body(InstDesc *const *descs,
             const int row = w.row0 + i;
             sdx[i] = d.dx[row];
             sr[i] = d.r[row];
-            sm0[i] = d.M0[row];
-            sm1[i] = d.M1[row];
+            if (kPersistMShared)
+            {
+                sm0[i] = d.M0[row];
+                sm1[i] = d.M1[row];
+            }
         }
     if (tid == 0)
     {
@@ -1632,7 +1635,7 @@ __device__ __forceinline__ void pcg_persistent_body(InstDesc *const *descs,
                 r = make_float3(fmaf(-af, qv.x, r.x), fmaf(-af, qv.y, r.y),
                                 fmaf(-af, qv.z, r.z));
                 float M[6];
-                if (SM)
+                if (SM && kPersistMShared)
                 {
                     const float4 u = sm0[li];
                     const float2 v = sm1[li];
