@@ -43,7 +43,10 @@ class Material(C.Structure):
     _fields_ = [("stretch_k", C.c_float * 3), ("bending_k", C.c_float * 2),
                 ("density", C.c_float), ("rayleigh_a", C.c_float), ("rayleigh_b", C.c_float),
                 ("default_timestep", C.c_double), ("gravity", C.c_double),
-                ("fix_fv_norm", C.c_int)]
+                ("fix_fv_norm", C.c_int), ("bending_model", C.c_int)]
+
+
+BENDING_MODELS = {"quadratic": 0, "dihedral": 1}
 
 
 class SolveParams(C.Structure):
@@ -159,6 +162,7 @@ SIGNATURES = {
     "cloth_get_dx": (C.c_int, [P, PD, C.c_int]),
     "cloth_export_system": (C.c_int, [P, PI, PF, PF, PF, PF]),
     "cloth_export_triangles": (C.c_int, [P, PF, PF]),
+    "cloth_export_dihedral": (C.c_int, [P, PI, PI, PF, PF]),
     "cloth_export_tables": (C.c_int, [P, PI, PF, PF, PF, PI]),
     "cloth_step_plain": (C.c_int, [P, C.c_double, C.POINTER(SolveParams), C.POINTER(SolveStats)]),
     "cloth_batch_step": (C.c_int, [P, C.POINTER(P), C.c_int, C.c_double,

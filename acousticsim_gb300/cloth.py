@@ -198,7 +198,8 @@ class BaraffClothGpu:
                           float(conf["cloth_density"]), float(conf.get("rayleigh_damping_a", 0.0)),
                           float(conf.get("rayleigh_damping_b", 0.0)),
                           float(conf["default_timestep"]), float(conf.get("gravity", -9.8)),
-                          int(conf.get("fix_fv_norm", 0)))
+                          int(conf.get("fix_fv_norm", 0)),
+                          N.BENDING_MODELS[conf.get("cloth_bending_model", "quadratic")])
 
     @property
     def handle(self):
@@ -365,6 +366,16 @@ class BaraffClothGpu:
         h = np.zeros((self.nt, 9, 3, 3), np.float32)
         N.call("cloth_export_triangles", self._h, N.ptr(f, C.c_float), N.ptr(h, C.c_float))
         return {"fint": f, "hess": h}
+
+    def export_dihedral(self) -> dict:
+        n = C.c_int()
+        N.call("cloth_export_dihedral", self._h, C.byref(n), None, None, None)
+        ids = np.zeros(n.value, np.int32)
+        g = np.zeros((n.value, 4, 3), np.float32)
+        cf = np.zeros((n.value, 2), np.float32)
+        N.call("cloth_export_dihedral", self._h, C.byref(n), N.ptr(ids, C.c_int),
+               N.ptr(g, C.c_float), N.ptr(cf, C.c_float))
+        return {"edge_ids": ids, "grad": g, "factor": cf[:, 0], "force_coef": cf[:, 1]}
 
     def export_tables(self) -> dict:
         ne = C.c_int()

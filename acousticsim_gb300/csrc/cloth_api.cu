@@ -68,13 +68,21 @@ struct Batch
     bool tuned = false;
     int grid_spmv = 1, grid_update = 1;
     int spmv_waves = 8, upd_waves = 8;
+    // a member carries skew block parts (dihedral bending): the SpMV variants
+    // that apply them
+    bool skew = false;
+    const GraphLoopVariant &spmv_variant(int v) const
+    {
+        return (skew ? kSpmvSkewVariants : kSpmvVariants)[v];
+    }
+    int spmv_occ(int v) const { return (skew ? ctx->occ_spmv_skew : ctx->occ_spmv)[v]; }
     void set_variants(int sv, int uv, int sw = 8, int uw = 8)
     {
         spmv_v = sv;
         upd_v = uv;
         spmv_waves = sw;
         upd_waves = uw;
-        grid_spmv = grid_for(kSpmvVariants[sv], ctx->occ_spmv[sv], sw);
+        grid_spmv = grid_for(spmv_variant(sv), spmv_occ(sv), sw);
         grid_update = grid_for(kUpdateVariants[uv], ctx->occ_update[uv], uw);
     }
     // one block per group of TPB tiles, at most `waves` full waves of resident
@@ -184,7 +192,8 @@ int upload_tables(cloth_s *c)
     const Tables &t = c->tab;
     const int n = t.nv, T = t.nt, W = t.width;
     const int S = int(align_up(size_t(n), 32));
-    const int ntr = (n + kTile - 1) / kTile, ntt = (T + kTile - 1) / kTile;
+    // the triangle pass also runs the dihedral edges (indices nt .. nt + n_dih)
+    const int ntr = (n + kTile - 1) / kTile, ntt = (T + t.n_dih + kTile - 1) / kTile;
     const size_t WS = size_t(W) * S;
     // planes of the stored (diagonal + upper) blocks and of the lower slots
     int Wu = 1, Wl = 0;
@@ -201,6 +210,16 @@ int upload_tables(cloth_s *c)
            o_tdest = L.take<int4>(3 * size_t(T));
     size_t o_col = L.take<int>(WS), o_hsrc = L.take<uint32_t>(WS), o_kb = L.take<float>(WS),
            o_lidx = L.take<uint32_t>(WlS), o_colu = L.take<int>(WuS);
+    const int nd = t.n_dih;
+    const bool dih = c->mat.bending_model == 1;
+    size_t o_dvid = 0, o_dfac = 0, o_dsrc = 0, o_dent = 0;
+    if (dih)
+    {
+        o_dvid = L.take<int4>(std::max(nd, 1));
+        o_dfac = L.take<double>(std::max(nd, 1));
+        o_dsrc = L.take<uint32_t>(WS);
+        o_dent = L.take<uint32_t>(std::max<size_t>(t.dih_ent.size(), 1));
+    }
     size_t o_rowinfo = L.take<int>(n), o_fptr = L.take<int>(n + 1),
            o_mass = L.take<float>(n), o_grav = L.take<float>(n);
     size_t o_pv = L.take<int>(n + 1), o_pt = L.take<float4>(n + 1);
@@ -225,6 +244,12 @@ int upload_tables(cloth_s *c)
     sl.q = W2.take<float4>(n);
     sl.w1 = W2.take<float4>(n);
     sl.part = W2.take<double>(3 * size_t(ntr));
+    if (dih)
+    {
+        sl.drec = W2.take<float4>(4 * size_t(std::max(nd, 1)));
+        sl.dfb = W2.take<float>(std::max(nd, 1));
+        sl.Aw = W2.take<float4>(WuS);
+    }
     sl.bytes = W2.off;
 
     char *base = nullptr;
@@ -320,6 +345,36 @@ int upload_tables(cloth_s *c)
                        cudaMemcpyHostToDevice, s));
     CK(cudaMemcpyAsync(base + o_rowinfo, rowinfo.data(), n * sizeof(int),
                        cudaMemcpyHostToDevice, s));
+    std::vector<int4> dvid;
+    std::vector<uint32_t> dsrc;
+    if (dih)
+    {
+        dvid.resize(nd);
+        for (int q = 0; q < nd; q++)
+        {
+            const int *st4 = &t.stencil[size_t(t.dih_edge[q]) * 4];
+            dvid[q] = make_int4(st4[0], st4[1], st4[2], st4[3]);
+        }
+        dsrc.assign(WS, 0u);
+        for (int v = 0; v < n; v++)
+            for (int sl = 0; sl < t.rowptr[v + 1] - t.rowptr[v]; sl++)
+            {
+                const size_t k = size_t(t.rowptr[v]) + sl;
+                dsrc[size_t(sl) * S + v] =
+                    (uint32_t(t.dih_start[k]) << 5) | uint32_t(t.dih_count[k]);
+            }
+        if (nd > 0)
+        {
+            CK(cudaMemcpyAsync(base + o_dvid, dvid.data(), nd * sizeof(int4),
+                               cudaMemcpyHostToDevice, s));
+            CK(cudaMemcpyAsync(base + o_dfac, t.dih_factor.data(), nd * sizeof(double),
+                               cudaMemcpyHostToDevice, s));
+            CK(cudaMemcpyAsync(base + o_dent, t.dih_ent.data(),
+                               t.dih_ent.size() * sizeof(uint32_t), cudaMemcpyHostToDevice, s));
+        }
+        CK(cudaMemcpyAsync(base + o_dsrc, dsrc.data(), WS * sizeof(uint32_t),
+                           cudaMemcpyHostToDevice, s));
+    }
     CK(cudaMemcpyAsync(base + o_fptr, t.f_rowptr.data(), (n + 1) * sizeof(int),
                        cudaMemcpyHostToDevice, s));
     CK(cudaMemcpyAsync(base + o_mass, mass.data(), n * sizeof(float),
@@ -351,6 +406,14 @@ int upload_tables(cloth_s *c)
     h.kb = reinterpret_cast<const float *>(base + o_kb);
     h.lidx = reinterpret_cast<const uint32_t *>(base + o_lidx);
     h.colu = reinterpret_cast<const int *>(base + o_colu);
+    if (dih)
+    {
+        h.n_dih = nd;
+        h.dvid = reinterpret_cast<const int4 *>(base + o_dvid);
+        h.dfac = reinterpret_cast<const double *>(base + o_dfac);
+        h.dsrc = reinterpret_cast<const uint32_t *>(base + o_dsrc);
+        h.dent = reinterpret_cast<const uint32_t *>(base + o_dent);
+    }
     h.rowinfo = reinterpret_cast<const int *>(base + o_rowinfo);
     h.fptr = reinterpret_cast<const int *>(base + o_fptr);
     h.mass = reinterpret_cast<const float *>(base + o_mass);
@@ -375,8 +438,13 @@ int upload_tables(cloth_s *c)
 void cloth::detail::bind_scratch(const cloth_s *c, InstDesc &h, char *base)
 {
     const ScratchLayout &sl = c->sl;
-    auto at = [&](size_t o) { return base ? base + o : nullptr; };
+    auto at = [&](size_t o) {
+        return (base && o != ScratchLayout::kAbsent) ? base + o : nullptr;
+    };
     h.hrec = reinterpret_cast<HRec *>(at(sl.hrec));
+    h.drec = reinterpret_cast<float4 *>(at(sl.drec));
+    h.dfb = reinterpret_cast<float *>(at(sl.dfb));
+    h.Aw = reinterpret_cast<float4 *>(at(sl.Aw));
     h.frec = reinterpret_cast<float4 *>(at(sl.frec));
     h.A0 = reinterpret_cast<float4 *>(at(sl.A0));
     h.A1 = reinterpret_cast<float2 *>(at(sl.A1));
@@ -569,8 +637,10 @@ int make_batch(cloth_ctx *ctx, const std::vector<cloth_s *> &members,
         inst.push_back(int(i));
         for (int s = 0; s < c->tab.nv; s += kTile)
             rt.push_back(Tile{int(i), s, c->d_desc, c->d_state});
-        for (int s = 0; s < c->tab.nt; s += kTile)
+        // the triangle pass also covers the dihedral edges (after the triangles)
+        for (int s = 0; s < c->tab.nt + c->tab.n_dih; s += kTile)
             tt.push_back(Tile{int(i), s, c->d_desc, c->d_state});
+        b->skew = b->skew || c->h.Aw != nullptr;
     }
     b->n_rt = int(rt.size());
     b->n_tt = int(tt.size());
@@ -602,6 +672,17 @@ int make_batch(cloth_ctx *ctx, const std::vector<cloth_s *> &members,
         return rc;
     out = std::move(b);
     return CLOTH_OK;
+}
+
+// The persistent kernel a plan launches.
+const void *persistent_kernel(const Batch *b)
+{
+    if (b->persist_1b)
+        return (const void *)k_pcg1_persistent;
+    if (b->skew)
+        return b->persist_sm ? (const void *)k_pcg_persistent_sm_skew
+                             : (const void *)k_pcg_persistent_gm_skew;
+    return b->persist_sm ? (const void *)k_pcg_persistent_sm : (const void *)k_pcg_persistent_gm;
 }
 
 // Team plan of the persistent solver: every instance gets blocks in
@@ -747,13 +828,17 @@ int plan_persistent(cloth_ctx *ctx, Batch *b)
     b->smem_persist = b->persist_sm ? sm_bytes : size_t(max_entries) * sizeof(float4);
     // the single-barrier variant keeps dx, p and M^-1 per own row (56 bytes)
     // next to u over the halo: it fits wherever the two-barrier one does
-    b->persist_1b = b->persist_sm && all_staged && ctx->solver == CLOTH_SOLVER_PERSISTENT_1B;
+    // (it has no skew block parts: launch sets with a dihedral-bending
+    // instance take the two-barrier kernel)
+    b->persist_1b = b->persist_sm && all_staged && ctx->solver == CLOTH_SOLVER_PERSISTENT_1B &&
+                    !b->skew;
     int occ2 = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-            &occ2,
-            b->persist_1b ? k_pcg1_persistent
-                          : (b->persist_sm ? k_pcg_persistent_sm : k_pcg_persistent_gm),
-            kPBlock, b->smem_persist) != cudaSuccess ||
+    if (cudaFuncSetAttribute(k_pcg_persistent_sm_skew, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             int(smem_cap_bytes)) != cudaSuccess ||
+        cudaFuncSetAttribute(k_pcg_persistent_gm_skew, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             int(smem_cap_bytes)) != cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ2, persistent_kernel(b), kPBlock,
+                                                      b->smem_persist) != cudaSuccess ||
         occ2 * ctx->num_sms < int(work.size()))
     {
         cudaGetLastError();
@@ -841,9 +926,7 @@ int build_graph(Batch *b, bool full, cudaGraphExec_t *exec)
         {
             cudaKernelNodeParams p;
             std::memset(&p, 0, sizeof(p));
-            p.func = b->persist_1b   ? (void *)k_pcg1_persistent
-                     : b->persist_sm ? (void *)k_pcg_persistent_sm
-                                     : (void *)k_pcg_persistent_gm;
+            p.func = const_cast<void *>(persistent_kernel(b));
             p.gridDim = dim3(b->grid_persist);
             p.blockDim = dim3(kPBlock);
             p.sharedMemBytes = unsigned(b->smem_persist);
@@ -878,7 +961,7 @@ int build_graph(Batch *b, bool full, cudaGraphExec_t *exec)
         {
             cudaGraph_t body = cp.conditional.phGraph_out[0];
             cudaGraphNode_t k1, k2;
-            const GraphLoopVariant &sv = kSpmvVariants[b->spmv_v];
+            const GraphLoopVariant &sv = b->spmv_variant(b->spmv_v);
             const GraphLoopVariant &uv = kUpdateVariants[b->upd_v];
             rc = add_kernel(body, &k1, nullptr, 0, const_cast<void *>(sv.func), b->grid_spmv,
                             kTile / sv.rows_per_thread, a_spmv);
@@ -927,9 +1010,7 @@ int launch_persistent(Batch *b)
     cloth_ctx *ctx = b->ctx;
     PhaseTimer t(ctx, PH_SPMV);
     void *args[] = {&b->d_descs, &b->d_work, &b->halo_cap, &b->rows_cap};
-    CK(cudaLaunchCooperativeKernel(b->persist_1b   ? (void *)k_pcg1_persistent
-                                   : b->persist_sm ? (void *)k_pcg_persistent_sm
-                                                   : (void *)k_pcg_persistent_gm,
+    CK(cudaLaunchCooperativeKernel(persistent_kernel(b),
                                    dim3(b->grid_persist), dim3(kPBlock), args,
                                    b->smem_persist, ctx->stream));
     return CLOTH_OK;
@@ -946,7 +1027,7 @@ int launch_solve_host(Batch *b, int max_iters)
     int *no_left = nullptr;
     void *a_spmv[] = {&b->d_descs, &b->d_rt, &b->d_ctl, &zero, &none};
     void *a_upd[] = {&b->d_descs, &b->d_rt, &b->d_ctl, &zero, &none, &no_left};
-    const GraphLoopVariant &sv = kSpmvVariants[b->spmv_v];
+    const GraphLoopVariant &sv = b->spmv_variant(b->spmv_v);
     const GraphLoopVariant &uv = kUpdateVariants[b->upd_v];
     int *h_active = nullptr;
     CK(cudaMallocHost(&h_active, sizeof(int)));
@@ -1105,11 +1186,11 @@ int autotune_graph_loop(Batch *b)
         float tv = 1e30f;
         for (int wv : kWaves)
         {
-            const int g = b->grid_for(kSpmvVariants[v], ctx->occ_spmv[v], wv);
+            const int g = b->grid_for(b->spmv_variant(v), b->spmv_occ(v), wv);
             float t = 1e30f;
             for (int rep = 0; rep < 4; rep++)
             {
-                const float ms = time_launch(kSpmvVariants[v], g, a_spmv);
+                const float ms = time_launch(b->spmv_variant(v), g, a_spmv);
                 if (rep > 0)
                     t = std::min(t, ms);
             }
@@ -1124,9 +1205,9 @@ int autotune_graph_loop(Batch *b)
         ctx->tune_ms_spmv[v] = tv;
     }
     // leave the state of iteration 0 with alpha set, as the loop expects it
-    cudaLaunchKernel(kSpmvVariants[best_s].func,
-                     dim3(b->grid_for(kSpmvVariants[best_s], ctx->occ_spmv[best_s], best_sw)),
-                     dim3(kTile / kSpmvVariants[best_s].rows_per_thread), a_spmv, 0, s);
+    cudaLaunchKernel(b->spmv_variant(best_s).func,
+                     dim3(b->grid_for(b->spmv_variant(best_s), b->spmv_occ(best_s), best_sw)),
+                     dim3(kTile / b->spmv_variant(best_s).rows_per_thread), a_spmv, 0, s);
     snap(0);
     t_best = 1e30f;
     for (int v = 0; v < kNumUpdateVariants; v++)
@@ -1321,10 +1402,16 @@ int cloth_ctx_create(int device, cloth_ctx **out)
     CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c->occ_row, k_row, kTile, 0));
     c->occ_spmv.assign(kNumSpmvVariants, 1);
     c->occ_update.assign(kNumUpdateVariants, 1);
+    c->occ_spmv_skew.assign(kNumSpmvVariants, 1);
     for (int v = 0; v < kNumSpmvVariants; v++)
+    {
         CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
             &c->occ_spmv[v], kSpmvVariants[v].func, kTile / kSpmvVariants[v].rows_per_thread,
             0));
+        CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+            &c->occ_spmv_skew[v], kSpmvSkewVariants[v].func,
+            kTile / kSpmvSkewVariants[v].rows_per_thread, 0));
+    }
     for (int v = 0; v < kNumUpdateVariants; v++)
         CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
             &c->occ_update[v], kUpdateVariants[v].func,
@@ -1574,6 +1661,7 @@ static void copy_material(const cloth_material *mat, Material &mt)
     mt.default_timestep = mat->default_timestep;
     mt.gravity = mat->gravity;
     mt.fix_fv_norm = mat->fix_fv_norm;
+    mt.bending_model = mat->bending_model;
 }
 
 int cloth_host_tables(const cloth_mesh_desc *mesh, const cloth_material *mat,
@@ -1737,6 +1825,9 @@ int cloth_set_material(cloth_t *c, const cloth_material *mat)
     std::lock_guard<std::recursive_mutex> lk(c->ctx->mu);
     CK(cudaSetDevice(c->ctx->device));
     Material &mt = c->mat;
+    if (mat->bending_model != mt.bending_model)
+        return fail(CLOTH_ERR_INVALID,
+                    "cloth_set_material: the bending model is fixed when the cloth is created");
     bool bend = mt.bending_k[0] != mat->bending_k[0] || mt.bending_k[1] != mat->bending_k[1];
     std::memcpy(mt.stretch_k, mat->stretch_k, sizeof(mt.stretch_k));
     std::memcpy(mt.bending_k, mat->bending_k, sizeof(mt.bending_k));
@@ -1755,6 +1846,12 @@ int cloth_set_material(cloth_t *c, const cloth_material *mat)
                 kb[size_t(s) * c->h.stride + v] = t.kbend[size_t(t.rowptr[v]) + s];
         CK(cudaMemcpy(const_cast<float *>(c->h.kb), kb.data(), kb.size() * sizeof(float),
                       cudaMemcpyHostToDevice));
+        if (mt.bending_model == 1 && c->tab.n_dih > 0)
+        {
+            rebuild_dihedral_factor(c->mesh, mt, c->tab);
+            CK(cudaMemcpy(const_cast<double *>(c->h.dfac), c->tab.dih_factor.data(),
+                          c->tab.dih_factor.size() * sizeof(double), cudaMemcpyHostToDevice));
+        }
     }
     set_material_fields(c);
     c->dt_set = -1.0; // damping may have changed
@@ -2047,10 +2144,12 @@ int cloth_export_system(cloth_t *c, int *ell, float *A, float *b, float *fint,
         // stored diagonal + upper blocks; a lower block is its transposed
         // upper block (the same symmetric 6 floats)
         const size_t WuS = size_t(c->width_up) * S;
-        std::vector<float4> a0(WuS);
+        std::vector<float4> a0(WuS), aw(c->h.Aw ? WuS : 0);
         std::vector<float2> a1(WuS);
         CK(cudaMemcpy(a0.data(), c->h.A0, WuS * sizeof(float4), cudaMemcpyDeviceToHost));
         CK(cudaMemcpy(a1.data(), c->h.A1, WuS * sizeof(float2), cudaMemcpyDeviceToHost));
+        if (c->h.Aw)
+            CK(cudaMemcpy(aw.data(), c->h.Aw, WuS * sizeof(float4), cudaMemcpyDeviceToHost));
         std::fill(A, A + size_t(n) * R * 9, 0.f);
         for (int v = 0; v < n; v++)
             for (int s = 0; s < t.rowptr[v + 1] - t.rowptr[v]; s++)
@@ -2068,6 +2167,19 @@ int cloth_export_system(cloth_t *c, int *ell, float *A, float *b, float *fint,
                 }
                 float e[6] = {a0[o].x, a0[o].y, a0[o].z, a0[o].w, a1[o].x, a1[o].y};
                 float full[9] = {e[0], e[1], e[2], e[1], e[3], e[4], e[2], e[4], e[5]};
+                if (c->h.Aw)
+                {
+                    // skew part: block p = S p + w x p; the lower block is
+                    // the transposed upper one, S p - w x p
+                    const float sg = s >= ds ? 1.f : -1.f;
+                    const float wx = sg * aw[o].x, wy = sg * aw[o].y, wz = sg * aw[o].z;
+                    full[1] -= wz;
+                    full[2] += wy;
+                    full[3] += wz;
+                    full[5] -= wx;
+                    full[6] -= wy;
+                    full[7] += wx;
+                }
                 std::memcpy(A + (size_t(v) * R + s) * 9, full, sizeof(full));
             }
     }
@@ -2084,10 +2196,19 @@ int cloth_export_system(cloth_t *c, int *ell, float *A, float *b, float *fint,
     }
     if (fint)
     {
-        // stretch part from the force records, bending part -K_b x
-        std::vector<float4> fr(size_t(t.nt) * 3), x32(n);
+        // stretch part from the force records, bending part -K_b x or the
+        // dihedral records' (c beta / 2) dbeta/dx
+        std::vector<float4> fr(size_t(t.nt) * 3), x32(n), dr(c->h.drec ? 4 * size_t(t.n_dih) : 0);
+        std::vector<float> dfb(c->h.drec ? t.n_dih : 0);
         CK(cudaMemcpy(fr.data(), c->h.frec, fr.size() * sizeof(float4), cudaMemcpyDeviceToHost));
         CK(cudaMemcpy(x32.data(), c->h.x32, x32.size() * sizeof(float4), cudaMemcpyDeviceToHost));
+        if (!dr.empty())
+        {
+            CK(cudaMemcpy(dr.data(), c->h.drec, dr.size() * sizeof(float4),
+                          cudaMemcpyDeviceToHost));
+            CK(cudaMemcpy(dfb.data(), c->h.dfb, dfb.size() * sizeof(float),
+                          cudaMemcpyDeviceToHost));
+        }
         for (int v = 0; v < n; v++)
         {
             float f[3] = {0, 0, 0};
@@ -2105,6 +2226,19 @@ int cloth_export_system(cloth_t *c, int *ell, float *A, float *b, float *fint,
                 f[1] -= t.kbend[k] * xc.y;
                 f[2] -= t.kbend[k] * xc.z;
             }
+            if (!dr.empty())
+            {
+                const size_t k = size_t(t.rowptr[v]) + t.diag_slot[v];
+                for (int j = 0; j < t.dih_count[k]; j++)
+                {
+                    const uint32_t en = t.dih_ent[size_t(t.dih_start[k]) + j];
+                    const float4 g = dr[4 * size_t(en >> 4) + ((en >> 2) & 3u)];
+                    const float fb = dfb[en >> 4];
+                    f[0] += fb * g.x;
+                    f[1] += fb * g.y;
+                    f[2] += fb * g.z;
+                }
+            }
             std::memcpy(fint + 3 * size_t(v), f, sizeof(f));
         }
     }
@@ -2114,6 +2248,44 @@ int cloth_export_system(cloth_t *c, int *ell, float *A, float *b, float *fint,
         for (int v = 0; v < n; v++)
             for (int s = 0; s < t.rowptr[v + 1] - t.rowptr[v]; s++)
                 kbend[size_t(v) * R + s] = t.kbend[size_t(t.rowptr[v]) + s];
+    }
+    return CLOTH_OK;
+}
+
+int cloth_export_dihedral(cloth_t *c, int *n_edges, int *edge_ids, float *grad, float *coef)
+{
+    if (!c)
+        return fail(CLOTH_ERR_INVALID, "cloth is NULL");
+    std::lock_guard<std::recursive_mutex> lk(c->ctx->mu);
+    const Tables &t = c->tab;
+    if (n_edges)
+        *n_edges = t.n_dih;
+    if (edge_ids && t.n_dih > 0)
+        std::memcpy(edge_ids, t.dih_edge.data(), t.dih_edge.size() * sizeof(int));
+    if ((!grad && !coef) || t.n_dih == 0)
+        return CLOTH_OK;
+    if (!c->scratch)
+        return fail(CLOTH_ERR_STATE, "export: the cloth is held by a server");
+    CK(cudaSetDevice(c->ctx->device));
+    CK(cudaStreamSynchronize(c->ctx->stream));
+    std::vector<float4> dr(4 * size_t(t.n_dih));
+    std::vector<float> dfb(t.n_dih);
+    CK(cudaMemcpy(dr.data(), c->h.drec, dr.size() * sizeof(float4), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(dfb.data(), c->h.dfb, dfb.size() * sizeof(float), cudaMemcpyDeviceToHost));
+    for (int q = 0; q < t.n_dih; q++)
+    {
+        for (int a = 0; a < 4 && grad; a++)
+        {
+            const float4 g = dr[4 * size_t(q) + a];
+            grad[size_t(q) * 12 + 3 * a + 0] = g.x;
+            grad[size_t(q) * 12 + 3 * a + 1] = g.y;
+            grad[size_t(q) * 12 + 3 * a + 2] = g.z;
+        }
+        if (coef)
+        {
+            coef[2 * size_t(q)] = dr[4 * size_t(q)].w;
+            coef[2 * size_t(q) + 1] = dfb[q];
+        }
     }
     return CLOTH_OK;
 }
@@ -2183,6 +2355,9 @@ int cloth_step_plain(cloth_t *c, double dt, const cloth_solve_params *params,
 {
     if (!c || !valid_params(params) || (params && params->max_iters > 100000))
         return fail(CLOTH_ERR_INVALID, "cloth_step_plain: bad argument");
+    if (c->mat.bending_model != 0)
+        return fail(CLOTH_ERR_INVALID, "cloth_step_plain: the reference-structured path has "
+                                       "the GPU cloth's quadratic bending only");
     std::lock_guard<std::recursive_mutex> lk(c->ctx->mu);
     CK(cudaSetDevice(c->ctx->device));
     CK(cudaStreamSynchronize(c->ctx->stream));

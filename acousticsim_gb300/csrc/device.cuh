@@ -99,12 +99,21 @@ struct InstDesc
     const int *pin_vid;     // npins
     const float4 *pin_tgt;  // npins
     int npins;
+    // dihedral bending (all null, n_dih = 0, with the quadratic model)
+    int n_dih;               // interior edges
+    const int4 *dvid;        // n_dih stencils (v0 v1 v2 v3)
+    const double *dfac;      // n_dih rest factors -K e / (h0 + h1)
+    const uint32_t *dsrc;    // [slot][stride] first entry << 5 | entry count
+    const uint32_t *dent;    // entries q << 4 | a << 2 | b
     // records written by the triangle pass
     HRec *hrec;
     float4 *frec;
+    float4 *drec;            // 4 per interior edge: dbeta/dx_a (xyz), factor (w)
+    float *dfb;              // per interior edge: factor * beta / 2
     // assembled system
     float4 *A0;          // [slot - diag_slot][stride]: diagonal and upper blocks
     float2 *A1;
+    float4 *Aw;          // skew part w of those blocks (block p = S p + w x p), or null
     float4 *M0; // block-Jacobi inverse, symmetric: (00 01 02 11)
     float2 *M1; // (12 22)
     float4 *b;

@@ -26,6 +26,7 @@ __global__ void k_cond(const BatchCtl *ctl, cudaGraphConditionalHandle h);
 //   spmv  (descs, tiles, ctl, use_cond, handle)
 //   update(descs, tiles, ctl, use_cond, handle, iters_left)
 extern const GraphLoopVariant kSpmvVariants[];
+extern const GraphLoopVariant kSpmvSkewVariants[]; // same variants, skew block parts applied
 extern const GraphLoopVariant kUpdateVariants[];
 extern const int kNumSpmvVariants;
 extern const int kNumUpdateVariants;
@@ -44,6 +45,10 @@ __global__ void k_pcg_persistent_sm(InstDesc *const *descs, const TeamBlock *wor
                                     int halo_cap, int rows_cap);
 __global__ void k_pcg_persistent_gm(InstDesc *const *descs, const TeamBlock *work,
                                     int halo_cap, int rows_cap);
+__global__ void k_pcg_persistent_sm_skew(InstDesc *const *descs, const TeamBlock *work,
+                                         int halo_cap, int rows_cap);
+__global__ void k_pcg_persistent_gm_skew(InstDesc *const *descs, const TeamBlock *work,
+                                         int halo_cap, int rows_cap);
 __global__ void k_pcg1_persistent(InstDesc *const *descs, const TeamBlock *work, int halo_cap,
                                   int rows_cap);
 
@@ -89,6 +94,9 @@ struct ScratchLayout
 {
     size_t hrec = 0, frec = 0, A0 = 0, A1 = 0, M0 = 0, M1 = 0, b = 0;
     size_t r = 0, z = 0, p0 = 0, p1 = 0, q = 0, w1 = 0, part = 0;
+    // dihedral bending only (kAbsent otherwise)
+    static constexpr size_t kAbsent = ~size_t(0);
+    size_t drec = kAbsent, dfb = kAbsent, Aw = kAbsent;
     size_t bytes = 0;
 };
 
@@ -109,6 +117,7 @@ struct cloth_ctx_s
     int num_sms = 0;
     int occ_tri = 1, occ_row = 1;
     std::vector<int> occ_spmv, occ_update; // resident blocks per SM of each variant
+    std::vector<int> occ_spmv_skew;         // the same for kSpmvSkewVariants
     bool autotune = true;                  // tune graph-loop batches on their first step
     int tune_spmv = cloth::kDefaultSpmvVariant, tune_update = cloth::kDefaultUpdateVariant;
     std::vector<float> tune_ms_spmv, tune_ms_update; // the last tuning's timings

@@ -73,6 +73,13 @@ __device__ __forceinline__ float3 symv(const float *s, float3 v)
                        fmaf(s[4], v.z, fmaf(s[3], v.y, s[1] * v.x)),
                        fmaf(s[5], v.z, fmaf(s[4], v.y, s[2] * v.x)));
 }
+// w x p: the skew part of a block of the dihedral-bending model (an upper
+// block is S p + w x p, its transposed lower block S p - w x p)
+__device__ __forceinline__ float3 skewv(float4 w, float3 p)
+{
+    return make_float3(fmaf(w.y, p.z, -(w.z * p.y)), fmaf(w.z, p.x, -(w.x * p.z)),
+                       fmaf(w.x, p.y, -(w.y * p.x)));
+}
 __device__ __forceinline__ void load_sym(const float4 *a0, const float2 *a1,
                                          size_t o, float *s)
 {
@@ -344,6 +351,82 @@ __device__ __forceinline__ void stretch_component(
     }
 }
 
+// ---- dihedral bending (cDihedralMaterial, DihedralBending.cpp:120-270, 382-450)
+struct D3
+{
+    double x, y, z;
+};
+__device__ __forceinline__ D3 d3sub(D3 a, D3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+__device__ __forceinline__ D3 d3add(D3 a, D3 b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+__device__ __forceinline__ D3 d3scale(D3 a, double s) { return {a.x * s, a.y * s, a.z * s}; }
+__device__ __forceinline__ double d3dot(D3 a, D3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ D3 d3cross(D3 a, D3 b)
+{
+    return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+}
+__device__ __forceinline__ D3 d3load(const double *p) { return {p[0], p[1], p[2]}; }
+__device__ __forceinline__ float4 d3f4(D3 a, float w)
+{
+    return make_float4(float(a.x), float(a.y), float(a.z), w);
+}
+
+// One interior edge with stencil (v0 v1 v2 v3), in FP64 from the FP64
+// positions: n0 = (v1 - v0) x (v2 - v1), n1 = (v0 - v1) x (v3 - v0),
+// e = v1 - v0, beta = atan2(e^.(n0^ x n1^), n0^.n1^).  dbeta/dn0 and
+// dbeta/dn1 are the closed forms -(e x n0) / (|e| |n0|^2) and
+// (e x n1) / (|e| |n1|^2): the values the reference's
+// -sign(sin beta) / sqrt(1 - (n0^.n1^)^2) (I - n^ n^T) / |n| n'^ expressions
+// take, without their cancellation as beta -> 0.  The vertex gradients follow
+// the reference's chain rule (DihedralBending.cpp:225-268).  Writes the four
+// gradients with the factor c in .w, and c beta / 2 (force = (c beta / 2)
+// dbeta/dx, Hessian c dbeta/dx dbeta/dx^T, DihedralBending.cpp:420-427).
+__device__ __forceinline__ void dihedral_edge(const InstDesc &d, int q)
+{
+    const int4 s = d.dvid[q];
+    const D3 v0 = d3load(d.x64 + 3 * size_t(s.x)), v1 = d3load(d.x64 + 3 * size_t(s.y)),
+             v2 = d3load(d.x64 + 3 * size_t(s.z)), v3 = d3load(d.x64 + 3 * size_t(s.w));
+    const D3 e = d3sub(v1, v0);
+    const D3 n0 = d3cross(e, d3sub(v2, v1));
+    const D3 n1 = d3cross(d3sub(v0, v1), d3sub(v3, v0));
+    const double nn0 = d3dot(n0, n0), nn1 = d3dot(n1, n1), le = sqrt(d3dot(e, e));
+    const double i0 = 1.0 / sqrt(nn0), i1 = 1.0 / sqrt(nn1), ie = 1.0 / le;
+    const D3 n0h = d3scale(n0, i0), n1h = d3scale(n1, i1), eh = d3scale(e, ie);
+    const double beta = atan2(d3dot(eh, d3cross(n0h, n1h)), d3dot(n0h, n1h));
+    const D3 g0 = d3scale(d3cross(e, n0), -1.0 / (le * nn0));
+    const D3 g1 = d3scale(d3cross(e, n1), 1.0 / (le * nn1));
+    const D3 gv0 = d3add(d3cross(d3sub(v1, v2), g0), d3cross(d3sub(v3, v1), g1));
+    const D3 gv1 = d3add(d3cross(d3sub(v2, v0), g0), d3cross(d3sub(v0, v3), g1));
+    const D3 gv2 = d3cross(d3sub(v0, v1), g0);
+    const D3 gv3 = d3cross(d3sub(v1, v0), g1);
+    const double c = d.dfac[q];
+    const float cf = float(c);
+    float4 *rec = d.drec + 4 * size_t(q);
+    rec[0] = d3f4(gv0, cf);
+    rec[1] = d3f4(gv1, cf);
+    rec[2] = d3f4(gv2, cf);
+    rec[3] = d3f4(gv3, cf);
+    d.dfb[q] = float(c * beta / 2);
+}
+
+// Block (a, b) of one dihedral edge, c g_a g_b^T, added as its symmetric part
+// S and skew vector w (S p + w x p = c g_a (g_b . p)).  S is formed
+// symmetrically in a and b and w changes sign with them, bit for bit, so the
+// row-a and row-b copies of a block pair are exact transposes.
+__device__ __forceinline__ void dihedral_block(float4 ga, float4 gb, float *K, float *w)
+{
+    const float c = ga.w, h = 0.5f * c;
+    K[0] += c * (ga.x * gb.x);
+    K[1] += h * (ga.x * gb.y + ga.y * gb.x);
+    K[2] += h * (ga.x * gb.z + ga.z * gb.x);
+    K[3] += c * (ga.y * gb.y);
+    K[4] += h * (ga.y * gb.z + ga.z * gb.y);
+    K[5] += c * (ga.z * gb.z);
+    // c/2 (g_a g_b^T - g_b g_a^T) p = c/2 (g_b x g_a) x p
+    w[0] += h * (gb.y * ga.z - gb.z * ga.y);
+    w[1] += h * (gb.z * ga.x - gb.x * ga.z);
+    w[2] += h * (gb.x * ga.y - gb.y * ga.x);
+}
+
 } // namespace
 
 // ------------------------------------------------------------------ pins
@@ -385,7 +468,12 @@ __global__ void __launch_bounds__(kTile) k_tri(InstDesc *const *descs,
         const InstDesc &d = *descs[tl.inst];
         const int t = tl.start + threadIdx.x;
         if (t >= d.nt)
+        {
+            // the dihedral edges follow the triangles in the tile list
+            if (t - d.nt < d.n_dih)
+                dihedral_edge(d, t - d.nt);
             continue;
+        }
         const int4 tv = d.tri[t];
         const float S = __int_as_float(tv.w);
         const float4 c0 = d.tcoef[3 * t + 0], c1 = d.tcoef[3 * t + 1],
@@ -483,10 +571,29 @@ __global__ void __launch_bounds__(kTile) k_row(InstDesc *const *descs,
                 K[0] -= kbv;
                 K[3] -= kbv;
                 K[5] -= kbv;
+                // dihedral bending: K += c g_a g_b^T over the stencils holding
+                // (row, c) in edge order; f += (c beta / 2) g_a at the diagonal
+                float wv[3] = {0.f, 0.f, 0.f};
+                if (d.dsrc)
+                {
+                    const uint32_t de = d.dsrc[o];
+                    const uint32_t e0 = de >> 5, ne = de & 31u;
+                    for (uint32_t k = 0; k < ne; k++)
+                    {
+                        const uint32_t en = d.dent[e0 + k];
+                        const float4 *rec = d.drec + 4 * size_t(en >> 4);
+                        const float4 ga = rec[(en >> 2) & 3u], gb = rec[en & 3u];
+                        dihedral_block(ga, gb, K, wv);
+                        if (s == ds)
+                            f = f + d.dfb[en >> 4] * xyz(ga);
+                    }
+                }
                 float A[6];
 #pragma unroll
                 for (int k = 0; k < 6; k++)
                     A[k] = d.c_stiff * K[k];
+                float4 Aw = make_float4(d.c_stiff * wv[0], d.c_stiff * wv[1], d.c_stiff * wv[2],
+                                        0.f);
                 bool zero = false;
                 if (s == ds)
                 {
@@ -504,6 +611,7 @@ __global__ void __launch_bounds__(kTile) k_row(InstDesc *const *descs,
 #pragma unroll
                     for (int k = 0; k < 6; k++)
                         A[k] = 0.f;
+                    Aw = make_float4(0.f, 0.f, 0.f, 0.f);
                 }
                 if (s >= ds)
                 {
@@ -512,9 +620,16 @@ __global__ void __launch_bounds__(kTile) k_row(InstDesc *const *descs,
                     const size_t ou = size_t(s - ds) * d.stride + row;
                     d.A0[ou] = make_float4(A[0], A[1], A[2], A[3]);
                     d.A1[ou] = make_float2(A[4], A[5]);
+                    if (d.Aw)
+                        d.Aw[ou] = Aw;
                 }
                 if (d.warm_start && !zero && !fixv)
-                    acc = acc + symv(A, xyz(d.dx[c]));
+                {
+                    const float3 xd = xyz(d.dx[c]);
+                    acc = acc + symv(A, xd);
+                    if (d.Aw)
+                        acc = acc + skewv(Aw, xd);
+                }
             }
             // AssembleSystemRHSKernel (BaraffClothGpu.cu:301-344)
             const float3 g = make_float3(0.f, d.grav[row], 0.f);
@@ -725,6 +840,7 @@ struct SpmvHdr
     const uint32_t *lidx;
     const float4 *A0;
     const float2 *A1;
+    const float4 *Aw; // skew parts (dihedral bending), or null
     const float4 *z, *pold;
     float4 *pnew, *q;
     double *part;
@@ -750,6 +866,7 @@ __device__ __forceinline__ void load_hdr(SpmvHdr &h, const Tile &tl)
     h.colu = ldg_ptr(&dp->colu);
     h.A0 = ldg_ptr(reinterpret_cast<float4 *const *>(&dp->A0));
     h.A1 = ldg_ptr(reinterpret_cast<float2 *const *>(&dp->A1));
+    h.Aw = ldg_ptr(reinterpret_cast<float4 *const *>(&dp->Aw));
     h.z = ldg_ptr(reinterpret_cast<float4 *const *>(&dp->z));
     float4 *p0 = ldg_ptr(&dp->p0), *p1 = ldg_ptr(&dp->p1);
     h.pold = (it & 1) ? p1 : p0;
@@ -766,8 +883,9 @@ __device__ __forceinline__ void load_hdr(SpmvHdr &h, const Tile &tl)
 // plane k for k < wl and upper plane k - wl after (wl, the instance's lower
 // plane count, is uniform), so every load instruction of a warp reads one
 // plane; at each step the loads of all R rows and U steps are in flight
-// together.
-template <int R, int U, int T>
+// together.  SKEW: the instance may carry skew block parts (dihedral
+// bending); they are read and applied when its header has them.
+template <int R, int U, int T, bool SKEW>
 __device__ __forceinline__ void spmv_rows(const SpmvHdr &d, int row0, float (&pq)[R][1])
 {
     const float beta = d.beta;
@@ -801,6 +919,7 @@ __device__ __forceinline__ void spmv_rows(const SpmvHdr &d, int row0, float (&pq
         int cc[R][U];
         float4 a0[R][U];
         float2 a1[R][U];
+        float4 aw[R][U];
         bool on[R][U];
 #pragma unroll
         for (int k = 0; k < U; k++)
@@ -819,6 +938,8 @@ __device__ __forceinline__ void spmv_rows(const SpmvHdr &d, int row0, float (&pq
                     const size_t oa = lower ? size_t(d.lidx[o]) : o;
                     a0[r][k] = d.A0[oa];
                     a1[r][k] = d.A1[oa];
+                    if (SKEW && d.Aw)
+                        aw[r][k] = d.Aw[oa];
                 }
             }
         }
@@ -842,6 +963,11 @@ __device__ __forceinline__ void spmv_rows(const SpmvHdr &d, int row0, float (&pq
                             pc = pc + beta * xyz(d.pold[c]);
                     }
                     q[r] = q[r] + symv(A, pc);
+                    if (SKEW && d.Aw)
+                    {
+                        const float3 cw = skewv(aw[r][k], pc);
+                        q[r] = (k0 + k < wl) ? q[r] - cw : q[r] + cw;
+                    }
                 }
     }
 #pragma unroll
@@ -901,7 +1027,7 @@ __device__ __forceinline__ void load_hdr(UpdHdr &h, const Tile &tl)
 // Blocks take TPB consecutive tile-list entries at a time (grid-stride over
 // those groups); the instance header is reloaded only when the instance
 // changes, so its dependent loads are paid once per run of tiles.
-template <int R, int U, int TPB>
+template <int R, int U, int TPB, bool SKEW>
 __global__ void __launch_bounds__(kTile / R) k_spmv_t(InstDesc *const *descs,
                                                       const Tile *tiles, BatchCtl *ctl,
                                                       int use_cond,
@@ -930,7 +1056,7 @@ __global__ void __launch_bounds__(kTile / R) k_spmv_t(InstDesc *const *descs,
             if (!d.active)
                 continue;
             float part[R][1];
-            spmv_rows<R, U, T>(d, tl.start + threadIdx.x, part);
+            spmv_rows<R, U, T, SKEW>(d, tl.start + threadIdx.x, part);
             double tot[1];
             if (tile_reduce_r<R, 1>(d.part, d.nt, d.st, tl.start / kTile, part, tot, sh,
                                     &flag) &&
@@ -1072,14 +1198,17 @@ __global__ void __launch_bounds__(kTile / R) k_update_t(InstDesc *const *descs,
 }
 
 // Variant table of the graph-loop kernels (the autotuner's search space).
-extern const GraphLoopVariant kSpmvVariants[] = {
-    {1, 1, 1, (const void *)k_spmv_t<1, 1, 1>}, {1, 2, 1, (const void *)k_spmv_t<1, 2, 1>},
-    {1, 3, 1, (const void *)k_spmv_t<1, 3, 1>}, {2, 1, 1, (const void *)k_spmv_t<2, 1, 1>},
-    {2, 2, 1, (const void *)k_spmv_t<2, 2, 1>}, {4, 1, 1, (const void *)k_spmv_t<4, 1, 1>},
-    {1, 1, 4, (const void *)k_spmv_t<1, 1, 4>}, {1, 2, 4, (const void *)k_spmv_t<1, 2, 4>},
-    {2, 1, 4, (const void *)k_spmv_t<2, 1, 4>}, {2, 2, 4, (const void *)k_spmv_t<2, 2, 4>},
-    {4, 1, 4, (const void *)k_spmv_t<4, 1, 4>}, {2, 1, 8, (const void *)k_spmv_t<2, 1, 8>},
-};
+#define SPMV_VARIANTS(SK)                                                                     \
+    {1, 1, 1, (const void *)k_spmv_t<1, 1, 1, SK>}, {1, 2, 1, (const void *)k_spmv_t<1, 2, 1, SK>}, \
+    {1, 3, 1, (const void *)k_spmv_t<1, 3, 1, SK>}, {2, 1, 1, (const void *)k_spmv_t<2, 1, 1, SK>}, \
+    {2, 2, 1, (const void *)k_spmv_t<2, 2, 1, SK>}, {4, 1, 1, (const void *)k_spmv_t<4, 1, 1, SK>}, \
+    {1, 1, 4, (const void *)k_spmv_t<1, 1, 4, SK>}, {1, 2, 4, (const void *)k_spmv_t<1, 2, 4, SK>}, \
+    {2, 1, 4, (const void *)k_spmv_t<2, 1, 4, SK>}, {2, 2, 4, (const void *)k_spmv_t<2, 2, 4, SK>}, \
+    {4, 1, 4, (const void *)k_spmv_t<4, 1, 4, SK>}, {2, 1, 8, (const void *)k_spmv_t<2, 1, 8, SK>}
+extern const GraphLoopVariant kSpmvVariants[] = {SPMV_VARIANTS(false)};
+// the same variants for launch sets holding a dihedral-bending instance
+extern const GraphLoopVariant kSpmvSkewVariants[] = {SPMV_VARIANTS(true)};
+#undef SPMV_VARIANTS
 extern const GraphLoopVariant kUpdateVariants[] = {
     {1, 0, 1, (const void *)k_update_t<1, 1>}, {2, 0, 1, (const void *)k_update_t<2, 1>},
     {4, 0, 1, (const void *)k_update_t<4, 1>}, {1, 0, 4, (const void *)k_update_t<1, 4>},
@@ -1089,6 +1218,7 @@ extern const GraphLoopVariant kUpdateVariants[] = {
 extern const int kNumSpmvVariants = 12;
 extern const int kNumUpdateVariants = 7;
 static_assert(sizeof(kSpmvVariants) / sizeof(kSpmvVariants[0]) == 12, "variant count");
+static_assert(sizeof(kSpmvSkewVariants) / sizeof(kSpmvSkewVariants[0]) == 12, "variant count");
 static_assert(sizeof(kUpdateVariants) / sizeof(kUpdateVariants[0]) == 7, "variant count");
 
 // Copies of the PCG state the autotuner disturbs (dx, r, z per row, the
@@ -1345,7 +1475,9 @@ template <int NQ> struct WarpFx
 
 // State of the block's own rows lives in shared memory (SM = true) or in
 // global memory (SM = false, for row ranges too long for shared memory).
-template <bool SM>
+// SKEW: the launch set holds a dihedral-bending instance; skew block parts
+// are read and applied where an instance has them.
+template <bool SM, bool SKEW>
 __device__ __forceinline__ void pcg_persistent_body(InstDesc *const *descs,
                                                     const TeamBlock *work, int halo_cap,
                                                     int rows_cap)
@@ -1533,6 +1665,7 @@ __device__ __forceinline__ void pcg_persistent_body(InstDesc *const *descs,
                     int cc[kSlotUnroll];
                     float4 a0[kSlotUnroll];
                     float2 a1[kSlotUnroll];
+                    float4 aw[kSlotUnroll];
                     bool on[kSlotUnroll];
 #pragma unroll
                     for (int k = 0; k < kSlotUnroll; k++)
@@ -1551,6 +1684,8 @@ __device__ __forceinline__ void pcg_persistent_body(InstDesc *const *descs,
                                       : o;
                             a0[k] = ld_keep(d.A0 + oa, keep);
                             a1[k] = ld_keep(d.A1 + oa, keep);
+                            if (SKEW && d.Aw)
+                                aw[k] = ld_keep(d.Aw + oa, keep);
                         }
                     }
 #pragma unroll
@@ -1578,6 +1713,11 @@ __device__ __forceinline__ void pcg_persistent_body(InstDesc *const *descs,
                                 }
                             }
                             q = q + symv(A, pc);
+                            if (SKEW && d.Aw)
+                            {
+                                const float3 cw = skewv(aw[k], pc);
+                                q = (k0 + k < wl) ? q - cw : q + cw;
+                            }
                         }
                 }
                 if (SM)
@@ -1734,14 +1874,29 @@ __global__ void __launch_bounds__(kPBlock, 1)
     k_pcg_persistent_sm(InstDesc *const *descs, const TeamBlock *work, int halo_cap,
                         int rows_cap)
 {
-    pcg_persistent_body<true>(descs, work, halo_cap, rows_cap);
+    pcg_persistent_body<true, false>(descs, work, halo_cap, rows_cap);
 }
 
 __global__ void __launch_bounds__(kPBlock, 1)
     k_pcg_persistent_gm(InstDesc *const *descs, const TeamBlock *work, int halo_cap,
                         int rows_cap)
 {
-    pcg_persistent_body<false>(descs, work, halo_cap, rows_cap);
+    pcg_persistent_body<false, false>(descs, work, halo_cap, rows_cap);
+}
+
+// launch sets holding a dihedral-bending instance
+__global__ void __launch_bounds__(kPBlock, 1)
+    k_pcg_persistent_sm_skew(InstDesc *const *descs, const TeamBlock *work, int halo_cap,
+                             int rows_cap)
+{
+    pcg_persistent_body<true, true>(descs, work, halo_cap, rows_cap);
+}
+
+__global__ void __launch_bounds__(kPBlock, 1)
+    k_pcg_persistent_gm_skew(InstDesc *const *descs, const TeamBlock *work, int halo_cap,
+                             int rows_cap)
+{
+    pcg_persistent_body<false, true>(descs, work, halo_cap, rows_cap);
 }
 
 // ------------------------------------------------------------------ single-barrier persistent PCG

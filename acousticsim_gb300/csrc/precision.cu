@@ -161,6 +161,17 @@ __device__ __forceinline__ void row_mul64(const InstDesc &d, int row, const doub
         y[0] += a[0] * x0 + a[1] * x1 + a[2] * x2;
         y[1] += a[1] * x0 + a[3] * x1 + a[4] * x2;
         y[2] += a[2] * x0 + a[4] * x1 + a[5] * x2;
+        if (d.Aw)
+        {
+            // skew part (dihedral bending): + w x v on stored blocks, - on
+            // the transposed ones
+            const float4 wf = d.Aw[oa];
+            const double sg = lower ? -1.0 : 1.0;
+            const double wx = sg * wf.x, wy = sg * wf.y, wz = sg * wf.z;
+            y[0] += wy * x2 - wz * x1;
+            y[1] += wz * x0 - wx * x2;
+            y[2] += wx * x1 - wy * x0;
+        }
     }
 }
 

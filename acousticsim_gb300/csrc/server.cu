@@ -318,9 +318,17 @@ int build_chunk_graph(cloth_server_s *s)
     const int n = int(s->cl.size());
     const int one_wave_tri = ctx->num_sms * std::max(1, ctx->occ_tri);
     const int one_wave_row = ctx->num_sms * std::max(1, ctx->occ_row);
-    const GraphLoopVariant &sv = kSpmvVariants[ctx->tune_spmv];
+    // SpMV variants that apply skew block parts when a dihedral-bending cloth
+    // is registered
+    bool skew = false;
+    for (const SrvCloth &sc : s->cl)
+        skew = skew || sc.c->h.Aw != nullptr || sc.c->mat.bending_model == 1;
+    const GraphLoopVariant &sv =
+        (skew ? kSpmvSkewVariants : kSpmvVariants)[ctx->tune_spmv];
     const GraphLoopVariant &uv = kUpdateVariants[ctx->tune_update];
-    const int one_wave_spmv = ctx->num_sms * std::max(1, ctx->occ_spmv[ctx->tune_spmv]);
+    const int one_wave_spmv =
+        ctx->num_sms *
+        std::max(1, (skew ? ctx->occ_spmv_skew : ctx->occ_spmv)[ctx->tune_spmv]);
     const int one_wave_upd = ctx->num_sms * std::max(1, ctx->occ_update[ctx->tune_update]);
     cudaGraph_t g = nullptr;
     SCK(cudaGraphCreate(&g, 0));
@@ -705,7 +713,7 @@ int cloth_server_add(cloth_server *s, cloth_t *c, double dt, const cloth_solve_p
     if (c->server)
         return sfail(CLOTH_ERR_STATE, "cloth_server_add: the cloth is held by a server");
     const int n = int(s->cl.size()) + 1;
-    const int ntr = (c->tab.nv + kTile - 1) / kTile, ntt = (c->tab.nt + kTile - 1) / kTile;
+    const int ntr = (c->tab.nv + kTile - 1) / kTile, ntt = (c->tab.nt + c->tab.n_dih + kTile - 1) / kTile;
     size_t max_scratch = c->sl.bytes;
     for (auto &cr : s->cl)
         max_scratch = std::max(max_scratch, cr.scratch);

@@ -268,7 +268,111 @@ void rebuild_bending(const Mesh &m, const Material &mat, Tables &t)
     }
     t.kbend.resize(acc.size());
     for (size_t k = 0; k < acc.size(); k++)
-        t.kbend[k] = float(acc[k]);
+        t.kbend[k] = mat.bending_model == 1 ? 0.f : float(acc[k]);
+}
+
+void rebuild_dihedral_factor(const Mesh &m, const Material &mat, Tables &t)
+{
+    // The CPU cloth hands the bending material (K, K, K) with K its first
+    // bending stiffness (BaraffCloth.cpp:38-43); the edge stiffness is their
+    // mean (BaseBendingMaterial.cpp:47).
+    const double K = double(mat.bending_k[0]);
+    const double kedge = ((K + K) + K) / 3.0;
+    // cDihedralMaterial::Init (DihedralBending.cpp:23-91): float rest edge
+    // lengths, float Heron areas from them (triangle edges (v0 v1), (v1 v2),
+    // (v2 v0), BuildTriangleEdgeId, Triangulator.cpp:11-31), float heights
+    // 2 A / e of the two triangles, and -K e / max(1e-7, h0 + h1) in double.
+    std::vector<float> len(m.ne);
+    std::map<std::pair<int, int>, int> eid;
+    for (int e = 0; e < m.ne; e++)
+    {
+        const int *ed = &m.edges[size_t(e) * 4];
+        const double *a = &m.pos[size_t(ed[0]) * 3], *b = &m.pos[size_t(ed[1]) * 3];
+        const double dx = a[0] - b[0], dy = a[1] - b[1], dz = a[2] - b[2];
+        len[e] = float(std::sqrt(dx * dx + dy * dy + dz * dz));
+        eid[std::make_pair(std::min(ed[0], ed[1]), std::max(ed[0], ed[1]))] = e;
+    }
+    auto edge_len = [&](int a, int b) {
+        return double(len[eid.at(std::make_pair(std::min(a, b), std::max(a, b)))]);
+    };
+    std::vector<float> area(m.nt);
+    for (int tt = 0; tt < m.nt; tt++)
+    {
+        const int *v = &m.tris[size_t(tt) * 3];
+        const double a = edge_len(v[0], v[1]), b = edge_len(v[1], v[2]),
+                     c = edge_len(v[2], v[0]);
+        const double p = (a + b + c) / 2;
+        area[tt] = float(std::sqrt(p * (p - a) * (p - b) * (p - c)));
+    }
+    t.dih_factor.assign(t.n_dih, 0.0);
+    for (int q = 0; q < t.n_dih; q++)
+    {
+        const int e = t.dih_edge[q];
+        const int *ed = &m.edges[size_t(e) * 4];
+        const float L = len[e];
+        const float h0 = (2.f * area[ed[2]]) / L, h1 = (2.f * area[ed[3]]) / L;
+        const float hs = std::max(1e-7f, h0 + h1);
+        t.dih_factor[q] = -kedge * double(L) / double(hs);
+    }
+}
+
+bool build_dihedral(const Mesh &m, const Material &mat, Tables &t, std::string &err)
+{
+    t.dih_edge.clear();
+    for (int e = 0; e < m.ne; e++)
+        if (t.stencil[size_t(e) * 4] >= 0)
+            t.dih_edge.push_back(e);
+    t.n_dih = int(t.dih_edge.size());
+    if (size_t(t.n_dih) * 16 >= (size_t(1) << 27))
+    {
+        err = "mesh: too many interior edges for dihedral bending in one cloth";
+        return false;
+    }
+    rebuild_dihedral_factor(m, mat, t);
+    // Entry (q, a, b) adds edge q's block (a, b) to row stencil[a], slot of
+    // stencil[b]; every pair of one stencil is in the ELL pattern.
+    const size_t nnzb = t.cols.size();
+    auto slot_of = [&](int row, int col) {
+        const int *b = &t.cols[t.rowptr[row]];
+        const int *en = &t.cols[t.rowptr[row + 1]];
+        return int(std::lower_bound(b, en, col) - b);
+    };
+    t.dih_count.assign(nnzb, 0);
+    std::vector<int> where(size_t(t.n_dih) * 16);
+    for (int q = 0; q < t.n_dih; q++)
+    {
+        const int *s = &t.stencil[size_t(t.dih_edge[q]) * 4];
+        for (int a = 0; a < 4; a++)
+            for (int b = 0; b < 4; b++)
+            {
+                const size_t k = size_t(t.rowptr[s[a]]) + slot_of(s[a], s[b]);
+                where[size_t(q) * 16 + a * 4 + b] = int(k);
+                t.dih_count[k]++;
+            }
+    }
+    t.dih_start.assign(nnzb, 0);
+    int run = 0;
+    for (size_t k = 0; k < nnzb; k++)
+    {
+        if (t.dih_count[k] > 31)
+        {
+            err = "mesh: more than 31 bending stencils meet in one block";
+            return false;
+        }
+        t.dih_start[k] = run;
+        run += t.dih_count[k];
+    }
+    // filled in edge order, so each block's entries are sorted by q
+    t.dih_ent.assign(size_t(run), 0u);
+    std::vector<int> fill(nnzb, 0);
+    for (int q = 0; q < t.n_dih; q++)
+        for (int ab = 0; ab < 16; ab++)
+        {
+            const int k = where[size_t(q) * 16 + ab];
+            t.dih_ent[size_t(t.dih_start[k]) + fill[k]++] =
+                (uint32_t(q) << 4) | uint32_t(ab >> 2) << 2 | uint32_t(ab & 3);
+        }
+    return true;
 }
 
 bool build_tables(const Mesh &m, const Material &mat, Tables &t,
@@ -504,6 +608,13 @@ bool build_tables(const Mesh &m, const Material &mat, Tables &t,
                 t.h_dest[size_t(tt) * 9 + a * 3 + b] = t.h_start[k] + h_fill[k]++;
             }
         }
+    }
+    if (mat.bending_model == 1)
+        return build_dihedral(m, mat, t, err);
+    if (mat.bending_model != 0)
+    {
+        err = "material: unknown bending model";
+        return false;
     }
     return true;
 }

@@ -35,6 +35,7 @@ struct Material
     double default_timestep;
     double gravity;
     int fix_fv_norm;
+    int bending_model = 0; // 0: quadratic (the GPU cloth's), 1: dihedral (the CPU cloth's)
 };
 
 // Everything derived from the mesh on the host.
@@ -59,6 +60,15 @@ struct Tables
     std::vector<int> h_count;       // nnzb
     std::vector<int> f_dest;        // nt*3  force record of local vertex a
     std::vector<int> f_rowptr;      // nv+1
+    // dihedral bending (bending_model 1): interior edges in edge order
+    int n_dih = 0;
+    std::vector<int> dih_edge;       // n_dih  edge id
+    std::vector<double> dih_factor;  // n_dih  -K e / max(1e-7, h0 + h1), rest state
+    // (row, slot) entries: q << 4 | a << 2 | b for stencil vertices a (the
+    // row) and b (the column) of interior edge q, sorted by (row, slot, q)
+    std::vector<uint32_t> dih_ent;
+    std::vector<int> dih_start;      // nnzb  first entry of each block
+    std::vector<int> dih_count;      // nnzb
 };
 
 // cTriangulator::BuildGeometry_UniformTriangle + BuildRectVertices +
@@ -78,6 +88,14 @@ bool build_tables(const Mesh &m, const Material &mat, Tables &t,
 
 // Only the material-dependent part (edge_k, kbend) for cloth_set_material.
 void rebuild_bending(const Mesh &m, const Material &mat, Tables &t);
+
+// cDihedralMaterial::Init (src/sim/cloth/DihedralBending.cpp:23-91) and the
+// (row, slot) entry lists of its per-edge Hessians; called by build_tables
+// when mat.bending_model is 1.
+bool build_dihedral(const Mesh &m, const Material &mat, Tables &t, std::string &err);
+
+// The stiffness-dependent part of it (dih_factor).
+void rebuild_dihedral_factor(const Mesh &m, const Material &mat, Tables &t);
 
 // FindVerticesIdFromUV (src/sim/cloth/BaseCloth.cpp:151-189).
 void find_vertices_from_uv(const Mesh &m, const float *uv, int n, int *out);

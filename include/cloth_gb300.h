@@ -23,7 +23,7 @@
 extern "C" {
 #endif
 
-#define CLOTH_ABI_VERSION 1
+#define CLOTH_ABI_VERSION 2
 #define CLOTH_ELL_REF_WIDTH 32 /* tCudaVector32i, src/sim/cloth/BaraffClothGpu.h:19 */
 
 enum cloth_status {
@@ -75,7 +75,18 @@ typedef struct {
     double gravity;           /* -9.8 (BaraffClothGpu.cpp:561) */
     int fix_fv_norm;          /* 0: reference Hessian, whose weft term uses |Fu|
                                  (BaraffClothGpu.cu:55); 1: use |Fv| */
+    int bending_model;        /* "cloth_bending_model": CLOTH_BENDING_QUADRATIC (the
+                                 GPU cloth's constant Q-bending) or CLOTH_BENDING_DIHEDRAL */
 } cloth_material;
+
+/* Bending models.  QUADRATIC: cBaraffClothGpu's constant Q-bending matrix
+ * (BaraffClothGpu.cpp:573-680).  DIHEDRAL: the CPU cloth's nonlinear
+ * dihedral-angle bending, cDihedralMaterial (src/sim/cloth/DihedralBending.cpp:
+ * 23-91, 382-488): per interior edge, force (c beta / 2) dbeta/dx and the
+ * Gauss-Newton stiffness c dbeta/dx dbeta/dx^T with c = -K e / (h0 + h1), both
+ * rebuilt from the current positions every step; stiffness K = bending_k[0]. */
+#define CLOTH_BENDING_QUADRATIC 0
+#define CLOTH_BENDING_DIHEDRAL 1
 
 /* PCG controls (PCGSolver::Solve, src/sim/cloth/gpu_solvers/PCGSolver.cu:332-481).
  * The reference runs at most 100 iterations and stops when the absolute
@@ -253,6 +264,14 @@ int cloth_export_system(cloth_t *cloth, int *ell, float *A, float *b,
 /* Per-triangle results of the last assembly: fint nt*9 (force on local vertex
  * a at [3a+k]) and hess nt*81 (block (a,b) at [9*(3a+b)], row-major). */
 int cloth_export_triangles(cloth_t *cloth, float *fint, float *hess);
+/* Per-interior-edge results of the last assembly of a dihedral-bending cloth
+ * (cDihedralMaterial::Update, src/sim/cloth/DihedralBending.cpp:382-450):
+ * n_edges, edge_ids (n_edges: edge index of each interior edge), grad
+ * (n_edges*12: dbeta/dx of stencil vertices v0 v1 v2 v3) and coef (n_edges*2:
+ * the factor c = -K e / (h0 + h1) and c beta / 2).  Zero edges for the
+ * quadratic model.  Any output pointer may be NULL. */
+int cloth_export_dihedral(cloth_t *cloth, int *n_edges, int *edge_ids, float *grad,
+                          float *coef);
 /* Init-time tables: stencil ne*4 (mEdgeAffectVertexId, -1 on the boundary),
  * coef nt*12 (Fu/Fv warp-weft, Fu/Fv diagonal), area nt, mass nv,
  * tri_slot nt*9 (ELL slot of vertex b in row of vertex a). */

@@ -393,12 +393,176 @@ void orc_triangles(int nt, const int *tris, const float *coef, const float *area
     }
 }
 
+/* ------------------------------------------------------------------ dihedral */
+static double len_f(const double *a, const double *b)
+{
+    const double dx = a[0] - b[0], dy = a[1] - b[1], dz = a[2] - b[2];
+    return (double)(float)sqrt((dx * dx + dy * dy) + dz * dz);
+}
+
+int orc_dihedral_rest(int nv, int nt, int ne, const double *pos, const int *tris,
+                      const int *edges, float bending_k0, double *factor)
+{
+    (void)nv;
+    /* cDihedralMaterial::Init (DihedralBending.cpp:23-91) with the edge
+     * stiffness mean(K, K, K) (BaseBendingMaterial.cpp:47, BaraffCloth.cpp:38-43):
+     * float edge lengths, float Heron areas over the triangle's edges
+     * (v0 v1), (v1 v2), (v2 v0) (BuildTriangleEdgeId, Triangulator.cpp:11-31),
+     * float heights 2 A / e, factor -K e / max(1e-7, h0 + h1) in double. */
+    const double K = (double)bending_k0;
+    const double kedge = ((K + K) + K) / 3.0;
+    float *area = (float *)malloc(sizeof(float) * (size_t)(nt > 0 ? nt : 1));
+    for (int t = 0; t < nt; t++)
+    {
+        const int *v = tris + 3 * (size_t)t;
+        const double a = len_f(pos + 3 * (size_t)v[0], pos + 3 * (size_t)v[1]);
+        const double b = len_f(pos + 3 * (size_t)v[1], pos + 3 * (size_t)v[2]);
+        const double c = len_f(pos + 3 * (size_t)v[2], pos + 3 * (size_t)v[0]);
+        const double p = (a + b + c) / 2;
+        area[t] = (float)sqrt(p * (p - a) * (p - b) * (p - c));
+    }
+    for (int e = 0; e < ne; e++)
+    {
+        const int *ed = edges + 4 * (size_t)e;
+        factor[e] = 0.0;
+        if (ed[3] < 0)
+            continue;
+        const float L = (float)len_f(pos + 3 * (size_t)ed[0], pos + 3 * (size_t)ed[1]);
+        const float h0 = (2.f * area[ed[2]]) / L, h1 = (2.f * area[ed[3]]) / L;
+        const float hs = (h0 + h1) > 1e-7f ? (h0 + h1) : 1e-7f;
+        factor[e] = -kedge * (double)L / (double)hs;
+    }
+    free(area);
+    return 0;
+}
+
+static void cross3(const double *a, const double *b, double *o)
+{
+    o[0] = a[1] * b[2] - a[2] * b[1];
+    o[1] = a[2] * b[0] - a[0] * b[2];
+    o[2] = a[0] * b[1] - a[1] * b[0];
+}
+static double dot3(const double *a, const double *b)
+{
+    return a[0] * b[0] + a[1] * b[1] + a[2] * b[2];
+}
+
+void orc_dihedral(int nv, int ne, const int *stencil, const double *factor,
+                  const double *x, const int *ell, double *fint, double *K,
+                  double *beta_out, double *grad_out)
+{
+    (void)nv;
+    /* cDihedralMaterial::Update + AssignForceAndMatrix (DihedralBending.cpp:
+     * 120-270, 382-488) and cBaseBendingMaterial::GetStiffnessMatrix
+     * (BaseBendingMaterial.cpp:13-16): per interior edge with stencil
+     * (v0 v1 v2 v3), n0 = (v1 - v0) x (v2 - v1), n1 = (v0 - v1) x (v3 - v0),
+     * e = v1 - v0, beta = atan2(e^.(n0^ x n1^), n0^.n1^).  dbeta/dn0 and
+     * dbeta/dn1 are taken in closed form, -(e x n0) / (|e| |n0|^2) and
+     * (e x n1) / (|e| |n1|^2): the values of the reference's
+     * -sign(sin beta) (I - n^ n^T) n'^ / (|n| sqrt(1 - (n0^.n1^)^2))
+     * (DihedralBending.cpp:160-222), without its loss of precision as
+     * beta -> 0.  Vertex gradients by the reference's chain rule (:225-268).
+     * force += ((c beta) g) / 2; stiffness block (a, b) += float((c g_a) g_b^T)
+     * (the Hessian is kept as float, DihedralBending.cpp:431), summed in
+     * double. */
+    for (int e = 0; e < ne; e++)
+    {
+        const int *s = stencil + 4 * (size_t)e;
+        if (s[0] < 0)
+        {
+            if (beta_out)
+                beta_out[e] = 0.0;
+            if (grad_out)
+                memset(grad_out + 12 * (size_t)e, 0, 12 * sizeof(double));
+            continue;
+        }
+        const double *v0 = x + 3 * (size_t)s[0], *v1 = x + 3 * (size_t)s[1],
+                     *v2 = x + 3 * (size_t)s[2], *v3 = x + 3 * (size_t)s[3];
+        double ev[3], a21[3], a01[3], a30[3], n0[3], n1[3];
+        for (int k = 0; k < 3; k++)
+        {
+            ev[k] = v1[k] - v0[k];
+            a21[k] = v2[k] - v1[k];
+            a01[k] = v0[k] - v1[k];
+            a30[k] = v3[k] - v0[k];
+        }
+        cross3(ev, a21, n0);
+        cross3(a01, a30, n1);
+        const double nn0 = dot3(n0, n0), nn1 = dot3(n1, n1), le = sqrt(dot3(ev, ev));
+        double n0h[3], n1h[3], eh[3], cx[3];
+        for (int k = 0; k < 3; k++)
+        {
+            n0h[k] = n0[k] / sqrt(nn0);
+            n1h[k] = n1[k] / sqrt(nn1);
+            eh[k] = ev[k] / le;
+        }
+        cross3(n0h, n1h, cx);
+        const double beta = atan2(dot3(eh, cx), dot3(n0h, n1h));
+        double g0[3], g1[3], t0[3], t1[3];
+        cross3(ev, n0, t0);
+        cross3(ev, n1, t1);
+        for (int k = 0; k < 3; k++)
+        {
+            g0[k] = -t0[k] / (le * nn0);
+            g1[k] = t1[k] / (le * nn1);
+        }
+        double g[12], d12[3], d31[3], d20[3], d03[3], u[3], w[3];
+        for (int k = 0; k < 3; k++)
+        {
+            d12[k] = v1[k] - v2[k];
+            d31[k] = v3[k] - v1[k];
+            d20[k] = v2[k] - v0[k];
+            d03[k] = v0[k] - v3[k];
+        }
+        cross3(d12, g0, u);
+        cross3(d31, g1, w);
+        for (int k = 0; k < 3; k++)
+            g[k] = u[k] + w[k];
+        cross3(d20, g0, u);
+        cross3(d03, g1, w);
+        for (int k = 0; k < 3; k++)
+            g[3 + k] = u[k] + w[k];
+        cross3(a01, g0, g + 6);
+        cross3(ev, g1, g + 9);
+        const double c = factor[e];
+        if (beta_out)
+            beta_out[e] = beta;
+        if (grad_out)
+            memcpy(grad_out + 12 * (size_t)e, g, sizeof(g));
+        for (int a = 0; a < 4; a++)
+        {
+            for (int k = 0; k < 3; k++)
+                fint[3 * (size_t)s[a] + k] += ((c * beta) * g[3 * a + k]) / 2;
+            const int *row = ell + (size_t)s[a] * W;
+            for (int b = 0; b < 4; b++)
+            {
+                const int slot = row_find(row, s[b]);
+                double *blk = K + ((size_t)s[a] * W + slot) * 9;
+                for (int r = 0; r < 3; r++)
+                    for (int q = 0; q < 3; q++)
+                        blk[3 * r + q] += (double)(float)((c * g[3 * a + r]) * g[3 * b + q]);
+            }
+        }
+    }
+}
+
 /* ------------------------------------------------------------------ system */
 void orc_system(int nv, int nt, const int *tris, const int *ell,
                 const double *tri_f, const double *tri_h, const double *kbend,
                 const double *mass, double gravity, const double *x,
                 const double *xpre, const unsigned char *fixed, double dt,
                 float ray_a, float ray_b, double *A, double *b, double *fint)
+{
+    orc_system_ex(nv, nt, tris, ell, tri_f, tri_h, kbend, NULL, NULL, mass, gravity, x, xpre,
+                  fixed, dt, ray_a, ray_b, A, b, fint);
+}
+
+void orc_system_ex(int nv, int nt, const int *tris, const int *ell,
+                   const double *tri_f, const double *tri_h, const double *kbend,
+                   const double *bend_K, const double *bend_f, const double *mass,
+                   double gravity, const double *x, const double *xpre,
+                   const unsigned char *fixed, double dt, float ray_a, float ray_b,
+                   double *A, double *b, double *fint)
 {
     /* K = stretch - K_b;  A = (1 + dt a) M + (dt b - dt^2) K
      * (BaraffClothGpu.cu:240-281, 445-483); b = dt^2 (g + f) + M (x - x_pre)
@@ -427,14 +591,22 @@ void orc_system(int nv, int nt, const int *tris, const int *ell,
             const int c = ell[(size_t)v * W + s];
             if (c < 0)
                 break;
-            const double kb = kbend[(size_t)v * W + s];
+            const double kb = kbend ? kbend[(size_t)v * W + s] : 0.0;
             double *blk = K + ((size_t)v * W + s) * 9;
             for (int k = 0; k < 3; k++)
             {
                 blk[4 * k] -= kb;
                 fint[3 * v + k] -= kb * x[3 * c + k];
             }
+            /* dihedral bending (CPU cloth, BaraffCloth.cpp:205-244): K += its
+             * stiffness, f += its force */
+            if (bend_K)
+                for (int k = 0; k < 9; k++)
+                    blk[k] += bend_K[((size_t)v * W + s) * 9 + k];
         }
+    if (bend_f)
+        for (size_t k = 0; k < (size_t)nv * 3; k++)
+            fint[k] += bend_f[k];
     const double cs = dt * (double)ray_b - dt * dt;
     const double cm = 1 + dt * (double)ray_a;
     for (int v = 0; v < nv; v++)

@@ -54,6 +54,26 @@ void orc_system(int nv, int nt, const int *tris, const int *ell,
                 const double *xpre, const unsigned char *fixed, double dt,
                 float ray_a, float ray_b, double *A, double *b, double *fint);
 
+/* The same with a second bending model added: bend_K nv*32*9 (added to K)
+ * and bend_f nv*3 (added to the internal force); kbend may be NULL. */
+void orc_system_ex(int nv, int nt, const int *tris, const int *ell,
+                   const double *tri_f, const double *tri_h, const double *kbend,
+                   const double *bend_K, const double *bend_f, const double *mass,
+                   double gravity, const double *x, const double *xpre,
+                   const unsigned char *fixed, double dt, float ray_a, float ray_b,
+                   double *A, double *b, double *fint);
+
+/* Dihedral bending of the CPU cloth (cDihedralMaterial, DihedralBending.cpp).
+ * Rest factors per edge (0 on the boundary): -K e / max(1e-7, h0 + h1) from
+ * float rest lengths and Heron areas, K = bending_k0. */
+int orc_dihedral_rest(int nv, int nt, int ne, const double *pos, const int *tris,
+                      const int *edges, float bending_k0, double *factor);
+/* Force and stiffness at positions x: fint nv*3 and K nv*32*9 are ADDED TO;
+ * beta_out (ne) and grad_out (ne*12, dbeta/dx of v0..v3) may be NULL. */
+void orc_dihedral(int nv, int ne, const int *stencil, const double *factor,
+                  const double *x, const int *ell, double *fint, double *K,
+                  double *beta_out, double *grad_out);
+
 /* y = A x over ELL blocks. */
 void orc_spmv(int nv, const int *ell, const double *A, const double *x, double *y);
 

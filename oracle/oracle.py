@@ -35,6 +35,13 @@ def lib() -> C.CDLL:
         L.orc_system.argtypes = [C.c_int, C.c_int, PI, PI, PD, PD, PD, PD, C.c_double, PD, PD,
                                  PU8, C.c_double, C.c_float, C.c_float, PD, PD, PD]
         L.orc_system.restype = None
+        L.orc_system_ex.argtypes = [C.c_int, C.c_int, PI, PI, PD, PD, PD, PD, PD, PD,
+                                    C.c_double, PD, PD, PU8, C.c_double, C.c_float,
+                                    C.c_float, PD, PD, PD]
+        L.orc_system_ex.restype = None
+        L.orc_dihedral_rest.argtypes = [C.c_int, C.c_int, C.c_int, PD, PI, PI, C.c_float, PD]
+        L.orc_dihedral.argtypes = [C.c_int, C.c_int, PI, PD, PD, PI, PD, PD, PD, PD]
+        L.orc_dihedral.restype = None
         L.orc_spmv.argtypes = [C.c_int, PI, PD, PD, PD]
         L.orc_spmv.restype = None
         L.orc_pcg.argtypes = [C.c_int, PI, PD, PD, PU8, PD, C.c_int, C.c_double, PD, C.c_int]
@@ -104,7 +111,9 @@ def triangles(mesh: dict, tab: dict, x: np.ndarray, stretch_k, fix_fv_norm=0):
 
 
 def system(mesh: dict, tab: dict, tri_f, tri_h, x, xpre, fixed, dt, ray_a, ray_b,
-           gravity=-9.8):
+           gravity=-9.8, bend=None):
+    """Assembled system.  bend=None: the GPU cloth's quadratic bending
+    (tab["kbend"]); bend=(K, f) from dihedral(): that model instead."""
     L = lib()
     tris = np.ascontiguousarray(mesh["tris"], np.int32)
     nv, nt = tab["ell"].shape[0], tris.shape[0]
@@ -114,13 +123,46 @@ def system(mesh: dict, tab: dict, tri_f, tri_h, x, xpre, fixed, dt, ray_a, ray_b
     A = np.zeros((nv, W, 3, 3))
     b = np.zeros((nv, 3))
     f = np.zeros((nv, 3))
-    L.orc_system(nv, nt, _p(tris, C.c_int), _p(tab["ell"], C.c_int),
-                 _p(np.ascontiguousarray(tri_f), C.c_double),
-                 _p(np.ascontiguousarray(tri_h), C.c_double), _p(tab["kbend"], C.c_double),
-                 _p(tab["mass"], C.c_double), float(gravity), _p(x, C.c_double),
-                 _p(xpre, C.c_double), _p(fixed, C.c_ubyte), float(dt), float(ray_a),
-                 float(ray_b), _p(A, C.c_double), _p(b, C.c_double), _p(f, C.c_double))
+    kb, bK, bf = _p(tab["kbend"], C.c_double), None, None
+    if bend is not None:
+        Kd = np.ascontiguousarray(bend[0], np.float64)
+        fd = np.ascontiguousarray(bend[1], np.float64)
+        kb, bK, bf = None, _p(Kd, C.c_double), _p(fd, C.c_double)
+    L.orc_system_ex(nv, nt, _p(tris, C.c_int), _p(tab["ell"], C.c_int),
+                    _p(np.ascontiguousarray(tri_f), C.c_double),
+                    _p(np.ascontiguousarray(tri_h), C.c_double), kb, bK, bf,
+                    _p(tab["mass"], C.c_double), float(gravity), _p(x, C.c_double),
+                    _p(xpre, C.c_double), _p(fixed, C.c_ubyte), float(dt), float(ray_a),
+                    float(ray_b), _p(A, C.c_double), _p(b, C.c_double), _p(f, C.c_double))
     return A, b, f
+
+
+def dihedral_rest(mesh: dict, bending_k0: float) -> np.ndarray:
+    """Per-edge rest factor -K e / (h0 + h1) of the dihedral model (0 on the boundary)."""
+    pos = np.ascontiguousarray(mesh["pos"], np.float64)
+    tris = np.ascontiguousarray(mesh["tris"], np.int32)
+    edges = np.ascontiguousarray(mesh["edges"], np.int32)
+    fac = np.zeros(edges.shape[0])
+    lib().orc_dihedral_rest(pos.shape[0], tris.shape[0], edges.shape[0], _p(pos, C.c_double),
+                            _p(tris, C.c_int), _p(edges, C.c_int), float(bending_k0),
+                            _p(fac, C.c_double))
+    return fac
+
+
+def dihedral(tab: dict, factor: np.ndarray, x: np.ndarray) -> dict:
+    """Dihedral force (nv,3), stiffness (nv,32,3,3), beta (ne) and dbeta/dx (ne,4,3)."""
+    nv = tab["ell"].shape[0]
+    ne = tab["stencil"].shape[0]
+    x = np.ascontiguousarray(x, np.float64).reshape(-1)
+    f = np.zeros((nv, 3))
+    K = np.zeros((nv, W, 3, 3))
+    beta = np.zeros(ne)
+    grad = np.zeros((ne, 4, 3))
+    fac = np.ascontiguousarray(factor, np.float64)
+    lib().orc_dihedral(nv, ne, _p(tab["stencil"], C.c_int), _p(fac, C.c_double),
+                       _p(x, C.c_double), _p(tab["ell"], C.c_int), _p(f, C.c_double),
+                       _p(K, C.c_double), _p(beta, C.c_double), _p(grad, C.c_double))
+    return {"f": f, "K": K, "beta": beta, "grad": grad}
 
 
 def spmv(ell, A, x):
@@ -149,12 +191,16 @@ def max_threads() -> int:
 
 
 class OracleCloth:
-    """FP64 CPU step of the GPU path (Q-bending, block-Jacobi PCG, pins)."""
+    """FP64 CPU step of the GPU path (Q-bending, or the CPU cloth's dihedral
+    bending with "cloth_bending_model": "dihedral"; block-Jacobi PCG, pins)."""
 
     def __init__(self, mesh: dict, conf: dict, pins):
         self.mesh = mesh
         self.conf = conf
         self.tab = tables(mesh, conf["cloth_density"], conf["cloth_bending_stiffness"][:2])
+        self.dihedral = conf.get("cloth_bending_model", "quadratic") == "dihedral"
+        self.dfac = (dihedral_rest(mesh, conf["cloth_bending_stiffness"][0])
+                     if self.dihedral else None)
         nv = mesh["pos"].shape[0]
         self.fixed = np.zeros(nv, np.uint8)
         self.fixed[np.asarray(pins, np.int64)] = 1
@@ -176,8 +222,13 @@ class OracleCloth:
         self.snap_pins()
         tf, th = triangles(self.mesh, self.tab, self.x, c["cloth_stretch_stiffness"][:3],
                            c.get("fix_fv_norm", 0))
+        bend = None
+        if self.dihedral:
+            dh = dihedral(self.tab, self.dfac, self.x)
+            bend = (dh["K"], dh["f"])
         A, b, f = system(self.mesh, self.tab, tf, th, self.x, self.xpre, self.fixed, dt,
-                         c.get("rayleigh_damping_a", 0.0), c.get("rayleigh_damping_b", 0.0))
+                         c.get("rayleigh_damping_a", 0.0), c.get("rayleigh_damping_b", 0.0),
+                         bend=bend)
         return A, b, f, tf, th
 
     def step(self, dt=None, rel_tol=1e-10, max_iters=100000, threads=1):

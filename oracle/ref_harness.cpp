@@ -15,6 +15,7 @@
 #include "geometries/Primitives.h"
 #include "sim/cloth/BaraffCloth.h"
 #include "sim/cloth/BaraffMaterial.h"
+#include "sim/cloth/DihedralBending.h"
 #include "sim/cloth/QBendingMaterial.h"
 #include "utils/JsonUtil.h"
 #include "utils/RotUtil.h"
@@ -275,6 +276,11 @@ struct Probe : public cBaraffCloth
                            .segment(0, 2);
         qb->Init(mVertexArray, mEdgeArray, mTriangleArray,
                  kb[0] * tVector3d::Ones());
+        // the CPU cloth's dihedral bending, initialised on the rest state as
+        // cBaraffCloth::Init does (BaraffCloth.cpp:36-43: K = (k0, k0, k0) in float)
+        auto dih = std::make_shared<cDihedralMaterial>();
+        dih->Init(mVertexArray, mEdgeArray, mTriangleArray,
+                  (tVector3f::Ones() * float(kb[0])).cast<double>());
         tVector3d ks = cJsonUtil::ReadVectorJson(
                            cJsonUtil::ParseAsValue("cloth_stretch_stiffness",
                                                    conf))
@@ -346,85 +352,134 @@ struct Probe : public cBaraffCloth
         double ra = cJsonUtil::ParseAsDouble("rayleigh_damping_a", conf);
         double rb = cJsonUtil::ParseAsDouble("rayleigh_damping_b", conf);
         std::vector<int> ellmap = ell();
-        std::vector<double> A(size_t(n) * kEll * 9, 0.0),
-            Kst(size_t(n) * kEll * 9, 0.0), Kbd(size_t(n) * kEll, 0.0),
-            Kbg(size_t(n) * kEll, 0.0);
-        tSparseMatd Kd = K; // row-major: coeff lookups
-        for (int i = 0; i < n; i++)
-            for (int s = 0; s < kEll; s++)
-            {
-                int j = ellmap[size_t(i) * kEll + s];
-                if (j < 0)
-                    break;
-                for (int r = 0; r < 3; r++)
-                    for (int c = 0; c < 3; c++)
-                    {
-                        double kv = Kd.coeff(3 * i + r, 3 * j + c);
-                        double a = (dt * rb - dt * dt) * kv;
-                        if (i == j && r == c)
-                            a += (1 + dt * ra) * mass[i];
-                        A[(size_t(i) * kEll + s) * 9 + r * 3 + c] = a;
-                        Kst[(size_t(i) * kEll + s) * 9 + r * 3 + c] =
-                            K_st.coeff(3 * i + r, 3 * j + c);
-                    }
-                Kbd[size_t(i) * kEll + s] = -K_qb.coeff(3 * i, 3 * j);
-                Kbg[size_t(i) * kEll + s] = Kb_gpu.coeff(3 * i, 3 * j);
-            }
-        std::vector<double> b(size_t(n) * 3);
-        for (int i = 0; i < n; i++)
-            for (int k = 0; k < 3; k++)
-            {
-                double g = (k == 1) ? -9.8 * mass[i] : 0.0;
-                b[3 * i + k] = dt * dt * (g + f_st[3 * i + k] + f_bd[3 * i + k]) +
-                               mass[i] * (x[3 * i + k] - xpre[3 * i + k]);
-            }
-
-        // Solve the pin-projected system (free rows and columns) exactly.
-        std::vector<int> dof_of(3 * n, -1);
+        // A by the GPU formula from a stiffness matrix (ELL blocks)
+        auto build_A = [&](const tSparseMatd &Kt, std::vector<double> &Aout) {
+            Aout.assign(size_t(n) * kEll * 9, 0.0);
+            for (int i = 0; i < n; i++)
+                for (int s = 0; s < kEll; s++)
+                {
+                    int j = ellmap[size_t(i) * kEll + s];
+                    if (j < 0)
+                        break;
+                    for (int r = 0; r < 3; r++)
+                        for (int c = 0; c < 3; c++)
+                        {
+                            double kv = Kt.coeff(3 * i + r, 3 * j + c);
+                            double a = (dt * rb - dt * dt) * kv;
+                            if (i == j && r == c)
+                                a += (1 + dt * ra) * mass[i];
+                            Aout[(size_t(i) * kEll + s) * 9 + r * 3 + c] = a;
+                        }
+                }
+        };
+        // b from the stretch force and a bending force
+        auto build_b = [&](const tVectorXd &fb, std::vector<double> &bout) {
+            bout.assign(size_t(n) * 3, 0.0);
+            for (int i = 0; i < n; i++)
+                for (int k = 0; k < 3; k++)
+                {
+                    double g = (k == 1) ? -9.8 * mass[i] : 0.0;
+                    bout[3 * i + k] = dt * dt * (g + f_st[3 * i + k] + fb[3 * i + k]) +
+                                      mass[i] * (x[3 * i + k] - xpre[3 * i + k]);
+                }
+        };
+        // the pin-projected system (free rows and columns) solved exactly
         std::vector<char> fixed(n, 0);
         for (int vid : mConstraint_StaticPointIds)
             fixed[vid] = 1;
-        int nf = 0;
+        auto solve = [&](const std::vector<double> &Am, const std::vector<double> &bm) {
+            std::vector<int> dof_of(3 * n, -1);
+            int nf = 0;
+            for (int i = 0; i < n; i++)
+                if (!fixed[i])
+                    for (int k = 0; k < 3; k++)
+                        dof_of[3 * i + k] = nf++;
+            std::vector<Eigen::Triplet<double>> trip;
+            for (int i = 0; i < n; i++)
+            {
+                if (fixed[i])
+                    continue;
+                for (int s = 0; s < kEll; s++)
+                {
+                    int j = ellmap[size_t(i) * kEll + s];
+                    if (j < 0)
+                        break;
+                    if (fixed[j])
+                        continue;
+                    for (int r = 0; r < 3; r++)
+                        for (int c = 0; c < 3; c++)
+                            trip.emplace_back(dof_of[3 * i + r], dof_of[3 * j + c],
+                                              Am[(size_t(i) * kEll + s) * 9 + r * 3 + c]);
+                }
+            }
+            Eigen::SparseMatrix<double> Af(nf, nf);
+            Af.setFromTriplets(trip.begin(), trip.end());
+            tVectorXd bf(nf);
+            for (int i = 0; i < 3 * n; i++)
+                if (dof_of[i] >= 0)
+                    bf[dof_of[i]] = bm[i];
+            Eigen::SimplicialLDLT<Eigen::SparseMatrix<double>> ldlt(Af);
+            if (ldlt.info() != Eigen::Success)
+            {
+                std::cerr << "LDLT factorisation failed\n";
+                exit(4);
+            }
+            tVectorXd dxf = ldlt.solve(bf);
+            std::vector<double> out(size_t(n) * 3, 0.0);
+            for (int i = 0; i < 3 * n; i++)
+                if (dof_of[i] >= 0)
+                    out[i] = dxf[dof_of[i]];
+            return out;
+        };
+
+        std::vector<double> A, b;
+        build_A(K, A);
+        build_b(f_bd, b);
+        std::vector<double> dx = solve(A, b);
+        std::vector<double> Kst(size_t(n) * kEll * 9, 0.0), Kbd(size_t(n) * kEll, 0.0),
+            Kbg(size_t(n) * kEll, 0.0);
         for (int i = 0; i < n; i++)
-            if (!fixed[i])
-                for (int k = 0; k < 3; k++)
-                    dof_of[3 * i + k] = nf++;
-        std::vector<Eigen::Triplet<double>> trip;
-        for (int i = 0; i < n; i++)
-        {
-            if (fixed[i])
-                continue;
             for (int s = 0; s < kEll; s++)
             {
                 int j = ellmap[size_t(i) * kEll + s];
                 if (j < 0)
                     break;
-                if (fixed[j])
-                    continue;
                 for (int r = 0; r < 3; r++)
                     for (int c = 0; c < 3; c++)
-                        trip.emplace_back(
-                            dof_of[3 * i + r], dof_of[3 * j + c],
-                            A[(size_t(i) * kEll + s) * 9 + r * 3 + c]);
+                        Kst[(size_t(i) * kEll + s) * 9 + r * 3 + c] =
+                            K_st.coeff(3 * i + r, 3 * j + c);
+                Kbd[size_t(i) * kEll + s] = -K_qb.coeff(3 * i, 3 * j);
+                Kbg[size_t(i) * kEll + s] = Kb_gpu.coeff(3 * i, 3 * j);
             }
-        }
-        Eigen::SparseMatrix<double> Af(nf, nf);
-        Af.setFromTriplets(trip.begin(), trip.end());
-        tVectorXd bf(nf);
-        for (int i = 0; i < 3 * n; i++)
-            if (dof_of[i] >= 0)
-                bf[dof_of[i]] = b[i];
-        Eigen::SimplicialLDLT<Eigen::SparseMatrix<double>> ldlt(Af);
-        if (ldlt.info() != Eigen::Success)
-        {
-            std::cerr << "LDLT factorisation failed\n";
-            exit(4);
-        }
-        tVectorXd dxf = ldlt.solve(bf);
-        std::vector<double> dx(size_t(n) * 3, 0.0);
-        for (int i = 0; i < 3 * n; i++)
-            if (dof_of[i] >= 0)
-                dx[i] = dxf[dof_of[i]];
+
+        // The CPU cloth's bending model (cDihedralMaterial, BaraffCloth.cpp:
+        // 36-45, 101, 205-244) on the same state: its force and stiffness
+        // replace the quadratic bending in the same GPU-path system.
+        dih->Update();
+        tVectorXd f_dih = dih->CalcForce(X);
+        tSparseMatd K_dih = dih->GetStiffnessMatrix();
+        tSparseMatd Kd_tot = K_st + K_dih;
+        std::vector<double> Adih, bdih, Kdih(size_t(n) * kEll * 9, 0.0);
+        build_A(Kd_tot, Adih);
+        build_b(f_dih, bdih);
+        std::vector<double> dxdih = solve(Adih, bdih);
+        for (int i = 0; i < n; i++)
+            for (int s = 0; s < kEll; s++)
+            {
+                int j = ellmap[size_t(i) * kEll + s];
+                if (j < 0)
+                    break;
+                for (int r = 0; r < 3; r++)
+                    for (int c = 0; c < 3; c++)
+                        Kdih[(size_t(i) * kEll + s) * 9 + r * 3 + c] =
+                            K_dih.coeff(3 * i + r, 3 * j + c);
+            }
+        std::vector<double> fdih(f_dih.data(), f_dih.data() + 3 * n);
+        d.put("dih_f", "f8", fdih, {n, 3});
+        d.put("dih_K", "f8", Kdih, {n, kEll, 3, 3});
+        d.put("dih_A", "f8", Adih, {n, kEll, 3, 3});
+        d.put("dih_b", "f8", bdih, {n, 3});
+        d.put("dih_dx", "f8", dxdih, {n, 3});
 
         std::vector<double> fst(f_st.data(), f_st.data() + 3 * n),
             fbd(f_bd.data(), f_bd.data() + 3 * n), xs(x), xps(xpre);

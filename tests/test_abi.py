@@ -43,7 +43,7 @@ def test_bindings_cover_every_declared_symbol(built):
 def test_abi_version_and_errors(built):
     from acousticsim_gb300 import _native
     lib = _native.load()
-    assert lib.cloth_abi_version() == 1
+    assert lib.cloth_abi_version() == 2
     assert lib.cloth_status_string(0) == b"ok"
     # NULL arguments are rejected with a status, not a crash
     assert lib.cloth_step(None, 0.0, None, None) == 1

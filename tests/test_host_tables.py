@@ -139,3 +139,26 @@ def test_rejects_bad_meshes(N):
            "tris": np.array([[0, 1 + k, 1 + (k + 1) % n] for k in range(n)], np.int32)}
     with pytest.raises(ClothError):
         host_tables(N, fan, mat, with_edges=False)
+
+
+def test_dihedral_model_tables(N):
+    """The dihedral model (the CPU cloth's bending) replaces the quadratic one:
+    no quadratic bending scalars, the same ELL pattern; unknown models are refused."""
+    import ctypes as C
+    g, conf = load_golden("grid20")
+    mesh = _grid(conf)
+    mat = _material(N, conf)
+    q = host_tables(N, mesh, mat)
+    mat.bending_model = 1
+    d = host_tables(N, mesh, mat)
+    assert np.array_equal(d["ell"], q["ell"])
+    assert np.any(q["kbend"] != 0) and np.all(d["kbend"] == 0)
+    mat.bending_model = 7
+    pos = np.ascontiguousarray(mesh["pos"], np.float64)
+    uv = np.ascontiguousarray(mesh["uv"], np.float32)
+    tris = np.ascontiguousarray(mesh["tris"], np.int32)
+    md = N.MeshDesc(pos.shape[0], tris.shape[0], 0, N.ptr(pos, C.c_double),
+                    N.ptr(uv, C.c_float), N.ptr(tris, C.c_int), None)
+    rc = N.load().cloth_host_tables(C.byref(md), C.byref(mat), None, None, None, None, None,
+                                    None, None, None, None)
+    assert rc != 0

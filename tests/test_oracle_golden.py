@@ -104,3 +104,78 @@ def test_oracle_rejects_wide_rows(orc):
     mesh = {"pos": pos, "uv": uv, "tris": tris, "edges": np.array(edges, np.int32)}
     with pytest.raises(ValueError):
         orc.tables(mesh, 0.1, [1e-3, 1e-3])
+
+
+# ---------------------------------------------------------------- dihedral bending
+# The CPU cloth's bending model (cDihedralMaterial): the golden arrays are the
+# reference's own force and stiffness on the fixture states, and the GPU-path
+# system and direct solve with that model in place of the quadratic one.
+
+def _dihedral_conf(conf):
+    return dict(conf, cloth_bending_model="dihedral")
+
+
+@pytest.mark.parametrize("case", GOLDEN_CASES)
+def test_dihedral_force_and_stiffness(orc, case):
+    g, conf = load_golden(case)
+    m = _mesh(orc, conf)
+    t = orc.tables(m, conf["cloth_density"], conf["cloth_bending_stiffness"])
+    fac = orc.dihedral_rest(m, conf["cloth_bending_stiffness"][0])
+    assert np.all(fac[m["edges"][:, 3] < 0] == 0.0)
+    assert np.all(fac[m["edges"][:, 3] >= 0] < 0.0)
+    oc = orc.OracleCloth(m, conf, g["topo_pins"])
+    oc.x = g["x_in"].reshape(-1).copy()
+    oc.snap_pins()
+    dh = orc.dihedral(t, fac, oc.x)
+    # the closed-form gradient equals the reference's expression away from
+    # beta = 0 (the fixtures' angles are 1e-3..1 rad)
+    assert rel(dh["f"], g["sys_dih_f"]) < 1e-9
+    # the stiffness is float-rounded per edge in both
+    assert rel(dh["K"], g["sys_dih_K"]) < 2e-7
+
+
+@pytest.mark.parametrize("case", GOLDEN_CASES)
+def test_dihedral_system_and_solve(orc, case):
+    g, conf = load_golden(case)
+    m = _mesh(orc, conf)
+    oc = orc.OracleCloth(m, _dihedral_conf(conf), g["topo_pins"])
+    oc.x = g["x_in"].reshape(-1).copy()
+    oc.xpre = g["xpre_in"].reshape(-1).copy()
+    A, b, _, _, _ = oc.system()
+    GA, Gb = project_pins(g["sys_dih_A"], g["sys_dih_b"], g["topo_ell"], g["topo_pins"])
+    assert rel(A, GA) < 1e-7
+    assert rel(b, Gb) < 1e-9
+    dx, it, res = orc.pcg(oc.tab["ell"], A, b, oc.fixed, rel_tol=1e-13)
+    assert rel(dx, g["sys_dih_dx"].reshape(-1)) < 1e-6
+
+
+def test_dihedral_gradient_is_the_derivative_of_beta(orc):
+    """dbeta/dx of the oracle against central differences of beta, over
+    random stencils, flat and folded ones included."""
+    rng = np.random.default_rng(7)
+    for trial in range(20):
+        P = rng.normal(size=(4, 3))
+        if trial < 5:
+            P[:, 2] = 0.0  # flat: beta = 0 or pi
+        mesh = {"pos": P, "tris": np.array([[0, 1, 2], [1, 0, 3]], np.int32),
+                "edges": np.array([[0, 1, 0, 1]], np.int32)}
+        tab = {"ell": np.full((4, 32), -1, np.int32), "stencil": np.array([[0, 1, 2, 3]],
+                                                                          np.int32)}
+        tab["ell"][:, :4] = np.arange(4)
+        fac = np.array([-1.0])
+
+        def beta(x):
+            return orc.dihedral(tab, fac, x)["beta"][0]
+
+        d = orc.dihedral(tab, fac, P)
+        h = 1e-6
+        num = np.zeros(12)
+        x0 = P.reshape(-1)
+        for k in range(12):
+            xp, xm = x0.copy(), x0.copy()
+            xp[k] += h
+            xm[k] -= h
+            db = beta(xp) - beta(xm)
+            db = (db + np.pi) % (2 * np.pi) - np.pi  # across the +-pi cut
+            num[k] = db / (2 * h)
+        assert np.allclose(d["grad"].reshape(-1), num, rtol=1e-5, atol=1e-6 * np.abs(num).max())
