@@ -39,20 +39,23 @@ MAX_ITERS = 20000
 L2_FLUSH_BYTES = 512 << 20
 
 
-def workload_conf(n=N_SIDE, dt=DT) -> dict:
+def workload_conf(n=N_SIDE, dt=DT, bending="quadratic") -> dict:
+    """bending: "quadratic" (the GPU cloth's constant Q-bending) or "dihedral"
+    (the CPU cloth's nonlinear dihedral-angle bending)."""
     return {"geometry_type": "regular_triangle", "cloth_size": [1.0, 1.0],
             "subdivision": [n - 1, n - 1], "cloth_init_pos": [0.0, 0.0, 0.0],
             "cloth_uv_rotation": 0, "cloth_stretch_stiffness": [1e3, 1e3, 1e2],
             "cloth_bending_stiffness": [1e-3, 1e-3], "cloth_density": 0.1,
             "rayleigh_damping_a": 0.01, "rayleigh_damping_b": 0.0,
-            "default_timestep": dt,
+            "default_timestep": dt, "cloth_bending_model": bending,
             "constraints": {"static_point": [[-0.5, 0.5], [0.5, 0.5]]}}
 
 
-def initial_state(pos: np.ndarray, seed: int, dt=DT):
+def initial_state(pos: np.ndarray, seed: int, dt=DT, sx=1e-3):
+    """x = rest + N(0, sx), v = N(0, 0.01), x_pre = x - dt v."""
     rng = np.random.default_rng(seed)
     p = pos.reshape(-1, 3)
-    x = p + rng.normal(0.0, 1e-3, p.shape)
+    x = p + rng.normal(0.0, sx, p.shape)
     v = rng.normal(0.0, 1e-2, p.shape)
     return x.reshape(-1).copy(), (x - dt * v).reshape(-1).copy()
 
@@ -178,7 +181,7 @@ def ncu_traffic(kernel: str, iterations: float) -> float | None:
     return float(v) * iterations if v is not None else None
 
 
-def algorithmic_bytes(nv: int, nnzb: int) -> dict:
+def algorithmic_bytes(nv: int, nnzb: int, skew: bool = False) -> dict:
     """Unique bytes one PCG iteration must move. The matrix is stored as its
     diagonal and upper blocks (FP32, 6 floats per symmetric block); a lower
     slot holds its column and the index of the transposed block:
@@ -187,13 +190,15 @@ def algorithmic_bytes(nv: int, nnzb: int) -> dict:
                      + 16*nv (p write) + 16*nv (q write)
       update phase : 16*nv (q) + 16*nv (dx) + 16*nv (r) + 24*nv (M^-1 read)
                      + 48*nv (dx, r, z write)   [p comes from shared memory]
-    with nnzb_up = (nnzb + nv) / 2 and nnzb_lo = (nnzb - nv) / 2.
+    with nnzb_up = (nnzb + nv) / 2 and nnzb_lo = (nnzb - nv) / 2.  With the
+    dihedral bending model every stored block also has a skew part (16 bytes).
     """
     up, lo = (nnzb + nv) // 2, (nnzb - nv) // 2
-    spmv = 24 * up + 4 * nnzb + 4 * lo + 68 * nv
+    matrix = (40 if skew else 24) * up + 4 * nnzb + 4 * lo
+    spmv = matrix + 68 * nv
     update = 120 * nv
     return {"spmv_dot": spmv, "update_dot": update, "iteration": spmv + update,
-            "matrix": 24 * up + 4 * nnzb + 4 * lo}
+            "matrix": matrix}
 
 
 def single_barrier_bytes(nv: int, nnzb: int) -> int:
@@ -231,15 +236,16 @@ def count_nnzb(n_side: int) -> int:
 
 
 # ---------------------------------------------------------------- CPU baseline
-def cpu_port_step_time(threads: int, sample_steps: int = 1, n_side: int = N_SIDE) -> dict:
+def cpu_port_step_time(threads: int, sample_steps: int = 1, n_side: int = N_SIDE,
+                       bending: str = "quadratic", sx: float = 1e-3) -> dict:
     """Times the FP64 CPU restatement of the same step (oracle port)."""
     from acousticsim_gb300 import build_grid
     from oracle import oracle as orc
-    conf = workload_conf(n_side)
+    conf = workload_conf(n_side, bending=bending)
     mesh = build_grid((1.0, 1.0), (n_side - 1, n_side - 1))
     pins = [n_side - 1, n_side * n_side - 1]
     oc = orc.OracleCloth(mesh, conf, pins)
-    x, xp = initial_state(mesh["pos"], 1234)
+    x, xp = initial_state(mesh["pos"], 1234, sx=sx)
     oc.x, oc.xpre = x, xp
     t0 = time.perf_counter()
     iters = []
@@ -261,15 +267,17 @@ def run_reference(args, rank, world, pg):
     # one full 512x512 step of the port takes tens of seconds, so the timed
     # sample is min(K, 2) full steps after a small-grid warm-up
     for _ in range(args.warmup):
-        cpu_port_step_time(threads, 1, 64)
+        cpu_port_step_time(threads, 1, 64, args.bending, args.noise)
     n = max(1, min(args.steps, 2))
-    r = cpu_port_step_time(threads, n)
+    r = cpu_port_step_time(threads, n, bending=args.bending, sx=args.noise)
     value = r["steps"] / r["seconds"]
     line = {"metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": args.gpus,
             "steps": n, "warmup": args.warmup,
             "ms_per_step": 1e3 * r["seconds"] / r["steps"], "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "impl": "reference", "config": config_block({"pcg_iters": r["pcg_iters"]}),
+            "impl": "reference", "config": config_block({"pcg_iters": r["pcg_iters"],
+                                                         "bending": args.bending,
+                                                         "x_noise": args.noise}),
             "cpu_baseline": {"value": value, "unit": "steps/s", "cores": threads, "kind": "port",
                              "sample": f"{r['steps']} full {N_SIDE}x{N_SIDE} steps, FP64 oracle "
                                        f"port (oracle/cloth_oracle.c), {threads} OpenMP threads"},
@@ -289,9 +297,9 @@ def run_ours(args, rank, world, local, pg):
     if args.solver:
         ctx.set_solver(args.solver)
     stream = torch.cuda.ExternalStream(ctx.stream_ptr(), device=torch.device("cuda", local))
-    conf = workload_conf()
+    conf = workload_conf(bending=args.bending)
     cloth = BaraffClothGpu(ctx, conf)
-    x0, xp0 = initial_state(cloth.GetInitPos(), 1234 + rank)
+    x0, xp0 = initial_state(cloth.GetInitPos(), 1234 + rank, sx=args.noise)
     cloth.SetPos(x0)
     cloth.SetPrePos(xp0)
     p = params(max_iters=MAX_ITERS, rel_tol=REL_TOL)
@@ -362,7 +370,7 @@ def run_ours(args, rank, world, local, pg):
     prof = ctx.profile()
     ctx.set_profiling(False)
     nnzb = count_nnzb(N_SIDE)
-    alg = algorithmic_bytes(nv, nnzb)
+    alg = algorithmic_bytes(nv, nnzb, skew=args.bending == "dihedral")
     peak = measured_peaks()
     total_ms = sum(v["ms"] for v in prof.values())
     shares = {k: round(v["ms"] / total_ms, 4) if total_ms else None for k, v in prof.items()}
@@ -379,6 +387,9 @@ def run_ours(args, rank, world, local, pg):
         kname = ("k_pcg1_persistent (single-barrier PCG, all iterations of the step in one "
                  "cooperative launch)" if solver == "persistent_1b" else
                  "k_pcg_persistent_sm (all PCG iterations of the step in one cooperative launch)")
+        if args.bending == "dihedral":
+            kname = ("k_pcg_persistent_sm_skew (all PCG iterations of the step in one "
+                     "cooperative launch; blocks with skew parts)")
     else:
         launch_ms = sp["ms"] / max(1, sp["launches"])
         bytes_launch = alg["spmv_dot"]
@@ -387,8 +398,7 @@ def run_ours(args, rank, world, local, pg):
     roof = {"bound": "hbm", "kernel": kname,
             "achieved": achieved, "peak": peak["hbm_gbs"], "unit": "GB/s",
             "frac": achieved / peak["hbm_gbs"], "peak_source": f"{peak['source']} hbm_gbs",
-            "traffic": ncu_traffic("k_pcg1_persistent" if solver == "persistent_1b"
-                                   else "k_pcg_persistent_sm", float(np.mean(prof_iters)))
+            "traffic": ncu_traffic(kname.split()[0], float(np.mean(prof_iters)))
             if solver.startswith("persistent") else None,
             "traffic_source": "profiles/ncu_traffic.json (ncu capture, 20 iterations of this workload, scaled by iterations)",
             "algorithmic_bytes_per_launch": bytes_launch,
@@ -402,7 +412,7 @@ def run_ours(args, rank, world, local, pg):
     if rank == 0:
         from oracle import oracle as orc
         threads = orc.max_threads()
-        r = cpu_port_step_time(threads, 1)
+        r = cpu_port_step_time(threads, 1, bending=args.bending, sx=args.noise)
         cpu = {"value": r["steps"] / r["seconds"], "unit": "steps/s", "cores": threads,
                "kind": "port",
                "sample": f"1 full {N_SIDE}x{N_SIDE} step (FP64 oracle port, {r['pcg_iters'][0]} "
@@ -415,6 +425,7 @@ def run_ours(args, rank, world, local, pg):
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32 (FP64 PCG reductions)",
                 "data": "synthetic (seeded perturbation of the flat 512x512 cloth)",
                 "config": config_block({"parallelism": f"replicas x{world}",
+                                        "bending": args.bending, "x_noise": args.noise,
                                         "pcg_iters_per_step": iters,
                                         "step_ms": [round(v, 3) for v in step_ms],
                                         "wall_s_timed_region": wall}),
@@ -899,8 +910,8 @@ def run_profile_case(args):
     ctx = ClothContext(0)
     if args.solver:
         ctx.set_solver(args.solver)
-    cloth = BaraffClothGpu(ctx, workload_conf(args.profile_side))
-    x0, xp0 = initial_state(cloth.GetInitPos(), 1234)
+    cloth = BaraffClothGpu(ctx, workload_conf(args.profile_side, bending=args.bending))
+    x0, xp0 = initial_state(cloth.GetInitPos(), 1234, sx=args.noise)
     cloth.SetPos(x0)
     cloth.SetPrePos(xp0)
     if args.solver == "graph_loop":
@@ -912,7 +923,7 @@ def run_profile_case(args):
     out = {"profile_case": st, "phases": ph, "grid": args.profile_side,
            "kernel_variant": ctx.kernel_variant()}
     mi = cloth.matrix_info()
-    ab = algorithmic_bytes(cloth.nv, mi["nnzb"])
+    ab = algorithmic_bytes(cloth.nv, mi["nnzb"], skew=args.bending == "dihedral")
     if st["solver"] == "graph_loop":
         peak = measured_peaks()["hbm_gbs"]
         for name, nbytes in (("spmv_dot", ab["matrix"] + 68 * cloth.nv),
@@ -939,6 +950,13 @@ def main():
                                          "graph_loop"], default=None)
     ap.add_argument("--profile-side", type=int, default=N_SIDE,
                     help="grid side of the single-cloth ncu case")
+    ap.add_argument("--bending", choices=["quadratic", "dihedral"], default="quadratic",
+                    help="bending model of the single-cloth step: the GPU cloth's quadratic "
+                         "one (the headline) or the CPU cloth's dihedral one")
+    ap.add_argument("--noise", type=float, default=1e-3,
+                    help="std of the seeded position perturbation of the single-cloth step "
+                         "(1e-3: the benchmark's; the dihedral model at 512x512 needs a "
+                         "milder one for FP32 PCG, e.g. 2e-4)")
     ap.add_argument("--mode", choices=["step", "batch", "serve", "precision"], default="step",
                     help="step: the 512x512 single-cloth headline; batch: 256 mixed cloths; "
                          "serve: Poisson request stream through the continuous-batching server")
