@@ -6,10 +6,10 @@ Python mirror of the reference's cloth API.
 """
 from . import _native
 from ._native import ClothError, REFERENCE_PARAMS, SolveParams, params
-from .cloth import BaraffClothGpu, ClothContext, ClothServer, build_grid
+from .cloth import BaraffClothGpu, ClothContext, ClothServer, build_grid, load_obj_mesh
 
 __all__ = ["BaraffClothGpu", "ClothContext", "ClothError", "ClothServer", "REFERENCE_PARAMS", "SolveParams",
-           "build_grid", "params", "load_library"]
+           "build_grid", "load_obj_mesh", "params", "load_library"]
 
 
 def load_library():

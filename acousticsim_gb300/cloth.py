@@ -129,6 +129,23 @@ def build_grid(cloth_size=(1.0, 1.0), subdivision=(19, 19), init_pos=(0.0, 0.0, 
     return {"pos": pos, "uv": uv, "tris": tris, "edges": edges}
 
 
+def load_obj_mesh(path: str, translation=(0.0, 0.0, 0.0), relocate: bool = False) -> dict:
+    """cBaseCloth::InitGeometry's OBJ branch ("enable_cloth_from_obj"); arrays in numpy."""
+    tr = (C.c_double * 3)(*translation)
+    p = str(path).encode()
+    nv, nt, ne = C.c_int(), C.c_int(), C.c_int()
+    N.call("cloth_mesh_from_obj", p, tr, int(relocate), C.byref(nv), C.byref(nt),
+           C.byref(ne), None, None, None, None)
+    pos = np.zeros((nv.value, 3), np.float64)
+    uv = np.zeros((nv.value, 2), np.float32)
+    tris = np.zeros((nt.value, 3), np.int32)
+    edges = np.zeros((ne.value, 4), np.int32)
+    N.call("cloth_mesh_from_obj", p, tr, int(relocate), None, None, None,
+           N.ptr(pos, C.c_double), N.ptr(uv, C.c_float), N.ptr(tris, C.c_int),
+           N.ptr(edges, C.c_int))
+    return {"pos": pos, "uv": uv, "tris": tris, "edges": edges}
+
+
 def _vec(conf: dict, key: str, default=None):
     v = conf.get(key, default)
     if v is None:
@@ -156,6 +173,10 @@ class BaraffClothGpu:
     # ---------------------------------------------------------------- init
     def Init(self, conf: dict, mesh: dict | None = None) -> None:
         """cBaraffClothGpu::Init (BaraffClothGpu.cpp:24-49)."""
+        if mesh is None and conf.get("enable_cloth_from_obj", False):
+            mesh = load_obj_mesh(conf["cloth_obj_path"],
+                                 tuple(_vec(conf, "cloth_obj_translation", [0, 0, 0])[:3]),
+                                 bool(conf.get("enable_relocate_obj", False)))
         if mesh is None:
             gt = conf.get("geometry_type", "regular_triangle")
             if gt != "regular_triangle":

@@ -1598,20 +1598,9 @@ int cloth_ctx_get_stream(cloth_ctx *ctx, void **stream)
     return CLOTH_OK;
 }
 
-int cloth_grid_build(const cloth_grid_desc *grid, int *nv, int *nt, int *ne,
-                     double *pos, float *uv, int *tris, int *edges)
+static void copy_out_mesh(const Mesh &m, int *nv, int *nt, int *ne, double *pos, float *uv,
+                          int *tris, int *edges)
 {
-    if (!grid)
-        return fail(CLOTH_ERR_INVALID, "grid is NULL");
-    GridDesc g;
-    std::memcpy(g.size, grid->cloth_size, sizeof(g.size));
-    std::memcpy(g.subdiv, grid->subdivision, sizeof(g.subdiv));
-    std::memcpy(g.init_pos, grid->init_pos, sizeof(g.init_pos));
-    g.uv_rotation_deg = grid->uv_rotation_deg;
-    Mesh m;
-    std::string err;
-    if (!build_grid(g, m, err))
-        return fail(CLOTH_ERR_INVALID, err);
     if (nv)
         *nv = m.nv;
     if (nt)
@@ -1626,6 +1615,37 @@ int cloth_grid_build(const cloth_grid_desc *grid, int *nv, int *nt, int *ne,
         std::memcpy(tris, m.tris.data(), m.tris.size() * sizeof(int));
     if (edges)
         std::memcpy(edges, m.edges.data(), m.edges.size() * sizeof(int));
+}
+
+int cloth_mesh_from_obj(const char *path, const double *translation, int relocate, int *nv,
+                        int *nt, int *ne, double *pos, float *uv, int *tris, int *edges)
+{
+    if (!path)
+        return fail(CLOTH_ERR_INVALID, "cloth_mesh_from_obj: path is NULL");
+    const double zero[3] = {0.0, 0.0, 0.0};
+    Mesh m;
+    std::string err;
+    if (!load_obj_cloth(path, translation ? translation : zero, relocate != 0, m, err))
+        return fail(CLOTH_ERR_MESH, err);
+    copy_out_mesh(m, nv, nt, ne, pos, uv, tris, edges);
+    return CLOTH_OK;
+}
+
+int cloth_grid_build(const cloth_grid_desc *grid, int *nv, int *nt, int *ne,
+                     double *pos, float *uv, int *tris, int *edges)
+{
+    if (!grid)
+        return fail(CLOTH_ERR_INVALID, "grid is NULL");
+    GridDesc g;
+    std::memcpy(g.size, grid->cloth_size, sizeof(g.size));
+    std::memcpy(g.subdiv, grid->subdivision, sizeof(g.subdiv));
+    std::memcpy(g.init_pos, grid->init_pos, sizeof(g.init_pos));
+    g.uv_rotation_deg = grid->uv_rotation_deg;
+    Mesh m;
+    std::string err;
+    if (!build_grid(g, m, err))
+        return fail(CLOTH_ERR_INVALID, err);
+    copy_out_mesh(m, nv, nt, ne, pos, uv, tris, edges);
     return CLOTH_OK;
 }
 

@@ -185,36 +185,37 @@ bool build_grid(const GridDesc &g, Mesh &m, std::string &err)
 
 bool derive_edges(Mesh &m, std::string &err)
 {
-    std::map<std::pair<int, int>, int> index;
-    std::vector<int> edges;
+    // cObjUtil::BuildEdge (src/utils/ObjUtil.cpp:140-240): one edge per
+    // vertex pair (v0 < v1), numbered in ascending (v0, v1) order; tri0/tri1
+    // are the first/second triangle (in triangle order) that uses the pair.
+    std::map<std::pair<int, int>, std::pair<int, int>> info;
     for (int t = 0; t < m.nt; t++)
     {
         const int *v = &m.tris[size_t(t) * 3];
         for (int k = 0; k < 3; k++)
         {
-            int a = v[k], b = v[(k + 1) % 3];
-            auto key = std::make_pair(std::min(a, b), std::max(a, b));
-            auto it = index.find(key);
-            if (it == index.end())
+            const int a = v[k], b = v[(k + 1) % 3];
+            const auto key = std::make_pair(std::min(a, b), std::max(a, b));
+            auto it = info.find(key);
+            if (it == info.end())
+                info.emplace(key, std::make_pair(t, -1));
+            else if (it->second.second != -1)
             {
-                index.emplace(key, int(edges.size() / 4));
-                int e[4] = {key.first, key.second, t, -1};
-                edges.insert(edges.end(), e, e + 4);
+                err = "mesh: edge shared by more than two triangles";
+                return false;
             }
             else
-            {
-                int *e = &edges[size_t(it->second) * 4];
-                if (e[3] != -1)
-                {
-                    err = "mesh: edge shared by more than two triangles";
-                    return false;
-                }
-                e[3] = t;
-            }
+                it->second.second = t;
         }
     }
-    m.edges.swap(edges);
-    m.ne = int(m.edges.size() / 4);
+    m.edges.clear();
+    m.edges.reserve(info.size() * 4);
+    for (const auto &kv : info)
+    {
+        const int e[4] = {kv.first.first, kv.first.second, kv.second.first, kv.second.second};
+        m.edges.insert(m.edges.end(), e, e + 4);
+    }
+    m.ne = int(info.size());
     return true;
 }
 

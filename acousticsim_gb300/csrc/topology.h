@@ -75,10 +75,18 @@ struct Tables
 // RotateMaterialCoordsAfterReset (src/geometries/Triangulator.cpp:32-457, 621-658).
 bool build_grid(const GridDesc &g, Mesh &m, std::string &err);
 
-// Edge list from triangles when the caller gives none: unique sorted vertex
-// pairs in order of first appearance; tri0/tri1 are the first/second triangle
-// that uses the pair.  Fails on edges shared by more than two triangles.
+// Edge list from triangles when the caller gives none, as cObjUtil::BuildEdge
+// numbers it: one edge per vertex pair (v0 < v1) in ascending pair order;
+// tri0/tri1 are the first/second triangle that uses the pair.  Fails on edges
+// shared by more than two triangles.
 bool derive_edges(Mesh &m, std::string &err);
+
+// A cloth mesh from an OBJ file as cBaseCloth::InitGeometry builds it with
+// "enable_cloth_from_obj" (BaseCloth.cpp:292-356, cObjUtil::LoadObj): float
+// coordinates, y + 0.2, uv * 10/3, + translation, MoveObjPos when relocating;
+// triangles and quads (split along the shorter diagonal).  objmesh.cpp.
+bool load_obj_cloth(const std::string &path, const double translation[3], bool relocate,
+                    Mesh &m, std::string &err);
 
 // cBaseCloth::InitGeometry tail, InitMass, cBaraffClothGpu::InitELLMatrix,
 // InitStretchCoef, InitBendingMatrix/UpdateBendingMatrix, and the triangle ->

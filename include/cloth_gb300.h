@@ -56,7 +56,7 @@ typedef struct {
 /* Triangle mesh handed to cloth_create (cBaseCloth::InitGeometry,
  * src/sim/cloth/BaseCloth.cpp:292-416). */
 typedef struct {
-    int nv, nt, ne;        /* ne = 0 with edges = NULL: edges are derived */
+    int nv, nt, ne;        /* ne = 0 with edges = NULL: edges are derived (cObjUtil::BuildEdge order) */
     const double *pos;     /* nv*3 rest positions; also the initial state */
     const float *uv;       /* nv*2 material coordinates (tVertex::muv) */
     const int *tris;       /* nt*3 vertex ids */
@@ -174,6 +174,18 @@ int cloth_ctx_get_stream(cloth_ctx *ctx, void **stream);
  * tri0, tri1); boundary edges have tri1 = -1. */
 int cloth_grid_build(const cloth_grid_desc *grid, int *nv, int *nt, int *ne,
                      double *pos, float *uv, int *tris, int *edges);
+
+/* A cloth mesh from an OBJ file, as cBaseCloth::InitGeometry builds it with
+ * "enable_cloth_from_obj": true (src/sim/cloth/BaseCloth.cpp:292-356 over
+ * cObjUtil::LoadObj and cObjUtil::BuildEdge, src/utils/ObjUtil.cpp:10-240):
+ * "cloth_obj_path" = path, "cloth_obj_translation" = translation (may be NULL
+ * for zero), "enable_relocate_obj" = relocate.  Vertex i is OBJ vertex i (all
+ * must be used by faces), coordinates read as float, y + 0.2, uv from the face
+ * corners' texture coordinates times 10/3; faces are triangles or quads (split
+ * along the shorter diagonal, as the reference's tinyobjloader does); edges
+ * numbered in ascending vertex-pair order.  Sizes and fill as cloth_grid_build. */
+int cloth_mesh_from_obj(const char *path, const double *translation, int relocate, int *nv,
+                        int *nt, int *ne, double *pos, float *uv, int *tris, int *edges);
 
 /* Host-only (no device needed): the init-time tables cloth_create builds, in
  * the reference's layout. Call with all outputs NULL to get *ne and *width.

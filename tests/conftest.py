@@ -13,7 +13,7 @@ if str(ROOT) not in sys.path:
     sys.path.insert(0, str(ROOT))
 
 GOLDEN = ROOT / "tests" / "golden"
-GOLDEN_CASES = ["grid20", "rect_rot45", "small_rot90"]
+GOLDEN_CASES = ["grid20", "rect_rot45", "small_rot90", "obj_irregular", "obj_relocated"]
 
 
 def pytest_configure(config):
@@ -23,7 +23,20 @@ def pytest_configure(config):
 def load_golden(name: str):
     g = np.load(GOLDEN / f"{name}.npz")
     conf = json.loads(bytes(g["config_json"]).decode())
+    if conf.get("enable_cloth_from_obj"):
+        conf["cloth_obj_path"] = str(GOLDEN / conf["cloth_obj_path"])
     return g, conf
+
+
+def golden_mesh(conf: dict) -> dict:
+    """The case's mesh from the library's host code: the OBJ loader for
+    "enable_cloth_from_obj" cases, else the regular-grid generator."""
+    from acousticsim_gb300 import build_grid, load_obj_mesh
+    if conf.get("enable_cloth_from_obj"):
+        return load_obj_mesh(conf["cloth_obj_path"], conf.get("cloth_obj_translation", [0, 0, 0]),
+                             conf.get("enable_relocate_obj", False))
+    return build_grid(tuple(conf["cloth_size"]), tuple(conf["subdivision"]),
+                      tuple(conf["cloth_init_pos"]), conf["cloth_uv_rotation"])
 
 
 def rel(a, ref) -> float:

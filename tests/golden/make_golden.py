@@ -62,6 +62,83 @@ CASES = [
 ]
 
 
+# OBJ cloths ("enable_cloth_from_obj"): (name, OBJ file under tests/golden,
+# config overrides, seed, position noise, velocity noise).  The OBJ is written
+# by irregular_obj() below; the config names it relative to tests/golden.
+OBJ_CASES = [
+    # 8 x 10 jittered lattice in the XY plane: per cell a quad (split by the
+    # loader), two triangles with either diagonal, or a fan around an added
+    # centre vertex; vertices numbered in shuffled order; two top pins.
+    ("obj_irregular", "irregular.obj",
+     {"cloth_obj_size": [0.8, 1.0], "cloth_obj_translation": [0.05, -0.1, 0.02],
+      "enable_relocate_obj": False,
+      "cloth_stretch_stiffness": [1e3, 8e2, 1e2], "cloth_bending_stiffness": [2e-3, 2e-3],
+      "cloth_density": 0.15, "rayleigh_damping_a": 0.01, "rayleigh_damping_b": 0.0,
+      "default_timestep": 4e-3,
+      "constraints": {"static_point": [[-0.4, 0.5], [0.4, 0.5]]}},
+     4, 1e-3, 1e-2),
+    # the same file relocated (MoveObjPos: top at y = 0.27, centred in x, z)
+    ("obj_relocated", "irregular.obj",
+     {"cloth_obj_size": [0.8, 1.0], "cloth_obj_translation": [0.3, 0.1, -0.2],
+      "enable_relocate_obj": True,
+      "cloth_stretch_stiffness": [1e3, 1e3, 1e2], "cloth_bending_stiffness": [1e-3, 1e-3],
+      "cloth_density": 0.1, "rayleigh_damping_a": 0.01, "rayleigh_damping_b": 0.0,
+      "default_timestep": 2e-3,
+      "constraints": {"static_point": [[-0.4, 0.5], [0.4, 0.5]]}},
+     5, 1e-3, 1e-2),
+]
+
+
+def irregular_obj(path: Path, seed: int = 17, nx: int = 8, ny: int = 10) -> None:
+    """A seeded irregular cloth mesh (triangles and quads) as an OBJ file."""
+    rng = np.random.default_rng(seed)
+    w, h = 0.8, 1.0
+    pts = []
+    for j in range(ny + 1):
+        for i in range(nx + 1):
+            x = -w / 2 + w * i / nx
+            y = -h / 2 + h * j / ny
+            if 0 < i < nx and 0 < j < ny:
+                x += rng.uniform(-0.2, 0.2) * w / nx
+                y += rng.uniform(-0.2, 0.2) * h / ny
+            pts.append((x, y))
+    idx = lambda i, j: j * (nx + 1) + i
+    faces = []
+    for j in range(ny):
+        for i in range(nx):
+            a, b, c, d = idx(i, j), idx(i + 1, j), idx(i + 1, j + 1), idx(i, j + 1)
+            kind = rng.integers(0, 4)
+            if kind == 0:
+                faces.append((a, b, c, d))
+            elif kind == 1:
+                faces += [(a, b, c), (a, c, d)]
+            elif kind == 2:
+                faces += [(a, b, d), (b, c, d)]
+            else:
+                cx = np.mean([pts[k][0] for k in (a, b, c, d)])
+                cy = np.mean([pts[k][1] for k in (a, b, c, d)])
+                pts.append((cx, cy))
+                m = len(pts) - 1
+                faces += [(a, b, m), (b, c, m), (c, d, m), (d, a, m)]
+    n = len(pts)
+    perm = rng.permutation(n)          # OBJ number of lattice point k
+    inv = np.argsort(perm)
+    vt_perm = rng.permutation(n)       # texture coordinate slot of OBJ vertex q
+    with open(path, "w") as f:
+        f.write("# seeded irregular cloth (tests/golden/make_golden.py)\n")
+        for q in range(n):
+            x, y = pts[inv[q]]
+            f.write(f"v {x:.6f} {y:.6f} 0.000000\n")
+        vt_of = np.empty(n, np.int64)
+        for slot in range(n):
+            q = int(np.flatnonzero(vt_perm == slot)[0])
+            x, y = pts[inv[q]]
+            f.write(f"vt {0.3 * x:.6f} {0.3 * y:.6f}\n")
+            vt_of[q] = slot
+        for fc in faces:
+            f.write("f " + " ".join(f"{perm[k] + 1}/{vt_of[perm[k]] + 1}" for k in fc) + "\n")
+
+
 def read_dump(d: Path) -> dict:
     out = {}
     for line in (d / "manifest.txt").read_text().splitlines():
@@ -74,15 +151,26 @@ def read_dump(d: Path) -> dict:
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--only", nargs="*", default=None, help="case names to regenerate")
     a = ap.parse_args()
     subprocess.run(["make", "-C", str(ROOT / "oracle"), f"REF={a.ref}", "-j8"], check=True,
                    stdout=subprocess.DEVNULL)
     harness = ROOT / "oracle" / "_ref" / "ref_harness"
-    for name, over, seed, sx, sv in CASES:
+    cases = [(name, over, seed, sx, sv, None) for name, over, seed, sx, sv in CASES]
+    for name, obj, over, seed, sx, sv in OBJ_CASES:
+        irregular_obj(OUT / obj)
+        o = dict(over, enable_cloth_from_obj=True, cloth_obj_path=obj)
+        cases.append((name, o, seed, sx, sv, obj))
+    for name, over, seed, sx, sv, obj in cases:
+        if a.only and name not in a.only:
+            continue
         conf = dict(BASE, **over)
+        run_conf = dict(conf)
+        if obj is not None:
+            run_conf["cloth_obj_path"] = str(OUT / obj)
         with tempfile.TemporaryDirectory() as td:
             td = Path(td)
-            (td / "cfg.json").write_text(json.dumps(conf))
+            (td / "cfg.json").write_text(json.dumps(run_conf))
             (td / "topo").mkdir()
             subprocess.run([str(harness), "topo", str(td / "cfg.json"), str(td / "topo")],
                            check=True, stdout=subprocess.DEVNULL)

@@ -19,9 +19,8 @@ def N(built):
 
 
 def _grid(conf):
-    from acousticsim_gb300 import build_grid
-    return build_grid(tuple(conf["cloth_size"]), tuple(conf["subdivision"]),
-                      tuple(conf["cloth_init_pos"]), conf["cloth_uv_rotation"])
+    from conftest import golden_mesh
+    return golden_mesh(conf)
 
 
 def _material(N, conf):

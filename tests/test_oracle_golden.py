@@ -6,7 +6,7 @@ from __future__ import annotations
 import numpy as np
 import pytest
 
-from conftest import GOLDEN_CASES, load_golden, project_pins, rel
+from conftest import GOLDEN_CASES, golden_mesh, load_golden, project_pins, rel
 
 
 @pytest.fixture(scope="module")
@@ -16,6 +16,9 @@ def orc(built):
 
 
 def _mesh(orc, conf):
+    if conf.get("enable_cloth_from_obj"):
+        # the library's OBJ loader (host code), pinned by the first test below
+        return golden_mesh(conf)
     return orc.grid(conf["cloth_size"], conf["subdivision"], conf["cloth_init_pos"],
                     conf["cloth_uv_rotation"])
 
