@@ -769,3 +769,579 @@ int orc_pcg(int nv, const int *ell, const double *A, const double *b,
     free(q);
     return it;
 }
+
+/* ------------------------------------------------------------------ collisions */
+/* The CPU cloth's collision handling against a static kinematic body
+ * (cBVHCollisionDetecter::PerformCD, src/sim/collision/BVHCollisionDetecter.cpp;
+ * cBaraffCloth::PrepareCollisionHessian and Repulsion, src/sim/cloth/
+ * BaraffCloth.cpp:614-990), with the cloth as object 0 and the body as 1. */
+
+static void nrm3(const double *a, double *o)
+{
+    const double n = sqrt(a[0] * a[0] + a[1] * a[1] + a[2] * a[2]);
+    for (int k = 0; k < 3; k++)
+        o[k] = a[k] / n;
+}
+
+static void tri_normal(const double *x, const int *t, double *n)
+{
+    /* cBaseObject::UpdateTriangleNormal (BaseObject.cpp:119-131) */
+    const double *v0 = x + 3 * (size_t)t[0], *v1 = x + 3 * (size_t)t[1],
+                 *v2 = x + 3 * (size_t)t[2];
+    double a[3], b[3], c[3];
+    for (int k = 0; k < 3; k++)
+    {
+        a[k] = v1[k] - v0[k];
+        b[k] = v2[k] - v1[k];
+    }
+    cross3(a, b, c);
+    nrm3(c, n);
+}
+
+void orc_body_normals(int nv, int nt, const double *pos, const int *tris, double *tnormal,
+                      double *vnormal)
+{
+    /* cKinematicBody::Init tail: CalcTriangleInitArea, UpdateTriangleNormal,
+     * UpdateVertexNormalFromTriangleNormal (BaseObject.cpp:119-160, 292-304):
+     * area-weighted sum of triangle normals, normalised. */
+    memset(vnormal, 0, sizeof(double) * 3 * (size_t)nv);
+    for (int t = 0; t < nt; t++)
+    {
+        const int *tv = tris + 3 * (size_t)t;
+        tri_normal(pos, tv, tnormal + 3 * (size_t)t);
+        const double *p0 = pos + 3 * (size_t)tv[0], *p1 = pos + 3 * (size_t)tv[1],
+                     *p2 = pos + 3 * (size_t)tv[2];
+        /* cMathUtil::CalcTriangleArea (MathUtil2.cpp:344-357): float */
+        double e1[3], e2[3], c[3];
+        for (int k = 0; k < 3; k++)
+        {
+            e1[k] = p1[k] - p0[k];
+            e2[k] = p2[k] - p0[k];
+        }
+        cross3(e1, e2, c);
+        const double area = (double)(float)(0.5 * sqrt(c[0] * c[0] + c[1] * c[1] + c[2] * c[2]));
+        for (int i = 0; i < 3; i++)
+            for (int k = 0; k < 3; k++)
+                vnormal[3 * (size_t)tv[i] + k] += tnormal[3 * (size_t)t + k] * area;
+    }
+    for (int v = 0; v < nv; v++)
+    {
+        double *n = vnormal + 3 * (size_t)v;
+        const double l = sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+        if (l > 0)
+            for (int k = 0; k < 3; k++)
+                n[k] /= l;
+    }
+}
+
+static float clampf01(float v) { return v < 0.0f ? 0.0f : (v > 1.0f ? 1.0f : v); }
+
+/* ClosestPtPointTriangle (BVHCollisionDetecter.cpp:17-86): Ericson's region
+ * test with the dot products rounded to float, as the reference keeps them. */
+static void closest_pt_tri(const double *p, const double *a, const double *b, const double *c,
+                           double *q, float *bary)
+{
+    double ab[3], ac[3], ap[3], bp[3], cp[3];
+    for (int k = 0; k < 3; k++)
+    {
+        ab[k] = b[k] - a[k];
+        ac[k] = c[k] - a[k];
+        ap[k] = p[k] - a[k];
+        bp[k] = p[k] - b[k];
+        cp[k] = p[k] - c[k];
+    }
+    bary[0] = bary[1] = bary[2] = 0.f;
+    const float d1 = (float)dot3(ab, ap), d2 = (float)dot3(ac, ap);
+    if (d1 <= 0.0f && d2 <= 0.0f)
+    {
+        bary[0] = 1;
+        memcpy(q, a, 3 * sizeof(double));
+        return;
+    }
+    const float d3 = (float)dot3(ab, bp), d4 = (float)dot3(ac, bp);
+    if (d3 >= 0.0f && d4 <= d3)
+    {
+        bary[1] = 1;
+        memcpy(q, b, 3 * sizeof(double));
+        return;
+    }
+    const float vc = d1 * d4 - d3 * d2;
+    if (vc <= 0.0f && d1 >= 0.0f && d3 <= 0.0f)
+    {
+        const float v = d1 / (d1 - d3);
+        bary[0] = 1 - v;
+        bary[1] = v;
+        for (int k = 0; k < 3; k++)
+            q[k] = a[k] + (double)v * ab[k];
+        return;
+    }
+    const float d5 = (float)dot3(ab, cp), d6 = (float)dot3(ac, cp);
+    if (d6 >= 0.0f && d5 <= d6)
+    {
+        bary[2] = 1;
+        memcpy(q, c, 3 * sizeof(double));
+        return;
+    }
+    const float vb = d5 * d2 - d1 * d6;
+    if (vb <= 0.0f && d2 >= 0.0f && d6 <= 0.0f)
+    {
+        const float w = d2 / (d2 - d6);
+        bary[0] = 1 - w;
+        bary[2] = w;
+        for (int k = 0; k < 3; k++)
+            q[k] = a[k] + (double)w * ac[k];
+        return;
+    }
+    const float va = d3 * d6 - d5 * d4;
+    if (va <= 0.0f && (d4 - d3) >= 0.0f && (d5 - d6) >= 0.0f)
+    {
+        const float w = (d4 - d3) / ((d4 - d3) + (d5 - d6));
+        bary[1] = 1 - w;
+        bary[2] = w;
+        for (int k = 0; k < 3; k++)
+            q[k] = b[k] + (double)w * (c[k] - b[k]);
+        return;
+    }
+    const float denom = 1.0f / (va + vb + vc);
+    const float v = vb * denom, w = vc * denom;
+    bary[0] = 1 - v - w;
+    bary[1] = v;
+    bary[2] = w;
+    for (int k = 0; k < 3; k++)
+        q[k] = a[k] + ab[k] * (double)v + ac[k] * (double)w;
+}
+
+/* EdgeEdgeDist (BVHCollisionDetecter.cpp:100-175): closest points of two
+ * segments, Ericson's method with float scalars; s on [p1 q1], t on [p2 q2]. */
+static void edge_edge(const double *p1, const double *q1, const double *p2, const double *q2,
+                      float *s_out, float *t_out)
+{
+    double d1[3], d2[3], r[3];
+    for (int k = 0; k < 3; k++)
+    {
+        d1[k] = q1[k] - p1[k];
+        d2[k] = q2[k] - p2[k];
+        r[k] = p1[k] - p2[k];
+    }
+    const float a = (float)dot3(d1, d1), e = (float)dot3(d2, d2), f = (float)dot3(d2, r);
+    const float EPS = 1e-10f;
+    float s = 0, t = 0;
+    if (a <= EPS && e <= EPS)
+        s = t = 0.0f; /* the reference goes on to the next test */
+    if (a <= EPS)
+    {
+        s = 0.0f;
+        t = clampf01(f / e);
+    }
+    else
+    {
+        const float c = (float)dot3(d1, r);
+        if (e <= EPS)
+        {
+            t = 0.0f;
+            s = clampf01(-c / a);
+        }
+        else
+        {
+            const float b = (float)dot3(d1, d2);
+            const float denom = a * e - b * b;
+            s = denom != 0.0f ? clampf01((b * f - c * e) / denom) : 0.0f;
+            t = (b * s + f) / e;
+            if (t < 0.0f)
+            {
+                t = 0.0f;
+                s = clampf01(-c / a);
+            }
+            else if (t > 1.0f)
+            {
+                t = 1.0f;
+                s = clampf01((b - c) / a);
+            }
+        }
+    }
+    *s_out = s;
+    *t_out = t;
+}
+
+typedef struct
+{
+    int a, b;
+} ipair;
+
+static int cmp_ipair(const void *x, const void *y)
+{
+    const ipair *p = (const ipair *)x, *q = (const ipair *)y;
+    if (p->a != q->a)
+        return p->a < q->a ? -1 : 1;
+    return p->b < q->b ? -1 : (p->b > q->b ? 1 : 0);
+}
+
+static size_t sort_unique(ipair *v, size_t n)
+{
+    if (n == 0)
+        return 0;
+    qsort(v, n, sizeof(ipair), cmp_ipair);
+    size_t m = 1;
+    for (size_t i = 1; i < n; i++)
+        if (cmp_ipair(&v[i], &v[m - 1]) != 0)
+            v[m++] = v[i];
+    return m;
+}
+
+/* triangle -> its edges (v0 v1), (v1 v2), (v2 v0) (BuildTriangleEdgeId) */
+static void tri_edges(int nt, int ne, const int *tris, const int *edges, int *te)
+{
+    for (int i = 0; i < 3 * nt; i++)
+        te[i] = -1;
+    for (int e = 0; e < ne; e++)
+        for (int s = 2; s <= 3; s++)
+        {
+            const int t = edges[4 * (size_t)e + s];
+            if (t < 0)
+                continue;
+            const int *v = tris + 3 * (size_t)t;
+            for (int k = 0; k < 3; k++)
+            {
+                const int a = v[k], b = v[(k + 1) % 3];
+                const int lo = a < b ? a : b, hi = a < b ? b : a;
+                if (lo == edges[4 * (size_t)e] && hi == edges[4 * (size_t)e + 1])
+                    te[3 * (size_t)t + k] = e;
+            }
+        }
+}
+
+static void aabb5(const double *x, const int *t, double *lo, double *hi)
+{
+    /* leaf AABB of cObjBVH::UpdateAABB: the triangle's box grown by 5 mm */
+    for (int k = 0; k < 3; k++)
+    {
+        double mn = x[3 * (size_t)t[0] + k], mx = mn;
+        for (int i = 1; i < 3; i++)
+        {
+            const double v = x[3 * (size_t)t[i] + k];
+            mn = v < mn ? v : mn;
+            mx = v > mx ? v : mx;
+        }
+        lo[k] = mn - 5e-3;
+        hi[k] = mx + 5e-3;
+    }
+}
+
+int orc_contacts(int nv, int nt, int ne, const double *x, const int *tris, const int *edges,
+                 int bnv, int bnt, int bne, const double *bpos, const int *btris,
+                 const int *bedges, const double *btn, const double *bvn, int max_pt,
+                 int *pt_i, double *pt_d, int *n_pt, int max_ee, int *ee_i, double *ee_d,
+                 int *n_ee)
+{
+    (void)nv;
+    (void)bnv;
+    /* broad phase: triangle pairs whose grown boxes meet (the BVH pair walk
+     * reaches exactly these leaves) */
+    double *tn = (double *)malloc(sizeof(double) * 3 * (size_t)nt);
+    double *clo = (double *)malloc(sizeof(double) * 3 * (size_t)nt),
+           *chi = (double *)malloc(sizeof(double) * 3 * (size_t)nt);
+    double *blo = (double *)malloc(sizeof(double) * 3 * (size_t)bnt),
+           *bhi = (double *)malloc(sizeof(double) * 3 * (size_t)bnt);
+    for (int t = 0; t < nt; t++)
+    {
+        tri_normal(x, tris + 3 * (size_t)t, tn + 3 * (size_t)t);
+        aabb5(x, tris + 3 * (size_t)t, clo + 3 * (size_t)t, chi + 3 * (size_t)t);
+    }
+    for (int t = 0; t < bnt; t++)
+        aabb5(bpos, btris + 3 * (size_t)t, blo + 3 * (size_t)t, bhi + 3 * (size_t)t);
+    size_t cap = 1024, np = 0;
+    ipair *tp = (ipair *)malloc(sizeof(ipair) * cap);
+    for (int T = 0; T < nt; T++)
+        for (int t = 0; t < bnt; t++)
+        {
+            const double *al = clo + 3 * (size_t)T, *ah = chi + 3 * (size_t)T,
+                         *bl = blo + 3 * (size_t)t, *bh = bhi + 3 * (size_t)t;
+            if (al[0] <= bh[0] && ah[0] >= bl[0] && al[1] <= bh[1] && ah[1] >= bl[1] &&
+                al[2] <= bh[2] && ah[2] >= bl[2])
+            {
+                if (np == cap)
+                {
+                    cap *= 2;
+                    tp = (ipair *)realloc(tp, sizeof(ipair) * cap);
+                }
+                tp[np].a = T;
+                tp[np].b = t;
+                np++;
+            }
+        }
+    int *te = (int *)malloc(sizeof(int) * 3 * (size_t)nt);
+    int *bte = (int *)malloc(sizeof(int) * 3 * (size_t)bnt);
+    tri_edges(nt, ne, tris, edges, te);
+    tri_edges(bnt, bne, btris, bedges, bte);
+    ipair *p01 = (ipair *)malloc(sizeof(ipair) * (3 * np + 1));
+    ipair *p10 = (ipair *)malloc(sizeof(ipair) * (3 * np + 1));
+    ipair *pee = (ipair *)malloc(sizeof(ipair) * (9 * np + 1));
+    for (size_t i = 0; i < np; i++)
+    {
+        const int T = tp[i].a, t = tp[i].b;
+        for (int k = 0; k < 3; k++)
+        {
+            p01[3 * i + k].a = tris[3 * (size_t)T + k];
+            p01[3 * i + k].b = t;
+            p10[3 * i + k].a = btris[3 * (size_t)t + k];
+            p10[3 * i + k].b = T;
+        }
+        for (int a = 0; a < 3; a++)
+            for (int b = 0; b < 3; b++)
+            {
+                pee[9 * i + 3 * a + b].a = te[3 * (size_t)T + a];
+                pee[9 * i + 3 * a + b].b = bte[3 * (size_t)t + b];
+            }
+    }
+    const size_t n01 = sort_unique(p01, 3 * np), n10 = sort_unique(p10, 3 * np),
+                 nee = sort_unique(pee, 9 * np);
+    int cpt = 0, cee = 0, overflow = 0;
+    /* narrow phase, point-triangle: cloth points against body triangles, then
+     * body points against cloth triangles (distance under 3 mm) */
+    for (int pass = 0; pass < 2; pass++)
+    {
+        const ipair *pl = pass == 0 ? p01 : p10;
+        const size_t n = pass == 0 ? n01 : n10;
+        for (size_t i = 0; i < n; i++)
+        {
+            const int p = pl[i].a, t = pl[i].b;
+            const double *pt = pass == 0 ? x + 3 * (size_t)p : bpos + 3 * (size_t)p;
+            const int *tv = pass == 0 ? btris + 3 * (size_t)t : tris + 3 * (size_t)t;
+            const double *tx = pass == 0 ? bpos : x;
+            double q[3], normal[3], dv[3];
+            float bary[3];
+            closest_pt_tri(pt, tx + 3 * (size_t)tv[0], tx + 3 * (size_t)tv[1],
+                           tx + 3 * (size_t)tv[2], q, bary);
+            if (pass == 0)
+            {
+                memcpy(normal, btn + 3 * (size_t)t, sizeof(normal));
+                for (int k = 0; k < 3; k++)
+                    dv[k] = pt[k] - q[k];
+            }
+            else
+            {
+                memcpy(normal, tn + 3 * (size_t)t, sizeof(normal));
+                if (dot3(normal, bvn + 3 * (size_t)p) < 0)
+                    for (int k = 0; k < 3; k++)
+                        normal[k] *= -1;
+                for (int k = 0; k < 3; k++)
+                    dv[k] = q[k] - pt[k];
+            }
+            if (sqrt(dot3(dv, dv)) < 3e-3)
+            {
+                if (cpt >= max_pt)
+                {
+                    overflow = 1;
+                    continue;
+                }
+                pt_i[3 * cpt + 0] = pass == 0 ? 1 : 0;
+                pt_i[3 * cpt + 1] = p;
+                pt_i[3 * cpt + 2] = t;
+                for (int k = 0; k < 3; k++)
+                    pt_d[7 * cpt + k] = normal[k];
+                pt_d[7 * cpt + 3] = (double)(float)dot3(dv, normal);
+                for (int k = 0; k < 3; k++)
+                    pt_d[7 * cpt + 4 + k] = (double)bary[k];
+                cpt++;
+            }
+        }
+    }
+    /* narrow phase, edge-edge: cloth edge e0 against body edge e1 */
+    for (size_t i = 0; i < nee; i++)
+    {
+        const int e0 = pee[i].a, e1 = pee[i].b;
+        const double *p0 = x + 3 * (size_t)edges[4 * (size_t)e0],
+                     *p1 = x + 3 * (size_t)edges[4 * (size_t)e0 + 1];
+        const double *p2 = bpos + 3 * (size_t)bedges[4 * (size_t)e1],
+                     *p3 = bpos + 3 * (size_t)bedges[4 * (size_t)e1 + 1];
+        float s, t;
+        edge_edge(p0, p1, p2, p3, &s, &t);
+        double c0[3], c1[3], d01[3], d23[3], cr[3], normal[3], on[3], dv[3];
+        const float s1 = 1 - s, t1 = 1 - t;
+        for (int k = 0; k < 3; k++)
+        {
+            c0[k] = (double)s1 * p0[k] + (double)s * p1[k];
+            c1[k] = (double)t1 * p2[k] + (double)t * p3[k];
+            d01[k] = p1[k] - p0[k];
+            d23[k] = p3[k] - p2[k];
+        }
+        cross3(d01, d23, cr);
+        nrm3(cr, normal);
+        const int bt0 = bedges[4 * (size_t)e1 + 2], bt1 = bedges[4 * (size_t)e1 + 3];
+        for (int k = 0; k < 3; k++)
+            on[k] = btn[3 * (size_t)bt0 + k] + (bt1 != -1 ? btn[3 * (size_t)bt1 + k] : 0.0);
+        {
+            double o2[3];
+            nrm3(on, o2);
+            if (dot3(o2, normal) < 0)
+                for (int k = 0; k < 3; k++)
+                    normal[k] *= -1;
+        }
+        for (int k = 0; k < 3; k++)
+            dv[k] = c0[k] - c1[k];
+        if (sqrt(dot3(dv, dv)) < 3e-3)
+        {
+            if (cee >= max_ee)
+            {
+                overflow = 1;
+                continue;
+            }
+            ee_i[3 * cee + 0] = 1;
+            ee_i[3 * cee + 1] = e0;
+            ee_i[3 * cee + 2] = e1;
+            for (int k = 0; k < 3; k++)
+                ee_d[6 * cee + k] = normal[k];
+            ee_d[6 * cee + 3] = (double)(float)dot3(dv, normal);
+            ee_d[6 * cee + 4] = (double)s;
+            ee_d[6 * cee + 5] = (double)t;
+            cee++;
+        }
+    }
+    *n_pt = cpt;
+    *n_ee = cee;
+    free(tn);
+    free(clo);
+    free(chi);
+    free(blo);
+    free(bhi);
+    free(tp);
+    free(te);
+    free(bte);
+    free(p01);
+    free(p10);
+    free(pee);
+    return overflow ? -1 : 0;
+}
+
+void orc_contact_hessian(int nv, const int *tris, const int *ell, int n_pt, const int *pt_i,
+                         const double *pt_d, double *H)
+{
+    (void)nv;
+    /* PrepareCollisionHessian (BaraffCloth.cpp:928-990): 1e-2 dC/dx dC/dx^T per
+     * point-triangle contact, dC/dx = N at a cloth point, -b_i N at the
+     * vertices of a cloth triangle; added to the system matrix unscaled */
+    for (int c = 0; c < n_pt; c++)
+    {
+        const double *N = pt_d + 7 * (size_t)c;
+        int vid[3];
+        double w[3];
+        int nvtx;
+        if (pt_i[3 * c] == 1)
+        {
+            vid[0] = pt_i[3 * c + 1];
+            w[0] = 1.0;
+            nvtx = 1;
+        }
+        else
+        {
+            const int *tv = tris + 3 * (size_t)pt_i[3 * c + 2];
+            for (int i = 0; i < 3; i++)
+            {
+                vid[i] = tv[i];
+                w[i] = -pt_d[7 * (size_t)c + 4 + i];
+            }
+            nvtx = 3;
+        }
+        for (int i = 0; i < nvtx; i++)
+            for (int j = 0; j < nvtx; j++)
+            {
+                const int slot = row_find(ell + (size_t)vid[i] * W, vid[j]);
+                double *blk = H + ((size_t)vid[i] * W + slot) * 9;
+                for (int a = 0; a < 3; a++)
+                    for (int b = 0; b < 3; b++)
+                        blk[3 * a + b] += 1e-2 * ((w[i] * N[a]) * (w[j] * N[b]));
+            }
+    }
+}
+
+void orc_repulsion(int nv, const int *tris, const int *edges, const double *mass,
+                   const float stretch_k[3], double dt, int n_pt, const int *pt_i,
+                   const double *pt_d, int n_ee, const int *ee_i, const double *ee_d,
+                   double *dx)
+{
+    (void)nv;
+    /* cBaraffCloth::Repulsion (BaraffCloth.cpp:626-926): Bridson-style
+     * impulses along the contact normals, edge-edge contacts first, then
+     * point-triangle ones, each reading dx as the earlier ones left it.
+     * |Ic| = m |vn| / 2 unless vn > 0.01; |Ir| = min(dt K d, m (0.1 d / dt - vn))
+     * unless vn > 0.1 d / dt, d = 3 mm - depth, K = mean stretch stiffness;
+     * increments scaled by 0.1. */
+    const float kmean = ((stretch_k[0] + stretch_k[1]) + stretch_k[2]) / 3.0f;
+    const double K = (double)kmean * 1;
+    const double v_thre = 0.01;
+    const double scale = (double)0.1f;
+    for (int c = 0; c < n_ee; c++)
+    {
+        /* the edge barycentric coordinates are float, and so is the
+         * arithmetic on them alone */
+        const double *N = ee_d + 6 * (size_t)c;
+        const float a = (float)ee_d[6 * (size_t)c + 4], b = (float)ee_d[6 * (size_t)c + 5];
+        const float a1 = 1 - a;
+        const int e = ee_i[3 * c + 1];
+        const int v0 = edges[4 * (size_t)e], v1 = edges[4 * (size_t)e + 1];
+        double vrel[3];
+        for (int k = 0; k < 3; k++)
+            vrel[k] = ((double)a1 * dx[3 * (size_t)v0 + k] + (double)a * dx[3 * (size_t)v1 + k]) / dt;
+        const double m = mass[v0] + mass[v1];
+        const double vn = dot3(vrel, N);
+        const double Ic = vn > v_thre ? 0 : m * fabs(vn) / 2;
+        const double d = 3e-3 - ee_d[6 * (size_t)c + 3];
+        double Ir = 0;
+        if (!(vn > 0.1f * d / dt))
+        {
+            const double Ir0 = dt * K * d, Ir1 = m * (0.1f * d / dt - vn);
+            Ir = Ir0 < Ir1 ? Ir0 : Ir1;
+        }
+        const double I = Ic + Ir;
+        const float den = 1 + a * a + (1 - a) * (1 - a) + b * b + (1 - b) * (1 - b);
+        const double It = 2 * I / (double)den;
+        for (int k = 0; k < 3; k++)
+        {
+            dx[3 * (size_t)v0 + k] += scale * dt * (double)a1 * It / m * N[k];
+            dx[3 * (size_t)v1 + k] += scale * dt * (double)a * It / m * N[k];
+        }
+    }
+    for (int c = 0; c < n_pt; c++)
+    {
+        const double *N = pt_d + 7 * (size_t)c;
+        const double *bary = pt_d + 7 * (size_t)c + 4;
+        double vrel[3], m;
+        const int *tv = tris + 3 * (size_t)pt_i[3 * c + 2];
+        if (pt_i[3 * c] == 1)
+        {
+            const int p = pt_i[3 * c + 1];
+            for (int k = 0; k < 3; k++)
+                vrel[k] = dx[3 * (size_t)p + k] / dt;
+            m = mass[p];
+        }
+        else
+        {
+            for (int k = 0; k < 3; k++)
+                vrel[k] = (dx[3 * (size_t)tv[0] + k] * bary[0] + dx[3 * (size_t)tv[1] + k] * bary[1] +
+                           dx[3 * (size_t)tv[2] + k] * bary[2]) /
+                          dt;
+            m = mass[tv[0]] + mass[tv[1]] + mass[tv[2]];
+        }
+        const double vn = dot3(vrel, N);
+        const double Ic = vn > v_thre ? 0 : m * fabs(vn) / 2;
+        const double d = 3e-3 - pt_d[7 * (size_t)c + 3];
+        double Ir = 0;
+        if (!(vn > 0.1 * d / dt))
+        {
+            const double Ir0 = dt * K * d, Ir1 = m * (0.1 * d / dt - vn);
+            Ir = Ir0 < Ir1 ? Ir0 : Ir1;
+        }
+        const double I = Ic + Ir;
+        const double It = 2 * I / (1 + dot3(bary, bary));
+        if (pt_i[3 * c] == 1)
+        {
+            const int p = pt_i[3 * c + 1];
+            for (int k = 0; k < 3; k++)
+                dx[3 * (size_t)p + k] += scale * (dt * It / m * N[k]);
+        }
+        else
+            for (int i = 0; i < 3; i++)
+                for (int k = 0; k < 3; k++)
+                    dx[3 * (size_t)tv[i] + k] += scale * (dt * bary[i] * It / m * N[k]);
+    }
+}

@@ -74,6 +74,28 @@ void orc_dihedral(int nv, int ne, const int *stencil, const double *factor,
                   const double *x, const int *ell, double *fint, double *K,
                   double *beta_out, double *grad_out);
 
+/* Collisions of the CPU cloth with one static kinematic body
+ * (cBVHCollisionDetecter, cBaraffCloth::PrepareCollisionHessian / Repulsion).
+ * Body normals as the body's Init leaves them: tnormal nt*3, vnormal nv*3. */
+void orc_body_normals(int nv, int nt, const double *pos, const int *tris, double *tnormal,
+                      double *vnormal);
+/* Contacts in the detecter's order.  pt_i: (cloth point?, point id, triangle
+ * id) with pt_d: (normal, depth, bary); ee_i: (1, cloth edge, body edge) with
+ * ee_d: (normal, depth, bary0, bary1).  Returns -1 when a list overflowed. */
+int orc_contacts(int nv, int nt, int ne, const double *x, const int *tris, const int *edges,
+                 int bnv, int bnt, int bne, const double *bpos, const int *btris,
+                 const int *bedges, const double *btn, const double *bvn, int max_pt,
+                 int *pt_i, double *pt_d, int *n_pt, int max_ee, int *ee_i, double *ee_d,
+                 int *n_ee);
+/* The contact Hessian added into H (nv*32*9). */
+void orc_contact_hessian(int nv, const int *tris, const int *ell, int n_pt, const int *pt_i,
+                         const double *pt_d, double *H);
+/* Repulsion of dx (nv*3, in place). */
+void orc_repulsion(int nv, const int *tris, const int *edges, const double *mass,
+                   const float stretch_k[3], double dt, int n_pt, const int *pt_i,
+                   const double *pt_d, int n_ee, const int *ee_i, const double *ee_d,
+                   double *dx);
+
 /* y = A x over ELL blocks. */
 void orc_spmv(int nv, const int *ell, const double *A, const double *x, double *y);
 

@@ -42,6 +42,16 @@ def lib() -> C.CDLL:
         L.orc_dihedral_rest.argtypes = [C.c_int, C.c_int, C.c_int, PD, PI, PI, C.c_float, PD]
         L.orc_dihedral.argtypes = [C.c_int, C.c_int, PI, PD, PD, PI, PD, PD, PD, PD]
         L.orc_dihedral.restype = None
+        L.orc_body_normals.argtypes = [C.c_int, C.c_int, PD, PI, PD, PD]
+        L.orc_body_normals.restype = None
+        L.orc_contacts.argtypes = [C.c_int, C.c_int, C.c_int, PD, PI, PI, C.c_int, C.c_int,
+                                   C.c_int, PD, PI, PI, PD, PD, C.c_int, PI, PD, PI, C.c_int,
+                                   PI, PD, PI]
+        L.orc_contact_hessian.argtypes = [C.c_int, PI, PI, C.c_int, PI, PD, PD]
+        L.orc_contact_hessian.restype = None
+        L.orc_repulsion.argtypes = [C.c_int, PI, PI, PD, PF, C.c_double, C.c_int, PI, PD,
+                                    C.c_int, PI, PD, PD]
+        L.orc_repulsion.restype = None
         L.orc_spmv.argtypes = [C.c_int, PI, PD, PD, PD]
         L.orc_spmv.restype = None
         L.orc_pcg.argtypes = [C.c_int, PI, PD, PD, PU8, PD, C.c_int, C.c_double, PD, C.c_int]
@@ -239,3 +249,68 @@ class OracleCloth:
         self.xpre = self.x.copy()
         self.x = self.x + dx
         return it, res
+
+
+# ---------------------------------------------------------------- collisions
+def body_normals(pos, tris):
+    """Triangle and vertex normals of a kinematic body as its Init leaves them."""
+    pos = np.ascontiguousarray(pos, np.float64)
+    tris = np.ascontiguousarray(tris, np.int32)
+    tn = np.zeros((tris.shape[0], 3))
+    vn = np.zeros((pos.shape[0], 3))
+    lib().orc_body_normals(pos.shape[0], tris.shape[0], _p(pos, C.c_double), _p(tris, C.c_int),
+                           _p(tn, C.c_double), _p(vn, C.c_double))
+    return tn, vn
+
+
+def contacts(mesh: dict, x, body: dict, max_pt=1 << 20, max_ee=1 << 20) -> dict:
+    """Contacts of the cloth (mesh, positions x) with a static body (pos,
+    tris, edges, tnormal, vnormal) in the collision detecter's order."""
+    x = np.ascontiguousarray(x, np.float64).reshape(-1)
+    tris = np.ascontiguousarray(mesh["tris"], np.int32)
+    edges = np.ascontiguousarray(mesh["edges"], np.int32)
+    bp = np.ascontiguousarray(body["pos"], np.float64)
+    bt = np.ascontiguousarray(body["tris"], np.int32)
+    be = np.ascontiguousarray(body["edges"], np.int32)
+    tn = np.ascontiguousarray(body["tnormal"], np.float64)
+    vn = np.ascontiguousarray(body["vnormal"], np.float64)
+    pt_i = np.zeros((max_pt, 3), np.int32)
+    pt_d = np.zeros((max_pt, 7))
+    ee_i = np.zeros((max_ee, 3), np.int32)
+    ee_d = np.zeros((max_ee, 6))
+    npt, nee = C.c_int(), C.c_int()
+    rc = lib().orc_contacts(x.size // 3, tris.shape[0], edges.shape[0], _p(x, C.c_double),
+                            _p(tris, C.c_int), _p(edges, C.c_int), bp.shape[0], bt.shape[0],
+                            be.shape[0], _p(bp, C.c_double), _p(bt, C.c_int), _p(be, C.c_int),
+                            _p(tn, C.c_double), _p(vn, C.c_double), max_pt, _p(pt_i, C.c_int),
+                            _p(pt_d, C.c_double), C.byref(npt), max_ee, _p(ee_i, C.c_int),
+                            _p(ee_d, C.c_double), C.byref(nee))
+    if rc != 0:
+        raise ValueError("oracle: contact list overflow")
+    return {"pt_i": pt_i[:npt.value].copy(), "pt_d": pt_d[:npt.value].copy(),
+            "ee_i": ee_i[:nee.value].copy(), "ee_d": ee_d[:nee.value].copy()}
+
+
+def contact_hessian(tab: dict, mesh: dict, con: dict) -> np.ndarray:
+    nv = tab["ell"].shape[0]
+    H = np.zeros((nv, W, 3, 3))
+    lib().orc_contact_hessian(nv, _p(np.ascontiguousarray(mesh["tris"], np.int32), C.c_int),
+                              _p(tab["ell"], C.c_int), con["pt_i"].shape[0],
+                              _p(np.ascontiguousarray(con["pt_i"]), C.c_int),
+                              _p(np.ascontiguousarray(con["pt_d"]), C.c_double),
+                              _p(H, C.c_double))
+    return H
+
+
+def repulsion(mesh: dict, mass, stretch_k, dt: float, con: dict, dx) -> np.ndarray:
+    out = np.array(dx, np.float64).reshape(-1).copy()
+    ks = np.asarray(stretch_k, np.float32)
+    lib().orc_repulsion(out.size // 3, _p(np.ascontiguousarray(mesh["tris"], np.int32), C.c_int),
+                        _p(np.ascontiguousarray(mesh["edges"], np.int32), C.c_int),
+                        _p(np.ascontiguousarray(mass, np.float64), C.c_double),
+                        _p(ks, C.c_float), float(dt), con["pt_i"].shape[0],
+                        _p(np.ascontiguousarray(con["pt_i"]), C.c_int),
+                        _p(np.ascontiguousarray(con["pt_d"]), C.c_double),
+                        con["ee_i"].shape[0], _p(np.ascontiguousarray(con["ee_i"]), C.c_int),
+                        _p(np.ascontiguousarray(con["ee_d"]), C.c_double), _p(out, C.c_double))
+    return out

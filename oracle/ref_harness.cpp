@@ -6,6 +6,9 @@
 //   topo   <cfg.json> <outdir>                     mesh, index maps, init-time data
 //   system <cfg.json> <x.bin> <xpre.bin> <outdir>  per-triangle f/H, bending, A, b, dx
 //   step   <cfg.json> <nsteps> [x.bin xpre.bin]    time the stock "fem" UpdatePos
+//   collide <cfg.json> <body.json> <x.bin> <dx.bin> <outdir>
+//                                                  contacts with one kinematic body,
+//                                                  contact Hessian, Repulsion
 //
 // Where the reference's GPU host code (src/sim/cloth/BaraffClothGpu.cpp) cannot
 // be compiled (it pulls in MSVC-only CUDA headers), the few lines of its init
@@ -16,6 +19,9 @@
 #include "sim/cloth/BaraffCloth.h"
 #include "sim/cloth/BaraffMaterial.h"
 #include "sim/cloth/DihedralBending.h"
+#include "sim/collision/BVHCollisionDetecter.h"
+#include "sim/collision/CollisionInfo.h"
+#include "sim/kinematic/KinematicBody.h"
 #include "sim/cloth/QBendingMaterial.h"
 #include "utils/JsonUtil.h"
 #include "utils/RotUtil.h"
@@ -497,6 +503,129 @@ struct Probe : public cBaraffCloth
         d.put("dx", "f8", dx, {n, 3});
     }
 
+    // The CPU cloth's collision handling against one kinematic body on the
+    // state x (cSimScene::PerformCollisionDetection, cBaraffCloth::
+    // PrepareCollisionHessian and Repulsion): the body's mesh and normals,
+    // the contacts cBVHCollisionDetecter finds, the contact Hessian as ELL
+    // blocks, and dx after Repulsion of the given dx.
+    void dump_collide(Dump &d, const Json::Value &kb_conf, std::vector<double> x,
+                      std::vector<double> dxin)
+    {
+        int n = nv();
+        auto kb = std::make_shared<cKinematicBody>(1);
+        kb->Init(kb_conf);
+        tVectorXd X = Eigen::Map<tVectorXd>(x.data(), 3 * n);
+        SetPos(X);
+        // cBaseCloth::Update refreshes the normals after every step
+        UpdateTriangleNormal();
+        UpdateVertexNormalFromTriangleNormal();
+        auto det = std::make_shared<cBVHCollisionDetecter>();
+        det->AddObject(shared_from_this(), false);
+        det->AddObject(kb, false);
+        det->Init();
+        det->PerformCD();
+        SetPointTriangleCollisionInfo(det->GetObjPointTriangleCollisionInfo(0));
+        SetEdgeEdgeCollisionInfo(det->GetObjEdgeEdgeCollisionInfo(0));
+
+        // the body
+        const auto &kv = kb->GetVertexArray();
+        const auto &kt = kb->GetTriangleArray();
+        const auto &ke = kb->GetEdgeArray();
+        std::vector<double> kpos, ktn, kvn;
+        std::vector<int> ktri, kedge;
+        for (auto &v : kv)
+            for (int k = 0; k < 3; k++)
+            {
+                kpos.push_back(v->mPos[k]);
+                kvn.push_back(v->mNormal[k]);
+            }
+        for (auto &t : kt)
+        {
+            ktri.push_back(t->mId0);
+            ktri.push_back(t->mId1);
+            ktri.push_back(t->mId2);
+            for (int k = 0; k < 3; k++)
+                ktn.push_back(t->mNormal[k]);
+        }
+        for (auto &e : ke)
+        {
+            kedge.push_back(e->mId0);
+            kedge.push_back(e->mId1);
+            kedge.push_back(e->mTriangleId0);
+            kedge.push_back(e->mIsBoundary ? -1 : e->mTriangleId1);
+        }
+        long nkv = long(kv.size()), nkt = long(kt.size()), nke = long(ke.size());
+        d.put("kb_pos", "f8", kpos, {nkv, 3});
+        d.put("kb_vnormal", "f8", kvn, {nkv, 3});
+        d.put("kb_tris", "i4", ktri, {nkt, 3});
+        d.put("kb_tnormal", "f8", ktn, {nkt, 3});
+        d.put("kb_edges", "i4", kedge, {nke, 4});
+
+        // contacts, in the detecter's order
+        std::vector<int> pt_i;      // obj0_is_cloth, vertex id, triangle id
+        std::vector<double> pt_d;   // normal xyz, depth, bary xyz
+        for (auto &c : mPointTriangleCollisionInfo)
+        {
+            pt_i.push_back(c->obj0_is_cloth_obj1_is_rb ? 1 : 0);
+            pt_i.push_back(c->mVertexId0);
+            pt_i.push_back(c->mTriangleId1);
+            for (int k = 0; k < 3; k++)
+                pt_d.push_back(c->mOuterNormal[k]);
+            pt_d.push_back(double(c->mDepth));
+            for (int k = 0; k < 3; k++)
+                pt_d.push_back(c->mBary[k]);
+        }
+        std::vector<int> ee_i;      // obj0_is_cloth, edge 0, edge 1
+        std::vector<double> ee_d;   // normal xyz, depth, bary0, bary1
+        for (auto &c : mEdgeEdgeCollisionInfo)
+        {
+            ee_i.push_back(c->obj0_is_cloth_obj1_is_rb ? 1 : 0);
+            ee_i.push_back(c->mEdgeId0);
+            ee_i.push_back(c->mEdgeId1);
+            for (int k = 0; k < 3; k++)
+                ee_d.push_back(c->mOuterNormal[k]);
+            ee_d.push_back(double(c->mDepth));
+            ee_d.push_back(double(c->mBary0));
+            ee_d.push_back(double(c->mBary1));
+        }
+        long npt = long(mPointTriangleCollisionInfo.size()),
+             nee = long(mEdgeEdgeCollisionInfo.size());
+        d.put("pt_i", "i4", pt_i, {npt, 3});
+        d.put("pt_d", "f8", pt_d, {npt, 7});
+        d.put("ee_i", "i4", ee_i, {nee, 3});
+        d.put("ee_d", "f8", ee_d, {nee, 6});
+
+        // contact Hessian as ELL blocks
+        tSparseMatd H = PrepareCollisionHessian();
+        std::vector<int> ellmap = ell();
+        std::vector<double> Hb(size_t(n) * kEll * 9, 0.0);
+        for (int i = 0; i < n; i++)
+            for (int s = 0; s < kEll; s++)
+            {
+                int j = ellmap[size_t(i) * kEll + s];
+                if (j < 0)
+                    break;
+                for (int r = 0; r < 3; r++)
+                    for (int c = 0; c < 3; c++)
+                        Hb[(size_t(i) * kEll + s) * 9 + r * 3 + c] =
+                            H.coeff(3 * i + r, 3 * j + c);
+            }
+        d.put("col_H", "f8", Hb, {n, kEll, 3, 3});
+
+        // Repulsion on the given dx
+        double dt = cJsonUtil::ParseAsDouble("default_timestep", conf);
+        tVectorXd DX = Eigen::Map<tVectorXd>(dxin.data(), 3 * n);
+        Repulsion(dt, DX);
+        std::vector<double> dxo(DX.data(), DX.data() + 3 * n), xs(x);
+        d.put("x", "f8", xs, {n, 3});
+        d.put("dx_in", "f8", dxin, {n, 3});
+        d.put("dx_out", "f8", dxo, {n, 3});
+        std::vector<double> mass_cpu(n);
+        for (int i = 0; i < n; i++)
+            mass_cpu[i] = mMassMatrixDiag[3 * i];
+        d.put("mass_cpu", "f8", mass_cpu, {n});
+    }
+
     void step(int nsteps)
     {
         double dt = cJsonUtil::ParseAsDouble("default_timestep", conf);
@@ -534,6 +663,15 @@ int main(int argc, char **argv)
         size_t n3 = size_t(c->nv()) * 3;
         Dump d(argv[5]);
         c->dump_system(d, read_doubles(argv[3], n3), read_doubles(argv[4], n3));
+    }
+    else if (mode == "collide" && argc >= 7)
+    {
+        Json::Value kb;
+        if (!cJsonUtil::LoadJson(argv[3], kb))
+            return 1;
+        size_t n3 = size_t(c->nv()) * 3;
+        Dump d(argv[6]);
+        c->dump_collide(d, kb, read_doubles(argv[4], n3), read_doubles(argv[5], n3));
     }
     else if (mode == "step" && argc >= 4)
     {

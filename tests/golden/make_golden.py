@@ -139,6 +139,44 @@ def irregular_obj(path: Path, seed: int = 17, nx: int = 8, ny: int = 10) -> None
             f.write("f " + " ".join(f"{perm[k] + 1}/{vt_of[perm[k]] + 1}" for k in fc) + "\n")
 
 
+# Collisions of the CPU cloth with one kinematic body (cBVHCollisionDetecter,
+# cBaraffCloth::PrepareCollisionHessian and Repulsion) on the grid20 state:
+# (name, cloth case whose config and state are used, kinematic body config).
+# "patch.obj" is written by contact_patch() below.
+COLLIDE_CASES = [
+    # a gently curved patch 1.5 mm in front of the cloth, normals towards it:
+    # cloth points near its triangles, its points near cloth triangles, and
+    # edge pairs all come within the 3 mm contact distance
+    ("col_patch", "grid20",
+     {"object_name": "patch", "object_type": "KinematicBody", "type": "custom",
+      "mesh_path": "patch.obj", "target_aabb": [0, 0, 0, 0], "scale": [1, 1, 1, 0],
+      "translation": [0, 0, 0, 0], "orientation": [0, 0, 0, 0]}),
+    # the reference's plane body (2 m square, two triangles) 1.5 mm in front
+    ("col_plane", "grid20",
+     {"object_name": "plane", "object_type": "KinematicBody", "type": "plane",
+      "equation": [0, 0, 1, -0.0015], "plane_scale": 1.0}),
+]
+
+
+def contact_patch(path: Path, n: int = 12) -> None:
+    """A curved n x n patch over x, y in [-0.35, 0.3] x [-0.25, 0.35] at
+    z = 1.5 mm + 0.04 r^2, triangle normals facing -z."""
+    xs = np.linspace(-0.35, 0.3, n + 1)
+    ys = np.linspace(-0.25, 0.35, n + 1)
+    with open(path, "w") as f:
+        f.write("# curved contact patch (tests/golden/make_golden.py)\n")
+        for y in ys:
+            for x in xs:
+                z = 0.0015 + 0.04 * ((x + 0.02) ** 2 + (y - 0.05) ** 2)
+                f.write(f"v {x:.6f} {y:.6f} {z:.6f}\n")
+        idx = lambda i, j: j * (n + 1) + i + 1
+        for j in range(n):
+            for i in range(n):
+                a, b, c, d = idx(i, j), idx(i + 1, j), idx(i + 1, j + 1), idx(i, j + 1)
+                # (v1 - v0) x (v2 - v1) along -z
+                f.write(f"f {a} {c} {b}\nf {a} {d} {c}\n")
+
+
 def read_dump(d: Path) -> dict:
     out = {}
     for line in (d / "manifest.txt").read_text().splitlines():
@@ -194,6 +232,32 @@ def main() -> None:
         arrays["config_json"] = np.frombuffer(json.dumps(conf).encode(), np.uint8)
         np.savez_compressed(OUT / f"{name}.npz", **arrays)
         print(name, "nv", pos.shape[0], "->", OUT / f"{name}.npz")
+    for name, cloth_case, kb in COLLIDE_CASES:
+        if a.only and name not in a.only:
+            continue
+        g = np.load(OUT / f"{cloth_case}.npz")
+        conf = json.loads(bytes(g["config_json"]).decode())
+        run_kb = dict(kb)
+        if kb.get("type") == "custom":
+            contact_patch(OUT / kb["mesh_path"])
+            run_kb["mesh_path"] = str(OUT / kb["mesh_path"])
+        with tempfile.TemporaryDirectory() as td:
+            td = Path(td)
+            (td / "cfg.json").write_text(json.dumps(conf))
+            (td / "kb.json").write_text(json.dumps(run_kb))
+            g["x_in"].astype(np.float64).tofile(td / "x.bin")
+            g["sys_dx"].astype(np.float64).tofile(td / "dx.bin")
+            (td / "col").mkdir()
+            subprocess.run([str(harness), "collide", str(td / "cfg.json"), str(td / "kb.json"),
+                            str(td / "x.bin"), str(td / "dx.bin"), str(td / "col")],
+                           check=True, stdout=subprocess.DEVNULL)
+            cold = read_dump(td / "col")
+        arrays = {f"col_{k}": v for k, v in cold.items()}
+        arrays["config_json"] = np.frombuffer(json.dumps(conf).encode(), np.uint8)
+        arrays["body_json"] = np.frombuffer(json.dumps(kb).encode(), np.uint8)
+        np.savez_compressed(OUT / f"{name}.npz", **arrays)
+        print(name, "contacts pt", cold["pt_i"].shape[0], "ee", cold["ee_i"].shape[0], "->",
+              OUT / f"{name}.npz")
 
 
 if __name__ == "__main__":

@@ -182,3 +182,45 @@ def test_dihedral_gradient_is_the_derivative_of_beta(orc):
             db = (db + np.pi) % (2 * np.pi) - np.pi  # across the +-pi cut
             num[k] = db / (2 * h)
         assert np.allclose(d["grad"].reshape(-1), num, rtol=1e-5, atol=1e-6 * np.abs(num).max())
+
+
+# ---------------------------------------------------------------- collisions
+# The CPU cloth's contacts with a kinematic body, its contact Hessian and its
+# Repulsion, as the reference's cBVHCollisionDetecter and cBaraffCloth write
+# them on the grid20 state (oracle/ref_harness.cpp "collide").
+
+COLLIDE_CASES = ["col_patch", "col_plane"]
+
+
+def load_collide(case):
+    import json
+    from conftest import GOLDEN
+    c = np.load(GOLDEN / f"{case}.npz")
+    return c, json.loads(bytes(c["config_json"]).decode())
+
+
+@pytest.mark.parametrize("case", COLLIDE_CASES)
+def test_contacts_match_reference(orc, case):
+    c, conf = load_collide(case)
+    m = _mesh(orc, conf)
+    tn, vn = orc.body_normals(c["col_kb_pos"], c["col_kb_tris"])
+    assert np.abs(tn - c["col_kb_tnormal"]).max() < 1e-15
+    assert np.abs(vn - c["col_kb_vnormal"]).max() < 1e-15
+    body = {"pos": c["col_kb_pos"], "tris": c["col_kb_tris"], "edges": c["col_kb_edges"],
+            "tnormal": tn, "vnormal": vn}
+    con = orc.contacts(m, c["col_x"], body)
+    # the same contacts in the same order; normals, depths and barycentric
+    # coordinates to the last bits
+    assert np.array_equal(con["pt_i"], c["col_pt_i"])
+    assert np.array_equal(con["ee_i"], c["col_ee_i"])
+    assert np.abs(con["pt_d"] - c["col_pt_d"]).max() < 1e-15
+    assert np.abs(con["ee_d"] - c["col_ee_d"]).max() < 1e-15
+    assert len(con["pt_i"]) > 50 and len(con["ee_i"]) > 50
+    tab = orc.tables(m, conf["cloth_density"], conf["cloth_bending_stiffness"])
+    H = orc.contact_hessian(tab, m, con)
+    assert rel(H, c["col_col_H"]) < 1e-15
+    dxo = orc.repulsion(m, c["col_mass_cpu"], conf["cloth_stretch_stiffness"],
+                        conf["default_timestep"], con, c["col_dx_in"])
+    d_ref = (c["col_dx_out"] - c["col_dx_in"]).reshape(-1)
+    assert np.abs(d_ref).max() > 0
+    assert rel(dxo - c["col_dx_in"].reshape(-1), d_ref) < 1e-13
