@@ -6,9 +6,9 @@ Python mirror of the reference's cloth API.
 """
 from . import _native
 from ._native import ClothError, REFERENCE_PARAMS, SolveParams, params
-from .cloth import BaraffClothGpu, ClothContext, ClothServer, build_grid, load_obj_mesh
+from .cloth import BaraffClothGpu, ClothBody, ClothContext, ClothServer, build_grid, load_obj_mesh
 
-__all__ = ["BaraffClothGpu", "ClothContext", "ClothError", "ClothServer", "REFERENCE_PARAMS", "SolveParams",
+__all__ = ["BaraffClothGpu", "ClothBody", "ClothContext", "ClothError", "ClothServer", "REFERENCE_PARAMS", "SolveParams",
            "build_grid", "load_obj_mesh", "params", "load_library"]
 
 

@@ -16,6 +16,7 @@ CLOTH_OK = 0
 STATUS_NAMES = {
     0: "OK", 1: "INVALID", 2: "CUDA", 3: "OOM", 4: "BUDGET", 5: "MESH", 6: "NAN",
     7: "BREAKDOWN", 8: "MAXITER", 9: "TIMEOUT", 10: "UNSUPPORTED", 11: "STATE",
+    12: "CONTACTS",
 }
 NUM_PHASES = 6
 PHASE_NAMES = ["pins", "tri_assemble", "row_assemble", "spmv_dot", "update_dot", "advance"]
@@ -47,6 +48,11 @@ class Material(C.Structure):
 
 
 BENDING_MODELS = {"quadratic": 0, "dihedral": 1}
+
+
+class ContactStats(C.Structure):
+    _fields_ = [("n_pt", C.c_int), ("n_ee", C.c_int), ("overflow", C.c_int),
+                ("repulsion_rounds", C.c_int)]
 
 
 class SolveParams(C.Structure):
@@ -164,6 +170,12 @@ SIGNATURES = {
     "cloth_export_system": (C.c_int, [P, PI, PF, PF, PF, PF]),
     "cloth_export_triangles": (C.c_int, [P, PF, PF]),
     "cloth_export_dihedral": (C.c_int, [P, PI, PI, PF, PF]),
+    "cloth_body_create": (C.c_int, [P, C.c_int, C.c_int, PD, PI, C.POINTER(P)]),
+    "cloth_body_destroy": (C.c_int, [P]),
+    "cloth_set_bodies": (C.c_int, [P, C.POINTER(P), C.c_int]),
+    "cloth_set_contact_capacity": (C.c_int, [P, C.c_int, C.c_int, C.c_int]),
+    "cloth_get_contacts": (C.c_int, [P, C.POINTER(ContactStats), PI, PD, PI, PD]),
+    "cloth_get_repulsed_dx": (C.c_int, [P, PD, C.c_int]),
     "cloth_export_tables": (C.c_int, [P, PI, PF, PF, PF, PI]),
     "cloth_step_plain": (C.c_int, [P, C.c_double, C.POINTER(SolveParams), C.POINTER(SolveStats)]),
     "cloth_batch_step": (C.c_int, [P, C.POINTER(P), C.c_int, C.c_double,

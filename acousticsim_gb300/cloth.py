@@ -23,6 +23,7 @@ class ClothContext:
         self._h = C.c_void_p()
         self._cloths = weakref.WeakSet()
         self._servers = weakref.WeakSet()
+        self._bodies = weakref.WeakSet()
         N.call("cloth_ctx_create", int(device), C.byref(self._h))
 
     @property
@@ -99,7 +100,7 @@ class ClothContext:
 
     def close(self) -> None:
         # the context frees every server and cloth it holds; their handles die with it
-        for c in list(self._cloths) + list(self._servers):
+        for c in list(self._cloths) + list(self._servers) + list(self._bodies):
             c._h = C.c_void_p()
         if self._h:
             N.load().cloth_ctx_destroy(self._h)
@@ -398,6 +399,37 @@ class BaraffClothGpu:
                N.ptr(g, C.c_float), N.ptr(cf, C.c_float))
         return {"edge_ids": ids, "grad": g, "factor": cf[:, 0], "force_coef": cf[:, 1]}
 
+    # ---------------------------------------------------------------- collisions
+    def set_bodies(self, bodies) -> None:
+        """Kinematic bodies this cloth collides with (the CPU cloth's contact
+        handling; an empty list turns it off)."""
+        bodies = list(bodies)
+        arr = (C.c_void_p * max(1, len(bodies)))(*[b.handle for b in bodies])
+        N.call("cloth_set_bodies", self._h, arr, len(bodies))
+        self._bodies = bodies
+
+    def set_contact_capacity(self, pairs=0, point_triangle=0, edge_edge=0) -> None:
+        N.call("cloth_set_contact_capacity", self._h, int(pairs), int(point_triangle),
+               int(edge_edge))
+
+    def get_contacts(self) -> dict:
+        """Contacts of the last step in the collision detecter's order."""
+        st = N.ContactStats()
+        N.call("cloth_get_contacts", self._h, C.byref(st), None, None, None, None)
+        pt_i = np.zeros((st.n_pt, 3), np.int32)
+        pt_d = np.zeros((st.n_pt, 7), np.float64)
+        ee_i = np.zeros((st.n_ee, 3), np.int32)
+        ee_d = np.zeros((st.n_ee, 6), np.float64)
+        N.call("cloth_get_contacts", self._h, C.byref(st), N.ptr(pt_i, C.c_int),
+               N.ptr(pt_d, C.c_double), N.ptr(ee_i, C.c_int), N.ptr(ee_d, C.c_double))
+        return {"pt_i": pt_i, "pt_d": pt_d, "ee_i": ee_i, "ee_d": ee_d,
+                "overflow": st.overflow, "repulsion_rounds": st.repulsion_rounds}
+
+    def get_repulsed_dx(self) -> np.ndarray:
+        dx = np.zeros(self.nv * 3, np.float64)
+        N.call("cloth_get_repulsed_dx", self._h, N.ptr(dx, C.c_double), self.nv)
+        return dx
+
     def export_tables(self) -> dict:
         ne = C.c_int()
         N.call("cloth_num_vertices", self._h, None, None, C.byref(ne))
@@ -420,6 +452,29 @@ class BaraffClothGpu:
             self.close()
         except Exception:
             pass
+
+
+class ClothBody:
+    """A static kinematic body (cKinematicBody after Init): a world-space
+    triangle mesh the cloths of a context can collide with."""
+
+    def __init__(self, ctx: ClothContext, pos, tris):
+        self.ctx = ctx
+        pos = np.ascontiguousarray(pos, np.float64).reshape(-1, 3)
+        tris = np.ascontiguousarray(tris, np.int32).reshape(-1, 3)
+        self._h = C.c_void_p()
+        N.call("cloth_body_create", ctx.handle, pos.shape[0], tris.shape[0],
+               N.ptr(pos, C.c_double), N.ptr(tris, C.c_int), C.byref(self._h))
+        self.pos, self.tris = pos, tris
+        ctx._bodies.add(self)
+
+    @property
+    def handle(self):
+        return self._h
+
+    def close(self) -> None:
+        if self._h and N.load().cloth_body_destroy(self._h) == N.CLOTH_OK:
+            self._h = C.c_void_p()
 
 
 class ClothServer:

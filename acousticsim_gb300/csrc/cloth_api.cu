@@ -71,6 +71,8 @@ struct Batch
     // a member carries skew block parts (dihedral bending): the SpMV variants
     // that apply them
     bool skew = false;
+    // the (single) member collides with kinematic bodies
+    bool collide = false;
     const GraphLoopVariant &spmv_variant(int v) const
     {
         return (skew ? kSpmvSkewVariants : kSpmvVariants)[v];
@@ -435,6 +437,18 @@ int upload_tables(cloth_s *c)
 
 } // namespace
 
+void cloth::detail::drop_launch_sets(cloth_s *c)
+{
+    c->self.reset();
+    if (c->ctx->last_batch)
+        for (auto *m : c->ctx->last_batch->members)
+            if (m == c)
+            {
+                c->ctx->last_batch.reset();
+                break;
+            }
+}
+
 void cloth::detail::bind_scratch(const cloth_s *c, InstDesc &h, char *base)
 {
     const ScratchLayout &sl = c->sl;
@@ -641,7 +655,11 @@ int make_batch(cloth_ctx *ctx, const std::vector<cloth_s *> &members,
         for (int s = 0; s < c->tab.nt + c->tab.n_dih; s += kTile)
             tt.push_back(Tile{int(i), s, c->d_desc, c->d_state});
         b->skew = b->skew || c->h.Aw != nullptr;
+        b->collide = b->collide || !c->bodies.empty();
     }
+    if (b->collide && members.size() > 1)
+        return fail(CLOTH_ERR_UNSUPPORTED, "a cloth with kinematic bodies is stepped alone "
+                                           "(not in a batch)");
     b->n_rt = int(rt.size());
     b->n_tt = int(tt.size());
     Layout L;
@@ -993,6 +1011,13 @@ int launch_assemble(Batch *b)
         k_pins<<<std::max(1, std::min(ninst, 1024)), kTile, 0, s>>>(b->d_descs,
                                                                   b->d_inst, ninst, nullptr);
     }
+    if (b->collide)
+    {
+        PhaseTimer t(ctx, PH_TRI);
+        int rc = collide_detect(b->members[0]);
+        if (rc != CLOTH_OK)
+            return rc;
+    }
     {
         PhaseTimer t(ctx, PH_TRI);
         k_tri<<<b->grid_tri, kTile, 0, s>>>(b->d_descs, b->d_tt, b->d_ctl);
@@ -1065,6 +1090,12 @@ int launch_solve_host(Batch *b, int max_iters)
 int launch_advance(Batch *b)
 {
     PhaseTimer t(b->ctx, PH_ADVANCE);
+    if (b->collide)
+    {
+        int rc = collide_repulse(b->members[0]);
+        if (rc != CLOTH_OK)
+            return rc;
+    }
     k_advance<<<b->grid_row, kTile, 0, b->ctx->stream>>>(b->d_descs, b->d_rt, b->d_ctl, 0);
     CK(cudaGetLastError());
     return CLOTH_OK;
@@ -1088,6 +1119,15 @@ int read_stats(Batch *b, cloth_solve_stats *stats)
         o.solver = !b->persist_ok  ? CLOTH_SOLVER_GRAPH_LOOP
                    : b->persist_1b ? CLOTH_SOLVER_PERSISTENT_1B
                                    : CLOTH_SOLVER_PERSISTENT;
+        if (b->collide && o.status == CLOTH_OK)
+        {
+            cloth_contact_stats cs;
+            int rc = cloth_get_contacts(b->members[i], &cs, nullptr, nullptr, nullptr, nullptr);
+            if (rc != CLOTH_OK)
+                return rc;
+            if (cs.overflow)
+                o.status = CLOTH_ERR_CONTACTS;
+        }
     }
     return CLOTH_OK;
 }
@@ -1267,6 +1307,23 @@ int run_step(Batch *b, double dt, const cloth_solve_params *params,
         if (rc == CLOTH_OK)
             rc = launch_advance(b);
     }
+    else if (b->collide)
+    {
+        // contacts and repulsion around the solve: host-driven launches on
+        // the stream (the counts stay on the device)
+        rc = launch_assemble(b);
+        if (rc == CLOTH_OK && b->persist_ok)
+            rc = launch_persistent(b);
+        else if (rc == CLOTH_OK)
+        {
+            if (!b->solve_exec)
+                rc = build_graph(b, false, &b->solve_exec);
+            if (rc == CLOTH_OK && cudaGraphLaunch(b->solve_exec, ctx->stream) != cudaSuccess)
+                rc = fail(CLOTH_ERR_CUDA, "cudaGraphLaunch failed");
+        }
+        if (rc == CLOTH_OK)
+            rc = launch_advance(b);
+    }
     else if (!b->persist_ok && !b->tuned && ctx->autotune)
     {
         // first step of a graph-loop launch set: assemble, tune on the real
@@ -1374,6 +1431,7 @@ const char *cloth_status_string(int s)
     case CLOTH_ERR_TIMEOUT: return "device wait timed out";
     case CLOTH_ERR_UNSUPPORTED: return "unsupported";
     case CLOTH_ERR_STATE: return "call out of order";
+    case CLOTH_ERR_CONTACTS: return "contact lists exceeded their capacity";
     default: return "unknown status";
     }
 }
@@ -1438,6 +1496,7 @@ int cloth_ctx_destroy(cloth_ctx *ctx)
         {
             c->self.reset();
             f64_free(c);
+            collide_free(c);
             if (c->arena)
                 cudaFree(c->arena);
             if (c->scratch)
@@ -1445,6 +1504,7 @@ int cloth_ctx_destroy(cloth_ctx *ctx)
             delete c;
         }
         ctx->cloths.clear();
+        body_release_all(ctx);
         for (auto &p : ctx->ev_pending)
         {
             cudaEventDestroy(p.second.first);
@@ -1798,6 +1858,7 @@ int cloth_destroy(cloth_t *c)
             }
     c->self.reset();
     f64_free(c);
+    collide_free(c);
     if (c->arena)
         cudaFree(c->arena);
     if (c->scratch)

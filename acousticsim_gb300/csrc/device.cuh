@@ -40,6 +40,39 @@ struct __align__(16) HRec
     float4 h1; // 12 22 pad pad
 };
 
+// Contacts of a cloth with kinematic bodies (the CPU cloth's collision
+// handling, src/sim/collision/BVHCollisionDetecter.cpp and
+// src/sim/cloth/BaraffCloth.cpp:614-990).
+struct PtContact
+{
+    int cloth_point;  // 1: cloth point p against body triangle t; 0: body point p against cloth triangle t
+    int p, t;
+    float depth;      // (distance vector).normal, kept as float as the reference does
+    double n[3];      // outer normal
+    float bary[3];    // barycentric coordinates of the closest point on t
+    int pad;
+};
+struct EeContact
+{
+    int e0, e1;       // cloth edge, body edge
+    float s, t;       // closest-point parameters on e0 and e1
+    double n[3];
+    float depth;
+    int pad;
+};
+// Entries of the per-vertex contact lists: an edge-edge contact index, or a
+// point-triangle index with this bit set (so a sorted list runs in the
+// reference's repulsion order: edge-edge contacts first).
+constexpr int kPtTag = 0x40000000;
+struct CollideCounts
+{
+    int n_pt, n_ee;   // contacts so far
+    int overflow;     // a list exceeded its capacity (contacts lost)
+    int rounds;       // repulsion rounds run
+    int cap_inc;      // capacity of the per-vertex contact lists
+    int pad[3];
+};
+
 struct InstState
 {
     // FP64 PCG scalars
@@ -114,6 +147,12 @@ struct InstDesc
     float4 *A0;          // [slot - diag_slot][stride]: diagonal and upper blocks
     float2 *A1;
     float4 *Aw;          // skew part w of those blocks (block p = S p + w x p), or null
+    // contacts with kinematic bodies (all null without bodies)
+    const PtContact *cpt;
+    const int *cinc_off;  // nv+1 per-vertex contact list ranges
+    const int *cinc;      // per-vertex contact lists (sorted)
+    const CollideCounts *ccount;
+    double *dxr;          // nv*3: dx after the repulsion (FP64), used by the advance
     float4 *M0; // block-Jacobi inverse, symmetric: (00 01 02 11)
     float2 *M1; // (12 22)
     float4 *b;

@@ -108,6 +108,8 @@ struct Batch;
 
 struct cloth_server_s;
 struct cloth_f64_s;
+struct cloth_body_s;
+struct cloth_collide_s;
 
 struct cloth_ctx_s
 {
@@ -131,6 +133,7 @@ struct cloth_ctx_s
     size_t bytes = 0;
     std::vector<cloth_s *> cloths;
     std::vector<cloth_server_s *> servers;
+    std::vector<cloth_body_s *> bodies;
     std::unique_ptr<cloth::detail::Batch> last_batch;
     ~cloth_ctx_s();
 };
@@ -167,6 +170,9 @@ struct cloth_s
     cloth::PlainState *plain = nullptr;
     std::vector<double> plain_x, plain_xp;
     bool plain_host_valid = false;
+    // kinematic bodies this cloth collides with, and the collision work arrays
+    std::vector<cloth_body_s *> bodies;
+    cloth_collide_s *col = nullptr;
     ~cloth_s();
 };
 
@@ -195,6 +201,15 @@ int f64_get_dx(cloth_s *c, double *dx, int nv);
 bool server_busy(const cloth_server_s *s, const cloth_s *c);
 // Detach every cloth of a server and free it (context teardown).
 void server_teardown(cloth_server_s *s);
+// Collisions with kinematic bodies (collide.cu): contacts of the current
+// positions (after the pins, before the row pass), and the repulsion of dx
+// after the solve; both enqueue on the context's stream.
+int collide_detect(cloth_s *c);
+// Drops the launch sets (own and the context's last batch) built with c.
+void drop_launch_sets(cloth_s *c);
+int collide_repulse(cloth_s *c);
+void collide_free(cloth_s *c);
+void body_release_all(cloth_ctx *ctx);
 
 } // namespace detail
 } // namespace cloth

@@ -541,6 +541,7 @@ __global__ void __launch_bounds__(kTile) k_row(InstDesc *const *descs,
             const int len = info & 255, ds = (info >> 8) & 255;
             const float4 xv = d.x32[row];
             const bool fixv = xv.w != 0.f;
+            const int ncinc = d.ccount ? d.ccount->cap_inc : 0;
             const float m = d.mass[row];
             float3 f = make_float3(0, 0, 0);
             for (int k = d.fptr[row]; k < d.fptr[row + 1]; k++)
@@ -594,6 +595,57 @@ __global__ void __launch_bounds__(kTile) k_row(InstDesc *const *descs,
                     A[k] = d.c_stiff * K[k];
                 float4 Aw = make_float4(d.c_stiff * wv[0], d.c_stiff * wv[1], d.c_stiff * wv[2],
                                         0.f);
+                // contact Hessian (PrepareCollisionHessian, BaraffCloth.cpp:928-990):
+                // 1e-2 (w_i N)(w_j N)^T per point-triangle contact holding row
+                // and c, w = 1 at a cloth point, -b at a cloth triangle's
+                // vertices; added to the system matrix unscaled, formed
+                // symmetrically so both rows of a pair hold the same block
+                float Hc[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+                if (d.cinc_off)
+                    for (int k = d.cinc_off[row]; k < min(d.cinc_off[row + 1], ncinc); k++)
+                    {
+                        const int tag = d.cinc[k];
+                        if (!(tag & kPtTag))
+                            continue;
+                        const PtContact &pc = d.cpt[tag & ~kPtTag];
+                        double wi = 0.0, wj = 0.0;
+                        bool hit = false;
+                        if (pc.cloth_point)
+                        {
+                            if (c == row)
+                            {
+                                wi = wj = 1.0;
+                                hit = true;
+                            }
+                        }
+                        else
+                        {
+                            const int4 tv = d.tri[pc.t];
+                            const int vv[3] = {tv.x, tv.y, tv.z};
+#pragma unroll
+                            for (int q = 0; q < 3; q++)
+                            {
+                                if (vv[q] == row)
+                                    wi = -double(pc.bary[q]);
+                                if (vv[q] == c)
+                                {
+                                    wj = -double(pc.bary[q]);
+                                    hit = true;
+                                }
+                            }
+                        }
+                        if (!hit)
+                            continue;
+                        const double N[3] = {pc.n[0], pc.n[1], pc.n[2]};
+                        const int pa[6] = {0, 0, 0, 1, 1, 2}, pb[6] = {0, 1, 2, 1, 2, 2};
+#pragma unroll
+                        for (int q = 0; q < 6; q++)
+                        {
+                            const double u = (wi * N[pa[q]]) * (wj * N[pb[q]]);
+                            const double v = (wi * N[pb[q]]) * (wj * N[pa[q]]);
+                            Hc[q] += float(1e-2 * (0.5 * (u + v)));
+                        }
+                    }
                 bool zero = false;
                 if (s == ds)
                 {
@@ -603,7 +655,10 @@ __global__ void __launch_bounds__(kTile) k_row(InstDesc *const *descs,
                     A[5] += md;
 #pragma unroll
                     for (int k = 0; k < 6; k++)
+                    {
+                        A[k] += Hc[k];
                         ad[k] = A[k];
+                    }
                 }
                 else if (fixv || xc.w != 0.f)
                 {
@@ -612,6 +667,12 @@ __global__ void __launch_bounds__(kTile) k_row(InstDesc *const *descs,
                     for (int k = 0; k < 6; k++)
                         A[k] = 0.f;
                     Aw = make_float4(0.f, 0.f, 0.f, 0.f);
+                }
+                else
+                {
+#pragma unroll
+                    for (int k = 0; k < 6; k++)
+                        A[k] += Hc[k];
                 }
                 if (s >= ds)
                 {
@@ -2283,7 +2344,14 @@ __global__ void __launch_bounds__(kTile) k_advance(InstDesc *const *descs,
             continue;
         const float4 dxv = d.dx[row];
         double x[3];
-        const double dd[3] = {double(dxv.x), double(dxv.y), double(dxv.z)};
+        double dd[3] = {double(dxv.x), double(dxv.y), double(dxv.z)};
+        if (d.dxr)
+        {
+            // dx after the contacts' repulsion (FP64)
+            dd[0] = d.dxr[3 * size_t(row)];
+            dd[1] = d.dxr[3 * size_t(row) + 1];
+            dd[2] = d.dxr[3 * size_t(row) + 2];
+        }
 #pragma unroll
         for (int k = 0; k < 3; k++)
         {

@@ -712,6 +712,9 @@ int cloth_server_add(cloth_server *s, cloth_t *c, double dt, const cloth_solve_p
         return sfail(CLOTH_ERR_STATE, "cloth_server_add: the server is running");
     if (c->server)
         return sfail(CLOTH_ERR_STATE, "cloth_server_add: the cloth is held by a server");
+    if (!c->bodies.empty())
+        return sfail(CLOTH_ERR_UNSUPPORTED, "cloth_server_add: a cloth with kinematic bodies "
+                                            "is stepped alone");
     const int n = int(s->cl.size()) + 1;
     const int ntr = (c->tab.nv + kTile - 1) / kTile, ntt = (c->tab.nt + c->tab.n_dih + kTile - 1) / kTile;
     size_t max_scratch = c->sl.bytes;

@@ -38,7 +38,8 @@ enum cloth_status {
     CLOTH_ERR_MAXITER = 8,     /* solve stopped at max_iters above tolerance (per-instance status) */
     CLOTH_ERR_TIMEOUT = 9,     /* a bounded device wait gave up */
     CLOTH_ERR_UNSUPPORTED = 10,
-    CLOTH_ERR_STATE = 11       /* call out of order (e.g. solve before assemble) */
+    CLOTH_ERR_STATE = 11,      /* call out of order (e.g. solve before assemble) */
+    CLOTH_ERR_CONTACTS = 12    /* contact lists exceeded their capacity (cloth_set_contact_capacity) */
 };
 
 typedef struct cloth_ctx_s cloth_ctx;
@@ -337,6 +338,48 @@ int cloth_solve_refined(cloth_t *cloth, const cloth_solve_params *inner, double 
  * reductions) from dx = 0, for comparison; recurrence residual in stats. */
 int cloth_solve_fp64(cloth_t *cloth, const cloth_solve_params *params,
                      cloth_solve_stats *stats);
+
+/* ---------------------------------------------------------------- collisions */
+/* Static kinematic bodies (cKinematicBody after Init, src/sim/kinematic/
+ * KinematicBody.cpp:27-121): a world-space triangle mesh; edges numbered as
+ * cObjUtil::BuildEdge numbers them, triangle normals (v1-v0)x(v2-v1)
+ * normalised, vertex normals the init-area-weighted sum of theirs. */
+typedef struct cloth_body_s cloth_body;
+int cloth_body_create(cloth_ctx *ctx, int nv, int nt, const double *pos, const int *tris,
+                      cloth_body **out);
+/* Fails while a cloth still collides with the body. */
+int cloth_body_destroy(cloth_body *body);
+
+/* The CPU cloth's collision handling (cSimScene::PerformCollisionDetection
+ * with cBVHCollisionDetecter, src/sim/collision/BVHCollisionDetecter.cpp, and
+ * cBaraffCloth::PrepareCollisionHessian / Repulsion, src/sim/cloth/
+ * BaraffCloth.cpp:614-990) in this cloth's step, against the bodies in order
+ * (the cloth being the first object of the scene).  Each step: contacts of
+ * the positions the step starts from (triangle pairs whose 5 mm boxes meet;
+ * cloth points and body triangles, body points and cloth triangles, cloth and
+ * body edges closer than 3 mm, in the detecter's order); 1e-2 dC/dx dC/dx^T
+ * per point-triangle contact added to the system matrix; after the solve the
+ * contacts' impulses on dx (edge-edge contacts first, each seeing dx as the
+ * earlier ones left it).  n = 0 turns collisions off.  A cloth with bodies is
+ * stepped alone (not in a batch or by the request server). */
+int cloth_set_bodies(cloth_t *cloth, cloth_body *const *bodies, int n);
+/* Capacities of the triangle-pair, point-triangle and edge-edge lists (0:
+ * the default for the cloth's size).  A step whose contacts do not fit
+ * reports CLOTH_ERR_CONTACTS. */
+int cloth_set_contact_capacity(cloth_t *cloth, int pairs, int point_triangle, int edge_edge);
+typedef struct {
+    int n_pt, n_ee;          /* contacts of the last step */
+    int overflow;            /* a list ran out of capacity */
+    int repulsion_rounds;    /* rounds of the ordered repulsion */
+} cloth_contact_stats;
+/* Contacts of the last step in the detecter's order: pt_i (cloth point?,
+ * point id, triangle id) n_pt*3, pt_d (normal xyz, depth, barycentric xyz)
+ * n_pt*7, ee_i (1, cloth edge, body edge) n_ee*3, ee_d (normal xyz, depth,
+ * s, t) n_ee*6.  Any pointer may be NULL. */
+int cloth_get_contacts(cloth_t *cloth, cloth_contact_stats *stats, int *pt_i, double *pt_d,
+                       int *ee_i, double *ee_d);
+/* dx after the last step's repulsion (nv*3, FP64). */
+int cloth_get_repulsed_dx(cloth_t *cloth, double *dx, int nv);
 
 /* ---------------------------------------------------------------- batch */
 /* Many cloths of uneven sizes stepped together: one launch per phase covers

@@ -204,9 +204,13 @@ class OracleCloth:
     """FP64 CPU step of the GPU path (Q-bending, or the CPU cloth's dihedral
     bending with "cloth_bending_model": "dihedral"; block-Jacobi PCG, pins)."""
 
-    def __init__(self, mesh: dict, conf: dict, pins):
+    def __init__(self, mesh: dict, conf: dict, pins, bodies=None):
+        """bodies: static kinematic bodies (dicts with pos, tris, edges,
+        tnormal, vnormal) the cloth collides with, in scene order."""
         self.mesh = mesh
         self.conf = conf
+        self.bodies = list(bodies or [])
+        self.last_contacts = None
         self.tab = tables(mesh, conf["cloth_density"], conf["cloth_bending_stiffness"][:2])
         self.dihedral = conf.get("cloth_bending_model", "quadratic") == "dihedral"
         self.dfac = (dihedral_rest(mesh, conf["cloth_bending_stiffness"][0])
@@ -241,13 +245,41 @@ class OracleCloth:
                          bend=bend)
         return A, b, f, tf, th
 
+    def contacts(self) -> dict:
+        """Contacts with every body at the current positions, concatenated in
+        the detecter's order (point-triangle lists body by body; edge-edge
+        lists body by body)."""
+        parts = [contacts(self.mesh, self.x, bd) for bd in self.bodies]
+        return {k: np.concatenate([p[k] for p in parts]) for k in ("pt_i", "pt_d", "ee_i", "ee_d")}
+
     def step(self, dt=None, rel_tol=1e-10, max_iters=100000, threads=1):
+        c = self.conf
+        dt = c["default_timestep"] if dt is None else dt
         A, b, _, _, _ = self.system(dt)
+        con = None
+        if self.bodies:
+            # PrepareCollisionHessian added to the system matrix, then the pin
+            # projection of the GPU solver again
+            con = self.contacts()
+            A = A + contact_hessian(self.tab, self.mesh, con)
+            ell = self.tab["ell"]
+            for v in range(ell.shape[0]):
+                for s_ in range(ell.shape[1]):
+                    col = ell[v, s_]
+                    if col < 0:
+                        break
+                    if col != v and (self.fixed[v] or self.fixed[col]):
+                        A[v, s_] = 0
         dx, it, res = pcg(self.tab["ell"], A, b, self.fixed, self.dx, max_iters, rel_tol,
                           threads)
         self.dx = dx
+        step_dx = dx
+        if con is not None:
+            step_dx = repulsion(self.mesh, self.tab["mass"], c["cloth_stretch_stiffness"][:3], dt,
+                                con, dx)
+        self.last_contacts = con
         self.xpre = self.x.copy()
-        self.x = self.x + dx
+        self.x = self.x + step_dx
         return it, res
 
 
