@@ -25,6 +25,7 @@
 #include "internal.h"
 
 #include <algorithm>
+#include <climits>
 #include <cmath>
 #include <cstring>
 #include <map>
@@ -418,6 +419,46 @@ __global__ void k_col_bt_sort(int bnt, const int *bt_off, int *bt, int cap)
     }
 }
 
+// Ascending unique values of a union of sorted segments [b_i, e_i) of one
+// array (a k-way merge; no copy of the candidates is kept).
+constexpr int kMaxLists = 64;
+struct MergeIter
+{
+    const int *a;
+    int cur[kMaxLists], end[kMaxLists];
+    int n;
+    __device__ void init(const int *arr)
+    {
+        a = arr;
+        n = 0;
+    }
+    __device__ bool add(int b, int e)
+    {
+        if (b >= e)
+            return true;
+        if (n >= kMaxLists)
+            return false;
+        cur[n] = b;
+        end[n] = e;
+        n++;
+        return true;
+    }
+    __device__ bool next(int &v)
+    {
+        int m = INT_MAX;
+        for (int i = 0; i < n; i++)
+            if (cur[i] < end[i] && a[cur[i]] < m)
+                m = a[cur[i]];
+        if (m == INT_MAX)
+            return false;
+        for (int i = 0; i < n; i++)
+            while (cur[i] < end[i] && a[cur[i]] == m)
+                cur[i]++;
+        v = m;
+        return true;
+    }
+};
+
 // 3a. cloth point p against body triangles (BVHCollisionDetecter.cpp:420-500,
 //     obj0 = cloth).  write = 0 counts into cntv[p]; write = 1 stores the
 //     contacts at cnt->n_pt + cntv[p] (exclusive offsets).
@@ -425,25 +466,24 @@ __global__ void k_col_pt_cloth(BodyView b, int nv, const double *x, const int *v
                                const int *vt, const int *tp_off, const int *tp, int cap_pairs,
                                int *cntv, PtContact *out, int cap, int write, CollideCounts *cnt)
 {
-    int cand[kLocalCand];
     for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < nv; p += gridDim.x * blockDim.x)
     {
-        int nc = 0;
-        bool full = false;
+        MergeIter it;
+        it.init(tp);
+        bool ok = true;
         for (int k = vt_off[p]; k < vt_off[p + 1]; k++)
         {
             const int T = vt[k];
-            for (int j = tp_off[T]; j < min(tp_off[T + 1], cap_pairs); j++)
-                full |= !insert_sorted(cand, nc, tp[j]);
+            ok &= it.add(min(tp_off[T], cap_pairs), min(tp_off[T + 1], cap_pairs));
         }
-        if (full)
+        if (!ok)
             atomicExch(&cnt->overflow, 1);
         const V3 pt = ld3(x + 3 * size_t(p));
         int n = 0;
         const int base = write ? cnt->n_pt + cntv[p] : 0;
-        for (int i = 0; i < nc; i++)
+        int t;
+        while (it.next(t))
         {
-            const int t = cand[i];
             const int *tv = b.tris + 3 * size_t(t);
             float bary[3];
             const V3 q = closest_pt_tri(pt, ld3(b.pos + 3 * size_t(tv[0])),
@@ -487,26 +527,25 @@ __global__ void k_col_pt_body(BodyView b, const double *x, const int4 *tri, cons
                               const int *bt_off, const int *bt, int cap_pairs, int *cntv,
                               PtContact *out, int cap, int write, CollideCounts *cnt)
 {
-    int cand[kLocalCand];
     for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < b.nv; q += gridDim.x * blockDim.x)
     {
-        int nc = 0;
-        bool full = false;
+        MergeIter it;
+        it.init(bt);
+        bool ok = true;
         for (int k = b.vt_off[q]; k < b.vt_off[q + 1]; k++)
         {
             const int t = b.vt[k];
-            for (int j = min(bt_off[t], cap_pairs); j < min(bt_off[t + 1], cap_pairs); j++)
-                full |= !insert_sorted(cand, nc, bt[j]);
+            ok &= it.add(min(bt_off[t], cap_pairs), min(bt_off[t + 1], cap_pairs));
         }
-        if (full)
+        if (!ok)
             atomicExch(&cnt->overflow, 1);
         const V3 pt = ld3(b.pos + 3 * size_t(q));
         const V3 rbn = ld3(b.vn + 3 * size_t(q));
         int n = 0;
         const int base = write ? cnt->n_pt + cntv[q] : 0;
-        for (int i = 0; i < nc; i++)
+        int T;
+        while (it.next(T))
         {
-            const int T = cand[i];
             const int4 tv = tri[T];
             float bary[3];
             const V3 c = closest_pt_tri(pt, ld3(x + 3 * size_t(tv.x)), ld3(x + 3 * size_t(tv.y)),
@@ -545,6 +584,79 @@ __global__ void k_col_pt_body(BodyView b, const double *x, const int4 *tri, cons
     }
 }
 
+// The body edges of the body triangles paired with a cloth edge's (at most
+// two) triangles, ascending: from a sorted local list when they fit, else by
+// repeated minimum search (no bound, slower).
+struct EdgeCands
+{
+    int buf[kLocalCand];
+    int nbuf;
+    bool spilled;
+    int last;
+    int pos;
+    MergeIter m;
+    const int *tedge;
+    int seg_b[2], seg_e[2], nseg;
+    const int *tp;
+    __device__ void init(const int *tp_, const int *tedge_, int b0, int e0, int b1, int e1)
+    {
+        tp = tp_;
+        tedge = tedge_;
+        nseg = 0;
+        if (b0 < e0)
+        {
+            seg_b[nseg] = b0;
+            seg_e[nseg] = e0;
+            nseg++;
+        }
+        if (b1 < e1)
+        {
+            seg_b[nseg] = b1;
+            seg_e[nseg] = e1;
+            nseg++;
+        }
+        nbuf = 0;
+        spilled = false;
+        m.init(tp);
+        for (int i = 0; i < nseg; i++)
+            m.add(seg_b[i], seg_e[i]);
+        int t;
+        while (!spilled && m.next(t))
+            for (int k = 0; k < 3 && !spilled; k++)
+                spilled = !insert_sorted(buf, nbuf, tedge[3 * size_t(t) + k]);
+        pos = 0;
+        last = -1;
+    }
+    __device__ bool next(int &f)
+    {
+        if (!spilled)
+        {
+            if (pos >= nbuf)
+                return false;
+            f = buf[pos++];
+            return true;
+        }
+        int best = INT_MAX;
+        MergeIter mm;
+        mm.init(tp);
+        for (int i = 0; i < nseg; i++)
+            mm.add(seg_b[i], seg_e[i]);
+        int t;
+        while (mm.next(t))
+            for (int k = 0; k < 3; k++)
+            {
+                const int e = tedge[3 * size_t(t) + k];
+                if (e > last && e < best)
+                    best = e;
+            }
+        if (best == INT_MAX)
+            return false;
+        last = best;
+        f = best;
+        return true;
+    }
+};
+
 // 3c. cloth edge e against body edges (BVHCollisionDetecter.cpp:507-630,
 //     obj0 = cloth): the cross product of the edges, turned to the side of
 //     the body edge's triangle normals
@@ -552,32 +664,21 @@ __global__ void k_col_ee(BodyView b, int ne, const int *edges, const double *x,
                          const int *tp_off, const int *tp, int cap_pairs, int *cntv,
                          EeContact *out, int cap, int write, CollideCounts *cnt)
 {
-    int cand[kLocalCand];
     for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < ne; e += gridDim.x * blockDim.x)
     {
         const int v0 = edges[4 * size_t(e)], v1 = edges[4 * size_t(e) + 1];
-        int nc = 0;
-        bool full = false;
-        for (int s2 = 2; s2 <= 3; s2++)
-        {
-            const int T = edges[4 * size_t(e) + s2];
-            if (T < 0)
-                continue;
-            for (int j = tp_off[T]; j < min(tp_off[T + 1], cap_pairs); j++)
-            {
-                const int t = tp[j];
-                for (int k = 0; k < 3; k++)
-                    full |= !insert_sorted(cand, nc, b.tedge[3 * size_t(t) + k]);
-            }
-        }
-        if (full)
-            atomicExch(&cnt->overflow, 1);
+        const int T0 = edges[4 * size_t(e) + 2], T1 = edges[4 * size_t(e) + 3];
+        EdgeCands ec;
+        ec.init(tp, b.tedge, T0 >= 0 ? min(tp_off[T0], cap_pairs) : 0,
+                T0 >= 0 ? min(tp_off[T0 + 1], cap_pairs) : 0,
+                T1 >= 0 ? min(tp_off[T1], cap_pairs) : 0,
+                T1 >= 0 ? min(tp_off[T1 + 1], cap_pairs) : 0);
         const V3 p0 = ld3(x + 3 * size_t(v0)), p1 = ld3(x + 3 * size_t(v1));
         int n = 0;
         const int base = write ? cnt->n_ee + cntv[e] : 0;
-        for (int i = 0; i < nc; i++)
+        int f;
+        while (ec.next(f))
         {
-            const int f = cand[i];
             const int *fe = b.edges + 4 * size_t(f);
             const V3 p2 = ld3(b.pos + 3 * size_t(fe[0])), p3 = ld3(b.pos + 3 * size_t(fe[1]));
             float s, t;
