@@ -18,8 +18,9 @@ STATUS_NAMES = {
     7: "BREAKDOWN", 8: "MAXITER", 9: "TIMEOUT", 10: "UNSUPPORTED", 11: "STATE",
     12: "CONTACTS",
 }
-NUM_PHASES = 6
-PHASE_NAMES = ["pins", "tri_assemble", "row_assemble", "spmv_dot", "update_dot", "advance"]
+NUM_PHASES = 8
+PHASE_NAMES = ["pins", "tri_assemble", "row_assemble", "spmv_dot", "update_dot", "advance",
+               "contacts", "repulsion"]
 ELL_REF_WIDTH = 32
 SOLVER_PERSISTENT = 0
 SOLVER_GRAPH_LOOP = 1

@@ -147,6 +147,22 @@ def load_obj_mesh(path: str, translation=(0.0, 0.0, 0.0), relocate: bool = False
     return {"pos": pos, "uv": uv, "tris": tris, "edges": edges}
 
 
+def derive_edges_host(tris) -> np.ndarray:
+    """Edges (v0, v1, tri0, tri1) of a triangle list as cObjUtil::BuildEdge
+    numbers them (ascending vertex pairs; tri1 = -1 on the boundary)."""
+    tris = np.asarray(tris, np.int64).reshape(-1, 3)
+    info = {}
+    for t, tv in enumerate(tris):
+        for k in range(3):
+            a, b = int(tv[k]), int(tv[(k + 1) % 3])
+            key = (min(a, b), max(a, b))
+            if key in info:
+                info[key][1] = t
+            else:
+                info[key] = [t, -1]
+    return np.array([[k[0], k[1], v[0], v[1]] for k, v in sorted(info.items())], np.int32)
+
+
 def _vec(conf: dict, key: str, default=None):
     v = conf.get(key, default)
     if v is None:

@@ -36,7 +36,9 @@ enum Phase
     PH_ROW,
     PH_SPMV,
     PH_UPDATE,
-    PH_ADVANCE
+    PH_ADVANCE,
+    PH_COLLIDE,
+    PH_REPULSE
 };
 
 } // namespace
@@ -1013,7 +1015,7 @@ int launch_assemble(Batch *b)
     }
     if (b->collide)
     {
-        PhaseTimer t(ctx, PH_TRI);
+        PhaseTimer t(ctx, PH_COLLIDE);
         int rc = collide_detect(b->members[0]);
         if (rc != CLOTH_OK)
             return rc;
@@ -1089,13 +1091,14 @@ int launch_solve_host(Batch *b, int max_iters)
 
 int launch_advance(Batch *b)
 {
-    PhaseTimer t(b->ctx, PH_ADVANCE);
     if (b->collide)
     {
+        PhaseTimer t(b->ctx, PH_REPULSE);
         int rc = collide_repulse(b->members[0]);
         if (rc != CLOTH_OK)
             return rc;
     }
+    PhaseTimer t(b->ctx, PH_ADVANCE);
     k_advance<<<b->grid_row, kTile, 0, b->ctx->stream>>>(b->d_descs, b->d_rt, b->d_ctl, 0);
     CK(cudaGetLastError());
     return CLOTH_OK;

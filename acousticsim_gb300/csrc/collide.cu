@@ -80,7 +80,10 @@ struct cloth_collide_s
     PtContact *pt = nullptr;
     EeContact *ee = nullptr;
     int *inc_off = nullptr, *inc_cur = nullptr, *inc = nullptr;
-    int *rptr = nullptr, *cstate = nullptr;
+    int *rptr = nullptr, *cstate = nullptr, *wa = nullptr, *wb = nullptr;
+    int *tile_sum = nullptr;
+    int4 *cverts = nullptr;   // cloth vertices of every contact (and their count)
+    int4 *clpos = nullptr, *csucc = nullptr; // place in, and successor on, each vertex's list
     double *dxr = nullptr;
     CollideCounts *cnt = nullptr;
     int *vt_off = nullptr, *vt = nullptr; // cloth vertex -> triangles
@@ -345,31 +348,66 @@ __global__ void k_col_pairs(BodyView b, int nt, const double *lo, const double *
     }
 }
 
-// Exclusive scan of a[0..n) in place, a[n] = total (one block); the total is
-// also left in *total.
-__global__ void __launch_bounds__(1024) k_col_scan(int *a, int n, int *total)
+// Exclusive scan of a[0..n) in place, a[n] = total, *total = total: blocks
+// of kScanTile elements scan their tiles and leave their sums; one block
+// scans the sums; the blocks add their tile's offset.
+constexpr int kScanTile = 4096;
+constexpr int kScanMaxTiles = 4096; // n up to 16 M
+
+__global__ void __launch_bounds__(1024) k_col_scan_tiles(int *a, int n, int *tile_sum)
 {
     __shared__ int part[1024];
-    const int tid = threadIdx.x;
-    const int chunk = (n + 1023) / 1024;
-    const int b0 = min(n, tid * chunk), b1 = min(n, b0 + chunk);
-    int s = 0;
-    for (int i = b0; i < b1; i++)
-        s += a[i];
+    const int base = blockIdx.x * kScanTile, tid = threadIdx.x;
+    const int i0 = min(n, base + tid * 4), i1 = min(n, i0 + 4);
+    int v[4] = {0, 0, 0, 0}, s = 0;
+    for (int i = i0; i < i1; i++)
+    {
+        v[i - i0] = a[i];
+        s += v[i - i0];
+    }
     part[tid] = s;
     __syncthreads();
     for (int o = 1; o < 1024; o <<= 1)
     {
-        const int v = tid >= o ? part[tid - o] : 0;
+        const int u = tid >= o ? part[tid - o] : 0;
         __syncthreads();
-        part[tid] += v;
+        part[tid] += u;
         __syncthreads();
     }
     int run = part[tid] - s;
-    for (int i = b0; i < b1; i++)
+    for (int i = i0; i < i1; i++)
     {
-        const int v = a[i];
         a[i] = run;
+        run += v[i - i0];
+    }
+    if (tid == 1023)
+        tile_sum[blockIdx.x] = part[1023];
+}
+
+__global__ void __launch_bounds__(1024) k_col_scan_top(int *tile_sum, int ntiles, int *a, int n,
+                                                       int *total)
+{
+    __shared__ int part[1024];
+    const int tid = threadIdx.x;
+    const int per = (ntiles + 1023) / 1024;
+    const int t0 = min(ntiles, tid * per), t1 = min(ntiles, t0 + per);
+    int s = 0;
+    for (int t = t0; t < t1; t++)
+        s += tile_sum[t];
+    part[tid] = s;
+    __syncthreads();
+    for (int o = 1; o < 1024; o <<= 1)
+    {
+        const int u = tid >= o ? part[tid - o] : 0;
+        __syncthreads();
+        part[tid] += u;
+        __syncthreads();
+    }
+    int run = part[tid] - s;
+    for (int t = t0; t < t1; t++)
+    {
+        const int v = tile_sum[t];
+        tile_sum[t] = run;
         run += v;
     }
     if (tid == 1023)
@@ -378,6 +416,15 @@ __global__ void __launch_bounds__(1024) k_col_scan(int *a, int n, int *total)
         if (total)
             *total = part[1023];
     }
+}
+
+__global__ void k_col_scan_add(int *a, int n, const int *tile_sum)
+{
+    const int off = tile_sum[blockIdx.x];
+    const int base = blockIdx.x * kScanTile;
+    if (off)
+        for (int i = base + threadIdx.x; i < min(n, base + kScanTile); i += blockDim.x)
+            a[i] += off;
 }
 
 // pairs grouped by body triangle: counts, then ids at atomic cursors, then
@@ -400,25 +447,6 @@ __global__ void k_col_bt_fill(int nt, const int *tp_off, const int *tp, int cap,
                 bt[pos] = T;
         }
 }
-__global__ void k_col_bt_sort(int bnt, const int *bt_off, int *bt, int cap)
-{
-    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < bnt; t += gridDim.x * blockDim.x)
-    {
-        const int b0 = min(bt_off[t], cap), b1 = min(bt_off[t + 1], cap);
-        for (int i = b0 + 1; i < b1; i++)
-        {
-            const int v = bt[i];
-            int j = i;
-            while (j > b0 && bt[j - 1] > v)
-            {
-                bt[j] = bt[j - 1];
-                j--;
-            }
-            bt[j] = v;
-        }
-    }
-}
-
 // Ascending unique values of a union of sorted segments [b_i, e_i) of one
 // array (a k-way merge; no copy of the candidates is kept).
 constexpr int kMaxLists = 64;
@@ -458,6 +486,74 @@ struct MergeIter
         return true;
     }
 };
+
+constexpr int kSortCap = 8192;   // candidates a block sorts in shared memory
+constexpr int kSortBlock = 256;
+
+// ascending bitonic sort of s[0..P) (P a power of two) by one block
+__device__ void block_bitonic(int *s, int P)
+{
+    for (int k = 2; k <= P; k <<= 1)
+        for (int j = k >> 1; j > 0; j >>= 1)
+        {
+            for (int i = threadIdx.x; i < P; i += blockDim.x)
+            {
+                const int ixj = i ^ j;
+                if (ixj > i)
+                {
+                    const bool up = (i & k) == 0;
+                    const int a = s[i], b = s[ixj];
+                    if ((a > b) == up)
+                    {
+                        s[i] = b;
+                        s[ixj] = a;
+                    }
+                }
+            }
+            __syncthreads();
+        }
+}
+
+// each body triangle's list of cloth triangles, ascending: one block per
+// list, sorted in shared memory (by one thread beyond kSortCap)
+__global__ void __launch_bounds__(kSortBlock) k_col_bt_sort(int bnt, const int *bt_off, int *bt,
+                                                            int cap)
+{
+    __shared__ int sv[kSortCap];
+    for (int t = blockIdx.x; t < bnt; t += gridDim.x)
+    {
+        const int b0 = min(bt_off[t], cap), b1 = min(bt_off[t + 1], cap);
+        const int n = b1 - b0;
+        if (n <= 1)
+            continue;
+        if (n <= kSortCap)
+        {
+            int P = 1;
+            while (P < n)
+                P <<= 1;
+            for (int i = threadIdx.x; i < P; i += blockDim.x)
+                sv[i] = i < n ? bt[b0 + i] : INT_MAX;
+            __syncthreads();
+            block_bitonic(sv, P);
+            for (int i = threadIdx.x; i < n; i += blockDim.x)
+                bt[b0 + i] = sv[i];
+            __syncthreads();
+        }
+        else if (threadIdx.x == 0)
+            for (int i = b0 + 1; i < b1; i++)
+            {
+                const int v = bt[i];
+                int j = i;
+                while (j > b0 && bt[j - 1] > v)
+                {
+                    bt[j] = bt[j - 1];
+                    j--;
+                }
+                bt[j] = v;
+            }
+        __syncthreads();
+    }
+}
 
 // 3a. cloth point p against body triangles (BVHCollisionDetecter.cpp:420-500,
 //     obj0 = cloth).  write = 0 counts into cntv[p]; write = 1 stores the
@@ -522,65 +618,182 @@ __global__ void k_col_pt_cloth(BodyView b, int nv, const double *x, const int *v
 }
 
 // 3b. body point q against cloth triangles (obj0 = body): the cloth
-//     triangle's normal, turned to the body point's normal side
-__global__ void k_col_pt_body(BodyView b, const double *x, const int4 *tri, const double *ctn,
-                              const int *bt_off, const int *bt, int cap_pairs, int *cntv,
-                              PtContact *out, int cap, int write, CollideCounts *cnt)
+//     triangle's normal, turned to the body point's normal side.
+__device__ __forceinline__ bool pt_body_hit(const BodyView &b, const double *x, const int4 *tri,
+                                            const double *ctn, int q, int T, PtContact *o)
 {
-    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < b.nv; q += gridDim.x * blockDim.x)
+    const V3 pt = ld3(b.pos + 3 * size_t(q));
+    const int4 tv = tri[T];
+    float bary[3];
+    const V3 c = closest_pt_tri(pt, ld3(x + 3 * size_t(tv.x)), ld3(x + 3 * size_t(tv.y)),
+                                ld3(x + 3 * size_t(tv.z)), bary);
+    V3 nn = ld3(ctn + 3 * size_t(T));
+    if (dot3(nn, ld3(b.vn + 3 * size_t(q))) < 0)
+        nn = {-nn.x, -nn.y, -nn.z};
+    const V3 dv = sub3(c, pt);
+    if (!(sqrt(dot3(dv, dv)) < 3e-3))
+        return false;
+    if (o)
     {
-        MergeIter it;
-        it.init(bt);
-        bool ok = true;
-        for (int k = b.vt_off[q]; k < b.vt_off[q + 1]; k++)
+        o->cloth_point = 0;
+        o->p = q;
+        o->t = T;
+        o->depth = float(dot3(dv, nn));
+        o->n[0] = nn.x;
+        o->n[1] = nn.y;
+        o->n[2] = nn.z;
+        o->bary[0] = bary[0];
+        o->bary[1] = bary[1];
+        o->bary[2] = bary[2];
+        o->pad = 0;
+    }
+    return true;
+}
+
+// One block per body point: its candidate cloth triangles (the union of its
+// triangles' sorted lists) sorted in shared memory; each thread takes a
+// contiguous run of the sorted candidates, so a block prefix sum over the
+// threads' hit counts gives every contact its place in the detecter's
+// order.  Beyond kSortCap candidates one thread merges the lists instead.
+__global__ void __launch_bounds__(kSortBlock) k_col_pt_body(
+    BodyView b, const double *x, const int4 *tri, const double *ctn, const int *bt_off,
+    const int *bt, int cap_pairs, int *cntv, PtContact *out, int cap, int write,
+    CollideCounts *cnt)
+{
+    __shared__ int sv[kSortCap];
+    __shared__ int s_part[kSortBlock];
+    __shared__ int s_n;
+    for (int q = blockIdx.x; q < b.nv; q += gridDim.x)
+    {
+        if (threadIdx.x == 0)
         {
-            const int t = b.vt[k];
-            ok &= it.add(min(bt_off[t], cap_pairs), min(bt_off[t + 1], cap_pairs));
-        }
-        if (!ok)
-            atomicExch(&cnt->overflow, 1);
-        const V3 pt = ld3(b.pos + 3 * size_t(q));
-        const V3 rbn = ld3(b.vn + 3 * size_t(q));
-        int n = 0;
-        const int base = write ? cnt->n_pt + cntv[q] : 0;
-        int T;
-        while (it.next(T))
-        {
-            const int4 tv = tri[T];
-            float bary[3];
-            const V3 c = closest_pt_tri(pt, ld3(x + 3 * size_t(tv.x)), ld3(x + 3 * size_t(tv.y)),
-                                        ld3(x + 3 * size_t(tv.z)), bary);
-            V3 nn = ld3(ctn + 3 * size_t(T));
-            if (dot3(nn, rbn) < 0)
-                nn = {-nn.x, -nn.y, -nn.z};
-            const V3 dv = sub3(c, pt);
-            if (!(sqrt(dot3(dv, dv)) < 3e-3))
-                continue;
-            if (write)
+            int n = 0;
+            for (int k = b.vt_off[q]; k < b.vt_off[q + 1]; k++)
             {
-                if (base + n < cap)
+                const int t = b.vt[k];
+                n += min(bt_off[t + 1], cap_pairs) - min(bt_off[t], cap_pairs);
+            }
+            s_n = n;
+        }
+        __syncthreads();
+        const int n = s_n;
+        const int base = write ? cnt->n_pt + cntv[q] : 0;
+        if (n > kSortCap)
+        {
+            // serial merge of the lists
+            if (threadIdx.x == 0)
+            {
+                MergeIter it;
+                it.init(bt);
+                bool ok = true;
+                for (int k = b.vt_off[q]; k < b.vt_off[q + 1]; k++)
+                {
+                    const int t = b.vt[k];
+                    ok &= it.add(min(bt_off[t], cap_pairs), min(bt_off[t + 1], cap_pairs));
+                }
+                if (!ok)
+                    atomicExch(&cnt->overflow, 1);
+                int h = 0, T;
+                while (it.next(T))
                 {
                     PtContact o;
-                    o.cloth_point = 0;
-                    o.p = q;
-                    o.t = T;
-                    o.depth = float(dot3(dv, nn));
-                    o.n[0] = nn.x;
-                    o.n[1] = nn.y;
-                    o.n[2] = nn.z;
-                    o.bary[0] = bary[0];
-                    o.bary[1] = bary[1];
-                    o.bary[2] = bary[2];
-                    o.pad = 0;
-                    out[base + n] = o;
+                    if (!pt_body_hit(b, x, tri, ctn, q, T, write ? &o : nullptr))
+                        continue;
+                    if (write)
+                    {
+                        if (base + h < cap)
+                            out[base + h] = o;
+                        else
+                            atomicExch(&cnt->overflow, 1);
+                    }
+                    h++;
                 }
-                else
-                    atomicExch(&cnt->overflow, 1);
+                if (!write)
+                    cntv[q] = h;
             }
-            n++;
+            __syncthreads();
+            continue;
         }
-        if (!write)
-            cntv[q] = n;
+        if (n == 0)
+        {
+            if (!write && threadIdx.x == 0)
+                cntv[q] = 0;
+            __syncthreads();
+            continue;
+        }
+        int P = 1;
+        while (P < n)
+            P <<= 1;
+        // gather the lists: list k starts at s_part[k] of the candidates
+        const int nl = b.vt_off[q + 1] - b.vt_off[q];
+        if (threadIdx.x == 0)
+        {
+            int o = 0;
+            for (int k = 0; k < nl && k < kSortBlock; k++)
+            {
+                const int t = b.vt[b.vt_off[q] + k];
+                s_part[k] = o;
+                o += min(bt_off[t + 1], cap_pairs) - min(bt_off[t], cap_pairs);
+            }
+        }
+        __syncthreads();
+        if (nl <= kSortBlock)
+            for (int k = 0; k < nl; k++)
+            {
+                const int t = b.vt[b.vt_off[q] + k];
+                const int b0 = min(bt_off[t], cap_pairs), b1 = min(bt_off[t + 1], cap_pairs);
+                for (int i = b0 + threadIdx.x; i < b1; i += blockDim.x)
+                    sv[s_part[k] + (i - b0)] = bt[i];
+            }
+        else if (threadIdx.x == 0)
+        {
+            int o = 0;
+            for (int k = b.vt_off[q]; k < b.vt_off[q + 1]; k++)
+            {
+                const int t = b.vt[k];
+                for (int i = min(bt_off[t], cap_pairs); i < min(bt_off[t + 1], cap_pairs); i++)
+                    sv[o++] = bt[i];
+            }
+        }
+        for (int i = n + threadIdx.x; i < P; i += blockDim.x)
+            sv[i] = INT_MAX;
+        __syncthreads();
+        block_bitonic(sv, P);
+        // contiguous runs of the sorted candidates, duplicates skipped
+        const int per = (n + blockDim.x - 1) / blockDim.x;
+        const int i0 = min(n, int(threadIdx.x) * per), i1 = min(n, i0 + per);
+        int h = 0;
+        for (int i = i0; i < i1; i++)
+            if ((i == 0 || sv[i] != sv[i - 1]) && pt_body_hit(b, x, tri, ctn, q, sv[i], nullptr))
+                h++;
+        s_part[threadIdx.x] = h;
+        __syncthreads();
+        for (int o = 1; o < int(blockDim.x); o <<= 1)
+        {
+            const int v = threadIdx.x >= o ? s_part[threadIdx.x - o] : 0;
+            __syncthreads();
+            s_part[threadIdx.x] += v;
+            __syncthreads();
+        }
+        if (write)
+        {
+            int pos = base + s_part[threadIdx.x] - h;
+            for (int i = i0; i < i1; i++)
+            {
+                PtContact o;
+                if ((i == 0 || sv[i] != sv[i - 1]) && pt_body_hit(b, x, tri, ctn, q, sv[i], &o))
+                {
+                    if (pos < cap)
+                        out[pos] = o;
+                    else
+                        atomicExch(&cnt->overflow, 1);
+                    pos++;
+                }
+            }
+        }
+        else if (threadIdx.x == blockDim.x - 1)
+            cntv[q] = s_part[threadIdx.x];
+        __syncthreads();
     }
 }
 
@@ -767,7 +980,8 @@ __device__ __forceinline__ int contact_vertices(const CollideCounts *cnt, const 
 
 __global__ void k_col_inc(const CollideCounts *cnt, int cap_pt, int cap_ee, const PtContact *pt,
                           const EeContact *ee, const int *edges, const int4 *tri, int *inc_off,
-                          int *inc_cur, int *inc, int cap_inc, int fill, CollideCounts *cw)
+                          int *inc_cur, int *inc, int cap_inc, int fill, CollideCounts *cw,
+                          int4 *cverts)
 {
     CollideCounts c = *cnt;
     c.n_pt = min(c.n_pt, cap_pt);
@@ -775,8 +989,10 @@ __global__ void k_col_inc(const CollideCounts *cnt, int cap_pt, int cap_ee, cons
     const int n = c.n_pt + c.n_ee;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
     {
-        int v[3], tag;
+        int v[3] = {-1, -1, -1}, tag;
         const int m = contact_vertices(&c, pt, ee, edges, tri, i, v, &tag);
+        if (fill)
+            cverts[i] = make_int4(v[0], v[1], v[2], m);
         for (int k = 0; k < m; k++)
         {
             if (!fill)
@@ -812,6 +1028,49 @@ __global__ void k_col_inc_sort(int nv, const int *inc_off, int *inc, int cap_inc
     }
 }
 
+// For every contact and each of its vertices: its place in that vertex's
+// list (clpos) and the contact after it there (csucc, -1 at the end).
+__global__ void k_col_links(int nv, const CollideCounts *cnt, int cap_pt, int cap_ee,
+                            const int *inc_off, const int *inc, int cap_inc, const int4 *cverts,
+                            int4 *clpos, int4 *csucc)
+{
+    const int n_ee = min(cnt->n_ee, cap_ee);
+    for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < nv; v += gridDim.x * blockDim.x)
+    {
+        const int b0 = min(inc_off[v], cap_inc), b1 = min(inc_off[v + 1], cap_inc);
+        for (int j = b0; j < b1; j++)
+        {
+            const int tg = inc[j];
+            const int i = (tg & kPtTag) ? n_ee + (tg & ~kPtTag) : tg;
+            int nx = -1;
+            if (j + 1 < b1)
+            {
+                const int t2 = inc[j + 1];
+                nx = (t2 & kPtTag) ? n_ee + (t2 & ~kPtTag) : t2;
+            }
+            const int4 cv = cverts[i];
+            int *lp = reinterpret_cast<int *>(&clpos[i]);
+            int *sc = reinterpret_cast<int *>(&csucc[i]);
+            if (cv.x == v)
+            {
+                lp[0] = j - b0;
+                sc[0] = nx;
+            }
+            else if (cv.y == v)
+            {
+                lp[1] = j - b0;
+                sc[1] = nx;
+            }
+            else if (cv.z == v)
+            {
+                lp[2] = j - b0;
+                sc[2] = nx;
+            }
+        }
+    }
+    (void)cap_pt;
+}
+
 __global__ void k_col_dxr(int nv, const float4 *dx, double *dxr, int *rptr, int ncs,
                           int *cstate)
 {
@@ -828,147 +1087,173 @@ __global__ void k_col_dxr(int nv, const float4 *dx, double *dxr, int *rptr, int 
         cstate[i] = 0;
 }
 
+// One contact's impulse on dxr (BaraffCloth.cpp:636-925), v: its cloth vertices.
+__device__ void repulse_one(const CollideCounts &c, const PtContact *pt, const EeContact *ee,
+                            int i, const int *v, const double *mass, double *dxr, double dt,
+                            double K)
+{
+    const double v_thre = 0.01, scale = double(0.1f);
+    if (i < c.n_ee)
+    {
+        const EeContact &e = ee[i];
+        const float a = e.s, b = e.t, a1 = 1 - a;
+        const int v0 = v[0], v1 = v[1];
+        double vrel[3];
+        for (int k = 0; k < 3; k++)
+            vrel[k] = (double(a1) * dxr[3 * size_t(v0) + k] + double(a) * dxr[3 * size_t(v1) + k]) /
+                      dt;
+        const double ms = mass[v0] + mass[v1];
+        const double vn = vrel[0] * e.n[0] + vrel[1] * e.n[1] + vrel[2] * e.n[2];
+        const double Ic = vn > v_thre ? 0 : ms * fabs(vn) / 2;
+        const double d = 3e-3 - double(e.depth);
+        double Ir = 0;
+        if (!(vn > double(0.1f) * d / dt))
+        {
+            const double Ir0 = dt * K * d, Ir1 = ms * (double(0.1f) * d / dt - vn);
+            Ir = Ir0 < Ir1 ? Ir0 : Ir1;
+        }
+        const double I = Ic + Ir;
+        const float den = 1 + a * a + (1 - a) * (1 - a) + b * b + (1 - b) * (1 - b);
+        const double It = 2 * I / double(den);
+        for (int k = 0; k < 3; k++)
+        {
+            dxr[3 * size_t(v0) + k] += scale * dt * double(a1) * It / ms * e.n[k];
+            dxr[3 * size_t(v1) + k] += scale * dt * double(a) * It / ms * e.n[k];
+        }
+        return;
+    }
+    const PtContact &p = pt[i - c.n_ee];
+    double vrel[3], ms;
+    const double bw[3] = {p.bary[0], p.bary[1], p.bary[2]};
+    if (p.cloth_point)
+    {
+        for (int k = 0; k < 3; k++)
+            vrel[k] = dxr[3 * size_t(v[0]) + k] / dt;
+        ms = mass[v[0]];
+    }
+    else
+    {
+        for (int k = 0; k < 3; k++)
+            vrel[k] = (dxr[3 * size_t(v[0]) + k] * bw[0] + dxr[3 * size_t(v[1]) + k] * bw[1] +
+                       dxr[3 * size_t(v[2]) + k] * bw[2]) /
+                      dt;
+        ms = mass[v[0]] + mass[v[1]] + mass[v[2]];
+    }
+    const double vn = vrel[0] * p.n[0] + vrel[1] * p.n[1] + vrel[2] * p.n[2];
+    const double Ic = vn > v_thre ? 0 : ms * fabs(vn) / 2;
+    const double d = 3e-3 - double(p.depth);
+    double Ir = 0;
+    if (!(vn > 0.1 * d / dt))
+    {
+        const double Ir0 = dt * K * d, Ir1 = ms * (0.1 * d / dt - vn);
+        Ir = Ir0 < Ir1 ? Ir0 : Ir1;
+    }
+    const double I = Ic + Ir;
+    const double It = 2 * I / (1 + (bw[0] * bw[0] + bw[1] * bw[1] + bw[2] * bw[2]));
+    if (p.cloth_point)
+        for (int k = 0; k < 3; k++)
+            dxr[3 * size_t(v[0]) + k] += scale * (dt * It / ms * p.n[k]);
+    else
+        for (int j = 0; j < 3; j++)
+            for (int k = 0; k < 3; k++)
+                dxr[3 * size_t(v[j]) + k] += scale * (dt * bw[j] * It / ms * p.n[k]);
+}
+
+
+
 // Repulsion (BaraffCloth.cpp:626-926) in rounds: a contact runs when it heads
-// the list of every vertex it touches (all earlier contacts there have run);
-// contacts that run in one round share no vertex.  cstate: 0 pending, 1 ran
-// this round, 2 done.
+// the list of every vertex it touches (every earlier contact there has run),
+// so the contacts of one round share no vertex and the result is that of the
+// sequential loop.  The first round's contacts come from a scan of all; after
+// that only the new heads of the vertices a round touched can become ready,
+// so each round visits just those (work lists wa / wb, a queued flag per
+// contact).
 __global__ void __launch_bounds__(kRepBlock) k_col_repulse(
     const CollideCounts *cnt_in, int cap_pt, int cap_ee, const PtContact *pt, const EeContact *ee,
-    const int *edges, const int4 *tri, const double *mass, const int *inc_off, const int *inc,
-    int cap_inc, int *rptr, int *cstate, double *dxr, double dt, double K, CollideCounts *cw)
+    const int4 *cverts, const int4 *clpos, const int4 *csucc, const double *mass, int *rptr,
+    int *queued, int *wa, int *wb, double *dxr, double dt, double K, CollideCounts *cw)
 {
-    __shared__ int s_left, s_ran;
+    __shared__ int s_na, s_nb, s_done;
     CollideCounts c = *cnt_in;
     c.n_pt = min(c.n_pt, cap_pt);
     c.n_ee = min(c.n_ee, cap_ee);
     const int n = c.n_pt + c.n_ee;
-    const double v_thre = 0.01, scale = double(0.1f);
-    int rounds = 0;
-    for (;;)
+    // contact i heads all its lists when every vertex has run exactly the
+    // contacts before it there
+    auto ready = [&](int i) {
+        const int4 cv = cverts[i], lp = clpos[i];
+        bool r = rptr[cv.x] == lp.x;
+        if (cv.w > 1)
+            r = r && rptr[cv.y] == lp.y;
+        if (cv.w > 2)
+            r = r && rptr[cv.z] == lp.z;
+        return r;
+    };
+    if (threadIdx.x == 0)
     {
+        s_na = 0;
+        s_nb = 0;
+        s_done = 0;
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < n; i += blockDim.x)
+        if (ready(i))
+        {
+            queued[i] = 1;
+            wa[atomicAdd(&s_na, 1)] = i;
+        }
+    __syncthreads();
+    int rounds = 0;
+    int *cur = wa, *nxt = wb;
+    while (s_na > 0 && rounds <= n)
+    {
+        const int na = s_na;
+        // run this round's contacts (vertex-disjoint), then move their
+        // vertices past them
+        for (int k = threadIdx.x; k < na; k += blockDim.x)
+        {
+            const int i = cur[k];
+            const int4 cv = cverts[i];
+            const int v[3] = {cv.x, cv.y, cv.z};
+            repulse_one(c, pt, ee, i, v, mass, dxr, dt, K);
+            for (int q = 0; q < cv.w; q++)
+                rptr[v[q]]++;
+        }
         if (threadIdx.x == 0)
         {
-            s_left = 0;
-            s_ran = 0;
+            s_done += na;
+            s_nb = 0;
         }
         __syncthreads();
-        // phase 1: run the ready contacts
-        for (int i = threadIdx.x; i < n; i += blockDim.x)
+        // their successors that now head all their lists
+        for (int k = threadIdx.x; k < na; k += blockDim.x)
         {
-            if (cstate[i] != 0)
-                continue;
-            atomicAdd(&s_left, 1);
-            int v[3], tag;
-            const int m = contact_vertices(&c, pt, ee, edges, tri, i, v, &tag);
-            bool ready = true;
-            for (int k = 0; k < m; k++)
+            const int i = cur[k];
+            const int4 sc = csucc[i];
+            const int m = cverts[i].w;
+            const int su[3] = {sc.x, sc.y, sc.z};
+            for (int q = 0; q < m; q++)
             {
-                const int pos = inc_off[v[k]] + rptr[v[k]];
-                const int head = (pos < inc_off[v[k] + 1] && pos < cap_inc) ? inc[pos] : -1;
-                if (head != tag)
-                    ready = false;
+                const int h = su[q];
+                if (h >= 0 && ready(h) && atomicExch(&queued[h], 1) == 0)
+                    nxt[atomicAdd(&s_nb, 1)] = h;
             }
-            if (!ready)
-                continue;
-            if (i < c.n_ee)
-            {
-                const EeContact &e = ee[i];
-                const float a = e.s, b = e.t, a1 = 1 - a;
-                const int v0 = v[0], v1 = v[1];
-                double vrel[3];
-                for (int k = 0; k < 3; k++)
-                    vrel[k] = (double(a1) * dxr[3 * size_t(v0) + k] +
-                               double(a) * dxr[3 * size_t(v1) + k]) /
-                              dt;
-                const double ms = double(mass[v0]) + double(mass[v1]);
-                const double vn = vrel[0] * e.n[0] + vrel[1] * e.n[1] + vrel[2] * e.n[2];
-                const double Ic = vn > v_thre ? 0 : ms * fabs(vn) / 2;
-                const double d = 3e-3 - double(e.depth);
-                double Ir = 0;
-                if (!(vn > double(0.1f) * d / dt))
-                {
-                    const double Ir0 = dt * K * d, Ir1 = ms * (double(0.1f) * d / dt - vn);
-                    Ir = Ir0 < Ir1 ? Ir0 : Ir1;
-                }
-                const double I = Ic + Ir;
-                const float den = 1 + a * a + (1 - a) * (1 - a) + b * b + (1 - b) * (1 - b);
-                const double It = 2 * I / double(den);
-                for (int k = 0; k < 3; k++)
-                {
-                    dxr[3 * size_t(v0) + k] += scale * dt * double(a1) * It / ms * e.n[k];
-                    dxr[3 * size_t(v1) + k] += scale * dt * double(a) * It / ms * e.n[k];
-                }
-            }
-            else
-            {
-                const PtContact &p = pt[i - c.n_ee];
-                double vrel[3], ms;
-                const double bw[3] = {p.bary[0], p.bary[1], p.bary[2]};
-                if (p.cloth_point)
-                {
-                    for (int k = 0; k < 3; k++)
-                        vrel[k] = dxr[3 * size_t(v[0]) + k] / dt;
-                    ms = double(mass[v[0]]);
-                }
-                else
-                {
-                    for (int k = 0; k < 3; k++)
-                        vrel[k] = (dxr[3 * size_t(v[0]) + k] * bw[0] +
-                                   dxr[3 * size_t(v[1]) + k] * bw[1] +
-                                   dxr[3 * size_t(v[2]) + k] * bw[2]) /
-                                  dt;
-                    ms = double(mass[v[0]]) + double(mass[v[1]]) + double(mass[v[2]]);
-                }
-                const double vn = vrel[0] * p.n[0] + vrel[1] * p.n[1] + vrel[2] * p.n[2];
-                const double Ic = vn > v_thre ? 0 : ms * fabs(vn) / 2;
-                const double d = 3e-3 - double(p.depth);
-                double Ir = 0;
-                if (!(vn > 0.1 * d / dt))
-                {
-                    const double Ir0 = dt * K * d, Ir1 = ms * (0.1 * d / dt - vn);
-                    Ir = Ir0 < Ir1 ? Ir0 : Ir1;
-                }
-                const double I = Ic + Ir;
-                const double It = 2 * I / (1 + (bw[0] * bw[0] + bw[1] * bw[1] + bw[2] * bw[2]));
-                if (p.cloth_point)
-                    for (int k = 0; k < 3; k++)
-                        dxr[3 * size_t(v[0]) + k] += scale * (dt * It / ms * p.n[k]);
-                else
-                    for (int j = 0; j < 3; j++)
-                        for (int k = 0; k < 3; k++)
-                            dxr[3 * size_t(v[j]) + k] += scale * (dt * bw[j] * It / ms * p.n[k]);
-            }
-            cstate[i] = 1;
-            atomicAdd(&s_ran, 1);
         }
         __syncthreads();
-        // phase 2: the vertices of the contacts that ran move past them
-        for (int i = threadIdx.x; i < n; i += blockDim.x)
-        {
-            if (cstate[i] != 1)
-                continue;
-            int v[3], tag;
-            const int m = contact_vertices(&c, pt, ee, edges, tri, i, v, &tag);
-            for (int k = 0; k < m; k++)
-                rptr[v[k]]++;
-            cstate[i] = 2;
-        }
-        __syncthreads();
+        if (threadIdx.x == 0)
+            s_na = s_nb;
+        int *t = cur;
+        cur = nxt;
+        nxt = t;
         rounds++;
-        const int left = s_left, ran = s_ran;
         __syncthreads();
-        if (left == 0)
-            break;
-        if (ran == 0 || rounds > n + 1)
-        {
-            // cannot happen: the first pending contact heads all its lists
-            if (threadIdx.x == 0)
-                cw->overflow = 1;
-            break;
-        }
     }
     if (threadIdx.x == 0)
+    {
         cw->rounds = rounds;
+        if (s_done != n)
+            cw->overflow = 1; // a contact never headed its lists (a lost list entry)
+    }
 }
 
 } // namespace
@@ -1024,6 +1309,9 @@ int collide_alloc(cloth_s *c)
     const long long cap_inc = 3 * cap_pt + 2 * cap_ee;
     if (cap_pairs > (1LL << 30) || cap_inc > (1LL << 30))
         return col_fail(CLOTH_ERR_INVALID, "collisions: contact capacities too large");
+    if (std::max({(long long)nt, (long long)ne, (long long)max_bnt, (long long)max_bnv}) >=
+        (long long)kScanTile * kScanMaxTiles)
+        return col_fail(CLOTH_ERR_INVALID, "collisions: mesh too large for the contact lists");
     if (w->mem)
     {
         cudaFree(w->mem);
@@ -1040,8 +1328,14 @@ int collide_alloc(cloth_s *c)
                  o_ee = L.take<EeContact>(size_t(cap_ee)),
                  o_incoff = L.take<int>(size_t(nv) + 1), o_inccur = L.take<int>(size_t(nv)),
                  o_inc = L.take<int>(size_t(cap_inc)), o_rptr = L.take<int>(size_t(nv)),
-                 o_cst = L.take<int>(size_t(cap_pt + cap_ee)), o_dxr = L.take<double>(3 * size_t(nv)),
+                 o_cst = L.take<int>(size_t(cap_pt + cap_ee)),
+                 o_wa = L.take<int>(size_t(cap_pt + cap_ee)), o_wb = L.take<int>(size_t(cap_pt + cap_ee)),
+                 o_dxr = L.take<double>(3 * size_t(nv)),
                  o_cnt = L.take<CollideCounts>(2), o_vtoff = L.take<int>(size_t(nv) + 1),
+                 o_tsum = L.take<int>(kScanMaxTiles),
+                 o_cvert = L.take<int4>(size_t(cap_pt + cap_ee)),
+                 o_clpos = L.take<int4>(size_t(cap_pt + cap_ee)),
+                 o_csucc = L.take<int4>(size_t(cap_pt + cap_ee)),
                  o_vt = L.take<int>(3 * size_t(nt)), o_edges = L.take<int>(4 * size_t(ne)),
                  o_mass = L.take<double>(size_t(nv));
     char *base = nullptr;
@@ -1070,8 +1364,14 @@ int collide_alloc(cloth_s *c)
     w->inc = reinterpret_cast<int *>(base + o_inc);
     w->rptr = reinterpret_cast<int *>(base + o_rptr);
     w->cstate = reinterpret_cast<int *>(base + o_cst);
+    w->wa = reinterpret_cast<int *>(base + o_wa);
+    w->wb = reinterpret_cast<int *>(base + o_wb);
     w->dxr = reinterpret_cast<double *>(base + o_dxr);
     w->cnt = reinterpret_cast<CollideCounts *>(base + o_cnt);
+    w->tile_sum = reinterpret_cast<int *>(base + o_tsum);
+    w->cverts = reinterpret_cast<int4 *>(base + o_cvert);
+    w->clpos = reinterpret_cast<int4 *>(base + o_clpos);
+    w->csucc = reinterpret_cast<int4 *>(base + o_csucc);
     w->vt_off = reinterpret_cast<int *>(base + o_vtoff);
     w->vt = reinterpret_cast<int *>(base + o_vt);
     w->edges = reinterpret_cast<int *>(base + o_edges);
@@ -1114,6 +1414,18 @@ int collide_alloc(cloth_s *c)
 
 } // namespace
 
+namespace {
+
+void col_scan(cloth_collide_s *w, int *a, int n, int *total, cudaStream_t s)
+{
+    const int tiles = std::max(1, (n + kScanTile - 1) / kScanTile);
+    k_col_scan_tiles<<<tiles, 1024, 0, s>>>(a, n, w->tile_sum);
+    k_col_scan_top<<<1, 1024, 0, s>>>(w->tile_sum, tiles, a, n, total);
+    k_col_scan_add<<<tiles, 256, 0, s>>>(a, n, w->tile_sum);
+}
+
+} // namespace
+
 int cloth::detail::collide_detect(cloth_s *c)
 {
     cloth_collide_s *w = c->col;
@@ -1135,7 +1447,7 @@ int cloth::detail::collide_detect(cloth_s *c)
         k_col_pairs<<<grid_blocks(ctx, nt), kColBlock, 0, s>>>(bv, nt, w->ctlo, w->cthi,
                                                                w->tp_off, w->tp, w->cap_pairs,
                                                                0, w->cnt);
-        k_col_scan<<<1, 1024, 0, s>>>(w->tp_off, nt, total);
+        col_scan(w, w->tp_off, nt, total, s);
         k_col_pairs<<<grid_blocks(ctx, nt), kColBlock, 0, s>>>(bv, nt, w->ctlo, w->cthi,
                                                                w->tp_off, w->tp, w->cap_pairs,
                                                                1, w->cnt);
@@ -1144,11 +1456,11 @@ int cloth::detail::collide_detect(cloth_s *c)
         CCK(cudaMemsetAsync(w->bt_cur, 0, size_t(bv.nt) * sizeof(int), s));
         k_col_bt_count<<<grid_blocks(ctx, nt), kColBlock, 0, s>>>(nt, w->tp_off, w->tp,
                                                                   w->cap_pairs, w->bt_off);
-        k_col_scan<<<1, 1024, 0, s>>>(w->bt_off, bv.nt, total);
+        col_scan(w, w->bt_off, bv.nt, total, s);
         k_col_bt_fill<<<grid_blocks(ctx, nt), kColBlock, 0, s>>>(
             nt, w->tp_off, w->tp, w->cap_pairs, w->bt_off, w->bt_cur, w->bt);
-        k_col_bt_sort<<<grid_blocks(ctx, bv.nt), kColBlock, 0, s>>>(bv.nt, w->bt_off, w->bt,
-                                                                    w->cap_pairs);
+        k_col_bt_sort<<<std::max(1, std::min(bv.nt, ctx->num_sms * 16)), kSortBlock, 0, s>>>(
+            bv.nt, w->bt_off, w->bt, w->cap_pairs);
         // cloth points against body triangles
         for (int pass = 0; pass < 2; pass++)
         {
@@ -1156,17 +1468,17 @@ int cloth::detail::collide_detect(cloth_s *c)
                 bv, nv, x, w->vt_off, w->vt, w->tp_off, w->tp, w->cap_pairs, w->lst, w->pt,
                 w->cap_pt, pass, w->cnt);
             if (pass == 0)
-                k_col_scan<<<1, 1024, 0, s>>>(w->lst, nv, total);
+                col_scan(w, w->lst, nv, total, s);
         }
         k_col_advance<<<1, 32, 0, s>>>(w->cnt, 0, total);
         // body points against cloth triangles
         for (int pass = 0; pass < 2; pass++)
         {
-            k_col_pt_body<<<grid_blocks(ctx, bv.nv), kColBlock, 0, s>>>(
+            k_col_pt_body<<<std::max(1, std::min(bv.nv, ctx->num_sms * 16)), kSortBlock, 0, s>>>(
                 bv, x, tri, w->ctn, w->bt_off, w->bt, w->cap_pairs, w->lst, w->pt, w->cap_pt,
                 pass, w->cnt);
             if (pass == 0)
-                k_col_scan<<<1, 1024, 0, s>>>(w->lst, bv.nv, total);
+                col_scan(w, w->lst, bv.nv, total, s);
         }
         k_col_advance<<<1, 32, 0, s>>>(w->cnt, 0, total);
         // cloth edges against body edges
@@ -1177,7 +1489,7 @@ int cloth::detail::collide_detect(cloth_s *c)
                                                                 w->lst, w->ee, w->cap_ee, pass,
                                                                 w->cnt);
             if (pass == 0)
-                k_col_scan<<<1, 1024, 0, s>>>(w->lst, ne, total);
+                col_scan(w, w->lst, ne, total, s);
         }
         k_col_advance<<<1, 32, 0, s>>>(w->cnt, 1, total);
     }
@@ -1187,13 +1499,16 @@ int cloth::detail::collide_detect(cloth_s *c)
     const int gc = grid_blocks(ctx, std::max(w->cap_pt, w->cap_ee));
     k_col_inc<<<gc, kColBlock, 0, s>>>(w->cnt, w->cap_pt, w->cap_ee, w->pt, w->ee, w->edges,
                                        tri, w->inc_off, w->inc_cur, w->inc, w->cap_inc, 0,
-                                       w->cnt);
-    k_col_scan<<<1, 1024, 0, s>>>(w->inc_off, nv, total);
+                                       w->cnt, w->cverts);
+    col_scan(w, w->inc_off, nv, total, s);
     k_col_inc<<<gc, kColBlock, 0, s>>>(w->cnt, w->cap_pt, w->cap_ee, w->pt, w->ee, w->edges,
                                        tri, w->inc_off, w->inc_cur, w->inc, w->cap_inc, 1,
-                                       w->cnt);
+                                       w->cnt, w->cverts);
     k_col_inc_sort<<<grid_blocks(ctx, nv), kColBlock, 0, s>>>(nv, w->inc_off, w->inc,
                                                               w->cap_inc);
+    k_col_links<<<grid_blocks(ctx, nv), kColBlock, 0, s>>>(nv, w->cnt, w->cap_pt, w->cap_ee,
+                                                           w->inc_off, w->inc, w->cap_inc,
+                                                           w->cverts, w->clpos, w->csucc);
     CCK(cudaGetLastError());
     return CLOTH_OK;
 }
@@ -1211,9 +1526,8 @@ int cloth::detail::collide_repulse(cloth_s *c)
     k_col_dxr<<<grid_blocks(ctx, std::max(nv, w->cap_pt + w->cap_ee)), kColBlock, 0, s>>>(
         nv, c->h.dx, w->dxr, w->rptr, w->cap_pt + w->cap_ee, w->cstate);
     k_col_repulse<<<1, kRepBlock, 0, s>>>(w->cnt, w->cap_pt, w->cap_ee, w->pt, w->ee,
-                                          w->edges, c->h.tri, w->mass64, w->inc_off, w->inc,
-                                          w->cap_inc, w->rptr, w->cstate, w->dxr, c->dt_set, K,
-                                          w->cnt);
+                                          w->cverts, w->clpos, w->csucc, w->mass64, w->rptr,
+                                          w->cstate, w->wa, w->wb, w->dxr, c->dt_set, K, w->cnt);
     CCK(cudaGetLastError());
     return CLOTH_OK;
 }

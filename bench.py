@@ -60,6 +60,38 @@ def initial_state(pos: np.ndarray, seed: int, dt=DT, sx=1e-3):
     return x.reshape(-1).copy(), (x - dt * v).reshape(-1).copy()
 
 
+def sphere_body(radius=0.25, center=(0.0, -0.05, 0.2515), n_lat=48, n_lon=96):
+    """A UV sphere (triangle normals outward) whose front touches the cloth
+    plane z = 0 at 1.5 mm: the obstacle of the collision workload."""
+    c = np.asarray(center, np.float64)
+    pts = [c + [0.0, radius, 0.0]]
+    for j in range(1, n_lat):
+        th = np.pi * j / n_lat
+        for i in range(n_lon):
+            ph = 2 * np.pi * i / n_lon
+            pts.append(c + radius * np.array([np.sin(th) * np.cos(ph), np.cos(th),
+                                              np.sin(th) * np.sin(ph)]))
+    pts.append(c + [0.0, -radius, 0.0])
+    pos = np.array(pts)
+    ring = lambda j, i: 1 + (j - 1) * n_lon + (i % n_lon)
+    tris = []
+    for i in range(n_lon):
+        tris.append((0, ring(1, i), ring(1, i + 1)))
+        tris.append((len(pts) - 1, ring(n_lat - 1, i + 1), ring(n_lat - 1, i)))
+    for j in range(1, n_lat - 1):
+        for i in range(n_lon):
+            a, b = ring(j, i), ring(j, i + 1)
+            cc, d = ring(j + 1, i + 1), ring(j + 1, i)
+            tris += [(a, d, cc), (a, cc, b)]
+    tris = np.array(tris, np.int32)
+    # orient every triangle outward: (v1 - v0) x (v2 - v1) away from the centre
+    v0, v1, v2 = pos[tris[:, 0]], pos[tris[:, 1]], pos[tris[:, 2]]
+    n = np.cross(v1 - v0, v2 - v1)
+    out = np.einsum("ij,ij->i", n, (v0 + v1 + v2) / 3 - c) > 0
+    tris[~out] = tris[~out][:, [0, 2, 1]]
+    return pos, tris
+
+
 def config_block(extra=None) -> dict:
     c = {"workload": f"single cloth {N_SIDE}x{N_SIDE} grid ({N_SIDE * N_SIDE} vertices, "
                      f"{2 * (N_SIDE - 1) ** 2} triangles), dt={DT}, PCG rel_tol={REL_TOL}",
@@ -237,14 +269,21 @@ def count_nnzb(n_side: int) -> int:
 
 # ---------------------------------------------------------------- CPU baseline
 def cpu_port_step_time(threads: int, sample_steps: int = 1, n_side: int = N_SIDE,
-                       bending: str = "quadratic", sx: float = 1e-3) -> dict:
+                       bending: str = "quadratic", sx: float = 1e-3, body: str = "none") -> dict:
     """Times the FP64 CPU restatement of the same step (oracle port)."""
     from acousticsim_gb300 import build_grid
     from oracle import oracle as orc
     conf = workload_conf(n_side, bending=bending)
     mesh = build_grid((1.0, 1.0), (n_side - 1, n_side - 1))
     pins = [n_side - 1, n_side * n_side - 1]
-    oc = orc.OracleCloth(mesh, conf, pins)
+    bodies = []
+    if body == "sphere":
+        from acousticsim_gb300.cloth import derive_edges_host
+        bp, bt = sphere_body()
+        tn, vn = orc.body_normals(bp, bt)
+        bodies = [{"pos": bp, "tris": bt, "edges": derive_edges_host(bt), "tnormal": tn,
+                   "vnormal": vn}]
+    oc = orc.OracleCloth(mesh, conf, pins, bodies=bodies)
     x, xp = initial_state(mesh["pos"], 1234, sx=sx)
     oc.x, oc.xpre = x, xp
     t0 = time.perf_counter()
@@ -269,7 +308,7 @@ def run_reference(args, rank, world, pg):
     for _ in range(args.warmup):
         cpu_port_step_time(threads, 1, 64, args.bending, args.noise)
     n = max(1, min(args.steps, 2))
-    r = cpu_port_step_time(threads, n, bending=args.bending, sx=args.noise)
+    r = cpu_port_step_time(threads, n, bending=args.bending, sx=args.noise, body=args.body)
     value = r["steps"] / r["seconds"]
     line = {"metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": args.gpus,
             "steps": n, "warmup": args.warmup,
@@ -277,7 +316,8 @@ def run_reference(args, rank, world, pg):
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "impl": "reference", "config": config_block({"pcg_iters": r["pcg_iters"],
                                                          "bending": args.bending,
-                                                         "x_noise": args.noise}),
+                                                         "x_noise": args.noise,
+                                                         "body": args.body}),
             "cpu_baseline": {"value": value, "unit": "steps/s", "cores": threads, "kind": "port",
                              "sample": f"{r['steps']} full {N_SIDE}x{N_SIDE} steps, FP64 oracle "
                                        f"port (oracle/cloth_oracle.c), {threads} OpenMP threads"},
@@ -302,6 +342,11 @@ def run_ours(args, rank, world, local, pg):
     x0, xp0 = initial_state(cloth.GetInitPos(), 1234 + rank, sx=args.noise)
     cloth.SetPos(x0)
     cloth.SetPrePos(xp0)
+    body = None
+    if args.body == "sphere":
+        from acousticsim_gb300 import ClothBody
+        body = ClothBody(ctx, *sphere_body())
+        cloth.set_bodies([body])
     p = params(max_iters=MAX_ITERS, rel_tol=REL_TOL)
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=f"cuda:{local}")
 
@@ -338,6 +383,14 @@ def run_ours(args, rank, world, local, pg):
     value = steps_total / t_max if t_max > 0 else 0.0
     per_step = 5 if st["solver"].startswith("persistent") else None
     launches = sum(per_step if per_step else 5 + 2 * i for i in iters)
+    contacts = None
+    if body is not None:
+        # contact detection (26 kernels for one body) and repulsion (2) per step
+        launches += 28 * args.steps
+        con = cloth.get_contacts()
+        contacts = {"point_triangle": int(len(con["pt_i"])), "edge_edge": int(len(con["ee_i"])),
+                    "repulsion_rounds": int(con["repulsion_rounds"]),
+                    "overflow": int(con["overflow"])}
 
     # ---- e2e: the same steps through the C ABI with host buffers, pinned
     nv = cloth.nv
@@ -412,7 +465,7 @@ def run_ours(args, rank, world, local, pg):
     if rank == 0:
         from oracle import oracle as orc
         threads = orc.max_threads()
-        r = cpu_port_step_time(threads, 1, bending=args.bending, sx=args.noise)
+        r = cpu_port_step_time(threads, 1, bending=args.bending, sx=args.noise, body=args.body)
         cpu = {"value": r["steps"] / r["seconds"], "unit": "steps/s", "cores": threads,
                "kind": "port",
                "sample": f"1 full {N_SIDE}x{N_SIDE} step (FP64 oracle port, {r['pcg_iters'][0]} "
@@ -426,12 +479,16 @@ def run_ours(args, rank, world, local, pg):
                 "data": "synthetic (seeded perturbation of the flat 512x512 cloth)",
                 "config": config_block({"parallelism": f"replicas x{world}",
                                         "bending": args.bending, "x_noise": args.noise,
+                                        "body": args.body, "contacts_last_step": contacts,
                                         "pcg_iters_per_step": iters,
                                         "step_ms": [round(v, 3) for v in step_ms],
                                         "wall_s_timed_region": wall}),
                 "e2e": e2e, "gpu_launches": launches, "clocks": clk,
                 "roofline": roof, "cpu_baseline": cpu}
         print(json.dumps(line), flush=True)
+    if body is not None:
+        cloth.set_bodies([])
+        body.close()
     cloth.close()
     ctx.close()
 
@@ -914,6 +971,9 @@ def run_profile_case(args):
     x0, xp0 = initial_state(cloth.GetInitPos(), 1234, sx=args.noise)
     cloth.SetPos(x0)
     cloth.SetPrePos(xp0)
+    if args.body == "sphere":
+        from acousticsim_gb300 import ClothBody
+        cloth.set_bodies([ClothBody(ctx, *sphere_body())])
     if args.solver == "graph_loop":
         # first step outside the profiler: the autotuner picks the kernel variants
         cloth.UpdatePos(0.0, params(max_iters=args.profile_iters, rel_tol=1e-12))
@@ -922,6 +982,10 @@ def run_profile_case(args):
     ph = ctx.profile()
     out = {"profile_case": st, "phases": ph, "grid": args.profile_side,
            "kernel_variant": ctx.kernel_variant()}
+    if args.body != "none":
+        con = cloth.get_contacts()
+        out["contacts"] = {"point_triangle": len(con["pt_i"]), "edge_edge": len(con["ee_i"]),
+                           "repulsion_rounds": con["repulsion_rounds"]}
     mi = cloth.matrix_info()
     ab = algorithmic_bytes(cloth.nv, mi["nnzb"], skew=args.bending == "dihedral")
     if st["solver"] == "graph_loop":
@@ -953,6 +1017,9 @@ def main():
     ap.add_argument("--bending", choices=["quadratic", "dihedral"], default="quadratic",
                     help="bending model of the single-cloth step: the GPU cloth's quadratic "
                          "one (the headline) or the CPU cloth's dihedral one")
+    ap.add_argument("--body", choices=["none", "sphere"], default="none",
+                    help="a kinematic body the single cloth collides with (the CPU cloth's "
+                         "contact handling): a UV sphere touching the cloth")
     ap.add_argument("--noise", type=float, default=1e-3,
                     help="std of the seeded position perturbation of the single-cloth step "
                          "(1e-3: the benchmark's; the dihedral model at 512x512 needs a "

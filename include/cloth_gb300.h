@@ -135,8 +135,9 @@ int cloth_ctx_destroy(cloth_ctx *ctx);
 int cloth_ctx_synchronize(cloth_ctx *ctx);
 /* Per-phase CUDA-event timers (cTimeUtil::Begin/End, src/utils/TimeUtil.hpp:7-32).
  * Phases: 0 pins, 1 triangle assembly, 2 row assembly + PCG init,
- * 3 SpMV + p.Ap, 4 update + residual, 5 position update. */
-#define CLOTH_NUM_PHASES 6
+ * 3 SpMV + p.Ap, 4 update + residual, 5 position update, 6 contact detection,
+ * 7 contact repulsion. */
+#define CLOTH_NUM_PHASES 8
 int cloth_ctx_set_profiling(cloth_ctx *ctx, int enable);
 int cloth_ctx_get_profile(cloth_ctx *ctx, double *ms_total, long long *launches);
 int cloth_ctx_reset_profile(cloth_ctx *ctx);

@@ -1049,26 +1049,130 @@ int orc_contacts(int nv, int nt, int ne, const double *x, const int *tris, const
     }
     for (int t = 0; t < bnt; t++)
         aabb5(bpos, btris + 3 * (size_t)t, blo + 3 * (size_t)t, bhi + 3 * (size_t)t);
+    /* body triangles binned on a uniform grid (only to find the box pairs
+     * faster; the set of pairs is that of the all-pairs test) */
+    double g0[3] = {1e300, 1e300, 1e300}, g1[3] = {-1e300, -1e300, -1e300}, cell = 1e-3;
+    for (int t = 0; t < bnt; t++)
+        for (int k = 0; k < 3; k++)
+        {
+            const double l = blo[3 * (size_t)t + k], h = bhi[3 * (size_t)t + k];
+            g0[k] = l < g0[k] ? l : g0[k];
+            g1[k] = h > g1[k] ? h : g1[k];
+            cell = (h - l) > cell ? (h - l) : cell;
+        }
+    int gd[3];
+    for (;;)
+    {
+        long long tot = 1;
+        for (int k = 0; k < 3; k++)
+        {
+            gd[k] = (int)ceil((g1[k] - g0[k]) / cell);
+            gd[k] = gd[k] < 1 ? 1 : gd[k];
+            tot *= gd[k];
+        }
+        if (tot <= (1 << 22))
+            break;
+        cell *= 1.5;
+    }
+#define ORC_CELL(v, k)                                                                        \
+    (floor(((v) - g0[k]) / cell) < 0.0                                                        \
+         ? 0                                                                                  \
+         : (floor(((v) - g0[k]) / cell) >= (double)gd[k] ? gd[k] - 1                          \
+                                                          : (int)floor(((v) - g0[k]) / cell)))
+    const size_t ncell = (size_t)gd[0] * gd[1] * gd[2];
+    int *coff = (int *)calloc(ncell + 1, sizeof(int));
+    for (int pass = 0; pass < 2; pass++)
+    {
+        int *ctr = pass ? (int *)calloc(ncell, sizeof(int)) : NULL;
+        for (int t = 0; t < bnt; t++)
+        {
+            int i0[3], i1[3];
+            for (int k = 0; k < 3; k++)
+            {
+                i0[k] = ORC_CELL(blo[3 * (size_t)t + k], k);
+                i1[k] = ORC_CELL(bhi[3 * (size_t)t + k], k);
+            }
+            for (int iz = i0[2]; iz <= i1[2]; iz++)
+                for (int iy = i0[1]; iy <= i1[1]; iy++)
+                    for (int ix = i0[0]; ix <= i1[0]; ix++)
+                    {
+                        const size_t c = ((size_t)iz * gd[1] + iy) * gd[0] + ix;
+                        if (!pass)
+                            coff[c + 1]++;
+                        else
+                            ctr[c]++;
+                    }
+        }
+        if (!pass)
+            for (size_t c = 0; c < ncell; c++)
+                coff[c + 1] += coff[c];
+        free(ctr);
+    }
+    int *ctri = (int *)malloc(sizeof(int) * ((size_t)coff[ncell] + 1));
+    {
+        int *fill = (int *)calloc(ncell, sizeof(int));
+        for (int t = 0; t < bnt; t++)
+        {
+            int i0[3], i1[3];
+            for (int k = 0; k < 3; k++)
+            {
+                i0[k] = ORC_CELL(blo[3 * (size_t)t + k], k);
+                i1[k] = ORC_CELL(bhi[3 * (size_t)t + k], k);
+            }
+            for (int iz = i0[2]; iz <= i1[2]; iz++)
+                for (int iy = i0[1]; iy <= i1[1]; iy++)
+                    for (int ix = i0[0]; ix <= i1[0]; ix++)
+                    {
+                        const size_t c = ((size_t)iz * gd[1] + iy) * gd[0] + ix;
+                        ctri[coff[c] + fill[c]++] = t;
+                    }
+        }
+        free(fill);
+    }
     size_t cap = 1024, np = 0;
     ipair *tp = (ipair *)malloc(sizeof(ipair) * cap);
     for (int T = 0; T < nt; T++)
-        for (int t = 0; t < bnt; t++)
+    {
+        const double *al = clo + 3 * (size_t)T, *ah = chi + 3 * (size_t)T;
+        int i0[3], i1[3], outside = 0;
+        for (int k = 0; k < 3; k++)
         {
-            const double *al = clo + 3 * (size_t)T, *ah = chi + 3 * (size_t)T,
-                         *bl = blo + 3 * (size_t)t, *bh = bhi + 3 * (size_t)t;
-            if (al[0] <= bh[0] && ah[0] >= bl[0] && al[1] <= bh[1] && ah[1] >= bl[1] &&
-                al[2] <= bh[2] && ah[2] >= bl[2])
-            {
-                if (np == cap)
-                {
-                    cap *= 2;
-                    tp = (ipair *)realloc(tp, sizeof(ipair) * cap);
-                }
-                tp[np].a = T;
-                tp[np].b = t;
-                np++;
-            }
+            if (ah[k] < g0[k] || al[k] > g1[k])
+                outside = 1;
+            i0[k] = ORC_CELL(al[k], k);
+            i1[k] = ORC_CELL(ah[k], k);
         }
+        if (outside)
+            continue;
+        const size_t np0 = np;
+        for (int iz = i0[2]; iz <= i1[2]; iz++)
+            for (int iy = i0[1]; iy <= i1[1]; iy++)
+                for (int ix = i0[0]; ix <= i1[0]; ix++)
+                {
+                    const size_t c = ((size_t)iz * gd[1] + iy) * gd[0] + ix;
+                    for (int q = coff[c]; q < coff[c + 1]; q++)
+                    {
+                        const int t = ctri[q];
+                        const double *bl = blo + 3 * (size_t)t, *bh = bhi + 3 * (size_t)t;
+                        if (al[0] <= bh[0] && ah[0] >= bl[0] && al[1] <= bh[1] && ah[1] >= bl[1] &&
+                            al[2] <= bh[2] && ah[2] >= bl[2])
+                        {
+                            if (np == cap)
+                            {
+                                cap *= 2;
+                                tp = (ipair *)realloc(tp, sizeof(ipair) * cap);
+                            }
+                            tp[np].a = T;
+                            tp[np].b = t;
+                            np++;
+                        }
+                    }
+                }
+        np = np0 + sort_unique(tp + np0, np - np0);
+    }
+#undef ORC_CELL
+    free(coff);
+    free(ctri);
     int *te = (int *)malloc(sizeof(int) * 3 * (size_t)nt);
     int *bte = (int *)malloc(sizeof(int) * 3 * (size_t)bnt);
     tri_edges(nt, ne, tris, edges, te);
