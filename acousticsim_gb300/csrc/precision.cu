@@ -100,14 +100,28 @@ __device__ bool grid_reduce(double (&v)[N], double *part, int nblk, unsigned *ti
     if (!last)
         return false;
     __threadfence();
+    // the last block adds the partials: thread t takes partials t, t + B, ...
+    // (fixed order), then the block sum as above
+#pragma unroll
+    for (int k = 0; k < N; k++)
+    {
+        double s = 0.0;
+        for (int j = threadIdx.x; j < nblk; j += kB64)
+            s += __ldcg(&part[k * nblk + j]);
+        s = sumw(s);
+        __syncthreads();
+        if (l == 0)
+            sh[k][w] = s;
+    }
+    __syncthreads();
     if (threadIdx.x == 0)
     {
 #pragma unroll
         for (int k = 0; k < N; k++)
         {
             double s = 0.0;
-            for (int j = 0; j < nblk; j++)
-                s += __ldcg(&part[k * nblk + j]);
+            for (int j = 0; j < kB64 / 32; j++)
+                s += sh[k][j];
             tot[k] = s;
         }
         *ticket = 0u;
@@ -115,23 +129,32 @@ __device__ bool grid_reduce(double (&v)[N], double *part, int nblk, unsigned *ti
     return true;
 }
 
-__device__ __forceinline__ void load_block64(const InstDesc &d, size_t o, double *a)
+// The fields of the assembled system the FP64 kernels read, loaded once per
+// thread (the descriptor lives in global memory; held in registers here the
+// slot loop does not reload them).
+struct Mat64
 {
-    const float4 u = d.A0[o];
-    const float2 w = d.A1[o];
-    a[0] = u.x;
-    a[1] = u.y;
-    a[2] = u.z;
-    a[3] = u.w;
-    a[4] = w.x;
-    a[5] = w.y;
-}
+    int nv, stride;
+    const int *__restrict__ rowinfo;
+    const int *__restrict__ col;
+    const int *__restrict__ colu;
+    const uint32_t *__restrict__ lidx;
+    const float4 *__restrict__ A0;
+    const float2 *__restrict__ A1;
+    const float4 *__restrict__ Aw;
+    const float4 *__restrict__ dx;
+    __device__ explicit Mat64(const InstDesc &d)
+        : nv(d.nv), stride(d.stride), rowinfo(d.rowinfo), col(d.col), colu(d.colu),
+          lidx(d.lidx), A0(d.A0), A1(d.A1), Aw(d.Aw), dx(d.dx)
+    {
+    }
+};
 
 // y = A v on one row in FP64, slots in column order: the lower ones (block at
 // the transposed position), then the diagonal and upper ones. v: nv*3
 // doubles, or the FP32 dx when v64 is null.
-__device__ __forceinline__ void row_mul64(const InstDesc &d, int row, const double *v64,
-                                          double *y)
+__device__ __forceinline__ void row_mul64(const Mat64 &d, int row,
+                                          const double *__restrict__ v64, double *y)
 {
     const int info = d.rowinfo[row];
     const int len = info & 255, ds = (info >> 8) & 255;
@@ -142,8 +165,9 @@ __device__ __forceinline__ void row_mul64(const InstDesc &d, int row, const doub
         const size_t o = lower ? size_t(s) * d.stride + row : size_t(s - ds) * d.stride + row;
         const int c = lower ? d.col[o] : d.colu[o];
         const size_t oa = lower ? size_t(d.lidx[o]) : o;
-        double a[6];
-        load_block64(d, oa, a);
+        const float4 u = d.A0[oa];
+        const float2 uw = d.A1[oa];
+        const double a[6] = {u.x, u.y, u.z, u.w, uw.x, uw.y};
         double x0, x1, x2;
         if (v64)
         {
@@ -158,9 +182,12 @@ __device__ __forceinline__ void row_mul64(const InstDesc &d, int row, const doub
             x1 = f.y;
             x2 = f.z;
         }
-        y[0] += a[0] * x0 + a[1] * x1 + a[2] * x2;
-        y[1] += a[1] * x0 + a[3] * x1 + a[4] * x2;
-        y[2] += a[2] * x0 + a[4] * x1 + a[5] * x2;
+        // fused multiply-adds written out (device code is built without
+        // contraction); GB300's FP64 pipe is narrow, so halving the FP64
+        // instructions is what this loop is about
+        y[0] = fma(a[2], x2, fma(a[1], x1, fma(a[0], x0, y[0])));
+        y[1] = fma(a[4], x2, fma(a[3], x1, fma(a[1], x0, y[1])));
+        y[2] = fma(a[5], x2, fma(a[4], x1, fma(a[2], x0, y[2])));
         if (d.Aw)
         {
             // skew part (dihedral bending): + w x v on stored blocks, - on
@@ -181,12 +208,13 @@ __global__ void __launch_bounds__(kB64) k64_resid(const InstDesc *dp, const doub
                                                   double *r64, F64Ptr f)
 {
     const InstDesc &d = *dp;
+    const Mat64 m(d);
     double v[2] = {0.0, 0.0};
-    for (int row = blockIdx.x * blockDim.x + threadIdx.x; row < d.nv;
+    for (int row = blockIdx.x * blockDim.x + threadIdx.x; row < m.nv;
          row += gridDim.x * blockDim.x)
     {
         double y[3];
-        row_mul64(d, row, dx64, y);
+        row_mul64(m, row, dx64, y);
         const float4 b = d.b[row];
         const double r0 = double(b.x) - y[0], r1 = double(b.y) - y[1], r2 = double(b.z) - y[2];
         r64[3 * row] = r0;
@@ -249,9 +277,9 @@ __global__ void k64_advance(const InstDesc *dp, const double *dx64)
 
 __device__ __forceinline__ void symv64(const double *m, const double *v, double *y)
 {
-    y[0] = m[0] * v[0] + m[1] * v[1] + m[2] * v[2];
-    y[1] = m[1] * v[0] + m[3] * v[1] + m[4] * v[2];
-    y[2] = m[2] * v[0] + m[4] * v[1] + m[5] * v[2];
+    y[0] = fma(m[2], v[2], fma(m[1], v[1], m[0] * v[0]));
+    y[1] = fma(m[4], v[2], fma(m[3], v[1], m[1] * v[0]));
+    y[2] = fma(m[5], v[2], fma(m[4], v[1], m[2] * v[0]));
 }
 
 // FP64 PCG start: M = inverse of the FP64 diagonal block (adjugate), dx = 0,
@@ -263,8 +291,10 @@ __global__ void __launch_bounds__(kB64) k64_init(const InstDesc *dp, F64Ptr f)
     for (int row = blockIdx.x * blockDim.x + threadIdx.x; row < d.nv;
          row += gridDim.x * blockDim.x)
     {
-        double a[6];
-        load_block64(d, size_t(row), a); // plane 0 holds the diagonal block
+        // plane 0 holds the diagonal block
+        const float4 u = d.A0[row];
+        const float2 uw = d.A1[row];
+        const double a[6] = {u.x, u.y, u.z, u.w, uw.x, uw.y};
         const double c00 = a[3] * a[5] - a[4] * a[4], c01 = a[2] * a[4] - a[1] * a[5],
                      c02 = a[1] * a[4] - a[2] * a[3], c11 = a[0] * a[5] - a[2] * a[2],
                      c12 = a[2] * a[1] - a[0] * a[4], c22 = a[0] * a[3] - a[1] * a[1];
@@ -286,8 +316,8 @@ __global__ void __launch_bounds__(kB64) k64_init(const InstDesc *dp, F64Ptr f)
             f.z[3 * row + k] = z[k];
             f.p[3 * row + k] = 0.0;
         }
-        v[0] += r[0] * z[0] + r[1] * z[1] + r[2] * z[2];
-        v[1] += r[0] * r[0] + r[1] * r[1] + r[2] * r[2];
+        v[0] = fma(r[2], z[2], fma(r[1], z[1], fma(r[0], z[0], v[0])));
+        v[1] = fma(r[2], r[2], fma(r[1], r[1], fma(r[0], r[0], v[1])));
     }
     v[2] = v[1];
     double tot[3];
@@ -323,7 +353,7 @@ __global__ void k64_p(const InstDesc *dp, F64Ptr f)
     const double beta = f.st->beta;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < 3 * d.nv;
          i += gridDim.x * blockDim.x)
-        f.p[i] = f.z[i] + beta * f.p[i];
+        f.p[i] = fma(beta, f.p[i], f.z[i]);
 }
 
 // q = A p, pq = p.q -> alpha
@@ -334,15 +364,16 @@ __global__ void __launch_bounds__(kB64) k64_spmv(const InstDesc *dp, F64Ptr f,
     if (!f.st->active)
         return;
     double v[1] = {0.0};
-    for (int row = blockIdx.x * blockDim.x + threadIdx.x; row < d.nv;
+    const Mat64 m(d);
+    for (int row = blockIdx.x * blockDim.x + threadIdx.x; row < m.nv;
          row += gridDim.x * blockDim.x)
     {
         double y[3];
-        row_mul64(d, row, f.p, y);
+        row_mul64(m, row, f.p, y);
 #pragma unroll
         for (int k = 0; k < 3; k++)
             f.q[3 * row + k] = y[k];
-        v[0] += f.p[3 * row] * y[0] + f.p[3 * row + 1] * y[1] + f.p[3 * row + 2] * y[2];
+        v[0] = fma(f.p[3 * row + 2], y[2], fma(f.p[3 * row + 1], y[1], fma(f.p[3 * row], y[0], v[0])));
     }
     double tot[1];
     if (grid_reduce<1>(v, f.part, f.nblk, &f.st->ticket, tot) && threadIdx.x == 0)
@@ -382,8 +413,8 @@ __global__ void __launch_bounds__(kB64) k64_update(const InstDesc *dp, F64Ptr f,
 #pragma unroll
         for (int k = 0; k < 3; k++)
         {
-            f.dx[3 * row + k] += alpha * f.p[3 * row + k];
-            r[k] = f.r[3 * row + k] - alpha * f.q[3 * row + k];
+            f.dx[3 * row + k] = fma(alpha, f.p[3 * row + k], f.dx[3 * row + k]);
+            r[k] = fma(-alpha, f.q[3 * row + k], f.r[3 * row + k]);
             f.r[3 * row + k] = r[k];
         }
 #pragma unroll
@@ -451,7 +482,7 @@ int f64_work(cloth_s *c, F64Work **out)
     {
         auto *p = new cloth_f64_s();
         const int n = c->tab.nv;
-        const int grid = std::max(1, c->ctx->num_sms * 4);
+        const int grid = std::max(1, c->ctx->num_sms * 8);
         Layout L;
         size_t o_dx = L.take<double>(3 * size_t(n)), o_r = L.take<double>(3 * size_t(n)),
                o_z = L.take<double>(3 * size_t(n)), o_p = L.take<double>(3 * size_t(n)),
