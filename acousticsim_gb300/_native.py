@@ -187,6 +187,8 @@ SIGNATURES = {
     "cloth_residual_fp64": (C.c_int, [P, PD]),
     "cloth_solve_refined": (C.c_int, [P, C.POINTER(SolveParams), C.c_double, C.c_int,
                                       C.POINTER(RefineStats)]),
+    "cloth_solve_flexible": (C.c_int, [P, C.POINTER(SolveParams), C.c_double, C.c_int,
+                                      C.POINTER(RefineStats)]),
     "cloth_solve_fp64": (C.c_int, [P, C.POINTER(SolveParams), C.POINTER(SolveStats)]),
     "cloth_server_now": (C.c_double, []),
     "cloth_server_create": (C.c_int, [P, C.POINTER(ServerConfig), C.POINTER(P)]),

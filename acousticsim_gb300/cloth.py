@@ -363,6 +363,14 @@ class BaraffClothGpu:
                C.byref(st))
         return st.as_dict()
 
+    def solve_flexible(self, inner: N.SolveParams, rel_tol: float = 1e-8,
+                       max_outer: int = 100000) -> dict:
+        """FP64 flexible CG with FP32 PCG inner solves (after assemble)."""
+        st = N.RefineStats()
+        N.call("cloth_solve_flexible", self._h, C.byref(inner), float(rel_tol), int(max_outer),
+               C.byref(st))
+        return st.as_dict()
+
     def solve_fp64(self, params: N.SolveParams) -> dict:
         """All-FP64 block-Jacobi PCG from zero (after assemble)."""
         st = N.SolveStats()

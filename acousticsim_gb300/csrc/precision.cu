@@ -358,7 +358,7 @@ __global__ void k64_p(const InstDesc *dp, F64Ptr f)
 
 // q = A p, pq = p.q -> alpha
 __global__ void __launch_bounds__(kB64) k64_spmv(const InstDesc *dp, F64Ptr f,
-                                                 cudaGraphConditionalHandle h)
+                                                 cudaGraphConditionalHandle h, int use_cond)
 {
     const InstDesc &d = *dp;
     if (!f.st->active)
@@ -392,7 +392,7 @@ __global__ void __launch_bounds__(kB64) k64_spmv(const InstDesc *dp, F64Ptr f,
         }
         else
             s.alpha = s.rho / tot[0];
-        if (!s.active)
+        if (!s.active && use_cond)
             cudaGraphSetConditional(h, 0u);
     }
 }
@@ -452,6 +452,83 @@ __global__ void __launch_bounds__(kB64) k64_update(const InstDesc *dp, F64Ptr f,
         if (!s.active)
             cudaGraphSetConditional(h, 0u);
     }
+}
+
+// ---- flexible CG with FP32 PCG inner solves (cloth_solve_flexible)
+// z = the FP32 inner solve's dx (or M r in FP64 when the inner solve failed:
+// NaN or breakdown); rho = z.r and zq = z.q (q = A p of the last outer step);
+// then beta = -zq / pq (Notay's FCG(1): p orthogonalised against the last
+// direction in the A inner product), 0 at the first step.
+__global__ void __launch_bounds__(kB64) k64_fcg_z(const InstDesc *dp, F64Ptr f, int first)
+{
+    const InstDesc &d = *dp;
+    const int st = d.st->status;
+    const bool use_inner = (st == CLOTH_OK || st == CLOTH_ERR_MAXITER);
+    double v[2] = {0.0, 0.0};
+    for (int row = blockIdx.x * blockDim.x + threadIdx.x; row < d.nv;
+         row += gridDim.x * blockDim.x)
+    {
+        double z[3], r[3];
+#pragma unroll
+        for (int k = 0; k < 3; k++)
+            r[k] = f.r[3 * row + k];
+        if (use_inner)
+        {
+            const float4 e = d.dx[row];
+            z[0] = e.x;
+            z[1] = e.y;
+            z[2] = e.z;
+        }
+        else
+        {
+            double m[6];
+#pragma unroll
+            for (int k = 0; k < 6; k++)
+                m[k] = f.M[6 * row + k];
+            symv64(m, r, z);
+        }
+#pragma unroll
+        for (int k = 0; k < 3; k++)
+            f.z[3 * row + k] = z[k];
+        v[0] = fma(z[2], r[2], fma(z[1], r[1], fma(z[0], r[0], v[0])));
+        if (!first)
+            v[1] = fma(z[2], f.q[3 * row + 2],
+                       fma(z[1], f.q[3 * row + 1], fma(z[0], f.q[3 * row], v[1])));
+    }
+    double tot[2];
+    if (grid_reduce<2>(v, f.part, f.nblk, &f.st->ticket, tot) && threadIdx.x == 0)
+    {
+        F64State &s = *f.st;
+        s.rho = tot[0];
+        s.beta = first ? 0.0 : -tot[1] / s.pq;
+        if (!use_inner)
+            s.pad[0]++; // inner solves replaced by M r
+    }
+}
+
+// dx += alpha p, r -= alpha q; rr = r.r
+__global__ void __launch_bounds__(kB64) k64_fcg_update(const InstDesc *dp, F64Ptr f)
+{
+    const InstDesc &d = *dp;
+    if (!f.st->active)
+        return;
+    const double alpha = f.st->alpha;
+    double v[1] = {0.0};
+    for (int row = blockIdx.x * blockDim.x + threadIdx.x; row < d.nv;
+         row += gridDim.x * blockDim.x)
+    {
+#pragma unroll
+        for (int k = 0; k < 3; k++)
+        {
+            f.dx[3 * row + k] = fma(alpha, f.p[3 * row + k], f.dx[3 * row + k]);
+            const double r = fma(-alpha, f.q[3 * row + k], f.r[3 * row + k]);
+            f.r[3 * row + k] = r;
+            v[0] = fma(r, r, v[0]);
+        }
+    }
+    double tot[1];
+    if (grid_reduce<1>(v, f.part, f.nblk, &f.st->ticket, tot) && threadIdx.x == 0)
+        f.st->rr = tot[0];
 }
 
 struct F64Work
@@ -556,7 +633,8 @@ int build_f64_graph(cloth_s *c, F64Work *w)
     void *a_init[] = {&dp, &f};
     void *a_cond[] = {&stc, &h};
     void *a_p[] = {&dp, &f};
-    void *a_spmv[] = {&dp, &f, &h};
+    int one = 1;
+    void *a_spmv[] = {&dp, &f, &h, &one};
     void *a_upd[] = {&dp, &f, &h};
     cudaGraphNode_t last = nullptr;
     rc = add_k(g, &last, (void *)k64_init, w->grid, kB64, a_init);
@@ -818,6 +896,102 @@ int cloth_solve_refined(cloth_t *c, const cloth_solve_params *inner, double rel_
         PCK(cudaGetLastError());
     }
     out.rel_residual = rel;
+    k64_to32<<<grid, 256, 0, s>>>(c->d_desc, w->dx64);
+    PCK(cudaGetLastError());
+    PCK(cudaStreamSynchronize(s));
+    c->dx64_valid = true;
+    c->pcg_stale = true;
+    if (stats)
+        *stats = out;
+    return CLOTH_OK;
+}
+
+int cloth_solve_flexible(cloth_t *c, const cloth_solve_params *inner, double rel_tol,
+                         int max_outer, cloth_refine_stats *stats)
+{
+    int rc = check_solvable(c, "cloth_solve_flexible");
+    if (rc != CLOTH_OK)
+        return rc;
+    if (!inner || inner->max_iters <= 0 || !(rel_tol > 0) || max_outer <= 0)
+        return pfail(CLOTH_ERR_INVALID, "cloth_solve_flexible: bad parameters");
+    std::lock_guard<std::recursive_mutex> lk(c->ctx->mu);
+    PCK(cudaSetDevice(c->ctx->device));
+    F64Work *w = nullptr;
+    rc = f64_work(c, &w);
+    if (rc != CLOTH_OK)
+        return rc;
+    cudaStream_t s = c->ctx->stream;
+    const int grid = w->grid;
+    const InstDesc *dp = c->d_desc;
+    F64Ptr f = w->f;
+    // FP64 start: dx = 0, r = b, the FP64 block-Jacobi inverse (fallback
+    // preconditioner), bb = b.b
+    F64State st0;
+    std::memset(&st0, 0, sizeof(st0));
+    st0.max_iters = 1; // k64_init marks the state active
+    PCK(cudaMemcpyAsync(f.st, &st0, sizeof(st0), cudaMemcpyHostToDevice, s));
+    k64_init<<<grid, kB64, 0, s>>>(dp, f);
+    PCK(cudaGetLastError());
+    F64State hs;
+    rc = sync_read_state(c, w, &hs);
+    if (rc != CLOTH_OK)
+        return rc;
+    const double bb = hs.bb;
+    cloth_refine_stats out;
+    std::memset(&out, 0, sizeof(out));
+    out.status = CLOTH_ERR_MAXITER;
+    out.initial_rel_residual = 1.0;
+    double rel = bb > 0 ? std::sqrt(hs.rr / bb) : 0.0;
+    cudaGraphConditionalHandle none = 0;
+    for (int k = 0; k < max_outer; k++)
+    {
+        if (!std::isfinite(rel))
+        {
+            out.status = CLOTH_ERR_NAN;
+            break;
+        }
+        if (rel <= rel_tol)
+        {
+            out.status = CLOTH_OK;
+            break;
+        }
+        // z ~ A^-1 r by max_iters FP32 PCG iterations from zero
+        cloth_solve_stats is;
+        rc = inner_solve(c, f.r, inner, &is);
+        if (rc != CLOTH_OK)
+            return rc;
+        out.inner_iters += is.iters;
+        out.last_inner_rel_residual = is.rel_residual;
+        k64_fcg_z<<<grid, kB64, 0, s>>>(dp, f, k == 0 ? 1 : 0);
+        k64_p<<<grid, kB64, 0, s>>>(dp, f);
+        k64_spmv<<<grid, kB64, 0, s>>>(dp, f, none, 0);
+        k64_fcg_update<<<grid, kB64, 0, s>>>(dp, f);
+        PCK(cudaGetLastError());
+        rc = sync_read_state(c, w, &hs);
+        if (rc != CLOTH_OK)
+            return rc;
+        out.outer++;
+        rel = bb > 0 ? std::sqrt(hs.rr / bb) : 0.0;
+        out.rejected = hs.pad[0];
+        if (!hs.active)
+        {
+            // p.Ap zero or not finite in the outer step
+            out.status = hs.status ? hs.status : CLOTH_ERR_BREAKDOWN;
+            break;
+        }
+    }
+    if (out.status == CLOTH_ERR_MAXITER && rel <= rel_tol)
+        out.status = CLOTH_OK;
+    // the recurrence residual agrees with the FP64 one to rounding; report
+    // the FP64 residual of the result
+    PCK(cudaMemcpyAsync(w->dx64, f.dx, size_t(c->tab.nv) * 3 * sizeof(double),
+                        cudaMemcpyDeviceToDevice, s));
+    double relt = 0.0;
+    rc = resid(c, w, w->dx64, &relt);
+    if (rc != CLOTH_OK)
+        return rc;
+    out.rel_residual = relt;
+    out.solver = CLOTH_SOLVER_FP64;
     k64_to32<<<grid, 256, 0, s>>>(c->d_desc, w->dx64);
     PCK(cudaGetLastError());
     PCK(cudaStreamSynchronize(s));

@@ -829,9 +829,10 @@ def sparse_direct(sysd):
 
 
 def precision_case(ctx, n, inner_tol, tol, ref_tol, direct: bool, fp32_cap: int,
-                   k_stretch=1e4, k_bend=1e-3):
-    """One assembled ill-conditioned system of an n x n cloth solved four ways:
-    FP32 PCG alone, FP32 PCG inside FP64 iterative refinement, all-FP64 PCG,
+                   k_stretch=1e4, k_bend=1e-3, flex_inner=30):
+    """One assembled ill-conditioned system of an n x n cloth solved five ways:
+    FP32 PCG alone, FP32 PCG inside FP64 iterative refinement, FP64 flexible CG
+    with flex_inner FP32 PCG iterations as its preconditioner, all-FP64 PCG,
     and a reference: a sparse direct solve in FP64 on the host (direct=True)
     or the FP64 PCG run to ref_tol (ref_tol > 0)."""
     from acousticsim_gb300 import BaraffClothGpu, params
@@ -854,18 +855,25 @@ def precision_case(ctx, n, inner_tol, tol, ref_tol, direct: bool, fp32_cap: int,
                       "inner_rel_tol": inner_tol}
     dx_ir = cloth.get_dx()
     t = time.perf_counter()
+    st = cloth.solve_flexible(params(max_iters=flex_inner, rel_tol=0.0, warm_start=0), tol,
+                              100000)
+    out["flexible"] = {"seconds": time.perf_counter() - t, **st, "inner_iters_per_outer": flex_inner}
+    dx_fx = cloth.get_dx()
+    t = time.perf_counter()
     st = cloth.solve_fp64(params(max_iters=200000, rel_tol=tol))
     out["fp64_pcg"] = {"seconds": time.perf_counter() - t, "iters": st["iters"],
                        "status": st["status"], "fp64_rel_residual": cloth.residual_fp64()}
     dx_64 = cloth.get_dx()
     out["refined_vs_fp64_pcg"] = rel(dx_ir, dx_64)
+    out["flexible_vs_fp64_pcg"] = rel(dx_fx, dx_64)
     if direct:
         t = time.perf_counter()
         # the exported system is the assembled one; the PCG state does not matter
         cloth.assemble(1e-2)
         x_d = sparse_direct(cloth.export_system())
         out["direct"] = {"seconds_host": time.perf_counter() - t,
-                         "refined_error": rel(dx_ir, x_d), "fp64_pcg_error": rel(dx_64, x_d)}
+                         "refined_error": rel(dx_ir, x_d), "flexible_error": rel(dx_fx, x_d),
+                         "fp64_pcg_error": rel(dx_64, x_d)}
     elif ref_tol > 0:
         t = time.perf_counter()
         st = cloth.solve_fp64(params(max_iters=300000, rel_tol=ref_tol))
@@ -873,6 +881,7 @@ def precision_case(ctx, n, inner_tol, tol, ref_tol, direct: bool, fp32_cap: int,
         out["fp64_reference"] = {"rel_tol": ref_tol, "iters": st["iters"],
                                  "seconds": time.perf_counter() - t,
                                  "refined_error": rel(dx_ir, x_ref),
+                                 "flexible_error": rel(dx_fx, x_ref),
                                  "fp64_pcg_error": rel(dx_64, x_ref)}
     cloth.close()
     return out
@@ -887,24 +896,30 @@ def run_precision(args):
     from acousticsim_gb300 import build as b
     b.build_all()
     ctx = ClothContext(0)
+    fi = args.prec_flex_inner
     big = precision_case(ctx, args.prec_side, args.prec_inner_tol, 1e-8, 1e-12, False,
-                         args.prec_fp32_cap)
+                         args.prec_fp32_cap, flex_inner=fi)
     # the same ratio with the single-cloth stretch stiffness (1e3 / 1e-4): a
     # ten times better conditioned system
     milder = precision_case(ctx, args.prec_side, args.prec_inner_tol, 1e-8, 0.0, False,
-                            args.prec_fp32_cap, k_stretch=1e3, k_bend=1e-4)
+                            args.prec_fp32_cap, k_stretch=1e3, k_bend=1e-4, flex_inner=fi)
     small = precision_case(ctx, args.prec_direct_side, args.prec_inner_tol, 1e-8, 0.0,
-                           True, args.prec_fp32_cap)
+                           True, args.prec_fp32_cap, flex_inner=fi)
     # the value: the fastest of the GPU solvers that reached 1e-8 (FP64-checked)
-    reached = [(big[m]["seconds"], m) for m in ("refined", "fp64_pcg")
+    reached = [(big[m]["seconds"], m) for m in ("refined", "flexible", "fp64_pcg")
                if big[m]["status"] == "OK"]
     best = min(reached) if reached else (None, None)
     line = {"metric": f"precision stress: seconds to 1e-8 FP64 residual, {args.prec_side}^2, "
                       "stiffness ratio 1e7, dt 10 ms",
             "value": best[0], "method": best[1], "unit": "s", "n_gpus": 1,
-            "higher_is_better": False, "dtype": "f32 PCG inside f64 refinement; f64 PCG",
+            "higher_is_better": False, "dtype": "f32 PCG inside f64 refinement; f64 flexible CG over f32 PCG; f64 PCG",
             "data": "synthetic (seeded perturbation)",
             "refined_reached_tol": big["refined"]["status"] == "OK",
+            "flexible_speedup_vs_fp64_pcg": {
+                k: (v["fp64_pcg"]["seconds"] / v["flexible"]["seconds"]
+                    if v["flexible"]["status"] == "OK" else None)
+                for k, v in (("full_size", big), ("full_size_stretch_1e3", milder),
+                             ("direct_check", small))},
             "refined_speedup_vs_fp64_pcg": {
                 k: (v["fp64_pcg"]["seconds"] / v["refined"]["seconds"]
                     if v["refined"]["status"] == "OK" else None)
@@ -1036,6 +1051,8 @@ def main():
     ap.add_argument("--prec-side", type=int, default=1024)
     ap.add_argument("--prec-direct-side", type=int, default=256)
     ap.add_argument("--prec-inner-tol", type=float, default=1e-4)
+    ap.add_argument("--prec-flex-inner", type=int, default=30,
+                    help="FP32 PCG iterations per flexible-CG step (precision mode)")
     ap.add_argument("--prec-fp32-cap", type=int, default=100000)
     ap.add_argument("--serve-light-rate", type=float, default=300.0,
                     help="second, sustainable Poisson stream (req/s; 0: skip)")

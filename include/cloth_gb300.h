@@ -339,6 +339,17 @@ int cloth_solve_refined(cloth_t *cloth, const cloth_solve_params *inner, double 
  * reductions) from dx = 0, for comparison; recurrence residual in stats. */
 int cloth_solve_fp64(cloth_t *cloth, const cloth_solve_params *params,
                      cloth_solve_stats *stats);
+/* Flexible CG in FP64 (Notay's FCG(1): each direction A-orthogonalised
+ * against the last) preconditioned by inner->max_iters FP32 PCG iterations
+ * from zero on the same assembled system; FP64 vectors and SpMV, stop at
+ * ||r|| <= rel_tol ||b|| (FP64), at most max_outer FP64 iterations.  Meant
+ * for systems too ill-conditioned for the FP32 corrections of
+ * cloth_solve_refined.  stats: outer = FP64 iterations, inner_iters = FP32
+ * iterations, rejected = inner solves that failed (NaN, breakdown) and were
+ * replaced by the FP64 block-Jacobi step; rel_residual is the FP64 residual of
+ * the result.  The FP64 dx is what cloth_get_dx and cloth_advance use. */
+int cloth_solve_flexible(cloth_t *cloth, const cloth_solve_params *inner, double rel_tol,
+                         int max_outer, cloth_refine_stats *stats);
 
 /* ---------------------------------------------------------------- collisions */
 /* Static kinematic bodies (cKinematicBody after Init, src/sim/kinematic/

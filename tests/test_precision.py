@@ -124,3 +124,44 @@ def test_advance_uses_the_fp64_result(ctx):
     c.advance()
     assert np.array_equal(c.GetPos(), x0 + dx)
     assert np.array_equal(c.GetPrePos(), x0)
+
+
+@pytest.mark.parametrize("k_stretch", [1e5, 1e7])
+def test_flexible_cg_matches_direct_solve(ctx, k_stretch):
+    """FP64 flexible CG with FP32 PCG inner solves reaches an FP64 residual
+    of 1e-10 in fewer FP64 iterations than the FP64 PCG needs for 1e-8, on
+    the answer of the direct solve.  (Its error at a given residual is larger
+    than the PCG's: the truncated recurrence does not minimise the A-norm
+    error, so the tolerance here is two orders tighter.)"""
+    from acousticsim_gb300 import BaraffClothGpu, params
+    c = BaraffClothGpu(ctx, _conf(48, k_stretch=k_stretch))
+    rng = np.random.default_rng(17)
+    x0 = c.GetInitPos().reshape(-1, 3)
+    c.SetPos((x0 + rng.normal(0, 1e-3, x0.shape)).reshape(-1))
+    c.SetPrePos(c.GetPos() - 1e-2 * rng.normal(0, 1e-2, x0.size))
+    c.assemble(1e-2)
+    M, b, x_direct = _direct(c.export_system())
+    tol = 1e-2 * REL_TOL
+    st = c.solve_flexible(params(max_iters=30, rel_tol=0.0, warm_start=0), tol, 2000)
+    assert st["status"] == "OK" and st["solver"] == "fp64", st
+    assert st["rel_residual"] <= tol and st["rejected"] == 0, st
+    assert st["inner_iters"] <= 30 * st["outer"]
+    dx = c.get_dx()
+    r_host = np.linalg.norm(b - M @ dx) / np.linalg.norm(b)
+    assert r_host <= 2 * tol
+    err = _rel(dx, x_direct)
+    st64 = c.solve_fp64(params(max_iters=100000, rel_tol=REL_TOL))
+    print(f"flexible: {st}, true residual {r_host:.2e}, error vs direct {err:.2e}; "
+          f"fp64 pcg iterations {st64['iters']}")
+    assert err < 1e-5
+    assert _rel(c.get_dx(), dx) < 1e-4
+    assert st["outer"] < st64["iters"]
+
+
+def test_flexible_cg_refuses_bad_parameters(ctx):
+    from acousticsim_gb300 import ClothError, params
+    c = _assembled(ctx, n=8)
+    with pytest.raises(ClothError):
+        c.solve_flexible(params(max_iters=0), REL_TOL, 10)
+    with pytest.raises(ClothError):
+        c.solve_flexible(params(max_iters=10), 0.0, 10)
