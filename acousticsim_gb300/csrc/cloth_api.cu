@@ -718,7 +718,9 @@ int plan_persistent(cloth_ctx *ctx, Batch *b)
     const size_t smem_cap_bytes =
         std::min<size_t>(size_t(std::max(ctx->max_smem_optin, 48 * 1024)) - 4096,
                          200 * 1024);
-    const int cap_entries = int(smem_cap_bytes / sizeof(float4));
+    // per-chunk partial sums (3 floats per 32-row chunk) follow the staged state
+    const size_t part_max = 3 * size_t(kMaxBlockRows / kRedRows) * sizeof(float);
+    const int cap_entries = int((smem_cap_bytes - part_max) / sizeof(float4));
     // occupancy at the largest staging size we may request
     int occ = 0;
     if (cudaFuncSetAttribute(k_pcg_persistent_sm, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -842,10 +844,13 @@ int plan_persistent(cloth_ctx *ctx, Batch *b)
     // carve-out, and the L1 left for the matrix and gathers halves.)
     b->halo_cap = max_entries;
     b->rows_cap = max_rows;
+    const size_t part_bytes =
+        align_up(3 * size_t((max_rows + kRedRows - 1) / kRedRows) * sizeof(float), 16);
     const size_t sm_bytes = size_t(max_entries) * sizeof(float4) +
-                            size_t(max_rows) * (kPersistMShared ? 72 : 48);
+                            size_t(max_rows) * (kPersistMShared ? 72 : 48) + part_bytes;
     b->persist_sm = sm_bytes <= smem_cap_bytes;
-    b->smem_persist = b->persist_sm ? sm_bytes : size_t(max_entries) * sizeof(float4);
+    b->smem_persist =
+        b->persist_sm ? sm_bytes : size_t(max_entries) * sizeof(float4) + part_bytes;
     // the single-barrier variant keeps dx, p and M^-1 per own row (56 bytes)
     // next to u over the halo: it fits wherever the two-barrier one does
     // (it has no skew block parts: launch sets with a dihedral-bending

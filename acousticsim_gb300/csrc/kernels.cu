@@ -1546,8 +1546,6 @@ __device__ __forceinline__ void pcg_persistent_body(InstDesc *const *descs,
     constexpr int NW = kPBlock / 32;
     extern __shared__ float4 sm_dyn[];
     __shared__ InstDesc d;
-    __shared__ unsigned long long wsum_h[2][kPBlock / 32], wsum_l[2][kPBlock / 32];
-    __shared__ float wsum_c[2][kPBlock / 32];
     // FP64 PCG scalars: owned by thread 0, the block reads the FP32 copies
     __shared__ double s_rho, s_beta, s_alpha, s_pq, s_rr;
     __shared__ float bc_af, bc_bf;
@@ -1568,6 +1566,12 @@ __device__ __forceinline__ void pcg_persistent_body(InstDesc *const *descs,
     float4 *sq = sr + rows_cap;
     float4 *sm0 = sq + rows_cap;
     float2 *sm1 = reinterpret_cast<float2 *>(sm0 + rows_cap);
+    // FP32 sums of the 32-row chunks, one array per quantity (p.q, r.z, r.r):
+    // kept in shared memory rather than in per-thread accumulators, which
+    // leaves the SpMV loop its registers
+    const int cps = (rows_cap + 31) / 32;
+    float *cpart = reinterpret_cast<float *>(
+        SM ? (kPersistMShared ? reinterpret_cast<float4 *>(sm1 + rows_cap) : sm0) : sdx);
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const unsigned long long keep = l2_keep_policy();
@@ -1597,26 +1601,28 @@ __device__ __forceinline__ void pcg_persistent_body(InstDesc *const *descs,
     }
     int it = 0, status = 0;
 
-    // Team sum of NQ quantities (q0.. in the accumulator): lane 0 of every
-    // warp leaves its fixed-point partials in shared memory, thread 0 folds
-    // them (exact integer adds) and sends one reduction per limb to the team
-    // buffer, then the team barrier. Returns false when the barrier gave up.
-    auto team_sum = [&](auto &wfx, int nq, int q0, int bq) -> bool {
-        if (lane == 0)
-            for (int q = 0; q < nq; q++)
-            {
-                wsum_h[q][warp] = (unsigned long long)wfx.H[q];
-                wsum_l[q][warp] = wfx.L[q];
-                wsum_c[q][warp] = wfx.chk[q];
-            }
+    // Team sum of nq quantities (q0.. of the chunk sums): warp 0 turns every
+    // chunk sum into fixed point (scale s of its quantity) and folds them
+    // (exact integer adds: any order gives the same limbs), lane 0 sends one
+    // reduction per limb to the team buffer, then the team barrier. Returns
+    // false when the barrier gave up.
+    auto team_sum = [&](int nq, int q0, int bq, const int *sc) -> bool {
         __syncthreads();
-        // warp 0 folds the 32 warps' limbs (integer adds: any order is exact)
-        static_assert(NW == 32, "one lane per warp");
         if (warp == 0)
             for (int q = 0; q < nq; q++)
             {
-                unsigned long long h = wsum_h[q][lane], l = wsum_l[q][lane];
-                float c = wsum_c[q][lane];
+                unsigned long long h = 0ull, l = 0ull;
+                float c = 0.f;
+                for (int ch = lane; ch < nch; ch += 32)
+                {
+                    const float v = cpart[(q0 + q) * cps + ch];
+                    long long hh;
+                    unsigned long long ll;
+                    fx_split(v, sc[q], hh, ll);
+                    h += (unsigned long long)hh;
+                    l += ll;
+                    c += v;
+                }
 #pragma unroll
                 for (int o = 16; o > 0; o >>= 1)
                 {
@@ -1687,8 +1693,6 @@ __device__ __forceinline__ void pcg_persistent_body(InstDesc *const *descs,
         __syncthreads();
         const int s0q = bc_s[0], s1q = bc_s[1], s2q = bc_s[2];
         // ---- q = A p on own rows; p.q per 32-row chunk
-        WarpFx<1> f1;
-        f1.clear();
         for (int ch = warp; ch < nch; ch += NW)
         {
             const int li = ch * 32 + lane;
@@ -1789,9 +1793,9 @@ __device__ __forceinline__ void pcg_persistent_body(InstDesc *const *descs,
             }
             part = warp_sum(part);
             if (lane == 0)
-                f1.add(0, part, s0q);
+                cpart[ch] = part;
         }
-        if (!team_sum(f1, 1, 0, bq))
+        if (!team_sum(1, 0, bq, &s0q))
         {
             status = 9; // CLOTH_ERR_TIMEOUT
             break;
@@ -1819,8 +1823,6 @@ __device__ __forceinline__ void pcg_persistent_body(InstDesc *const *descs,
         }
         const float af = bc_af;
         // ---- dx += alpha p, r -= alpha q, z = M^-1 r; r.z and r.r per chunk
-        WarpFx<2> f2;
-        f2.clear();
         for (int ch = warp; ch < nch; ch += NW)
         {
             const int li = ch * 32 + lane;
@@ -1868,11 +1870,12 @@ __device__ __forceinline__ void pcg_persistent_body(InstDesc *const *descs,
             prr = warp_sum(prr);
             if (lane == 0)
             {
-                f2.add(0, pr, s1q);
-                f2.add(1, prr, s2q);
+                cpart[cps + ch] = pr;
+                cpart[2 * cps + ch] = prr;
             }
         }
-        if (!team_sum(f2, 2, 1, bq))
+        const int s12[2] = {s1q, s2q};
+        if (!team_sum(2, 1, bq, s12))
         {
             status = 9;
             break;
