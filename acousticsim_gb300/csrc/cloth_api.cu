@@ -869,7 +869,9 @@ int plan_persistent(cloth_ctx *ctx, Batch *b)
         cudaGetLastError();
         return CLOTH_OK;
     }
-    CK(cudaMalloc(&b->d_work, work.size() * sizeof(TeamBlock)));
+    // the work list, then one arrival count per block slot (the team barrier
+    // of the two-barrier kernels), zeroed before every launch
+    CK(cudaMalloc(&b->d_work, work.size() * (sizeof(TeamBlock) + sizeof(unsigned long long))));
     CK(cudaMemcpy(b->d_work, work.data(), work.size() * sizeof(TeamBlock),
                   cudaMemcpyHostToDevice));
     b->grid_persist = int(work.size());
@@ -947,6 +949,22 @@ int build_graph(Batch *b, bool full, cudaGraphExec_t *exec)
     if (b->persist_ok)
     {
         void *a_per[] = {&b->d_descs, &b->d_work, &b->halo_cap, &b->rows_cap};
+        if (rc == CLOTH_OK)
+        {
+            // the team barriers' arrival counts start at zero
+            cudaMemsetParams mp;
+            std::memset(&mp, 0, sizeof(mp));
+            mp.dst = b->d_work + b->grid_persist;
+            mp.value = 0;
+            mp.elementSize = 4;
+            mp.width = size_t(b->grid_persist) * 2;
+            mp.height = 1;
+            if (cudaGraphAddMemsetNode(&n, g, last ? &last : nullptr, last ? 1 : 0, &mp) !=
+                cudaSuccess)
+                rc = fail(CLOTH_ERR_CUDA, "cudaGraphAddMemsetNode failed");
+            else
+                last = n;
+        }
         if (rc == CLOTH_OK)
         {
             cudaKernelNodeParams p;
@@ -1042,6 +1060,8 @@ int launch_persistent(Batch *b)
     cloth_ctx *ctx = b->ctx;
     PhaseTimer t(ctx, PH_SPMV);
     void *args[] = {&b->d_descs, &b->d_work, &b->halo_cap, &b->rows_cap};
+    CK(cudaMemsetAsync(b->d_work + b->grid_persist, 0,
+                       size_t(b->grid_persist) * sizeof(unsigned long long), ctx->stream));
     CK(cudaLaunchCooperativeKernel(persistent_kernel(b),
                                    dim3(b->grid_persist), dim3(kPBlock), args,
                                    b->smem_persist, ctx->stream));

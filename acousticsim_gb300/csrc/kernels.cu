@@ -1405,6 +1405,50 @@ __device__ __forceinline__ bool team_barrier(InstState *st, int nblk)
     return ok != 0;
 }
 
+// Barrier of the two-barrier persistent kernels: a monotonic arrival count
+// per team (zeroed before every launch); barrier k of a launch waits for
+// k * nblk arrivals. One thread per block arrives with a release reduction
+// (it covers the writes the CTA barrier ordered before it, the partial sums
+// included) and polls with acquire loads; no thread waits for its own
+// arrival to return. Returns false when the bounded wait gave up (the team's
+// error flag is set then).
+__device__ __forceinline__ bool team_barrier_count(unsigned long long *count,
+                                                   unsigned long long target, InstState *st,
+                                                   int nblk)
+{
+    __shared__ int ok;
+    __syncthreads();
+    if (threadIdx.x == 0)
+    {
+        ok = 1;
+        if (nblk > 1)
+        {
+            asm volatile("red.release.gpu.global.add.u64 [%0], 1;" ::"l"(count) : "memory");
+            unsigned n = 0;
+            for (;;)
+            {
+                unsigned long long v;
+                asm volatile("ld.acquire.gpu.global.u64 %0, [%1];"
+                             : "=l"(v)
+                             : "l"(count)
+                             : "memory");
+                if (v >= target)
+                    break;
+                if (++n > kSpinLimit)
+                {
+                    atomicExch(&st->bar_err, 1);
+                    ok = 0;
+                    break;
+                }
+                if (n > 256)
+                    __nanosleep(32);
+            }
+        }
+    }
+    __syncthreads();
+    return ok != 0;
+}
+
 __device__ __forceinline__ float4 ldcg4(const float4 *p) { return __ldcg(p); }
 
 // Loads of the matrix carry an L2 evict_last policy: A is re-read every PCG
@@ -1600,6 +1644,15 @@ __device__ __forceinline__ void pcg_persistent_body(InstDesc *const *descs,
         bc_bf = 0.f;
     }
     int it = 0, status = 0;
+    // the team's arrival count: after the work list, one word per block slot,
+    // the team using its first block's
+    __shared__ unsigned long long s_nbar; // arrivals barrier k waits for (thread 0)
+    if (tid == 0)
+        s_nbar = 0ull;
+    auto team_count = [&]() {
+        return reinterpret_cast<unsigned long long *>(const_cast<TeamBlock *>(work) + gridDim.x) +
+               (blockIdx.x - w.rank);
+    };
 
     // Team sum of nq quantities (q0.. of the chunk sums): warp 0 turns every
     // chunk sum into fixed point (scale s of its quantity) and folds them
@@ -1637,7 +1690,9 @@ __device__ __forceinline__ void pcg_persistent_body(InstDesc *const *descs,
                     atomicAdd(&st->acc_chk[bq][q0 + q], c);
                 }
             }
-        return team_barrier(st, w.nblk);
+        if (tid == 0)
+            s_nbar += (unsigned long long)w.nblk;
+        return team_barrier_count(team_count(), s_nbar, st, w.nblk);
     };
     // Reads a team sum after the barrier; flags a fixed-point overflow when it
     // disagrees with the FP32 magnitude check.
