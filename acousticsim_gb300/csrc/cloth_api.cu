@@ -819,9 +819,10 @@ int plan_persistent(cloth_ctx *ctx, Batch *b)
             }
             w.halo0 = lo;
             w.halo1 = hi + 1;
-            w.pad = 0;
+            w.p_global = 0;
             team.push_back(w);
         }
+        bool team_staged = true;
         for (auto &w : team)
         {
             w.nblk = int(team.size());
@@ -830,9 +831,17 @@ int plan_persistent(cloth_ctx *ctx, Batch *b)
             {
                 w.halo0 = w.halo1 = -1;
                 all_staged = false;
+                team_staged = false;
             }
             else
                 max_entries = std::max(max_entries, w.halo1 - w.halo0);
+        }
+        // staged blocks keep p over their halo in shared memory from one
+        // iteration to the next; a block that reads p from global memory needs
+        // its neighbours to write it there
+        for (auto &w : team)
+        {
+            w.p_global = team_staged ? 0 : 1;
             work.push_back(w);
         }
     }

@@ -187,7 +187,7 @@ struct TeamBlock
     int nblk;   // team size
     int row0, row1;
     int halo0, halo1;
-    int pad;
+    int p_global; // the team keeps p in global memory (a block of it is not staged)
 };
 
 // Fixed-point scale: sums are carried as round(v * 2^s) with s chosen from
@@ -201,6 +201,7 @@ constexpr int kPBlock = 1024;                // threads per persistent block
 constexpr bool kPersistMShared = true; // measured: false is 3 % slower at 512^2
 constexpr int kRedRows = 32;                 // team ranges align to 32-row chunks (the FP32 warp sums)
 constexpr int kSlotUnroll = 2;               // ELL slots whose loads are issued together
+constexpr int kStageUnroll = 2;              // staged z rows per thread loaded together
 constexpr int kMaxBlockRows = 16384;         // rows one persistent block may own
 constexpr unsigned kSpinLimit = 1u << 25;    // bounded barrier wait (~seconds)
 

@@ -1654,15 +1654,17 @@ __device__ __forceinline__ void pcg_persistent_body(InstDesc *const *descs,
                (blockIdx.x - w.rank);
     };
 
-    // Team sum of nq quantities (q0.. of the chunk sums): warp 0 turns every
-    // chunk sum into fixed point (scale s of its quantity) and folds them
-    // (exact integer adds: any order gives the same limbs), lane 0 sends one
-    // reduction per limb to the team buffer, then the team barrier. Returns
-    // false when the barrier gave up.
-    auto team_sum = [&](int nq, int q0, int bq, const int *sc) -> bool {
+    // Team sum of nq quantities (q0.. of the chunk sums): warp q turns every
+    // chunk sum of quantity q0 + q into fixed point (scale sc[q]) and folds
+    // them (exact integer adds: any order gives the same limbs), its lane 0
+    // sends one reduction per limb to the team buffer, then the team barrier.
+    // Returns false when the barrier gave up.
+    auto team_sum = [&](int nq, int q0, int bq, int sc0, int sc1) -> bool {
         __syncthreads();
-        if (warp == 0)
-            for (int q = 0; q < nq; q++)
+        if (warp < nq)
+        {
+            const int q = warp;
+            const int sq = q == 0 ? sc0 : sc1;
             {
                 unsigned long long h = 0ull, l = 0ull;
                 float c = 0.f;
@@ -1671,7 +1673,7 @@ __device__ __forceinline__ void pcg_persistent_body(InstDesc *const *descs,
                     const float v = cpart[(q0 + q) * cps + ch];
                     long long hh;
                     unsigned long long ll;
-                    fx_split(v, sc[q], hh, ll);
+                    fx_split(v, sq, hh, ll);
                     h += (unsigned long long)hh;
                     l += ll;
                     c += v;
@@ -1690,6 +1692,7 @@ __device__ __forceinline__ void pcg_persistent_body(InstDesc *const *descs,
                     atomicAdd(&st->acc_chk[bq][q0 + q], c);
                 }
             }
+        }
         if (tid == 0)
             s_nbar += (unsigned long long)w.nblk;
         return team_barrier_count(team_count(), s_nbar, st, w.nblk);
@@ -1730,21 +1733,40 @@ __device__ __forceinline__ void pcg_persistent_body(InstDesc *const *descs,
                 }
             }
         }
-        // ---- p = z + beta p_old over the staged range
+        // ---- p = z + beta p_old over the staged range. The staged p of the
+        // last iteration is still in shared memory (every block computes p of
+        // a row with the same operation on the same values as its owner), so
+        // only z is read; kStageUnroll rows per thread have their loads in
+        // flight together.
         if (staged)
-            for (int i = tid; i < w.halo1 - w.halo0; i += kPBlock)
+        {
+            const int nh = w.halo1 - w.halo0;
+            for (int i0 = tid; i0 < nh; i0 += kStageUnroll * kPBlock)
             {
-                const int c = w.halo0 + i;
-                float4 pn = ldcg4(d.z + c);
-                if (!first)
+                float4 zz[kStageUnroll];
+#pragma unroll
+                for (int u = 0; u < kStageUnroll; u++)
+                    if (i0 + u * kPBlock < nh)
+                        zz[u] = ldcg4(d.z + w.halo0 + i0 + u * kPBlock);
+#pragma unroll
+                for (int u = 0; u < kStageUnroll; u++)
                 {
-                    const float4 po = ldcg4(pold + c);
-                    pn.x = fmaf(bf, po.x, pn.x);
-                    pn.y = fmaf(bf, po.y, pn.y);
-                    pn.z = fmaf(bf, po.z, pn.z);
+                    const int i = i0 + u * kPBlock;
+                    if (i < nh)
+                    {
+                        float4 pn = zz[u];
+                        if (!first)
+                        {
+                            const float4 po = sp[i];
+                            pn.x = fmaf(bf, po.x, pn.x);
+                            pn.y = fmaf(bf, po.y, pn.y);
+                            pn.z = fmaf(bf, po.z, pn.z);
+                        }
+                        sp[i] = pn;
+                    }
                 }
-                sp[i] = pn;
             }
+        }
         __syncthreads();
         const int s0q = bc_s[0], s1q = bc_s[1], s2q = bc_s[2];
         // ---- q = A p on own rows; p.q per 32-row chunk
@@ -1769,7 +1791,8 @@ __device__ __forceinline__ void pcg_persistent_body(InstDesc *const *descs,
                                          fmaf(bf, po.z, zz.z));
                     }
                 }
-                pnew[row] = f4(pv);
+                if (!staged || w.p_global)
+                    pnew[row] = f4(pv);
                 const int info = ld_keep(d.rowinfo + row, keep);
                 const int len = info & 255, ds = (info >> 8) & 255;
                 float3 q = make_float3(0, 0, 0);
@@ -1850,7 +1873,7 @@ __device__ __forceinline__ void pcg_persistent_body(InstDesc *const *descs,
             if (lane == 0)
                 cpart[ch] = part;
         }
-        if (!team_sum(1, 0, bq, &s0q))
+        if (!team_sum(1, 0, bq, s0q, s0q))
         {
             status = 9; // CLOTH_ERR_TIMEOUT
             break;
@@ -1929,8 +1952,7 @@ __device__ __forceinline__ void pcg_persistent_body(InstDesc *const *descs,
                 cpart[2 * cps + ch] = prr;
             }
         }
-        const int s12[2] = {s1q, s2q};
-        if (!team_sum(2, 1, bq, s12))
+        if (!team_sum(2, 1, bq, s1q, s2q))
         {
             status = 9;
             break;
