@@ -1741,15 +1741,18 @@ __device__ __forceinline__ void pcg_persistent_body(InstDesc *const *descs,
         if (staged)
         {
             const int nh = w.halo1 - w.halo0;
-            for (int i0 = tid; i0 < nh; i0 += kStageUnroll * kPBlock)
+            // (the skew kernels, one more plane in the SpMV, have no registers
+            // for a second row)
+            constexpr int SU = SKEW ? 1 : kStageUnroll;
+            for (int i0 = tid; i0 < nh; i0 += SU * kPBlock)
             {
-                float4 zz[kStageUnroll];
+                float4 zz[SU];
 #pragma unroll
-                for (int u = 0; u < kStageUnroll; u++)
+                for (int u = 0; u < SU; u++)
                     if (i0 + u * kPBlock < nh)
                         zz[u] = ldcg4(d.z + w.halo0 + i0 + u * kPBlock);
 #pragma unroll
-                for (int u = 0; u < kStageUnroll; u++)
+                for (int u = 0; u < SU; u++)
                 {
                     const int i = i0 + u * kPBlock;
                     if (i < nh)
