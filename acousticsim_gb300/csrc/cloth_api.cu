@@ -921,6 +921,7 @@ int build_graph(Batch *b, bool full, cudaGraphExec_t *exec)
     void *a_row[] = {&b->d_descs, &b->d_rt, &b->d_ctl};
     void *a_cond[] = {&b->d_ctl, &hnd};
     void *a_spmv[] = {&b->d_descs, &b->d_rt, &b->d_ctl, &one, &hnd};
+    void *a_red[] = {&b->d_descs, &b->d_inst, &ninst, &no_count, &b->d_ctl, &one, &hnd};
     int *no_left = nullptr;
     void *a_upd[] = {&b->d_descs, &b->d_rt, &b->d_ctl, &one, &hnd, &no_left};
     void *a_adv[] = {&b->d_descs, &b->d_rt, &b->d_ctl, &all_rows};
@@ -1015,11 +1016,17 @@ int build_graph(Batch *b, bool full, cudaGraphExec_t *exec)
             cudaGraphNode_t k1, k2;
             const GraphLoopVariant &sv = b->spmv_variant(b->spmv_v);
             const GraphLoopVariant &uv = kUpdateVariants[b->upd_v];
+            cudaGraphNode_t k3, k4;
+            const int gred = reduce_grid(ninst);
             rc = add_kernel(body, &k1, nullptr, 0, const_cast<void *>(sv.func), b->grid_spmv,
                             kTile / sv.rows_per_thread, a_spmv);
             if (rc == CLOTH_OK)
-                rc = add_kernel(body, &k2, &k1, 1, const_cast<void *>(uv.func),
+                rc = add_kernel(body, &k3, &k1, 1, (void *)k_reduce_pq, gred, kTile, a_red);
+            if (rc == CLOTH_OK)
+                rc = add_kernel(body, &k2, &k3, 1, const_cast<void *>(uv.func),
                                 b->grid_update, kTile / uv.rows_per_thread, a_upd);
+            if (rc == CLOTH_OK)
+                rc = add_kernel(body, &k4, &k2, 1, (void *)k_reduce_rz, gred, kTile, a_red);
             last = cn;
         }
     }
@@ -1088,6 +1095,10 @@ int launch_solve_host(Batch *b, int max_iters)
     int *no_left = nullptr;
     void *a_spmv[] = {&b->d_descs, &b->d_rt, &b->d_ctl, &zero, &none};
     void *a_upd[] = {&b->d_descs, &b->d_rt, &b->d_ctl, &zero, &none, &no_left};
+    int ninst = int(b->members.size());
+    const int *no_count = nullptr;
+    void *a_red[] = {&b->d_descs, &b->d_inst, &ninst, &no_count, &b->d_ctl, &zero, &none};
+    const int gred = reduce_grid(ninst);
     const GraphLoopVariant &sv = b->spmv_variant(b->spmv_v);
     const GraphLoopVariant &uv = kUpdateVariants[b->upd_v];
     int *h_active = nullptr;
@@ -1102,11 +1113,13 @@ int launch_solve_host(Batch *b, int max_iters)
                 PhaseTimer t(ctx, PH_SPMV);
                 cudaLaunchKernel(sv.func, dim3(b->grid_spmv), dim3(kTile / sv.rows_per_thread),
                                  a_spmv, 0, s);
+                cudaLaunchKernel((const void *)k_reduce_pq, dim3(gred), dim3(kTile), a_red, 0, s);
             }
             {
                 PhaseTimer t(ctx, PH_UPDATE);
                 cudaLaunchKernel(uv.func, dim3(b->grid_update),
                                  dim3(kTile / uv.rows_per_thread), a_upd, 0, s);
+                cudaLaunchKernel((const void *)k_reduce_rz, dim3(gred), dim3(kTile), a_red, 0, s);
             }
         }
         if (cudaMemcpyAsync(h_active, &b->d_ctl->n_active, sizeof(int),
@@ -1285,6 +1298,13 @@ int autotune_graph_loop(Batch *b)
     cudaLaunchKernel(b->spmv_variant(best_s).func,
                      dim3(b->grid_for(b->spmv_variant(best_s), b->spmv_occ(best_s), best_sw)),
                      dim3(kTile / b->spmv_variant(best_s).rows_per_thread), a_spmv, 0, s);
+    {
+        const int *no_count = nullptr;
+        int ni = ninst;
+        void *a_red[] = {&b->d_descs, &b->d_inst, &ni, &no_count, &b->d_ctl, &zero, &none};
+        cudaLaunchKernel((const void *)k_reduce_pq, dim3(reduce_grid(ninst)), dim3(kTile), a_red,
+                         0, s);
+    }
     snap(0);
     t_best = 1e30f;
     for (int v = 0; v < kNumUpdateVariants; v++)

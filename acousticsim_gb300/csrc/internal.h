@@ -22,6 +22,16 @@ __global__ void k_pins(InstDesc *const *descs, const int *inst_list, int ninst,
 __global__ void k_tri(InstDesc *const *descs, const Tile *tiles, const BatchCtl *ctl);
 __global__ void k_row(InstDesc *const *descs, const Tile *tiles, BatchCtl *ctl);
 __global__ void k_cond(const BatchCtl *ctl, cudaGraphConditionalHandle h);
+// instance totals after the graph-loop SpMV (p.q -> alpha) and update (r.z,
+// r.r -> beta, convergence): one block per instance of inst_list (ninst of
+// them, or *ninst_dev when that is not null)
+__global__ void k_reduce_pq(InstDesc *const *descs, const int *inst_list, int ninst,
+                            const int *ninst_dev, BatchCtl *ctl, int use_cond,
+                            cudaGraphConditionalHandle h);
+__global__ void k_reduce_rz(InstDesc *const *descs, const int *inst_list, int ninst,
+                            const int *ninst_dev, BatchCtl *ctl, int use_cond,
+                            cudaGraphConditionalHandle h);
+inline int reduce_grid(int ninst) { return ninst < 1 ? 1 : (ninst > 1024 ? 1024 : ninst); }
 // graph-loop kernel variants (k_spmv_t<R, U>, k_update_t<R>); arguments:
 //   spmv  (descs, tiles, ctl, use_cond, handle)
 //   update(descs, tiles, ctl, use_cond, handle, iters_left)

@@ -847,40 +847,21 @@ __device__ __forceinline__ void group_sum_d(double (&vv)[R][N], double (&v)[N],
     __syncthreads();
 }
 
-// tile_reduce for R rows per thread (same order as tile_reduce); the
-// instance's partials, tile count and state come from the caller's header.
+// The tile's partial sums of the graph-loop kernels (group_sum: the same
+// block sums for every kernel variant); the instance totals are formed by
+// k_reduce_pq / k_reduce_rz after the kernel, so no tile waits for a fence
+// and a ticket.
 template <int R, int N>
-__device__ bool tile_reduce_r(double *part, int nt, InstState *st, int tile_idx,
-                              const float (&vf)[R][N], double (&totals)[N],
-                              double (*sh)[kTile / 32], int *flag)
+__device__ __forceinline__ void tile_partial_r(double *part, int nt, int tile_idx,
+                                               const float (&vf)[R][N],
+                                               double (*sh)[kTile / 32])
 {
-    constexpr int T = kTile / R;
     double v[N];
     group_sum<R, N>(vf, v, sh);
     if (threadIdx.x == 0)
-    {
 #pragma unroll
         for (int k = 0; k < N; k++)
             part[k * nt + tile_idx] = v[k];
-        __threadfence();
-        unsigned prev = atomicAdd(&st->ticket, 1u);
-        *flag = (prev == unsigned(nt - 1));
-    }
-    __syncthreads();
-    if (!*flag)
-        return false;
-    __threadfence();
-    double s[R][N];
-#pragma unroll
-    for (int r = 0; r < R; r++)
-    {
-#pragma unroll
-        for (int k = 0; k < N; k++)
-            s[r][k] = 0.0;
-        sum_strided<N>(part, nt, r * T + threadIdx.x, s[r]);
-    }
-    group_sum_d<R, N>(s, totals, sh);
-    return true;
 }
 
 // Read-only load of a pointer field (the descriptor is constant during a kernel).
@@ -1045,9 +1026,8 @@ __device__ __forceinline__ void spmv_rows(const SpmvHdr &d, int row0, float (&pq
 
 struct UpdHdr
 {
-    int inst, nv, nt, active, iter, max_iters, check_every;
+    int inst, nv, nt, active, iter;
     float alpha;
-    double rel_tol2, abs_tol2;
     const float4 *pnew, *q;
     float4 *dx, *r, *z;
     const float4 *M0;
@@ -1067,10 +1047,6 @@ __device__ __forceinline__ void load_hdr(UpdHdr &h, const Tile &tl)
     h.alpha = float(st->alpha);
     h.nv = __ldg(&dp->nv);
     h.nt = __ldg(&dp->ntile_rows);
-    h.max_iters = __ldg(&dp->max_iters);
-    h.check_every = __ldg(&dp->check_every);
-    h.rel_tol2 = __ldg(&dp->rel_tol2);
-    h.abs_tol2 = __ldg(&dp->abs_tol2);
     float4 *p0 = ldg_ptr(&dp->p0), *p1 = ldg_ptr(&dp->p1);
     h.pnew = (h.iter & 1) ? p0 : p1;
     h.q = ldg_ptr(&dp->q);
@@ -1096,7 +1072,6 @@ __global__ void __launch_bounds__(kTile / R) k_spmv_t(InstDesc *const *descs,
 {
     constexpr int T = kTile / R;
     __shared__ double sh[1][kTile / 32];
-    __shared__ int flag;
     __shared__ SpmvHdr d; // the current instance's header (thread 0 loads it)
     const int ntiles = ctl->n_tiles_rows;
     int cur = -1;
@@ -1118,32 +1093,7 @@ __global__ void __launch_bounds__(kTile / R) k_spmv_t(InstDesc *const *descs,
                 continue;
             float part[R][1];
             spmv_rows<R, U, T, SKEW>(d, tl.start + threadIdx.x, part);
-            double tot[1];
-            if (tile_reduce_r<R, 1>(d.part, d.nt, d.st, tl.start / kTile, part, tot, sh,
-                                    &flag) &&
-                threadIdx.x == 0)
-            {
-                InstState &st = *d.st;
-                st.ticket = 0u;
-                st.pq = tot[0];
-                if (!isfinite(tot[0]))
-                {
-                    st.status = 6;
-                    st.active = 0;
-                    retire(ctl, use_cond, h);
-                }
-                else if (tot[0] == 0.0)
-                {
-                    // PCGSolver.cu:259-263 clamps alpha to zero; nothing moves
-                    // afterwards, so the loop ends here. (p.Ap < 0 goes on with a
-                    // negative alpha, as the reference does.)
-                    st.status = 7;
-                    st.active = 0;
-                    retire(ctl, use_cond, h);
-                }
-                else
-                    st.alpha = st.rho / tot[0];
-            }
+            tile_partial_r<R, 1>(d.part, d.nt, tl.start / kTile, part, sh);
         }
     }
 }
@@ -1157,7 +1107,6 @@ __global__ void __launch_bounds__(kTile / R) k_update_t(InstDesc *const *descs,
 {
     constexpr int T = kTile / R;
     __shared__ double sh[2][kTile / 32];
-    __shared__ int flag;
     // chunked loops (the request server): the last iteration of a chunk ends
     // the while loop; the condition is read after the body completes
     if (iters_left && blockIdx.x == 0 && threadIdx.x == 0)
@@ -1213,36 +1162,96 @@ __global__ void __launch_bounds__(kTile / R) k_update_t(InstDesc *const *descs,
                     part[r][1] = fdot(rr, rr);
                 }
             }
-            double tot[2];
-            if (tile_reduce_r<R, 2>(d.part, d.nt, d.st, tl.start / kTile, part, tot, sh,
-                                    &flag) &&
-                threadIdx.x == 0)
+            tile_partial_r<R, 2>(d.part, d.nt, tl.start / kTile, part, sh);
+        }
+    }
+}
+
+// Instance totals of a graph-loop half-iteration (k_reduce_pq, k_reduce_rz):
+// one block per instance of the list adds the instance's per-tile partials (sum_strided over kTile
+// lanes, then group_sum_d: one order, whatever the kernel variant that
+// wrote the partials) and takes the scalar step. KIND 0 (after the SpMV): p.q -> alpha,
+// or the end of the solve when p.q is zero or not finite. KIND 1
+// (k_reduce_rz, after the update): r.z, r.r -> beta, the iteration count and the convergence test.
+namespace {
+template <int KIND>
+__device__ __forceinline__ void reduce_body(InstDesc *const *descs, const int *inst_list,
+                                            int ninst, const int *ninst_dev, BatchCtl *ctl,
+                                            int use_cond, cudaGraphConditionalHandle h)
+{
+    constexpr int N = KIND == 0 ? 1 : 2;
+    __shared__ double sh[2][kTile / 32];
+    if (ninst_dev)
+        ninst = *ninst_dev;
+    for (int b = blockIdx.x; b < ninst; b += gridDim.x)
+    {
+        const InstDesc *dp = descs[inst_list[b]];
+        InstState *stp = ldg_ptr(&dp->st);
+        // read by every thread before thread 0 may clear it (group_sum_d syncs)
+        if (!__ldcg(&stp->active))
+            continue;
+        const int nt = __ldg(&dp->ntile_rows);
+        const double *part = ldg_ptr(&dp->part);
+        double sv[1][N];
+#pragma unroll
+        for (int k = 0; k < N; k++)
+            sv[0][k] = 0.0;
+        sum_strided<N>(part, nt, threadIdx.x, sv[0]);
+        double tot[N];
+        group_sum_d<1, N>(sv, tot, sh);
+        if (threadIdx.x == 0)
+        {
+            InstState &st = *stp;
+            if (KIND == 0)
             {
-                InstState &st = *d.st;
-                st.ticket = 0u;
+                st.pq = tot[0];
+                if (!isfinite(tot[0]))
+                {
+                    st.status = 6;
+                    st.active = 0;
+                    retire(ctl, use_cond, h);
+                }
+                else if (tot[0] == 0.0)
+                {
+                    // PCGSolver.cu:259-263 clamps alpha to zero; nothing moves
+                    // afterwards, so the loop ends here. (p.Ap < 0 goes on with a
+                    // negative alpha, as the reference does.)
+                    st.status = 7;
+                    st.active = 0;
+                    retire(ctl, use_cond, h);
+                }
+                else
+                    st.alpha = st.rho / tot[0];
+            }
+            else
+            {
                 const double rho_new = tot[0];
+                const double rr = tot[N - 1];
                 st.beta = (st.rho == 0.0) ? 0.0 : rho_new / st.rho;
                 st.rho = rho_new;
-                st.rr = tot[1];
-                st.iter = d.iter + 1;
-                const int n = st.iter;
+                st.rr = rr;
+                const int n = st.iter + 1;
+                st.iter = n;
+                const int check_every = __ldg(&dp->check_every);
+                const int max_iters = __ldg(&dp->max_iters);
+                const double rel_tol2 = __ldg(&dp->rel_tol2), abs_tol2 = __ldg(&dp->abs_tol2);
                 bool stop = false;
-                if (!isfinite(tot[0]) || !isfinite(tot[1]))
+                if (!isfinite(rho_new) || !isfinite(rr))
                 {
                     st.status = 6;
                     stop = true;
                 }
                 else
                 {
-                    const bool check = ((n - 1) % d.check_every) == 0 || n >= d.max_iters;
-                    const bool conv = (d.rel_tol2 > 0.0 && tot[1] <= d.rel_tol2 * st.bb) ||
-                                      (d.abs_tol2 > 0.0 && tot[1] <= d.abs_tol2);
+                    const bool check = ((n - 1) % check_every) == 0 || n >= max_iters;
+                    const bool conv = (rel_tol2 > 0.0 && rr <= rel_tol2 * st.bb) ||
+                                      (abs_tol2 > 0.0 && rr <= abs_tol2);
                     if (check && conv)
                     {
                         st.status = 0;
                         stop = true;
                     }
-                    else if (n >= d.max_iters)
+                    else if (n >= max_iters)
                     {
                         st.status = 8; // CLOTH_ERR_MAXITER
                         stop = true;
@@ -1256,6 +1265,21 @@ __global__ void __launch_bounds__(kTile / R) k_update_t(InstDesc *const *descs,
             }
         }
     }
+}
+} // namespace
+
+__global__ void __launch_bounds__(kTile)
+    k_reduce_pq(InstDesc *const *descs, const int *inst_list, int ninst, const int *ninst_dev,
+                BatchCtl *ctl, int use_cond, cudaGraphConditionalHandle h)
+{
+    reduce_body<0>(descs, inst_list, ninst, ninst_dev, ctl, use_cond, h);
+}
+
+__global__ void __launch_bounds__(kTile)
+    k_reduce_rz(InstDesc *const *descs, const int *inst_list, int ninst, const int *ninst_dev,
+                BatchCtl *ctl, int use_cond, cudaGraphConditionalHandle h)
+{
+    reduce_body<1>(descs, inst_list, ninst, ninst_dev, ctl, use_cond, h);
 }
 
 // Variant table of the graph-loop kernels (the autotuner's search space).

@@ -10,7 +10,7 @@
 //                 per-solve arrays now point into the pool)
 //   k_pins, k_tri, k_row         assembly and PCG start of those requests only
 //   k_srv_begin   admitted-and-iterating count, chunk iteration budget
-//   while (any iterating && budget left) { k_spmv; k_update }   over every
+//   while (any iterating && budget left) { k_spmv; k_reduce; k_update; k_reduce }   over every
 //                 request on the GPU (finished ones skip their tiles)
 //   k_advance     x_pre = x, x += dx for requests whose solve ended
 //   k_srv_status  one record per request on the GPU; ended ones are closed
@@ -349,6 +349,8 @@ int build_chunk_graph(cloth_server_s *s)
     void *a_row[] = {&s->d_ptrs, &s->d_new_rt, &s->d_ctl_new};
     void *a_begin[] = {&s->d_ctl_new, &s->d_ctl_act, &s->d_sc, &hnd};
     void *a_spmv[] = {&s->d_ptrs, &s->d_act_rt, &s->d_ctl_act, &one, &hnd};
+    const int *n_inflight = &s->d_sc->n_inflight;
+    void *a_red[] = {&s->d_ptrs, &s->d_inflight, &zero, &n_inflight, &s->d_ctl_act, &one, &hnd};
     void *a_upd[] = {&s->d_ptrs, &s->d_act_rt, &s->d_ctl_act, &one, &hnd, &left};
     void *a_adv[] = {&s->d_ptrs, &s->d_act_rt, &s->d_ctl_act, &one};
     void *a_stat[] = {&s->d_ptrs, &s->d_inflight, &s->d_sc, &s->d_status};
@@ -380,8 +382,12 @@ int build_chunk_graph(cloth_server_s *s)
             rc = add_node(body, &bn, &bl, const_cast<void *>(sv.func), one_wave_spmv,
                           kTile / sv.rows_per_thread, a_spmv);
             if (rc == CLOTH_OK)
+                rc = add_node(body, &bn, &bl, (void *)k_reduce_pq, reduce_grid(n), kTile, a_red);
+            if (rc == CLOTH_OK)
                 rc = add_node(body, &bn, &bl, const_cast<void *>(uv.func), one_wave_upd,
                               kTile / uv.rows_per_thread, a_upd);
+            if (rc == CLOTH_OK)
+                rc = add_node(body, &bn, &bl, (void *)k_reduce_rz, reduce_grid(n), kTile, a_red);
             last = cn;
         }
     }
