@@ -1185,18 +1185,38 @@ __device__ __forceinline__ void reduce_body(InstDesc *const *descs, const int *i
         ninst = *ninst_dev;
     for (int b = blockIdx.x; b < ninst; b += gridDim.x)
     {
+        // loads grouped by dependence level (a latency chain, not bandwidth):
+        // the descriptor's fields, then the state and the partials together
         const InstDesc *dp = descs[inst_list[b]];
         InstState *stp = ldg_ptr(&dp->st);
-        // read by every thread before thread 0 may clear it (group_sum_d syncs)
-        if (!__ldcg(&stp->active))
-            continue;
         const int nt = __ldg(&dp->ntile_rows);
         const double *part = ldg_ptr(&dp->part);
+        int check_every = 1, max_iters = 0;
+        double rel_tol2 = 0.0, abs_tol2 = 0.0;
+        if (KIND == 1 && threadIdx.x == 0)
+        {
+            check_every = __ldg(&dp->check_every);
+            max_iters = __ldg(&dp->max_iters);
+            rel_tol2 = __ldg(&dp->rel_tol2);
+            abs_tol2 = __ldg(&dp->abs_tol2);
+        }
+        // read by every thread before thread 0 may clear it (group_sum_d syncs)
+        const int active = __ldcg(&stp->active);
+        double rho0 = 0.0, bb0 = 0.0;
+        int it0 = 0;
+        if (threadIdx.x == 0)
+        {
+            rho0 = __ldcg(&stp->rho);
+            bb0 = __ldcg(&stp->bb);
+            it0 = __ldcg(&stp->iter);
+        }
         double sv[1][N];
 #pragma unroll
         for (int k = 0; k < N; k++)
             sv[0][k] = 0.0;
         sum_strided<N>(part, nt, threadIdx.x, sv[0]);
+        if (!active)
+            continue;
         double tot[N];
         group_sum_d<1, N>(sv, tot, sh);
         if (threadIdx.x == 0)
@@ -1221,20 +1241,17 @@ __device__ __forceinline__ void reduce_body(InstDesc *const *descs, const int *i
                     retire(ctl, use_cond, h);
                 }
                 else
-                    st.alpha = st.rho / tot[0];
+                    st.alpha = rho0 / tot[0];
             }
             else
             {
                 const double rho_new = tot[0];
                 const double rr = tot[N - 1];
-                st.beta = (st.rho == 0.0) ? 0.0 : rho_new / st.rho;
+                st.beta = (rho0 == 0.0) ? 0.0 : rho_new / rho0;
                 st.rho = rho_new;
                 st.rr = rr;
-                const int n = st.iter + 1;
+                const int n = it0 + 1;
                 st.iter = n;
-                const int check_every = __ldg(&dp->check_every);
-                const int max_iters = __ldg(&dp->max_iters);
-                const double rel_tol2 = __ldg(&dp->rel_tol2), abs_tol2 = __ldg(&dp->abs_tol2);
                 bool stop = false;
                 if (!isfinite(rho_new) || !isfinite(rr))
                 {
@@ -1244,7 +1261,7 @@ __device__ __forceinline__ void reduce_body(InstDesc *const *descs, const int *i
                 else
                 {
                     const bool check = ((n - 1) % check_every) == 0 || n >= max_iters;
-                    const bool conv = (rel_tol2 > 0.0 && rr <= rel_tol2 * st.bb) ||
+                    const bool conv = (rel_tol2 > 0.0 && rr <= rel_tol2 * bb0) ||
                                       (abs_tol2 > 0.0 && rr <= abs_tol2);
                     if (check && conv)
                     {
