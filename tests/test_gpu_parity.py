@@ -373,3 +373,56 @@ def test_plain_reference_schedule(ctx):
         st = c.UpdatePosPlain()
         assert st["iters"] in [1 + 10 * k for k in range(10)] + [100], st
     c.close()
+
+
+def _shuffled_grid_obj(path, n, first, seed):
+    """An n x n grid cloth as OBJ whose vertex ids from `first` on are randomly
+    permuted: rows there reference columns all over the permuted range."""
+    rng = np.random.default_rng(seed)
+    perm = np.arange(n * n)
+    perm[first:] = first + rng.permutation(n * n - first)
+    pos = np.zeros((n * n, 3))
+    uv = np.zeros((n * n, 2))
+    for j in range(n):
+        for i in range(n):
+            pos[perm[j * n + i]] = (i / (n - 1) - 0.5, 0.5 - j / (n - 1), 0.0)
+            # texture coordinates (the rest shape): the loader scales them by 10/3
+            uv[perm[j * n + i]] = (0.3 * i / (n - 1), 0.3 * j / (n - 1))
+    lines = [f"v {x:.9f} {y:.9f} {z:.9f}" for x, y, z in pos]
+    lines += [f"vt {u:.9f} {v:.9f}" for u, v in uv]
+    for j in range(n - 1):
+        for i in range(n - 1):
+            a, b = perm[j * n + i] + 1, perm[j * n + i + 1] + 1
+            c, d = perm[(j + 1) * n + i] + 1, perm[(j + 1) * n + i + 1] + 1
+            lines += [f"f {a}/{a} {c}/{c} {b}/{b}", f"f {b}/{b} {c}/{c} {d}/{d}"]
+    path.write_text("\n".join(lines) + "\n")
+
+
+def test_unstaged_blocks_agree(ctx, tmp_path):
+    """A mesh whose later vertex ids are shuffled: the persistent blocks over
+    the shuffled rows reference more columns than shared memory holds and read
+    p from global memory, the others stage it; the team keeps p in global
+    memory for them.  The result agrees with the graph loop."""
+    from acousticsim_gb300 import params
+    n = 160
+    obj = tmp_path / "shuffled.obj"
+    _shuffled_grid_obj(obj, n, n * n // 4, 5)
+    conf = dict(_grid_conf(n), enable_cloth_from_obj=True, cloth_obj_path=str(obj),
+                cloth_obj_translation=[0.0, 0.0, 0.0], enable_relocate_obj=False)
+    conf.pop("geometry_type")
+    p = params(max_iters=20000, rel_tol=1e-6)
+    out = {}
+    for sv in ("persistent", "graph_loop"):
+        ctx.set_solver(sv)
+        c = make(ctx, conf)
+        x, xp = _perturbed(c, 3, 2e-3)
+        c.SetPos(x)
+        c.SetPrePos(xp)
+        st = c.UpdatePos(0.0, p)
+        assert st["status"] == "OK" and st["solver"] == sv, st
+        out[sv] = (c.GetPos() - x, st["iters"])
+        c.close()
+    ctx.set_solver("persistent")
+    assert abs(out["persistent"][1] - out["graph_loop"][1]) <= 3, (out["persistent"][1],
+                                                                   out["graph_loop"][1])
+    assert rel(out["persistent"][0], out["graph_loop"][0]) < 1e-4
