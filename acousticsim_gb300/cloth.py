@@ -15,16 +15,34 @@ import numpy as np
 from . import _native as N
 
 
+import atexit
+import weakref
+
+# Contexts still open when the interpreter exits are closed here, while the
+# native library and this module are intact (finalizers that run during
+# interpreter teardown may find neither).
+_open_contexts: "weakref.WeakSet[ClothContext]" = weakref.WeakSet()
+
+
+@atexit.register
+def _close_open_contexts() -> None:
+    for ctx in list(_open_contexts):
+        try:
+            ctx.close()
+        except Exception:
+            pass
+
+
 class ClothContext:
     """One device and one CUDA stream (cloth_ctx)."""
 
     def __init__(self, device: int = 0):
-        import weakref
         self._h = C.c_void_p()
         self._cloths = weakref.WeakSet()
         self._servers = weakref.WeakSet()
         self._bodies = weakref.WeakSet()
         N.call("cloth_ctx_create", int(device), C.byref(self._h))
+        _open_contexts.add(self)
 
     @property
     def handle(self):
