@@ -46,7 +46,8 @@ struct F64State
     double rel_tol2, abs_tol2;
     int iter, active, status, max_iters;
     unsigned ticket;
-    int pad[3];
+    int fallbacks; // flexible CG: inner solves replaced by the FP64 block-Jacobi step
+    int pad[2];
 };
 
 struct F64Ptr
@@ -502,7 +503,7 @@ __global__ void __launch_bounds__(kB64) k64_fcg_z(const InstDesc *dp, F64Ptr f, 
         s.rho = tot[0];
         s.beta = first ? 0.0 : -tot[1] / s.pq;
         if (!use_inner)
-            s.pad[0]++; // inner solves replaced by M r
+            s.fallbacks++;
     }
 }
 
@@ -972,7 +973,7 @@ int cloth_solve_flexible(cloth_t *c, const cloth_solve_params *inner, double rel
             return rc;
         out.outer++;
         rel = bb > 0 ? std::sqrt(hs.rr / bb) : 0.0;
-        out.rejected = hs.pad[0];
+        out.rejected = hs.fallbacks;
         if (!hs.active)
         {
             // p.Ap zero or not finite in the outer step
