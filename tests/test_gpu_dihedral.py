@@ -300,6 +300,11 @@ def test_dihedral_fp64_solvers(ctx, orc):
     assert rs["status"] == "OK", rs
     assert c.residual_fp64() < 1e-8
     assert rel(c.get_dx(), g["sys_dih_dx"].reshape(-1)) < 1e-5
+    # flexible CG over FP32 PCG steps (the skew block parts in both)
+    fs = c.solve_flexible(params(max_iters=20, rel_tol=0.0, warm_start=0), 1e-10, 5000)
+    assert fs["status"] == "OK" and fs["rejected"] == 0, fs
+    assert c.residual_fp64() < 2e-10
+    assert rel(c.get_dx(), g["sys_dih_dx"].reshape(-1)) < 1e-5
     c.close()
 
 
