@@ -16,6 +16,7 @@ from . import _native as N
 
 
 import atexit
+import sys
 import weakref
 
 # Contexts still open when the interpreter exits are closed here, while the
@@ -125,7 +126,12 @@ class ClothContext:
             self._h = C.c_void_p()
 
     def __del__(self):
+        # during interpreter teardown the native library, the CUDA runtime's
+        # users (torch) and this module may already be half gone: the atexit
+        # handler has closed every context before that point, so do nothing
         try:
+            if sys.is_finalizing():
+                return
             self.close()
         except Exception:
             pass
@@ -490,7 +496,12 @@ class BaraffClothGpu:
             self._h = C.c_void_p()
 
     def __del__(self):
+        # during interpreter teardown the native library, the CUDA runtime's
+        # users (torch) and this module may already be half gone: the atexit
+        # handler has closed every context before that point, so do nothing
         try:
+            if sys.is_finalizing():
+                return
             self.close()
         except Exception:
             pass
@@ -574,7 +585,12 @@ class ClothServer:
         self._held = []
 
     def __del__(self):
+        # during interpreter teardown the native library, the CUDA runtime's
+        # users (torch) and this module may already be half gone: the atexit
+        # handler has closed every context before that point, so do nothing
         try:
+            if sys.is_finalizing():
+                return
             self.close()
         except Exception:
             pass

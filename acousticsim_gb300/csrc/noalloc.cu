@@ -26,7 +26,6 @@ void set_last_error(const std::string &msg); // cloth_api.cu: message for cloth_
 
 #include <cmath>
 #include <cstdint>
-#include <mutex>
 
 namespace {
 
@@ -40,6 +39,7 @@ struct NaState
     double rho, pq, alpha, beta, rr, bb;
     int iter, active, status;
     unsigned ticket;
+    int bad_col; // set by k_na_init when an ELL column id is >= nv
     int max_iters, check_every;
     double rel_tol2, abs_tol2;
 };
@@ -190,6 +190,13 @@ __global__ void __launch_bounds__(kNaTile) k_na_init(unsigned char *base, const 
             const int c = ell[row * kNaWidth + s];
             if (c < 0)
                 break;
+            if (c >= nv)
+            {
+                // a column id outside the system: record it, touch nothing;
+                // the solve then ends with CLOTH_ERR_INVALID before any SpMV
+                atomicExch(&v.st->bad_col, 1);
+                break;
+            }
             const float *a = A + (size_t(row) * kNaWidth + s) * 9;
             if (c == row)
                 for (int k = 0; k < 9; k++)
@@ -253,6 +260,11 @@ __global__ void __launch_bounds__(kNaTile) k_na_init(unsigned char *base, const 
             s.status = CLOTH_ERR_NAN;
             s.active = 0;
         }
+        if (atomicAdd(&s.bad_col, 0) != 0)
+        {
+            s.status = CLOTH_ERR_INVALID;
+            s.active = 0;
+        }
     }
 }
 
@@ -280,7 +292,7 @@ __global__ void __launch_bounds__(kNaTile) k_na_spmv(unsigned char *base, const 
             for (int s = 0; s < kNaWidth; s++)
             {
                 const int c = ell[row * kNaWidth + s];
-                if (c < 0)
+                if (c < 0 || c >= nv)
                     break;
                 if (v.fixed[c])
                     continue;
@@ -368,39 +380,27 @@ __global__ void __launch_bounds__(kNaTile) k_na_update(unsigned char *base, floa
     }
 }
 
-std::mutex na_mu;
-unsigned char *na_ptr[128] = {};
-
 int na_fail(int code, const std::string &m)
 {
     cloth::set_last_error(m);
     return code;
 }
 
-// Device address of the scratch on the current device: looked up once per
-// device, with that device current, and cached.
+// Device address of the scratch on the current device, looked up on every
+// call with that device current (a lookup costs about a microsecond, and a
+// cached address would go stale after cudaDeviceReset reloads the module).
 int na_scratch(unsigned char **out)
 {
-    int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 128)
+    void *p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || !p)
     {
         cudaGetLastError();
-        return na_fail(CLOTH_ERR_CUDA, "cloth_pcg_solve_ell32_noalloc: no current CUDA device");
+        return na_fail(CLOTH_ERR_CUDA, std::string("cloth_pcg_solve_ell32_noalloc: "
+                                                   "cudaGetSymbolAddress: ") +
+                                           cudaGetErrorString(e));
     }
-    std::lock_guard<std::mutex> lk(na_mu);
-    if (!na_ptr[dev])
-    {
-        void *p = nullptr;
-        const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (e != cudaSuccess || !p)
-        {
-            cudaGetLastError();
-            return na_fail(CLOTH_ERR_CUDA, std::string("cudaGetSymbolAddress: ") +
-                                               cudaGetErrorString(e));
-        }
-        na_ptr[dev] = static_cast<unsigned char *>(p);
-    }
-    *out = na_ptr[dev];
+    *out = static_cast<unsigned char *>(p);
     return CLOTH_OK;
 }
 
@@ -420,11 +420,23 @@ extern "C" int cloth_pcg_solve_ell32_noalloc(int nv, const int *ell_dev, const f
                        "cloth_pcg_solve_ell32_noalloc: " + std::to_string(nv) +
                            " vertices exceed the static scratch limit of " +
                            std::to_string(kNaMaxVertices));
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    // The call waits on the host for the solver state every few iterations,
+    // which a stream under capture cannot do: refuse before touching it.
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(s, &cap) != cudaSuccess)
+    {
+        cudaGetLastError();
+        return na_fail(CLOTH_ERR_CUDA, "cloth_pcg_solve_ell32_noalloc: cudaStreamIsCapturing failed");
+    }
+    if (cap != cudaStreamCaptureStatusNone)
+        return na_fail(CLOTH_ERR_STATE,
+                       "cloth_pcg_solve_ell32_noalloc: the stream is being captured; this call "
+                       "synchronises with the host and cannot be captured");
     unsigned char *base = nullptr;
     int rc = na_scratch(&base);
     if (rc != CLOTH_OK)
         return rc;
-    cudaStream_t s = static_cast<cudaStream_t>(stream);
     NaState init{};
     const int max_iters = params ? params->max_iters : 1000;
     const double rel = params ? params->rel_tol : 1e-6, abs = params ? params->abs_tol : 0.0;
@@ -448,11 +460,14 @@ extern "C" int cloth_pcg_solve_ell32_noalloc(int nv, const int *ell_dev, const f
     NA_CK(cudaGetLastError());
     NaState h{};
     const int chunk = 8;
-    for (int done = 0;; done += chunk)
+    // the device stops at max_iters; the host bound (in 64-bit) only guards
+    // against a state that never reports inactive
+    const long long limit = static_cast<long long>(init.max_iters) + 2 * chunk;
+    for (long long done = 0;; done += chunk)
     {
         NA_CK(cudaMemcpyAsync(&h, v.st, sizeof(h), cudaMemcpyDeviceToHost, s));
         NA_CK(cudaStreamSynchronize(s));
-        if (!h.active || done > init.max_iters + chunk)
+        if (!h.active || h.bad_col || done > limit)
             break;
         for (int k = 0; k < chunk; k++)
         {
@@ -462,6 +477,10 @@ extern "C" int cloth_pcg_solve_ell32_noalloc(int nv, const int *ell_dev, const f
         NA_CK(cudaGetLastError());
     }
 #undef NA_CK
+    if (h.active && h.status == CLOTH_OK)
+        h.status = CLOTH_ERR_MAXITER;
+    if (h.bad_col)
+        h.status = CLOTH_ERR_INVALID;
     if (stats)
     {
         stats->iters = h.iter;
@@ -471,5 +490,10 @@ extern "C" int cloth_pcg_solve_ell32_noalloc(int nv, const int *ell_dev, const f
         stats->rel_residual = stats->rhs_norm > 0 ? stats->res_norm / stats->rhs_norm : stats->res_norm;
         stats->solver = CLOTH_SOLVER_GRAPH_LOOP;
     }
-    return CLOTH_OK;
+    // no stats object outlives the call, so the return value carries the
+    // solve's own outcome: CLOTH_OK only when it reached the tolerance
+    if (h.status == CLOTH_ERR_INVALID)
+        return na_fail(CLOTH_ERR_INVALID,
+                       "cloth_pcg_solve_ell32_noalloc: an ELL column id is >= nv");
+    return h.status;
 }

@@ -496,10 +496,16 @@ int cloth_server_destroy(cloth_server *srv);
  * device; the work runs on `stream` (a cudaStream_t, NULL = default stream).
  * Nothing is allocated: the solver's scratch (4 MiB) is a static array that
  * every GPU loading this library holds until the process exits, which limits
- * nv to 32768; larger systems are rejected with CLOTH_ERR_INVALID. The first
- * call on a device looks up that array's device address, so make it before
- * any stream capture. Every call reuses the same array: calls that may
- * overlap on the GPU race and must be serialised by the caller. */
+ * nv to 32768; larger systems are rejected with CLOTH_ERR_INVALID, and so is
+ * an ELL column id >= nv (found before any SpMV runs). Every call looks up the
+ * array's device address on the current device and reuses the same array:
+ * calls that may overlap on the GPU race and must be serialised by the caller.
+ * The call blocks the host: it waits on `stream` for the solver state every
+ * eight iterations, so it can never be stream-captured; on a capturing stream
+ * it returns CLOTH_ERR_STATE and leaves the stream alone. Returns the solve's
+ * own status: CLOTH_OK only when the tolerance was reached, else
+ * CLOTH_ERR_MAXITER, CLOTH_ERR_NAN or CLOTH_ERR_BREAKDOWN (stats, when given,
+ * say the same). */
 int cloth_pcg_solve_ell32_noalloc(int nv, const int *ell_dev, const float *A_dev,
                                   const float *b_dev, float *x_dev, const int *fixed_dev,
                                   int nfixed, const cloth_solve_params *params,

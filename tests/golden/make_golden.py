@@ -1,6 +1,6 @@
 """Generates the golden fixtures of tests/golden/*.npz from the reference itself.
 
-    python tests/golden/make_golden.py [--ref /root/reference]
+    python tests/golden/make_golden.py [--ref <reference source tree>]
 
 Builds the reference's CPU cloth code with oracle/Makefile (outputs only into
 oracle/_ref/), runs oracle/_ref/ref_harness on seeded inputs and stores what it
@@ -188,10 +188,13 @@ def read_dump(d: Path) -> dict:
 
 def main() -> None:
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=None,
+                    help="reference source tree (default: $ACOUSTICSIM_REF, else the "
+                         "Makefile's REF)")
     ap.add_argument("--only", nargs="*", default=None, help="case names to regenerate")
     a = ap.parse_args()
-    subprocess.run(["make", "-C", str(ROOT / "oracle"), f"REF={a.ref}", "-j8"], check=True,
+    ref_arg = [f"REF={a.ref}"] if a.ref else []
+    subprocess.run(["make", "-C", str(ROOT / "oracle"), *ref_arg, "-j8"], check=True,
                    stdout=subprocess.DEVNULL)
     harness = ROOT / "oracle" / "_ref" / "ref_harness"
     cases = [(name, over, seed, sx, sv, None) for name, over, seed, sx, sv in CASES]

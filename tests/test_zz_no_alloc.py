@@ -20,9 +20,9 @@ from conftest import rel
 
 pytestmark = pytest.mark.gpu
 
-# same bound as the other solve tests: both solves stop at 1e-6 relative
-# residual, the solutions agree to well within 1e-3 relative
-TOL_DX = 1e-3
+# both solves stop at 1e-6 relative residual; their solutions agree to a few
+# 1e-6 relative (the solve tests' dx bound)
+TOL_DX = 2e-4
 
 
 def _conf(n):
@@ -106,3 +106,75 @@ def test_noalloc_rejects_oversized_systems(built):
                                                 None, None, None)
     assert rc == 1  # CLOTH_ERR_INVALID, nothing launched
     assert b"exceed" in N.load().cloth_last_error()
+
+
+def _small_system(n=16):
+    from acousticsim_gb300 import BaraffClothGpu, ClothContext
+    ctx = ClothContext(0)
+    cloth = BaraffClothGpu(ctx, _conf(n))
+    cloth.assemble()
+    sysd = cloth.export_system()
+    pins = cloth.GetConstraintStaticVertices()
+    cloth.close()
+    ctx.close()
+    return sysd, pins
+
+
+def test_noalloc_rejects_column_ids_outside_the_system(built):
+    """A caller-built ELL map with a column id >= nv is reported as
+    CLOTH_ERR_INVALID; the id is caught before anything is read through it."""
+    import torch
+    from acousticsim_gb300 import _native as N, params
+    sysd, pins = _small_system()
+    nv = sysd["b"].shape[0]
+    ell = np.array(sysd["ell"], np.int32, copy=True)
+    row = nv // 2
+    ell[row, 1] = nv + 5  # a column past the last vertex
+    dev = torch.device("cuda", 0)
+    A = np.ascontiguousarray(np.swapaxes(sysd["A"], 2, 3), np.float32)
+    ell_d = torch.from_numpy(ell).to(dev)
+    A_d = torch.from_numpy(A).to(dev)
+    b_d = torch.from_numpy(np.ascontiguousarray(sysd["b"], np.float32)).to(dev)
+    x_d = torch.zeros(sysd["b"].shape, dtype=torch.float32, device=dev)
+    st = N.SolveStats()
+    p = params(max_iters=500, rel_tol=1e-6, warm_start=0)
+    rc = N.load().cloth_pcg_solve_ell32_noalloc(nv, ell_d.data_ptr(), A_d.data_ptr(),
+                                                b_d.data_ptr(), x_d.data_ptr(), None, 0,
+                                                C.byref(p), C.byref(st), None)
+    torch.cuda.synchronize(dev)
+    assert rc == 1, rc  # CLOTH_ERR_INVALID
+    assert st.status == 1 and st.iters == 0
+    assert b"column" in N.load().cloth_last_error()
+    # the same call with the map restored solves normally
+    ell_d.copy_(torch.from_numpy(np.ascontiguousarray(sysd["ell"], np.int32)).to(dev))
+    x_d.zero_()
+    rc = N.load().cloth_pcg_solve_ell32_noalloc(nv, ell_d.data_ptr(), A_d.data_ptr(),
+                                                b_d.data_ptr(), x_d.data_ptr(), None, 0,
+                                                C.byref(p), C.byref(st), None)
+    torch.cuda.synchronize(dev)
+    assert rc == 0 and st.status == 0, (rc, st.status)
+
+
+def test_noalloc_refuses_a_capturing_stream(built):
+    """The call reads the solver state on the host, so under stream capture it
+    returns CLOTH_ERR_STATE and leaves the capture intact."""
+    import torch
+    from acousticsim_gb300 import _native as N
+    dev = torch.device("cuda", 0)
+    sysd, _ = _small_system()
+    nv = sysd["b"].shape[0]
+    buf = torch.zeros(nv * 32 * 9, dtype=torch.float32, device=dev)
+    ell_d = torch.from_numpy(np.ascontiguousarray(sysd["ell"], np.int32)).to(dev)
+    side = torch.cuda.Stream(dev)
+    y = torch.zeros(4, device=dev)
+    g = torch.cuda.CUDAGraph()
+    rcs = []
+    with torch.cuda.graph(g, stream=side):
+        y.add_(1.0)
+        rcs.append(N.load().cloth_pcg_solve_ell32_noalloc(
+            nv, ell_d.data_ptr(), buf.data_ptr(), buf.data_ptr(), buf.data_ptr(), None, 0,
+            None, None, C.c_void_p(side.cuda_stream)))
+    g.replay()
+    torch.cuda.synchronize(dev)
+    assert rcs == [11], rcs  # CLOTH_ERR_STATE
+    assert float(y[0]) == 1.0  # the captured work is intact
