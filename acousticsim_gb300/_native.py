@@ -18,9 +18,9 @@ STATUS_NAMES = {
     7: "BREAKDOWN", 8: "MAXITER", 9: "TIMEOUT", 10: "UNSUPPORTED", 11: "STATE",
     12: "CONTACTS",
 }
-NUM_PHASES = 8
+NUM_PHASES = 9
 PHASE_NAMES = ["pins", "tri_assemble", "row_assemble", "spmv_dot", "update_dot", "advance",
-               "contacts", "repulsion"]
+               "contacts", "repulsion", "reduce"]
 ELL_REF_WIDTH = 32
 SOLVER_PERSISTENT = 0
 SOLVER_GRAPH_LOOP = 1
@@ -134,6 +134,7 @@ SIGNATURES = {
     "cloth_ctx_get_profile": (C.c_int, [P, PD, C.POINTER(C.c_longlong)]),
     "cloth_ctx_reset_profile": (C.c_int, [P]),
     "cloth_ctx_set_solver": (C.c_int, [P, C.c_int]),
+    "cloth_ctx_set_spin_limit": (C.c_int, [P, C.c_uint, C.c_uint]),
     "cloth_ctx_device_bytes": (C.c_int, [P, C.POINTER(C.c_size_t)]),
     "cloth_ctx_set_kernel_variant": (C.c_int, [P, C.c_int, C.c_int, C.c_int, C.c_int,
                                                C.c_int, C.c_int]),

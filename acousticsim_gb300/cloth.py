@@ -74,8 +74,19 @@ class ClothContext:
                 "persistent_2b": N.SOLVER_PERSISTENT_2B}[solver]
         N.call("cloth_ctx_set_solver", self._h, code)
 
+    def set_spin_limit(self, polls: int = 0, extra_arrivals: int = 0) -> None:
+        """Bounded team-barrier waits of the persistent solvers: give up after
+        `polls` polls (0: the default) with status TIMEOUT.  `extra_arrivals`
+        makes every barrier wait for arrivals no block makes (a test of the
+        timeout path); 0 in normal use."""
+        N.call("cloth_ctx_set_spin_limit", self._h, int(polls), int(extra_arrivals))
+
+    # (rows per thread, slot unroll, tiles per block); slot unroll 0: the
+    # bulk-staged SpMV, whose third number is its ring of stages and whose
+    # first is 1 when it also stages p over each tile's column range
     SPMV_VARIANTS = [(1, 1, 1), (1, 2, 1), (1, 3, 1), (2, 1, 1), (2, 2, 1), (4, 1, 1),
-                     (1, 1, 4), (1, 2, 4), (2, 1, 4), (2, 2, 4), (4, 1, 4), (2, 1, 8)]
+                     (1, 1, 4), (1, 2, 4), (2, 1, 4), (2, 2, 4), (4, 1, 4), (2, 1, 8),
+                     (1, 0, 2), (1, 0, 3), (0, 0, 2), (0, 0, 3), (0, 0, 4)]
     UPDATE_VARIANTS = [(1, 1), (2, 1), (4, 1), (1, 4), (2, 4), (1, 8), (2, 8)]
 
     def set_kernel_variant(self, spmv=(1, 3, 1), update=(1, 1), autotune: bool = False) -> None:

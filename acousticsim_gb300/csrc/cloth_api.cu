@@ -38,7 +38,8 @@ enum Phase
     PH_UPDATE,
     PH_ADVANCE,
     PH_COLLIDE,
-    PH_REPULSE
+    PH_REPULSE,
+    PH_REDUCE
 };
 
 } // namespace
@@ -69,6 +70,7 @@ struct Batch
     int spmv_v = kDefaultSpmvVariant, upd_v = kDefaultUpdateVariant;
     bool tuned = false;
     int grid_spmv = 1, grid_update = 1;
+    unsigned smem_spmv = 0; // dynamic shared memory of the chosen SpMV variant
     int spmv_waves = 8, upd_waves = 8;
     // a member carries skew block parts (dihedral bending): the SpMV variants
     // that apply them
@@ -79,20 +81,41 @@ struct Batch
     {
         return (skew ? kSpmvSkewVariants : kSpmvVariants)[v];
     }
-    int spmv_occ(int v) const { return (skew ? ctx->occ_spmv_skew : ctx->occ_spmv)[v]; }
+    // stage bytes of the bulk-staged SpMV variants for these members, without
+    // and with the halo of p
+    unsigned bulk_stage[2] = {0, 0};
+    unsigned stage_of(const GraphLoopVariant &sv) const { return bulk_stage[sv.bulk_halo ? 1 : 0]; }
+    int spmv_occ(int v) const
+    {
+        const GraphLoopVariant &sv = spmv_variant(v);
+        if (sv.bulk_stages)
+            return bulk_occupancy(sv, stage_of(sv), ctx->max_smem_optin);
+        return (skew ? ctx->occ_spmv_skew : ctx->occ_spmv)[v];
+    }
+    unsigned spmv_smem_of(int v) const
+    {
+        return bulk_smem(spmv_variant(v), stage_of(spmv_variant(v)));
+    }
+    bool spmv_usable(int v) const { return !spmv_variant(v).bulk_stages || spmv_occ(v) > 0; }
     void set_variants(int sv, int uv, int sw = 8, int uw = 8)
     {
+        if (!spmv_usable(sv))
+            sv = kDefaultSpmvVariant;
         spmv_v = sv;
         upd_v = uv;
         spmv_waves = sw;
         upd_waves = uw;
         grid_spmv = grid_for(spmv_variant(sv), spmv_occ(sv), sw);
+        smem_spmv = spmv_smem_of(sv);
         grid_update = grid_for(kUpdateVariants[uv], ctx->occ_update[uv], uw);
     }
     // one block per group of TPB tiles, at most `waves` full waves of resident
-    // blocks (fewer waves: each block walks more tiles, grid-stride)
+    // blocks (fewer waves: each block walks more tiles, grid-stride); the
+    // bulk-staged SpMV runs one wave of resident blocks, each walking its tiles
     int grid_for(const GraphLoopVariant &v, int occ, int waves = 8) const
     {
+        if (v.bulk_stages)
+            return std::max(1, std::min(n_rt, ctx->num_sms * std::max(occ, 1)));
         const int groups = (n_rt + v.tiles_per_block - 1) / v.tiles_per_block;
         return std::max(1, std::min(groups, ctx->num_sms * occ * waves));
     }
@@ -104,6 +127,7 @@ struct Batch
     int grid_persist = 0;
     int halo_cap = 0, rows_cap = 0;
     size_t smem_persist = 0;
+    SpinCfg spin = {kSpinLimitDefault, 0u}; // the context's setting when the set was built
     cudaGraphExec_t step_exec = nullptr;
     cudaGraphExec_t solve_exec = nullptr;
     ~Batch()
@@ -224,6 +248,7 @@ int upload_tables(cloth_s *c)
         o_dsrc = L.take<uint32_t>(WS);
         o_dent = L.take<uint32_t>(std::max<size_t>(t.dih_ent.size(), 1));
     }
+    size_t o_thalo = L.take<int2>(ntr);
     size_t o_rowinfo = L.take<int>(n), o_fptr = L.take<int>(n + 1),
            o_mass = L.take<float>(n), o_grav = L.take<float>(n);
     size_t o_pv = L.take<int>(n + 1), o_pt = L.take<float4>(n + 1);
@@ -325,6 +350,21 @@ int upload_tables(cloth_s *c)
         mass[v] = float(t.mass[v]);
         grav[v] = float(c->mat.gravity * t.mass[v]);
     }
+    // column range of each 128-row tile (the bulk SpMV stages p over it)
+    std::vector<int2> thalo(ntr);
+    c->max_halo = 0;
+    for (int tt = 0; tt < ntr; tt++)
+    {
+        int lo = n, hi = 0;
+        for (int v = tt * kTile; v < std::min(n, (tt + 1) * kTile); v++)
+            for (int k = t.rowptr[v]; k < t.rowptr[v + 1]; k++)
+            {
+                lo = std::min(lo, t.cols[k]);
+                hi = std::max(hi, t.cols[k] + 1);
+            }
+        thalo[tt] = make_int2(lo, std::max(lo, hi));
+        c->max_halo = std::max(c->max_halo, hi - lo);
+    }
     std::vector<double> x64(c->mesh.pos);
     std::vector<float4> x32(n);
     for (int v = 0; v < n; v++)
@@ -348,6 +388,8 @@ int upload_tables(cloth_s *c)
     CK(cudaMemcpyAsync(base + o_colu, colu.data(), WuS * sizeof(int),
                        cudaMemcpyHostToDevice, s));
     CK(cudaMemcpyAsync(base + o_rowinfo, rowinfo.data(), n * sizeof(int),
+                       cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(base + o_thalo, thalo.data(), ntr * sizeof(int2),
                        cudaMemcpyHostToDevice, s));
     std::vector<int4> dvid;
     std::vector<uint32_t> dsrc;
@@ -419,6 +461,7 @@ int upload_tables(cloth_s *c)
         h.dent = reinterpret_cast<const uint32_t *>(base + o_dent);
     }
     h.rowinfo = reinterpret_cast<const int *>(base + o_rowinfo);
+    h.thalo = reinterpret_cast<const int2 *>(base + o_thalo);
     h.fptr = reinterpret_cast<const int *>(base + o_fptr);
     h.mass = reinterpret_cast<const float *>(base + o_mass);
     h.grav = reinterpret_cast<const float *>(base + o_grav);
@@ -633,6 +676,50 @@ namespace {
 // ------------------------------------------------------------ batches
 int plan_persistent(cloth_ctx *ctx, Batch *b);
 
+} // namespace
+
+// room left for the bulk SpMV's static shared memory (barriers, stage headers)
+constexpr unsigned kBulkStaticReserve = 2048;
+
+unsigned cloth::detail::bulk_stage_bytes(const std::vector<cloth_s *> &cloths, bool skew,
+                                         bool halo)
+{
+    unsigned best = 0;
+    for (const cloth_s *c : cloths)
+    {
+        const unsigned wl = unsigned(c->h.width_lo), wu = unsigned(c->h.width_up);
+        const bool sk = skew && (c->h.Aw != nullptr || c->mat.bending_model == 1);
+        unsigned b = kTile * 4u + wl * kTile * 8u + wu * kTile * (28u + (sk ? 16u : 0u));
+        if (halo)
+            b += 32u * unsigned(std::min(c->max_halo, kBulkHaloCap));
+        best = std::max(best, (b + 127u) & ~127u);
+    }
+    return best;
+}
+
+unsigned cloth::detail::bulk_smem(const GraphLoopVariant &v, unsigned stage_bytes)
+{
+    return v.bulk_stages ? unsigned(v.bulk_stages) * stage_bytes : 0u;
+}
+
+int cloth::detail::bulk_occupancy(const GraphLoopVariant &v, unsigned stage_bytes, int max_smem)
+{
+    const unsigned sm = bulk_smem(v, stage_bytes);
+    // the kernels' dynamic shared memory limit is set to max_smem - kBulkStaticReserve
+    if (!v.bulk_stages || sm == 0 || sm + kBulkStaticReserve > unsigned(max_smem))
+        return 0;
+    int occ = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, v.func, kBulkThreads, sm) !=
+        cudaSuccess)
+    {
+        cudaGetLastError();
+        return 0;
+    }
+    return occ;
+}
+
+namespace {
+
 int make_batch(cloth_ctx *ctx, const std::vector<cloth_s *> &members,
                std::unique_ptr<Batch> &out)
 {
@@ -686,6 +773,8 @@ int make_batch(cloth_ctx *ctx, const std::vector<cloth_s *> &members,
     auto cap = [&](int occ) { return std::max(1, ctx->num_sms * occ * 8); };
     b->grid_tri = std::max(1, std::min(b->n_tt, cap(ctx->occ_tri)));
     b->grid_row = std::max(1, std::min(b->n_rt, cap(ctx->occ_row)));
+    b->bulk_stage[0] = bulk_stage_bytes(members, b->skew, false);
+    b->bulk_stage[1] = bulk_stage_bytes(members, b->skew, true);
     b->set_variants(ctx->tune_spmv, ctx->tune_update);
     int rc = plan_persistent(ctx, b.get());
     if (rc != CLOTH_OK)
@@ -889,13 +978,14 @@ int plan_persistent(cloth_ctx *ctx, Batch *b)
 }
 
 int add_kernel(cudaGraph_t g, cudaGraphNode_t *node, const cudaGraphNode_t *deps,
-               size_t ndeps, void *func, int grid, int block, void **args)
+               size_t ndeps, void *func, int grid, int block, void **args, unsigned smem = 0)
 {
     cudaKernelNodeParams p;
     std::memset(&p, 0, sizeof(p));
     p.func = func;
     p.gridDim = dim3(grid);
     p.blockDim = dim3(block);
+    p.sharedMemBytes = smem;
     p.kernelParams = args;
     CK(cudaGraphAddKernelNode(node, g, deps, ndeps, &p));
     return CLOTH_OK;
@@ -958,7 +1048,8 @@ int build_graph(Batch *b, bool full, cudaGraphExec_t *exec)
     }
     if (b->persist_ok)
     {
-        void *a_per[] = {&b->d_descs, &b->d_work, &b->halo_cap, &b->rows_cap};
+        b->spin = b->ctx->spin;
+        void *a_per[] = {&b->d_descs, &b->d_work, &b->halo_cap, &b->rows_cap, &b->spin};
         if (rc == CLOTH_OK)
         {
             // the team barriers' arrival counts start at zero
@@ -1019,7 +1110,7 @@ int build_graph(Batch *b, bool full, cudaGraphExec_t *exec)
             cudaGraphNode_t k3, k4;
             const int gred = reduce_grid(ninst);
             rc = add_kernel(body, &k1, nullptr, 0, const_cast<void *>(sv.func), b->grid_spmv,
-                            kTile / sv.rows_per_thread, a_spmv);
+                            spmv_block(sv), a_spmv, b->smem_spmv);
             if (rc == CLOTH_OK)
                 rc = add_kernel(body, &k3, &k1, 1, (void *)k_reduce_pq, gred, kTile, a_red);
             if (rc == CLOTH_OK)
@@ -1075,7 +1166,8 @@ int launch_persistent(Batch *b)
 {
     cloth_ctx *ctx = b->ctx;
     PhaseTimer t(ctx, PH_SPMV);
-    void *args[] = {&b->d_descs, &b->d_work, &b->halo_cap, &b->rows_cap};
+    b->spin = ctx->spin;
+    void *args[] = {&b->d_descs, &b->d_work, &b->halo_cap, &b->rows_cap, &b->spin};
     CK(cudaMemsetAsync(b->d_work + b->grid_persist, 0,
                        size_t(b->grid_persist) * sizeof(unsigned long long), ctx->stream));
     CK(cudaLaunchCooperativeKernel(persistent_kernel(b),
@@ -1111,14 +1203,20 @@ int launch_solve_host(Batch *b, int max_iters)
         {
             {
                 PhaseTimer t(ctx, PH_SPMV);
-                cudaLaunchKernel(sv.func, dim3(b->grid_spmv), dim3(kTile / sv.rows_per_thread),
-                                 a_spmv, 0, s);
+                cudaLaunchKernel(sv.func, dim3(b->grid_spmv), dim3(spmv_block(sv)), a_spmv,
+                                 b->smem_spmv, s);
+            }
+            {
+                PhaseTimer t(ctx, PH_REDUCE);
                 cudaLaunchKernel((const void *)k_reduce_pq, dim3(gred), dim3(kTile), a_red, 0, s);
             }
             {
                 PhaseTimer t(ctx, PH_UPDATE);
                 cudaLaunchKernel(uv.func, dim3(b->grid_update),
                                  dim3(kTile / uv.rows_per_thread), a_upd, 0, s);
+            }
+            {
+                PhaseTimer t(ctx, PH_REDUCE);
                 cudaLaunchKernel((const void *)k_reduce_rz, dim3(gred), dim3(kTile), a_red, 0, s);
             }
         }
@@ -1162,7 +1260,8 @@ int read_stats(Batch *b, cloth_solve_stats *stats)
         CK(cudaMemcpy(&st, b->members[i]->d_state, sizeof(st), cudaMemcpyDeviceToHost));
         cloth_solve_stats &o = stats[i];
         o.iters = st.iter;
-        o.status = st.status;
+        // a bounded device wait that gave up flags the team (bar_err)
+        o.status = st.bar_err ? CLOTH_ERR_TIMEOUT : st.status;
         o.res_norm = std::sqrt(std::max(0.0, st.rr));
         o.rhs_norm = std::sqrt(std::max(0.0, st.bb));
         o.rel_residual = o.rhs_norm > 0 ? o.res_norm / o.rhs_norm : o.res_norm;
@@ -1256,9 +1355,10 @@ int autotune_graph_loop(Batch *b)
         k_snap_state<<<std::max(1, std::min(ninst, 1024)), 64, 0, s>>>(
             b->d_descs, b->d_inst, ninst, sts, b->d_ctl, ctl_buf, restore);
     };
-    auto time_launch = [&](const GraphLoopVariant &v, int grid, void **args) -> float {
+    auto time_launch = [&](const GraphLoopVariant &v, int grid, void **args,
+                           unsigned smem = 0) -> float {
         cudaEventRecord(e0, s);
-        cudaLaunchKernel(v.func, dim3(grid), dim3(kTile / v.rows_per_thread), args, 0, s);
+        cudaLaunchKernel(v.func, dim3(grid), dim3(spmv_block(v)), args, smem, s);
         cudaEventRecord(e1, s);
         cudaEventSynchronize(e1);
         float ms = 0.f;
@@ -1274,13 +1374,18 @@ int autotune_graph_loop(Batch *b)
     for (int v = 0; v < kNumSpmvVariants; v++)
     {
         float tv = 1e30f;
+        if (!b->spmv_usable(v))
+        {
+            ctx->tune_ms_spmv[v] = 0.f; // its stages do not fit in shared memory
+            continue;
+        }
         for (int wv : kWaves)
         {
             const int g = b->grid_for(b->spmv_variant(v), b->spmv_occ(v), wv);
             float t = 1e30f;
             for (int rep = 0; rep < 4; rep++)
             {
-                const float ms = time_launch(b->spmv_variant(v), g, a_spmv);
+                const float ms = time_launch(b->spmv_variant(v), g, a_spmv, b->spmv_smem_of(v));
                 if (rep > 0)
                     t = std::min(t, ms);
             }
@@ -1297,7 +1402,8 @@ int autotune_graph_loop(Batch *b)
     // leave the state of iteration 0 with alpha set, as the loop expects it
     cudaLaunchKernel(b->spmv_variant(best_s).func,
                      dim3(b->grid_for(b->spmv_variant(best_s), b->spmv_occ(best_s), best_sw)),
-                     dim3(kTile / b->spmv_variant(best_s).rows_per_thread), a_spmv, 0, s);
+                     dim3(spmv_block(b->spmv_variant(best_s))), a_spmv,
+                     b->spmv_smem_of(best_s), s);
     {
         const int *no_count = nullptr;
         int ni = ninst;
@@ -1520,12 +1626,15 @@ int cloth_ctx_create(int device, cloth_ctx **out)
     c->occ_spmv_skew.assign(kNumSpmvVariants, 1);
     for (int v = 0; v < kNumSpmvVariants; v++)
     {
+        for (const GraphLoopVariant *tab : {kSpmvVariants, kSpmvSkewVariants})
+            if (tab[v].bulk_stages)
+                CK(cudaFuncSetAttribute(tab[v].func, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        c->max_smem_optin - int(kBulkStaticReserve)));
         CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-            &c->occ_spmv[v], kSpmvVariants[v].func, kTile / kSpmvVariants[v].rows_per_thread,
+            &c->occ_spmv[v], kSpmvVariants[v].func, spmv_block(kSpmvVariants[v]), 0));
+        CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+            &c->occ_spmv_skew[v], kSpmvSkewVariants[v].func, spmv_block(kSpmvSkewVariants[v]),
             0));
-        CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-            &c->occ_spmv_skew[v], kSpmvSkewVariants[v].func,
-            kTile / kSpmvSkewVariants[v].rows_per_thread, 0));
     }
     for (int v = 0; v < kNumUpdateVariants; v++)
         CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
@@ -1632,6 +1741,21 @@ int cloth_ctx_set_solver(cloth_ctx *ctx, int solver)
     std::lock_guard<std::recursive_mutex> lk(ctx->mu);
     cudaStreamSynchronize(ctx->stream);
     ctx->solver = solver;
+    ctx->last_batch.reset();
+    for (auto *c : ctx->cloths)
+        c->self.reset();
+    return CLOTH_OK;
+}
+
+int cloth_ctx_set_spin_limit(cloth_ctx *ctx, unsigned polls, unsigned extra_arrivals)
+{
+    if (!ctx)
+        return fail(CLOTH_ERR_INVALID, "cloth_ctx_set_spin_limit: NULL context");
+    std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+    cudaStreamSynchronize(ctx->stream);
+    ctx->spin.limit = polls ? polls : kSpinLimitDefault;
+    ctx->spin.extra = extra_arrivals;
+    // launch sets carry the setting in their kernel arguments: rebuild them
     ctx->last_batch.reset();
     for (auto *c : ctx->cloths)
         c->self.reset();
@@ -2226,7 +2350,7 @@ int cloth_get_stats(cloth_t *c, cloth_solve_stats *stats)
     InstState st;
     CK(cudaMemcpy(&st, c->d_state, sizeof(st), cudaMemcpyDeviceToHost));
     stats->iters = st.iter;
-    stats->status = st.status;
+    stats->status = st.bar_err ? CLOTH_ERR_TIMEOUT : st.status;
     stats->res_norm = std::sqrt(std::max(0.0, st.rr));
     stats->rhs_norm = std::sqrt(std::max(0.0, st.bb));
     stats->rel_residual = stats->rhs_norm > 0 ? stats->res_norm / stats->rhs_norm

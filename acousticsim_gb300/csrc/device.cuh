@@ -125,6 +125,7 @@ struct InstDesc
     const uint32_t *hsrc; // [slot][stride] first record << 5 | record count
     const float *kb;      // [slot][stride] bending scalar (+K_b)
     const int *rowinfo;   // len | diag_slot << 8
+    const int2 *thalo;    // per 128-row tile: the column range [x, y) its rows touch
     const int *fptr;      // nv+1 force-record ranges
     const float *mass;    // nv
     const float *grav;    // nv: gravity force (y component)
@@ -203,7 +204,18 @@ constexpr int kRedRows = 32;                 // team ranges align to 32-row chun
 constexpr int kSlotUnroll = 2;               // ELL slots whose loads are issued together
 constexpr int kStageUnroll = 2;              // staged z rows per thread loaded together
 constexpr int kMaxBlockRows = 16384;         // rows one persistent block may own
-constexpr unsigned kSpinLimit = 1u << 25;    // bounded barrier wait (~seconds)
+constexpr unsigned kSpinLimitDefault = 1u << 25; // bounded barrier wait (~seconds)
+
+// Bounded waits of the persistent solvers' team barriers: a wait gives up
+// after `limit` polls (the team's error flag is set and the solve ends with
+// CLOTH_ERR_TIMEOUT).  `extra` arrivals are added to every barrier's target:
+// 0 in normal use; a test sets it to make the waits run out (arrivals that no
+// block makes), which exercises the timeout path without any device fault.
+struct SpinCfg
+{
+    unsigned limit;
+    unsigned extra;
+};
 
 // One variant of a graph-loop kernel: R rows per thread (blocks of kTile / R
 // threads), U ELL slots whose loads are issued together (SpMV only), TPB
@@ -214,7 +226,15 @@ struct GraphLoopVariant
     int slot_unroll;
     int tiles_per_block;
     const void *func;
+    int bulk_stages; // > 0: bulk-staged SpMV with a ring of this many stages
+    int bulk_halo;   // the bulk SpMV also stages p over each tile's column range
 };
+
+// Bulk-staged SpMV (k_spmv_bulk): kTile consumer threads plus one producer
+// warp per block; a tile's staged column range (halo) holds at most
+// kBulkHaloCap rows, wider tiles gather p from global memory.
+constexpr int kBulkThreads = kTile + 32;
+constexpr int kBulkHaloCap = 2048;
 
 // Batch-wide control words (one per launch set).
 struct BatchCtl

@@ -41,6 +41,11 @@ extern const GraphLoopVariant kUpdateVariants[];
 extern const int kNumSpmvVariants;
 extern const int kNumUpdateVariants;
 constexpr int kDefaultSpmvVariant = 3;   // R = 2, U = 1, TPB = 1 until a tuner says otherwise
+// threads per block of an SpMV variant
+inline int spmv_block(const GraphLoopVariant &v)
+{
+    return v.bulk_stages ? kBulkThreads : kTile / v.rows_per_thread;
+}
 constexpr int kDefaultUpdateVariant = 1; // R = 2, TPB = 1
 __global__ void k_snap_rows(InstDesc *const *descs, const Tile *tiles, const BatchCtl *ctl,
                             float4 *buf, int restore);
@@ -52,15 +57,15 @@ __global__ void k_sync_x32(InstDesc *d);
 __global__ void k_ir_start(InstDesc *const *descs, const Tile *tiles, BatchCtl *ctl,
                            const double *rhs64);
 __global__ void k_pcg_persistent_sm(InstDesc *const *descs, const TeamBlock *work,
-                                    int halo_cap, int rows_cap);
+                                    int halo_cap, int rows_cap, SpinCfg sc);
 __global__ void k_pcg_persistent_gm(InstDesc *const *descs, const TeamBlock *work,
-                                    int halo_cap, int rows_cap);
+                                    int halo_cap, int rows_cap, SpinCfg sc);
 __global__ void k_pcg_persistent_sm_skew(InstDesc *const *descs, const TeamBlock *work,
-                                         int halo_cap, int rows_cap);
+                                         int halo_cap, int rows_cap, SpinCfg sc);
 __global__ void k_pcg_persistent_gm_skew(InstDesc *const *descs, const TeamBlock *work,
-                                         int halo_cap, int rows_cap);
+                                         int halo_cap, int rows_cap, SpinCfg sc);
 __global__ void k_pcg1_persistent(InstDesc *const *descs, const TeamBlock *work, int halo_cap,
-                                  int rows_cap);
+                                  int rows_cap, SpinCfg sc);
 
 // ---------------------------------------------------------------- plain path
 struct PlainState;
@@ -134,6 +139,9 @@ struct cloth_ctx_s
     int tune_spmv = cloth::kDefaultSpmvVariant, tune_update = cloth::kDefaultUpdateVariant;
     std::vector<float> tune_ms_spmv, tune_ms_update; // the last tuning's timings
     int max_smem_optin = 0;
+    // bounded waits of the persistent solvers (cloth_ctx_set_spin_limit; the
+    // extra arrivals are the timeout test's hook, 0 otherwise)
+    cloth::SpinCfg spin = {cloth::kSpinLimitDefault, 0u};
     int solver = 0; // 0: persistent cooperative PCG when the set fits, 1: graph loop
     bool prof = false;
     double prof_ms[CLOTH_NUM_PHASES] = {};
@@ -165,6 +173,7 @@ struct cloth_s
     size_t scratch_bytes = 0;
     cloth::ScratchLayout sl;
     int width_up = 1;         // planes of the stored (diagonal + upper) blocks
+    int max_halo = 0;         // widest column range of a 128-row tile
     cloth_server_s *server = nullptr;
     cloth_f64_s *f64 = nullptr; // FP64 work arrays (refinement, FP64 PCG), on first use
     bool dx64_valid = false;    // the last solve left an FP64 dx (refined or FP64 PCG)
@@ -188,6 +197,17 @@ struct cloth_s
 
 namespace cloth {
 namespace detail {
+
+// Shared memory of one stage of the bulk-staged SpMV for a set of cloths:
+// the widest cloth's row info, lower-slot columns and transposed-block
+// indices, upper-slot columns and stored blocks (skew parts with `skew`) for
+// 128 rows, plus p_old and z over its widest tile halo (at most kBulkHaloCap
+// rows), rounded to 128 bytes.
+unsigned bulk_stage_bytes(const std::vector<cloth_s *> &cloths, bool skew, bool halo);
+// Dynamic shared memory and resident blocks per SM of a bulk SpMV variant
+// with that stage size (0 blocks: it does not fit).
+unsigned bulk_smem(const GraphLoopVariant &v, unsigned stage_bytes);
+int bulk_occupancy(const GraphLoopVariant &v, unsigned stage_bytes, int max_smem);
 
 // Points the scratch fields of h at base (null: clears them).
 void bind_scratch(const cloth_s *c, InstDesc &h, char *base);

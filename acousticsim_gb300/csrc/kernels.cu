@@ -1167,6 +1167,554 @@ __global__ void __launch_bounds__(kTile / R) k_update_t(InstDesc *const *descs,
     }
 }
 
+// ------------------------------------------------------------------ bulk-staged SpMV
+// The same SpMV as k_spmv_t (R = 1: one row per thread, the same slot order
+// and arithmetic, so the results are bit-identical), with the streamed data
+// moved by the copy engine instead of by dependent loads.  For every tile, one
+// thread issues bulk asynchronous copies (cp.async.bulk, completion counted
+// on an mbarrier) of the tile's row info, lower-slot columns and
+// transposed-block indices, upper-slot columns and stored blocks, and the z
+// and p_old rows of the tile's column range (its halo); a ring of NST stages
+// in shared memory keeps NST - 1 tiles in flight while the block computes one.
+// The compute then reads everything from shared memory except the lower
+// slots' transposed blocks, gathered from L2 (a neighbouring tile streamed
+// them moments before).  p = z + beta p_old is formed once per halo row in
+// shared memory.  A tile whose halo does not fit in its stage gathers z and
+// p_old from global memory instead.
+namespace {
+
+struct BulkHdr
+{
+    int go;                 // instance active: the stage is (being) filled
+    int start, nrows;       // first row, rows of the tile in the instance
+    int h0, nh;             // halo rows [h0, h0 + nh) staged (nh = 0: not staged)
+    int skew;               // the stage holds skew block parts
+    int tile_idx, nt;       // partial-sum slot
+    float beta;
+    unsigned o_cl, o_li, o_cu, o_a0, o_a1, o_aw, o_z, o_p; // byte offsets in the stage
+    const float4 *A0;       // transposed-block gathers
+    const float2 *A1;
+    const float4 *Aw;
+    const float4 *z, *pold; // halo fallback gathers
+    float4 *pnew, *q;
+    double *part;
+    InstState *st;
+};
+
+__device__ __forceinline__ unsigned smem_addr(const void *p)
+{
+    return static_cast<unsigned>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void mbar_init(uint64_t *bar, unsigned count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count)
+                 : "memory");
+}
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *bar, unsigned bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.release.cta.shared::cta.b64 _, [%0], %1;" ::"r"(
+                     smem_addr(bar)),
+                 "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar)
+{
+    asm volatile("mbarrier.arrive.release.cta.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar))
+                 : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, unsigned parity)
+{
+    unsigned ok;
+    asm volatile("{\n\t.reg .pred p;\n\t"
+                 "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                 "selp.u32 %0, 1, 0, p;\n\t}"
+                 : "=r"(ok)
+                 : "r"(smem_addr(bar)), "r"(parity)
+                 : "memory");
+    return ok != 0;
+}
+// global -> shared bulk copy (16-byte aligned addresses, size a multiple of 16)
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, unsigned bytes,
+                                         uint64_t *bar)
+{
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], "
+                 "%2, [%3];" ::"r"(smem_addr(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_addr(bar))
+                 : "memory");
+}
+__device__ __forceinline__ unsigned dynamic_smem_bytes()
+{
+    unsigned r;
+    asm("mov.u32 %0, %%dynamic_smem_size;" : "=r"(r));
+    return r;
+}
+
+// A stage's wait gives up after this long (each try_wait may suspend the
+// thread for a while, so the bound is on the global timer, not on polls).
+constexpr unsigned long long kBulkWaitNs = 2000000000ull;
+__device__ __forceinline__ unsigned long long global_ns()
+{
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// What the producer warp needs of one tile: its lane k resolves tile
+// j + k's dependent loads (tile list -> descriptor -> halo table, and the
+// instance state) for 32 tiles at once, ahead of their copies.
+struct BulkMeta
+{
+    int go, start, nv, S, wl, wu, nt, it;
+    int hx, hy;
+    float beta;
+    const int *rowinfo, *col, *colu;
+    const uint32_t *lidx;
+    const float4 *A0, *Aw, *z;
+    const float2 *A1;
+    float4 *p0, *p1, *q;
+    double *part;
+    InstState *st;
+};
+
+__device__ __forceinline__ void bulk_meta(const Tile *tiles, int ti, BulkMeta &m)
+{
+    const Tile tl = tiles[ti];
+    const InstDesc *dp = tl.d;
+    m.st = tl.st;
+    m.start = tl.start;
+    m.go = __ldcg(&tl.st->active);
+    m.it = __ldcg(&tl.st->iter);
+    m.beta = float(__ldcg(&tl.st->beta));
+    m.nv = __ldg(&dp->nv);
+    m.S = __ldg(&dp->stride);
+    m.wl = __ldg(&dp->width_lo);
+    m.wu = __ldg(&dp->width_up);
+    m.nt = __ldg(&dp->ntile_rows);
+    m.rowinfo = ldg_ptr(&dp->rowinfo);
+    m.col = ldg_ptr(&dp->col);
+    m.colu = ldg_ptr(&dp->colu);
+    m.lidx = ldg_ptr(&dp->lidx);
+    m.A0 = ldg_ptr(reinterpret_cast<float4 *const *>(&dp->A0));
+    m.A1 = ldg_ptr(reinterpret_cast<float2 *const *>(&dp->A1));
+    m.Aw = ldg_ptr(reinterpret_cast<float4 *const *>(&dp->Aw));
+    m.z = ldg_ptr(reinterpret_cast<float4 *const *>(&dp->z));
+    m.p0 = ldg_ptr(&dp->p0);
+    m.p1 = ldg_ptr(&dp->p1);
+    m.q = ldg_ptr(&dp->q);
+    m.part = ldg_ptr(&dp->part);
+    const int2 hh = __ldg(ldg_ptr(&dp->thalo) + tl.start / kTile);
+    m.hx = hh.x;
+    m.hy = hh.y;
+}
+
+template <class T> __device__ __forceinline__ T *shfl_ptr(T *p, int src)
+{
+    return reinterpret_cast<T *>(
+        __shfl_sync(0xffffffffu, reinterpret_cast<unsigned long long>(p), src));
+}
+
+// The producer warp fills one stage with the tile whose metadata lane `src`
+// holds (nothing but the phase when its instance is done): lane 0 writes the
+// header and arrives with the stage's byte count, then the lanes share the
+// copies (row info, each plane, the halo of z and p_old).
+template <bool SKEW, bool HALO>
+__device__ __forceinline__ void bulk_issue_warp(const BulkMeta &m, int src, BulkHdr &h,
+                                                unsigned char *stage, unsigned stage_bytes,
+                                                uint64_t *bar, int lane)
+{
+    constexpr unsigned FULLM = 0xffffffffu;
+    const int go = __shfl_sync(FULLM, m.go, src);
+    if (!go)
+    {
+        if (lane == 0)
+        {
+            h.go = 0;
+            mbar_arrive(bar); // nothing to copy: complete the phase now
+        }
+        __syncwarp();
+        return;
+    }
+    const int start = __shfl_sync(FULLM, m.start, src), nv = __shfl_sync(FULLM, m.nv, src);
+    const int S = __shfl_sync(FULLM, m.S, src), wl = __shfl_sync(FULLM, m.wl, src);
+    const int wu = __shfl_sync(FULLM, m.wu, src), it = __shfl_sync(FULLM, m.it, src);
+    const int hx = __shfl_sync(FULLM, m.hx, src), hy = __shfl_sync(FULLM, m.hy, src);
+    const float beta = __shfl_sync(FULLM, m.beta, src);
+    const float4 *A0 = shfl_ptr(m.A0, src), *Aw = shfl_ptr(m.Aw, src), *z = shfl_ptr(m.z, src);
+    const float2 *A1 = shfl_ptr(m.A1, src);
+    float4 *p0 = shfl_ptr(m.p0, src), *p1 = shfl_ptr(m.p1, src);
+    const float4 *pold = (it & 1) ? p1 : p0;
+    const int nrows = min(kTile, nv - start);
+    const int prow = min(kTile, S - start); // plane rows copied: a multiple of 32
+    const bool skew = SKEW && Aw != nullptr;
+    const unsigned o_cl = kTile * 4;
+    const unsigned o_li = o_cl + unsigned(wl) * kTile * 4;
+    const unsigned o_cu = o_li + unsigned(wl) * kTile * 4;
+    const unsigned o_a0 = o_cu + unsigned(wu) * kTile * 4;
+    const unsigned o_a1 = o_a0 + unsigned(wu) * kTile * 16;
+    const unsigned o_aw = o_a1 + unsigned(wu) * kTile * 8;
+    const unsigned o_z = o_aw + (skew ? unsigned(wu) * kTile * 16 : 0u);
+    int nh = hy - hx;
+    const bool two = beta != 0.f;
+    unsigned halo = unsigned(nh) * 16u * (two ? 2u : 1u);
+    if (!HALO || nh <= 0 || o_z + halo > stage_bytes)
+    {
+        nh = 0;
+        halo = 0;
+    }
+    const unsigned o_p = o_z + unsigned(nh) * 16u;
+    const unsigned ri_bytes = unsigned((nrows + 3) & ~3) * 4u;
+    const unsigned pb = unsigned(prow) * 4u;
+    const int kinds = skew ? 4 : 3; // colu, A0, A1 (, Aw) planes per upper slot
+    if (lane == 0)
+    {
+        // the whole header before the arrival: its release publishes the
+        // header to the consumers that acquire the completed phase
+        h.go = 1;
+        h.start = start;
+        h.nrows = nrows;
+        h.h0 = hx;
+        h.nh = nh;
+        h.skew = skew ? 1 : 0;
+        h.tile_idx = start / kTile;
+        h.nt = m.nt;
+        h.beta = beta;
+        h.o_cl = o_cl;
+        h.o_li = o_li;
+        h.o_cu = o_cu;
+        h.o_a0 = o_a0;
+        h.o_a1 = o_a1;
+        h.o_aw = o_aw;
+        h.o_z = o_z;
+        h.o_p = o_p;
+        h.A0 = A0;
+        h.A1 = A1;
+        h.Aw = Aw;
+        h.z = z;
+        h.pold = pold;
+        h.pnew = (it & 1) ? p0 : p1;
+        h.q = m.q;
+        h.part = m.part;
+        h.st = m.st;
+    }
+    // lane 0 holds nt, q, part and st of its own tile only: broadcast them
+    // above when src != 0
+    if (src != 0)
+    {
+        const int nt = __shfl_sync(FULLM, m.nt, src);
+        float4 *q = shfl_ptr(m.q, src);
+        double *part = shfl_ptr(m.part, src);
+        InstState *st = shfl_ptr(m.st, src);
+        if (lane == 0)
+        {
+            h.nt = nt;
+            h.q = q;
+            h.part = part;
+            h.st = st;
+        }
+    }
+    const unsigned tx = ri_bytes + unsigned(wl) * 2u * pb +
+                        unsigned(wu) * (pb + 4u * pb + 2u * pb + (skew ? 4u * pb : 0u)) + halo;
+    if (lane == 0)
+        mbar_arrive_expect_tx(bar, tx);
+    __syncwarp();
+    const int *rowinfo = shfl_ptr(m.rowinfo, src), *col = shfl_ptr(m.col, src),
+              *colu = shfl_ptr(m.colu, src);
+    const uint32_t *lidx = shfl_ptr(m.lidx, src);
+    const int ncopy = 1 + 2 * wl + kinds * wu + (nh ? (two ? 2 : 1) : 0);
+    for (int c = lane; c < ncopy; c += 32)
+    {
+        if (c == 0)
+            bulk_g2s(stage, rowinfo + start, ri_bytes, bar);
+        else if (c <= wl)
+            bulk_g2s(stage + o_cl + (c - 1) * kTile * 4, col + size_t(c - 1) * S + start, pb, bar);
+        else if (c <= 2 * wl)
+            bulk_g2s(stage + o_li + (c - 1 - wl) * kTile * 4,
+                     lidx + size_t(c - 1 - wl) * S + start, pb, bar);
+        else if (c < 1 + 2 * wl + kinds * wu)
+        {
+            const int k = c - 1 - 2 * wl, kind = k / wu, u = k - kind * wu;
+            const size_t g = size_t(u) * S + start;
+            if (kind == 0)
+                bulk_g2s(stage + o_cu + u * kTile * 4, colu + g, pb, bar);
+            else if (kind == 1)
+                bulk_g2s(stage + o_a0 + u * kTile * 16, A0 + g, 4u * pb, bar);
+            else if (kind == 2)
+                bulk_g2s(stage + o_a1 + u * kTile * 8, A1 + g, 2u * pb, bar);
+            else
+                bulk_g2s(stage + o_aw + u * kTile * 16, Aw + g, 4u * pb, bar);
+        }
+        else if (c == 1 + 2 * wl + kinds * wu)
+            bulk_g2s(stage + o_z, z + hx, unsigned(nh) * 16u, bar);
+        else
+            bulk_g2s(stage + o_p, pold + hx, unsigned(nh) * 16u, bar);
+    }
+}
+
+// What a consumer thread needs of a stage, copied from its header into
+// registers once per tile (the header sits in shared memory, and stores
+// through generic pointers would otherwise force it to be re-read).
+struct BulkRegs
+{
+    int start, h0;
+    float beta;
+    bool skew;
+    const unsigned char *stage;
+    unsigned o_cl, o_li, o_cu, o_a0, o_a1, o_aw, o_z;
+    const float4 *A0;
+    const float2 *A1;
+    const float4 *Aw;
+    const float4 *z, *pold;
+    float4 *pnew, *q;
+};
+
+__device__ __forceinline__ BulkRegs bulk_regs(const BulkHdr &h, const unsigned char *stage)
+{
+    BulkRegs r;
+    r.start = h.start;
+    r.h0 = h.h0;
+    r.beta = h.beta;
+    r.skew = h.skew != 0;
+    r.stage = stage;
+    r.o_cl = h.o_cl;
+    r.o_li = h.o_li;
+    r.o_cu = h.o_cu;
+    r.o_a0 = h.o_a0;
+    r.o_a1 = h.o_a1;
+    r.o_aw = h.o_aw;
+    r.o_z = h.o_z;
+    r.A0 = h.A0;
+    r.A1 = h.A1;
+    r.Aw = h.Aw;
+    r.z = h.z;
+    r.pold = h.pold;
+    r.pnew = h.pnew;
+    r.q = h.q;
+    return r;
+}
+
+// One row of q = A p from a filled stage (thread t = row start + t); returns
+// p.q.  STAGED: p over the tile's column range is in the stage (formed there);
+// otherwise p = z + beta p_old is gathered from global memory at each column.
+template <bool SKEW, bool STAGED>
+__device__ __forceinline__ float bulk_row(const BulkRegs &r, int t)
+{
+    constexpr int CH = 4; // transposed-block gathers in flight together
+    const unsigned char *__restrict__ stage = r.stage;
+    const int row = r.start + t;
+    const int info = reinterpret_cast<const int *>(stage)[t];
+    const int len = info & 255, ds = (info >> 8) & 255;
+    const float4 *__restrict__ P = reinterpret_cast<const float4 *>(stage + r.o_z);
+    const float beta = r.beta;
+    auto pcol = [&](int c) -> float3 {
+        if (STAGED)
+            return xyz(P[c - r.h0]);
+        float3 pc = xyz(__ldg(r.z + c));
+        if (beta != 0.f)
+            pc = pc + beta * xyz(__ldg(r.pold + c));
+        return pc;
+    };
+    const float3 pv = pcol(row);
+    const int *__restrict__ cl = reinterpret_cast<const int *>(stage + r.o_cl) + t;
+    const uint32_t *__restrict__ li = reinterpret_cast<const uint32_t *>(stage + r.o_li) + t;
+    const bool sk = SKEW && r.skew;
+    float3 q = make_float3(0.f, 0.f, 0.f);
+    // lower slots, column order: blocks at the transposed position (L2)
+    for (int s0 = 0; s0 < ds; s0 += CH)
+    {
+        float4 a0[CH], aw[CH];
+        float2 a1[CH];
+        float3 pc[CH];
+#pragma unroll
+        for (int k = 0; k < CH; k++)
+            if (s0 + k < ds)
+            {
+                const uint32_t o = li[(s0 + k) * kTile];
+                a0[k] = __ldcg(r.A0 + o);
+                a1[k] = __ldcg(r.A1 + o);
+                if (sk)
+                    aw[k] = __ldcg(r.Aw + o);
+                pc[k] = pcol(cl[(s0 + k) * kTile]);
+            }
+#pragma unroll
+        for (int k = 0; k < CH; k++)
+            if (s0 + k < ds)
+            {
+                const float A[6] = {a0[k].x, a0[k].y, a0[k].z, a0[k].w, a1[k].x, a1[k].y};
+                q = q + symv(A, pc[k]);
+                if (sk)
+                    q = q - skewv(aw[k], pc[k]);
+            }
+    }
+    // diagonal and upper slots: everything staged
+    const int *__restrict__ cu = reinterpret_cast<const int *>(stage + r.o_cu) + t;
+    const float4 *__restrict__ a0s = reinterpret_cast<const float4 *>(stage + r.o_a0) + t;
+    const float2 *__restrict__ a1s = reinterpret_cast<const float2 *>(stage + r.o_a1) + t;
+    const float4 *__restrict__ aws = reinterpret_cast<const float4 *>(stage + r.o_aw) + t;
+    const int nu = len - ds;
+    for (int u = 0; u < nu; u++)
+    {
+        const float4 a0 = a0s[u * kTile];
+        const float2 a1 = a1s[u * kTile];
+        const float3 pc = (!STAGED && u == 0) ? pv : pcol(cu[u * kTile]);
+        const float A[6] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y};
+        q = q + symv(A, pc);
+        if (sk)
+            q = q + skewv(aws[u * kTile], pc);
+    }
+    r.pnew[row] = f4(pv);
+    r.q[row] = f4(q);
+    return fdot(pv, q);
+}
+
+} // namespace
+
+// Block: kTile consumer threads (one row each) and one producer warp.  The
+// producer walks the block's tiles (blockIdx.x, + gridDim.x, ...), waits for a
+// stage to be released (empty barrier: one arrival per consumer warp), and
+// fills it (full barrier: its arrival plus the copies' bytes); a done
+// instance's tile is announced with go = 0 and no copies.  Consumers sync
+// among themselves on named barrier 1 (the producer never joins it).
+namespace {
+__device__ __forceinline__ void consumer_sync()
+{
+    asm volatile("bar.sync 1, %0;" ::"n"(kTile) : "memory");
+}
+__device__ __forceinline__ bool consumer_all(bool v)
+{
+    unsigned r;
+    asm volatile("{\n\t.reg .pred p, q;\n\t"
+                 "setp.ne.u32 p, %1, 0;\n\t"
+                 "bar.red.and.pred q, 1, %2, p;\n\t"
+                 "selp.u32 %0, 1, 0, q;\n\t}"
+                 : "=r"(r)
+                 : "r"(v ? 1u : 0u), "n"(kTile)
+                 : "memory");
+    return r != 0;
+}
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, unsigned parity)
+{
+    if (mbar_try_wait(bar, parity))
+        return true;
+    const unsigned long long t0 = global_ns();
+    while (!mbar_try_wait(bar, parity))
+        if (global_ns() - t0 > kBulkWaitNs)
+            return false;
+    return true;
+}
+} // namespace
+
+template <int NST, bool SKEW, bool HALO>
+__global__ void __launch_bounds__(kBulkThreads) k_spmv_bulk(InstDesc *const *descs,
+                                                            const Tile *tiles, BatchCtl *ctl,
+                                                            int use_cond,
+                                                            cudaGraphConditionalHandle hcond)
+{
+    extern __shared__ __align__(128) unsigned char bulk_smem[];
+    __shared__ __align__(8) uint64_t full[NST], empty[NST];
+    __shared__ BulkHdr hdr[NST];
+    __shared__ double wsum[kTile / 32];
+    const unsigned stage_bytes = (dynamic_smem_bytes() / NST) & ~127u;
+    const int ntiles = ctl->n_tiles_rows;
+    const int G = gridDim.x;
+    const int nmine = int(blockIdx.x) < ntiles ? (ntiles - 1 - int(blockIdx.x)) / G + 1 : 0;
+    const int tid = threadIdx.x;
+    if (tid == 0)
+    {
+        for (int k = 0; k < NST; k++)
+        {
+            mbar_init(&full[k], 1);
+            mbar_init(&empty[k], kTile / 32);
+        }
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    if (tid >= kTile)
+    {
+        // ---- producer warp: lane k resolves tile j + k's metadata for 32
+        // tiles at a time; the lanes share each tile's copies
+        const int lane = tid - kTile;
+        BulkMeta m;
+        for (int j = 0; j < nmine; j++)
+        {
+            const int stg = j % NST;
+            if ((j & 31) == 0)
+            {
+                m.go = 0;
+                if (j + lane < nmine)
+                    bulk_meta(tiles, blockIdx.x + (j + lane) * G, m);
+            }
+            if (j >= NST)
+            {
+                const bool ok = mbar_wait_bounded(&empty[stg], ((j / NST) - 1) & 1);
+                if (!__all_sync(0xffffffffu, ok))
+                    return; // consumers stuck: they give up on their own bounded waits
+            }
+            bulk_issue_warp<SKEW, HALO>(m, j & 31, hdr[stg], bulk_smem + stg * stage_bytes,
+                                        stage_bytes, &full[stg], lane);
+        }
+        return;
+    }
+    // ---- consumers: one row per thread
+    const int lane = tid & 31, warp = tid >> 5;
+    for (int j = 0; j < nmine; j++)
+    {
+        const int stg = j % NST;
+        unsigned char *stage = bulk_smem + stg * stage_bytes;
+        const bool got = mbar_wait_bounded(&full[stg], (j / NST) & 1);
+        if (!consumer_all(got))
+        {
+            // the stage never completed: flag the instance's team and end its
+            // solve through its sums (a NaN partial), then stop
+            const BulkHdr &hd = hdr[stg];
+            if (tid == 0 && hd.go)
+            {
+                atomicExch(&hd.st->bar_err, 1);
+                hd.part[hd.tile_idx] = __longlong_as_double(0x7ff8000000000000ll);
+            }
+            return;
+        }
+        const BulkHdr &hd = hdr[stg];
+        if (hd.go)
+        {
+            if (hd.nh && hd.beta != 0.f)
+            {
+                // p = z + beta p_old over the halo, in place of z
+                float4 *Z = reinterpret_cast<float4 *>(stage + hd.o_z);
+                const float4 *Po = reinterpret_cast<const float4 *>(stage + hd.o_p);
+                for (int k = tid; k < hd.nh; k += kTile)
+                    Z[k] = f4(xyz(Z[k]) + hd.beta * xyz(Po[k]));
+                consumer_sync();
+            }
+            float pq = 0.f;
+            if (tid < hd.nrows)
+            {
+                const BulkRegs r = bulk_regs(hd, stage);
+                pq = hd.nh ? bulk_row<SKEW, true>(r, tid) : bulk_row<SKEW, false>(r, tid);
+            }
+            // the tile's p.q: FP32 warp sums, FP64 over the warps in order
+            // (group_sum's arithmetic and order)
+            const float t = warp_sum(pq);
+            if (lane == 0)
+                wsum[warp] = double(t);
+            consumer_sync();
+            if (tid == 0)
+            {
+                double v = wsum[0];
+#pragma unroll
+                for (int k = 1; k < kTile / 32; k++)
+                    v += wsum[k];
+                hd.part[hd.tile_idx] = v;
+            }
+        }
+        // release the stage: generic writes to it (the halo's p) are ordered
+        // before the copy engine refills it, and the header before its rewrite
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        consumer_sync();
+        if (lane == 0)
+            mbar_arrive(&empty[stg]);
+    }
+}
+
 // Instance totals of a graph-loop half-iteration (k_reduce_pq, k_reduce_rz):
 // one block per instance of the list adds the instance's per-tile partials (sum_strided over kTile
 // lanes, then group_sum_d: one order, whatever the kernel variant that
@@ -1306,7 +1854,12 @@ __global__ void __launch_bounds__(kTile)
     {2, 2, 1, (const void *)k_spmv_t<2, 2, 1, SK>}, {4, 1, 1, (const void *)k_spmv_t<4, 1, 1, SK>}, \
     {1, 1, 4, (const void *)k_spmv_t<1, 1, 4, SK>}, {1, 2, 4, (const void *)k_spmv_t<1, 2, 4, SK>}, \
     {2, 1, 4, (const void *)k_spmv_t<2, 1, 4, SK>}, {2, 2, 4, (const void *)k_spmv_t<2, 2, 4, SK>}, \
-    {4, 1, 4, (const void *)k_spmv_t<4, 1, 4, SK>}, {2, 1, 8, (const void *)k_spmv_t<2, 1, 8, SK>}
+    {4, 1, 4, (const void *)k_spmv_t<4, 1, 4, SK>}, {2, 1, 8, (const void *)k_spmv_t<2, 1, 8, SK>}, \
+    {1, 0, 2, (const void *)k_spmv_bulk<2, SK, true>, 2, 1},                                  \
+    {1, 0, 3, (const void *)k_spmv_bulk<3, SK, true>, 3, 1},                                  \
+    {0, 0, 2, (const void *)k_spmv_bulk<2, SK, false>, 2, 0},                                 \
+    {0, 0, 3, (const void *)k_spmv_bulk<3, SK, false>, 3, 0},                                 \
+    {0, 0, 4, (const void *)k_spmv_bulk<4, SK, false>, 4, 0}
 extern const GraphLoopVariant kSpmvVariants[] = {SPMV_VARIANTS(false)};
 // the same variants for launch sets holding a dihedral-bending instance
 extern const GraphLoopVariant kSpmvSkewVariants[] = {SPMV_VARIANTS(true)};
@@ -1317,10 +1870,10 @@ extern const GraphLoopVariant kUpdateVariants[] = {
     {2, 0, 4, (const void *)k_update_t<2, 4>}, {1, 0, 8, (const void *)k_update_t<1, 8>},
     {2, 0, 8, (const void *)k_update_t<2, 8>},
 };
-extern const int kNumSpmvVariants = 12;
+extern const int kNumSpmvVariants = 17;
 extern const int kNumUpdateVariants = 7;
-static_assert(sizeof(kSpmvVariants) / sizeof(kSpmvVariants[0]) == 12, "variant count");
-static_assert(sizeof(kSpmvSkewVariants) / sizeof(kSpmvSkewVariants[0]) == 12, "variant count");
+static_assert(sizeof(kSpmvVariants) / sizeof(kSpmvVariants[0]) == 17, "variant count");
+static_assert(sizeof(kSpmvSkewVariants) / sizeof(kSpmvSkewVariants[0]) == 17, "variant count");
 static_assert(sizeof(kUpdateVariants) / sizeof(kUpdateVariants[0]) == 7, "variant count");
 
 // Copies of the PCG state the autotuner disturbs (dx, r, z per row, the
@@ -1410,7 +1963,7 @@ __device__ __forceinline__ unsigned ld_acquire(const unsigned *a)
     return v;
 }
 
-__device__ __forceinline__ bool team_barrier(InstState *st, int nblk)
+__device__ __forceinline__ bool team_barrier(InstState *st, int nblk, const SpinCfg &sc)
 {
     __shared__ int ok;
     __syncthreads();
@@ -1420,7 +1973,7 @@ __device__ __forceinline__ bool team_barrier(InstState *st, int nblk)
         if (nblk > 1)
         {
             const unsigned g = ld_acquire(&st->bar_gen);
-            if (atom_add_acq_rel(&st->bar_count, 1u) == unsigned(nblk - 1))
+            if (atom_add_acq_rel(&st->bar_count, 1u) == unsigned(nblk - 1) + sc.extra)
             {
                 st->bar_count = 0u;
                 red_add_release(&st->bar_gen, 1u);
@@ -1430,7 +1983,7 @@ __device__ __forceinline__ bool team_barrier(InstState *st, int nblk)
                 unsigned n = 0;
                 while (ld_acquire(&st->bar_gen) == g)
                 {
-                    if (++n > kSpinLimit)
+                    if (++n > sc.limit)
                     {
                         atomicExch(&st->bar_err, 1);
                         ok = 0;
@@ -1455,8 +2008,9 @@ __device__ __forceinline__ bool team_barrier(InstState *st, int nblk)
 // error flag is set then).
 __device__ __forceinline__ bool team_barrier_count(unsigned long long *count,
                                                    unsigned long long target, InstState *st,
-                                                   int nblk)
+                                                   int nblk, const SpinCfg &sc)
 {
+    target += sc.extra;
     __shared__ int ok;
     __syncthreads();
     if (threadIdx.x == 0)
@@ -1475,7 +2029,7 @@ __device__ __forceinline__ bool team_barrier_count(unsigned long long *count,
                              : "memory");
                 if (v >= target)
                     break;
-                if (++n > kSpinLimit)
+                if (++n > sc.limit)
                 {
                     atomicExch(&st->bar_err, 1);
                     ok = 0;
@@ -1626,7 +2180,7 @@ template <int NQ> struct WarpFx
 template <bool SM, bool SKEW>
 __device__ __forceinline__ void pcg_persistent_body(InstDesc *const *descs,
                                                     const TeamBlock *work, int halo_cap,
-                                                    int rows_cap)
+                                                    int rows_cap, SpinCfg sc)
 {
     constexpr int NW = kPBlock / 32;
     extern __shared__ float4 sm_dyn[];
@@ -1736,7 +2290,7 @@ __device__ __forceinline__ void pcg_persistent_body(InstDesc *const *descs,
         }
         if (tid == 0)
             s_nbar += (unsigned long long)w.nblk;
-        return team_barrier_count(team_count(), s_nbar, st, w.nblk);
+        return team_barrier_count(team_count(), s_nbar, st, w.nblk, sc);
     };
     // Reads a team sum after the barrier; flags a fixed-point overflow when it
     // disagrees with the FP32 magnitude check.
@@ -2057,31 +2611,31 @@ __device__ __forceinline__ void pcg_persistent_body(InstDesc *const *descs,
 
 __global__ void __launch_bounds__(kPBlock, 1)
     k_pcg_persistent_sm(InstDesc *const *descs, const TeamBlock *work, int halo_cap,
-                        int rows_cap)
+                        int rows_cap, SpinCfg sc)
 {
-    pcg_persistent_body<true, false>(descs, work, halo_cap, rows_cap);
+    pcg_persistent_body<true, false>(descs, work, halo_cap, rows_cap, sc);
 }
 
 __global__ void __launch_bounds__(kPBlock, 1)
     k_pcg_persistent_gm(InstDesc *const *descs, const TeamBlock *work, int halo_cap,
-                        int rows_cap)
+                        int rows_cap, SpinCfg sc)
 {
-    pcg_persistent_body<false, false>(descs, work, halo_cap, rows_cap);
+    pcg_persistent_body<false, false>(descs, work, halo_cap, rows_cap, sc);
 }
 
 // launch sets holding a dihedral-bending instance
 __global__ void __launch_bounds__(kPBlock, 1)
     k_pcg_persistent_sm_skew(InstDesc *const *descs, const TeamBlock *work, int halo_cap,
-                             int rows_cap)
+                             int rows_cap, SpinCfg sc)
 {
-    pcg_persistent_body<true, true>(descs, work, halo_cap, rows_cap);
+    pcg_persistent_body<true, true>(descs, work, halo_cap, rows_cap, sc);
 }
 
 __global__ void __launch_bounds__(kPBlock, 1)
     k_pcg_persistent_gm_skew(InstDesc *const *descs, const TeamBlock *work, int halo_cap,
-                             int rows_cap)
+                             int rows_cap, SpinCfg sc)
 {
-    pcg_persistent_body<false, true>(descs, work, halo_cap, rows_cap);
+    pcg_persistent_body<false, true>(descs, work, halo_cap, rows_cap, sc);
 }
 
 // ------------------------------------------------------------------ single-barrier persistent PCG
@@ -2116,7 +2670,7 @@ __device__ __forceinline__ float3 cg1_residual(float3 r, float3 w, float3 s, flo
 
 __global__ void __launch_bounds__(kPBlock, 1)
     k_pcg1_persistent(InstDesc *const *descs, const TeamBlock *work, int halo_cap,
-                      int rows_cap)
+                      int rows_cap, SpinCfg sc)
 {
     constexpr int NW = kPBlock / 32;
     extern __shared__ float4 sm_dyn[];
@@ -2199,7 +2753,7 @@ __global__ void __launch_bounds__(kPBlock, 1)
                 atomicAdd(&st->acc[bq][q][1], ll);
                 atomicAdd(&st->acc_chk[bq][q], c);
             }
-        return team_barrier(st, w.nblk);
+        return team_barrier(st, w.nblk, sc);
     };
     auto team_value = [&](int q, int bq, int s, int *bad) -> double {
         const double v = fx_value(__ldcg(&st->acc[bq][q][0]), __ldcg(&st->acc[bq][q][1]), s);

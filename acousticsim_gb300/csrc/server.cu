@@ -299,13 +299,14 @@ size_t own_bytes_for(int n, int total_rt, int total_tt, Layout *L = nullptr,
 }
 
 int add_node(cudaGraph_t g, cudaGraphNode_t *node, cudaGraphNode_t *last, void *func,
-             int grid, int block, void **args)
+             int grid, int block, void **args, unsigned smem = 0)
 {
     cudaKernelNodeParams p;
     std::memset(&p, 0, sizeof(p));
     p.func = func;
     p.gridDim = dim3(std::max(1, grid));
     p.blockDim = dim3(block);
+    p.sharedMemBytes = smem;
     p.kernelParams = args;
     SCK(cudaGraphAddKernelNode(node, g, *last ? last : nullptr, *last ? 1 : 0, &p));
     *last = *node;
@@ -323,12 +324,30 @@ int build_chunk_graph(cloth_server_s *s)
     bool skew = false;
     for (const SrvCloth &sc : s->cl)
         skew = skew || sc.c->h.Aw != nullptr || sc.c->mat.bending_model == 1;
-    const GraphLoopVariant &sv =
-        (skew ? kSpmvSkewVariants : kSpmvVariants)[ctx->tune_spmv];
+    const GraphLoopVariant *table = skew ? kSpmvSkewVariants : kSpmvVariants;
+    int sv_i = ctx->tune_spmv;
+    int occ_sv = (skew ? ctx->occ_spmv_skew : ctx->occ_spmv)[sv_i];
+    unsigned smem_sv = 0;
+    if (table[sv_i].bulk_stages)
+    {
+        // stages sized for every registered cloth; the default variant when
+        // they do not fit in shared memory
+        std::vector<cloth_s *> cl;
+        for (const SrvCloth &sc : s->cl)
+            cl.push_back(sc.c);
+        const unsigned stage = bulk_stage_bytes(cl, skew, table[sv_i].bulk_halo != 0);
+        occ_sv = bulk_occupancy(table[sv_i], stage, ctx->max_smem_optin);
+        if (occ_sv > 0)
+            smem_sv = bulk_smem(table[sv_i], stage);
+        else
+        {
+            sv_i = kDefaultSpmvVariant;
+            occ_sv = (skew ? ctx->occ_spmv_skew : ctx->occ_spmv)[sv_i];
+        }
+    }
+    const GraphLoopVariant &sv = table[sv_i];
     const GraphLoopVariant &uv = kUpdateVariants[ctx->tune_update];
-    const int one_wave_spmv =
-        ctx->num_sms *
-        std::max(1, (skew ? ctx->occ_spmv_skew : ctx->occ_spmv)[ctx->tune_spmv]);
+    const int one_wave_spmv = ctx->num_sms * std::max(1, occ_sv);
     const int one_wave_upd = ctx->num_sms * std::max(1, ctx->occ_update[ctx->tune_update]);
     cudaGraph_t g = nullptr;
     SCK(cudaGraphCreate(&g, 0));
@@ -380,7 +399,7 @@ int build_chunk_graph(cloth_server_s *s)
             cudaGraph_t body = cp.conditional.phGraph_out[0];
             cudaGraphNode_t bl = nullptr, bn = nullptr;
             rc = add_node(body, &bn, &bl, const_cast<void *>(sv.func), one_wave_spmv,
-                          kTile / sv.rows_per_thread, a_spmv);
+                          spmv_block(sv), a_spmv, smem_sv);
             if (rc == CLOTH_OK)
                 rc = add_node(body, &bn, &bl, (void *)k_reduce_pq, reduce_grid(n), kTile, a_red);
             if (rc == CLOTH_OK)

@@ -136,21 +136,33 @@ int cloth_ctx_synchronize(cloth_ctx *ctx);
 /* Per-phase CUDA-event timers (cTimeUtil::Begin/End, src/utils/TimeUtil.hpp:7-32).
  * Phases: 0 pins, 1 triangle assembly, 2 row assembly + PCG init,
  * 3 SpMV + p.Ap, 4 update + residual, 5 position update, 6 contact detection,
- * 7 contact repulsion. */
-#define CLOTH_NUM_PHASES 8
+ * 7 contact repulsion, 8 instance totals of the graph-loop PCG (k_reduce_*). */
+#define CLOTH_NUM_PHASES 9
 int cloth_ctx_set_profiling(cloth_ctx *ctx, int enable);
 int cloth_ctx_get_profile(cloth_ctx *ctx, double *ms_total, long long *launches);
 int cloth_ctx_reset_profile(cloth_ctx *ctx);
 /* Preferred PCG driver for launch sets built after the call. */
 int cloth_ctx_set_solver(cloth_ctx *ctx, int solver);
+/* Bounded waits of the persistent PCG drivers (no counterpart in the
+ * reference, whose solver never waits on the device). A team barrier gives up
+ * after `polls` polls (0: the default, 2^25, seconds); the solve then ends
+ * with stats status CLOTH_ERR_TIMEOUT and the context stays usable.
+ * `extra_arrivals` is a test hook: every barrier waits for that many arrivals
+ * that no block makes, so the waits run out on purpose (0 in normal use).
+ * Applies to launch sets built afterwards (cached ones are dropped). */
+int cloth_ctx_set_spin_limit(cloth_ctx *ctx, unsigned polls, unsigned extra_arrivals);
 /* Graph-loop kernel variants (the batched and served PCG): rows per thread R
  * of the SpMV and update kernels, the SpMV's slot unroll U and the tiles a
  * block takes at a time (TPB). With autotune on (the default) every graph-loop
  * launch set times all variants on its first step and keeps the fastest; the
  * choice becomes the context's default, which the request server uses. Every
  * variant computes bit-identical results. Variants (SpMV R,U,TPB): 1,1,1
- * 1,2,1 1,3,1 2,1,1 2,2,1 4,1,1 1,1,4 1,2,4 2,1,4 2,2,4 4,1,4 2,1,8;
- * (update R,TPB): 1,1 2,1 4,1 1,4 2,4 1,8 2,8. Others: CLOTH_ERR_INVALID.
+ * 1,2,1 1,3,1 2,1,1 2,2,1 4,1,1 1,1,4 1,2,4 2,1,4 2,2,4 4,1,4 2,1,8, and
+ * 1,0,2 1,0,3: the bulk-staged SpMV (a producer warp streams each tile's
+ * matrix planes and p over its column range into a ring of 2 or 3
+ * shared-memory stages with bulk asynchronous copies; used when the stages
+ * fit in shared memory); (update R,TPB): 1,1 2,1 4,1 1,4 2,4 1,8 2,8.
+ * Others: CLOTH_ERR_INVALID.
  * Applies to launch sets built afterwards. */
 int cloth_ctx_set_kernel_variant(cloth_ctx *ctx, int spmv_rows_per_thread,
                                  int spmv_slot_unroll, int spmv_tiles_per_block,

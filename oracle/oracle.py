@@ -21,6 +21,22 @@ PI = C.POINTER(C.c_int)
 PU8 = C.POINTER(C.c_ubyte)
 
 
+def build(force: bool = False) -> Path:
+    """Compiles libcloth_oracle.so from oracle/cloth_oracle.c when it is missing
+    or older than its sources (gcc, OpenMP, no contraction of multiply-adds)."""
+    import os
+    import subprocess
+    src = [LIB.parent / "cloth_oracle.c", LIB.parent / "cloth_oracle.h"]
+    if not force and LIB.exists() and all(LIB.stat().st_mtime >= p.stat().st_mtime
+                                          for p in src):
+        return LIB
+    tmp = LIB.with_name("libcloth_oracle.build.so")
+    subprocess.run(["gcc", "-O2", "-std=gnu11", "-fPIC", "-shared", "-ffp-contract=off",
+                    "-fopenmp", "-o", str(tmp), str(src[0]), "-lm"], check=True)
+    os.replace(tmp, LIB)
+    return LIB
+
+
 def lib() -> C.CDLL:
     global _lib
     if _lib is None:
@@ -284,6 +300,23 @@ class OracleCloth:
 
 
 # ---------------------------------------------------------------- collisions
+def derive_edges(tris) -> np.ndarray:
+    """Edges (v0, v1, tri0, tri1) of a triangle list in cObjUtil::BuildEdge's
+    numbering (src/utils/ObjUtil.cpp: ascending vertex pairs, first and second
+    triangle, tri1 = -1 on the boundary)."""
+    tris = np.asarray(tris, np.int64).reshape(-1, 3)
+    seen = {}
+    for t, tv in enumerate(tris):
+        for k in range(3):
+            a, b = int(tv[k]), int(tv[(k + 1) % 3])
+            key = (a, b) if a < b else (b, a)
+            if key in seen:
+                seen[key][1] = t
+            else:
+                seen[key] = [t, -1]
+    return np.array([[k[0], k[1], v[0], v[1]] for k, v in sorted(seen.items())], np.int32)
+
+
 def body_normals(pos, tris):
     """Triangle and vertex normals of a kinematic body as its Init leaves them."""
     pos = np.ascontiguousarray(pos, np.float64)

@@ -99,7 +99,9 @@ def test_solve_matches_direct_solve(ctx, orc, case, solver):
     err = rel(dx, g["sys_dx"].reshape(-1))
     print(case, "iters", st["iters"], "true residual", true_rel, "dx error", err)
     assert true_rel < 5e-6
-    assert err < 1e-3
+    # both solutions are within 1e-6 relative residual of the same system:
+    # measured 4e-6..4e-5 apart on the golden cases
+    assert err < 2e-4
     c.close()
 
 
@@ -154,7 +156,8 @@ def test_multi_step_trajectory_vs_oracle(ctx, orc, solver):
     xg = c.GetPos()
     disp_err = rel(xg - x, oc.x - x)
     print("displacement error after 20 steps", disp_err)
-    assert disp_err < 1e-3
+    # measured ~5e-5 (FP32 assembly and PCG at 1e-7 against the FP64 oracle)
+    assert disp_err < 2e-4
     pins = c.GetConstraintStaticVertices()
     x0 = c.GetInitPos().reshape(-1, 3)
     tgt = x0[pins].astype(np.float32).astype(np.float64)
@@ -201,6 +204,14 @@ def test_kernel_variants_bit_identical(ctx):
     sizes = [12, 40, 23, 33]
     confs = [_grid_conf(n, 2e-3, ks=(10 ** (2 + k % 2), 10 ** (2 + k % 2), 10 ** (1 + k % 2)))
              for k, n in enumerate(sizes)]
+    # a 1100 x 4 strip numbered along its length: its 128-row tiles touch
+    # ~2,300 rows, more than the bulk SpMV stages, so that kernel gathers p
+    # from global memory for it (the other cloths' halos are staged)
+    strip = _grid_conf(4, 2e-3)
+    strip["subdivision"] = [1099, 3]
+    strip["cloth_size"] = [1.1, 0.003]
+    strip["cloth_density"] = 200.0  # heavy enough for the long strip to converge quickly
+    confs.append(strip)
 
     def run(variant, autotune=False):
         ctx.set_solver("graph_loop")
