@@ -219,6 +219,8 @@ int upload_tables(cloth_s *c)
 {
     const Tables &t = c->tab;
     const int n = t.nv, T = t.nt, W = t.width;
+    if (n >= kMaxClothVertices)
+        return fail(CLOTH_ERR_MESH, "cloth_create: more than 2^24 vertices in one cloth");
     const int S = int(align_up(size_t(n), 32));
     // the triangle pass also runs the dihedral edges (indices nt .. nt + n_dih)
     const int ntr = (n + kTile - 1) / kTile, ntt = (T + t.n_dih + kTile - 1) / kTile;
@@ -231,13 +233,14 @@ int upload_tables(cloth_s *c)
         Wu = std::max(Wu, len - t.diag_slot[v]);
         Wl = std::max(Wl, t.diag_slot[v]);
     }
-    const size_t WuS = size_t(Wu) * S, WlS = size_t(std::max(Wl, 1)) * S;
+    // tile-major planes (up_idx / lo_idx): whole 128-row tiles
+    const size_t WuS = size_t(Wu) * ntr * kTile, WlS = size_t(std::max(Wl, 1)) * ntr * kTile;
     c->width_up = Wu;
     Layout L;
     size_t o_tri = L.take<int4>(T), o_tcoef = L.take<float4>(3 * size_t(T)),
            o_tdest = L.take<int4>(3 * size_t(T));
     size_t o_col = L.take<int>(WS), o_hsrc = L.take<uint32_t>(WS), o_kb = L.take<float>(WS),
-           o_lidx = L.take<uint32_t>(WlS), o_colu = L.take<int>(WuS);
+           o_lref = L.take<uint32_t>(WlS), o_colu = L.take<int>(WuS);
     const int nd = t.n_dih;
     const bool dih = c->mat.bending_model == 1;
     size_t o_dvid = 0, o_dfac = 0, o_dsrc = 0, o_dent = 0;
@@ -323,7 +326,7 @@ int upload_tables(cloth_s *c)
         tdest[3 * i + 2] = make_int4(hd[8], fd[0], fd[1], fd[2]);
     }
     std::vector<int> col(WS, 0), colu(WuS, 0), rowinfo(n);
-    std::vector<uint32_t> hsrc(WS, 0u), lidx(WlS, 0u);
+    std::vector<uint32_t> hsrc(WS, 0u), lref(WlS, 0u);
     std::vector<float> kb(WS, 0.f), mass(n), grav(n);
     for (int v = 0; v < n; v++)
     {
@@ -337,14 +340,14 @@ int upload_tables(cloth_s *c)
             hsrc[o] = (uint32_t(t.h_start[k]) << 5) | uint32_t(t.h_count[k]);
             kb[o] = t.kbend[k];
             if (sl >= t.diag_slot[v])
-                colu[size_t(sl - t.diag_slot[v]) * S + v] = t.cols[k];
+                colu[up_idx(sl - t.diag_slot[v], v, Wu)] = t.cols[k];
             if (sl < t.diag_slot[v])
             {
                 // transposed block: row cols[k], the slot holding column v
                 const int cr = t.cols[k];
                 const int *b0 = &t.cols[t.rowptr[cr]], *b1 = &t.cols[t.rowptr[cr + 1]];
                 const int s2 = int(std::lower_bound(b0, b1, v) - b0);
-                lidx[o] = uint32_t(size_t(s2 - t.diag_slot[cr]) * S + size_t(cr));
+                lref[lo_idx(sl, v, Wl)] = (uint32_t(s2 - t.diag_slot[cr]) << 24) | uint32_t(cr);
             }
         }
         mass[v] = float(t.mass[v]);
@@ -383,7 +386,7 @@ int upload_tables(cloth_s *c)
                        cudaMemcpyHostToDevice, s));
     CK(cudaMemcpyAsync(base + o_kb, kb.data(), WS * sizeof(float),
                        cudaMemcpyHostToDevice, s));
-    CK(cudaMemcpyAsync(base + o_lidx, lidx.data(), WlS * sizeof(uint32_t),
+    CK(cudaMemcpyAsync(base + o_lref, lref.data(), WlS * sizeof(uint32_t),
                        cudaMemcpyHostToDevice, s));
     CK(cudaMemcpyAsync(base + o_colu, colu.data(), WuS * sizeof(int),
                        cudaMemcpyHostToDevice, s));
@@ -450,7 +453,7 @@ int upload_tables(cloth_s *c)
     h.col = reinterpret_cast<const int *>(base + o_col);
     h.hsrc = reinterpret_cast<const uint32_t *>(base + o_hsrc);
     h.kb = reinterpret_cast<const float *>(base + o_kb);
-    h.lidx = reinterpret_cast<const uint32_t *>(base + o_lidx);
+    h.lref = reinterpret_cast<const uint32_t *>(base + o_lref);
     h.colu = reinterpret_cast<const int *>(base + o_colu);
     if (dih)
     {
@@ -689,7 +692,7 @@ unsigned cloth::detail::bulk_stage_bytes(const std::vector<cloth_s *> &cloths, b
     {
         const unsigned wl = unsigned(c->h.width_lo), wu = unsigned(c->h.width_up);
         const bool sk = skew && (c->h.Aw != nullptr || c->mat.bending_model == 1);
-        unsigned b = kTile * 4u + wl * kTile * 8u + wu * kTile * (28u + (sk ? 16u : 0u));
+        unsigned b = kTile * 4u + wl * kTile * 4u + wu * kTile * (28u + (sk ? 16u : 0u));
         if (halo)
             b += 32u * unsigned(std::min(c->max_halo, kBulkHaloCap));
         best = std::max(best, (b + 127u) & ~127u);
@@ -1254,14 +1257,19 @@ int read_stats(Batch *b, cloth_solve_stats *stats)
     if (!stats)
         return CLOTH_OK;
     CK(cudaStreamSynchronize(b->ctx->stream));
+    // a bounded wait of the graph-loop kernels that gave up (sticky: cleared here)
+    int ctl_err = 0;
+    CK(cudaMemcpy(&ctl_err, &b->d_ctl->err, sizeof(int), cudaMemcpyDeviceToHost));
+    if (ctl_err)
+        CK(cudaMemset(&b->d_ctl->err, 0, sizeof(int)));
     for (size_t i = 0; i < b->members.size(); i++)
     {
         InstState st;
         CK(cudaMemcpy(&st, b->members[i]->d_state, sizeof(st), cudaMemcpyDeviceToHost));
         cloth_solve_stats &o = stats[i];
         o.iters = st.iter;
-        // a bounded device wait that gave up flags the team (bar_err)
-        o.status = st.bar_err ? CLOTH_ERR_TIMEOUT : st.status;
+        // a bounded device wait that gave up flags the team (bar_err) or the set
+        o.status = (st.bar_err || ctl_err) ? CLOTH_ERR_TIMEOUT : st.status;
         o.res_norm = std::sqrt(std::max(0.0, st.rr));
         o.rhs_norm = std::sqrt(std::max(0.0, st.bb));
         o.rel_residual = o.rhs_norm > 0 ? o.res_norm / o.rhs_norm : o.res_norm;
@@ -2405,7 +2413,7 @@ int cloth_export_system(cloth_t *c, int *ell, float *A, float *b, float *fint,
     {
         // stored diagonal + upper blocks; a lower block is its transposed
         // upper block (the same symmetric 6 floats)
-        const size_t WuS = size_t(c->width_up) * S;
+        const size_t WuS = size_t(c->width_up) * c->h.ntile_rows * kTile;
         std::vector<float4> a0(WuS), aw(c->h.Aw ? WuS : 0);
         std::vector<float2> a1(WuS);
         CK(cudaMemcpy(a0.data(), c->h.A0, WuS * sizeof(float4), cudaMemcpyDeviceToHost));
@@ -2419,13 +2427,13 @@ int cloth_export_system(cloth_t *c, int *ell, float *A, float *b, float *fint,
                 const int ds = t.diag_slot[v];
                 size_t o;
                 if (s >= ds)
-                    o = size_t(s - ds) * S + v;
+                    o = up_idx(s - ds, v, c->width_up);
                 else
                 {
                     const int cr = t.cols[size_t(t.rowptr[v]) + s];
                     const int *b0 = &t.cols[t.rowptr[cr]], *b1 = &t.cols[t.rowptr[cr + 1]];
                     const int s2 = int(std::lower_bound(b0, b1, v) - b0);
-                    o = size_t(s2 - t.diag_slot[cr]) * S + size_t(cr);
+                    o = up_idx(s2 - t.diag_slot[cr], cr, c->width_up);
                 }
                 float e[6] = {a0[o].x, a0[o].y, a0[o].z, a0[o].w, a1[o].x, a1[o].y};
                 float full[9] = {e[0], e[1], e[2], e[1], e[3], e[4], e[2], e[4], e[5]};

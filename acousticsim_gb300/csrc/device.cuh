@@ -16,13 +16,14 @@
 // symmetric, the pin projection zeroes both), so only the diagonal and upper
 // blocks (column >= row) are stored: row i's slots are sorted by column, the
 // first diag_slot(i) of them are lower, and upper slot s lives in plane
-// u = s - diag_slot(i) (u = 0: the diagonal block).  A lower slot keeps its
-// column and the plane index of its transposed block (lidx); the SpMV fetches
-// that block, which another row of the same launch has just streamed, from
-// L2.  The SpMV walks the lower slots by s and the upper ones by u, with the
-// upper columns in planes of their own (colu), so that at every step the 32
-// rows of a warp read one plane of each array: coalesced, whatever the rows'
-// diag_slot.
+// u = s - diag_slot(i) (u = 0: the diagonal block).  A lower slot keeps a
+// reference to its transposed block (lref: that block's plane and column);
+// the SpMV fetches the block, which another row of the same launch has just
+// streamed, from L2.  The SpMV walks the lower slots by s and the upper ones
+// by u, with the upper columns in planes of their own (colu), so that at
+// every step the 32 rows of a warp read one plane of each array: coalesced,
+// whatever the rows' diag_slot.  The stored blocks, colu and lref are kept
+// tile-major (up_idx / lo_idx below).
 #pragma once
 #include <cstdint>
 #include <cuda_runtime.h>
@@ -102,7 +103,7 @@ struct InstState
 struct InstDesc
 {
     int nv, nt, width, stride;   // stride: padded row count of slot-major planes
-    int width_lo, width_up;      // planes of lower slots (lidx) and of stored blocks
+    int width_lo, width_up;      // planes of lower slots (lref) and of stored blocks
     int ntile_rows, ntile_tris;
     int warm_start;
     int fix_fv_norm;
@@ -120,8 +121,9 @@ struct InstDesc
     const int4 *tdest;    // 3 per triangle: h_dest[9], f_dest[3]
     // rows
     const int *col;       // [slot][stride] column (vertex) ids
-    const uint32_t *lidx; // [slot][stride], lower slots: index of the transposed block in A0/A1
-    const int *colu;      // [slot - diag_slot][stride]: columns of the upper slots
+    const uint32_t *lref; // lower slots, tile-major (lo_idx): u << 24 | column, the
+                          // transposed block being upper plane u of that column's row
+    const int *colu;      // upper slots, tile-major (up_idx): columns
     const uint32_t *hsrc; // [slot][stride] first record << 5 | record count
     const float *kb;      // [slot][stride] bending scalar (+K_b)
     const int *rowinfo;   // len | diag_slot << 8
@@ -145,7 +147,7 @@ struct InstDesc
     float4 *drec;            // 4 per interior edge: dbeta/dx_a (xyz), factor (w)
     float *dfb;              // per interior edge: factor * beta / 2
     // assembled system
-    float4 *A0;          // [slot - diag_slot][stride]: diagonal and upper blocks
+    float4 *A0;          // diagonal and upper blocks, tile-major (up_idx)
     float2 *A1;
     float4 *Aw;          // skew part w of those blocks (block p = S p + w x p), or null
     // contacts with kinematic bodies (all null without bodies)
@@ -165,6 +167,32 @@ struct InstDesc
     double *part;        // 3 * ntile_rows reduction partials
     InstState *st;
 };
+
+// Tile-major planes.  The arrays of the stored (diagonal and upper) blocks
+// and of the lower-slot references are kept per 128-row tile: entry (row,
+// plane u) of an array with w planes is at ((row / 128) * w + u) * 128 +
+// row % 128.  A warp's 32 rows still read 32 consecutive entries of one
+// plane, and one tile's planes of an array are contiguous (a single bulk
+// copy).  A lower-slot reference packs the transposed block's plane and
+// column: u << 24 | c (meshes of up to 2^24 vertices).
+static_assert(kTile == 128, "tile-major plane indexing assumes 128-row tiles");
+constexpr uint32_t kLrefColMask = 0xFFFFFFu;
+constexpr int kMaxClothVertices = 1 << 24;
+__host__ __device__ __forceinline__ uint32_t up_idx(int u, int row, int width_up)
+{
+    return (uint32_t(row >> 7) * uint32_t(width_up) + uint32_t(u)) * uint32_t(kTile) +
+           uint32_t(row & (kTile - 1));
+}
+__host__ __device__ __forceinline__ uint32_t lo_idx(int s, int row, int width_lo)
+{
+    return (uint32_t(row >> 7) * uint32_t(width_lo) + uint32_t(s)) * uint32_t(kTile) +
+           uint32_t(row & (kTile - 1));
+}
+__host__ __device__ __forceinline__ int lref_col(uint32_t ref) { return int(ref & kLrefColMask); }
+__host__ __device__ __forceinline__ uint32_t lref_block(uint32_t ref, int width_up)
+{
+    return up_idx(int(ref >> 24), int(ref & kLrefColMask), width_up);
+}
 
 // A tile carries its instance's descriptor and state addresses, so the PCG
 // kernels reach both with one dependent load instead of walking the
@@ -242,7 +270,7 @@ struct BatchCtl
     int n_active;    // instances still iterating
     int n_tiles_rows;
     int n_tiles_tris;
-    int pad;
+    int err;         // a bounded wait of the graph-loop kernels gave up (sticky until read)
 };
 
 } // namespace cloth

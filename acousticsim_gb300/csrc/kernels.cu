@@ -678,7 +678,7 @@ __global__ void __launch_bounds__(kTile) k_row(InstDesc *const *descs,
                 {
                     // stored: diagonal and upper blocks (the lower ones are
                     // the same values, held by the transposed position)
-                    const size_t ou = size_t(s - ds) * d.stride + row;
+                    const size_t ou = up_idx(s - ds, row, d.width_up);
                     d.A0[ou] = make_float4(A[0], A[1], A[2], A[3]);
                     d.A1[ou] = make_float2(A[4], A[5]);
                     if (d.Aw)
@@ -876,10 +876,10 @@ template <class T> __device__ __forceinline__ T *ldg_ptr(T *const *addr)
 // the kernel; the scalars are the ones the previous kernel left).
 struct SpmvHdr
 {
-    int inst, nv, stride, nt, active, wl;
+    int inst, nv, wu, nt, active, wl;
     float beta;
-    const int *rowinfo, *col, *colu;
-    const uint32_t *lidx;
+    const int *rowinfo, *colu;
+    const uint32_t *lref;
     const float4 *A0;
     const float2 *A1;
     const float4 *Aw; // skew parts (dihedral bending), or null
@@ -899,12 +899,11 @@ __device__ __forceinline__ void load_hdr(SpmvHdr &h, const Tile &tl)
     const int it = st->iter;
     h.beta = float(st->beta);
     h.nv = __ldg(&dp->nv);
-    h.stride = __ldg(&dp->stride);
+    h.wu = __ldg(&dp->width_up);
     h.wl = __ldg(&dp->width_lo);
     h.nt = __ldg(&dp->ntile_rows);
     h.rowinfo = ldg_ptr(&dp->rowinfo);
-    h.col = ldg_ptr(&dp->col);
-    h.lidx = ldg_ptr(&dp->lidx);
+    h.lref = ldg_ptr(&dp->lref);
     h.colu = ldg_ptr(&dp->colu);
     h.A0 = ldg_ptr(reinterpret_cast<float4 *const *>(&dp->A0));
     h.A1 = ldg_ptr(reinterpret_cast<float2 *const *>(&dp->A1));
@@ -975,9 +974,18 @@ __device__ __forceinline__ void spmv_rows(const SpmvHdr &d, int row0, float (&pq
                 on[r][k] = ok[r] && (lower ? kk < ds[r] : kk < kend[r]);
                 if (on[r][k])
                 {
-                    const size_t o = size_t(lower ? kk : kk - wl) * d.stride + row;
-                    cc[r][k] = lower ? d.col[o] : d.colu[o];
-                    const size_t oa = lower ? size_t(d.lidx[o]) : o;
+                    uint32_t oa;
+                    if (lower)
+                    {
+                        const uint32_t ref = d.lref[lo_idx(kk, row, wl)];
+                        cc[r][k] = lref_col(ref);
+                        oa = lref_block(ref, d.wu);
+                    }
+                    else
+                    {
+                        oa = up_idx(kk - wl, row, d.wu);
+                        cc[r][k] = d.colu[oa];
+                    }
                     a0[r][k] = d.A0[oa];
                     a1[r][k] = d.A1[oa];
                     if (SKEW && d.Aw)
@@ -1190,8 +1198,9 @@ struct BulkHdr
     int h0, nh;             // halo rows [h0, h0 + nh) staged (nh = 0: not staged)
     int skew;               // the stage holds skew block parts
     int tile_idx, nt;       // partial-sum slot
+    int wu;                 // upper planes (transposed-block indexing)
     float beta;
-    unsigned o_cl, o_li, o_cu, o_a0, o_a1, o_aw, o_z, o_p; // byte offsets in the stage
+    unsigned o_lr, o_cu, o_a0, o_a1, o_aw, o_z, o_p; // byte offsets in the stage
     const float4 *A0;       // transposed-block gathers
     const float2 *A1;
     const float4 *Aw;
@@ -1264,11 +1273,11 @@ __device__ __forceinline__ unsigned long long global_ns()
 // instance state) for 32 tiles at once, ahead of their copies.
 struct BulkMeta
 {
-    int go, start, nv, S, wl, wu, nt, it;
+    int go, start, nv, wl, wu, nt, it;
     int hx, hy;
     float beta;
-    const int *rowinfo, *col, *colu;
-    const uint32_t *lidx;
+    const int *rowinfo, *colu;
+    const uint32_t *lref;
     const float4 *A0, *Aw, *z;
     const float2 *A1;
     float4 *p0, *p1, *q;
@@ -1286,14 +1295,12 @@ __device__ __forceinline__ void bulk_meta(const Tile *tiles, int ti, BulkMeta &m
     m.it = __ldcg(&tl.st->iter);
     m.beta = float(__ldcg(&tl.st->beta));
     m.nv = __ldg(&dp->nv);
-    m.S = __ldg(&dp->stride);
     m.wl = __ldg(&dp->width_lo);
     m.wu = __ldg(&dp->width_up);
     m.nt = __ldg(&dp->ntile_rows);
     m.rowinfo = ldg_ptr(&dp->rowinfo);
-    m.col = ldg_ptr(&dp->col);
     m.colu = ldg_ptr(&dp->colu);
-    m.lidx = ldg_ptr(&dp->lidx);
+    m.lref = ldg_ptr(&dp->lref);
     m.A0 = ldg_ptr(reinterpret_cast<float4 *const *>(&dp->A0));
     m.A1 = ldg_ptr(reinterpret_cast<float2 *const *>(&dp->A1));
     m.Aw = ldg_ptr(reinterpret_cast<float4 *const *>(&dp->Aw));
@@ -1335,7 +1342,7 @@ __device__ __forceinline__ void bulk_issue_warp(const BulkMeta &m, int src, Bulk
         return;
     }
     const int start = __shfl_sync(FULLM, m.start, src), nv = __shfl_sync(FULLM, m.nv, src);
-    const int S = __shfl_sync(FULLM, m.S, src), wl = __shfl_sync(FULLM, m.wl, src);
+    const int wl = __shfl_sync(FULLM, m.wl, src);
     const int wu = __shfl_sync(FULLM, m.wu, src), it = __shfl_sync(FULLM, m.it, src);
     const int hx = __shfl_sync(FULLM, m.hx, src), hy = __shfl_sync(FULLM, m.hy, src);
     const float beta = __shfl_sync(FULLM, m.beta, src);
@@ -1344,11 +1351,9 @@ __device__ __forceinline__ void bulk_issue_warp(const BulkMeta &m, int src, Bulk
     float4 *p0 = shfl_ptr(m.p0, src), *p1 = shfl_ptr(m.p1, src);
     const float4 *pold = (it & 1) ? p1 : p0;
     const int nrows = min(kTile, nv - start);
-    const int prow = min(kTile, S - start); // plane rows copied: a multiple of 32
     const bool skew = SKEW && Aw != nullptr;
-    const unsigned o_cl = kTile * 4;
-    const unsigned o_li = o_cl + unsigned(wl) * kTile * 4;
-    const unsigned o_cu = o_li + unsigned(wl) * kTile * 4;
+    const unsigned o_lr = kTile * 4;
+    const unsigned o_cu = o_lr + unsigned(wl) * kTile * 4;
     const unsigned o_a0 = o_cu + unsigned(wu) * kTile * 4;
     const unsigned o_a1 = o_a0 + unsigned(wu) * kTile * 16;
     const unsigned o_aw = o_a1 + unsigned(wu) * kTile * 8;
@@ -1363,8 +1368,7 @@ __device__ __forceinline__ void bulk_issue_warp(const BulkMeta &m, int src, Bulk
     }
     const unsigned o_p = o_z + unsigned(nh) * 16u;
     const unsigned ri_bytes = unsigned((nrows + 3) & ~3) * 4u;
-    const unsigned pb = unsigned(prow) * 4u;
-    const int kinds = skew ? 4 : 3; // colu, A0, A1 (, Aw) planes per upper slot
+    const unsigned pb = kTile * 4u; // one plane of 4-byte entries (tile-major, whole tiles)
     if (lane == 0)
     {
         // the whole header before the arrival: its release publishes the
@@ -1377,9 +1381,9 @@ __device__ __forceinline__ void bulk_issue_warp(const BulkMeta &m, int src, Bulk
         h.skew = skew ? 1 : 0;
         h.tile_idx = start / kTile;
         h.nt = m.nt;
+        h.wu = wu;
         h.beta = beta;
-        h.o_cl = o_cl;
-        h.o_li = o_li;
+        h.o_lr = o_lr;
         h.o_cu = o_cu;
         h.o_a0 = o_a0;
         h.o_a1 = o_a1;
@@ -1412,41 +1416,47 @@ __device__ __forceinline__ void bulk_issue_warp(const BulkMeta &m, int src, Bulk
             h.st = st;
         }
     }
-    const unsigned tx = ri_bytes + unsigned(wl) * 2u * pb +
+    const unsigned tx = ri_bytes + unsigned(wl) * pb +
                         unsigned(wu) * (pb + 4u * pb + 2u * pb + (skew ? 4u * pb : 0u)) + halo;
     if (lane == 0)
         mbar_arrive_expect_tx(bar, tx);
     __syncwarp();
-    const int *rowinfo = shfl_ptr(m.rowinfo, src), *col = shfl_ptr(m.col, src),
-              *colu = shfl_ptr(m.colu, src);
-    const uint32_t *lidx = shfl_ptr(m.lidx, src);
-    const int ncopy = 1 + 2 * wl + kinds * wu + (nh ? (two ? 2 : 1) : 0);
+    const int *rowinfo = shfl_ptr(m.rowinfo, src), *colu = shfl_ptr(m.colu, src);
+    const uint32_t *lref = shfl_ptr(m.lref, src);
+    // one copy per array: a tile's planes are contiguous (tile-major)
+    const size_t tl = size_t(start / kTile);
+    const int ncopy = 5 + (skew ? 1 : 0) + (nh ? (two ? 2 : 1) : 0);
     for (int c = lane; c < ncopy; c += 32)
     {
-        if (c == 0)
-            bulk_g2s(stage, rowinfo + start, ri_bytes, bar);
-        else if (c <= wl)
-            bulk_g2s(stage + o_cl + (c - 1) * kTile * 4, col + size_t(c - 1) * S + start, pb, bar);
-        else if (c <= 2 * wl)
-            bulk_g2s(stage + o_li + (c - 1 - wl) * kTile * 4,
-                     lidx + size_t(c - 1 - wl) * S + start, pb, bar);
-        else if (c < 1 + 2 * wl + kinds * wu)
+        const int k = (c >= 5 && !skew) ? c + 1 : c; // 5: Aw, 6: z, 7: p_old
+        switch (k)
         {
-            const int k = c - 1 - 2 * wl, kind = k / wu, u = k - kind * wu;
-            const size_t g = size_t(u) * S + start;
-            if (kind == 0)
-                bulk_g2s(stage + o_cu + u * kTile * 4, colu + g, pb, bar);
-            else if (kind == 1)
-                bulk_g2s(stage + o_a0 + u * kTile * 16, A0 + g, 4u * pb, bar);
-            else if (kind == 2)
-                bulk_g2s(stage + o_a1 + u * kTile * 8, A1 + g, 2u * pb, bar);
-            else
-                bulk_g2s(stage + o_aw + u * kTile * 16, Aw + g, 4u * pb, bar);
-        }
-        else if (c == 1 + 2 * wl + kinds * wu)
+        case 0:
+            bulk_g2s(stage, rowinfo + start, ri_bytes, bar);
+            break;
+        case 1:
+            if (wl)
+                bulk_g2s(stage + o_lr, lref + tl * wl * kTile, unsigned(wl) * pb, bar);
+            break;
+        case 2:
+            bulk_g2s(stage + o_cu, colu + tl * wu * kTile, unsigned(wu) * pb, bar);
+            break;
+        case 3:
+            bulk_g2s(stage + o_a0, A0 + tl * wu * kTile, unsigned(wu) * 4u * pb, bar);
+            break;
+        case 4:
+            bulk_g2s(stage + o_a1, A1 + tl * wu * kTile, unsigned(wu) * 2u * pb, bar);
+            break;
+        case 5:
+            bulk_g2s(stage + o_aw, Aw + tl * wu * kTile, unsigned(wu) * 4u * pb, bar);
+            break;
+        case 6:
             bulk_g2s(stage + o_z, z + hx, unsigned(nh) * 16u, bar);
-        else
+            break;
+        default:
             bulk_g2s(stage + o_p, pold + hx, unsigned(nh) * 16u, bar);
+            break;
+        }
     }
 }
 
@@ -1459,7 +1469,8 @@ struct BulkRegs
     float beta;
     bool skew;
     const unsigned char *stage;
-    unsigned o_cl, o_li, o_cu, o_a0, o_a1, o_aw, o_z;
+    int wu;
+    unsigned o_lr, o_cu, o_a0, o_a1, o_aw, o_z;
     const float4 *A0;
     const float2 *A1;
     const float4 *Aw;
@@ -1475,8 +1486,8 @@ __device__ __forceinline__ BulkRegs bulk_regs(const BulkHdr &h, const unsigned c
     r.beta = h.beta;
     r.skew = h.skew != 0;
     r.stage = stage;
-    r.o_cl = h.o_cl;
-    r.o_li = h.o_li;
+    r.wu = h.wu;
+    r.o_lr = h.o_lr;
     r.o_cu = h.o_cu;
     r.o_a0 = h.o_a0;
     r.o_a1 = h.o_a1;
@@ -1514,8 +1525,7 @@ __device__ __forceinline__ float bulk_row(const BulkRegs &r, int t)
         return pc;
     };
     const float3 pv = pcol(row);
-    const int *__restrict__ cl = reinterpret_cast<const int *>(stage + r.o_cl) + t;
-    const uint32_t *__restrict__ li = reinterpret_cast<const uint32_t *>(stage + r.o_li) + t;
+    const uint32_t *__restrict__ lr = reinterpret_cast<const uint32_t *>(stage + r.o_lr) + t;
     const bool sk = SKEW && r.skew;
     float3 q = make_float3(0.f, 0.f, 0.f);
     // lower slots, column order: blocks at the transposed position (L2)
@@ -1528,12 +1538,13 @@ __device__ __forceinline__ float bulk_row(const BulkRegs &r, int t)
         for (int k = 0; k < CH; k++)
             if (s0 + k < ds)
             {
-                const uint32_t o = li[(s0 + k) * kTile];
+                const uint32_t ref = lr[(s0 + k) * kTile];
+                const uint32_t o = lref_block(ref, r.wu);
                 a0[k] = __ldcg(r.A0 + o);
                 a1[k] = __ldcg(r.A1 + o);
                 if (sk)
                     aw[k] = __ldcg(r.Aw + o);
-                pc[k] = pcol(cl[(s0 + k) * kTile]);
+                pc[k] = pcol(lref_col(ref));
             }
 #pragma unroll
         for (int k = 0; k < CH; k++)
@@ -1631,48 +1642,61 @@ __global__ void __launch_bounds__(kBulkThreads) k_spmv_bulk(InstDesc *const *des
     if (tid >= kTile)
     {
         // ---- producer warp: lane k resolves tile j + k's metadata for 32
-        // tiles at a time; the lanes share each tile's copies
+        // tiles at a time; tiles of instances that are done are skipped
+        // without a stage; the lanes share each tile's copies; after the last
+        // tile a header with go = -1 tells the consumers to stop
         const int lane = tid - kTile;
         BulkMeta m;
+        int used = 0; // stages filled so far
+        auto acquire = [&](int stg) -> bool {
+            if (used < NST)
+                return true;
+            const bool ok = mbar_wait_bounded(&empty[stg], ((used / NST) - 1) & 1);
+            return __all_sync(0xffffffffu, ok);
+        };
         for (int j = 0; j < nmine; j++)
         {
-            const int stg = j % NST;
             if ((j & 31) == 0)
             {
                 m.go = 0;
                 if (j + lane < nmine)
                     bulk_meta(tiles, blockIdx.x + (j + lane) * G, m);
             }
-            if (j >= NST)
-            {
-                const bool ok = mbar_wait_bounded(&empty[stg], ((j / NST) - 1) & 1);
-                if (!__all_sync(0xffffffffu, ok))
-                    return; // consumers stuck: they give up on their own bounded waits
-            }
+            if (!__shfl_sync(0xffffffffu, m.go, j & 31))
+                continue;
+            const int stg = used % NST;
+            if (!acquire(stg))
+                return; // consumers stuck: they give up on their own bounded waits
             bulk_issue_warp<SKEW, HALO>(m, j & 31, hdr[stg], bulk_smem + stg * stage_bytes,
                                         stage_bytes, &full[stg], lane);
+            used++;
+        }
+        const int stg = used % NST;
+        if (acquire(stg) && lane == 0)
+        {
+            hdr[stg].go = -1;
+            mbar_arrive(&full[stg]);
         }
         return;
     }
-    // ---- consumers: one row per thread
+    // ---- consumers: one row per thread, one stage after the other until
+    // the producer's end marker
     const int lane = tid & 31, warp = tid >> 5;
-    for (int j = 0; j < nmine; j++)
+    for (int j = 0;; j++)
     {
         const int stg = j % NST;
         unsigned char *stage = bulk_smem + stg * stage_bytes;
         const bool got = mbar_wait_bounded(&full[stg], (j / NST) & 1);
         if (!consumer_all(got))
         {
-            // the stage never completed: flag the instance's team and end its
-            // solve through its sums (a NaN partial), then stop
-            const BulkHdr &hd = hdr[stg];
-            if (tid == 0 && hd.go)
-            {
-                atomicExch(&hd.st->bar_err, 1);
-                hd.part[hd.tile_idx] = __longlong_as_double(0x7ff8000000000000ll);
-            }
+            // the stage never completed: record it for the launch set (the
+            // host reports the solve as timed out) and stop
+            if (tid == 0)
+                atomicExch(&ctl->err, 1);
             return;
         }
+        if (hdr[stg].go < 0)
+            break;
         const BulkHdr &hd = hdr[stg];
         if (hd.go)
         {
@@ -2416,13 +2440,20 @@ __device__ __forceinline__ void pcg_persistent_body(InstDesc *const *descs,
                         on[k] = lower ? kk < ds : kk < kend;
                         if (on[k])
                         {
-                            const uint32_t o = uint32_t(lower ? kk : kk - wl) * uint32_t(d.stride) +
-                                               uint32_t(row);
-                            cc[k] = ld_keep(lower ? d.col + o : d.colu + o, keep);
-                            const uint32_t oa =
-                                lower ? uint32_t(ld_keep(reinterpret_cast<const int *>(d.lidx) + o,
-                                                         keep))
-                                      : o;
+                            uint32_t oa;
+                            if (lower)
+                            {
+                                const uint32_t ref = uint32_t(ld_keep(
+                                    reinterpret_cast<const int *>(d.lref) + lo_idx(kk, row, wl),
+                                    keep));
+                                cc[k] = lref_col(ref);
+                                oa = lref_block(ref, d.width_up);
+                            }
+                            else
+                            {
+                                oa = up_idx(kk - wl, row, d.width_up);
+                                cc[k] = ld_keep(d.colu + oa, keep);
+                            }
                             a0[k] = ld_keep(d.A0 + oa, keep);
                             a1[k] = ld_keep(d.A1 + oa, keep);
                             if (SKEW && d.Aw)
@@ -2782,12 +2813,19 @@ __global__ void __launch_bounds__(kPBlock, 1)
                 on[k] = lower ? kk < ds : kk < kend;
                 if (on[k])
                 {
-                    const uint32_t o =
-                        uint32_t(lower ? kk : kk - wl) * uint32_t(d.stride) + uint32_t(row);
-                    cc[k] = ld_keep(lower ? d.col + o : d.colu + o, keep);
-                    const uint32_t oa =
-                        lower ? uint32_t(ld_keep(reinterpret_cast<const int *>(d.lidx) + o, keep))
-                              : o;
+                    uint32_t oa;
+                    if (lower)
+                    {
+                        const uint32_t ref = uint32_t(ld_keep(
+                            reinterpret_cast<const int *>(d.lref) + lo_idx(kk, row, wl), keep));
+                        cc[k] = lref_col(ref);
+                        oa = lref_block(ref, d.width_up);
+                    }
+                    else
+                    {
+                        oa = up_idx(kk - wl, row, d.width_up);
+                        cc[k] = ld_keep(d.colu + oa, keep);
+                    }
                     a0[k] = ld_keep(d.A0 + oa, keep);
                     a1[k] = ld_keep(d.A1 + oa, keep);
                 }

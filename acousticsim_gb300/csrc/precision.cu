@@ -135,18 +135,17 @@ __device__ bool grid_reduce(double (&v)[N], double *part, int nblk, unsigned *ti
 // slot loop does not reload them).
 struct Mat64
 {
-    int nv, stride;
+    int nv, wl, wu;
     const int *__restrict__ rowinfo;
-    const int *__restrict__ col;
     const int *__restrict__ colu;
-    const uint32_t *__restrict__ lidx;
+    const uint32_t *__restrict__ lref;
     const float4 *__restrict__ A0;
     const float2 *__restrict__ A1;
     const float4 *__restrict__ Aw;
     const float4 *__restrict__ dx;
     __device__ explicit Mat64(const InstDesc &d)
-        : nv(d.nv), stride(d.stride), rowinfo(d.rowinfo), col(d.col), colu(d.colu),
-          lidx(d.lidx), A0(d.A0), A1(d.A1), Aw(d.Aw), dx(d.dx)
+        : nv(d.nv), wl(d.width_lo), wu(d.width_up), rowinfo(d.rowinfo), colu(d.colu),
+          lref(d.lref), A0(d.A0), A1(d.A1), Aw(d.Aw), dx(d.dx)
     {
     }
 };
@@ -163,9 +162,19 @@ __device__ __forceinline__ void row_mul64(const Mat64 &d, int row,
     for (int s = 0; s < len; s++)
     {
         const bool lower = s < ds;
-        const size_t o = lower ? size_t(s) * d.stride + row : size_t(s - ds) * d.stride + row;
-        const int c = lower ? d.col[o] : d.colu[o];
-        const size_t oa = lower ? size_t(d.lidx[o]) : o;
+        int c;
+        uint32_t oa;
+        if (lower)
+        {
+            const uint32_t ref = d.lref[lo_idx(s, row, d.wl)];
+            c = lref_col(ref);
+            oa = lref_block(ref, d.wu);
+        }
+        else
+        {
+            oa = up_idx(s - ds, row, d.wu);
+            c = d.colu[oa];
+        }
         const float4 u = d.A0[oa];
         const float2 uw = d.A1[oa];
         const double a[6] = {u.x, u.y, u.z, u.w, uw.x, uw.y};
@@ -293,8 +302,8 @@ __global__ void __launch_bounds__(kB64) k64_init(const InstDesc *dp, F64Ptr f)
          row += gridDim.x * blockDim.x)
     {
         // plane 0 holds the diagonal block
-        const float4 u = d.A0[row];
-        const float2 uw = d.A1[row];
+        const float4 u = d.A0[up_idx(0, row, d.width_up)];
+        const float2 uw = d.A1[up_idx(0, row, d.width_up)];
         const double a[6] = {u.x, u.y, u.z, u.w, uw.x, uw.y};
         const double c00 = a[3] * a[5] - a[4] * a[4], c01 = a[2] * a[4] - a[1] * a[5],
                      c02 = a[1] * a[4] - a[2] * a[3], c11 = a[0] * a[5] - a[2] * a[2],

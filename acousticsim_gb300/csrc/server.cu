@@ -326,25 +326,24 @@ int build_chunk_graph(cloth_server_s *s)
         skew = skew || sc.c->h.Aw != nullptr || sc.c->mat.bending_model == 1;
     const GraphLoopVariant *table = skew ? kSpmvSkewVariants : kSpmvVariants;
     int sv_i = ctx->tune_spmv;
-    int occ_sv = (skew ? ctx->occ_spmv_skew : ctx->occ_spmv)[sv_i];
-    unsigned smem_sv = 0;
     if (table[sv_i].bulk_stages)
     {
-        // stages sized for every registered cloth; the default variant when
-        // they do not fit in shared memory
-        std::vector<cloth_s *> cl;
-        for (const SrvCloth &sc : s->cl)
-            cl.push_back(sc.c);
-        const unsigned stage = bulk_stage_bytes(cl, skew, table[sv_i].bulk_halo != 0);
-        occ_sv = bulk_occupancy(table[sv_i], stage, ctx->max_smem_optin);
-        if (occ_sv > 0)
-            smem_sv = bulk_smem(table[sv_i], stage);
-        else
-        {
-            sv_i = kDefaultSpmvVariant;
-            occ_sv = (skew ? ctx->occ_spmv_skew : ctx->occ_spmv)[sv_i];
-        }
+        // The bulk-staged SpMV stages p over every tile's column range; the
+        // served cloths (up to 256 vertices a side) make that range five
+        // tiles wide, and the served chunks were measured slower with it.
+        // Take the fastest register variant of the context's last tuning.
+        sv_i = kDefaultSpmvVariant;
+        float best = 1e30f;
+        for (int v = 0; v < kNumSpmvVariants && v < int(ctx->tune_ms_spmv.size()); v++)
+            if (!table[v].bulk_stages && ctx->tune_ms_spmv[v] > 0.f &&
+                ctx->tune_ms_spmv[v] < best)
+            {
+                best = ctx->tune_ms_spmv[v];
+                sv_i = v;
+            }
     }
+    const int occ_sv = (skew ? ctx->occ_spmv_skew : ctx->occ_spmv)[sv_i];
+    const unsigned smem_sv = 0;
     const GraphLoopVariant &sv = table[sv_i];
     const GraphLoopVariant &uv = kUpdateVariants[ctx->tune_update];
     const int one_wave_spmv = ctx->num_sms * std::max(1, occ_sv);
