@@ -27,7 +27,8 @@ SOLVER_GRAPH_LOOP = 1
 SOLVER_FP64 = 2
 SOLVER_PERSISTENT_1B = 3
 SOLVER_PERSISTENT_2B = 4
-SOLVER_NAMES = {0: "persistent", 1: "graph_loop", 2: "fp64", 3: "persistent_1b", -1: "plain"}
+SOLVER_NAMES = {0: "persistent", 1: "graph_loop", 2: "fp64", 3: "persistent_1b",
+                4: "persistent_2b", 5: "escalated_fp64", -1: "plain"}
 
 
 class GridDesc(C.Structure):
@@ -135,6 +136,7 @@ SIGNATURES = {
     "cloth_ctx_reset_profile": (C.c_int, [P]),
     "cloth_ctx_set_solver": (C.c_int, [P, C.c_int]),
     "cloth_ctx_set_spin_limit": (C.c_int, [P, C.c_uint, C.c_uint]),
+    "cloth_ctx_set_escalation": (C.c_int, [P, C.c_int]),
     "cloth_ctx_device_bytes": (C.c_int, [P, C.POINTER(C.c_size_t)]),
     "cloth_ctx_set_kernel_variant": (C.c_int, [P, C.c_int, C.c_int, C.c_int, C.c_int,
                                                C.c_int, C.c_int]),

@@ -81,6 +81,12 @@ class ClothContext:
         timeout path); 0 in normal use."""
         N.call("cloth_ctx_set_spin_limit", self._h, int(polls), int(extra_arrivals))
 
+    def set_escalation(self, on: bool = True) -> None:
+        """Steps whose FP32 PCG ends in NaN or breakdown are re-solved by the
+        FP64 PCG and advanced; stats report the solver "escalated_fp64".  On by
+        default; a step called without stats (step_async) is not escalated."""
+        N.call("cloth_ctx_set_escalation", self._h, int(bool(on)))
+
     # (rows per thread, slot unroll, tiles per block); slot unroll 0: the
     # bulk-staged SpMV, whose third number is its ring of stages and whose
     # first is 1 when it also stages p over each tile's column range
@@ -372,13 +378,16 @@ class BaraffClothGpu:
                None)
 
     def step_host(self, x_in, xpre_in, x_out, dt: float = 0.0,
-                  params: N.SolveParams | None = None) -> None:
-        """Step with host buffers (upload x, x_pre; download x), as UpdatePos exchanges them."""
+                  params: N.SolveParams | None = None) -> dict:
+        """Step with host buffers (upload x, x_pre; download x), as UpdatePos
+        exchanges them; returns the step's stats."""
+        st = N.SolveStats()
         N.call("cloth_step_host", self._h, float(dt),
                C.byref(params) if params is not None else None,
                N.ptr(x_in, C.c_double) if x_in is not None else None,
                N.ptr(xpre_in, C.c_double) if xpre_in is not None else None,
-               N.ptr(x_out, C.c_double) if x_out is not None else None, None)
+               N.ptr(x_out, C.c_double) if x_out is not None else None, C.byref(st))
+        return st.as_dict()
 
     # ---------------------------------------------------------------- seam
     def assemble(self, dt: float = 0.0) -> None:

@@ -1466,7 +1466,10 @@ int run_step(Batch *b, double dt, const cloth_solve_params *params,
 {
     cloth_ctx *ctx = b->ctx;
     for (auto *c : b->members)
+    {
         c->plain_host_valid = false;
+        c->escalated_valid = false;
+    }
     int rc = prepare(b->members, dt, params);
     if (rc != CLOTH_OK)
         return rc;
@@ -1521,8 +1524,34 @@ int run_step(Batch *b, double dt, const cloth_solve_params *params,
     }
     if (rc != CLOTH_OK)
         return rc;
+    if (!stats)
+    {
+        // asynchronous step: no escalation (a failed solve leaves the state)
+        end_step(b->members);
+        return CLOTH_OK;
+    }
+    rc = read_stats(b, stats);
+    // precision escalation: a member whose FP32 PCG ended in NaN or breakdown
+    // kept its pre-step state and assembled system (the advance skipped it);
+    // re-solve it in FP64 and advance
+    if (rc == CLOTH_OK && ctx->escalate && !b->collide)
+    {
+        const cloth_solve_params p = params ? *params : default_params();
+        for (size_t i = 0; i < b->members.size() && rc == CLOTH_OK; i++)
+            if (stats[i].status == CLOTH_ERR_NAN || stats[i].status == CLOTH_ERR_BREAKDOWN)
+            {
+                cloth_s *c = b->members[i];
+                c->assembled = true; // this step's system is still in its work arrays
+                rc = escalate_step(c, &p, &stats[i]);
+                if (rc == CLOTH_OK)
+                {
+                    c->escalated = stats[i];
+                    c->escalated_valid = true;
+                }
+            }
+    }
     end_step(b->members);
-    return read_stats(b, stats);
+    return rc;
 }
 
 Batch *self_batch(cloth_s *c, int *rc)
@@ -1752,6 +1781,15 @@ int cloth_ctx_set_solver(cloth_ctx *ctx, int solver)
     ctx->last_batch.reset();
     for (auto *c : ctx->cloths)
         c->self.reset();
+    return CLOTH_OK;
+}
+
+int cloth_ctx_set_escalation(cloth_ctx *ctx, int enable)
+{
+    if (!ctx)
+        return fail(CLOTH_ERR_INVALID, "cloth_ctx_set_escalation: NULL context");
+    std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+    ctx->escalate = enable != 0;
     return CLOTH_OK;
 }
 
@@ -2357,6 +2395,11 @@ int cloth_get_stats(cloth_t *c, cloth_solve_stats *stats)
     CK(cudaStreamSynchronize(c->ctx->stream));
     InstState st;
     CK(cudaMemcpy(&st, c->d_state, sizeof(st), cudaMemcpyDeviceToHost));
+    if (c->escalated_valid)
+    {
+        *stats = c->escalated; // the last step was re-solved in FP64
+        return CLOTH_OK;
+    }
     stats->iters = st.iter;
     stats->status = st.bar_err ? CLOTH_ERR_TIMEOUT : st.status;
     stats->res_norm = std::sqrt(std::max(0.0, st.rr));

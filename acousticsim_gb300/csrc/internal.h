@@ -143,6 +143,7 @@ struct cloth_ctx_s
     // extra arrivals are the timeout test's hook, 0 otherwise)
     cloth::SpinCfg spin = {cloth::kSpinLimitDefault, 0u};
     int solver = 0; // 0: persistent cooperative PCG when the set fits, 1: graph loop
+    bool escalate = true; // FP32 PCG ending in NaN / breakdown: re-solve the step in FP64
     bool prof = false;
     double prof_ms[CLOTH_NUM_PHASES] = {};
     long long prof_n[CLOTH_NUM_PHASES] = {};
@@ -178,6 +179,8 @@ struct cloth_s
     cloth_f64_s *f64 = nullptr; // FP64 work arrays (refinement, FP64 PCG), on first use
     bool dx64_valid = false;    // the last solve left an FP64 dx (refined or FP64 PCG)
     bool pcg_stale = false;     // the FP32 PCG start of the assembly was overwritten
+    bool escalated_valid = false; // the last step was re-solved in FP64 (its stats)
+    cloth_solve_stats escalated = {};
     cloth::InstDesc h;        // host copy of the descriptor
     cloth::InstDesc *d_desc = nullptr;
     cloth::InstState *d_state = nullptr;
@@ -227,6 +230,9 @@ int inner_solve(cloth_s *c, const double *rhs64, const cloth_solve_params *p,
 void f64_free(cloth_s *c);
 int f64_advance(cloth_s *c);
 int f64_get_dx(cloth_s *c, double *dx, int nv);
+// Re-solve an assembled step whose FP32 PCG ended in NaN or breakdown with
+// the FP64 flexible CG, then advance in FP64; fills the step's stats.
+int escalate_step(cloth_s *c, const cloth_solve_params *p, cloth_solve_stats *out);
 // A server's view of one of its cloths: true while requests are queued or running.
 bool server_busy(const cloth_server_s *s, const cloth_s *c);
 // Detach every cloth of a server and free it (context teardown).

@@ -3055,6 +3055,11 @@ __global__ void __launch_bounds__(kTile) k_advance(InstDesc *const *descs,
         // open (the request server's tile list holds running ones too)
         if (finished_only && (d.st->active || !d.st->open))
             continue;
+        // a solve that ended in NaN, breakdown or a timed-out wait leaves the
+        // state as it was (the step driver may re-solve it in FP64)
+        const int status = d.st->status;
+        if (status == 6 || status == 7 || status == 9)
+            continue;
         const int row = tl.start + threadIdx.x;
         if (row >= d.nv)
             continue;

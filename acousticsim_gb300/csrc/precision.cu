@@ -738,6 +738,50 @@ int cloth::detail::f64_advance(cloth_s *c)
     return CLOTH_OK;
 }
 
+// FP32 copy of the FP64 solution (the next step's warm start)
+__global__ void k64_dx32(const InstDesc *dp, const double *dx64)
+{
+    const InstDesc &d = *dp;
+    for (int row = blockIdx.x * blockDim.x + threadIdx.x; row < d.nv;
+         row += gridDim.x * blockDim.x)
+        d.dx[row] = make_float4(float(dx64[3 * row]), float(dx64[3 * row + 1]),
+                                float(dx64[3 * row + 2]), 0.f);
+}
+
+int cloth::detail::escalate_step(cloth_s *c, const cloth_solve_params *p,
+                                 cloth_solve_stats *out)
+{
+    // the FP32 PCG ended in NaN or breakdown on the assembled system (the
+    // advance left the state alone): the system is beyond FP32 there, so the
+    // step is re-solved by the all-FP64 block-Jacobi PCG from zero to the
+    // step's tolerance, then x += dx in FP64
+    cloth_solve_params q = *p;
+    q.warm_start = 0;
+    if (!(q.rel_tol > 0) && !(q.abs_tol > 0))
+        q.rel_tol = 1e-6;
+    q.max_iters = std::max(q.max_iters, 100000);
+    const double rhs = out->rhs_norm;
+    int rc = cloth_solve_fp64(c, &q, out);
+    if (rc != CLOTH_OK)
+        return rc;
+    out->solver = CLOTH_SOLVER_ESCALATED;
+    if (!(out->rhs_norm > 0))
+        out->rhs_norm = rhs;
+    if (out->status != CLOTH_OK)
+        return CLOTH_OK;
+    F64Work *w = nullptr;
+    rc = f64_work(c, &w);
+    if (rc != CLOTH_OK)
+        return rc;
+    rc = f64_advance(c);
+    if (rc != CLOTH_OK)
+        return rc;
+    const int grid = std::max(1, std::min(c->ctx->num_sms * 8, (c->tab.nv + 255) / 256));
+    k64_dx32<<<grid, 256, 0, c->ctx->stream>>>(c->d_desc, w->dx64);
+    PCK(cudaGetLastError());
+    return CLOTH_OK;
+}
+
 int cloth::detail::f64_get_dx(cloth_s *c, double *dx, int nv)
 {
     F64Work *w = nullptr;

@@ -452,6 +452,7 @@ def run_ours(args, rank, world, local, pg):
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
           for _ in range(args.steps)]
     iters = []
+    escalated = 0
     clocks = ClockSampler(local)
     clocks.start()
     barrier(pg)
@@ -461,10 +462,11 @@ def run_ours(args, rank, world, local, pg):
         with torch.cuda.stream(stream):
             flush.fill_(float(k))
         ev[k][0].record(stream)
-        cloth.step_async(0.0, p)
+        st = cloth.UpdatePos(0.0, p)  # with its stats: a failed FP32 solve is escalated
         ev[k][1].record(stream)
-        st = cloth.stats()
         iters.append(st["iters"])
+        if st["solver"] == "escalated_fp64":
+            escalated += 1
         if st["status"] != "OK":
             raise RuntimeError(f"step {k + 1}: {st}")
     torch.cuda.synchronize()
@@ -503,8 +505,10 @@ def run_ours(args, rank, world, local, pg):
             flush.fill_(float(k))
         torch.cuda.synchronize()
         e0 = time.perf_counter()
-        cloth.step_host(hx, hxp, hout, 0.0, p)
+        st_e = cloth.step_host(hx, hxp, hout, 0.0, p)
         e_sum += time.perf_counter() - e0
+        if st_e["status"] != "OK":
+            raise RuntimeError(f"e2e step {k + 1}: {st_e}")
         hxp[:] = hx
         hx[:] = hout
     e_t = max_over_ranks(pg, e_sum)
@@ -553,6 +557,7 @@ def run_ours(args, rank, world, local, pg):
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32 (FP64 PCG reductions)",
                 "data": DATA, "config": config_block(args, world),
                 "pcg_iters_per_step": iters,
+                "escalated_steps": escalated,
                 "ms_per_pcg_iteration": sum(step_ms) / max(1, it_sum),
                 "step_ms": [round(v, 3) for v in step_ms], "wall_s_timed_region": wall,
                 "contacts_last_step": contacts,
