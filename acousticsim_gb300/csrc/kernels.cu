@@ -1509,7 +1509,7 @@ __device__ __forceinline__ BulkRegs bulk_regs(const BulkHdr &h, const unsigned c
 template <bool SKEW, bool STAGED>
 __device__ __forceinline__ float bulk_row(const BulkRegs &r, int t)
 {
-    constexpr int CH = 4; // transposed-block gathers in flight together
+    constexpr int CH = 4; // transposed-block gathers in flight together (8: 235 registers, one block per SM, slower)
     const unsigned char *__restrict__ stage = r.stage;
     const int row = r.start + t;
     const int info = reinterpret_cast<const int *>(stage)[t];

@@ -226,18 +226,19 @@ def ncu_dram_per_iteration(kernel: str) -> float | None:
 
 def algorithmic_bytes(nv: int, nnzb: int, skew: bool = False) -> dict:
     """Unique bytes one PCG iteration must move. The matrix is stored as its
-    diagonal and upper blocks (FP32, 6 floats per symmetric block); a lower
-    slot holds its column and the index of the transposed block:
-      SpMV phase   : 24*nnzb_up (A) + 4*nnzb (cols) + 4*nnzb_lo (transposed index)
-                     + 4*nv (row info) + 16*nv (z) + 16*nv (p_old)
-                     + 16*nv (p write) + 16*nv (q write)
+    diagonal and upper blocks (FP32, 6 floats per symmetric block, with their
+    columns); a lower slot holds one 4-byte reference to its transposed block
+    (that block's plane and column):
+      SpMV phase   : 24*nnzb_up (A) + 4*nnzb_up (upper columns) + 4*nnzb_lo
+                     (lower references) + 4*nv (row info) + 16*nv (z)
+                     + 16*nv (p_old) + 16*nv (p write) + 16*nv (q write)
       update phase : 16*nv (q) + 16*nv (dx) + 16*nv (r) + 24*nv (M^-1 read)
                      + 48*nv (dx, r, z write)   [p comes from shared memory]
     with nnzb_up = (nnzb + nv) / 2 and nnzb_lo = (nnzb - nv) / 2.  With the
     dihedral bending model every stored block also has a skew part (16 bytes).
     """
     up, lo = (nnzb + nv) // 2, (nnzb - nv) // 2
-    matrix = (40 if skew else 24) * up + 4 * nnzb + 4 * lo
+    matrix = (40 if skew else 24) * up + 4 * up + 4 * lo
     spmv = matrix + 68 * nv
     update = 120 * nv
     return {"spmv_dot": spmv, "update_dot": update, "iteration": spmv + update,
@@ -670,17 +671,26 @@ def graph_loop_roofline(prof: dict, bytes_spmv: float, bytes_upd: float) -> dict
     algorithmic bytes they moved (per instance: iterations x bytes per
     iteration) over their summed CUDA-event times."""
     peak = measured_peaks()
+    tp = ROOT / "profiles" / "ncu_traffic.json"
+    traffic = json.loads(tp.read_text()) if tp.exists() else {}
     out = {}
-    for name, kname, nbytes in (("spmv_dot", "k_spmv_t", bytes_spmv),
+    for name, kname, nbytes in (("spmv_dot", "k_spmv (graph loop)", bytes_spmv),
                                 ("update_dot", "k_update_t", bytes_upd)):
         ms = prof[name]["ms"]
         if ms > 0:
             gbs = nbytes / (ms * 1e-3) / 1e9
+            # DRAM bytes per algorithmic byte of the committed ncu capture (all
+            # instances active) applied to this solve's algorithmic bytes
+            t = traffic.get("k_spmv_bulk" if name == "spmv_dot" else "k_update_t", {})
+            ratio = (t["dram_bytes_per_launch"] / t["algorithmic_bytes_per_launch"]
+                     if t.get("algorithmic_bytes_per_launch") else None)
             out[kname] = {"bound": "hbm", "achieved": gbs, "peak": peak["hbm_gbs"],
                           "unit": "GB/s", "frac": gbs / peak["hbm_gbs"],
                           "launches": prof[name]["launches"], "ms_total": ms,
                           "algorithmic_bytes": nbytes,
-                          "traffic_source": "profiles/graph_loop_kernels.md (ncu)"}
+                          "traffic": nbytes * ratio if ratio else None,
+                          "traffic_source": "profiles/ncu_traffic.json (ncu DRAM bytes per "
+                                            "algorithmic byte of one all-active launch)"}
     out["reduce_ms_total"] = prof["reduce"]["ms"]
     return out
 
