@@ -6,10 +6,11 @@ Python mirror of the reference's cloth API.
 """
 from . import _native
 from ._native import ClothError, REFERENCE_PARAMS, SolveParams, params
-from .cloth import BaraffClothGpu, ClothBody, ClothContext, ClothServer, build_grid, load_obj_mesh
+from .cloth import (BaraffClothGpu, ClothBody, ClothContext, ClothServer, build_grid,
+                    kinematic_pose, load_obj_mesh)
 
 __all__ = ["BaraffClothGpu", "ClothBody", "ClothContext", "ClothError", "ClothServer", "REFERENCE_PARAMS", "SolveParams",
-           "build_grid", "load_obj_mesh", "params", "load_library"]
+           "build_grid", "kinematic_pose", "load_obj_mesh", "params", "load_library"]
 
 
 def load_library():

@@ -176,6 +176,12 @@ SIGNATURES = {
     "cloth_export_dihedral": (C.c_int, [P, PI, PI, PF, PF]),
     "cloth_body_create": (C.c_int, [P, C.c_int, C.c_int, PD, PI, C.POINTER(P)]),
     "cloth_body_destroy": (C.c_int, [P]),
+    "cloth_body_set_pos": (C.c_int, [P, PD]),
+    "cloth_body_set_motion": (C.c_int, [P, PD, PD, PD, PD, PD, C.c_double]),
+    "cloth_body_update": (C.c_int, [P, C.c_float]),
+    "cloth_body_get_pos": (C.c_int, [P, PD]),
+    "cloth_kinematic_pose": (C.c_int, [C.c_int, PD, PD, PD, PD, PD, C.c_double, C.c_float,
+                                       PD]),
     "cloth_set_bodies": (C.c_int, [P, C.POINTER(P), C.c_int]),
     "cloth_set_contact_capacity": (C.c_int, [P, C.c_int, C.c_int, C.c_int]),
     "cloth_get_contacts": (C.c_int, [P, C.POINTER(ContactStats), PI, PD, PI, PD]),

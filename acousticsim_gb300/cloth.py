@@ -527,9 +527,28 @@ class BaraffClothGpu:
             pass
 
 
+def _vec3(v) -> np.ndarray:
+    return np.ascontiguousarray(np.asarray(v, np.float64).reshape(-1)[:3])
+
+
+def kinematic_pose(local, init_pos, init_ori, target_pos, target_ori, elapsed_sec: float,
+                   time: float) -> np.ndarray:
+    """cKinematicBody's pose of a moving body at body time `time` applied to
+    its local mesh (host only): world positions, nv x 3."""
+    local = np.ascontiguousarray(local, np.float64).reshape(-1, 3)
+    out = np.zeros_like(local)
+    vs = [_vec3(v) for v in (init_pos, init_ori, target_pos, target_ori)]
+    N.call("cloth_kinematic_pose", local.shape[0], N.ptr(local, C.c_double),
+           *[N.ptr(v, C.c_double) for v in vs], float(elapsed_sec), float(time),
+           N.ptr(out, C.c_double))
+    return out
+
+
 class ClothBody:
-    """A static kinematic body (cKinematicBody after Init): a world-space
-    triangle mesh the cloths of a context can collide with."""
+    """A kinematic body (cKinematicBody after Init): a world-space triangle
+    mesh the cloths of a context can collide with.  Static unless moved with
+    set_pos, or given the reference's time-driven motion (set_motion, then
+    update(dt) per frame)."""
 
     def __init__(self, ctx: ClothContext, pos, tris):
         self.ctx = ctx
@@ -544,6 +563,25 @@ class ClothBody:
     @property
     def handle(self):
         return self._h
+
+    def set_pos(self, pos) -> None:
+        pos = np.ascontiguousarray(pos, np.float64).reshape(-1)
+        N.call("cloth_body_set_pos", self._h, N.ptr(pos, C.c_double))
+
+    def set_motion(self, local, init_pos, init_ori, target_pos, target_ori,
+                   elapsed_sec: float) -> None:
+        local = np.ascontiguousarray(local, np.float64).reshape(-1)
+        vs = [_vec3(v) for v in (init_pos, init_ori, target_pos, target_ori)]
+        N.call("cloth_body_set_motion", self._h, N.ptr(local, C.c_double),
+               *[N.ptr(v, C.c_double) for v in vs], float(elapsed_sec))
+
+    def update(self, dt: float) -> None:
+        N.call("cloth_body_update", self._h, float(dt))
+
+    def get_pos(self) -> np.ndarray:
+        out = np.zeros((self.pos.shape[0], 3), np.float64)
+        N.call("cloth_body_get_pos", self._h, N.ptr(out, C.c_double))
+        return out
 
     def close(self) -> None:
         if self._h and N.load().cloth_body_destroy(self._h) == N.CLOTH_OK:

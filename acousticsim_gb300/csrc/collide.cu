@@ -65,6 +65,16 @@ struct cloth_body_s
     char *mem = nullptr;
     size_t bytes = 0;
     BodyView v{};
+    // host copies: the triangles and the normals the body's Init left (a
+    // moving body keeps them, as cKinematicBody::Update does)
+    std::vector<int> tris;
+    std::vector<double> tn, vn;
+    // time-driven motion (cloth_body_set_motion); unused for other bodies
+    bool moving = false;
+    std::vector<double> local;
+    double ip[3] = {0, 0, 0}, io[3] = {0, 0, 0}, tp[3] = {0, 0, 0}, to[3] = {0, 0, 0};
+    double elapsed = 0.0;
+    float time = 0.f;
 };
 
 struct cloth_collide_s
@@ -1562,15 +1572,16 @@ void cloth::detail::body_release_all(cloth_ctx *ctx)
 }
 
 // ------------------------------------------------------------------ ABI
-int cloth_body_create(cloth_ctx *ctx, int nv, int nt, const double *pos, const int *tris,
-                      cloth_body **out)
+namespace {
+
+// A body's device arrays from world-space positions: edges, normals (those
+// given, else computed as the body's Init computes them), grown boxes,
+// vertex -> triangle lists and the uniform grid, in a fresh allocation that
+// b->mem / b->bytes / b->v then describe (the caller owns any older one).
+// Called with the context's lock held and its device current.
+int body_build(cloth_ctx *ctx, int nv, int nt, const double *pos, const int *tris,
+               const double *keep_tn, const double *keep_vn, cloth_body_s *b)
 {
-    if (!ctx || !pos || !tris || !out || nv < 3 || nt < 1)
-        return col_fail(CLOTH_ERR_INVALID, "cloth_body_create: bad argument");
-    *out = nullptr;
-    for (int k = 0; k < 3 * nt; k++)
-        if (tris[k] < 0 || tris[k] >= nv)
-            return col_fail(CLOTH_ERR_MESH, "cloth_body_create: triangle vertex id out of range");
     Mesh m;
     m.nv = nv;
     m.nt = nt;
@@ -1594,7 +1605,7 @@ int cloth_body_create(cloth_ctx *ctx, int nv, int nt, const double *pos, const i
     // normals as the body's Init leaves them (cKinematicBody::Init:
     // CalcTriangleInitArea, UpdateTriangleNormal, UpdateVertexNormalFromTriangleNormal)
     std::vector<double> tn(3 * size_t(nt)), vn(3 * size_t(nv), 0.0);
-    for (int t = 0; t < nt; t++)
+    for (int t = 0; t < nt && !keep_tn; t++)
     {
         const double *p0 = pos + 3 * size_t(tris[3 * t]), *p1 = pos + 3 * size_t(tris[3 * t + 1]),
                      *p2 = pos + 3 * size_t(tris[3 * t + 2]);
@@ -1615,13 +1626,18 @@ int cloth_body_create(cloth_ctx *ctx, int nv, int nt, const double *pos, const i
             for (int k = 0; k < 3; k++)
                 vn[3 * size_t(tris[3 * t + i]) + k] += tn[3 * size_t(t) + k] * area;
     }
-    for (int v = 0; v < nv; v++)
+    for (int v = 0; v < nv && !keep_tn; v++)
     {
         double *n = &vn[3 * size_t(v)];
         const double l = std::sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
         if (l > 0)
             for (int k = 0; k < 3; k++)
                 n[k] /= l;
+    }
+    if (keep_tn)
+    {
+        tn.assign(keep_tn, keep_tn + 3 * size_t(nt));
+        vn.assign(keep_vn, keep_vn + 3 * size_t(nv));
     }
     // grown boxes, vertex -> triangles, uniform grid over the boxes
     std::vector<double> blo(3 * size_t(nt)), bhi(3 * size_t(nt));
@@ -1705,18 +1721,13 @@ int cloth_body_create(cloth_ctx *ctx, int nv, int nt, const double *pos, const i
                  o_lo = L.take<double>(3 * size_t(nt)), o_hi = L.take<double>(3 * size_t(nt)),
                  o_vo = L.take<int>(size_t(nv) + 1), o_vl = L.take<int>(3 * size_t(nt)),
                  o_co = L.take<int>(size_t(ncell) + 1), o_ct = L.take<int>(std::max<size_t>(reg.size(), 1));
-    std::lock_guard<std::recursive_mutex> lk(ctx->mu);
-    CCK(cudaSetDevice(ctx->device));
-    auto b = new cloth_body_s();
-    b->ctx = ctx;
-    b->nv = nv;
-    b->nt = nt;
     b->ne = ne;
+    b->mem = nullptr;
     if (cudaMalloc(&b->mem, L.off) != cudaSuccess)
     {
         cudaGetLastError();
-        delete b;
-        return col_fail(CLOTH_ERR_OOM, "cloth_body_create: device allocation failed");
+        b->mem = nullptr;
+        return col_fail(CLOTH_ERR_OOM, "cloth body: device allocation failed");
     }
     b->bytes = L.off;
     char *base = b->mem;
@@ -1732,9 +1743,9 @@ int cloth_body_create(cloth_ctx *ctx, int nv, int nt, const double *pos, const i
               (ctris.empty() || up(o_ct, ctris.data(), ctris.size() * 4));
     if (!ok)
     {
-        body_free(b);
-        delete b;
-        return col_fail(CLOTH_ERR_CUDA, "cloth_body_create: upload failed");
+        cudaFree(b->mem);
+        b->mem = nullptr;
+        return col_fail(CLOTH_ERR_CUDA, "cloth body: upload failed");
     }
     BodyView &v = b->v;
     v.nv = nv;
@@ -1758,9 +1769,210 @@ int cloth_body_create(cloth_ctx *ctx, int nv, int nt, const double *pos, const i
         v.gdim[k] = gdim[k];
     }
     v.cell = cell;
+    b->tn = std::move(tn);
+    b->vn = std::move(vn);
+    (void)ctx;
+    return CLOTH_OK;
+}
+
+// cKinematicBody's world transform at body time t (KinematicBody.cpp
+// UpdateCurWorldTransformByTime, GetWorldTransform; RotUtil.cpp
+// EulerAnglesToRotMat, XYZ order: Rz * Ry * Rx) applied to the local mesh.
+// Products are summed term by term in index order, as the reference's 4x4
+// products evaluate them.
+void kinematic_pose(int nv, const double *local, const double *ip, const double *io,
+                    const double *tp, const double *to, double elapsed, float time,
+                    double *world)
+{
+    float ct = time;
+    if (ct > elapsed)
+        ct = float(elapsed);
+    const double a = (elapsed - double(ct)) / elapsed, c = double(ct) / elapsed;
+    double pos[3], ori[3];
+    for (int k = 0; k < 3; k++)
+    {
+        pos[k] = a * ip[k] + c * tp[k];
+        ori[k] = a * io[k] + c * to[k];
+    }
+    auto rot = [](int axis, double ang, double m[4][4]) {
+        for (int i = 0; i < 4; i++)
+            for (int j = 0; j < 4; j++)
+                m[i][j] = i == j ? 1.0 : 0.0;
+        const double cs = std::cos(ang), sn = std::sin(ang);
+        const int p = axis == 0 ? 1 : 0, q = axis == 2 ? 1 : 2;
+        m[p][p] = cs;
+        m[q][q] = cs;
+        if (axis == 1) // about y: (0 2) = sin, (2 0) = -sin
+        {
+            m[p][q] = sn;
+            m[q][p] = -sn;
+        }
+        else
+        {
+            m[p][q] = -sn;
+            m[q][p] = sn;
+        }
+    };
+    auto mul = [](const double l[4][4], const double r[4][4], double o[4][4]) {
+        for (int i = 0; i < 4; i++)
+            for (int j = 0; j < 4; j++)
+            {
+                double s = l[i][0] * r[0][j];
+                for (int k = 1; k < 4; k++)
+                    s = l[i][k] * r[k][j] + s;
+                o[i][j] = s;
+            }
+    };
+    double rx[4][4], ry[4][4], rz[4][4], zy[4][4], r[4][4];
+    rot(0, ori[0], rx);
+    rot(1, ori[1], ry);
+    rot(2, ori[2], rz);
+    mul(rz, ry, zy);
+    mul(zy, rx, r);
+    double tr[4][4];
+    for (int i = 0; i < 4; i++)
+        for (int j = 0; j < 4; j++)
+            tr[i][j] = (i < 3 && j < 3) ? r[i][j] : (i == j ? 1.0 : 0.0);
+    for (int i = 0; i < 3; i++)
+        tr[i][3] = pos[i];
+    for (int v = 0; v < nv; v++)
+    {
+        const double x[4] = {local[3 * size_t(v)], local[3 * size_t(v) + 1],
+                             local[3 * size_t(v) + 2], 1.0};
+        for (int i = 0; i < 3; i++)
+        {
+            double s = tr[i][0] * x[0];
+            for (int k = 1; k < 4; k++)
+                s = tr[i][k] * x[k] + s;
+            world[3 * size_t(v) + i] = s;
+        }
+    }
+}
+
+// New device arrays for new positions; keep_normals: the body's current ones
+int body_move(cloth_body_s *b, const double *pos, bool keep_normals)
+{
+    cloth_ctx *ctx = b->ctx;
+    CCK(cudaSetDevice(ctx->device));
+    CCK(cudaStreamSynchronize(ctx->stream)); // no detection still reads the old arrays
+    cloth_body_s nb;
+    nb.ctx = ctx;
+    nb.nv = b->nv;
+    nb.nt = b->nt;
+    const int rc = body_build(ctx, b->nv, b->nt, pos, b->tris.data(),
+                              keep_normals ? b->tn.data() : nullptr,
+                              keep_normals ? b->vn.data() : nullptr, &nb);
+    if (rc != CLOTH_OK)
+        return rc;
+    cudaFree(b->mem);
+    ctx->bytes = ctx->bytes - b->bytes + nb.bytes;
+    b->mem = nb.mem;
+    b->bytes = nb.bytes;
+    b->v = nb.v;
+    b->tn = std::move(nb.tn);
+    b->vn = std::move(nb.vn);
+    return CLOTH_OK;
+}
+
+} // namespace
+
+int cloth_body_create(cloth_ctx *ctx, int nv, int nt, const double *pos, const int *tris,
+                      cloth_body **out)
+{
+    if (!ctx || !pos || !tris || !out || nv < 3 || nt < 1)
+        return col_fail(CLOTH_ERR_INVALID, "cloth_body_create: bad argument");
+    *out = nullptr;
+    for (int k = 0; k < 3 * nt; k++)
+        if (tris[k] < 0 || tris[k] >= nv)
+            return col_fail(CLOTH_ERR_MESH, "cloth_body_create: triangle vertex id out of range");
+    std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+    CCK(cudaSetDevice(ctx->device));
+    auto b = new cloth_body_s();
+    b->ctx = ctx;
+    b->nv = nv;
+    b->nt = nt;
+    b->tris.assign(tris, tris + 3 * size_t(nt));
+    const int rc = body_build(ctx, nv, nt, pos, tris, nullptr, nullptr, b);
+    if (rc != CLOTH_OK)
+    {
+        delete b;
+        return rc;
+    }
     ctx->bodies.push_back(b);
     ctx->bytes += b->bytes;
     *out = b;
+    return CLOTH_OK;
+}
+
+int cloth_kinematic_pose(int nv, const double *local, const double *init_pos,
+                         const double *init_ori, const double *target_pos,
+                         const double *target_ori, double elapsed_sec, float time,
+                         double *world)
+{
+    if (nv < 1 || !local || !init_pos || !init_ori || !target_pos || !target_ori || !world ||
+        !(elapsed_sec > 0))
+        return col_fail(CLOTH_ERR_INVALID, "cloth_kinematic_pose: bad argument");
+    kinematic_pose(nv, local, init_pos, init_ori, target_pos, target_ori, elapsed_sec, time,
+                   world);
+    return CLOTH_OK;
+}
+
+int cloth_body_set_pos(cloth_body *b, const double *pos)
+{
+    if (!b || !pos)
+        return col_fail(CLOTH_ERR_INVALID, "cloth_body_set_pos: bad argument");
+    std::lock_guard<std::recursive_mutex> lk(b->ctx->mu);
+    return body_move(b, pos, true);
+}
+
+int cloth_body_set_motion(cloth_body *b, const double *local, const double *init_pos,
+                          const double *init_ori, const double *target_pos,
+                          const double *target_ori, double elapsed_sec)
+{
+    if (!b || !local || !init_pos || !init_ori || !target_pos || !target_ori ||
+        !(elapsed_sec > 0))
+        return col_fail(CLOTH_ERR_INVALID, "cloth_body_set_motion: bad argument");
+    std::lock_guard<std::recursive_mutex> lk(b->ctx->mu);
+    b->local.assign(local, local + 3 * size_t(b->nv));
+    for (int k = 0; k < 3; k++)
+    {
+        b->ip[k] = init_pos[k];
+        b->io[k] = init_ori[k];
+        b->tp[k] = target_pos[k];
+        b->to[k] = target_ori[k];
+    }
+    b->elapsed = elapsed_sec;
+    b->time = 0.f;
+    b->moving = true;
+    // placed at the initial pose, normals from there (the body's Init)
+    std::vector<double> w(3 * size_t(b->nv));
+    kinematic_pose(b->nv, b->local.data(), b->ip, b->io, b->tp, b->to, b->elapsed, b->time,
+                   w.data());
+    return body_move(b, w.data(), false);
+}
+
+int cloth_body_update(cloth_body *b, float dt)
+{
+    if (!b)
+        return col_fail(CLOTH_ERR_INVALID, "cloth_body_update: NULL body");
+    std::lock_guard<std::recursive_mutex> lk(b->ctx->mu);
+    b->time += dt; // the body clock is a float, as mCurTime is
+    if (!b->moving)
+        return CLOTH_OK;
+    std::vector<double> w(3 * size_t(b->nv));
+    kinematic_pose(b->nv, b->local.data(), b->ip, b->io, b->tp, b->to, b->elapsed, b->time,
+                   w.data());
+    return body_move(b, w.data(), true);
+}
+
+int cloth_body_get_pos(cloth_body *b, double *pos)
+{
+    if (!b || !pos)
+        return col_fail(CLOTH_ERR_INVALID, "cloth_body_get_pos: bad argument");
+    std::lock_guard<std::recursive_mutex> lk(b->ctx->mu);
+    CCK(cudaSetDevice(b->ctx->device));
+    CCK(cudaStreamSynchronize(b->ctx->stream));
+    CCK(cudaMemcpy(pos, b->v.pos, 3 * size_t(b->nv) * sizeof(double), cudaMemcpyDeviceToHost));
     return CLOTH_OK;
 }
 

@@ -384,6 +384,29 @@ int cloth_body_create(cloth_ctx *ctx, int nv, int nt, const double *pos, const i
                       cloth_body **out);
 /* Fails while a cloth still collides with the body. */
 int cloth_body_destroy(cloth_body *body);
+/* Moving bodies (cKinematicBody with "is_static": false, KinematicBody.cpp:
+ * Update, UpdateCurWorldTransformByTime, SetMeshPos). A body's normals stay
+ * those its Init computed, as the reference's moving body keeps them; the
+ * broad-phase boxes and grid are rebuilt for the new positions, and the next
+ * step of a cloth colliding with the body detects contacts against them.
+ * set_pos: any new world-space vertex positions (nv*3, same triangles). */
+int cloth_body_set_pos(cloth_body *body, const double *pos);
+/* The reference's time-driven motion: the body's vertices are the local mesh
+ * (nv*3; the scaled OBJ vertices) posed by a translation and XYZ Euler angles
+ * (Rz Ry Rx) interpolated linearly from init to target over elapsed_sec of
+ * body time, then held. set_motion places the body at the initial pose (body
+ * time 0) and recomputes its normals there (Init); update adds dt to the
+ * body clock (a float, as mCurTime) and moves the body to its pose. */
+int cloth_body_set_motion(cloth_body *body, const double *local, const double *init_pos,
+                          const double *init_ori, const double *target_pos,
+                          const double *target_ori, double elapsed_sec);
+int cloth_body_update(cloth_body *body, float dt);
+int cloth_body_get_pos(cloth_body *body, double *pos);
+/* The same pose on the host, no device needed: world = pose(time) * local. */
+int cloth_kinematic_pose(int nv, const double *local, const double *init_pos,
+                         const double *init_ori, const double *target_pos,
+                         const double *target_ori, double elapsed_sec, float time,
+                         double *world);
 
 /* The CPU cloth's collision handling (cSimScene::PerformCollisionDetection
  * with cBVHCollisionDetecter, src/sim/collision/BVHCollisionDetecter.cpp, and

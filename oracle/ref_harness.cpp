@@ -43,6 +43,15 @@ extern tVector CalcCotangentCoeff(const tVector3d &x0, const tVector3d &x1,
 
 static const int kEll = 32; // tCudaVector32i width (BaraffClothGpu.h:19)
 
+// The reference's kinematic body, with its scaled local mesh (the vertices
+// the pose transforms) readable for the motion fixture.
+struct MotionBody : public cKinematicBody
+{
+    explicit MotionBody(int id) : cKinematicBody(id) {}
+    const tVectorXd &local() const { return mScaledMeshVertices; }
+    float time() const { return mCurTime; }
+};
+
 // ------------------------------------------------------------------ output
 struct Dump
 {
@@ -626,6 +635,48 @@ struct Probe : public cBaraffCloth
         d.put("mass_cpu", "f8", mass_cpu, {n});
     }
 
+    // cKinematicBody::Update(dt) `steps` times on a moving body: the local
+    // mesh, the vertex positions at Init and after every update, the body
+    // clock, and the normals (Init's, which Update leaves alone)
+    static void dump_motion(Dump &d, const Json::Value &kb_conf, float dt, int steps)
+    {
+        auto kb = std::make_shared<MotionBody>(1);
+        kb->Init(kb_conf);
+        const auto &kv = kb->GetVertexArray();
+        const long n = long(kv.size());
+        std::vector<double> local(kb->local().data(), kb->local().data() + 3 * n);
+        std::vector<double> pos, vn0, vn1;
+        std::vector<float> times;
+        auto grab = [&](std::vector<double> &out, bool normal) {
+            for (auto &v : kv)
+                for (int k = 0; k < 3; k++)
+                    out.push_back(normal ? v->mNormal[k] : v->mPos[k]);
+        };
+        grab(pos, false);
+        grab(vn0, true);
+        times.push_back(kb->time());
+        for (int s = 0; s < steps; s++)
+        {
+            kb->Update(dt);
+            grab(pos, false);
+            times.push_back(kb->time());
+        }
+        grab(vn1, true);
+        std::vector<int> tris;
+        for (auto &t : kb->GetTriangleArray())
+        {
+            tris.push_back(t->mId0);
+            tris.push_back(t->mId1);
+            tris.push_back(t->mId2);
+        }
+        d.put("local", "f8", local, {n, 3});
+        d.put("pos", "f8", pos, {long(steps) + 1, n, 3});
+        d.put("time", "f4", times, {long(steps) + 1});
+        d.put("vnormal_init", "f8", vn0, {n, 3});
+        d.put("vnormal_end", "f8", vn1, {n, 3});
+        d.put("tris", "i4", tris, {long(tris.size() / 3), 3});
+    }
+
     void step(int nsteps)
     {
         double dt = cJsonUtil::ParseAsDouble("default_timestep", conf);
@@ -672,6 +723,15 @@ int main(int argc, char **argv)
         size_t n3 = size_t(c->nv()) * 3;
         Dump d(argv[6]);
         c->dump_collide(d, kb, read_doubles(argv[4], n3), read_doubles(argv[5], n3));
+    }
+    else if (mode == "motion" && argc >= 7)
+    {
+        // motion <cloth cfg> <body cfg> <dt> <steps> <outdir>
+        Json::Value kb;
+        if (!cJsonUtil::LoadJson(argv[3], kb))
+            return 1;
+        Dump d(argv[6]);
+        Probe::dump_motion(d, kb, float(std::atof(argv[4])), std::atoi(argv[5]));
     }
     else if (mode == "step" && argc >= 4)
     {

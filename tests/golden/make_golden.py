@@ -158,6 +158,21 @@ COLLIDE_CASES = [
 ]
 
 
+# A moving kinematic body (cKinematicBody with "is_static": false): the
+# curved patch, posed by translation and XYZ Euler angles interpolated from
+# init to target over elasped_time_sec, stepped by Update(dt) past that time
+# (name, body config, dt, updates).
+MOTION_CASES = [
+    ("body_motion",
+     {"object_name": "patch", "object_type": "KinematicBody", "type": "custom",
+      "mesh_path": "patch.obj", "target_aabb": [0, 0, 0, 0], "scale": [1, 1, 1, 0],
+      "translation": [0.02, -0.01, 0.005, 0], "orientation": [0.1, 0.2, -0.05, 0],
+      "is_static": False, "target_translation": [-0.03, 0.04, 0.02, 0],
+      "target_orientation": [0.25, -0.15, 0.3, 0], "elasped_time_sec": 0.02},
+     0.003, 10),
+]
+
+
 def contact_patch(path: Path, n: int = 12) -> None:
     """A curved n x n patch over x, y in [-0.35, 0.3] x [-0.25, 0.35] at
     z = 1.5 mm + 0.04 r^2, triangle normals facing -z."""
@@ -260,6 +275,29 @@ def main() -> None:
         arrays["body_json"] = np.frombuffer(json.dumps(kb).encode(), np.uint8)
         np.savez_compressed(OUT / f"{name}.npz", **arrays)
         print(name, "contacts pt", cold["pt_i"].shape[0], "ee", cold["ee_i"].shape[0], "->",
+              OUT / f"{name}.npz")
+    for name, kb, dt, steps in MOTION_CASES:
+        if a.only and name not in a.only:
+            continue
+        g = np.load(OUT / "grid20.npz")
+        conf = json.loads(bytes(g["config_json"]).decode())
+        run_kb = dict(kb)
+        contact_patch(OUT / kb["mesh_path"])
+        run_kb["mesh_path"] = str(OUT / kb["mesh_path"])
+        with tempfile.TemporaryDirectory() as td:
+            td = Path(td)
+            (td / "cfg.json").write_text(json.dumps(conf))
+            (td / "kb.json").write_text(json.dumps(run_kb))
+            (td / "mo").mkdir()
+            subprocess.run([str(harness), "motion", str(td / "cfg.json"), str(td / "kb.json"),
+                            repr(dt), str(steps), str(td / "mo")], check=True,
+                           stdout=subprocess.DEVNULL)
+            mo = read_dump(td / "mo")
+        arrays = {f"mo_{k}": v for k, v in mo.items()}
+        arrays["body_json"] = np.frombuffer(json.dumps(kb).encode(), np.uint8)
+        arrays["dt"] = np.array(dt, np.float32)
+        np.savez_compressed(OUT / f"{name}.npz", **arrays)
+        print(name, "vertices", mo["local"].shape[0], "updates", steps, "->",
               OUT / f"{name}.npz")
 
 

@@ -143,7 +143,7 @@ def test_collision_trajectory_vs_oracle(ctx, orc):
     assert all(a == b for a, b in counts[:3])
     disp = rel(cl.GetPos() - x, oc.x - x)
     print("displacement error after 10 steps", disp)
-    assert disp < 1e-3
+    assert disp < 1e-4  # measured 6.5e-6
     cl.set_bodies([])
     cl.close()
     body.close()
@@ -180,3 +180,59 @@ def test_collision_refusals(ctx):
     a.set_bodies([])
     a.close()
     b.close()
+
+
+def test_moving_body_trajectory_vs_oracle(ctx, orc):
+    """The curved patch as a moving body (the reference's time-driven motion:
+    translation and XYZ Euler angles interpolated over 40 ms), pressed 3 mm
+    towards the pinned 20x20 cloth and turned a little while the cloth steps:
+    before each step the body advances by dt (cloth_body_update), and the FP64
+    oracle steps against the same body positions (the host pose, pinned to the
+    reference's cKinematicBody by tests/test_body_motion.py) with the normals
+    of the initial pose, as the reference's moving body keeps them."""
+    from acousticsim_gb300 import ClothBody, kinematic_pose, params
+    m = np.load(GOLDEN / "body_motion.npz")
+    local, tris = m["mo_local"], m["mo_tris"]
+    ip, io = [0.0, 0.0, 0.0], [0.0, 0.0, 0.0]
+    tp, to = [0.004, -0.003, -0.003], [0.02, -0.015, 0.03]
+    elapsed = 0.04
+    _, conf = _load("col_patch")
+    g = np.load(GOLDEN / "grid20.npz")
+    dt = np.float32(conf["default_timestep"])
+    cl = _cloth(ctx, conf, pins=True)
+    body = ClothBody(ctx, local, tris)
+    body.set_motion(local, ip, io, tp, to, elapsed)
+    p0 = kinematic_pose(local, ip, io, tp, to, elapsed, 0.0)
+    assert np.array_equal(body.get_pos(), p0)
+    x, xp = g["x_in"].reshape(-1), g["xpre_in"].reshape(-1)
+    cl.SetPos(x)
+    cl.SetPrePos(xp)
+    cl.set_bodies([body])
+    tn, vn = orc.body_normals(p0, tris)
+    bd = {"pos": p0, "tris": tris, "edges": orc.derive_edges(tris), "tnormal": tn,
+          "vnormal": vn}
+    oc = orc.OracleCloth(cl.mesh, conf, cl.GetConstraintStaticVertices(), bodies=[bd])
+    oc.x, oc.xpre = x.copy(), xp.copy()
+    t = np.float32(0.0)
+    counts = []
+    for _ in range(10):
+        body.update(float(dt))
+        t = np.float32(t + dt)
+        pk = kinematic_pose(local, ip, io, tp, to, elapsed, float(t))
+        assert np.array_equal(body.get_pos(), pk)
+        bd["pos"] = pk
+        st = cl.UpdatePos(0.0, params(max_iters=20000, rel_tol=1e-8))
+        assert st["status"] == "OK", st
+        con = cl.get_contacts()
+        oc.step(rel_tol=1e-12)
+        counts.append(((len(con["pt_i"]), len(con["ee_i"])),
+                       (len(oc.last_contacts["pt_i"]), len(oc.last_contacts["ee_i"]))))
+    print("moving body: contacts per step (device, oracle):", counts)
+    assert all(a == b for a, b in counts[:3])
+    assert sum(a[0] + a[1] for a, _ in counts) > 0
+    disp = rel(cl.GetPos() - x, oc.x - x)
+    print("moving body: displacement error after 10 steps", disp)
+    assert disp < 1e-4
+    cl.set_bodies([])
+    cl.close()
+    body.close()

@@ -101,7 +101,7 @@ def test_dihedral_solve_matches_direct_solve(ctx, orc, case, solver):
     err = rel(dx, g["sys_dih_dx"].reshape(-1))
     print(case, "iters", st["iters"], "true residual", true_rel, "dx error", err)
     assert true_rel < 5e-6
-    assert err < 1e-3
+    assert err < 2e-4  # measured up to 4e-5
     # the FP64 residual kernel applies the skew parts too: it equals the
     # residual of the exported system formed here in FP64, up to the one
     # extra float rounding of the exported entries that hold a skew part
@@ -187,7 +187,7 @@ def test_dihedral_trajectory_vs_oracle(ctx, orc, solver):
         oc.step(rel_tol=1e-12)
     disp_err = rel(c.GetPos() - x, oc.x - x)
     print("displacement error after 20 steps", disp_err)
-    assert disp_err < 1e-3
+    assert disp_err < 2e-4  # measured 4.9e-5
     c.close()
 
 

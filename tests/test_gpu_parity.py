@@ -366,7 +366,7 @@ def test_plain_baseline_matches_fast_path(ctx, orc):
     oc.step(rel_tol=1e-12)
     da, db, do = a.GetPos() - x, b.GetPos() - x, oc.x - x
     print("fast vs oracle", rel(da, do), "plain vs oracle", rel(db, do), "iters", sa["iters"], sb["iters"])
-    assert rel(da, do) < 1e-3 and rel(db, do) < 1e-3
+    assert rel(da, do) < 2e-4 and rel(db, do) < 2e-4  # measured 4.8e-5 both
     assert np.array_equal(b.GetPrePos(), a.GetPrePos())
     a.close()
     b.close()
