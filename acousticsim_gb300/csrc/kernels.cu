@@ -1503,16 +1503,57 @@ __device__ __forceinline__ BulkRegs bulk_regs(const BulkHdr &h, const unsigned c
     return r;
 }
 
-// One row of q = A p from a filled stage (thread t = row start + t); returns
-// p.q.  STAGED: p over the tile's column range is in the stage (formed there);
-// otherwise p = z + beta p_old is gathered from global memory at each column.
-template <bool SKEW, bool STAGED>
-__device__ __forceinline__ float bulk_row(const BulkRegs &r, int t)
+// The lower slots' transposed blocks of one row, gathered from global memory
+// (L2) before the stage's p is formed, so that their latency overlaps the
+// halo pass and the upper slots' products: the first PF lower slots.
+template <bool SKEW>
+struct BulkLower
 {
-    constexpr int CH = 4; // transposed-block gathers in flight together (8: 235 registers, one block per SM, slower)
+    static constexpr int PF = 6;
+    float4 a0[PF];
+    float2 a1[PF];
+    float4 aw[SKEW ? PF : 1];
+    uint32_t ref[PF];
+};
+
+template <bool SKEW>
+__device__ __forceinline__ void bulk_lower_issue(const BulkHdr &h, const unsigned char *stage,
+                                                 int t, int ds, BulkLower<SKEW> &L)
+{
+    const uint32_t *__restrict__ lr = reinterpret_cast<const uint32_t *>(stage + h.o_lr) + t;
+    const bool sk = SKEW && h.skew;
+    const int wu = h.wu;
+    const float4 *__restrict__ A0 = h.A0;
+    const float2 *__restrict__ A1 = h.A1;
+#pragma unroll
+    for (int k = 0; k < BulkLower<SKEW>::PF; k++)
+        if (k < ds)
+        {
+            const uint32_t ref = lr[k * kTile];
+            const uint32_t o = lref_block(ref, wu);
+            L.ref[k] = ref;
+            L.a0[k] = __ldcg(A0 + o);
+            L.a1[k] = __ldcg(A1 + o);
+            if (sk)
+                L.aw[k] = __ldcg(h.Aw + o);
+        }
+}
+
+// One row of q = A p from a filled stage (thread t = row start + t, `info`
+// its row info, L its first lower slots' blocks); returns p.q.  STAGED: p over
+// the tile's column range is in the stage (formed there); otherwise
+// p = z + beta p_old is gathered from global memory at each column.  The sum
+// runs in the one order of every SpMV: lower slots in column order, then the
+// diagonal and upper slots; the upper slots' block products are formed first
+// (each product rounds the same wherever it is formed).
+template <bool SKEW, bool STAGED>
+__device__ __forceinline__ float bulk_row(const BulkRegs &r, int t, int info,
+                                          const BulkLower<SKEW> &L)
+{
+    constexpr int CH = 4; // lower slots past the prefetched ones: gathers in flight together
+    constexpr int PU = 0; // upper slots whose products are formed ahead (more: spills)
     const unsigned char *__restrict__ stage = r.stage;
     const int row = r.start + t;
-    const int info = reinterpret_cast<const int *>(stage)[t];
     const int len = info & 255, ds = (info >> 8) & 255;
     const float4 *__restrict__ P = reinterpret_cast<const float4 *>(stage + r.o_z);
     const float beta = r.beta;
@@ -1525,11 +1566,42 @@ __device__ __forceinline__ float bulk_row(const BulkRegs &r, int t)
         return pc;
     };
     const float3 pv = pcol(row);
-    const uint32_t *__restrict__ lr = reinterpret_cast<const uint32_t *>(stage + r.o_lr) + t;
     const bool sk = SKEW && r.skew;
+    const int *__restrict__ cu = reinterpret_cast<const int *>(stage + r.o_cu) + t;
+    const float4 *__restrict__ a0s = reinterpret_cast<const float4 *>(stage + r.o_a0) + t;
+    const float2 *__restrict__ a1s = reinterpret_cast<const float2 *>(stage + r.o_a1) + t;
+    const float4 *__restrict__ aws = reinterpret_cast<const float4 *>(stage + r.o_aw) + t;
+    const int nu = len - ds;
+    // diagonal and upper slots (all staged): products of the first PU
+    float3 su[PU > 0 ? PU : 1], wu_[SKEW && PU > 0 ? PU : 1];
+#pragma unroll
+    for (int k = 0; k < PU; k++)
+        if (k < nu)
+        {
+            const float4 a0 = a0s[k * kTile];
+            const float2 a1 = a1s[k * kTile];
+            const float3 pc = (!STAGED && k == 0) ? pv : pcol(cu[k * kTile]);
+            const float A[6] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y};
+            su[k] = symv(A, pc);
+            if (sk)
+                wu_[SKEW ? k : 0] = skewv(aws[k * kTile], pc);
+        }
     float3 q = make_float3(0.f, 0.f, 0.f);
-    // lower slots, column order: blocks at the transposed position (L2)
-    for (int s0 = 0; s0 < ds; s0 += CH)
+    // lower slots, column order: the prefetched transposed blocks ...
+#pragma unroll
+    for (int k = 0; k < BulkLower<SKEW>::PF; k++)
+        if (k < ds)
+        {
+            const float3 pc = pcol(lref_col(L.ref[k]));
+            const float A[6] = {L.a0[k].x, L.a0[k].y, L.a0[k].z, L.a0[k].w, L.a1[k].x, L.a1[k].y};
+            q = q + symv(A, pc);
+            if (sk)
+                q = q - skewv(L.aw[SKEW ? k : 0], pc);
+        }
+    // ... and any further ones, gathered here (L2)
+    const uint32_t *__restrict__ lr = reinterpret_cast<const uint32_t *>(stage + r.o_lr) + t;
+#pragma unroll 1
+    for (int s0 = BulkLower<SKEW>::PF; s0 < ds; s0 += CH)
     {
         float4 a0[CH], aw[CH];
         float2 a1[CH];
@@ -1556,17 +1628,21 @@ __device__ __forceinline__ float bulk_row(const BulkRegs &r, int t)
                     q = q - skewv(aw[k], pc[k]);
             }
     }
-    // diagonal and upper slots: everything staged
-    const int *__restrict__ cu = reinterpret_cast<const int *>(stage + r.o_cu) + t;
-    const float4 *__restrict__ a0s = reinterpret_cast<const float4 *>(stage + r.o_a0) + t;
-    const float2 *__restrict__ a1s = reinterpret_cast<const float2 *>(stage + r.o_a1) + t;
-    const float4 *__restrict__ aws = reinterpret_cast<const float4 *>(stage + r.o_aw) + t;
-    const int nu = len - ds;
-    for (int u = 0; u < nu; u++)
+    // diagonal and upper slots in slot order
+#pragma unroll
+    for (int k = 0; k < PU; k++)
+        if (k < nu)
+        {
+            q = q + su[k];
+            if (sk)
+                q = q + wu_[SKEW ? k : 0];
+        }
+#pragma unroll 1
+    for (int u = PU; u < nu; u++)
     {
         const float4 a0 = a0s[u * kTile];
         const float2 a1 = a1s[u * kTile];
-        const float3 pc = (!STAGED && u == 0) ? pv : pcol(cu[u * kTile]);
+        const float3 pc = pcol(cu[u * kTile]);
         const float A[6] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y};
         q = q + symv(A, pc);
         if (sk)
@@ -1615,7 +1691,7 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, unsigned parity
 } // namespace
 
 template <int NST, bool SKEW, bool HALO>
-__global__ void __launch_bounds__(kBulkThreads) k_spmv_bulk(InstDesc *const *descs,
+__global__ void __launch_bounds__(kBulkThreads, SKEW ? 1 : 2) k_spmv_bulk(InstDesc *const *descs,
                                                             const Tile *tiles, BatchCtl *ctl,
                                                             int use_cond,
                                                             cudaGraphConditionalHandle hcond)
@@ -1623,7 +1699,7 @@ __global__ void __launch_bounds__(kBulkThreads) k_spmv_bulk(InstDesc *const *des
     extern __shared__ __align__(128) unsigned char bulk_smem[];
     __shared__ __align__(8) uint64_t full[NST], empty[NST];
     __shared__ BulkHdr hdr[NST];
-    __shared__ double wsum[kTile / 32];
+    __shared__ double wsum[2][kTile / 32];
     const unsigned stage_bytes = (dynamic_smem_bytes() / NST) & ~127u;
     const int ntiles = ctl->n_tiles_rows;
     const int G = gridDim.x;
@@ -1700,6 +1776,12 @@ __global__ void __launch_bounds__(kBulkThreads) k_spmv_bulk(InstDesc *const *des
         const BulkHdr &hd = hdr[stg];
         if (hd.go)
         {
+            const bool act = tid < hd.nrows;
+            const int info = act ? reinterpret_cast<const int *>(stage)[tid] : 0;
+            // the lower slots' gathers go out first, ahead of the halo pass
+            BulkLower<SKEW> L;
+            if (act)
+                bulk_lower_issue<SKEW>(hd, stage, tid, (info >> 8) & 255, L);
             if (hd.nh && hd.beta != 0.f)
             {
                 // p = z + beta p_old over the halo, in place of z
@@ -1710,32 +1792,42 @@ __global__ void __launch_bounds__(kBulkThreads) k_spmv_bulk(InstDesc *const *des
                 consumer_sync();
             }
             float pq = 0.f;
-            if (tid < hd.nrows)
+            if (act)
             {
                 const BulkRegs r = bulk_regs(hd, stage);
-                pq = hd.nh ? bulk_row<SKEW, true>(r, tid) : bulk_row<SKEW, false>(r, tid);
+                pq = hd.nh ? bulk_row<SKEW, true>(r, tid, info, L)
+                           : bulk_row<SKEW, false>(r, tid, info, L);
             }
+            double *const part = hd.part + hd.tile_idx;
             // the tile's p.q: FP32 warp sums, FP64 over the warps in order
-            // (group_sum's arithmetic and order)
+            // (group_sum's arithmetic and order); the partials alternate
+            // between two buffers, so one barrier per tile serves both the
+            // partials and the stage's release
             const float t = warp_sum(pq);
             if (lane == 0)
-                wsum[warp] = double(t);
+                wsum[j & 1][warp] = double(t);
+            // generic writes to the stage (the halo's p) are ordered before
+            // the copy engine refills it
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
             consumer_sync();
+            if (lane == 0)
+                mbar_arrive(&empty[stg]);
             if (tid == 0)
             {
-                double v = wsum[0];
+                double v = wsum[j & 1][0];
 #pragma unroll
                 for (int k = 1; k < kTile / 32; k++)
-                    v += wsum[k];
-                hd.part[hd.tile_idx] = v;
+                    v += wsum[j & 1][k];
+                *part = v;
             }
         }
-        // release the stage: generic writes to it (the halo's p) are ordered
-        // before the copy engine refills it, and the header before its rewrite
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        consumer_sync();
-        if (lane == 0)
-            mbar_arrive(&empty[stg]);
+        else
+        {
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            consumer_sync();
+            if (lane == 0)
+                mbar_arrive(&empty[stg]);
+        }
     }
 }
 
