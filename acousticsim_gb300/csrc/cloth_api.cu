@@ -64,6 +64,10 @@ struct Batch
     int *d_inst = nullptr;
     Tile *d_rt = nullptr, *d_tt = nullptr;
     BatchCtl *d_ctl = nullptr;
+    // the members' solve states gathered after a step, read back in one copy
+    InstState *d_states = nullptr;
+    BatchCtl *d_ctl_copy = nullptr;
+    char *h_pinned = nullptr; // pinned: the members' states, then the set's control word
     int n_rt = 0, n_tt = 0;
     int grid_tri = 1, grid_row = 1;
     // graph-loop kernel variants (autotuned on the first step) and their grids
@@ -138,6 +142,8 @@ struct Batch
             cudaGraphExecDestroy(solve_exec);
         if (mem)
             cudaFree(mem);
+        if (h_pinned)
+            cudaFreeHost(h_pinned);
         if (d_work)
             cudaFree(d_work);
     }
@@ -757,8 +763,12 @@ int make_batch(cloth_ctx *ctx, const std::vector<cloth_s *> &members,
     Layout L;
     size_t o_d = L.take<InstDesc *>(descs.size()), o_i = L.take<int>(inst.size()),
            o_rt = L.take<Tile>(rt.size()), o_tt = L.take<Tile>(tt.size()),
-           o_c = L.take<BatchCtl>(1);
+           o_c = L.take<BatchCtl>(1), o_st = L.take<InstState>(members.size()),
+           o_cc = L.take<BatchCtl>(1);
     CK(cudaMalloc(&b->mem, L.off));
+    b->d_states = reinterpret_cast<InstState *>(b->mem + o_st);
+    b->d_ctl_copy = reinterpret_cast<BatchCtl *>(b->mem + o_cc);
+    CK(cudaMallocHost(&b->h_pinned, members.size() * sizeof(InstState) + sizeof(BatchCtl)));
     b->d_descs = reinterpret_cast<InstDesc **>(b->mem + o_d);
     b->d_inst = reinterpret_cast<int *>(b->mem + o_i);
     b->d_rt = reinterpret_cast<Tile *>(b->mem + o_rt);
@@ -1256,16 +1266,25 @@ int read_stats(Batch *b, cloth_solve_stats *stats)
 {
     if (!stats)
         return CLOTH_OK;
-    CK(cudaStreamSynchronize(b->ctx->stream));
+    // every member's state and the set's control word: gathered on the
+    // device, one copy back
+    cudaStream_t s = b->ctx->stream;
+    const int n = int(b->members.size());
+    InstState *h_st = reinterpret_cast<InstState *>(b->h_pinned);
+    BatchCtl *h_ctl = reinterpret_cast<BatchCtl *>(b->h_pinned + n * sizeof(InstState));
+    k_snap_state<<<std::min(n, 1024), 64, 0, s>>>(b->d_descs, b->d_inst, n, b->d_states,
+                                                   b->d_ctl, b->d_ctl_copy, 0);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(h_st, b->d_states, n * sizeof(InstState), cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(h_ctl, b->d_ctl_copy, sizeof(BatchCtl), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
     // a bounded wait of the graph-loop kernels that gave up (sticky: cleared here)
-    int ctl_err = 0;
-    CK(cudaMemcpy(&ctl_err, &b->d_ctl->err, sizeof(int), cudaMemcpyDeviceToHost));
+    const int ctl_err = h_ctl->err;
     if (ctl_err)
         CK(cudaMemset(&b->d_ctl->err, 0, sizeof(int)));
-    for (size_t i = 0; i < b->members.size(); i++)
+    for (int i = 0; i < n; i++)
     {
-        InstState st;
-        CK(cudaMemcpy(&st, b->members[i]->d_state, sizeof(st), cudaMemcpyDeviceToHost));
+        const InstState &st = h_st[i];
         cloth_solve_stats &o = stats[i];
         o.iters = st.iter;
         // a bounded device wait that gave up flags the team (bar_err) or the set
