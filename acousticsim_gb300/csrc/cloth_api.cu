@@ -1004,7 +1004,8 @@ int add_kernel(cudaGraph_t g, cudaGraphNode_t *node, const cudaGraphNode_t *deps
     return CLOTH_OK;
 }
 
-// Graph of the PCG loop: k_cond, then while (any active) { spmv; update }.
+// Graph of the PCG loop: k_cond, then while (any active) { kLoopBodyIters x
+// (spmv; reduce p.q; update; reduce r.z) }.
 // With full = true the assembly in front and the position update behind are
 // part of the graph too (one launch per step).
 int build_graph(Batch *b, bool full, cudaGraphExec_t *exec)
@@ -1120,17 +1121,25 @@ int build_graph(Batch *b, bool full, cudaGraphExec_t *exec)
             cudaGraphNode_t k1, k2;
             const GraphLoopVariant &sv = b->spmv_variant(b->spmv_v);
             const GraphLoopVariant &uv = kUpdateVariants[b->upd_v];
-            cudaGraphNode_t k3, k4;
+            cudaGraphNode_t k3, k4, prev = nullptr;
             const int gred = reduce_grid(ninst);
-            rc = add_kernel(body, &k1, nullptr, 0, const_cast<void *>(sv.func), b->grid_spmv,
-                            spmv_block(sv), a_spmv, b->smem_spmv);
-            if (rc == CLOTH_OK)
-                rc = add_kernel(body, &k3, &k1, 1, (void *)k_reduce_pq, gred, kTile, a_red);
-            if (rc == CLOTH_OK)
-                rc = add_kernel(body, &k2, &k3, 1, const_cast<void *>(uv.func),
-                                b->grid_update, kTile / uv.rows_per_thread, a_upd);
-            if (rc == CLOTH_OK)
-                rc = add_kernel(body, &k4, &k2, 1, (void *)k_reduce_rz, gred, kTile, a_red);
+            // kLoopBodyIters PCG iterations per evaluation of the while
+            // condition (each evaluation costs about as much as a small
+            // kernel); an instance that ends inside the body skips its tiles
+            for (int u = 0; u < kLoopBodyIters && rc == CLOTH_OK; u++)
+            {
+                rc = add_kernel(body, &k1, prev ? &prev : nullptr, prev ? 1 : 0,
+                                const_cast<void *>(sv.func), b->grid_spmv, spmv_block(sv),
+                                a_spmv, b->smem_spmv);
+                if (rc == CLOTH_OK)
+                    rc = add_kernel(body, &k3, &k1, 1, (void *)k_reduce_pq, gred, kTile, a_red);
+                if (rc == CLOTH_OK)
+                    rc = add_kernel(body, &k2, &k3, 1, const_cast<void *>(uv.func),
+                                    b->grid_update, kTile / uv.rows_per_thread, a_upd);
+                if (rc == CLOTH_OK)
+                    rc = add_kernel(body, &k4, &k2, 1, (void *)k_reduce_rz, gred, kTile, a_red);
+                prev = k4;
+            }
             last = cn;
         }
     }

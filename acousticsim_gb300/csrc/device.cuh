@@ -258,6 +258,11 @@ struct GraphLoopVariant
     int bulk_halo;   // the bulk SpMV also stages p over each tile's column range
 };
 
+// PCG iterations per body of the graph loop's conditional while node
+// (measured on 256 cloths: 1, 2, 4 iterations per body give 38.1, 36.7 and
+// 35.8 ms per batched step)
+constexpr int kLoopBodyIters = 4;
+
 // Bulk-staged SpMV (k_spmv_bulk): kTile consumer threads plus one producer
 // warp per block; a tile's staged column range (halo) holds at most
 // kBulkHaloCap rows, wider tiles gather p from global memory.

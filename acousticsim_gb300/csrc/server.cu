@@ -10,7 +10,7 @@
 //                 per-solve arrays now point into the pool)
 //   k_pins, k_tri, k_row         assembly and PCG start of those requests only
 //   k_srv_begin   admitted-and-iterating count, chunk iteration budget
-//   while (any iterating && budget left) { k_spmv; k_reduce; k_update; k_reduce }   over every
+//   while (any iterating && budget left) { 1, 2 or 4 x (k_spmv; k_reduce; k_update; k_reduce) }   over every
 //                 request on the GPU (finished ones skip their tiles)
 //   k_advance     x_pre = x, x += dx for requests whose solve ended
 //   k_srv_status  one record per request on the GPU; ended ones are closed
@@ -397,15 +397,26 @@ int build_chunk_graph(cloth_server_s *s)
         {
             cudaGraph_t body = cp.conditional.phGraph_out[0];
             cudaGraphNode_t bl = nullptr, bn = nullptr;
-            rc = add_node(body, &bn, &bl, const_cast<void *>(sv.func), one_wave_spmv,
-                          spmv_block(sv), a_spmv, smem_sv);
-            if (rc == CLOTH_OK)
-                rc = add_node(body, &bn, &bl, (void *)k_reduce_pq, reduce_grid(n), kTile, a_red);
-            if (rc == CLOTH_OK)
-                rc = add_node(body, &bn, &bl, const_cast<void *>(uv.func), one_wave_upd,
-                              kTile / uv.rows_per_thread, a_upd);
-            if (rc == CLOTH_OK)
-                rc = add_node(body, &bn, &bl, (void *)k_reduce_rz, reduce_grid(n), kTile, a_red);
+            // several iterations per evaluation of the condition, as many as
+            // divide the chunk's iteration budget (the update of the budget's
+            // last iteration clears the condition)
+            const int ci = s->cfg.chunk_iters;
+            const int per_body = ci % 4 == 0 ? std::min(4, kLoopBodyIters)
+                                 : ci % 2 == 0 ? std::min(2, kLoopBodyIters) : 1;
+            for (int u = 0; u < per_body && rc == CLOTH_OK; u++)
+            {
+                rc = add_node(body, &bn, &bl, const_cast<void *>(sv.func), one_wave_spmv,
+                              spmv_block(sv), a_spmv, smem_sv);
+                if (rc == CLOTH_OK)
+                    rc = add_node(body, &bn, &bl, (void *)k_reduce_pq, reduce_grid(n), kTile,
+                                  a_red);
+                if (rc == CLOTH_OK)
+                    rc = add_node(body, &bn, &bl, const_cast<void *>(uv.func), one_wave_upd,
+                                  kTile / uv.rows_per_thread, a_upd);
+                if (rc == CLOTH_OK)
+                    rc = add_node(body, &bn, &bl, (void *)k_reduce_rz, reduce_grid(n), kTile,
+                                  a_red);
+            }
             last = cn;
         }
     }
