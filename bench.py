@@ -775,11 +775,51 @@ def batch_measure(args, ctx) -> dict:
                        "one_per_launch_sample": f"{len(sample)} cloths, stratified by size"}}
 
 
+def batch_iteration_caps(args, ctx) -> dict:
+    """Where the time of a batched step goes: the same 256-cloth step with the
+    PCG capped at N iterations (best of three per cap), and how many cloths
+    still iterate at each cap (from the uncapped solve)."""
+    import torch
+    from acousticsim_gb300 import params
+    confs = batch_confs(args.batch_count)
+    ctx.set_solver("persistent")
+    cloths, states = make_batch(ctx, confs)
+
+    def reset_all():
+        for c, (x, xp) in zip(cloths, states):
+            reset_state(c, x, xp)
+
+    p = params(max_iters=MAX_ITERS, rel_tol=REL_TOL)
+    for _ in range(2):
+        reset_all()
+        st = ctx.batch_step(cloths, 0.0, p)
+    iters = np.array([s["iters"] for s in st])
+    out = {}
+    for cap in [int(v) for v in args.iter_caps.split(",")]:
+        best = 1e30
+        for _ in range(3):
+            reset_all()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            ctx.batch_step(cloths, 0.0, params(max_iters=cap, rel_tol=REL_TOL))
+            best = min(best, time.perf_counter() - t0)
+        out[str(cap)] = {"ms": best * 1e3, "cloths_iterating": int((iters >= cap).sum())}
+    for c in cloths:
+        c.close()
+    return {"metric": "batched step time by PCG iteration cap, 256 cloths 16..128 per side",
+            "max_pcg_iters": int(iters.max()), "mean_pcg_iters": float(iters.mean()),
+            "by_cap": out}
+
+
 def run_batch(args):
     from acousticsim_gb300 import ClothContext
     from acousticsim_gb300 import build as b
     b.build_all()
     ctx = ClothContext(0)
+    if args.iter_caps:
+        print(json.dumps(batch_iteration_caps(args, ctx)), flush=True)
+        ctx.close()
+        return
     r = batch_measure(args, ctx)
     ctx.close()
     print(json.dumps({"value": r["solves_per_s"], "n_gpus": 1, "higher_is_better": True,
@@ -1280,6 +1320,9 @@ def main():
     ap.add_argument("--spmv-variant", default=None,
                     help="profile mode: a fixed graph-loop SpMV variant 'R,U,TPB' (no tuning)")
     ap.add_argument("--batch-count", type=int, default=256)
+    ap.add_argument("--iter-caps", default=None,
+                    help="--mode batch: time the batched step with the PCG capped at each "
+                         "of these iteration counts (comma-separated) instead")
     ap.add_argument("--batch-sample", type=int, default=32,
                     help="cloths timed one at a time for the unbatched comparisons")
     args = ap.parse_args()
