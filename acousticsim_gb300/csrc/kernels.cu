@@ -1505,7 +1505,7 @@ __device__ __forceinline__ BulkRegs bulk_regs(const BulkHdr &h, const unsigned c
 
 // The lower slots' transposed blocks of one row, gathered from global memory
 // (L2) before the stage's p is formed, so that their latency overlaps the
-// halo pass and the upper slots' products: the first PF lower slots.
+// halo pass: the first PF lower slots.
 template <bool SKEW>
 struct BulkLower
 {
@@ -1544,14 +1544,12 @@ __device__ __forceinline__ void bulk_lower_issue(const BulkHdr &h, const unsigne
 // the tile's column range is in the stage (formed there); otherwise
 // p = z + beta p_old is gathered from global memory at each column.  The sum
 // runs in the one order of every SpMV: lower slots in column order, then the
-// diagonal and upper slots; the upper slots' block products are formed first
-// (each product rounds the same wherever it is formed).
+// diagonal and upper slots.
 template <bool SKEW, bool STAGED>
 __device__ __forceinline__ float bulk_row(const BulkRegs &r, int t, int info,
                                           const BulkLower<SKEW> &L)
 {
     constexpr int CH = 4; // lower slots past the prefetched ones: gathers in flight together
-    constexpr int PU = 0; // upper slots whose products are formed ahead (more: spills)
     const unsigned char *__restrict__ stage = r.stage;
     const int row = r.start + t;
     const int len = info & 255, ds = (info >> 8) & 255;
@@ -1572,20 +1570,6 @@ __device__ __forceinline__ float bulk_row(const BulkRegs &r, int t, int info,
     const float2 *__restrict__ a1s = reinterpret_cast<const float2 *>(stage + r.o_a1) + t;
     const float4 *__restrict__ aws = reinterpret_cast<const float4 *>(stage + r.o_aw) + t;
     const int nu = len - ds;
-    // diagonal and upper slots (all staged): products of the first PU
-    float3 su[PU > 0 ? PU : 1], wu_[SKEW && PU > 0 ? PU : 1];
-#pragma unroll
-    for (int k = 0; k < PU; k++)
-        if (k < nu)
-        {
-            const float4 a0 = a0s[k * kTile];
-            const float2 a1 = a1s[k * kTile];
-            const float3 pc = (!STAGED && k == 0) ? pv : pcol(cu[k * kTile]);
-            const float A[6] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y};
-            su[k] = symv(A, pc);
-            if (sk)
-                wu_[SKEW ? k : 0] = skewv(aws[k * kTile], pc);
-        }
     float3 q = make_float3(0.f, 0.f, 0.f);
     // lower slots, column order: the prefetched transposed blocks ...
 #pragma unroll
@@ -1628,21 +1612,18 @@ __device__ __forceinline__ float bulk_row(const BulkRegs &r, int t, int info,
                     q = q - skewv(aw[k], pc[k]);
             }
     }
-    // diagonal and upper slots in slot order
-#pragma unroll
-    for (int k = 0; k < PU; k++)
-        if (k < nu)
-        {
-            q = q + su[k];
-            if (sk)
-                q = q + wu_[SKEW ? k : 0];
-        }
+    // diagonal and upper slots in slot order (all staged), software-pipelined:
+    // the next slot's column is read while this slot's product is formed
+    int cn = nu > 0 ? cu[0] : 0;
 #pragma unroll 1
-    for (int u = PU; u < nu; u++)
+    for (int u = 0; u < nu; u++)
     {
+        const int c = cn;
+        if (u + 1 < nu)
+            cn = cu[(u + 1) * kTile];
         const float4 a0 = a0s[u * kTile];
         const float2 a1 = a1s[u * kTile];
-        const float3 pc = pcol(cu[u * kTile]);
+        const float3 pc = pcol(c);
         const float A[6] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y};
         q = q + symv(A, pc);
         if (sk)
