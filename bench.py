@@ -1034,6 +1034,10 @@ def run_serve(args):
     from acousticsim_gb300 import build as b
     b.build_all()
     ctx = ClothContext(0)
+    if args.spmv_variant:
+        # the server's SpMV fixed (it otherwise takes the context's last tuning)
+        ctx.set_kernel_variant(spmv=tuple(int(v) for v in args.spmv_variant.split(",")),
+                               update=(4, 1), autotune=False)
     r = serve_measure(args, ctx)
     ctx.close()
     print(json.dumps({"value": r["solves_per_s"], "n_gpus": 1, "higher_is_better": True,
@@ -1318,7 +1322,8 @@ def main():
     ap.add_argument("--serve-sample", type=int, default=300,
                     help="prefix of the stream replayed one request per launch")
     ap.add_argument("--spmv-variant", default=None,
-                    help="profile mode: a fixed graph-loop SpMV variant 'R,U,TPB' (no tuning)")
+                    help="profile and serve modes: a fixed graph-loop SpMV variant 'R,U,TPB' "
+                         "(no tuning)")
     ap.add_argument("--batch-count", type=int, default=256)
     ap.add_argument("--iter-caps", default=None,
                     help="--mode batch: time the batched step with the PCG capped at each "
