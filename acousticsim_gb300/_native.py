@@ -144,6 +144,8 @@ SIGNATURES = {
     "cloth_ctx_get_tuning_times": (C.c_int, [P, PF, C.c_int, PF, C.c_int]),
     "cloth_ctx_get_stream": (C.c_int, [P, C.POINTER(P)]),
     "cloth_grid_build": (C.c_int, [C.POINTER(GridDesc), PI, PI, PI, PD, PF, PI, PI]),
+    "cloth_geometry_build": (C.c_int, [C.POINTER(GridDesc), C.c_char_p, C.c_ulonglong, PI, PI,
+                                       PI, PD, PF, PI, PI]),
     "cloth_mesh_from_obj": (C.c_int, [C.c_char_p, PD, C.c_int, PI, PI, PI, PD, PF, PI, PI]),
     "cloth_host_tables": (C.c_int, [C.POINTER(MeshDesc), C.POINTER(Material), PI, PI, PI, PI, PF,
                                     PF, PD, PF, PI]),

@@ -155,19 +155,25 @@ class ClothContext:
 
 
 def build_grid(cloth_size=(1.0, 1.0), subdivision=(19, 19), init_pos=(0.0, 0.0, 0.0),
-               uv_rotation_deg: float = 0.0) -> dict:
-    """cTriangulator::BuildGeometry for "regular_triangle"; arrays in numpy."""
+               uv_rotation_deg: float = 0.0, geometry_type: str = "regular_triangle",
+               seed: int = 0) -> dict:
+    """cTriangulator::BuildGeometry for geometry_type "regular_triangle",
+    "regular_triangle_perturb" or "delaunay" (the last two draw from the
+    reference's generator seeded with `seed`; its main seeds it with 0);
+    arrays in numpy."""
     g = N.GridDesc((C.c_double * 2)(*cloth_size), (C.c_int * 2)(*subdivision),
                    (C.c_double * 3)(*init_pos), float(uv_rotation_deg))
+    gt = str(geometry_type).encode()
     nv, nt, ne = C.c_int(), C.c_int(), C.c_int()
-    N.call("cloth_grid_build", C.byref(g), C.byref(nv), C.byref(nt), C.byref(ne),
-           None, None, None, None)
+    N.call("cloth_geometry_build", C.byref(g), gt, int(seed), C.byref(nv), C.byref(nt),
+           C.byref(ne), None, None, None, None)
     pos = np.zeros((nv.value, 3), np.float64)
     uv = np.zeros((nv.value, 2), np.float32)
     tris = np.zeros((nt.value, 3), np.int32)
     edges = np.zeros((ne.value, 4), np.int32)
-    N.call("cloth_grid_build", C.byref(g), None, None, None, N.ptr(pos, C.c_double),
-           N.ptr(uv, C.c_float), N.ptr(tris, C.c_int), N.ptr(edges, C.c_int))
+    N.call("cloth_geometry_build", C.byref(g), gt, int(seed), None, None, None,
+           N.ptr(pos, C.c_double), N.ptr(uv, C.c_float), N.ptr(tris, C.c_int),
+           N.ptr(edges, C.c_int))
     return {"pos": pos, "uv": uv, "tris": tris, "edges": edges}
 
 
@@ -214,7 +220,9 @@ def _vec(conf: dict, key: str, default=None):
 class BaraffClothGpu:
     """cBaraffClothGpu on the GB300 library.
 
-    conf uses the reference's keys: geometry_type ("regular_triangle"),
+    conf uses the reference's keys: geometry_type ("regular_triangle",
+    "regular_triangle_perturb" or "delaunay"; "rand_seed", default 0, seeds
+    the random ones),
     cloth_size, subdivision, cloth_init_pos, cloth_init_orientation (zero),
     cloth_uv_rotation, cloth_stretch_stiffness, cloth_bending_stiffness,
     cloth_density, rayleigh_damping_a/b, default_timestep and
@@ -237,14 +245,17 @@ class BaraffClothGpu:
                                  bool(conf.get("enable_relocate_obj", False)))
         if mesh is None:
             gt = conf.get("geometry_type", "regular_triangle")
-            if gt != "regular_triangle":
+            if gt not in ("regular_triangle", "regular_triangle_perturb", "delaunay"):
                 raise ValueError(f"geometry_type '{gt}' is not supported")
             orient = conf.get("cloth_init_orientation", [0, 0, 0, 0])
             if any(float(a) != 0.0 for a in orient):
                 raise ValueError("cloth_init_orientation must be zero")
+            # "rand_seed": the state of the reference's generator the random
+            # geometries draw from (its main seeds it with 0)
             mesh = build_grid(tuple(_vec(conf, "cloth_size")), tuple(int(s) for s in _vec(conf, "subdivision")),
                               tuple(_vec(conf, "cloth_init_pos", [0, 0, 0])[:3]),
-                              float(conf.get("cloth_uv_rotation", 0)))
+                              float(conf.get("cloth_uv_rotation", 0)), gt,
+                              int(conf.get("rand_seed", 0)))
         self.mesh = {k: np.ascontiguousarray(v) for k, v in mesh.items()}
         pos = np.ascontiguousarray(self.mesh["pos"], np.float64)
         uv = np.ascontiguousarray(self.mesh["uv"], np.float32)

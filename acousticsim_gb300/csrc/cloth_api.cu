@@ -1964,6 +1964,36 @@ int cloth_grid_build(const cloth_grid_desc *grid, int *nv, int *nt, int *ne,
     return CLOTH_OK;
 }
 
+int cloth_geometry_build(const cloth_grid_desc *grid, const char *geometry_type,
+                         unsigned long long seed, int *nv, int *nt, int *ne, double *pos,
+                         float *uv, int *tris, int *edges)
+{
+    if (!grid || !geometry_type)
+        return fail(CLOTH_ERR_INVALID, "cloth_geometry_build: NULL argument");
+    GridDesc g;
+    std::memcpy(g.size, grid->cloth_size, sizeof(g.size));
+    std::memcpy(g.subdiv, grid->subdivision, sizeof(g.subdiv));
+    std::memcpy(g.init_pos, grid->init_pos, sizeof(g.init_pos));
+    g.uv_rotation_deg = grid->uv_rotation_deg;
+    const std::string type(geometry_type);
+    Mesh m;
+    std::string err;
+    bool ok;
+    if (type == "regular_triangle")
+        ok = build_grid(g, m, err);
+    else if (type == "regular_triangle_perturb")
+        ok = perturb_grid(g, seed, m, err);
+    else if (type == "delaunay")
+        ok = delaunay_cloth(g, seed, m, err);
+    else
+        return fail(CLOTH_ERR_UNSUPPORTED, "cloth_geometry_build: unknown geometry_type '" +
+                                               type + "'");
+    if (!ok)
+        return fail(CLOTH_ERR_INVALID, err);
+    copy_out_mesh(m, nv, nt, ne, pos, uv, tris, edges);
+    return CLOTH_OK;
+}
+
 static bool copy_mesh(const cloth_mesh_desc *mesh, Mesh &m, std::string &err)
 {
     if (!mesh || mesh->nv <= 0 || mesh->nt <= 0 || !mesh->pos || !mesh->uv ||

@@ -75,6 +75,12 @@ struct Tables
 // RotateMaterialCoordsAfterReset (src/geometries/Triangulator.cpp:32-457, 621-658).
 bool build_grid(const GridDesc &g, Mesh &m, std::string &err);
 
+// "regular_triangle_perturb" and "delaunay" of cTriangulator::BuildGeometry
+// (Triangulator.cpp:100-110) with the reference's generator seeded with
+// `seed` right before the build.  geometry.cpp.
+bool perturb_grid(const GridDesc &g, unsigned long long seed, Mesh &m, std::string &err);
+bool delaunay_cloth(const GridDesc &g, unsigned long long seed, Mesh &m, std::string &err);
+
 // Edge list from triangles when the caller gives none, as cObjUtil::BuildEdge
 // numbers it: one edge per vertex pair (v0 < v1) in ascending pair order;
 // tri0/tri1 are the first/second triangle that uses the pair.  Fails on edges

@@ -199,6 +199,21 @@ int cloth_ctx_get_stream(cloth_ctx *ctx, void **stream);
  * tri0, tri1); boundary edges have tri1 = -1. */
 int cloth_grid_build(const cloth_grid_desc *grid, int *nv, int *nt, int *ne,
                      double *pos, float *uv, int *tris, int *edges);
+/* cTriangulator::BuildGeometry (Triangulator.cpp:32-139) for geometry_type
+ * "regular_triangle", "regular_triangle_perturb" (the grid with its interior
+ * vertices jittered by up to a fifth of an edge, BuildRectVertices :395-457) or
+ * "delaunay" (subdivision[0] * subdivision[1] points: the rectangle boundary,
+ * then random points farther apart than sqrt(area / (n pi)), Delaunay-
+ * triangulated counter-clockwise; TriangulatorDelaunay.cpp:41-216).  The two
+ * random geometries draw from the reference's generator (std::default_random_
+ * engine, uniform doubles) seeded with `seed` (the reference's main seeds it
+ * with 0), so the points match the reference's bit for bit; the Delaunay
+ * triangles are the same set, in this library's order (edges numbered by first
+ * appearance over them).  Sizes and fill as cloth_grid_build; an unknown type
+ * is CLOTH_ERR_UNSUPPORTED. */
+int cloth_geometry_build(const cloth_grid_desc *grid, const char *geometry_type,
+                         unsigned long long seed, int *nv, int *nt, int *ne, double *pos,
+                         float *uv, int *tris, int *edges);
 
 /* A cloth mesh from an OBJ file, as cBaseCloth::InitGeometry builds it with
  * "enable_cloth_from_obj": true (src/sim/cloth/BaseCloth.cpp:292-356 over

@@ -9,6 +9,8 @@
 //   collide <cfg.json> <body.json> <x.bin> <dx.bin> <outdir>
 //                                                  contacts with one kinematic body,
 //                                                  contact Hessian, Repulsion
+//   geom   <cfg.json> <seed> <outdir>              cTriangulator::BuildGeometry right
+//                                                  after cMathUtil::SeedRand(seed)
 //
 // Where the reference's GPU host code (src/sim/cloth/BaraffClothGpu.cpp) cannot
 // be compiled (it pulls in MSVC-only CUDA headers), the few lines of its init
@@ -16,6 +18,8 @@
 // (CalcBaraffStretchCoef, CalcCotangentCoeff, cRotUtil::RotMat2D), each with
 // the file:line it follows.  Blocks are written row-major: (i,j) -> [3*i+j].
 #include "geometries/Primitives.h"
+#include "geometries/Triangulator.h"
+#include "utils/MathUtil.h"
 #include "sim/cloth/BaraffCloth.h"
 #include "sim/cloth/BaraffMaterial.h"
 #include "sim/cloth/DihedralBending.h"
@@ -701,6 +705,46 @@ int main(int argc, char **argv)
     Json::Value conf;
     if (!cJsonUtil::LoadJson(argv[2], conf))
         return 1;
+    if (mode == "geom" && argc >= 5)
+    {
+        // the geometry generators that draw from the global generator
+        // ("regular_triangle_perturb", "delaunay"); main seeds it with 0
+        cMathUtil::SeedRand(std::strtoul(argv[3], nullptr, 10));
+        std::vector<tVertexPtr> va;
+        std::vector<tEdgePtr> ea;
+        std::vector<tTrianglePtr> ta;
+        cTriangulator::BuildGeometry(conf, va, ea, ta);
+        const long n = long(va.size()), T = long(ta.size()), E = long(ea.size());
+        std::vector<double> pos(size_t(n) * 3);
+        std::vector<float> uv(size_t(n) * 2);
+        std::vector<int> tris(size_t(T) * 3), edges(size_t(E) * 5);
+        for (long i = 0; i < n; i++)
+        {
+            for (int k = 0; k < 3; k++)
+                pos[size_t(i) * 3 + k] = va[i]->mPos[k];
+            uv[size_t(i) * 2 + 0] = va[i]->muv[0];
+            uv[size_t(i) * 2 + 1] = va[i]->muv[1];
+        }
+        for (long t = 0; t < T; t++)
+        {
+            tris[size_t(t) * 3 + 0] = ta[t]->mId0;
+            tris[size_t(t) * 3 + 1] = ta[t]->mId1;
+            tris[size_t(t) * 3 + 2] = ta[t]->mId2;
+        }
+        for (long e = 0; e < E; e++)
+        {
+            int row[5] = {ea[e]->mId0, ea[e]->mId1, ea[e]->mTriangleId0, ea[e]->mTriangleId1,
+                          ea[e]->mIsBoundary ? 1 : 0};
+            for (int k = 0; k < 5; k++)
+                edges[size_t(e) * 5 + k] = row[k];
+        }
+        Dump d(argv[4]);
+        d.put("pos", "f8", pos, {n, 3});
+        d.put("uv", "f4", uv, {n, 2});
+        d.put("tris", "i4", tris, {T, 3});
+        d.put("edges", "i4", edges, {E, 5});
+        return 0;
+    }
     auto c = std::make_shared<Probe>(0);
     c->conf = conf;
     c->Init(conf);

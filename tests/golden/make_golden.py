@@ -173,6 +173,25 @@ MOTION_CASES = [
 ]
 
 
+# The geometry generators that draw from the reference's global generator,
+# right after cMathUtil::SeedRand(seed): (case, config, seed), all written to
+# geometry.npz.
+GEOM_CASES = [
+    ("perturb_13x17", {"geometry_type": "regular_triangle_perturb", "cloth_size": [1.2, 0.9],
+                       "subdivision": [13, 17], "cloth_init_pos": [0.1, 0.2, 0.3],
+                       "cloth_init_orientation": [0, 0, 0], "cloth_uv_rotation": 45}, 0),
+    ("perturb_20x20", {"geometry_type": "regular_triangle_perturb", "cloth_size": [1.0, 1.0],
+                       "subdivision": [19, 19], "cloth_init_pos": [0, 0, 0],
+                       "cloth_init_orientation": [0, 0, 0], "cloth_uv_rotation": 0}, 7),
+    ("delaunay_25x31", {"geometry_type": "delaunay", "cloth_size": [0.7, 1.3],
+                        "subdivision": [25, 31], "cloth_init_pos": [0.1, -0.2, 0.05],
+                        "cloth_init_orientation": [0, 0, 0], "cloth_uv_rotation": 90}, 3),
+    ("delaunay_20x20", {"geometry_type": "delaunay", "cloth_size": [1.0, 1.0],
+                        "subdivision": [20, 20], "cloth_init_pos": [0, 0, 0],
+                        "cloth_init_orientation": [0, 0, 0], "cloth_uv_rotation": 0}, 0),
+]
+
+
 def contact_patch(path: Path, n: int = 12) -> None:
     """A curved n x n patch over x, y in [-0.35, 0.3] x [-0.25, 0.35] at
     z = 1.5 mm + 0.04 r^2, triangle normals facing -z."""
@@ -276,6 +295,25 @@ def main() -> None:
         np.savez_compressed(OUT / f"{name}.npz", **arrays)
         print(name, "contacts pt", cold["pt_i"].shape[0], "ee", cold["ee_i"].shape[0], "->",
               OUT / f"{name}.npz")
+    geom = {}
+    for name, conf, seed in GEOM_CASES:
+        if a.only and name not in a.only and "geometry" not in a.only:
+            continue
+        with tempfile.TemporaryDirectory() as td:
+            td = Path(td)
+            (td / "cfg.json").write_text(json.dumps(conf))
+            (td / "g").mkdir()
+            subprocess.run([str(harness), "geom", str(td / "cfg.json"), str(seed), str(td / "g")],
+                           check=True, stdout=subprocess.DEVNULL)
+            gd = read_dump(td / "g")
+        for k, v in gd.items():
+            geom[f"{name}_{k}"] = v
+        geom[f"{name}_config_json"] = np.frombuffer(json.dumps(conf).encode(), np.uint8)
+        geom[f"{name}_seed"] = np.array(seed, np.int64)
+        print(name, "nv", gd["pos"].shape[0], "nt", gd["tris"].shape[0])
+    if geom:
+        np.savez_compressed(OUT / "geometry.npz", **geom)
+        print("->", OUT / "geometry.npz")
     for name, kb, dt, steps in MOTION_CASES:
         if a.only and name not in a.only:
             continue

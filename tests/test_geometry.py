@@ -1,0 +1,118 @@
+"""The random cloth geometries of cTriangulator::BuildGeometry
+("regular_triangle_perturb", "delaunay"; src/geometries/Triangulator.cpp:100-110,
+TriangulatorDelaunay.cpp) against the reference's own generators
+(tests/golden/geometry.npz, written by oracle/ref_harness's geom mode right
+after cMathUtil::SeedRand(seed)).  Host code only: no GPU."""
+from __future__ import annotations
+
+import json
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+
+CASES = ["perturb_13x17", "perturb_20x20", "delaunay_25x31", "delaunay_20x20"]
+
+
+@pytest.fixture(scope="module")
+def golden():
+    return np.load(GOLDEN / "geometry.npz")
+
+
+def _build(g, case):
+    from acousticsim_gb300 import build_grid
+    conf = json.loads(bytes(g[f"{case}_config_json"]).decode())
+    return conf, build_grid(tuple(conf["cloth_size"]), tuple(conf["subdivision"]),
+                            tuple(conf["cloth_init_pos"]), float(conf["cloth_uv_rotation"]),
+                            conf["geometry_type"], int(g[f"{case}_seed"]))
+
+
+def _orient(pos, tris):
+    a, b, c = (pos[tris[:, k], :2] for k in range(3))
+    return (b[:, 0] - a[:, 0]) * (c[:, 1] - a[:, 1]) - (b[:, 1] - a[:, 1]) * (c[:, 0] - a[:, 0])
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_points_match_reference(built, golden, case):
+    """The generator's draws (after SeedRand's own), the boundary points, the
+    rejection of close points, the init translation and the material
+    coordinates: bit for bit."""
+    _, m = _build(golden, case)
+    assert np.array_equal(m["pos"], golden[f"{case}_pos"])
+    assert np.array_equal(m["uv"], golden[f"{case}_uv"])
+
+
+@pytest.mark.parametrize("case", [c for c in CASES if c.startswith("perturb")])
+def test_perturbed_grid_topology_matches_reference(built, golden, case):
+    from acousticsim_gb300 import build_grid
+    conf, m = _build(golden, case)
+    assert np.array_equal(m["tris"], golden[f"{case}_tris"])
+    assert np.array_equal(m["edges"], golden[f"{case}_edges"][:, :4])
+    # interior vertices moved by at most a fifth of an edge, the rim not at all
+    flat = build_grid(tuple(conf["cloth_size"]), tuple(conf["subdivision"]),
+                      tuple(conf["cloth_init_pos"]), float(conf["cloth_uv_rotation"]))
+    d = np.abs(m["pos"] - flat["pos"])
+    hd, wd = conf["subdivision"]
+    uh, uw = conf["cloth_size"][0] / hd, conf["cloth_size"][1] / wd
+    assert (d[:, 0] <= uw / 5).all() and (d[:, 1] <= uh / 5).all() and (d[:, 2] == 0).all()
+    assert (d.sum(axis=1) > 0).sum() > 0.5 * len(d)
+
+
+@pytest.mark.parametrize("case", [c for c in CASES if c.startswith("delaunay")])
+def test_delaunay_triangles_match_reference(built, golden, case):
+    """The same triangle set as the reference's triangulation, every triangle
+    counter-clockwise in x, y (as the reference turns them), the empty-
+    circumcircle property, and edges numbered by first appearance over the
+    triangles with their two triangles."""
+    _, m = _build(golden, case)
+    ref_t = golden[f"{case}_tris"]
+    canon = lambda t: sorted(tuple(sorted(r)) for r in t.tolist())
+    assert canon(m["tris"]) == canon(ref_t)
+    pos = m["pos"]
+    assert (_orient(pos, m["tris"]) > 0).all()
+    assert (_orient(golden[f"{case}_pos"], ref_t) > 0).all()
+    # empty circumcircles (a sample of triangles against every vertex)
+    xy = pos[:, :2]
+    for t in m["tris"][:: max(1, len(m["tris"]) // 60)]:
+        a, b, c = xy[t]
+        d = xy
+        ax, ay = a[0] - d[:, 0], a[1] - d[:, 1]
+        bx, by = b[0] - d[:, 0], b[1] - d[:, 1]
+        cx, cy = c[0] - d[:, 0], c[1] - d[:, 1]
+        det = ((ax * ax + ay * ay) * (bx * cy - cx * by) + (bx * bx + by * by) * (cx * ay - ax * cy)
+               + (cx * cx + cy * cy) * (ax * by - bx * ay))
+        others = np.setdiff1d(np.arange(len(xy)), t)
+        assert (det[others] <= 1e-12).all()
+    # edges: first appearance order over (v0 v1, v1 v2, v2 v0) of each triangle
+    seen, order = {}, []
+    for ti, t in enumerate(m["tris"].tolist()):
+        for k in range(3):
+            key = tuple(sorted((t[k], t[(k + 1) % 3])))
+            if key not in seen:
+                seen[key] = [ti, -1]
+                order.append(key)
+            else:
+                seen[key][1] = ti
+    exp = np.array([[k[0], k[1], *seen[k]] for k in order], np.int32)
+    assert np.array_equal(m["edges"], exp)
+    assert len(m["edges"]) == len(golden[f"{case}_edges"])
+    ref_bnd = int((golden[f"{case}_edges"][:, 4] == 1).sum())
+    assert int((m["edges"][:, 3] == -1).sum()) == ref_bnd
+
+
+def test_seed_changes_points_and_refusals(built, golden):
+    from acousticsim_gb300 import ClothError, build_grid
+    # (the reference's engine, minstd_rand0, takes seed 0 as 1: seeds 0 and 1
+    # give the same stream)
+    a = build_grid((1.0, 1.0), (12, 12), geometry_type="delaunay", seed=0)
+    b = build_grid((1.0, 1.0), (12, 12), geometry_type="delaunay", seed=2)
+    assert not np.array_equal(a["pos"], b["pos"])
+    c = build_grid((1.0, 1.0), (12, 12), geometry_type="delaunay", seed=0)
+    assert np.array_equal(a["pos"], c["pos"]) and np.array_equal(a["tris"], c["tris"])
+    with pytest.raises(ClothError):
+        build_grid((1.0, 1.0), (12, 12), geometry_type="single_triangle")
+    with pytest.raises(ClothError):
+        build_grid((1.0, 1.0), (1, 2), geometry_type="delaunay")
+    with pytest.raises(ClothError):
+        build_grid((1.0, 1.0), (12, 12), uv_rotation_deg=30.0, geometry_type="delaunay")

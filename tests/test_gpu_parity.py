@@ -165,6 +165,32 @@ def test_multi_step_trajectory_vs_oracle(ctx, orc, solver):
     c.close()
 
 
+@pytest.mark.parametrize("geometry", ["regular_triangle_perturb", "delaunay"])
+def test_random_geometry_trajectory_vs_oracle(ctx, orc, geometry):
+    """The reference's random cloth geometries (a 40x40 perturbed grid, a
+    1,521-point Delaunay cloth; their points pinned to the reference's by
+    tests/test_geometry.py): ten steps against the FP64 oracle stepping the
+    same mesh and state."""
+    from acousticsim_gb300 import params
+    n, dt = 40, 2e-3
+    conf = dict(_grid_conf(n, dt), geometry_type=geometry, rand_seed=0)
+    c = make(ctx, conf)
+    assert c.mesh["pos"].shape[0] == (n * n if geometry != "delaunay" else (n - 1) ** 2)
+    x, xp = _perturbed(c, 11, dt)
+    c.SetPos(x)
+    c.SetPrePos(xp)
+    oc = orc.OracleCloth(c.mesh, conf, c.GetConstraintStaticVertices())
+    oc.x, oc.xpre = x.copy(), xp.copy()
+    for _ in range(10):
+        st = c.UpdatePos(0.0, params(max_iters=20000, rel_tol=1e-7))
+        assert st["status"] == "OK", st
+        oc.step(rel_tol=1e-12)
+    disp_err = rel(c.GetPos() - x, oc.x - x)
+    print(geometry, "displacement error after 10 steps", disp_err)
+    assert disp_err < 2e-4
+    c.close()
+
+
 def test_batch_equals_alone_bit_exact(ctx, solver):
     """Each cloth's result in a mixed batch is bit-identical to stepping it alone."""
     from acousticsim_gb300 import params
