@@ -165,6 +165,36 @@ def test_multi_step_trajectory_vs_oracle(ctx, orc, solver):
     c.close()
 
 
+@pytest.mark.parametrize("n", [20, 64])
+def test_hundred_step_trajectory_vs_oracle(ctx, orc, n):
+    """100 steps of the 20x20 and 64x64 cloths (pinned corners, the benchmark's
+    materials and perturbation) against the FP64 oracle stepping the same
+    states: the displacement after 1 and after 100 steps."""
+    from acousticsim_gb300 import params
+    dt = 2e-3
+    conf = _grid_conf(n, dt)
+    c = make(ctx, conf)
+    x, xp = _perturbed(c, 23, dt)
+    c.SetPos(x)
+    c.SetPrePos(xp)
+    oc = orc.OracleCloth(c.mesh, conf, c.GetConstraintStaticVertices())
+    oc.x, oc.xpre = x.copy(), xp.copy()
+    errs = []
+    for k in range(100):
+        st = c.UpdatePos(0.0, params(max_iters=20000, rel_tol=1e-7))
+        assert st["status"] == "OK", (k, st)
+        oc.step(rel_tol=1e-12)
+        if k in (0, 99):
+            errs.append(rel(c.GetPos() - x, oc.x - x))
+    print(n, "displacement error after 1 and 100 steps", errs)
+    # ~5x the measured errors (20: 3.9e-6, 1.8e-5; 64: 2.1e-4, 6.7e-4): the GPU
+    # solves to 1e-7, the oracle to 1e-12, and the larger cloth's system is
+    # worse conditioned
+    tol1, tol100 = {20: (2e-5, 1e-4), 64: (1e-3, 3.5e-3)}[n]
+    assert errs[0] < tol1 and errs[1] < tol100
+    c.close()
+
+
 @pytest.mark.parametrize("geometry", ["regular_triangle_perturb", "delaunay"])
 def test_random_geometry_trajectory_vs_oracle(ctx, orc, geometry):
     """The reference's random cloth geometries (a 40x40 perturbed grid, a
