@@ -135,6 +135,7 @@ SIGNATURES = {
     "cloth_ctx_get_profile": (C.c_int, [P, PD, C.POINTER(C.c_longlong)]),
     "cloth_ctx_reset_profile": (C.c_int, [P]),
     "cloth_ctx_set_solver": (C.c_int, [P, C.c_int]),
+    "cloth_ctx_set_tail_hand_off": (C.c_int, [P, C.c_int]),
     "cloth_ctx_set_spin_limit": (C.c_int, [P, C.c_uint, C.c_uint]),
     "cloth_ctx_set_escalation": (C.c_int, [P, C.c_int]),
     "cloth_ctx_device_bytes": (C.c_int, [P, C.POINTER(C.c_size_t)]),

@@ -74,6 +74,12 @@ class ClothContext:
                 "persistent_2b": N.SOLVER_PERSISTENT_2B}[solver]
         N.call("cloth_ctx_set_solver", self._h, code)
 
+    def set_tail_hand_off(self, max_instances: int = -1) -> None:
+        """Graph-loop launch sets hand their last `max_instances` iterating
+        cloths to the persistent kernel (same results bit for bit; -1: the SM
+        count / 4, 0: never).  For launch sets built after the call."""
+        N.call("cloth_ctx_set_tail_hand_off", self._h, int(max_instances))
+
     def set_spin_limit(self, polls: int = 0, extra_arrivals: int = 0) -> None:
         """Bounded team-barrier waits of the persistent solvers: give up after
         `polls` polls (0: the default) with status TIMEOUT.  `extra_arrivals`

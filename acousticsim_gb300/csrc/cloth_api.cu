@@ -1,6 +1,7 @@
 // C ABI of the GB300 implicit cloth step: contexts, cloth instances, the
 // step driver (one CUDA graph per launch set, PCG as a device-side while loop),
 // batches and exports.  Declarations and reference mapping: include/cloth_gb300.h.
+#include <map>
 #include "internal.h"
 
 #include <algorithm>
@@ -132,6 +133,11 @@ struct Batch
     int halo_cap = 0, rows_cap = 0;
     size_t smem_persist = 0;
     SpinCfg spin = {kSpinLimitDefault, 0u}; // the context's setting when the set was built
+    // graph loop: the active count at which the loop stops and the persistent
+    // kernel finishes the rest (0: the loop runs to the end), and the launch
+    // sets of those rests, by member indices
+    int hand_off = 0;
+    std::map<std::vector<int>, std::unique_ptr<Batch>> tails;
     cudaGraphExec_t step_exec = nullptr;
     cudaGraphExec_t solve_exec = nullptr;
     ~Batch()
@@ -774,7 +780,7 @@ int make_batch(cloth_ctx *ctx, const std::vector<cloth_s *> &members,
     b->d_rt = reinterpret_cast<Tile *>(b->mem + o_rt);
     b->d_tt = reinterpret_cast<Tile *>(b->mem + o_tt);
     b->d_ctl = reinterpret_cast<BatchCtl *>(b->mem + o_c);
-    BatchCtl ctl = {0, b->n_rt, b->n_tt, 0};
+    BatchCtl ctl = {0, b->n_rt, b->n_tt, 0, 0, {0, 0, 0}};
     CK(cudaMemcpy(b->d_descs, descs.data(), descs.size() * sizeof(InstDesc *),
                   cudaMemcpyHostToDevice));
     CK(cudaMemcpy(b->d_inst, inst.data(), inst.size() * sizeof(int),
@@ -792,6 +798,17 @@ int make_batch(cloth_ctx *ctx, const std::vector<cloth_s *> &members,
     int rc = plan_persistent(ctx, b.get());
     if (rc != CLOTH_OK)
         return rc;
+    // a graph-loop set whose drivers agree bit for bit (the persistent solver,
+    // two barriers) hands its last few iterating cloths to the persistent
+    // kernel: the graph loop's iterations cost about the same however few
+    // cloths remain
+    const int ho = ctx->tail_hand_off < 0 ? ctx->num_sms / 4 : ctx->tail_hand_off;
+    if (!b->persist_ok && !b->collide && ho > 0 && int(members.size()) > ho &&
+        (ctx->solver == CLOTH_SOLVER_PERSISTENT || ctx->solver == CLOTH_SOLVER_PERSISTENT_2B))
+    {
+        b->hand_off = ho;
+        CK(cudaMemcpy(&b->d_ctl->hand_off, &ho, sizeof(int), cudaMemcpyHostToDevice));
+    }
     out = std::move(b);
     return CLOTH_OK;
 }
@@ -1143,7 +1160,8 @@ int build_graph(Batch *b, bool full, cudaGraphExec_t *exec)
             last = cn;
         }
     }
-    if (full)
+    // (a set that hands its last cloths over advances after they finish)
+    if (full && b->hand_off == 0)
         chain((void *)k_advance, b->grid_row, a_adv);
     if (rc == CLOTH_OK && cudaGraphInstantiate(exec, g, 0) != cudaSuccess)
         rc = fail(CLOTH_ERR_CUDA, "cudaGraphInstantiate failed");
@@ -1360,10 +1378,11 @@ void end_step(const std::vector<cloth_s *> &members)
 
 // Autotuner of the graph-loop kernels: right after the assembly of a launch
 // set's first step (PCG at iteration 0) every SpMV variant is timed on the
-// real data - at iteration 0 the SpMV is idempotent (p = z, q = A z, alpha) -
-// and every update variant is timed from a snapshot of the state it changes
-// (dx, r, z, the instance scalars, the active count), restored after each
-// run. All variants compute bit-identical results, so the choice only moves
+// real data - at iteration 0 the SpMV writes p = z and q = A z, the same every
+// time, and adds its tile sums to the instance states, restored before each
+// run - and every update variant is timed from a snapshot of the state it
+// changes (dx, r, z, the instance states, the active count), restored after
+// each run; the loop then starts from the states before the first SpMV. All variants compute bit-identical results, so the choice only moves
 // the time. The fastest pair is kept for the launch set and becomes the
 // context's default (the request server builds its chunks with it).
 int autotune_graph_loop(Batch *b)
@@ -1372,11 +1391,13 @@ int autotune_graph_loop(Batch *b)
     cudaStream_t s = ctx->stream;
     const int ninst = int(b->members.size());
     float4 *rows = nullptr;
-    InstState *sts = nullptr;
-    BatchCtl *ctl_buf = nullptr;
+    InstState *sts = nullptr, *sts0 = nullptr;
+    BatchCtl *ctl_buf = nullptr, *ctl0 = nullptr;
     CK(cudaMalloc(&rows, size_t(b->n_rt) * kTile * 3 * sizeof(float4)));
     CK(cudaMalloc(&sts, size_t(ninst) * sizeof(InstState)));
+    CK(cudaMalloc(&sts0, size_t(ninst) * sizeof(InstState)));
     CK(cudaMalloc(&ctl_buf, sizeof(BatchCtl)));
+    CK(cudaMalloc(&ctl0, sizeof(BatchCtl)));
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
@@ -1391,6 +1412,13 @@ int autotune_graph_loop(Batch *b)
         k_snap_state<<<std::max(1, std::min(ninst, 1024)), 64, 0, s>>>(
             b->d_descs, b->d_inst, ninst, sts, b->d_ctl, ctl_buf, restore);
     };
+    // the instance states before the first SpMV (the SpMV adds its tile sums
+    // to them, so every timed run starts from this copy)
+    auto snap0 = [&](int restore) {
+        k_snap_state<<<std::max(1, std::min(ninst, 1024)), 64, 0, s>>>(
+            b->d_descs, b->d_inst, ninst, sts0, b->d_ctl, ctl0, restore);
+    };
+    snap0(0);
     auto time_launch = [&](const GraphLoopVariant &v, int grid, void **args,
                            unsigned smem = 0) -> float {
         cudaEventRecord(e0, s);
@@ -1421,6 +1449,7 @@ int autotune_graph_loop(Batch *b)
             float t = 1e30f;
             for (int rep = 0; rep < 4; rep++)
             {
+                snap0(1);
                 const float ms = time_launch(b->spmv_variant(v), g, a_spmv, b->spmv_smem_of(v));
                 if (rep > 0)
                     t = std::min(t, ms);
@@ -1435,7 +1464,8 @@ int autotune_graph_loop(Batch *b)
         }
         ctx->tune_ms_spmv[v] = tv;
     }
-    // leave the state of iteration 0 with alpha set, as the loop expects it
+    // the update variants run from the state after the first SpMV and p.q
+    snap0(1);
     cudaLaunchKernel(b->spmv_variant(best_s).func,
                      dim3(b->grid_for(b->spmv_variant(best_s), b->spmv_occ(best_s), best_sw)),
                      dim3(spmv_block(b->spmv_variant(best_s))), a_spmv,
@@ -1473,13 +1503,18 @@ int autotune_graph_loop(Batch *b)
         }
         ctx->tune_ms_update[v] = tv;
     }
+    // back to the state the loop starts from: the rows the SpMV leaves as they
+    // are, the instance states before it
     snap(1);
+    snap0(1);
     cudaError_t err = cudaStreamSynchronize(s);
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     cudaFree(rows);
     cudaFree(sts);
+    cudaFree(sts0);
     cudaFree(ctl_buf);
+    cudaFree(ctl0);
     if (err != cudaSuccess)
         return fail(CLOTH_ERR_CUDA, std::string("autotune: ") + cudaGetErrorString(err));
     b->set_variants(best_s, best_u, best_sw, best_uw);
@@ -1487,6 +1522,54 @@ int autotune_graph_loop(Batch *b)
     ctx->tune_spmv = best_s;
     ctx->tune_update = best_u;
     return CLOTH_OK;
+}
+
+// The end of a hand-off set's solve: the graph loop stopped once
+// b->hand_off cloths or fewer still iterated; the persistent kernel (whose
+// arithmetic is the graph loop's, bit for bit) finishes them from where they
+// are.  Where those cloths do not fit one persistent launch, the graph loop
+// runs on to the end instead.
+int finish_tail(Batch *b)
+{
+    cloth_ctx *ctx = b->ctx;
+    cudaStream_t s = ctx->stream;
+    const int n = int(b->members.size());
+    InstState *h_st = reinterpret_cast<InstState *>(b->h_pinned);
+    k_snap_state<<<std::min(n, 1024), 64, 0, s>>>(b->d_descs, b->d_inst, n, b->d_states,
+                                                   b->d_ctl, b->d_ctl_copy, 0);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(h_st, b->d_states, n * sizeof(InstState), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    std::vector<int> rest;
+    for (int i = 0; i < n; i++)
+        if (h_st[i].active)
+            rest.push_back(i);
+    if (rest.empty())
+        return CLOTH_OK;
+    std::unique_ptr<Batch> &tb = b->tails[rest];
+    if (!tb)
+    {
+        std::vector<cloth_s *> sub;
+        for (int i : rest)
+            sub.push_back(b->members[size_t(i)]);
+        int rc = make_batch(ctx, sub, tb);
+        if (rc != CLOTH_OK)
+            return rc;
+    }
+    if (tb->persist_ok && !tb->persist_1b)
+        return launch_persistent(tb.get());
+    // the loop to the end
+    const int zero = 0;
+    CK(cudaMemcpyAsync(&b->d_ctl->hand_off, &zero, sizeof(int), cudaMemcpyHostToDevice, s));
+    int rc = CLOTH_OK;
+    if (!b->solve_exec)
+        rc = build_graph(b, false, &b->solve_exec);
+    if (rc == CLOTH_OK && cudaGraphLaunch(b->solve_exec, s) != cudaSuccess)
+        rc = fail(CLOTH_ERR_CUDA, "cudaGraphLaunch failed");
+    CK(cudaMemcpyAsync(&b->d_ctl->hand_off, &b->hand_off, sizeof(int), cudaMemcpyHostToDevice,
+                       s));
+    CK(cudaStreamSynchronize(s));
+    return rc;
 }
 
 int run_step(Batch *b, double dt, const cloth_solve_params *params,
@@ -1537,6 +1620,8 @@ int run_step(Batch *b, double dt, const cloth_solve_params *params,
             rc = build_graph(b, false, &b->solve_exec);
         if (rc == CLOTH_OK && cudaGraphLaunch(b->solve_exec, ctx->stream) != cudaSuccess)
             rc = fail(CLOTH_ERR_CUDA, "cudaGraphLaunch failed");
+        if (rc == CLOTH_OK && b->hand_off > 0)
+            rc = finish_tail(b);
         if (rc == CLOTH_OK)
             rc = launch_advance(b);
     }
@@ -1549,6 +1634,13 @@ int run_step(Batch *b, double dt, const cloth_solve_params *params,
                 return rc;
         }
         CK(cudaGraphLaunch(b->step_exec, ctx->stream));
+        // (a hand-off set's graph ends with the loop)
+        if (b->hand_off > 0)
+        {
+            rc = finish_tail(b);
+            if (rc == CLOTH_OK)
+                rc = launch_advance(b);
+        }
     }
     if (rc != CLOTH_OK)
         return rc;
@@ -1795,6 +1887,16 @@ int cloth_ctx_reset_profile(cloth_ctx *ctx)
         ctx->prof_ms[k] = 0;
         ctx->prof_n[k] = 0;
     }
+    return CLOTH_OK;
+}
+
+int cloth_ctx_set_tail_hand_off(cloth_ctx *ctx, int max_instances)
+{
+    if (!ctx || max_instances < -1)
+        return fail(CLOTH_ERR_INVALID, "cloth_ctx_set_tail_hand_off: bad argument");
+    std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+    ctx->tail_hand_off = max_instances;
+    ctx->last_batch.reset();
     return CLOTH_OK;
 }
 

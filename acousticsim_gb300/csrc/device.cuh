@@ -276,6 +276,9 @@ struct BatchCtl
     int n_tiles_rows;
     int n_tiles_tris;
     int err;         // a bounded wait of the graph-loop kernels gave up (sticky until read)
+    int hand_off;    // the graph loop ends once this many instances or fewer iterate
+                     // (the host finishes them with the persistent kernel); 0: to the end
+    int pad[3];
 };
 
 } // namespace cloth

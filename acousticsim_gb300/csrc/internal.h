@@ -31,7 +31,8 @@ __global__ void k_reduce_pq(InstDesc *const *descs, const int *inst_list, int ni
 __global__ void k_reduce_rz(InstDesc *const *descs, const int *inst_list, int ninst,
                             const int *ninst_dev, BatchCtl *ctl, int use_cond,
                             cudaGraphConditionalHandle h);
-inline int reduce_grid(int ninst) { return ninst < 1 ? 1 : (ninst > 1024 ? 1024 : ninst); }
+// one thread per instance, blocks of kTile threads
+inline int reduce_grid(int ninst) { return ninst < 1 ? 1 : (ninst + 127) / 128; }
 // graph-loop kernel variants (k_spmv_t<R, U>, k_update_t<R>); arguments:
 //   spmv  (descs, tiles, ctl, use_cond, handle)
 //   update(descs, tiles, ctl, use_cond, handle, iters_left)
@@ -143,6 +144,9 @@ struct cloth_ctx_s
     // extra arrivals are the timeout test's hook, 0 otherwise)
     cloth::SpinCfg spin = {cloth::kSpinLimitDefault, 0u};
     int solver = 0; // 0: persistent cooperative PCG when the set fits, 1: graph loop
+    // graph-loop launch sets of more cloths than this hand their last this-many
+    // iterating cloths to the persistent kernel (-1: num_sms / 4; 0: never)
+    int tail_hand_off = -1;
     bool escalate = true; // FP32 PCG ending in NaN / breakdown: re-solve the step in FP64
     bool prof = false;
     double prof_ms[CLOTH_NUM_PHASES] = {};

@@ -73,6 +73,12 @@ __device__ __forceinline__ float3 symv(const float *s, float3 v)
                        fmaf(s[4], v.z, fmaf(s[3], v.y, s[1] * v.x)),
                        fmaf(s[5], v.z, fmaf(s[4], v.y, s[2] * v.x)));
 }
+// p = z + beta p_old with one rounding per component (the persistent
+// kernels' form, so every PCG driver forms the same p)
+__device__ __forceinline__ float3 pform(float3 z, float beta, float3 po)
+{
+    return make_float3(fmaf(beta, po.x, z.x), fmaf(beta, po.y, z.y), fmaf(beta, po.z, z.z));
+}
 // w x p: the skew part of a block of the dihedral-bending model (an upper
 // block is S p + w x p, its transposed lower block S p - w x p)
 __device__ __forceinline__ float3 skewv(float4 w, float3 p)
@@ -260,7 +266,7 @@ __device__ __forceinline__ void begin_solve(const InstDesc &d, const double (&to
     st.bb = tot[2];
     st.beta = 0.0;
     st.alpha = 0.0;
-    st.pq = 0.0;
+    st.pq = tot[0]; // the estimate the first p.q's fixed-point scale comes from
     st.iter = 0;
     st.status = 0;
     st.bar_count = 0u;
@@ -289,13 +295,77 @@ __device__ __forceinline__ void begin_solve(const InstDesc &d, const double (&to
     }
 }
 
-// An instance leaves the loop: the thread that retires the last active one
-// clears the graph's while condition.
+// round(v * 2^s) as a signed 128-bit integer, returned as H * 2^32 + L with
+// 0 <= L < 2^32 (integer operations only).  Exact addition of these limbs
+// makes a team sum independent of how the rows are split over blocks.
+__device__ __forceinline__ void fx_split(float v, int s, long long &H,
+                                         unsigned long long &L)
+{
+    const unsigned bits = __float_as_uint(v);
+    const int e = int((bits >> 23) & 0xffu);
+    H = 0;
+    L = 0;
+    if (e == 0 || e == 255)
+        return; // zero, subnormal (below any scale in use) or Inf/NaN (check sum)
+    const unsigned long long m = (bits & 0x7fffffu) | 0x800000u;
+    const int sh = e - 150 + s; // |v| = m * 2^(e - 150)
+    unsigned long long fh = 0ull, fl = 0ull;
+    if (sh >= 104)
+    {
+        fh = 0x3fffffffffffffffull; // saturate; the check sum flags it
+        fl = ~0ull;
+    }
+    else if (sh >= 64)
+        fh = m << (sh - 64);
+    else if (sh > 0)
+    {
+        fl = m << sh;
+        fh = m >> (64 - sh);
+    }
+    else if (sh == 0)
+        fl = m;
+    else if (sh > -25)
+        fl = (m + (1ull << (-sh - 1))) >> (-sh);
+    if (bits & 0x80000000u)
+    {
+        fl = ~fl + 1ull;
+        fh = ~fh + (fl == 0ull ? 1ull : 0ull);
+    }
+    L = fl & 0xffffffffull;
+    H = (long long)((fh << 32) | (fl >> 32));
+}
+
+// Scale exponent for an estimate of a sum (from the double's exponent bits).
+__device__ __forceinline__ int fx_scale(double est)
+{
+    const long long b = __double_as_longlong(est);
+    const int e = int((b >> 52) & 0x7ff);
+    if (e == 0 || e == 0x7ff)
+        return 100;
+    const int s = kFxTop - (e - 1023);
+    return max(-900, min(900, s));
+}
+
+// 2^e for |e| < 1000, built from the exponent field
+__device__ __forceinline__ double pow2(int e)
+{
+    return __longlong_as_double((long long)(1023 + e) << 52);
+}
+
+__device__ __forceinline__ double fx_value(unsigned long long H, unsigned long long L,
+                                           int s)
+{
+    return double((long long)H) * pow2(32 - s) + double(L) * pow2(-s);
+}
+
+// An instance leaves the loop: the thread that brings the active count down
+// to the launch set's hand-off count (0: the last active instance) clears the
+// graph's while condition.
 __device__ __forceinline__ void retire(BatchCtl *ctl, bool use_cond,
                                        cudaGraphConditionalHandle h)
 {
     int prev = atomicSub(&ctl->n_active, 1);
-    if (use_cond && prev == 1)
+    if (use_cond && prev - 1 == ctl->hand_off)
         cudaGraphSetConditional(h, 0u);
 }
 
@@ -770,7 +840,7 @@ __global__ void __launch_bounds__(kTile) k_ir_start(InstDesc *const *descs,
 // Sets the while condition from the active count (one thread).
 __global__ void k_cond(const BatchCtl *ctl, cudaGraphConditionalHandle h)
 {
-    cudaGraphSetConditional(h, ctl->n_active > 0 ? 1u : 0u);
+    cudaGraphSetConditional(h, ctl->n_active > ctl->hand_off ? 1u : 0u);
 }
 
 // ------------------------------------------------------------------ PCG
@@ -847,21 +917,51 @@ __device__ __forceinline__ void group_sum_d(double (&vv)[R][N], double (&v)[N],
     __syncthreads();
 }
 
-// The tile's partial sums of the graph-loop kernels (group_sum: the same
-// block sums for every kernel variant); the instance totals are formed by
-// k_reduce_pq / k_reduce_rz after the kernel, so no tile waits for a fence
-// and a ticket.
+// A tile's N sums (rows held R per thread) into quantities q0.. of the
+// instance's team-sum buffer bq: the FP32 butterfly of each 32-row group (the
+// persistent kernels' chunks: their team ranges are aligned to 32 rows), each
+// group sum as fixed-point limbs at scale sc[k] (fx_split; lane r N + k
+// converts group (r, k), side by side), the limbs of a warp's groups added
+// with shuffles and sent with one reduction per limb by lanes 0 .. N-1.  The
+// totals are exact, so every kernel variant and every PCG driver gets the
+// same ones.  R and N are powers of two.
 template <int R, int N>
-__device__ __forceinline__ void tile_partial_r(double *part, int nt, int tile_idx,
-                                               const float (&vf)[R][N],
-                                               double (*sh)[kTile / 32])
+__device__ __forceinline__ void tile_fx_add(const float (&vf)[R][N], InstState *st, int bq,
+                                            int q0, const int (&sc)[N])
 {
-    double v[N];
-    group_sum<R, N>(vf, v, sh);
-    if (threadIdx.x == 0)
+    constexpr unsigned FULLM = 0xffffffffu;
+    const int l = threadIdx.x & 31;
+    float tsum[R][N];
+#pragma unroll
+    for (int r = 0; r < R; r++)
 #pragma unroll
         for (int k = 0; k < N; k++)
-            part[k * nt + tile_idx] = v[k];
+            tsum[r][k] = warp_sum(vf[r][k]);
+    long long hh = 0;
+    unsigned long long ll = 0ull;
+    float c = 0.f;
+#pragma unroll
+    for (int r = 0; r < R; r++)
+#pragma unroll
+        for (int k = 0; k < N; k++)
+            if (l == r * N + k)
+            {
+                fx_split(tsum[r][k], sc[k], hh, ll);
+                c = tsum[r][k];
+            }
+#pragma unroll
+    for (int o = (R / 2) * N; o >= N && o > 0; o >>= 1)
+    {
+        hh += __shfl_xor_sync(FULLM, hh, o);
+        ll += __shfl_xor_sync(FULLM, ll, o);
+        c += __shfl_xor_sync(FULLM, c, o);
+    }
+    if (l < N)
+    {
+        atomicAdd(&st->acc[bq][q0 + l][0], (unsigned long long)hh);
+        atomicAdd(&st->acc[bq][q0 + l][1], ll);
+        atomicAdd(&st->acc_chk[bq][q0 + l], c);
+    }
 }
 
 // Read-only load of a pointer field (the descriptor is constant during a kernel).
@@ -877,6 +977,7 @@ template <class T> __device__ __forceinline__ T *ldg_ptr(T *const *addr)
 struct SpmvHdr
 {
     int inst, nv, wu, nt, active, wl;
+    int it, s_pq; // iteration (team-sum buffer it % 3) and the p.q scale
     float beta;
     const int *rowinfo, *colu;
     const uint32_t *lref;
@@ -897,6 +998,8 @@ __device__ __forceinline__ void load_hdr(SpmvHdr &h, const Tile &tl)
     h.inst = inst;
     h.active = st->active;
     const int it = st->iter;
+    h.it = it;
+    h.s_pq = fx_scale(st->pq);
     h.beta = float(st->beta);
     h.nv = __ldg(&dp->nv);
     h.wu = __ldg(&dp->width_up);
@@ -949,7 +1052,7 @@ __device__ __forceinline__ void spmv_rows(const SpmvHdr &d, int row0, float (&pq
             ds[r] = (info >> 8) & 255;
             pv[r] = xyz(d.z[row]);
             if (beta != 0.f)
-                pv[r] = pv[r] + beta * xyz(d.pold[row]);
+                pv[r] = pform(pv[r], beta, xyz(d.pold[row]));
             d.pnew[row] = f4(pv[r]);
         }
         kend[r] = wl + (len[r] - ds[r]);
@@ -1010,7 +1113,7 @@ __device__ __forceinline__ void spmv_rows(const SpmvHdr &d, int row0, float (&pq
                     {
                         pc = xyz(d.z[c]);
                         if (beta != 0.f)
-                            pc = pc + beta * xyz(d.pold[c]);
+                            pc = pform(pc, beta, xyz(d.pold[c]));
                     }
                     q[r] = q[r] + symv(A, pc);
                     if (SKEW && d.Aw)
@@ -1035,6 +1138,7 @@ __device__ __forceinline__ void spmv_rows(const SpmvHdr &d, int row0, float (&pq
 struct UpdHdr
 {
     int inst, nv, nt, active, iter;
+    int s_rz, s_rr; // scales of the new r.z and r.r
     float alpha;
     const float4 *pnew, *q;
     float4 *dx, *r, *z;
@@ -1052,6 +1156,8 @@ __device__ __forceinline__ void load_hdr(UpdHdr &h, const Tile &tl)
     h.inst = inst;
     h.active = st->active;
     h.iter = st->iter;
+    h.s_rz = fx_scale(st->rho);
+    h.s_rr = fx_scale(st->rr);
     h.alpha = float(st->alpha);
     h.nv = __ldg(&dp->nv);
     h.nt = __ldg(&dp->ntile_rows);
@@ -1079,7 +1185,6 @@ __global__ void __launch_bounds__(kTile / R) k_spmv_t(InstDesc *const *descs,
                                                       cudaGraphConditionalHandle h)
 {
     constexpr int T = kTile / R;
-    __shared__ double sh[1][kTile / 32];
     __shared__ SpmvHdr d; // the current instance's header (thread 0 loads it)
     const int ntiles = ctl->n_tiles_rows;
     int cur = -1;
@@ -1101,7 +1206,8 @@ __global__ void __launch_bounds__(kTile / R) k_spmv_t(InstDesc *const *descs,
                 continue;
             float part[R][1];
             spmv_rows<R, U, T, SKEW>(d, tl.start + threadIdx.x, part);
-            tile_partial_r<R, 1>(d.part, d.nt, tl.start / kTile, part, sh);
+            const int sc[1] = {d.s_pq};
+            tile_fx_add<R, 1>(part, d.st, d.it % 3, 0, sc);
         }
     }
 }
@@ -1114,7 +1220,6 @@ __global__ void __launch_bounds__(kTile / R) k_update_t(InstDesc *const *descs,
                                                         int *iters_left)
 {
     constexpr int T = kTile / R;
-    __shared__ double sh[2][kTile / 32];
     // chunked loops (the request server): the last iteration of a chunk ends
     // the while loop; the condition is read after the body completes
     if (iters_left && blockIdx.x == 0 && threadIdx.x == 0)
@@ -1170,7 +1275,8 @@ __global__ void __launch_bounds__(kTile / R) k_update_t(InstDesc *const *descs,
                     part[r][1] = fdot(rr, rr);
                 }
             }
-            tile_partial_r<R, 2>(d.part, d.nt, tl.start / kTile, part, sh);
+            const int sc[2] = {d.s_rz, d.s_rr};
+            tile_fx_add<R, 2>(part, d.st, d.iter % 3, 1, sc);
         }
     }
 }
@@ -1208,6 +1314,7 @@ struct BulkHdr
     float4 *pnew, *q;
     double *part;
     InstState *st;
+    int it, s_pq; // iteration (team-sum buffer it % 3) and the p.q scale
 };
 
 __device__ __forceinline__ unsigned smem_addr(const void *p)
@@ -1273,7 +1380,7 @@ __device__ __forceinline__ unsigned long long global_ns()
 // instance state) for 32 tiles at once, ahead of their copies.
 struct BulkMeta
 {
-    int go, start, nv, wl, wu, nt, it;
+    int go, start, nv, wl, wu, nt, it, s_pq;
     int hx, hy;
     float beta;
     const int *rowinfo, *colu;
@@ -1293,6 +1400,7 @@ __device__ __forceinline__ void bulk_meta(const Tile *tiles, int ti, BulkMeta &m
     m.start = tl.start;
     m.go = __ldcg(&tl.st->active);
     m.it = __ldcg(&tl.st->iter);
+    m.s_pq = fx_scale(__ldcg(&tl.st->pq));
     m.beta = float(__ldcg(&tl.st->beta));
     m.nv = __ldg(&dp->nv);
     m.wl = __ldg(&dp->width_lo);
@@ -1399,9 +1507,13 @@ __device__ __forceinline__ void bulk_issue_warp(const BulkMeta &m, int src, Bulk
         h.q = m.q;
         h.part = m.part;
         h.st = m.st;
+        h.it = it;
     }
     // lane 0 holds nt, q, part and st of its own tile only: broadcast them
     // above when src != 0
+    const int s_pq = __shfl_sync(FULLM, m.s_pq, src);
+    if (lane == 0)
+        h.s_pq = s_pq;
     if (src != 0)
     {
         const int nt = __shfl_sync(FULLM, m.nt, src);
@@ -1560,7 +1672,7 @@ __device__ __forceinline__ float bulk_row(const BulkRegs &r, int t, int info,
             return xyz(P[c - r.h0]);
         float3 pc = xyz(__ldg(r.z + c));
         if (beta != 0.f)
-            pc = pc + beta * xyz(__ldg(r.pold + c));
+            pc = pform(pc, beta, xyz(__ldg(r.pold + c)));
         return pc;
     };
     const float3 pv = pcol(row);
@@ -1680,7 +1792,9 @@ __global__ void __launch_bounds__(kBulkThreads, SKEW ? 1 : 2) k_spmv_bulk(InstDe
     extern __shared__ __align__(128) unsigned char bulk_smem[];
     __shared__ __align__(8) uint64_t full[NST], empty[NST];
     __shared__ BulkHdr hdr[NST];
-    __shared__ double wsum[2][kTile / 32];
+    // the p.q of a stage's tile per consumer warp; the producer turns them
+    // into the instance's fixed-point total when it takes the stage back
+    __shared__ float wsumf[NST][kTile / 32];
     const unsigned stage_bytes = (dynamic_smem_bytes() / NST) & ~127u;
     const int ntiles = ctl->n_tiles_rows;
     const int G = gridDim.x;
@@ -1711,6 +1825,54 @@ __global__ void __launch_bounds__(kBulkThreads, SKEW ? 1 : 2) k_spmv_bulk(InstDe
             const bool ok = mbar_wait_bounded(&empty[stg], ((used / NST) - 1) & 1);
             return __all_sync(0xffffffffu, ok);
         };
+        // the released stage's tile p.q into its instance's team-sum buffer,
+        // in two halves around the stage's refill (so the refill does not
+        // wait): grab reads the tile's consumer-warp sums and its header
+        // before they are overwritten, send (lane k converts warp k's FP32
+        // sum to fixed-point limbs, tile_fx_add's arithmetic; the limbs are
+        // added exactly; lane 0 sends one reduction per limb) runs after
+        struct Grab
+        {
+            int go, it, s;
+            InstState *st;
+            float v;
+        };
+        auto grab = [&](int stg) -> Grab {
+            const BulkHdr &o = hdr[stg];
+            Grab g{o.go, o.it, o.s_pq, o.st, 0.f};
+            if (lane < kTile / 32)
+                g.v = wsumf[stg][lane];
+            __syncwarp();
+            return g;
+        };
+        auto send = [&](const Grab &g) {
+            if (g.go != 1)
+                return;
+            constexpr unsigned M4 = (1u << (kTile / 32)) - 1u;
+            if (lane < kTile / 32)
+            {
+                long long hh;
+                unsigned long long ll;
+                fx_split(g.v, g.s, hh, ll);
+                float c = g.v;
+#pragma unroll
+                for (int k = (kTile / 32) / 2; k > 0; k >>= 1)
+                {
+                    hh += __shfl_xor_sync(M4, hh, k);
+                    ll += __shfl_xor_sync(M4, ll, k);
+                    c += __shfl_xor_sync(M4, c, k);
+                }
+                if (lane == 0)
+                {
+                    const int bq = g.it % 3;
+                    atomicAdd(&g.st->acc[bq][0][0], (unsigned long long)hh);
+                    atomicAdd(&g.st->acc[bq][0][1], ll);
+                    atomicAdd(&g.st->acc_chk[bq][0], c);
+                }
+            }
+            __syncwarp();
+        };
+        auto flush = [&](int stg) { send(grab(stg)); };
         for (int j = 0; j < nmine; j++)
         {
             if ((j & 31) == 0)
@@ -1724,15 +1886,42 @@ __global__ void __launch_bounds__(kBulkThreads, SKEW ? 1 : 2) k_spmv_bulk(InstDe
             const int stg = used % NST;
             if (!acquire(stg))
                 return; // consumers stuck: they give up on their own bounded waits
+            Grab g{0, 0, 0, nullptr, 0.f};
+            if (used >= NST)
+                g = grab(stg);
             bulk_issue_warp<SKEW, HALO>(m, j & 31, hdr[stg], bulk_smem + stg * stage_bytes,
                                         stage_bytes, &full[stg], lane);
+            send(g);
             used++;
         }
         const int stg = used % NST;
-        if (acquire(stg) && lane == 0)
+        if (!acquire(stg))
+            return;
+        if (used >= NST)
+            flush(stg);
+        if (lane == 0)
         {
             hdr[stg].go = -1;
             mbar_arrive(&full[stg]);
+        }
+        __syncwarp();
+        // the other stages' last tiles: fill f = used - NST + k went to stage
+        // f % NST, and its release completes phase f / NST of that stage's
+        // empty barrier
+        for (int k = 1; k < NST; k++)
+        {
+            const int f = used - NST + k;
+            if (f < 0)
+                continue;
+            const bool ok = __all_sync(0xffffffffu,
+                                       mbar_wait_bounded(&empty[f % NST], (f / NST) & 1));
+            if (!ok)
+            {
+                if (lane == 0)
+                    atomicExch(&ctl->err, 1);
+                return;
+            }
+            flush(f % NST);
         }
         return;
     }
@@ -1769,7 +1958,7 @@ __global__ void __launch_bounds__(kBulkThreads, SKEW ? 1 : 2) k_spmv_bulk(InstDe
                 float4 *Z = reinterpret_cast<float4 *>(stage + hd.o_z);
                 const float4 *Po = reinterpret_cast<const float4 *>(stage + hd.o_p);
                 for (int k = tid; k < hd.nh; k += kTile)
-                    Z[k] = f4(xyz(Z[k]) + hd.beta * xyz(Po[k]));
+                    Z[k] = f4(pform(xyz(Z[k]), hd.beta, xyz(Po[k])));
                 consumer_sync();
             }
             float pq = 0.f;
@@ -1779,28 +1968,18 @@ __global__ void __launch_bounds__(kBulkThreads, SKEW ? 1 : 2) k_spmv_bulk(InstDe
                 pq = hd.nh ? bulk_row<SKEW, true>(r, tid, info, L)
                            : bulk_row<SKEW, false>(r, tid, info, L);
             }
-            double *const part = hd.part + hd.tile_idx;
-            // the tile's p.q: FP32 warp sums, FP64 over the warps in order
-            // (group_sum's arithmetic and order); the partials alternate
-            // between two buffers, so one barrier per tile serves both the
-            // partials and the stage's release
+            // the tile's p.q: FP32 sums of its 32-row groups (one per consumer
+            // warp), which the producer adds to the instance's fixed-point
+            // total when it takes the stage back
             const float t = warp_sum(pq);
             if (lane == 0)
-                wsum[j & 1][warp] = double(t);
+                wsumf[stg][warp] = t;
             // generic writes to the stage (the halo's p) are ordered before
             // the copy engine refills it
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
             consumer_sync();
             if (lane == 0)
                 mbar_arrive(&empty[stg]);
-            if (tid == 0)
-            {
-                double v = wsum[j & 1][0];
-#pragma unroll
-                for (int k = 1; k < kTile / 32; k++)
-                    v += wsum[j & 1][k];
-                *part = v;
-            }
         }
         else
         {
@@ -1812,118 +1991,111 @@ __global__ void __launch_bounds__(kBulkThreads, SKEW ? 1 : 2) k_spmv_bulk(InstDe
     }
 }
 
-// Instance totals of a graph-loop half-iteration (k_reduce_pq, k_reduce_rz):
-// one block per instance of the list adds the instance's per-tile partials (sum_strided over kTile
-// lanes, then group_sum_d: one order, whatever the kernel variant that
-// wrote the partials) and takes the scalar step. KIND 0 (after the SpMV): p.q -> alpha,
-// or the end of the solve when p.q is zero or not finite. KIND 1
-// (k_reduce_rz, after the update): r.z, r.r -> beta, the iteration count and the convergence test.
+// Instance totals of a graph-loop half-iteration (k_reduce_pq, k_reduce_rz),
+// one thread per instance of the list: the exact fixed-point totals the tiles
+// added (decoded at the scales the tiles used: the previous p.q, the current
+// r.z and r.r, as the persistent kernels take them), then the scalar step.
+// KIND 0 (after the SpMV): p.q -> alpha, or the end of the solve when p.q is
+// zero or not finite.  KIND 1 (after the update): r.z, r.r -> beta, the
+// iteration count and the convergence test; the next iteration's buffer
+// (last used two iterations ago) is cleared.
 namespace {
+__device__ __forceinline__ double loop_total(const InstState *st, int bq, int q, int s,
+                                             int *bad)
+{
+    const double v = fx_value(__ldcg(&st->acc[bq][q][0]), __ldcg(&st->acc[bq][q][1]), s);
+    const float chk = __ldcg(&st->acc_chk[bq][q]);
+    if (!isfinite(chk) || fabs(v - double(chk)) > 1e-3 * fabs(double(chk)) + 1e-30)
+        *bad = 1;
+    return v;
+}
+
 template <int KIND>
 __device__ __forceinline__ void reduce_body(InstDesc *const *descs, const int *inst_list,
                                             int ninst, const int *ninst_dev, BatchCtl *ctl,
                                             int use_cond, cudaGraphConditionalHandle h)
 {
-    constexpr int N = KIND == 0 ? 1 : 2;
-    __shared__ double sh[2][kTile / 32];
     if (ninst_dev)
         ninst = *ninst_dev;
-    for (int b = blockIdx.x; b < ninst; b += gridDim.x)
+    for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < ninst;
+         b += gridDim.x * blockDim.x)
     {
-        // loads grouped by dependence level (a latency chain, not bandwidth):
-        // the descriptor's fields, then the state and the partials together
         const InstDesc *dp = descs[inst_list[b]];
         InstState *stp = ldg_ptr(&dp->st);
-        const int nt = __ldg(&dp->ntile_rows);
-        const double *part = ldg_ptr(&dp->part);
-        int check_every = 1, max_iters = 0;
-        double rel_tol2 = 0.0, abs_tol2 = 0.0;
-        if (KIND == 1 && threadIdx.x == 0)
-        {
-            check_every = __ldg(&dp->check_every);
-            max_iters = __ldg(&dp->max_iters);
-            rel_tol2 = __ldg(&dp->rel_tol2);
-            abs_tol2 = __ldg(&dp->abs_tol2);
-        }
-        // read by every thread before thread 0 may clear it (group_sum_d syncs)
-        const int active = __ldcg(&stp->active);
-        double rho0 = 0.0, bb0 = 0.0;
-        int it0 = 0;
-        if (threadIdx.x == 0)
-        {
-            rho0 = __ldcg(&stp->rho);
-            bb0 = __ldcg(&stp->bb);
-            it0 = __ldcg(&stp->iter);
-        }
-        double sv[1][N];
-#pragma unroll
-        for (int k = 0; k < N; k++)
-            sv[0][k] = 0.0;
-        sum_strided<N>(part, nt, threadIdx.x, sv[0]);
-        if (!active)
+        if (!__ldcg(&stp->active))
             continue;
-        double tot[N];
-        group_sum_d<1, N>(sv, tot, sh);
-        if (threadIdx.x == 0)
+        InstState &st = *stp;
+        const int it0 = st.iter;
+        const int bq = it0 % 3;
+        int bad = 0;
+        if (KIND == 0)
         {
-            InstState &st = *stp;
-            if (KIND == 0)
+            const double pq = loop_total(stp, bq, 0, fx_scale(st.pq), &bad);
+            st.pq = pq;
+            if (bad || !isfinite(pq))
             {
-                st.pq = tot[0];
-                if (!isfinite(tot[0]))
-                {
-                    st.status = 6;
-                    st.active = 0;
-                    retire(ctl, use_cond, h);
-                }
-                else if (tot[0] == 0.0)
-                {
-                    // PCGSolver.cu:259-263 clamps alpha to zero; nothing moves
-                    // afterwards, so the loop ends here. (p.Ap < 0 goes on with a
-                    // negative alpha, as the reference does.)
-                    st.status = 7;
-                    st.active = 0;
-                    retire(ctl, use_cond, h);
-                }
-                else
-                    st.alpha = rho0 / tot[0];
+                st.status = 6;
+                st.active = 0;
+                retire(ctl, use_cond, h);
+            }
+            else if (pq == 0.0)
+            {
+                // PCGSolver.cu:259-263 clamps alpha to zero; nothing moves
+                // afterwards, so the loop ends here. (p.Ap < 0 goes on with a
+                // negative alpha, as the reference does.)
+                st.status = 7;
+                st.active = 0;
+                retire(ctl, use_cond, h);
+            }
+            else
+                st.alpha = st.rho / pq;
+        }
+        else
+        {
+            const double rho0 = st.rho;
+            const double rho_new = loop_total(stp, bq, 1, fx_scale(rho0), &bad);
+            const double rr = loop_total(stp, bq, 2, fx_scale(st.rr), &bad);
+            const int nb = (it0 + 1) % 3;
+            for (int q = 0; q < 3; q++)
+            {
+                st.acc[nb][q][0] = 0ull;
+                st.acc[nb][q][1] = 0ull;
+                st.acc_chk[nb][q] = 0.f;
+            }
+            st.beta = (rho0 == 0.0) ? 0.0 : rho_new / rho0;
+            st.rho = rho_new;
+            st.rr = rr;
+            const int n = it0 + 1;
+            st.iter = n;
+            bool stop = false;
+            if (bad || !isfinite(rho_new) || !isfinite(rr))
+            {
+                st.status = 6;
+                stop = true;
             }
             else
             {
-                const double rho_new = tot[0];
-                const double rr = tot[N - 1];
-                st.beta = (rho0 == 0.0) ? 0.0 : rho_new / rho0;
-                st.rho = rho_new;
-                st.rr = rr;
-                const int n = it0 + 1;
-                st.iter = n;
-                bool stop = false;
-                if (!isfinite(rho_new) || !isfinite(rr))
+                const int check_every = __ldg(&dp->check_every);
+                const int max_iters = __ldg(&dp->max_iters);
+                const double rel_tol2 = __ldg(&dp->rel_tol2), abs_tol2 = __ldg(&dp->abs_tol2);
+                const bool check = ((n - 1) % check_every) == 0 || n >= max_iters;
+                const bool conv = (rel_tol2 > 0.0 && rr <= rel_tol2 * st.bb) ||
+                                  (abs_tol2 > 0.0 && rr <= abs_tol2);
+                if (check && conv)
                 {
-                    st.status = 6;
+                    st.status = 0;
                     stop = true;
                 }
-                else
+                else if (n >= max_iters)
                 {
-                    const bool check = ((n - 1) % check_every) == 0 || n >= max_iters;
-                    const bool conv = (rel_tol2 > 0.0 && rr <= rel_tol2 * bb0) ||
-                                      (abs_tol2 > 0.0 && rr <= abs_tol2);
-                    if (check && conv)
-                    {
-                        st.status = 0;
-                        stop = true;
-                    }
-                    else if (n >= max_iters)
-                    {
-                        st.status = 8; // CLOTH_ERR_MAXITER
-                        stop = true;
-                    }
+                    st.status = 8; // CLOTH_ERR_MAXITER
+                    stop = true;
                 }
-                if (stop)
-                {
-                    st.active = 0;
-                    retire(ctl, use_cond, h);
-                }
+            }
+            if (stop)
+            {
+                st.active = 0;
+                retire(ctl, use_cond, h);
             }
         }
     }
@@ -2178,69 +2350,6 @@ __device__ __forceinline__ int ld_keep(const int *ptr, unsigned long long pol)
 
 namespace {
 
-// round(v * 2^s) as a signed 128-bit integer, returned as H * 2^32 + L with
-// 0 <= L < 2^32 (integer operations only).  Exact addition of these limbs
-// makes a team sum independent of how the rows are split over blocks.
-__device__ __forceinline__ void fx_split(float v, int s, long long &H,
-                                         unsigned long long &L)
-{
-    const unsigned bits = __float_as_uint(v);
-    const int e = int((bits >> 23) & 0xffu);
-    H = 0;
-    L = 0;
-    if (e == 0 || e == 255)
-        return; // zero, subnormal (below any scale in use) or Inf/NaN (check sum)
-    const unsigned long long m = (bits & 0x7fffffu) | 0x800000u;
-    const int sh = e - 150 + s; // |v| = m * 2^(e - 150)
-    unsigned long long fh = 0ull, fl = 0ull;
-    if (sh >= 104)
-    {
-        fh = 0x3fffffffffffffffull; // saturate; the check sum flags it
-        fl = ~0ull;
-    }
-    else if (sh >= 64)
-        fh = m << (sh - 64);
-    else if (sh > 0)
-    {
-        fl = m << sh;
-        fh = m >> (64 - sh);
-    }
-    else if (sh == 0)
-        fl = m;
-    else if (sh > -25)
-        fl = (m + (1ull << (-sh - 1))) >> (-sh);
-    if (bits & 0x80000000u)
-    {
-        fl = ~fl + 1ull;
-        fh = ~fh + (fl == 0ull ? 1ull : 0ull);
-    }
-    L = fl & 0xffffffffull;
-    H = (long long)((fh << 32) | (fl >> 32));
-}
-
-// Scale exponent for an estimate of a sum (from the double's exponent bits).
-__device__ __forceinline__ int fx_scale(double est)
-{
-    const long long b = __double_as_longlong(est);
-    const int e = int((b >> 52) & 0x7ff);
-    if (e == 0 || e == 0x7ff)
-        return 100;
-    const int s = kFxTop - (e - 1023);
-    return max(-900, min(900, s));
-}
-
-// 2^e for |e| < 1000, built from the exponent field
-__device__ __forceinline__ double pow2(int e)
-{
-    return __longlong_as_double((long long)(1023 + e) << 52);
-}
-
-__device__ __forceinline__ double fx_value(unsigned long long H, unsigned long long L,
-                                           int s)
-{
-    return double((long long)H) * pow2(32 - s) + double(L) * pow2(-s);
-}
-
 // Per-warp fixed-point accumulator of NQ chunk sums (held by lane 0).
 template <int NQ> struct WarpFx
 {
@@ -2326,16 +2435,23 @@ __device__ __forceinline__ void pcg_persistent_body(InstDesc *const *descs,
                 sm1[i] = d.M1[row];
             }
         }
+    // the solve's state: at its start (PCG start bookkeeping: no iteration,
+    // beta = 0, p.q estimate = r.z) or where a graph loop handed it over
+    // (its iteration count, scalars and p_old in global memory)
+    __shared__ int s_it0;
     if (tid == 0)
     {
+        s_it0 = __ldcg(&st->iter);
         s_rho = __ldcg(&st->rho);
         s_rr = __ldcg(&st->rr);
-        s_pq = s_rho;
-        s_beta = 0.0;
-        s_alpha = 0.0;
-        bc_bf = 0.f;
+        s_pq = __ldcg(&st->pq);
+        s_beta = __ldcg(&st->beta);
+        s_alpha = __ldcg(&st->alpha);
+        bc_bf = float(s_beta);
     }
-    int it = 0, status = 0;
+    __syncthreads();
+    const int it0 = s_it0;
+    int it = it0, status = 0;
     // the team's arrival count: after the work list, one word per block slot,
     // the team using its first block's
     __shared__ unsigned long long s_nbar; // arrivals barrier k waits for (thread 0)
@@ -2452,7 +2568,12 @@ __device__ __forceinline__ void pcg_persistent_body(InstDesc *const *descs,
                         float4 pn = zz[u];
                         if (!first)
                         {
-                            const float4 po = sp[i];
+                            // the previous p: staged by the last iteration,
+                            // or in global memory on the first one after a
+                            // hand-over
+                            const float4 po = (it == it0 && it0 > 0)
+                                                  ? ldcg4(pold + w.halo0 + i)
+                                                  : sp[i];
                             pn.x = fmaf(bf, po.x, pn.x);
                             pn.y = fmaf(bf, po.y, pn.y);
                             pn.z = fmaf(bf, po.z, pn.z);

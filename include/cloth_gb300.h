@@ -148,6 +148,14 @@ int cloth_ctx_get_profile(cloth_ctx *ctx, double *ms_total, long long *launches)
 int cloth_ctx_reset_profile(cloth_ctx *ctx);
 /* Preferred PCG driver for launch sets built after the call. */
 int cloth_ctx_set_solver(cloth_ctx *ctx, int solver);
+/* Launch sets of more cloths than fit one persistent launch run the graph
+ * loop; with the persistent solver (two barriers) chosen, such a set hands
+ * its last max_instances iterating cloths to the persistent kernel, whose
+ * arithmetic is the graph loop's bit for bit (results do not change; the few
+ * slowest cloths' iterations stop paying the graph loop's per-iteration
+ * latency).  -1 (the default): the GPU's SM count / 4; 0: never.  For launch
+ * sets built after the call. */
+int cloth_ctx_set_tail_hand_off(cloth_ctx *ctx, int max_instances);
 /* Bounded waits of the persistent PCG drivers (no counterpart in the
  * reference, whose solver never waits on the device). A team barrier gives up
  * after `polls` polls (0: the default, 2^25, seconds); the solve then ends
