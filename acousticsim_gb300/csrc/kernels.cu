@@ -12,9 +12,10 @@
 //                                                              BlockJacobPreconditioner,
 //                                                              Calc_r0_d0_r0Minvr0)
 //   k_spmv         p = z + beta p (recomputed at the gathered columns), q = A p,
-//                  FP64 p.q                                   (Calc_dTAd_zi, UpdateDirection)
-//   k_update       dx += alpha p, r -= alpha q, z = M^-1 r, FP64 r.z and r.r,
-//                  per-instance convergence test              (Calc_rnext_rnextMinvrnext_xnext)
+//                  p.q as exact fixed-point sums              (Calc_dTAd_zi, UpdateDirection)
+//   k_update       dx += alpha p, r -= alpha q, z = M^-1 r, r.z and r.r as exact
+//                  fixed-point sums                           (Calc_rnext_rnextMinvrnext_xnext)
+//   k_reduce_*     per-instance totals, alpha / beta, the convergence test
 //   k_advance      x_pre = x, x += dx in FP64                 (BaraffClothGpu.cpp:246-258)
 //
 // Reference kernels: src/sim/cloth/BaraffClothGpu.cu, src/sim/cloth/gpu_solvers/PCGSolver.cu.

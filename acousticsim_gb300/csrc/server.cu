@@ -23,9 +23,9 @@
 // inactive there: no kernel touches its per-solve arrays, so its pool range
 // may be handed to a request of chunk k+1 (stream order keeps them apart).
 //
-// Per-instance arithmetic is the graph-loop solver's (tile partial sums per
-// instance, reduced in tile order), so a request's result does not depend on
-// what else is in the chunk: it is bit-identical to stepping the cloth alone.
+// Per-instance arithmetic is the graph-loop solver's (exact fixed-point sums
+// per instance), so a request's result does not depend on what else is in the
+// chunk: it is bit-identical to stepping the cloth alone.
 #include "internal.h"
 
 #include <algorithm>
