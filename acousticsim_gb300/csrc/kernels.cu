@@ -854,70 +854,6 @@ __global__ void k_cond(const BatchCtl *ctl, cudaGraphConditionalHandle h)
 // does not change any result.
 namespace {
 
-// Tile sum of N values per row, rows held R per thread: FP32 butterfly per
-// 32-row group, FP64 over the groups in order (block_sum for R = 1).
-template <int R, int N>
-__device__ __forceinline__ void group_sum(const float (&vf)[R][N], double (&v)[N],
-                                          double (*sh)[kTile / 32])
-{
-    constexpr int WPB = kTile / R / 32; // warps per block
-    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
-#pragma unroll
-    for (int r = 0; r < R; r++)
-#pragma unroll
-        for (int k = 0; k < N; k++)
-        {
-            const float t = warp_sum(vf[r][k]);
-            if (l == 0)
-                sh[k][r * WPB + w] = double(t);
-        }
-    __syncthreads();
-    if (threadIdx.x == 0)
-#pragma unroll
-        for (int k = 0; k < N; k++)
-        {
-            double s = sh[k][0];
-#pragma unroll
-            for (int j = 1; j < kTile / 32; j++)
-                s += sh[k][j];
-            v[k] = s;
-        }
-    __syncthreads();
-}
-
-// FP64 counterpart over virtual threads v = r * (kTile/R) + t (block_sum_d for R = 1).
-template <int R, int N>
-__device__ __forceinline__ void group_sum_d(double (&vv)[R][N], double (&v)[N],
-                                            double (*sh)[kTile / 32])
-{
-    constexpr int WPB = kTile / R / 32;
-    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
-#pragma unroll
-    for (int r = 0; r < R; r++)
-#pragma unroll
-        for (int k = 0; k < N; k++)
-        {
-            double x = vv[r][k];
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1)
-                x += __shfl_down_sync(0xffffffffu, x, o);
-            if (l == 0)
-                sh[k][r * WPB + w] = x;
-        }
-    __syncthreads();
-    if (threadIdx.x == 0)
-#pragma unroll
-        for (int k = 0; k < N; k++)
-        {
-            double s = sh[k][0];
-#pragma unroll
-            for (int j = 1; j < kTile / 32; j++)
-                s += sh[k][j];
-            v[k] = s;
-        }
-    __syncthreads();
-}
-
 // A tile's N sums (rows held R per thread) into quantities q0.. of the
 // instance's team-sum buffer bq: the FP32 butterfly of each 32-row group (the
 // persistent kernels' chunks: their team ranges are aligned to 32 rows), each
