@@ -77,7 +77,7 @@ class ClothContext:
     def set_tail_hand_off(self, max_instances: int = -1) -> None:
         """Graph-loop launch sets hand their last `max_instances` iterating
         cloths to the persistent kernel (same results bit for bit; -1: the SM
-        count / 4, 0: never).  For launch sets built after the call."""
+        count / 16, 0: never).  For launch sets built after the call."""
         N.call("cloth_ctx_set_tail_hand_off", self._h, int(max_instances))
 
     def set_spin_limit(self, polls: int = 0, extra_arrivals: int = 0) -> None:

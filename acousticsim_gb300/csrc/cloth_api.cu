@@ -802,7 +802,7 @@ int make_batch(cloth_ctx *ctx, const std::vector<cloth_s *> &members,
     // two barriers) hands its last few iterating cloths to the persistent
     // kernel: the graph loop's iterations cost about the same however few
     // cloths remain
-    const int ho = ctx->tail_hand_off < 0 ? ctx->num_sms / 4 : ctx->tail_hand_off;
+    const int ho = ctx->tail_hand_off < 0 ? std::max(1, ctx->num_sms / 16) : ctx->tail_hand_off;
     if (!b->persist_ok && !b->collide && ho > 0 && int(members.size()) > ho &&
         (ctx->solver == CLOTH_SOLVER_PERSISTENT || ctx->solver == CLOTH_SOLVER_PERSISTENT_2B))
     {

@@ -145,7 +145,7 @@ struct cloth_ctx_s
     cloth::SpinCfg spin = {cloth::kSpinLimitDefault, 0u};
     int solver = 0; // 0: persistent cooperative PCG when the set fits, 1: graph loop
     // graph-loop launch sets of more cloths than this hand their last this-many
-    // iterating cloths to the persistent kernel (-1: num_sms / 4; 0: never)
+    // iterating cloths to the persistent kernel (-1: num_sms / 16; 0: never)
     int tail_hand_off = -1;
     bool escalate = true; // FP32 PCG ending in NaN / breakdown: re-solve the step in FP64
     bool prof = false;

@@ -153,7 +153,7 @@ int cloth_ctx_set_solver(cloth_ctx *ctx, int solver);
  * its last max_instances iterating cloths to the persistent kernel, whose
  * arithmetic is the graph loop's bit for bit (results do not change; the few
  * slowest cloths' iterations stop paying the graph loop's per-iteration
- * latency).  -1 (the default): the GPU's SM count / 4; 0: never.  For launch
+ * latency).  -1 (the default): the GPU's SM count / 16; 0: never.  For launch
  * sets built after the call. */
 int cloth_ctx_set_tail_hand_off(cloth_ctx *ctx, int max_instances);
 /* Bounded waits of the persistent PCG drivers (no counterpart in the
