@@ -1546,6 +1546,10 @@ int finish_tail(Batch *b)
             rest.push_back(i);
     if (rest.empty())
         return CLOTH_OK;
+    // (a simulation whose slowest cloths keep changing would grow the cache
+    // of tail launch sets without end: it is dropped past a few dozen)
+    if (b->tails.size() >= 32 && b->tails.find(rest) == b->tails.end())
+        b->tails.clear();
     std::unique_ptr<Batch> &tb = b->tails[rest];
     if (!tb)
     {
