@@ -741,6 +741,36 @@ def batch_measure(args, ctx) -> dict:
         b_spmv += s_["iters"] * (algorithmic_bytes(c.nv, mi["nnzb"])["matrix"] + 68 * c.nv)
         b_upd += s_["iters"] * 136 * c.nv
     roof = graph_loop_roofline(prof, b_spmv, b_upd)
+    # the same kernels while every cloth iterates: a profiled step capped at
+    # the fewest PCG iterations any cloth ran, rounded down to the host
+    # driver's chunk of 8 launches so that no launch runs empty (the slow tail
+    # launches, with few cloths left, pull the whole-solve figure down)
+    capped = min(40, min(s_["iters"] for s_ in stp)) // 8 * 8
+    if capped >= 8:
+        reset_all()
+        ctx.set_profiling(True)
+        ctx.reset_profile()
+        ctx.batch_step(cloths, 0.0, params(max_iters=capped, rel_tol=REL_TOL))
+        prof40 = ctx.profile()
+        ctx.set_profiling(False)
+        peak = measured_peaks()["hbm_gbs"]
+        bytes_it = {"spmv_dot": 0.0, "update_dot": 0.0}
+        for c in cloths:
+            mi = c.matrix_info()
+            bytes_it["spmv_dot"] += algorithmic_bytes(c.nv, mi["nnzb"])["matrix"] + 68 * c.nv
+            bytes_it["update_dot"] += 136 * c.nv
+        roof["all_active"] = {}
+        for name in ("spmv_dot", "update_dot"):
+            ph = prof40[name]
+            if ph["launches"] and ph["ms"] > 0:
+                us = ph["ms"] * 1e3 / ph["launches"]
+                gbs = bytes_it[name] / (us * 1e-6) / 1e9
+                roof["all_active"][name] = {"us_per_launch": us, "achieved": gbs,
+                                            "unit": "GB/s", "frac": gbs / peak,
+                                            "launches": ph["launches"]}
+        roof["all_active"]["note"] = (f"the first {capped} PCG iterations of the same step, "
+                                      "every cloth iterating: algorithmic bytes of one launch "
+                                      "over its average CUDA-event time")
     variant = {"variant": ctx.kernel_variant(), "times_ms": ctx.tuning_times()}
     # one cloth per launch on a size-stratified sample of the same solves
     sample = stratified([n for n, _ in confs], args.batch_sample)
