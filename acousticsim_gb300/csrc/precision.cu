@@ -56,6 +56,12 @@ struct F64Ptr
     double *part;                     // 3 * nblk partials
     F64State *st;
     int nblk;
+    // the stored blocks in FP64 (the assembled FP32 planes converted, exactly,
+    // by k64_mat before each solve): GB300's FP64 pipe is narrow, and the
+    // conversions would otherwise run in the SpMV's inner loop every iteration
+    double4_32a *B0;
+    double2 *B1;
+    double4_32a *Bw; // skew parts (dihedral bending), else null
 };
 
 __device__ __forceinline__ double sumw(double v)
@@ -150,10 +156,52 @@ struct Mat64
     }
 };
 
+// The stored blocks' entries as FP64 values: the assembled FP32 planes
+// (converted as they are read) or their FP64 copy; both give the same values.
+struct F32Blocks
+{
+    const float4 *__restrict__ A0;
+    const float2 *__restrict__ A1;
+    const float4 *__restrict__ Aw;
+    __device__ explicit F32Blocks(const Mat64 &m) : A0(m.A0), A1(m.A1), Aw(m.Aw) {}
+    __device__ bool skew() const { return Aw != nullptr; }
+    __device__ void sym(uint32_t o, double a[6]) const
+    {
+        const float4 u = A0[o];
+        const float2 w = A1[o];
+        a[0] = u.x, a[1] = u.y, a[2] = u.z, a[3] = u.w, a[4] = w.x, a[5] = w.y;
+    }
+    __device__ void w3(uint32_t o, double w[3]) const
+    {
+        const float4 u = Aw[o];
+        w[0] = u.x, w[1] = u.y, w[2] = u.z;
+    }
+};
+struct F64Blocks
+{
+    const double4_32a *__restrict__ B0;
+    const double2 *__restrict__ B1;
+    const double4_32a *__restrict__ Bw;
+    __device__ explicit F64Blocks(const F64Ptr &f) : B0(f.B0), B1(f.B1), Bw(f.Bw) {}
+    __device__ bool skew() const { return Bw != nullptr; }
+    __device__ void sym(uint32_t o, double a[6]) const
+    {
+        const double4_32a u = B0[o];
+        const double2 w = B1[o];
+        a[0] = u.x, a[1] = u.y, a[2] = u.z, a[3] = u.w, a[4] = w.x, a[5] = w.y;
+    }
+    __device__ void w3(uint32_t o, double w[3]) const
+    {
+        const double4_32a u = Bw[o];
+        w[0] = u.x, w[1] = u.y, w[2] = u.z;
+    }
+};
+
 // y = A v on one row in FP64, slots in column order: the lower ones (block at
 // the transposed position), then the diagonal and upper ones. v: nv*3
 // doubles, or the FP32 dx when v64 is null.
-__device__ __forceinline__ void row_mul64(const Mat64 &d, int row,
+template <class Blocks>
+__device__ __forceinline__ void row_mul64(const Mat64 &d, const Blocks &B, int row,
                                           const double *__restrict__ v64, double *y)
 {
     const int info = d.rowinfo[row];
@@ -175,9 +223,8 @@ __device__ __forceinline__ void row_mul64(const Mat64 &d, int row,
             oa = up_idx(s - ds, row, d.wu);
             c = d.colu[oa];
         }
-        const float4 u = d.A0[oa];
-        const float2 uw = d.A1[oa];
-        const double a[6] = {u.x, u.y, u.z, u.w, uw.x, uw.y};
+        double a[6];
+        B.sym(oa, a);
         double x0, x1, x2;
         if (v64)
         {
@@ -198,13 +245,14 @@ __device__ __forceinline__ void row_mul64(const Mat64 &d, int row,
         y[0] = fma(a[2], x2, fma(a[1], x1, fma(a[0], x0, y[0])));
         y[1] = fma(a[4], x2, fma(a[3], x1, fma(a[1], x0, y[1])));
         y[2] = fma(a[5], x2, fma(a[4], x1, fma(a[2], x0, y[2])));
-        if (d.Aw)
+        if (B.skew())
         {
             // skew part (dihedral bending): + w x v on stored blocks, - on
-            // the transposed ones
-            const float4 wf = d.Aw[oa];
-            const double sg = lower ? -1.0 : 1.0;
-            const double wx = sg * wf.x, wy = sg * wf.y, wz = sg * wf.z;
+            // the transposed ones (a sign flip, exact)
+            double w[3];
+            B.w3(oa, w);
+            const double wx = lower ? -w[0] : w[0], wy = lower ? -w[1] : w[1],
+                         wz = lower ? -w[2] : w[2];
             y[0] += wy * x2 - wz * x1;
             y[1] += wz * x0 - wx * x2;
             y[2] += wx * x1 - wy * x0;
@@ -224,7 +272,7 @@ __global__ void __launch_bounds__(kB64) k64_resid(const InstDesc *dp, const doub
          row += gridDim.x * blockDim.x)
     {
         double y[3];
-        row_mul64(m, row, dx64, y);
+        row_mul64(m, F32Blocks(m), row, dx64, y);
         const float4 b = d.b[row];
         const double r0 = double(b.x) - y[0], r1 = double(b.y) - y[1], r2 = double(b.z) - y[2];
         r64[3 * row] = r0;
@@ -366,6 +414,27 @@ __global__ void k64_p(const InstDesc *dp, F64Ptr f)
         f.p[i] = fma(beta, f.p[i], f.z[i]);
 }
 
+// The stored blocks in FP64 (every plane entry, padding included), before a
+// solve that runs k64_spmv.
+__global__ void __launch_bounds__(kB64) k64_mat(const InstDesc *dp, F64Ptr f)
+{
+    const InstDesc &d = *dp;
+    const size_t n = size_t(d.width_up) * size_t(d.ntile_rows) * kTile;
+    for (size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n;
+         i += size_t(gridDim.x) * blockDim.x)
+    {
+        const float4 a = d.A0[i];
+        const float2 b = d.A1[i];
+        f.B0[i] = make_double4_32a(a.x, a.y, a.z, a.w);
+        f.B1[i] = make_double2(b.x, b.y);
+        if (f.Bw && d.Aw)
+        {
+            const float4 w = d.Aw[i];
+            f.Bw[i] = make_double4_32a(w.x, w.y, w.z, 0.0);
+        }
+    }
+}
+
 // q = A p, pq = p.q -> alpha
 __global__ void __launch_bounds__(kB64) k64_spmv(const InstDesc *dp, F64Ptr f,
                                                  cudaGraphConditionalHandle h, int use_cond)
@@ -375,11 +444,12 @@ __global__ void __launch_bounds__(kB64) k64_spmv(const InstDesc *dp, F64Ptr f,
         return;
     double v[1] = {0.0};
     const Mat64 m(d);
+    const F64Blocks B(f);
     for (int row = blockIdx.x * blockDim.x + threadIdx.x; row < m.nv;
          row += gridDim.x * blockDim.x)
     {
         double y[3];
-        row_mul64(m, row, f.p, y);
+        row_mul64(m, B, row, f.p, y);
 #pragma unroll
         for (int k = 0; k < 3; k++)
             f.q[3 * row + k] = y[k];
@@ -577,6 +647,11 @@ int f64_work(cloth_s *c, F64Work **out)
                o_dx64 = L.take<double>(3 * size_t(n)), o_r64 = L.take<double>(3 * size_t(n)),
                o_prev = L.take<double>(3 * size_t(n)),
                o_part = L.take<double>(3 * size_t(grid)), o_st = L.take<F64State>(1);
+        // FP64 copies of the stored blocks (every plane entry of whole tiles)
+        const size_t nb = size_t(c->h.width_up) * size_t(c->h.ntile_rows) * kTile;
+        const bool dih = c->mat.bending_model == 1;
+        const size_t o_B0 = L.take<double4_32a>(nb), o_B1 = L.take<double2>(nb),
+                     o_Bw = dih ? L.take<double4_32a>(nb) : 0;
         if (cudaMalloc(&p->w.mem, L.off) != cudaSuccess)
         {
             cudaGetLastError();
@@ -594,6 +669,9 @@ int f64_work(cloth_s *c, F64Work **out)
         p->w.f.part = reinterpret_cast<double *>(b + o_part);
         p->w.f.st = reinterpret_cast<F64State *>(b + o_st);
         p->w.f.nblk = grid;
+        p->w.f.B0 = reinterpret_cast<double4_32a *>(b + o_B0);
+        p->w.f.B1 = reinterpret_cast<double2 *>(b + o_B1);
+        p->w.f.Bw = dih ? reinterpret_cast<double4_32a *>(b + o_Bw) : nullptr;
         p->w.dx64 = reinterpret_cast<double *>(b + o_dx64);
         p->w.r64 = reinterpret_cast<double *>(b + o_r64);
         p->w.dx64_prev = reinterpret_cast<double *>(b + o_prev);
@@ -833,6 +911,8 @@ int cloth_solve_fp64(cloth_t *c, const cloth_solve_params *params, cloth_solve_s
     st0.abs_tol2 = params->abs_tol > 0 ? params->abs_tol * params->abs_tol : 0.0;
     st0.max_iters = params->max_iters;
     PCK(cudaMemcpyAsync(w->f.st, &st0, sizeof(st0), cudaMemcpyHostToDevice, c->ctx->stream));
+    k64_mat<<<w->grid, kB64, 0, c->ctx->stream>>>(c->d_desc, w->f);
+    PCK(cudaGetLastError());
     PCK(cudaGraphLaunch(w->pcg, c->ctx->stream));
     PCK(cudaMemcpyAsync(w->dx64, w->f.dx, size_t(c->tab.nv) * 3 * sizeof(double),
                         cudaMemcpyDeviceToDevice, c->ctx->stream));
@@ -984,6 +1064,7 @@ int cloth_solve_flexible(cloth_t *c, const cloth_solve_params *inner, double rel
     std::memset(&st0, 0, sizeof(st0));
     st0.max_iters = 1; // k64_init marks the state active
     PCK(cudaMemcpyAsync(f.st, &st0, sizeof(st0), cudaMemcpyHostToDevice, s));
+    k64_mat<<<grid, kB64, 0, s>>>(dp, f);
     k64_init<<<grid, kB64, 0, s>>>(dp, f);
     PCK(cudaGetLastError());
     F64State hs;
