@@ -382,7 +382,12 @@ int cloth_residual_fp64(cloth_t *cloth, double *rel_residual);
 int cloth_solve_refined(cloth_t *cloth, const cloth_solve_params *inner, double rel_tol,
                         int max_outer, cloth_refine_stats *stats);
 /* All-FP64 block-Jacobi PCG (FP64 vectors, FP64 inverse diagonal blocks, FP64
- * reductions) from dx = 0, for comparison; recurrence residual in stats. */
+ * reductions) from dx = 0, for comparison; recurrence residual in stats.
+ * The FP64 paths allocate their work arrays on a cloth's first FP64 call and
+ * keep them (cloth_ctx_device_bytes counts them): FP64 vectors, and an FP64
+ * copy of the stored blocks that each solve refreshes (48 B per stored block,
+ * 80 B with dihedral bending), since GB300's FP64 pipe, not memory, bounds the
+ * FP64 SpMV. */
 int cloth_solve_fp64(cloth_t *cloth, const cloth_solve_params *params,
                      cloth_solve_stats *stats);
 /* Flexible CG in FP64 (Notay's FCG(1): each direction A-orthogonalised
