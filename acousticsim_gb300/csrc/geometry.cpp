@@ -448,6 +448,26 @@ bool delaunay_cloth(const GridDesc &g, unsigned long long seed, Mesh &m, std::st
     if (!triangulate(xy, m.tris, err))
         return false;
     m.nt = int(m.tris.size() / 3);
+    // A strip far thinner than its subdivision (e.g. 0.01 x 3.0 split 3 x 120)
+    // keeps, of its boundary-first point list, only points on one or two
+    // boundary lines: collinear (no triangle at all) or joined to the rest by
+    // slivers only.  Such a mesh is no cloth: refused, not returned in part.
+    {
+        std::vector<char> used(size_t(target), 0);
+        for (int i : m.tris)
+            used[size_t(i)] = 1;
+        int unused = 0;
+        for (char u : used)
+            unused += u ? 0 : 1;
+        if (unused > 0)
+        {
+            err = "delaunay: " + std::to_string(unused) + " of the " + std::to_string(target) +
+                  " points are in no triangle (a strip too thin for its subdivision: its "
+                  "points are collinear or nearly so); use a wider cloth or fewer subdivisions "
+                  "along its length";
+            return false;
+        }
+    }
     place(g, xy, m);
     return edges_by_appearance(m, err);
 }

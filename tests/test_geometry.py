@@ -116,3 +116,31 @@ def test_seed_changes_points_and_refusals(built, golden):
         build_grid((1.0, 1.0), (1, 2), geometry_type="delaunay")
     with pytest.raises(ClothError):
         build_grid((1.0, 1.0), (12, 12), uv_rotation_deg=30.0, geometry_type="delaunay")
+
+
+@pytest.mark.parametrize("size,sub", [((0.01, 3.0), (3, 5)), ((0.01, 3.0), (3, 120)),
+                                      ((0.03, 3.0), (3, 40))])
+def test_delaunay_refuses_strips_too_thin_for_their_subdivision(built, size, sub):
+    """A strip far thinner than its subdivision keeps only boundary points on
+    one or two lines (collinear, or joined to the rest by slivers): refused
+    rather than returned as a partial mesh."""
+    from acousticsim_gb300 import ClothError, build_grid
+    with pytest.raises(ClothError, match="in no triangle"):
+        build_grid(size, sub, geometry_type="delaunay", seed=7)
+
+
+def test_delaunay_meshes_are_complete(built):
+    """Random sizes and subdivisions (aspect ratios up to 15:1): every point in
+    a counter-clockwise triangle, T = 2V - B - 2 for the B boundary edges, every
+    edge in one or two triangles."""
+    from acousticsim_gb300 import build_grid
+    rng = np.random.default_rng(0)
+    for _ in range(60):
+        sub = (int(rng.integers(2, 40)), int(rng.integers(2, 40)))
+        size = (float(rng.uniform(0.2, 3.0)), float(rng.uniform(0.2, 3.0)))
+        m = build_grid(size, sub, geometry_type="delaunay", seed=int(rng.integers(0, 10**6)))
+        pos, tris, edges = m["pos"], m["tris"], m["edges"]
+        assert (_orient(pos, tris) > 0).all()
+        assert np.isin(np.arange(len(pos)), tris).all()
+        nb = int((edges[:, 3] == -1).sum())
+        assert len(tris) == 2 * len(pos) - nb - 2, (size, sub)
