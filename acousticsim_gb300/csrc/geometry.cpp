@@ -123,11 +123,44 @@ bool triangulate(const std::vector<double> &pts, std::vector<int> &out, std::str
     };
     std::vector<Bnd> bnd;
     unsigned walk_rng = 12345u;
+    // walk starts (the cavity of a point, every triangle whose circumcircle
+    // holds it, does not depend on where the walk starts; a near start keeps
+    // the walks short): tri_of[v] is a live triangle at vertex v (a cavity
+    // keeps every vertex of the triangles it removes on its boundary, and each
+    // boundary vertex gets a new triangle), and a coarse grid over the points'
+    // box holds the vertex inserted last in each cell
+    std::vector<int> tri_of(size_t(n) + 3, 0);
+    const int gside = std::max(1, int(std::sqrt(double(n) / 4.0)));
+    const double gw = std::max(hi[0] - lo[0], 1e-300), gh = std::max(hi[1] - lo[1], 1e-300);
+    std::vector<int> cell_vertex(size_t(gside) * gside, -1);
+    auto cell_xy = [&](const double *q, int &cx, int &cy) {
+        cx = std::min(gside - 1, std::max(0, int((q[0] - lo[0]) / gw * gside)));
+        cy = std::min(gside - 1, std::max(0, int((q[1] - lo[1]) / gh * gside)));
+    };
     for (int p = 0; p < n; p++)
     {
         const double *pp = at(p);
-        // 1. walk to a triangle holding p (p on an edge counts as inside)
+        int gx, gy;
+        cell_xy(pp, gx, gy);
+        // 1. walk to a triangle holding p (p on an edge counts as inside),
+        // from a vertex inserted in p's cell or one next to it
         int t = last;
+        for (int r = 0, found = 0; r <= 1 && !found; r++)
+            for (int dy = -r; dy <= r && !found; dy++)
+                for (int dx = -r; dx <= r && !found; dx++)
+                {
+                    const int x = gx + dx, y = gy + dy;
+                    if (x < 0 || y < 0 || x >= gside || y >= gside)
+                        continue;
+                    const int v = cell_vertex[size_t(y) * gside + x];
+                    if (v >= 0)
+                    {
+                        t = tri_of[size_t(v)];
+                        found = 1;
+                    }
+                }
+        if (!T[size_t(t)].alive)
+            t = last;
         for (int steps = 0;; steps++)
         {
             if (steps > 4 * int(T.size()) + 64)
@@ -215,6 +248,8 @@ bool triangulate(const std::vector<double> &pts, std::vector<int> &out, std::str
                     if (to.v[(k + 1) % 3] == e.b && to.v[(k + 2) % 3] == e.a)
                         to.nb[k] = id;
             }
+            tri_of[size_t(e.a)] = id;
+            tri_of[size_t(e.b)] = id;
             stamp1[size_t(e.a)] = p;
             first_of[size_t(e.a)] = id;  // the new triangle with edge p -> a
             stamp2[size_t(e.b)] = p;
@@ -235,6 +270,8 @@ bool triangulate(const std::vector<double> &pts, std::vector<int> &out, std::str
             tr.nb[1] = second_of[size_t(a)];
         }
         last = base;
+        tri_of[size_t(p)] = base;
+        cell_vertex[size_t(gy) * gside + gx] = p;
     }
     out.clear();
     for (const Tri &tr : T)
