@@ -87,11 +87,13 @@ class ClothContext:
         timeout path); 0 in normal use."""
         N.call("cloth_ctx_set_spin_limit", self._h, int(polls), int(extra_arrivals))
 
-    def set_escalation(self, on: bool = True) -> None:
+    def set_escalation(self, on: bool | int = True) -> None:
         """Steps whose FP32 PCG ends in NaN or breakdown are re-solved by the
         FP64 PCG and advanced; stats report the solver "escalated_fp64".  On by
-        default; a step called without stats (step_async) is not escalated."""
-        N.call("cloth_ctx_set_escalation", self._h, int(bool(on)))
+        default (level 1); level 2 (on=2) escalates steps whose FP32 PCG ends at
+        max_iters too; a step called without stats (step_async) is not
+        escalated."""
+        N.call("cloth_ctx_set_escalation", self._h, int(on))
 
     # (rows per thread, slot unroll, tiles per block); slot unroll 0: the
     # bulk-staged SpMV, whose third number is its ring of stages and whose

@@ -590,7 +590,7 @@ void set_material_fields(cloth_s *c)
 
 } // namespace
 
-void cloth::detail::set_params(cloth_s *c, const cloth_solve_params *p)
+void cloth::detail::set_params(cloth_s *c, const cloth_solve_params *p, int hold_maxiter)
 {
     cloth_solve_params q = p ? *p : default_params();
     InstDesc &h = c->h;
@@ -599,14 +599,16 @@ void cloth::detail::set_params(cloth_s *c, const cloth_solve_params *p)
     double rt = q.rel_tol > 0 ? q.rel_tol * q.rel_tol : 0.0;
     double at = q.abs_tol > 0 ? q.abs_tol * q.abs_tol : 0.0;
     int ws = q.warm_start ? 1 : 0;
+    const int hm = hold_maxiter ? 1 : 0;
     if (h.max_iters != mi || h.check_every != ce || h.rel_tol2 != rt ||
-        h.abs_tol2 != at || h.warm_start != ws)
+        h.abs_tol2 != at || h.warm_start != ws || h.hold_maxiter != hm)
     {
         h.max_iters = mi;
         h.check_every = ce;
         h.rel_tol2 = rt;
         h.abs_tol2 = at;
         h.warm_start = ws;
+        h.hold_maxiter = hm;
         c->desc_dirty = true;
     }
 }
@@ -1345,11 +1347,11 @@ int max_iters_of(const Batch *b)
 
 // Prepare every member for a step with dt and params.
 int prepare(const std::vector<cloth_s *> &members, double dt,
-            const cloth_solve_params *params)
+            const cloth_solve_params *params, int hold_maxiter = 0)
 {
     for (auto *c : members)
     {
-        set_params(c, params);
+        set_params(c, params, hold_maxiter);
         set_dt(c, dt);
         int rc = sync_pins(c);
         if (rc != CLOTH_OK)
@@ -1585,7 +1587,9 @@ int run_step(Batch *b, double dt, const cloth_solve_params *params,
         c->plain_host_valid = false;
         c->escalated_valid = false;
     }
-    int rc = prepare(b->members, dt, params);
+    // a step that escalates solves ending at max_iters keeps their state
+    const bool escalating = stats && ctx->escalate > 0 && !b->collide;
+    int rc = prepare(b->members, dt, params, escalating && ctx->escalate >= 2 ? 1 : 0);
     if (rc != CLOTH_OK)
         return rc;
     if (ctx->prof)
@@ -1658,11 +1662,12 @@ int run_step(Batch *b, double dt, const cloth_solve_params *params,
     // precision escalation: a member whose FP32 PCG ended in NaN or breakdown
     // kept its pre-step state and assembled system (the advance skipped it);
     // re-solve it in FP64 and advance
-    if (rc == CLOTH_OK && ctx->escalate && !b->collide)
+    if (rc == CLOTH_OK && escalating)
     {
         const cloth_solve_params p = params ? *params : default_params();
         for (size_t i = 0; i < b->members.size() && rc == CLOTH_OK; i++)
-            if (stats[i].status == CLOTH_ERR_NAN || stats[i].status == CLOTH_ERR_BREAKDOWN)
+            if (stats[i].status == CLOTH_ERR_NAN || stats[i].status == CLOTH_ERR_BREAKDOWN ||
+                (ctx->escalate >= 2 && stats[i].status == CLOTH_ERR_MAXITER))
             {
                 cloth_s *c = b->members[i];
                 c->assembled = true; // this step's system is still in its work arrays
@@ -1922,8 +1927,10 @@ int cloth_ctx_set_escalation(cloth_ctx *ctx, int enable)
 {
     if (!ctx)
         return fail(CLOTH_ERR_INVALID, "cloth_ctx_set_escalation: NULL context");
+    if (enable < 0 || enable > 2)
+        return fail(CLOTH_ERR_INVALID, "cloth_ctx_set_escalation: level must be 0, 1 or 2");
     std::lock_guard<std::recursive_mutex> lk(ctx->mu);
-    ctx->escalate = enable != 0;
+    ctx->escalate = enable;
     return CLOTH_OK;
 }
 

@@ -109,6 +109,8 @@ struct InstDesc
     int fix_fv_norm;
     int max_iters;
     int check_every;
+    int hold_maxiter; // a solve ending at max_iters keeps the state too (to be escalated)
+    int pad_hold;
     double rel_tol2; // rel_tol^2 (0 = off)
     double abs_tol2; // abs_tol^2 (0 = off)
     float k_warp, k_weft, k_bias;

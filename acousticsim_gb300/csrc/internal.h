@@ -147,7 +147,9 @@ struct cloth_ctx_s
     // graph-loop launch sets of more cloths than this hand their last this-many
     // iterating cloths to the persistent kernel (-1: num_sms / 16; 0: never)
     int tail_hand_off = -1;
-    bool escalate = true; // FP32 PCG ending in NaN / breakdown: re-solve the step in FP64
+    // precision escalation of stepped solves: 0 off, 1 an FP32 PCG ending in
+    // NaN / breakdown is re-solved in FP64, 2 one ending at max_iters too
+    int escalate = 1;
     bool prof = false;
     double prof_ms[CLOTH_NUM_PHASES] = {};
     long long prof_n[CLOTH_NUM_PHASES] = {};
@@ -222,7 +224,9 @@ void bind_scratch(const cloth_s *c, InstDesc &h, char *base);
 int alloc_own_scratch(cloth_s *c);
 void free_own_scratch(cloth_s *c);
 // Parameters, time step and pins of the next step, as the step driver sets them.
-void set_params(cloth_s *c, const cloth_solve_params *p);
+// hold_maxiter: the step escalates a solve that ends at max_iters, so the
+// advance must leave that cloth's state (only the escalating step driver)
+void set_params(cloth_s *c, const cloth_solve_params *p, int hold_maxiter = 0);
 void set_dt(cloth_s *c, double dt);
 int sync_pins(cloth_s *c);
 int sync_desc(cloth_s *c);

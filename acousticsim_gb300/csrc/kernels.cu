@@ -3187,9 +3187,10 @@ __global__ void __launch_bounds__(kTile) k_advance(InstDesc *const *descs,
         if (finished_only && (d.st->active || !d.st->open))
             continue;
         // a solve that ended in NaN, breakdown or a timed-out wait leaves the
-        // state as it was (the step driver may re-solve it in FP64)
+        // state as it was (the step driver may re-solve it in FP64), and so
+        // does one that ended at max_iters in a step that escalates those
         const int status = d.st->status;
-        if (status == 6 || status == 7 || status == 9)
+        if (status == 6 || status == 7 || status == 9 || (status == 8 && d.hold_maxiter))
             continue;
         const int row = tl.start + threadIdx.x;
         if (row >= d.nv)

@@ -829,10 +829,11 @@ __global__ void k64_dx32(const InstDesc *dp, const double *dx64)
 int cloth::detail::escalate_step(cloth_s *c, const cloth_solve_params *p,
                                  cloth_solve_stats *out)
 {
-    // the FP32 PCG ended in NaN or breakdown on the assembled system (the
-    // advance left the state alone): the system is beyond FP32 there, so the
-    // step is re-solved by the all-FP64 block-Jacobi PCG from zero to the
-    // step's tolerance, then x += dx in FP64
+    // the FP32 PCG ended in NaN or breakdown (or, at escalation level 2, at
+    // max_iters) on the assembled system (the advance left the state alone):
+    // the system is beyond FP32 there, so the step is re-solved by the
+    // all-FP64 block-Jacobi PCG from zero to the step's tolerance, then
+    // x += dx in FP64
     cloth_solve_params q = *p;
     q.warm_start = 0;
     if (!(q.rel_tol > 0) && !(q.abs_tol > 0))

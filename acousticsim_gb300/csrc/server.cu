@@ -501,6 +501,7 @@ int launch_chunk(cloth_server_s *s, Stage &sg, long long chunk_no, bool *launche
             AdmitRec &ar = sg.admit[n_admit];
             ar.id = id;
             ar.desc = cr.c->h;
+            ar.desc.hold_maxiter = 0; // served solves always advance
             bind_scratch(cr.c, ar.desc, s->pool + off);
             sg.new_ids[n_admit] = id;
             n_admit++;

@@ -123,7 +123,8 @@ typedef struct {
 #define CLOTH_SOLVER_PERSISTENT_1B 3
 #define CLOTH_SOLVER_PERSISTENT_2B 4
 /* ESCALATED: the step's FP32 PCG ended in NaN or breakdown (a system beyond
- * FP32, e.g. stiff dihedral bending on a fine mesh); the step was re-solved by
+ * FP32, e.g. stiff dihedral bending on a fine mesh), or at max_iters at
+ * escalation level 2; the step was re-solved by
  * the all-FP64 PCG (cloth_solve_fp64) from zero and advanced in FP64; iters
  * and rel_residual are that solve's. See cloth_ctx_set_escalation. */
 #define CLOTH_SOLVER_ESCALATED 5
@@ -164,11 +165,16 @@ int cloth_ctx_set_tail_hand_off(cloth_ctx *ctx, int max_instances);
  * that no block makes, so the waits run out on purpose (0 in normal use).
  * Applies to launch sets built afterwards (cached ones are dropped). */
 int cloth_ctx_set_spin_limit(cloth_ctx *ctx, unsigned polls, unsigned extra_arrivals);
-/* Precision escalation of cloth_step / cloth_batch_step (on by default; no
- * counterpart in the reference, whose FP32 solver simply returns): a cloth
- * whose FP32 PCG ends in NaN or breakdown keeps its pre-step state, is
- * re-solved in FP64 (CLOTH_SOLVER_ESCALATED) and advanced. Off: such a step
- * reports the status and leaves the cloth's state unchanged. */
+/* Precision escalation of cloth_step / cloth_batch_step (level 1 by default;
+ * no counterpart in the reference, whose FP32 solver simply returns). Level 1:
+ * a cloth whose FP32 PCG ends in NaN or breakdown keeps its pre-step state, is
+ * re-solved in FP64 (CLOTH_SOLVER_ESCALATED) and advanced. Level 2: the same
+ * for a cloth whose FP32 PCG ends at max_iters (CLOTH_ERR_MAXITER; a system
+ * the FP32 PCG stalls on, e.g. stiff dihedral bending); at level 1 such a step
+ * is advanced with the dx it reached, as the reference does. Level 0: a step
+ * ending in NaN or breakdown reports the status and leaves the cloth's state
+ * unchanged. Steps made without stats, and cloths with bodies, are not
+ * escalated. Other levels: CLOTH_ERR_INVALID. */
 int cloth_ctx_set_escalation(cloth_ctx *ctx, int enable);
 /* Graph-loop kernel variants (the batched and served PCG): rows per thread R
  * of the SpMV and update kernels, the SpMV's slot unroll U and the tiles a

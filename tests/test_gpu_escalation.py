@@ -89,3 +89,55 @@ def test_failed_fp32_step_is_resolved_in_fp64(built):
     assert st2["status"] == "OK", st2
     c.close()
     ctx.close()
+
+
+def test_maxiter_step_is_escalated_at_level_2(built):
+    """Escalation level 2 also re-solves a step whose FP32 PCG ends at
+    max_iters (a capped solve here: 3 iterations on a 32 x 32 cloth); at
+    level 1 that step is advanced with the dx it reached, as the reference
+    does, and so is a step made without stats at level 2."""
+    from acousticsim_gb300 import BaraffClothGpu, ClothContext, ClothError, params
+    conf = _conf()
+    conf["subdivision"] = [31, 31]
+    conf["cloth_bending_model"] = "quadratic"
+    p = params(max_iters=3, rel_tol=1e-6)
+    ctx = ClothContext(0)
+    c = BaraffClothGpu(ctx, conf)
+    x0, xp0 = _seeded(c.GetInitPos())
+
+    def reset():
+        c.Reset()
+        c.SetPos(x0)
+        c.SetPrePos(xp0)
+
+    # level 1 (the default): the capped solve is advanced
+    reset()
+    st = c.UpdatePos(0.0, p)
+    assert st["status"] == "MAXITER" and st["solver"] != "escalated_fp64", st
+    x_capped = c.GetPos()
+    assert not np.array_equal(x_capped, x0)
+
+    # level 2: re-solved in FP64 from the pre-step state and advanced
+    ctx.set_escalation(2)
+    reset()
+    st = c.UpdatePos(0.0, p)
+    assert st["status"] == "OK" and st["solver"] == "escalated_fp64", st
+    assert st["rel_residual"] <= 1e-6
+    x_esc = c.GetPos()
+    reset()
+    c.assemble()
+    st64 = c.solve_fp64(params(max_iters=100000, rel_tol=1e-6, warm_start=0))
+    assert st64["status"] == "OK" and st64["iters"] == st["iters"], st64
+    c.advance()
+    assert np.array_equal(c.GetPos(), x_esc)
+
+    # level 2, no stats: not escalated, the capped dx is applied
+    reset()
+    c.step_async(0.0, p)
+    assert np.array_equal(c.GetPos(), x_capped)
+
+    with pytest.raises(ClothError):
+        ctx.set_escalation(3)
+    ctx.set_escalation(True)
+    c.close()
+    ctx.close()
