@@ -692,6 +692,11 @@ def graph_loop_roofline(prof: dict, bytes_spmv: float, bytes_upd: float) -> dict
                           "traffic_source": "profiles/ncu_traffic.json (ncu DRAM bytes per "
                                             "algorithmic byte of one all-active launch)"}
     out["reduce_ms_total"] = prof["reduce"]["ms"]
+    out["reduce_note"] = ("k_reduce_pq + k_reduce_rz (one thread per cloth) in the profiled, "
+                          "host-launched step: CUDA-event time around each launch, which for "
+                          "kernels this small includes the GPU waiting for the host's next "
+                          "launch; in the graph-launched step all four kernels of an iteration "
+                          "take ~19 us together once few cloths iterate")
     return out
 
 
